@@ -1,0 +1,91 @@
+// Molecular Hamiltonian input: the Molpro FCIDUMP reader/writer, the
+// dmrg.conf keyword subset of the sweep hot path, the seeded synthetic
+// Hamiltonian generator, and orbital reordering.
+//
+// FCIDUMP layout follows Input::readorbitalsfile (input.C:1407-1681): header
+// `&FCI NORB=,NELEC=,MS2=,ORBSYM=,ISYM= &END`, then `value i j k l` lines,
+// 1-based; `k=l=0` marks one-electron integrals and `i=j=k=l=0` the core
+// energy.  Two-electron integrals are chemist-notation (ij|kl) with 8-fold
+// permutational symmetry.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace bgpu {
+
+struct Integrals {
+  int norb = 0, nelec = 0, ms2 = 0, isym = 0;  // isym 0-based
+  std::vector<int> orbsym;                     // 0-based irreps
+  double ecore = 0.0;
+  std::vector<double> t;  // norb^2
+  std::vector<double> v;  // norb^4, (ij|kl) = v[((i*n+j)*n+k)*n+l]
+  double h(int i, int j) const { return t[(size_t)i * norb + j]; }
+  double g(int i, int j, int k, int l) const {
+    return v[(((size_t)i * norb + j) * norb + k) * norb + l];
+  }
+  void resize(int n);
+  void set_eri(int i, int j, int k, int l, double x);  // sets all 8 permutations
+};
+
+Integrals read_fcidump(const std::string& path);
+void write_fcidump(const Integrals& I, const std::string& path);
+// new orbital i is old orbital perm[i]
+Integrals reorder(const Integrals& I, const std::vector<int>& perm);
+// Fiedler ordering of the exchange-integral graph (fiedler.C:47-81,
+// genetic/ReadIntegral.C:11-62)
+std::vector<int> fiedler_order(const Integrals& I);
+// Orbital order requested by a configuration (fiedler | noreorder | file:<path>,
+// the reorder file holding 1-based orbitals in their new order).
+std::vector<int> orbital_order(const Integrals& I, const std::string& reorder);
+
+// Seeded generator of the synthetic Cholesky-factorised Hamiltonian:
+// h symmetric, diag linspace(dlo, dhi), off-diagonal N(0, hsd);
+// (pq|rs) = sum_k L^k_pq L^k_rs with symmetric L^k_pq ~ N(0, lsd).
+// With `d2h_round_robin`, orbital p carries D2h irrep p mod 8 and every
+// integral whose irrep product is not totally symmetric is zeroed.
+Integrals synthetic_hamiltonian(int norb, int nelec, int nchol, uint64_t seed, bool d2h_round_robin,
+                                double dlo = -3.0, double dhi = 1.0, double hsd = 0.05, double lsd = 0.1);
+
+// Small deterministic PRNG (splitmix64 + Box-Muller), identical on every host.
+struct Rng {
+  uint64_t s;
+  explicit Rng(uint64_t seed) : s(seed) {}
+  uint64_t next();
+  double uniform();  // (0,1)
+  double normal();
+};
+
+struct ScheduleEntry {
+  int iter = 0, M = 0;
+  double davidson_tol = 1e-8, noise = 0.0;
+};
+
+struct Config {
+  int nelec = -1, spin = 0, irrep = 0;  // irrep 0-based
+  std::string sym = "c1";
+  std::string orbitals;  // FCIDUMP path
+  std::vector<ScheduleEntry> schedule;
+  bool schedule_default = false;
+  int startM = 250, maxM = 0;
+  int maxiter = 10;
+  double sweep_tol = 1e-5;
+  int nroots = 1;
+  std::vector<double> weights;
+  std::string reorder = "fiedler";  // fiedler | noreorder | file:<path>
+  int outputlevel = 0;
+  int deflation_min = 2, deflation_max = 20;
+  uint64_t seed = 12345;  // warm-up rotations and Davidson guesses
+  std::string warmup = "random";
+  // the remaining keywords are recognised and ignored (twodot_to_onedot,
+  // hf_occ, onepdm/twopdm, noise columns ...)
+  const ScheduleEntry& entry(int sweep) const;
+};
+
+Config parse_config(const std::string& path);
+Config parse_config_text(const std::string& text, const std::string& base_dir);
+// The reference's default schedule (Schedule.C generateDefaultSchedule) for
+// `schedule default` with startM/maxM.
+void make_default_schedule(Config& c);
+
+}  // namespace bgpu

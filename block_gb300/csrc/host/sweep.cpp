@@ -1,0 +1,389 @@
+#include "sweep.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <limits>
+#include <numeric>
+#include <stdexcept>
+
+#include "dense.h"
+
+namespace bgpu {
+
+SweepDriver::SweepDriver(const Integrals& I, const Config& c, Engine& e, DriverOptions opt)
+    : I_(I), C_(c), E_(e), opt_(std::move(opt)) {
+  g_ = PointGroup::from_name(C_.sym);
+  N_ = I_.norb;
+  const int nelec = C_.nelec >= 0 ? C_.nelec : I_.nelec;
+  filter_.nelec = nelec;
+  filter_.s2 = C_.spin;
+  filter_.norb = N_;
+  target_ = {nelec, C_.spin, C_.irrep};
+  left_.resize(N_);
+  right_.resize(N_);
+  dots_.resize(N_);
+  for (int x = 0; x < N_; ++x) {
+    dots_[x] = std::make_unique<Block>(make_dot_block(x));
+  }
+}
+
+SweepDriver::~SweepDriver() {
+  for (auto* v : {&left_, &right_, &dots_})
+    for (auto& b : *v)
+      if (b && b->handle >= 0) E_.release_block(*b);
+}
+
+void SweepDriver::log(int level, const char* fmt, ...) const {
+  if (opt_.verbose < level) return;
+  va_list ap;
+  va_start(ap, fmt);
+  std::vfprintf(stderr, fmt, ap);
+  va_end(ap);
+}
+
+Block SweepDriver::make_dot_block(int x) {
+  DotOps d = make_dot(x, I_, g_);
+  Block b;
+  b.sites = {x};
+  b.si = d.si;
+  b.ops = d.set;
+  b.is_dot = true;
+  E_.create_block(b);
+  E_.upload_block(b, d.data);
+  return b;
+}
+
+bool SweepDriver::loop_is_left(int p) const { return (p + 1) <= (N_ - 1 - p); }
+
+CatalogSpec SweepDriver::sigma_spec(const std::vector<int>& own, const std::vector<int>& other, bool is_loop,
+                                    const std::vector<int>& loop_sites) const {
+  CatalogSpec s;
+  s.sites = own;
+  s.ccd_sites = other;
+  s.normal = is_loop;
+  if (!is_loop)
+    for (int a : loop_sites)
+      for (int b : loop_sites)
+        if (a >= b) s.comp_pairs.push_back({a, b});
+  return s;
+}
+
+CatalogSpec SweepDriver::renorm_spec(const std::vector<int>& own, int /*next_dot*/, bool next_big_is_loop) const {
+  CatalogSpec s;
+  s.sites = own;
+  std::vector<int> comp;
+  for (int i = 0; i < N_; ++i)
+    if (std::find(own.begin(), own.end(), i) == own.end()) comp.push_back(i);
+  s.ccd_sites = comp;
+  s.normal = next_big_is_loop;
+  for (int a : comp)
+    for (int b : comp)
+      if (a >= b) s.comp_pairs.push_back({a, b});
+  return s;
+}
+
+void SweepDriver::merge(CatalogSpec& a, const CatalogSpec& b) const {
+  a.normal = a.normal || b.normal;
+  for (int x : b.ccd_sites)
+    if (std::find(a.ccd_sites.begin(), a.ccd_sites.end(), x) == a.ccd_sites.end()) a.ccd_sites.push_back(x);
+  for (auto& p : b.comp_pairs)
+    if (std::find(a.comp_pairs.begin(), a.comp_pairs.end(), p) == a.comp_pairs.end()) a.comp_pairs.push_back(p);
+}
+
+Block SweepDriver::make_enlarged(const Block& sys, int x, bool dot_on_right, const CatalogSpec& spec) {
+  const Block& dot = *dots_[x];
+  const Block& a = dot_on_right ? sys : dot;
+  const Block& b = dot_on_right ? dot : sys;
+  Block big;
+  big.sites = a.sites;
+  big.sites.insert(big.sites.end(), b.sites.begin(), b.sites.end());
+  big.si = product_stateinfo(a.si, b.si, g_, &filter_, (int)big.sites.size(), nullptr);
+  std::set<OpKey> keys = catalog_keys(spec);
+  big.ops = make_opset(big.si, keys, I_.orbsym, g_);
+  std::vector<std::pair<OpKey, std::vector<BuildTerm>>> recipes;
+  for (const auto& kv : big.ops.ops) recipes.push_back({kv.first, build_terms(kv.first, a.sites, b.sites, I_)});
+  // check that every operand exists
+  for (auto& r : recipes)
+    for (auto& t : r.second) {
+      if (!t.a.identity && !a.ops.has(t.a.key))
+        throw std::runtime_error("build of " + r.first.str() + " needs " + t.a.key.str() + " on left sub-block");
+      if (!t.b.identity && !b.ops.has(t.b.key))
+        throw std::runtime_error("build of " + r.first.str() + " needs " + t.b.key.str() + " on right sub-block");
+    }
+  E_.create_block(big);
+  E_.build_block(big, a, b, recipes);
+  return big;
+}
+
+Superblock SweepDriver::make_superblock(const Block& L, const Block& R) const {
+  Superblock sb;
+  sb.L = &L;
+  sb.R = &R;
+  sb.target = target_;
+  sb.si = product_stateinfo(L.si, R.si, g_, nullptr, N_, &target_);
+  const int p = L.sites.back();
+  sb.loop_left = loop_is_left(p);
+  sb.terms = sigma_terms(L.sites, R.sites, sb.loop_left);
+  sb.ecore = I_.ecore;
+  for (int lq = 0; lq < L.si.size(); ++lq)
+    for (int rq = 0; rq < R.si.size(); ++rq) {
+      if (!quantum_allowed(target_, L.si.quanta[lq], R.si.quanta[rq], g_)) continue;
+      Superblock::Sector s;
+      s.lq = lq;
+      s.rq = rq;
+      s.rows = L.si.states[lq];
+      s.cols = R.si.states[rq];
+      s.offset = sb.size;
+      sb.size += (int64_t)s.rows * s.cols;
+      sb.sectors.push_back(s);
+    }
+  for (auto& t : sb.terms) {
+    if (!t.l.identity && !L.ops.has(t.l.key)) throw std::runtime_error("sigma needs " + t.l.key.str() + " on L");
+    if (!t.r.identity && !R.ops.has(t.r.key)) throw std::runtime_error("sigma needs " + t.r.key.str() + " on R");
+  }
+  return sb;
+}
+
+Block& SweepDriver::left_block(int last) {
+  if (last == 0) return *dots_[0];
+  if (!left_[last]) throw std::runtime_error("left block missing");
+  return *left_[last];
+}
+
+Block& SweepDriver::right_block(int first) {
+  if (first == N_ - 1) return *dots_[N_ - 1];
+  if (!right_[first]) throw std::runtime_error("right block missing");
+  return *right_[first];
+}
+
+// Heuristic quanta distribution of a warm-up block (the reference guesses a
+// distribution too, initblocks.C:229-300): weight of a quantum ~ its size
+// times a Gaussian in the particle number around the Hartree-Fock filling of
+// the block's orbitals.  Returns the kept count per quantum.
+std::vector<int> SweepDriver::warmup_rotation(Block& big, int M, uint64_t seed) {
+  const int nsites = (int)big.sites.size();
+  std::vector<int> order(N_);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return I_.h(a, a) < I_.h(b, b); });
+  std::vector<int> occ(N_, 0);
+  int left_e = target_.n;
+  for (int o : order) {
+    const int k = std::min(2, left_e);
+    occ[o] = k;
+    left_e -= k;
+  }
+  double nhf = 0;
+  for (int s : big.sites) nhf += occ[s];
+  const double sig = std::max(1.0, std::sqrt((double)nsites));
+  std::vector<double> w(big.si.size());
+  double tot = 0;
+  for (int q = 0; q < big.si.size(); ++q) {
+    const double dn = big.si.quanta[q].n - nhf;
+    w[q] = big.si.states[q] * std::exp(-dn * dn / (2 * sig * sig)) / (1.0 + big.si.quanta[q].s2);
+    tot += w[q];
+  }
+  std::vector<int> kept(big.si.size(), 0);
+  const long total = big.si.total_states();
+  int budget = (int)std::min<long>(M, total);
+  std::vector<int> idx(big.si.size());
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return w[a] > w[b]; });
+  for (int q : idx) {
+    if (budget <= 0) break;
+    if (w[q] <= 1e-12 * tot) continue;
+    kept[q] = 1;
+    --budget;
+  }
+  while (budget > 0) {
+    bool any = false;
+    for (int q : idx) {
+      if (budget <= 0) break;
+      const int want = (int)std::ceil(M * w[q] / tot);
+      if (kept[q] < std::min(want, big.si.states[q])) {
+        ++kept[q];
+        --budget;
+        any = true;
+      }
+    }
+    if (!any) {
+      for (int q : idx) {
+        if (budget <= 0) break;
+        if (kept[q] < big.si.states[q]) {
+          ++kept[q];
+          --budget;
+          any = true;
+        }
+      }
+      if (!any) break;
+    }
+  }
+  Rng rng(seed);
+  std::vector<std::vector<double>> rot(big.si.size());
+  for (int q = 0; q < big.si.size(); ++q) {
+    const int n = big.si.states[q], m = kept[q];
+    if (m == 0) continue;
+    rot[q].resize((size_t)n * m);
+    for (auto& x : rot[q]) x = rng.normal();
+    orthonormalise_columns(n, m, rot[q].data());
+  }
+  E_.set_rotation(rot, kept);
+  return kept;
+}
+
+std::unique_ptr<Block> SweepDriver::renormalised(const Block& big, const std::vector<int>& kept,
+                                                 const CatalogSpec& spec) {
+  auto nb = std::make_unique<Block>();
+  nb->sites = big.sites;
+  std::vector<int> map;
+  nb->si = truncated_stateinfo(big.si, kept, map);
+  nb->ops = make_opset(nb->si, catalog_keys(spec), I_.orbsym, g_);
+  for (const auto& kv : nb->ops.ops)
+    if (!big.ops.has(kv.first)) throw std::runtime_error("renormalised block needs " + kv.first.str());
+  E_.create_block(*nb);
+  E_.renormalise(*nb, big);
+  return nb;
+}
+
+void SweepDriver::warmup() {
+  const int M = C_.schedule.front().M;
+  cur_M_ = M;
+  for (int p = N_ - 2; p >= 3; --p) {
+    Block& sys = right_block(p + 1);
+    std::vector<int> own;
+    for (int i = p; i < N_; ++i) own.push_back(i);
+    CatalogSpec spec = renorm_spec(own, p - 1, !loop_is_left(p - 2));
+    Block big = make_enlarged(sys, p, /*dot_on_right=*/false, spec);
+    std::vector<int> kept = warmup_rotation(big, M, C_.seed + 7919ull * (uint64_t)p);
+    if (right_[p]) E_.release_block(*right_[p]);
+    right_[p] = renormalised(big, kept, spec);
+    E_.release_block(big);
+    log(2, "warmup right block [%d..%d]: %ld states\n", p, N_ - 1, right_[p]->si.total_states());
+  }
+}
+
+// Truncation: keep the M largest density-matrix eigenvalues above 1e-13
+// (makeRotateMatrix / sort_weights / assign_matrix_by_dm,
+// renormalise.C:135-166, rotationmat.C:149-339); returns discarded weight.
+static double choose_kept(const DensitySpectrum& spec, int M, std::vector<std::vector<int>>& kept_idx,
+                          std::vector<int>& kept) {
+  struct W { double w; int q, i; };
+  std::vector<W> all;
+  double norm = 0.0;
+  for (int q = 0; q < (int)spec.eig.size(); ++q)
+    for (int i = 0; i < (int)spec.eig[q].size(); ++i) {
+      double w = spec.eig[q][i];
+      if (w < 1e-14) w = 0.0;
+      all.push_back({w, q, i});
+      norm += w;
+    }
+  std::stable_sort(all.begin(), all.end(), [](const W& a, const W& b) { return a.w > b.w; });
+  kept_idx.assign(spec.eig.size(), {});
+  kept.assign(spec.eig.size(), 0);
+  double keptw = 0.0;
+  const int nk = std::min<int>(M, (int)all.size());
+  for (int t = 0; t < nk; ++t) {
+    if (all[t].w <= 1e-13) continue;
+    kept_idx[all[t].q].push_back(all[t].i);
+    keptw += all[t].w;
+  }
+  for (size_t q = 0; q < kept_idx.size(); ++q) {
+    // keep the eigenvectors of each sector in descending weight order
+    std::sort(kept_idx[q].begin(), kept_idx[q].end(), std::greater<int>());
+    kept[q] = (int)kept_idx[q].size();
+  }
+  return norm - keptw;
+}
+
+double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<double>& energies) {
+  const ScheduleEntry& se = C_.entry(sweep_index);
+  std::vector<int> Ls, Rs;
+  for (int i = 0; i <= p; ++i) Ls.push_back(i);
+  for (int i = p + 1; i < N_; ++i) Rs.push_back(i);
+  const bool loopL = loop_is_left(p);
+  const std::vector<int>& loop_sites = loopL ? Ls : Rs;
+  CatalogSpec specL = sigma_spec(Ls, Rs, loopL, loop_sites);
+  CatalogSpec specR = sigma_spec(Rs, Ls, !loopL, loop_sites);
+  CatalogSpec keepspec;
+  if (forward) {
+    keepspec = renorm_spec(Ls, p + 1, loop_is_left(p + 1));
+    merge(specL, keepspec);
+  } else {
+    keepspec = renorm_spec(Rs, p, !loop_is_left(p - 1));
+    merge(specR, keepspec);
+  }
+  Block L = make_enlarged(left_block(p - 1), p, true, specL);
+  Block R = make_enlarged(right_block(p + 2), p + 1, false, specR);
+  Superblock sb = make_superblock(L, R);
+  DavidsonParams dp;
+  dp.nroots = C_.nroots;
+  dp.tol = se.davidson_tol;
+  dp.deflation_min = C_.deflation_min;
+  dp.deflation_max = C_.deflation_max;
+  dp.seed = C_.seed + 104729ull * (uint64_t)(sweep_index * N_ + p);
+  const int iters = E_.solve(sb, dp, energies);
+  if (opt_.on_step) opt_.on_step(sb, sweep_index, p);
+  DensitySpectrum spec;
+  E_.density(sb, forward, C_.weights, spec);
+  std::vector<std::vector<int>> kept_idx;
+  std::vector<int> kept;
+  const double disc = choose_kept(spec, se.M, kept_idx, kept);
+  E_.select_rotation(kept_idx);
+  if (forward) {
+    if (left_[p]) E_.release_block(*left_[p]);
+    left_[p] = renormalised(L, kept, keepspec);
+  } else {
+    if (right_[p + 1]) E_.release_block(*right_[p + 1]);
+    right_[p + 1] = renormalised(R, kept, keepspec);
+  }
+  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f  disc=%.3e\n", forward ? "fwd" : "bwd", p,
+      L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], disc);
+  E_.release_block(L);
+  E_.release_block(R);
+  return disc;
+}
+
+double SweepDriver::sweep(bool forward, int sweep_index) {
+  std::vector<double> best;
+  double emin = std::numeric_limits<double>::infinity();
+  double maxdisc = 0.0;
+  auto one = [&](int p) {
+    std::vector<double> e;
+    maxdisc = std::max(maxdisc, step(forward, p, sweep_index, e));
+    if (!e.empty() && e[0] < emin) {
+      emin = e[0];
+      best = e;
+    }
+    last_energies_ = e;
+  };
+  if (forward)
+    for (int p = 1; p <= N_ - 3; ++p) one(p);
+  else
+    for (int p = N_ - 3; p >= 1; --p) one(p);
+  last_discarded_ = maxdisc;
+  return emin;
+}
+
+SweepResult SweepDriver::run() {
+  SweepResult res;
+  warmup();
+  double eprev = std::numeric_limits<double>::infinity();
+  const int last_sched = C_.schedule.back().iter;
+  for (int s = 0; s < C_.maxiter; ++s) {
+    const bool forward = (s % 2 == 0);
+    const double e = sweep(forward, s);
+    res.sweep_energies.push_back(e);
+    res.sweeps = s + 1;
+    log(1, "sweep %d (%s) M=%d  E=%.12f  dE=%.3e  maxdisc=%.3e\n", s, forward ? "fwd" : "bwd", C_.entry(s).M, e,
+        e - eprev, last_discarded_);
+    if (s >= last_sched && std::fabs(e - eprev) <= C_.sweep_tol) break;
+    eprev = e;
+  }
+  res.energies = last_energies_;
+  res.discarded = last_discarded_;
+  return res;
+}
+
+}  // namespace bgpu

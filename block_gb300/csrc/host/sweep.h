@@ -1,0 +1,146 @@
+// Two-site DMRG sweep driver (host side).
+//
+// Restates the control flow of Sweep::do_one / BlockAndDecimate
+// (sweep.C:180-545), InitBlocks (initblocks.C), RenormaliseFrom
+// (renormalise.C:39-130) and dmrg() (dmrg.C:600-706) for the spin-adapted,
+// two-dot, noise-free hot path.  All floating-point work on operators and
+// wavefunctions is delegated to an Engine: the CUDA engine of this library
+// in production, and the CPU restatement that serves as the test oracle.
+#pragma once
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "integrals.h"
+#include "ops.h"
+#include "stateinfo.h"
+
+namespace bgpu {
+
+// A block of consecutive sites with its state space and operator catalogue.
+struct Block {
+  std::vector<int> sites;
+  StateInfo si;
+  OpSet ops;
+  bool is_dot = false;
+  int handle = -1;  // engine-side storage id
+};
+
+// The superblock L|R of one sweep step.
+struct Superblock {
+  const Block* L = nullptr;
+  const Block* R = nullptr;
+  StateInfo si;       // single target quantum; parts = (lq, rq) sectors of psi
+  Quantum target;
+  bool loop_left = true;
+  std::vector<PairTerm> terms;
+  double ecore = 0.0;
+  // flattened psi layout: sector s = (lq, rq), offset, rows = states(lq), cols = states(rq)
+  struct Sector { int lq, rq, rows, cols; int64_t offset; };
+  std::vector<Sector> sectors;
+  int64_t size = 0;
+};
+
+// Per-step Davidson settings (linear.C:179-385).
+struct DavidsonParams {
+  int nroots = 1;
+  double tol = 1e-8;  // on the squared residual norm
+  int max_iter = 200;
+  int deflation_min = 2, deflation_max = 20;
+  uint64_t seed = 1;
+};
+
+// Density-matrix spectrum of the block being renormalised: per sector of
+// that block, eigenvalues ascending.
+struct DensitySpectrum {
+  std::vector<std::vector<double>> eig;
+};
+
+class Engine {
+ public:
+  virtual ~Engine() = default;
+  virtual std::string name() const = 0;
+  // storage
+  virtual void create_block(Block& b) = 0;  // allocates b.ops.arena elements
+  virtual void release_block(Block& b) = 0;
+  virtual void upload_block(Block& b, const std::vector<double>& arena) = 0;
+  virtual void download_block(const Block& b, std::vector<double>& arena) = 0;
+  // big = a (x) b built by per-operator recipes
+  virtual void build_block(Block& big, const Block& a, const Block& b,
+                           const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) = 0;
+  // Davidson on the superblock; energies of the converged roots.  The
+  // wavefunctions stay inside the engine.
+  virtual int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) = 0;
+  // reduced density matrix of the left (forward) or right (backward) block
+  // from the engine's current wavefunctions and its eigen-decomposition.
+  virtual void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) = 0;
+  // keep eigenvectors `kept[q]` (indices into the ascending spectrum) of
+  // every sector as the rotation of the block being renormalised
+  virtual void select_rotation(const std::vector<std::vector<int>>& kept) = 0;
+  // or use an explicit host rotation (warm-up): per sector, rows x kept, row-major
+  virtual void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) = 0;
+  // small = rotation^T big rotation for every operator of small's catalogue
+  virtual void renormalise(Block& small, const Block& big) = 0;
+};
+
+struct SweepResult {
+  std::vector<double> energies;         // final energy per root
+  std::vector<double> sweep_energies;   // lowest root, per sweep
+  double discarded = 0.0;
+  int sweeps = 0;
+  double sigma_seconds = 0.0;
+  long sigma_calls = 0;
+};
+
+struct DriverOptions {
+  int verbose = 0;
+  // optional hooks for tests: called after each superblock solve
+  std::function<void(const Superblock&, int sweep, int step)> on_step;
+};
+
+class SweepDriver {
+ public:
+  SweepDriver(const Integrals& I, const Config& c, Engine& e, DriverOptions opt = {});
+  ~SweepDriver();
+  SweepResult run();
+  // pieces used by tests and the bench
+  void warmup();
+  double sweep(bool forward, int sweep_index);
+  const Integrals& integrals() const { return I_; }
+  // builds the superblock of a forward step at partition p (L = [0..p])
+  // using current blocks; useful for snapshots.
+  Superblock make_superblock(const Block& L, const Block& R) const;
+  Block& left_block(int last_site);   // renormalised [0..last_site]
+  Block& right_block(int first_site); // renormalised [first_site..N-1]
+  Block make_enlarged(const Block& sys, int dot_site, bool dot_on_right, const CatalogSpec& spec);
+  bool loop_is_left(int p) const;  // partition L=[0..p], R=[p+1..N-1]
+  CatalogSpec sigma_spec(const std::vector<int>& own, const std::vector<int>& other, bool is_loop,
+                         const std::vector<int>& loop_sites) const;
+  CatalogSpec renorm_spec(const std::vector<int>& own, int next_dot, bool next_big_is_loop) const;
+  void merge(CatalogSpec& a, const CatalogSpec& b) const;
+  void log(int level, const char* fmt, ...) const;
+
+ private:
+  std::vector<int> warmup_rotation(Block& big, int M, uint64_t seed);
+  std::unique_ptr<Block> renormalised(const Block& big, const std::vector<int>& kept, const CatalogSpec& spec);
+  double step(bool forward, int p, int sweep_index, std::vector<double>& energies);
+  Block make_dot_block(int x);
+
+  Integrals I_;
+  Config C_;
+  Engine& E_;
+  DriverOptions opt_;
+  PointGroup g_;
+  QuantumFilter filter_;
+  Quantum target_;
+  int N_;
+  std::vector<std::unique_ptr<Block>> left_;   // left_[p] = [0..p]
+  std::vector<std::unique_ptr<Block>> right_;  // right_[p] = [p..N-1]
+  std::vector<std::unique_ptr<Block>> dots_;
+  int cur_M_ = 0;
+  std::vector<double> last_energies_;
+  double last_discarded_ = 0.0;
+};
+
+}  // namespace bgpu

@@ -1,0 +1,504 @@
+// TEST INFRASTRUCTURE ONLY: CPU oracle of the sweep hot path (see cpu_engine.h).
+#include "cpu_engine.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+
+#include "../block_gb300/csrc/host/dense.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace oracle {
+
+// ------------------------------------------------------------------ dgemm
+// Row-major DGEMM used where the reference calls MatrixMultiply -> DGEMM
+// (MatrixBLAS.C:438-498).  Operands are packed to row-major non-transposed
+// panels, then an i-k-j loop with a 64-column tile keeps B rows in cache.
+void dgemm(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+           double beta, double* C, int ldc) {
+  if (m <= 0 || n <= 0) return;
+  if (beta != 1.0)
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < n; ++j) C[(size_t)i * ldc + j] = (beta == 0.0) ? 0.0 : beta * C[(size_t)i * ldc + j];
+  if (k <= 0 || alpha == 0.0) return;
+  std::vector<double> Ap, Bp;
+  const double* a = A;
+  int la = lda;
+  if (ta) {
+    Ap.resize((size_t)m * k);
+    for (int p = 0; p < k; ++p)
+      for (int i = 0; i < m; ++i) Ap[(size_t)i * k + p] = A[(size_t)p * lda + i];
+    a = Ap.data();
+    la = k;
+  }
+  const double* b = B;
+  int lb = ldb;
+  if (tb) {
+    Bp.resize((size_t)k * n);
+    for (int j = 0; j < n; ++j)
+      for (int p = 0; p < k; ++p) Bp[(size_t)p * n + j] = B[(size_t)j * ldb + p];
+    b = Bp.data();
+    lb = n;
+  }
+  const int JT = 256, KT = 128;
+  for (int j0 = 0; j0 < n; j0 += JT) {
+    const int j1 = std::min(n, j0 + JT);
+    for (int p0 = 0; p0 < k; p0 += KT) {
+      const int p1 = std::min(k, p0 + KT);
+      for (int i = 0; i < m; ++i) {
+        double* c = C + (size_t)i * ldc;
+        const double* ai = a + (size_t)i * la;
+        for (int p = p0; p < p1; ++p) {
+          const double s = alpha * ai[p];
+          if (s == 0.0) continue;
+          const double* bp = b + (size_t)p * lb;
+          for (int j = j0; j < j1; ++j) c[j] += s * bp[j];
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- helpers
+
+namespace {
+
+// A reduced block of an operand: element (r, c) = scale * (trans ? p[c*ld + r] : p[r*ld + c]).
+struct View {
+  const double* p = nullptr;  // nullptr for the identity
+  int rows = 0, cols = 0, ld = 0;
+  bool trans = false;
+  double scale = 1.0;
+  double at(int r, int c) const {
+    if (!p) return r == c ? 1.0 : 0.0;
+    return scale * (trans ? p[(size_t)c * ld + r] : p[(size_t)r * ld + c]);
+  }
+};
+
+bool view(const Block& B, const double* arena, const Operand& o, int bra, int ket, View& v) {
+  if (o.identity) {
+    if (bra != ket) return false;
+    v.p = nullptr;
+    v.rows = v.cols = B.si.states[bra];
+    v.scale = 1.0;
+    return true;
+  }
+  const OpEntry& e = B.ops.at(o.key);
+  const OpLayout& L = B.ops.layouts[e.layout];
+  if (!o.trans) {
+    const int i = L.find(bra, ket);
+    if (i < 0) return false;
+    const OpBlock& b = L.blocks[i];
+    v.p = arena + e.base + b.offset;
+    v.rows = b.rows;
+    v.cols = b.cols;
+    v.ld = b.cols;
+    v.trans = false;
+    v.scale = 1.0;
+  } else {
+    const int i = L.find(ket, bra);
+    if (i < 0) return false;
+    const OpBlock& b = L.blocks[i];
+    v.p = arena + e.base + b.offset;
+    v.rows = b.cols;
+    v.cols = b.rows;
+    v.ld = b.cols;
+    v.trans = true;
+    v.scale = transpose_scaling(B.si.quanta[bra].s2, B.si.quanta[ket].s2, o.key.k2);
+  }
+  return true;
+}
+
+int rank2(const Operand& o) { return o.identity ? 0 : o.key.k2; }
+bool fermion(const Operand& o) { return !o.identity && op_fermion(o.key); }
+
+// dense copy of a view (scaled)
+void dense(const View& v, std::vector<double>& out) {
+  out.assign((size_t)v.rows * v.cols, 0.0);
+  for (int r = 0; r < v.rows; ++r)
+    for (int c = 0; c < v.cols; ++c) out[(size_t)r * v.cols + c] = v.at(r, c);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- engine
+
+CpuEngine::CpuEngine(int t) {
+#ifdef _OPENMP
+  threads = t > 0 ? t : omp_get_max_threads();
+#else
+  threads = 1;
+  (void)t;
+#endif
+}
+
+void CpuEngine::create_block(Block& b) {
+  b.handle = next_handle_++;
+  store_[b.handle].assign(b.ops.arena, 0.0);
+}
+
+void CpuEngine::release_block(Block& b) {
+  store_.erase(b.handle);
+  b.handle = -1;
+}
+
+void CpuEngine::upload_block(Block& b, const std::vector<double>& a) {
+  if ((int64_t)a.size() != b.ops.arena) throw std::runtime_error("upload size mismatch");
+  store_.at(b.handle) = a;
+}
+
+void CpuEngine::download_block(const Block& b, std::vector<double>& a) { a = store_.at(b.handle); }
+
+// TensorProduct of two sub-block operators into an operator of the block
+// made of both (operatorfunctions.C:146-254; MatrixTensorProduct,
+// MatrixBLAS.C:125-291).  Reduced factor: scale * 9j * transpose scalings *
+// fermion sign of the right operator passing the left ket.
+static void tensor_product(const Block& big, const OpKey& tk, double* T, const Block& A, const double* Aar,
+                           const Operand& oa, const Block& B, const double* Bar, const Operand& ob, double coef) {
+  const OpLayout& TL = big.ops.layout_of(tk);
+  const int kA = rank2(oa), kB = rank2(ob), kC = tk.k2;
+  const bool fB = fermion(ob);
+  for (const OpBlock& tb : TL.blocks) {
+    const int cq = tb.bra, cqp = tb.ket;
+    const Quantum& Q = big.si.quanta[cq];
+    const Quantum& Qp = big.si.quanta[cqp];
+    double* Tblk = T + TL.blocks[TL.find(cq, cqp)].offset;
+    const int ldT = tb.cols;
+    for (const SectorPart& pr : big.si.parts[cq])
+      for (const SectorPart& pc : big.si.parts[cqp]) {
+        View va, vb;
+        if (!view(A, Aar, oa, pr.lq, pc.lq, va)) continue;
+        if (!view(B, Bar, ob, pr.rq, pc.rq, vb)) continue;
+        double f = coef * ninej(A.si.quanta[pc.lq].s2, B.si.quanta[pc.rq].s2, Qp.s2, kA, kB, kC,
+                                A.si.quanta[pr.lq].s2, B.si.quanta[pr.rq].s2, Q.s2);
+        if (fB && is_fermion(A.si.quanta[pc.lq])) f = -f;
+        if (f == 0.0) continue;
+        const int br = vb.rows, bc = vb.cols;
+        for (int ia = 0; ia < va.rows; ++ia)
+          for (int ja = 0; ja < va.cols; ++ja) {
+            const double fa = f * va.at(ia, ja);
+            if (fa == 0.0) continue;
+            for (int ib = 0; ib < br; ++ib) {
+              double* trow = Tblk + (size_t)(pr.offset + ia * br + ib) * ldT + pc.offset + ja * bc;
+              for (int jb = 0; jb < bc; ++jb) trow[jb] += fa * vb.at(ib, jb);
+            }
+          }
+      }
+  }
+}
+
+void CpuEngine::build_block(Block& big, const Block& a, const Block& b,
+                            const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) {
+  std::vector<double>& T = store_.at(big.handle);
+  std::fill(T.begin(), T.end(), 0.0);
+  const double* Aar = store_.at(a.handle).data();
+  const double* Bar = store_.at(b.handle).data();
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+  for (int r = 0; r < (int)recipes.size(); ++r) {
+    const OpKey& tk = recipes[r].first;
+    double* Tp = T.data() + big.ops.at(tk).base;
+    for (const BuildTerm& t : recipes[r].second) tensor_product(big, tk, Tp, a, Aar, t.a, b, Bar, t.b, t.coef);
+  }
+}
+
+// sigma = H psi by operator pairs: TensorMultiply (operatorfunctions.C:485-537)
+// over the pair list of SpinBlock::multiplyH (spinblock.C:722-789), with
+// per-thread sigma copies reduced at the end (distribute.h:128-224).
+void CpuEngine::sigma(const Superblock& sb, const double* psi, double* out) {
+  auto t0 = std::chrono::steady_clock::now();
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const double* Lar = store_.at(L.handle).data();
+  const double* Rar = store_.at(R.handle).data();
+  const int nL = L.si.size(), nR = R.si.size();
+  std::vector<int> sec((size_t)nL * nR, -1);
+  for (int s = 0; s < (int)sb.sectors.size(); ++s) sec[(size_t)sb.sectors[s].lq * nR + sb.sectors[s].rq] = s;
+  const int J = sb.target.s2;
+  const int nth = threads;
+  std::vector<std::vector<double>> part(nth, std::vector<double>(sb.size, 0.0));
+#pragma omp parallel num_threads(nth)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double* V = part[tid].data();
+    std::vector<double> m, bufA, bufB;
+#pragma omp for schedule(dynamic)
+    for (int ti = 0; ti < (int)sb.terms.size(); ++ti) {
+      const PairTerm& t = sb.terms[ti];
+      const int kL = rank2(t.l), kR = rank2(t.r);
+      const bool fR = fermion(t.r);
+      for (int lQ = 0; lQ < nL; ++lQ)
+        for (int rQp = 0; rQp < nR; ++rQp)
+          for (int lQp = 0; lQp < nL; ++lQp) {
+            const int cs = sec[(size_t)lQp * nR + rQp];
+            if (cs < 0) continue;
+            View va;
+            if (!view(L, Lar, t.l, lQ, lQp, va)) continue;
+            const auto& S = sb.sectors[cs];
+            const int mr = L.si.states[lQ], mc = R.si.states[rQp];
+            // m = A(lQ,lQ') C(lQ',rQ')
+            m.assign((size_t)mr * mc, 0.0);
+            if (!va.p) {
+              std::memcpy(m.data(), psi + S.offset, sizeof(double) * mr * mc);
+            } else {
+              dgemm(va.trans, false, mr, mc, S.rows, va.scale, va.p, va.ld, psi + S.offset, S.cols, 0.0, m.data(), mc);
+            }
+            for (int rQ = 0; rQ < nR; ++rQ) {
+              const int vs = sec[(size_t)lQ * nR + rQ];
+              if (vs < 0) continue;
+              View vb;
+              if (!view(R, Rar, t.r, rQ, rQp, vb)) continue;
+              double f = t.coef * ninej(L.si.quanta[lQp].s2, R.si.quanta[rQp].s2, J, kL, kR, 0, L.si.quanta[lQ].s2,
+                                        R.si.quanta[rQ].s2, J);
+              if (fR && is_fermion(L.si.quanta[lQp])) f = -f;
+              if (f == 0.0) continue;
+              const auto& SV = sb.sectors[vs];
+              if (!vb.p) {
+                double* v = V + SV.offset;
+                for (size_t e = 0; e < m.size(); ++e) v[e] += f * m[e];
+              } else {
+                // V += f * m * B(rQ,rQ')^T
+                dgemm(false, !vb.trans, mr, SV.cols, mc, f * vb.scale, m.data(), mc, vb.p, vb.ld, 1.0, V + SV.offset,
+                      SV.cols);
+              }
+            }
+          }
+    }
+  }
+  std::fill(out, out + sb.size, 0.0);
+  for (int t = 0; t < nth; ++t)
+    for (int64_t i = 0; i < sb.size; ++i) out[i] += part[t][i];
+  if (sb.ecore != 0.0)
+    for (int64_t i = 0; i < sb.size; ++i) out[i] += sb.ecore * psi[i];
+  sigma_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ++sigma_calls;
+}
+
+// Diagonal of H (SpinBlock::diagonalH, spinblock.C:855-899; diagonal
+// TensorTrace / TensorProduct, operatorfunctions.C:653-762).
+void CpuEngine::hdiag(const Superblock& sb, double* d) {
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const double* Lar = store_.at(L.handle).data();
+  const double* Rar = store_.at(R.handle).data();
+  const int J = sb.target.s2;
+  std::fill(d, d + sb.size, sb.ecore);
+  for (const PairTerm& t : sb.terms) {
+    const int kL = rank2(t.l), kR = rank2(t.r);
+    const bool fR = fermion(t.r);
+    for (const auto& S : sb.sectors) {
+      View va, vb;
+      if (!view(L, Lar, t.l, S.lq, S.lq, va)) continue;
+      if (!view(R, Rar, t.r, S.rq, S.rq, vb)) continue;
+      double f = t.coef * ninej(L.si.quanta[S.lq].s2, R.si.quanta[S.rq].s2, J, kL, kR, 0, L.si.quanta[S.lq].s2,
+                                R.si.quanta[S.rq].s2, J);
+      if (fR && is_fermion(L.si.quanta[S.lq])) f = -f;
+      if (f == 0.0) continue;
+      for (int i = 0; i < S.rows; ++i) {
+        const double a = f * va.at(i, i);
+        if (a == 0.0) continue;
+        for (int j = 0; j < S.cols; ++j) d[S.offset + (int64_t)i * S.cols + j] += a * vb.at(j, j);
+      }
+    }
+  }
+}
+
+static double dot(const std::vector<double>& a, const std::vector<double>& b) {
+  double s = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+static void axpy(double s, const std::vector<double>& x, std::vector<double>& y) {
+  for (size_t i = 0; i < x.size(); ++i) y[i] += s * x[i];
+}
+static void scal(double s, std::vector<double>& x) {
+  for (auto& v : x) v *= s;
+}
+
+// Davidson preconditioner r_i /= (e - diag_i) (Linear::precondition, linear.C:27-47)
+static void precondition(std::vector<double>& r, double e, const std::vector<double>& d) {
+  for (size_t i = 0; i < r.size(); ++i)
+    if (std::fabs(e - d[i]) > 1e-12) r[i] /= (e - d[i]);
+}
+
+// Block Davidson (Linear::block_davidson, linear.C:179-385) with the Olsen
+// correction (linear.C:50-60), deflation and the squared-residual test.
+int CpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) {
+  const int64_t n = sb.size;
+  std::vector<double> diag(n);
+  hdiag(sb, diag.data());
+  const int nroots = p.nroots;
+  if (n < nroots) throw std::runtime_error("superblock smaller than number of roots");
+  // basic guess: unit vectors on the lowest diagonal elements, slightly perturbed
+  std::vector<int64_t> order(n);
+  for (int64_t i = 0; i < n; ++i) order[i] = i;
+  std::partial_sort(order.begin(), order.begin() + nroots, order.end(),
+                    [&](int64_t a, int64_t b) { return diag[a] < diag[b]; });
+  Rng rng(p.seed);
+  std::vector<std::vector<double>> b(nroots, std::vector<double>(n, 0.0)), sigma;
+  for (int r = 0; r < nroots; ++r) {
+    for (int64_t i = 0; i < n; ++i) b[r][i] = 1e-3 * (rng.uniform() - 0.5);
+    b[r][order[r]] = 1.0;
+  }
+  for (int i = 0; i < nroots; ++i) {
+    for (int j = 0; j < i; ++j) axpy(-dot(b[j], b[i]), b[j], b[i]);
+    scal(1.0 / std::sqrt(dot(b[i], b[i])), b[i]);
+  }
+  int converged = 0, iter = 0;
+  std::vector<double> lam;
+  while (true) {
+    ++iter;
+    for (size_t i = sigma.size(); i < b.size(); ++i) {
+      sigma.emplace_back(n);
+      this->sigma(sb, b[i].data(), sigma.back().data());
+    }
+    const int k = (int)b.size();
+    std::vector<double> h((size_t)k * k), alpha((size_t)k * k);
+    lam.assign(k, 0.0);
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j <= i; ++j) h[(size_t)i * k + j] = h[(size_t)j * k + i] = dot(b[i], sigma[j]);
+    jacobi_eigh(k, h.data(), lam.data(), alpha.data());
+    {
+      std::vector<std::vector<double>> bt = b, st = sigma;
+      for (int j = 0; j < k; ++j) {
+        std::fill(b[j].begin(), b[j].end(), 0.0);
+        std::fill(sigma[j].begin(), sigma[j].end(), 0.0);
+        for (int i = 0; i < k; ++i) {
+          axpy(alpha[(size_t)i * k + j], bt[i], b[j]);
+          axpy(alpha[(size_t)i * k + j], st[i], sigma[j]);
+        }
+      }
+    }
+    std::vector<double> r;
+    for (int i = 0; i < converged; ++i) {
+      r = sigma[i];
+      axpy(-lam[i], b[i], r);
+      if (dot(r, r) > p.tol) {
+        converged = i;
+        break;
+      }
+    }
+    r = sigma[converged];
+    axpy(-lam[converged], b[converged], r);
+    const double rnorm = dot(r, r);
+    {  // Olsen preconditioning
+      std::vector<double> c0 = b[converged];
+      precondition(c0, lam[converged], diag);
+      const double num = dot(c0, r), den = dot(b[converged], c0);
+      axpy(-num / den, b[converged], r);
+      precondition(r, lam[converged], diag);
+    }
+    if (rnorm < p.tol) {
+      ++converged;
+      if (converged == nroots) break;
+    } else {
+      if ((int)b.size() >= p.deflation_max) {
+        b.resize(p.deflation_min);
+        sigma.resize(p.deflation_min);
+      }
+      for (size_t j = 0; j < b.size(); ++j) {
+        scal(1.0 / std::sqrt(dot(r, r)), r);
+        axpy(-dot(r, b[j]), b[j], r);
+      }
+      scal(1.0 / std::sqrt(dot(r, r)), r);
+      b.push_back(r);
+    }
+    if (iter >= p.max_iter) break;
+  }
+  energies.assign(lam.begin(), lam.begin() + nroots);
+  waves_.assign(b.begin(), b.begin() + nroots);
+  return iter;
+}
+
+// Reduced density matrix sum_r w_r psi_r psi_r^T of the block being
+// renormalised (DensityMatrix::makedensitymatrix, density.C:27-90;
+// MultiplyProduct, operatorfunctions.C:630-650) and its per-sector
+// eigen-decomposition (diagonalise_dm, rotationmat.C:258-279).
+void CpuEngine::density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) {
+  const Block& B = left ? *sb.L : *sb.R;
+  const int nq = B.si.size();
+  std::vector<std::vector<double>> rho(nq);
+  for (int q = 0; q < nq; ++q) rho[q].assign((size_t)B.si.states[q] * B.si.states[q], 0.0);
+  for (size_t r = 0; r < waves_.size(); ++r) {
+    const double w = r < weights.size() ? weights[r] : 1.0 / waves_.size();
+    for (const auto& S : sb.sectors) {
+      const double* psi = waves_[r].data() + S.offset;
+      if (left)
+        dgemm(false, true, S.rows, S.rows, S.cols, w, psi, S.cols, psi, S.cols, 1.0, rho[S.lq].data(), S.rows);
+      else
+        dgemm(true, false, S.cols, S.cols, S.rows, w, psi, S.cols, psi, S.cols, 1.0, rho[S.rq].data(), S.cols);
+    }
+  }
+  spec.eig.assign(nq, {});
+  dm_vecs_.assign(nq, {});
+  dm_dims_.assign(nq, 0);
+  for (int q = 0; q < nq; ++q) {
+    const int d = B.si.states[q];
+    dm_dims_[q] = d;
+    spec.eig[q].resize(d);
+    dm_vecs_[q].resize((size_t)d * d);
+    jacobi_eigh(d, rho[q].data(), spec.eig[q].data(), dm_vecs_[q].data());
+  }
+}
+
+void CpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {
+  const int nq = (int)kept.size();
+  rot_.assign(nq, {});
+  rot_kept_.assign(nq, 0);
+  for (int q = 0; q < nq; ++q) {
+    const int d = dm_dims_[q], m = (int)kept[q].size();
+    rot_kept_[q] = m;
+    rot_[q].resize((size_t)d * m);
+    for (int c = 0; c < m; ++c)
+      for (int r = 0; r < d; ++r) rot_[q][(size_t)r * m + c] = dm_vecs_[q][(size_t)r * d + kept[q][c]];
+  }
+}
+
+void CpuEngine::set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) {
+  rot_ = rot;
+  rot_kept_ = kept;
+}
+
+// O'(b',k') = U_b^T O(b,k) U_k for every operator of the new block
+// (SparseMatrix::renormalise_transform, BaseOperator.C:341-363;
+// MatrixRotate, MatrixBLAS.C:553-572).
+void CpuEngine::renormalise(Block& small, const Block& big) {
+  std::vector<double>& S = store_.at(small.handle);
+  const std::vector<double>& Bg = store_.at(big.handle);
+  std::vector<std::pair<const OpKey*, const OpEntry*>> list;
+  for (const auto& kv : small.ops.ops) list.push_back({&kv.first, &kv.second});
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+  for (int oi = 0; oi < (int)list.size(); ++oi) {
+    const OpKey& k = *list[oi].first;
+    const OpEntry& se = *list[oi].second;
+    const OpLayout& SL = small.ops.layouts[se.layout];
+    const OpEntry& be = big.ops.at(k);
+    const OpLayout& BL = big.ops.layouts[be.layout];
+    std::vector<double> tmp;
+    for (const OpBlock& sbk : SL.blocks) {
+      const int b = big.si.find(small.si.quanta[sbk.bra]);
+      const int kk = big.si.find(small.si.quanta[sbk.ket]);
+      const int bi = BL.find(b, kk);
+      double* dst = S.data() + se.base + sbk.offset;
+      if (bi < 0) {
+        std::fill(dst, dst + (size_t)sbk.rows * sbk.cols, 0.0);
+        continue;
+      }
+      const OpBlock& bb = BL.blocks[bi];
+      const double* O = Bg.data() + be.base + bb.offset;
+      const int mb = rot_kept_[b], mk = rot_kept_[kk];
+      // tmp = O U_k  (rows(b) x mk), dst = U_b^T tmp
+      tmp.assign((size_t)bb.rows * mk, 0.0);
+      dgemm(false, false, bb.rows, mk, bb.cols, 1.0, O, bb.cols, rot_[kk].data(), mk, 0.0, tmp.data(), mk);
+      dgemm(true, false, mb, mk, bb.rows, 1.0, rot_[b].data(), mb, tmp.data(), mk, 0.0, dst, sbk.cols);
+    }
+  }
+}
+
+}  // namespace oracle

@@ -1,0 +1,58 @@
+// TEST INFRASTRUCTURE ONLY.  CPU restatement (FP64) of the sweep hot path,
+// used as the oracle the CUDA engine is checked against and as the timed
+// CPU baseline.  Nothing in the block_gb300 package may link or call this.
+//
+// Parity is pinned by the reference's golden energies (dmrg_tests/runtest,
+// pydmrg/tests/test_dmrg_simple.py), reproduced by tests/test_oracle_golden.py.
+#pragma once
+#include <map>
+#include <vector>
+
+#include "../block_gb300/csrc/host/sweep.h"
+
+namespace oracle {
+
+using namespace bgpu;
+
+// Row-major C = alpha * op(A) * op(B) + beta * C, op = transpose when t* is true.
+void dgemm(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+           double beta, double* C, int ldc);
+
+class CpuEngine : public Engine {
+ public:
+  explicit CpuEngine(int threads = 0);
+  std::string name() const override { return "cpu-oracle"; }
+  void create_block(Block& b) override;
+  void release_block(Block& b) override;
+  void upload_block(Block& b, const std::vector<double>& arena) override;
+  void download_block(const Block& b, std::vector<double>& arena) override;
+  void build_block(Block& big, const Block& a, const Block& b,
+                   const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) override;
+  int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) override;
+  void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
+  void select_rotation(const std::vector<std::vector<int>>& kept) override;
+  void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
+  void renormalise(Block& small, const Block& big) override;
+
+  // pieces exposed for tests and the bench
+  void sigma(const Superblock& sb, const double* psi, double* out);
+  void hdiag(const Superblock& sb, double* diag);
+  const std::vector<double>& arena(const Block& b) const { return store_.at(b.handle); }
+  std::vector<double>& arena(Block& b) { return store_.at(b.handle); }
+  const std::vector<std::vector<double>>& wavefunctions() const { return waves_; }
+  void set_wavefunctions(const std::vector<std::vector<double>>& w) { waves_ = w; }
+  double sigma_seconds = 0.0;
+  long sigma_calls = 0;
+  int threads = 1;
+
+ private:
+  std::map<int, std::vector<double>> store_;
+  int next_handle_ = 0;
+  std::vector<std::vector<double>> waves_;
+  std::vector<std::vector<double>> dm_vecs_;  // eigenvectors per density-matrix sector (columns, ascending)
+  std::vector<int> dm_dims_;
+  std::vector<std::vector<double>> rot_;       // per big sector: rows x kept
+  std::vector<int> rot_kept_;
+};
+
+}  // namespace oracle
