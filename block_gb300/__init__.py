@@ -1,0 +1,231 @@
+"""GB300-native sweep hot path of spin-adapted two-site DMRG (sanshar/Block).
+
+Python mirror of the library's C ABI (include/bgpu.h).  The compute path is
+the in-tree CUDA library block_gb300/_build/libblockgb300.so; importing the
+package never falls back to anything else, and every call raises if the
+library or a GPU is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Context", "BgpuError", "load_library", "LIB_PATH", "OP", "PREC"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libblockgb300.so")
+
+OP = dict(HAM=0, CRE=1, CRE_DES=2, CRE_CRE=3, CRE_DESCOMP=4, DES_DESCOMP=5, CRE_CRE_DESCOMP=6, OVERLAP=7)
+PREC = dict(fp64=0, bf16x3=1, fp16x2=2)
+
+_lib = None
+
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_P = ctypes.c_void_p
+_IP = ctypes.POINTER(ctypes.c_int)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_DP = ctypes.POINTER(ctypes.c_double)
+_CP = ctypes.c_char_p
+
+_SIGS = {
+    "bgpu_create": (_I, [ctypes.POINTER(_P), _I]),
+    "bgpu_destroy": (_I, [_P]),
+    "bgpu_last_error_string": (_CP, [_P]),
+    "bgpu_version": (_CP, []),
+    "bgpu_set_precision": (_I, [_P, _I]),
+    "bgpu_block_define": (_I, [_P, _I, _IP, _CP, _I, _IP, _IP, _I, _IP, _I, _IP, _I64P]),
+    "bgpu_block_op_offsets": (_I, [_P, _I, _I64P, _I]),
+    "bgpu_block_upload": (_I, [_P, _I, _DP, _I64]),
+    "bgpu_block_download": (_I, [_P, _I, _DP, _I64]),
+    "bgpu_block_free": (_I, [_P, _I]),
+    "bgpu_superblock_define": (_I, [_P, _I, _I, _IP, _I, _DP, _IP, _D, _IP, _I64P]),
+    "bgpu_superblock_free": (_I, [_P, _I]),
+    "bgpu_superblock_work": (_I, [_P, _I, _DP, _DP]),
+    "bgpu_sigma": (_I, [_P, _I, _DP, _DP]),
+    "bgpu_sigma_device": (_I, [_P, _I, _P, _P]),
+    "bgpu_hdiag": (_I, [_P, _I, _DP]),
+    "bgpu_davidson": (_I, [_P, _I, _I, _D, _I, _DP, _DP, _IP]),
+    "bgpu_density_eig": (_I, [_P, _I, _I, _I, _DP, _DP, _I64]),
+    "bgpu_device_alloc": (_I, [_P, _I64, ctypes.POINTER(_P)]),
+    "bgpu_device_free": (_I, [_P, _P]),
+    "bgpu_copy_to_device": (_I, [_P, _P, _DP, _I64]),
+    "bgpu_copy_to_host": (_I, [_P, _DP, _P, _I64]),
+    "bgpu_synchronize": (_I, [_P]),
+    "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
+    "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
+}
+
+EXPORTED = sorted(_SIGS)
+
+
+class BgpuError(RuntimeError):
+    pass
+
+
+def load_library(path=LIB_PATH):
+    """Load the CUDA library; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise BgpuError("native library missing: %s (run __graft_entry__.build())" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+class Context:
+    """One CUDA context of the library (bgpu_create / bgpu_destroy)."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = _P()
+        rc = self.lib.bgpu_create(ctypes.byref(h), device)
+        self.h = h
+        if rc != 0:
+            msg = self.lib.bgpu_last_error_string(h).decode() if h else "bgpu_create failed"
+            if h:
+                self.lib.bgpu_destroy(h)
+            self.h = None
+            raise BgpuError(msg)
+
+    def close(self):
+        if self.h:
+            self.lib.bgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise BgpuError(self.lib.bgpu_last_error_string(self.h).decode())
+
+    def set_precision(self, prec):
+        self._check(self.lib.bgpu_set_precision(self.h, PREC[prec] if isinstance(prec, str) else int(prec)))
+
+    # ---- blocks and superblocks (SpinBlock / SpinBlock::multiplyH boundary)
+    def block_define(self, orbsym, group, quanta, states, op_keys, is_dot=False):
+        orbsym = np.ascontiguousarray(orbsym, dtype=np.int32)
+        quanta = np.ascontiguousarray(quanta, dtype=np.int32).reshape(-1)
+        states = np.ascontiguousarray(states, dtype=np.int32)
+        op_keys = np.ascontiguousarray(op_keys, dtype=np.int32).reshape(-1)
+        h = _I()
+        n = _I64()
+        self._check(self.lib.bgpu_block_define(self.h, len(orbsym), _ip(orbsym), group.encode(), len(states),
+                                               _ip(quanta), _ip(states), len(op_keys) // 4, _ip(op_keys),
+                                               int(is_dot), ctypes.byref(h), ctypes.byref(n)))
+        return h.value, n.value
+
+    def block_upload(self, handle, arena):
+        arena = np.ascontiguousarray(arena, dtype=np.float64)
+        self._check(self.lib.bgpu_block_upload(self.h, handle, _dp(arena), arena.size))
+
+    def block_download(self, handle, n):
+        out = np.empty(n, dtype=np.float64)
+        self._check(self.lib.bgpu_block_download(self.h, handle, _dp(out), n))
+        return out
+
+    def superblock_define(self, left, right, target, coef, term_ops, ecore=0.0):
+        target = np.ascontiguousarray(target, dtype=np.int32)
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        term_ops = np.ascontiguousarray(term_ops, dtype=np.int32).reshape(-1)
+        sb = _I()
+        n = _I64()
+        self._check(self.lib.bgpu_superblock_define(self.h, left, right, _ip(target), len(coef), _dp(coef),
+                                                    _ip(term_ops), float(ecore), ctypes.byref(sb), ctypes.byref(n)))
+        return sb.value, n.value
+
+    def prepare_superblock(self, conf_path, partition):
+        sb = _I()
+        n = _I64()
+        self._check(self.lib.bgpu_prepare_superblock(self.h, conf_path.encode(), partition, ctypes.byref(sb),
+                                                     ctypes.byref(n)))
+        return sb.value, n.value
+
+    def superblock_work(self, sb):
+        f = _D()
+        b = _D()
+        self._check(self.lib.bgpu_superblock_work(self.h, sb, ctypes.byref(f), ctypes.byref(b)))
+        return f.value, b.value
+
+    def sigma(self, sb, psi):
+        psi = np.ascontiguousarray(psi, dtype=np.float64)
+        out = np.empty_like(psi)
+        self._check(self.lib.bgpu_sigma(self.h, sb, _dp(psi), _dp(out)))
+        return out
+
+    def sigma_device(self, sb, psi_ptr, out_ptr):
+        self._check(self.lib.bgpu_sigma_device(self.h, sb, _P(psi_ptr), _P(out_ptr)))
+
+    def hdiag(self, sb, n):
+        out = np.empty(n, dtype=np.float64)
+        self._check(self.lib.bgpu_hdiag(self.h, sb, _dp(out)))
+        return out
+
+    def davidson(self, sb, n, nroots=1, tol=1e-10, max_iter=200, vectors=False):
+        e = np.empty(nroots, dtype=np.float64)
+        v = np.empty((nroots, n), dtype=np.float64) if vectors else None
+        it = _I()
+        self._check(self.lib.bgpu_davidson(self.h, sb, nroots, tol, max_iter, _dp(e),
+                                           _dp(v) if v is not None else None, ctypes.byref(it)))
+        return e, v, it.value
+
+    def density_eig(self, sb, left, nstates, weights):
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        out = np.empty(nstates, dtype=np.float64)
+        self._check(self.lib.bgpu_density_eig(self.h, sb, int(left), len(w), _dp(w), _dp(out), nstates))
+        return out
+
+    def device_alloc(self, n):
+        p = _P()
+        self._check(self.lib.bgpu_device_alloc(self.h, n, ctypes.byref(p)))
+        return p.value
+
+    def device_free(self, p):
+        self._check(self.lib.bgpu_device_free(self.h, _P(p)))
+
+    def to_device(self, dst, src):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        self._check(self.lib.bgpu_copy_to_device(self.h, _P(dst), _dp(src), src.size))
+
+    def to_host(self, src, n):
+        out = np.empty(n, dtype=np.float64)
+        self._check(self.lib.bgpu_copy_to_host(self.h, _dp(out), _P(src), n))
+        return out
+
+    def synchronize(self):
+        self._check(self.lib.bgpu_synchronize(self.h))
+
+    # ---- full sweep (block.spin_adapted dmrg.conf)
+    def run_dmrg(self, conf_path, verbose=0, max_roots=32):
+        e = np.zeros(max_roots, dtype=np.float64)
+        st = np.zeros(8, dtype=np.float64)
+        self._check(self.lib.bgpu_run_dmrg(self.h, conf_path.encode(), verbose, _dp(e), max_roots, _dp(st)))
+        nroots = int(st[7])
+        stats = dict(sweeps=int(st[0]), sigma_calls=int(st[1]), sigma_seconds=st[2], sigma_flops=st[3],
+                     seconds=st[4], discarded=st[5], last_sweep_energy=st[6])
+        return e[:nroots].copy(), stats

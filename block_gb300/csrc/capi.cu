@@ -1,0 +1,415 @@
+// extern "C" boundary of the library (declarations and reference mapping in
+// include/bgpu.h).
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+
+#include "../../include/bgpu.h"
+#include "cuda/gpu_engine.h"
+#include "host/sweep.h"
+
+using namespace bgpu;
+
+struct bgpu_ctx {
+  std::unique_ptr<GpuEngine> eng;
+  std::string err;
+  int device = 0;
+  struct BlockRec {
+    Block b;
+    std::vector<OpKey> decl;  // declaration order
+    std::vector<int> orbsym;
+  };
+  std::map<int, std::unique_ptr<BlockRec>> blocks;
+  struct SbRec {
+    Superblock sb;
+    SigmaPlan plan;
+    double* psi = nullptr;
+    double* sig = nullptr;
+    // superblocks prepared from a configuration own their blocks
+    std::unique_ptr<Block> ownL, ownR;
+    std::unique_ptr<SweepDriver> drv;
+  };
+  std::map<int, std::unique_ptr<SbRec>> sbs;
+  int next = 1;
+};
+
+namespace {
+template <class F>
+int guarded(bgpu_ctx* ctx, F&& f) {
+  if (!ctx) return BGPU_ERR_INVALID;
+  try {
+    f();
+    ctx->err.clear();
+    return BGPU_OK;
+  } catch (const CudaError& e) {
+    ctx->err = e.what();
+    return BGPU_ERR_CUDA;
+  } catch (const std::invalid_argument& e) {
+    ctx->err = e.what();
+    return BGPU_ERR_INVALID;
+  } catch (const std::exception& e) {
+    ctx->err = e.what();
+    return BGPU_ERR_RUNTIME;
+  }
+}
+void need(bool c, const char* what) {
+  if (!c) throw std::invalid_argument(what);
+}
+}  // namespace
+
+extern "C" {
+
+const char* bgpu_version(void) { return "block_gb300 0.1 (sm_103a)"; }
+
+int bgpu_create(bgpu_ctx** out, int device) {
+  if (!out) return BGPU_ERR_INVALID;
+  *out = nullptr;
+  auto* c = new bgpu_ctx;
+  c->device = device;
+  int rc = guarded(c, [&] { c->eng = std::make_unique<GpuEngine>(device); });
+  if (rc != BGPU_OK) {
+    // keep the context so the caller can read the message
+    *out = c;
+    return rc;
+  }
+  *out = c;
+  return BGPU_OK;
+}
+
+int bgpu_destroy(bgpu_ctx* ctx) {
+  if (!ctx) return BGPU_ERR_INVALID;
+  try {
+    if (ctx->eng) {
+      for (auto& kv : ctx->sbs) {
+        ctx->eng->free_plan(kv.second->plan);
+        ctx->eng->free(kv.second->psi);
+        ctx->eng->free(kv.second->sig);
+      }
+      for (auto& kv : ctx->blocks) ctx->eng->release_block(kv.second->b);
+      ctx->eng->sync();
+    }
+  } catch (...) {
+  }
+  delete ctx;
+  return BGPU_OK;
+}
+
+const char* bgpu_last_error_string(const bgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bgpu_set_precision(bgpu_ctx* ctx, int p) {
+  return guarded(ctx, [&] {
+    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_FP16X2, "unknown precision");
+    need(ctx->eng != nullptr, "no device");
+    ctx->eng->precision = (Precision)p;
+  });
+}
+
+int bgpu_block_define(bgpu_ctx* ctx, int norb, const int* orbsym, const char* group, int nquanta, const int* quanta,
+                      const int* states, int nops, const int* op_keys, int is_dot, int* handle, int64_t* arena_elems) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    need(norb > 0 && orbsym && quanta && states && handle && arena_elems, "null argument");
+    need(nquanta > 0 && nops >= 0 && (nops == 0 || op_keys), "bad sizes");
+    auto rec = std::make_unique<bgpu_ctx::BlockRec>();
+    rec->orbsym.assign(orbsym, orbsym + norb);
+    PointGroup g = PointGroup::from_name(group ? group : "c1");
+    for (int q = 0; q < nquanta; ++q) {
+      Quantum Q{quanta[3 * q], quanta[3 * q + 1], quanta[3 * q + 2]};
+      need(Q.s2 >= 0 && Q.irrep >= 0 && Q.irrep < g.nirrep, "bad quantum");
+      need(states[q] > 0, "sector without states");
+      if (q) need(rec->b.si.quanta.back() < Q, "quanta must be sorted ascending and unique");
+      rec->b.si.quanta.push_back(Q);
+      rec->b.si.states.push_back(states[q]);
+    }
+    std::set<OpKey> keys;
+    for (int o = 0; o < nops; ++o) {
+      const int t = op_keys[4 * o], i = op_keys[4 * o + 1], j = op_keys[4 * o + 2], k2 = op_keys[4 * o + 3];
+      need(t >= 0 && t <= BGPU_OP_OVERLAP, "bad operator type");
+      need(i < norb && j < norb, "orbital index out of range");
+      OpKey k;
+      k.type = (OpType)t;
+      k.i = (int16_t)i;
+      k.j = (int16_t)j;
+      k.k2 = (int8_t)k2;
+      need(keys.insert(k).second, "duplicate operator key");
+      rec->decl.push_back(k);
+    }
+    rec->b.ops = make_opset(rec->b.si, keys, rec->orbsym, g);
+    rec->b.is_dot = is_dot != 0;
+    rec->b.sites.clear();
+    ctx->eng->create_block(rec->b);
+    *arena_elems = rec->b.ops.arena;
+    *handle = ctx->next++;
+    ctx->blocks[*handle] = std::move(rec);
+  });
+}
+
+int bgpu_block_op_offsets(bgpu_ctx* ctx, int handle, int64_t* offsets, int nops) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(handle);
+    need(it != ctx->blocks.end() && offsets, "bad block");
+    need(nops == (int)it->second->decl.size(), "nops mismatch");
+    for (int o = 0; o < nops; ++o) offsets[o] = it->second->b.ops.at(it->second->decl[o]).base;
+  });
+}
+
+int bgpu_block_upload(bgpu_ctx* ctx, int handle, const double* a, int64_t n) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(handle);
+    need(it != ctx->blocks.end() && a, "bad block");
+    need(n == it->second->b.ops.arena, "arena size mismatch");
+    ctx->eng->upload_block(it->second->b, std::vector<double>(a, a + n));
+  });
+}
+
+int bgpu_block_download(bgpu_ctx* ctx, int handle, double* a, int64_t n) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(handle);
+    need(it != ctx->blocks.end() && a, "bad block");
+    need(n == it->second->b.ops.arena, "arena size mismatch");
+    std::vector<double> h;
+    ctx->eng->download_block(it->second->b, h);
+    std::memcpy(a, h.data(), n * sizeof(double));
+  });
+}
+
+int bgpu_block_free(bgpu_ctx* ctx, int handle) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(handle);
+    need(it != ctx->blocks.end(), "bad block");
+    ctx->eng->release_block(it->second->b);
+    ctx->blocks.erase(it);
+  });
+}
+
+int bgpu_superblock_define(bgpu_ctx* ctx, int left, int right, const int* target, int nterms, const double* coef,
+                           const int* term_ops, double ecore, int* sbh, int64_t* psi_elems) {
+  return guarded(ctx, [&] {
+    auto li = ctx->blocks.find(left), ri = ctx->blocks.find(right);
+    need(li != ctx->blocks.end() && ri != ctx->blocks.end(), "bad block handle");
+    need(target && sbh && psi_elems && (nterms == 0 || (coef && term_ops)), "null argument");
+    auto rec = std::make_unique<bgpu_ctx::SbRec>();
+    Superblock& sb = rec->sb;
+    sb.L = &li->second->b;
+    sb.R = &ri->second->b;
+    sb.target = {target[0], target[1], target[2]};
+    sb.ecore = ecore;
+    const auto& L = *sb.L;
+    const auto& R = *sb.R;
+    for (int lq = 0; lq < L.si.size(); ++lq)
+      for (int rq = 0; rq < R.si.size(); ++rq) {
+        const Quantum& a = L.si.quanta[lq];
+        const Quantum& b = R.si.quanta[rq];
+        // abelian irreps: XOR product
+        Quantum t = sb.target;
+        if (t.n != a.n + b.n || t.irrep != (a.irrep ^ b.irrep) || t.s2 < std::abs(a.s2 - b.s2) || t.s2 > a.s2 + b.s2 ||
+            ((t.s2 + a.s2 + b.s2) & 1))
+          continue;
+        Superblock::Sector s;
+        s.lq = lq;
+        s.rq = rq;
+        s.rows = L.si.states[lq];
+        s.cols = R.si.states[rq];
+        s.offset = sb.size;
+        sb.size += (int64_t)s.rows * s.cols;
+        sb.sectors.push_back(s);
+      }
+    need(sb.size > 0, "no sector couples to the target");
+    for (int t = 0; t < nterms; ++t) {
+      PairTerm p;
+      p.coef = coef[t];
+      const int lo = term_ops[4 * t], lt = term_ops[4 * t + 1], ro = term_ops[4 * t + 2], rt = term_ops[4 * t + 3];
+      need(lo >= -1 && lo < (int)li->second->decl.size() && ro >= -1 && ro < (int)ri->second->decl.size(),
+           "term operator index out of range");
+      p.l = lo < 0 ? ident() : op(li->second->decl[lo], lt != 0);
+      p.r = ro < 0 ? ident() : op(ri->second->decl[ro], rt != 0);
+      need(!(p.l.identity && p.r.identity), "identity x identity term: use ecore");
+      sb.terms.push_back(p);
+    }
+    ctx->eng->plan_sigma(sb, rec->plan);
+    rec->psi = ctx->eng->alloc(sb.size);
+    rec->sig = ctx->eng->alloc(sb.size);
+    *psi_elems = sb.size;
+    *sbh = ctx->next++;
+    ctx->sbs[*sbh] = std::move(rec);
+  });
+}
+
+int bgpu_superblock_free(bgpu_ctx* ctx, int sb) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end(), "bad superblock");
+    ctx->eng->free_plan(it->second->plan);
+    ctx->eng->free(it->second->psi);
+    ctx->eng->free(it->second->sig);
+    if (it->second->ownL) ctx->eng->release_block(*it->second->ownL);
+    if (it->second->ownR) ctx->eng->release_block(*it->second->ownR);
+    ctx->sbs.erase(it);
+  });
+}
+
+int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end(), "bad superblock");
+    if (flops) *flops = it->second->plan.flops;
+    if (bytes) *bytes = it->second->plan.bytes;
+  });
+}
+
+int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && psi && sigma, "bad arguments");
+    auto& r = *it->second;
+    const int64_t n = r.sb.size;
+    cuda_check(cudaMemcpyAsync(r.psi, psi, n * sizeof(double), cudaMemcpyHostToDevice, ctx->eng->stream()), "h2d");
+    ctx->eng->sigma(r.sb, r.plan, r.psi, r.sig);
+    cuda_check(cudaMemcpyAsync(sigma, r.sig, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->eng->stream()), "d2h");
+    ctx->eng->sync();
+  });
+}
+
+int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && psi && sigma, "bad arguments");
+    ctx->eng->sigma(it->second->sb, it->second->plan, psi, sigma);
+  });
+}
+
+int bgpu_hdiag(bgpu_ctx* ctx, int sb, double* diag) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && diag, "bad arguments");
+    auto& r = *it->second;
+    ctx->eng->hdiag(r.sb, r.plan, r.sig);
+    cuda_check(cudaMemcpyAsync(diag, r.sig, r.sb.size * sizeof(double), cudaMemcpyDeviceToHost, ctx->eng->stream()),
+               "d2h");
+    ctx->eng->sync();
+  });
+}
+
+int bgpu_davidson(bgpu_ctx* ctx, int sb, int nroots, double tol, int max_iter, double* energies, double* vectors,
+                  int* iterations) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && energies && nroots > 0, "bad arguments");
+    DavidsonParams p;
+    p.nroots = nroots;
+    p.tol = tol;
+    p.max_iter = max_iter > 0 ? max_iter : 200;
+    p.deflation_min = std::max(2, nroots);
+    p.deflation_max = std::max(20, nroots + 20);
+    if (p.deflation_max + 1 > 32) p.deflation_max = 31;
+    std::vector<double> e;
+    const int iters = ctx->eng->solve(it->second->sb, p, e);
+    for (int r = 0; r < nroots; ++r) energies[r] = e[r];
+    if (vectors)
+      cuda_check(cudaMemcpyAsync(vectors, ctx->eng->waves(), (size_t)nroots * it->second->sb.size * sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->eng->stream()),
+                 "d2h");
+    ctx->eng->sync();
+    if (iterations) *iterations = iters;
+  });
+}
+
+int bgpu_density_eig(bgpu_ctx* ctx, int sb, int left, int nroots, const double* weights, double* eig, int64_t n) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && eig, "bad arguments");
+    const Block& B = left ? *it->second->sb.L : *it->second->sb.R;
+    need(n == B.si.total_states(), "eigenvalue buffer size must equal the block's states");
+    std::vector<double> w(weights ? weights : nullptr, weights ? weights + nroots : nullptr);
+    DensitySpectrum spec;
+    ctx->eng->density(it->second->sb, left != 0, w, spec);
+    int64_t o = 0;
+    for (auto& v : spec.eig)
+      for (double x : v) eig[o++] = x;
+  });
+}
+
+int bgpu_device_alloc(bgpu_ctx* ctx, int64_t n, double** p) {
+  return guarded(ctx, [&] {
+    need(p && n > 0, "bad arguments");
+    *p = ctx->eng->alloc(n);
+    ctx->eng->sync();
+  });
+}
+int bgpu_device_free(bgpu_ctx* ctx, double* p) {
+  return guarded(ctx, [&] {
+    ctx->eng->free(p);
+    ctx->eng->sync();
+  });
+}
+int bgpu_copy_to_device(bgpu_ctx* ctx, double* dst, const double* src, int64_t n) {
+  return guarded(ctx, [&] {
+    cuda_check(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->eng->stream()), "h2d");
+  });
+}
+int bgpu_copy_to_host(bgpu_ctx* ctx, double* dst, const double* src, int64_t n) {
+  return guarded(ctx, [&] {
+    cuda_check(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->eng->stream()), "d2h");
+    ctx->eng->sync();
+  });
+}
+int bgpu_synchronize(bgpu_ctx* ctx) {
+  return guarded(ctx, [&] { ctx->eng->sync(); });
+}
+
+int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition, int* sbh, int64_t* psi_elems) {
+  return guarded(ctx, [&] {
+    need(conf_path && sbh && psi_elems, "null argument");
+    Config c = parse_config(conf_path);
+    Integrals I = load_integrals(c);
+    need(partition >= 1 && partition <= I.norb - 3, "partition out of range");
+    auto rec = std::make_unique<bgpu_ctx::SbRec>();
+    rec->drv = std::make_unique<SweepDriver>(I, c, *ctx->eng);
+    rec->ownL = std::make_unique<Block>();
+    rec->ownR = std::make_unique<Block>();
+    rec->sb = rec->drv->prepare_partition(partition, *rec->ownL, *rec->ownR);
+    rec->sb.L = rec->ownL.get();
+    rec->sb.R = rec->ownR.get();
+    rec->drv.reset();  // warm-up blocks are no longer needed
+    ctx->eng->plan_sigma(rec->sb, rec->plan);
+    rec->psi = ctx->eng->alloc(rec->sb.size);
+    rec->sig = ctx->eng->alloc(rec->sb.size);
+    *psi_elems = rec->sb.size;
+    *sbh = ctx->next++;
+    ctx->sbs[*sbh] = std::move(rec);
+  });
+}
+
+int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
+                  double* stats) {
+  return guarded(ctx, [&] {
+    need(conf_path && energies && max_roots > 0, "bad arguments");
+    auto t0 = std::chrono::steady_clock::now();
+    Config c = parse_config(conf_path);
+    Integrals I = load_integrals(c);
+    DriverOptions opt;
+    opt.verbose = verbose;
+    const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops;
+    const long c0 = ctx->eng->sigma_calls;
+    SweepResult r;
+    {
+      SweepDriver drv(I, c, *ctx->eng, opt);
+      r = drv.run();
+    }
+    for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
+    if (stats) {
+      stats[0] = r.sweeps;
+      stats[1] = (double)(ctx->eng->sigma_calls - c0);
+      stats[2] = ctx->eng->sigma_seconds - s0;
+      stats[3] = ctx->eng->sigma_flops - f0;
+      stats[4] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      stats[5] = r.discarded;
+      stats[6] = r.sweep_energies.empty() ? 0.0 : r.sweep_energies.back();
+      stats[7] = (double)r.energies.size();
+    }
+  });
+}
+
+}  // extern "C"

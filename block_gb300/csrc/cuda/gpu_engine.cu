@@ -1,0 +1,912 @@
+// Host side of the CUDA engine: compiles the operator algebra of a sweep
+// step into device work lists and drives the kernels of kernels.cu.
+#include "gpu_engine.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+
+#include "../host/dense.h"
+
+namespace bgpu {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+void DevArray<T>::upload(const std::vector<T>& h, cudaStream_t s) {
+  release(s);
+  n = h.size();
+  if (n == 0) return;
+  cuda_check(cudaMallocAsync((void**)&d, n * sizeof(T), s), "cudaMallocAsync(desc)");
+  cuda_check(cudaMemcpyAsync(d, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, s), "upload desc");
+}
+template <class T>
+void DevArray<T>::release(cudaStream_t s) {
+  if (d) cudaFreeAsync(d, s);
+  d = nullptr;
+  n = 0;
+}
+
+GpuEngine::GpuEngine(int device) : device_(device) {
+  cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+  cudaMemPool_t pool;
+  cuda_check(cudaDeviceGetDefaultMemPool(&pool, device_), "mempool");
+  uint64_t thr = UINT64_MAX;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  cuda_check(cudaEventCreate(&ev0_), "event");
+  cuda_check(cudaEventCreate(&ev1_), "event");
+}
+
+GpuEngine::~GpuEngine() {
+  if (have_plan_) free_plan(plan_);
+  for (auto& kv : blocks_)
+    if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
+  if (waves_) cudaFreeAsync(waves_, stream_);
+  if (dm_vecs_) cudaFreeAsync(dm_vecs_, stream_);
+  if (rot_) cudaFreeAsync(rot_, stream_);
+  cudaStreamSynchronize(stream_);
+  cudaEventDestroy(ev0_);
+  cudaEventDestroy(ev1_);
+  cudaStreamDestroy(stream_);
+}
+
+double* GpuEngine::alloc(int64_t elems) {
+  double* p = nullptr;
+  if (elems <= 0) elems = 1;
+  cuda_check(cudaMallocAsync((void**)&p, (size_t)elems * sizeof(double), stream_), "cudaMallocAsync");
+  return p;
+}
+void GpuEngine::free(double* p) {
+  if (p) cudaFreeAsync(p, stream_);
+}
+void GpuEngine::sync() { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
+
+void GpuEngine::create_block(Block& b) {
+  b.handle = next_handle_++;
+  DevBlock& d = blocks_[b.handle];
+  d.n = b.ops.arena;
+  d.d = alloc(d.n);
+  d.dot = b.is_dot;
+  cuda_check(cudaMemsetAsync(d.d, 0, (size_t)std::max<int64_t>(d.n, 1) * sizeof(double), stream_), "memset");
+}
+
+void GpuEngine::release_block(Block& b) {
+  auto it = blocks_.find(b.handle);
+  if (it != blocks_.end()) {
+    free(it->second.d);
+    blocks_.erase(it);
+  }
+  b.handle = -1;
+}
+
+void GpuEngine::upload_block(Block& b, const std::vector<double>& a) {
+  DevBlock& d = blocks_.at(b.handle);
+  if ((int64_t)a.size() != d.n) throw std::runtime_error("upload_block: size mismatch");
+  cuda_check(cudaMemcpyAsync(d.d, a.data(), a.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "upload");
+  if (b.is_dot || d.dot) d.host = a;
+  sync();
+}
+
+void GpuEngine::download_block(const Block& b, std::vector<double>& a) {
+  const DevBlock& d = blocks_.at(b.handle);
+  a.resize(d.n);
+  cuda_check(cudaMemcpyAsync(a.data(), d.d, a.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_), "download");
+  sync();
+}
+
+double* GpuEngine::arena(const Block& b) const { return blocks_.at(b.handle).d; }
+
+// ------------------------------------------------------------------ views
+
+namespace {
+struct HostView {
+  bool ok = false, identity = false, trans = false;
+  int64_t off = 0;  // element offset of the stored block in its arena
+  int rows = 0, cols = 0, ld = 0;
+  double scale = 1.0;
+};
+
+HostView hview(const Block& B, const Operand& o, int bra, int ket) {
+  HostView v;
+  if (o.identity) {
+    if (bra != ket) return v;
+    v.ok = v.identity = true;
+    v.rows = v.cols = B.si.states[bra];
+    return v;
+  }
+  const OpEntry& e = B.ops.at(o.key);
+  const OpLayout& L = B.ops.layouts[e.layout];
+  if (!o.trans) {
+    const int i = L.find(bra, ket);
+    if (i < 0) return v;
+    const OpBlock& b = L.blocks[i];
+    v.ok = true;
+    v.off = e.base + b.offset;
+    v.rows = b.rows;
+    v.cols = b.cols;
+    v.ld = b.cols;
+  } else {
+    const int i = L.find(ket, bra);
+    if (i < 0) return v;
+    const OpBlock& b = L.blocks[i];
+    v.ok = true;
+    v.trans = true;
+    v.off = e.base + b.offset;
+    v.rows = b.cols;
+    v.cols = b.rows;
+    v.ld = b.cols;
+    v.scale = transpose_scaling(B.si.quanta[bra].s2, B.si.quanta[ket].s2, o.key.k2);
+  }
+  return v;
+}
+inline int rank2(const Operand& o) { return o.identity ? 0 : o.key.k2; }
+inline bool fermion(const Operand& o) { return !o.identity && op_fermion(o.key); }
+
+void add_tasks(std::vector<dev::GemmTask>& t, int unit, int m, int n) {
+  for (int a = 0; a < (m + 63) / 64; ++a)
+    for (int b = 0; b < (n + 63) / 64; ++b) t.push_back({unit, a, b});
+}
+}  // namespace
+
+// ------------------------------------------------------------------ build
+
+void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
+                            const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) {
+  const DevBlock& da = blocks_.at(a.handle);
+  const DevBlock& db = blocks_.at(b.handle);
+  // which factor is the single-site one whose values fold into the factors
+  const bool a_scalar = da.dot && !db.dot;
+  const bool b_scalar = !a_scalar;  // if both are dots, b folds
+  if (b_scalar && !db.dot) throw std::runtime_error("build_block: one sub-block must be a single site");
+  const DevBlock& dsc = a_scalar ? da : db;
+  const Block& sblk = a_scalar ? a : b;
+  std::vector<dev::CopyUnit> units;
+  std::vector<dev::CopyItem> items;
+  for (const auto& rec : recipes) {
+    const OpKey& tk = rec.first;
+    const OpEntry& te = big.ops.at(tk);
+    const OpLayout& TL = big.ops.layouts[te.layout];
+    const int kC = tk.k2;
+    for (const OpBlock& tb : TL.blocks) {
+      const Quantum& Q = big.si.quanta[tb.bra];
+      const Quantum& Qp = big.si.quanta[tb.ket];
+      for (const SectorPart& pr : big.si.parts[tb.bra])
+        for (const SectorPart& pc : big.si.parts[tb.ket]) {
+          const int ibeg = (int)items.size();
+          for (const BuildTerm& t : rec.second) {
+            HostView va = hview(a, t.a, pr.lq, pc.lq);
+            if (!va.ok) continue;
+            HostView vb = hview(b, t.b, pr.rq, pc.rq);
+            if (!vb.ok) continue;
+            double f = t.coef * ninej(a.si.quanta[pc.lq].s2, b.si.quanta[pc.rq].s2, Qp.s2, rank2(t.a), rank2(t.b), kC,
+                                      a.si.quanta[pr.lq].s2, b.si.quanta[pr.rq].s2, Q.s2);
+            if (fermion(t.b) && is_fermion(a.si.quanta[pc.lq])) f = -f;
+            if (f == 0.0) continue;
+            const HostView& vs = a_scalar ? va : vb;  // single-site factor
+            const HostView& vg = a_scalar ? vb : va;  // factor copied from HBM
+            double sv = 1.0;
+            if (!vs.identity) sv = vs.scale * dsc.host[vs.off];  // 1x1 block
+            (void)sblk;
+            f *= sv;
+            if (f == 0.0) continue;
+            dev::CopyItem it;
+            it.alpha = f * (vg.identity ? 1.0 : vg.scale);
+            it.trans = vg.trans ? 1 : 0;
+            it.lds = vg.ld;
+            it.s_off = vg.off;
+            it.s_buf = vg.identity ? -1 : (a_scalar ? 1 : 0);
+            it.pad = 0;
+            items.push_back(it);
+          }
+          if ((int)items.size() == ibeg) continue;
+          dev::CopyUnit u;
+          u.c_off = te.base + tb.offset + (int64_t)pr.offset * tb.cols + pc.offset;
+          u.ldc = tb.cols;
+          u.m = pr.size;
+          u.n = pc.size;
+          u.ibeg = ibeg;
+          u.iend = (int)items.size();
+          units.push_back(u);
+        }
+    }
+  }
+  DevBlock& dt = blocks_.at(big.handle);
+  cuda_check(cudaMemsetAsync(dt.d, 0, (size_t)std::max<int64_t>(dt.n, 1) * sizeof(double), stream_), "memset");
+  DevArray<dev::CopyUnit> du;
+  DevArray<dev::CopyItem> di;
+  du.upload(units, stream_);
+  di.upload(items, stream_);
+  dev::Bufs bufs{};
+  bufs.p[0] = da.d;
+  bufs.p[1] = db.d;
+  cuda_check(dev::launch_copy(bufs, dt.d, du.d, di.d, (int)units.size(), stream_), "build copy");
+  du.release(stream_);
+  di.release(stream_);
+  if (big.is_dot) {
+    dt.host.resize(dt.n);
+    cuda_check(cudaMemcpyAsync(dt.host.data(), dt.d, dt.n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+  }
+  sync();
+}
+
+// ------------------------------------------------------------------ sigma
+
+// Compiles TensorMultiply (operatorfunctions.C:485-537) over all operator
+// pairs of SpinBlock::multiplyH into two grouped-GEMM launches:
+//   stage 1: M[t,lQ,lQ',rQ'] = s_L * A(lQ,lQ') * psi(lQ',rQ')
+//   stage 2: sigma(lQ,rQ) = sum over (t, rQ') of f * M * B(rQ,rQ')^T
+// plus direct products for pairs with one identity factor.  Every output
+// sector is owned by one unit (no atomics).
+void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const int nL = L.si.size(), nR = R.si.size();
+  std::vector<int> sec((size_t)nL * nR, -1);
+  for (int s = 0; s < (int)sb.sectors.size(); ++s) sec[(size_t)sb.sectors[s].lq * nR + sb.sectors[s].rq] = s;
+  const int J = sb.target.s2;
+  // buffers: 0 = L arena, 1 = R arena, 2 = psi, 3 = sigma, 4 = scratch
+  std::vector<dev::GemmUnit> u1;
+  std::vector<dev::GemmItem> i1;
+  std::vector<std::vector<dev::GemmItem>> per_sector(sb.sectors.size());
+  int64_t scratch = 0;
+  double flops = 0.0, bytes = 0.0;
+  std::map<std::pair<int, int64_t>, bool> touched;  // (buf, off) of operator blocks read
+  auto touch = [&](int buf, int64_t off, int64_t elems) {
+    if (touched.emplace(std::make_pair(buf, off), true).second) bytes += 8.0 * elems;
+  };
+  for (const PairTerm& t : sb.terms) {
+    const int kL = rank2(t.l), kR = rank2(t.r);
+    const bool fR = fermion(t.r);
+    for (int lQ = 0; lQ < nL; ++lQ)
+      for (int rQp = 0; rQp < nR; ++rQp)
+        for (int lQp = 0; lQp < nL; ++lQp) {
+          const int cs = sec[(size_t)lQp * nR + rQp];
+          if (cs < 0) continue;
+          HostView va = hview(L, t.l, lQ, lQp);
+          if (!va.ok) continue;
+          const auto& S = sb.sectors[cs];
+          // collect stage-2 partners
+          struct P { int vs; HostView vb; double f; };
+          std::vector<P> parts;
+          for (int rQ = 0; rQ < nR; ++rQ) {
+            const int vs = sec[(size_t)lQ * nR + rQ];
+            if (vs < 0) continue;
+            HostView vb = hview(R, t.r, rQ, rQp);
+            if (!vb.ok) continue;
+            double f = t.coef * ninej(L.si.quanta[lQp].s2, R.si.quanta[rQp].s2, J, kL, kR, 0, L.si.quanta[lQ].s2,
+                                      R.si.quanta[rQ].s2, J);
+            if (fR && is_fermion(L.si.quanta[lQp])) f = -f;
+            if (f == 0.0) continue;
+            parts.push_back({vs, vb, f});
+          }
+          if (parts.empty()) continue;
+          const int mr = L.si.states[lQ], mc = R.si.states[rQp];
+          if (va.identity) {
+            // L identity: sigma(lQ,rQ) += f psi(lQ,rQ') B^T
+            for (auto& pt : parts) {
+              const auto& SV = sb.sectors[pt.vs];
+              dev::GemmItem g{};
+              g.a_buf = 2;
+              g.a_off = S.offset;
+              g.lda = S.cols;
+              g.ta = 0;
+              if (pt.vb.identity) throw std::runtime_error("identity x identity pair term");
+              g.b_buf = 1;
+              g.b_off = pt.vb.off;
+              g.ldb = pt.vb.ld;
+              g.tb = pt.vb.trans ? 0 : 1;
+              g.k = mc;
+              g.alpha = pt.f * pt.vb.scale;
+              per_sector[pt.vs].push_back(g);
+              flops += 2.0 * SV.rows * SV.cols * mc;
+              touch(1, pt.vb.off, (int64_t)pt.vb.rows * pt.vb.cols);
+            }
+            continue;
+          }
+          touch(0, va.off, (int64_t)va.rows * va.cols);
+          bool r_identity = parts.size() == 1 && parts[0].vb.identity;
+          if (r_identity) {
+            // R identity: sigma(lQ,rQ') += f s_L A psi(lQ',rQ')
+            auto& pt = parts[0];
+            dev::GemmItem g{};
+            g.a_buf = 0;
+            g.a_off = va.off;
+            g.lda = va.ld;
+            g.ta = va.trans ? 1 : 0;
+            g.b_buf = 2;
+            g.b_off = S.offset;
+            g.ldb = S.cols;
+            g.tb = 0;
+            g.k = S.rows;
+            g.alpha = pt.f * va.scale;
+            per_sector[pt.vs].push_back(g);
+            flops += 2.0 * mr * mc * S.rows;
+            continue;
+          }
+          // stage 1: M = s_L A psi
+          dev::GemmUnit u{};
+          u.c_buf = 4;
+          u.c_off = scratch;
+          u.ldc = mc;
+          u.m = mr;
+          u.n = mc;
+          u.beta_one = 0;
+          u.ibeg = (int)i1.size();
+          dev::GemmItem g{};
+          g.a_buf = 0;
+          g.a_off = va.off;
+          g.lda = va.ld;
+          g.ta = va.trans ? 1 : 0;
+          g.b_buf = 2;
+          g.b_off = S.offset;
+          g.ldb = S.cols;
+          g.tb = 0;
+          g.k = S.rows;
+          g.alpha = va.scale;
+          i1.push_back(g);
+          u.iend = (int)i1.size();
+          u1.push_back(u);
+          flops += 2.0 * mr * mc * S.rows;
+          for (auto& pt : parts) {
+            const auto& SV = sb.sectors[pt.vs];
+            dev::GemmItem h{};
+            h.a_buf = 4;
+            h.a_off = scratch;
+            h.lda = mc;
+            h.ta = 0;
+            if (pt.vb.identity) throw std::runtime_error("unexpected identity partner");
+            h.b_buf = 1;
+            h.b_off = pt.vb.off;
+            h.ldb = pt.vb.ld;
+            h.tb = pt.vb.trans ? 0 : 1;
+            h.k = mc;
+            h.alpha = pt.f * pt.vb.scale;
+            per_sector[pt.vs].push_back(h);
+            flops += 2.0 * SV.rows * SV.cols * mc;
+            touch(1, pt.vb.off, (int64_t)pt.vb.rows * pt.vb.cols);
+          }
+          scratch += (int64_t)mr * mc;
+        }
+  }
+  std::vector<dev::GemmUnit> u2;
+  std::vector<dev::GemmItem> i2;
+  std::vector<dev::GemmTask> t1, t2;
+  for (size_t s = 0; s < sb.sectors.size(); ++s) {
+    const auto& S = sb.sectors[s];
+    dev::GemmUnit u{};
+    u.c_buf = 3;
+    u.c_off = S.offset;
+    u.ldc = S.cols;
+    u.m = S.rows;
+    u.n = S.cols;
+    u.beta_one = 0;
+    u.ibeg = (int)i2.size();
+    for (auto& g : per_sector[s]) i2.push_back(g);
+    u.iend = (int)i2.size();
+    u2.push_back(u);
+  }
+  for (int u = 0; u < (int)u1.size(); ++u) add_tasks(t1, u, u1[u].m, u1[u].n);
+  // heavier output tiles first
+  std::vector<std::pair<double, int>> cost;
+  for (int u = 0; u < (int)u2.size(); ++u) {
+    double c = 0;
+    for (int i = u2[u].ibeg; i < u2[u].iend; ++i) c += i2[i].k;
+    cost.push_back({-c, u});
+  }
+  std::stable_sort(cost.begin(), cost.end());
+  for (auto& c : cost) add_tasks(t2, c.second, u2[c.second].m, u2[c.second].n);
+  plan.u1.upload(u1, stream_);
+  plan.i1.upload(i1, stream_);
+  plan.t1.upload(t1, stream_);
+  plan.u2.upload(u2, stream_);
+  plan.i2.upload(i2, stream_);
+  plan.t2.upload(t2, stream_);
+  plan.scratch_elems = scratch;
+  plan.scratch = alloc(scratch);
+  plan.flops = flops;
+  plan.bytes = bytes + 2.0 * 8.0 * sb.size;
+  plan.n = sb.size;
+  plan.ecore = sb.ecore;
+  plan.nstage1_units = (int)u1.size();
+  plan.nstage2_units = (int)u2.size();
+  plan.nitems = (int)(i1.size() + i2.size());
+  // diagonal work list (diagonalH, spinblock.C:855-899)
+  std::vector<dev::DiagUnit> du;
+  std::vector<dev::DiagItem> di;
+  for (const auto& S : sb.sectors) {
+    dev::DiagUnit u{};
+    u.d_off = S.offset;
+    u.rows = S.rows;
+    u.cols = S.cols;
+    u.ibeg = (int)di.size();
+    for (const PairTerm& t : sb.terms) {
+      HostView va = hview(L, t.l, S.lq, S.lq);
+      if (!va.ok) continue;
+      HostView vb = hview(R, t.r, S.rq, S.rq);
+      if (!vb.ok) continue;
+      double f = t.coef * ninej(L.si.quanta[S.lq].s2, R.si.quanta[S.rq].s2, J, rank2(t.l), rank2(t.r), 0,
+                                L.si.quanta[S.lq].s2, R.si.quanta[S.rq].s2, J);
+      if (fermion(t.r) && is_fermion(L.si.quanta[S.lq])) f = -f;
+      if (f == 0.0) continue;
+      dev::DiagItem it{};
+      it.a_off = va.identity ? -1 : va.off;
+      it.a_stride = va.ld + 1;
+      it.a_buf = 0;
+      it.b_off = vb.identity ? -1 : vb.off;
+      it.b_stride = vb.ld + 1;
+      it.b_buf = 1;
+      it.alpha = f * va.scale * vb.scale;
+      di.push_back(it);
+    }
+    u.iend = (int)di.size();
+    du.push_back(u);
+  }
+  plan.du.upload(du, stream_);
+  plan.di.upload(di, stream_);
+  sync();
+}
+
+void GpuEngine::free_plan(SigmaPlan& p) {
+  p.u1.release(stream_);
+  p.u2.release(stream_);
+  p.i1.release(stream_);
+  p.i2.release(stream_);
+  p.t1.release(stream_);
+  p.t2.release(stream_);
+  p.du.release(stream_);
+  p.di.release(stream_);
+  free(p.scratch);
+  p.scratch = nullptr;
+}
+
+void GpuEngine::sigma(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out) {
+  dev::Bufs bufs{};
+  bufs.p[0] = arena(*sb.L);
+  bufs.p[1] = arena(*sb.R);
+  bufs.p[2] = const_cast<double*>(psi);
+  bufs.p[3] = out;
+  bufs.p[4] = p.scratch;
+  cuda_check(dev::launch_gemm(bufs, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "sigma stage 1");
+  cuda_check(dev::launch_gemm(bufs, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "sigma stage 2");
+  if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
+  sigma_flops += p.flops;
+  ++sigma_calls;
+}
+
+void GpuEngine::hdiag(const Superblock& sb, const SigmaPlan& p, double* d) {
+  dev::Bufs bufs{};
+  bufs.p[0] = arena(*sb.L);
+  bufs.p[1] = arena(*sb.R);
+  cuda_check(dev::launch_fill(d, sb.ecore, sb.size, stream_), "fill");
+  cuda_check(dev::launch_diag(bufs, d, p.du.d, p.di.d, (int)p.du.n, stream_), "hdiag");
+}
+
+// ------------------------------------------------------------------ Davidson
+
+// Linear::block_davidson (linear.C:179-385) with vectors and all O(n) work
+// on the GPU; the host only steers with the small subspace quantities.
+int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) {
+  if (have_plan_) free_plan(plan_);
+  plan_sigma(sb, plan_);
+  have_plan_ = true;
+  const int64_t n = sb.size;
+  const int nroots = p.nroots;
+  if (n < nroots) throw std::runtime_error("superblock smaller than number of roots");
+  const int kmax = std::max(p.deflation_max, nroots) + 1;
+  if (kmax > 32) throw std::runtime_error("Davidson subspace larger than 32 vectors");
+  double* diag = alloc(n);
+  double* B = alloc((int64_t)kmax * n);
+  double* S = alloc((int64_t)kmax * n);
+  double* T = alloc((int64_t)kmax * n);
+  double* r = alloc(n);
+  double* c0 = alloc(n);
+  double* work = alloc((int64_t)dev::kGramBlocks * 32);
+  double* red = alloc(64);
+  double* hmat = alloc(32 * 32);
+  double* hvec = alloc(32 * 32);
+  double* hw = alloc(32);
+  int64_t* offs = nullptr;
+  int* dims = nullptr;
+  int* status = nullptr;
+  cuda_check(cudaMallocAsync((void**)&offs, 2 * sizeof(int64_t), stream_), "alloc");
+  cuda_check(cudaMallocAsync((void**)&dims, sizeof(int), stream_), "alloc");
+  cuda_check(cudaMallocAsync((void**)&status, sizeof(int), stream_), "alloc");
+  hdiag(sb, plan_, diag);
+  std::vector<double> hd(n);
+  cuda_check(cudaMemcpyAsync(hd.data(), diag, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h diag");
+  sync();
+  // basic guess (as the oracle): unit vectors on the lowest diagonal + small noise
+  std::vector<int64_t> order(n);
+  for (int64_t i = 0; i < n; ++i) order[i] = i;
+  std::partial_sort(order.begin(), order.begin() + nroots, order.end(),
+                    [&](int64_t a, int64_t b) { return hd[a] < hd[b]; });
+  Rng rng(p.seed);
+  {
+    std::vector<double> g((size_t)nroots * n);
+    for (int rr = 0; rr < nroots; ++rr) {
+      for (int64_t i = 0; i < n; ++i) g[(size_t)rr * n + i] = 1e-3 * (rng.uniform() - 0.5);
+      g[(size_t)rr * n + order[rr]] = 1.0;
+    }
+    cuda_check(cudaMemcpyAsync(B, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "guess");
+    sync();
+  }
+  auto dot = [&](const double* x, const double* y) {
+    cuda_check(dev::launch_gram(x, 1, y, 1, n, n, work, red, stream_), "dot");
+    double h;
+    cuda_check(cudaMemcpyAsync(&h, red, sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
+    return h;
+  };
+  auto row = [&](double* M, int i) { return M + (int64_t)i * n; };
+  for (int i = 0; i < nroots; ++i) {
+    for (int j = 0; j < i; ++j) cuda_check(dev::launch_axpy(-dot(row(B, j), row(B, i)), row(B, j), row(B, i), n, stream_), "gs");
+    cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(row(B, i), row(B, i))), row(B, i), n, stream_), "norm");
+  }
+  int k = nroots, ks = 0;  // basis size, number of sigma vectors
+  int converged = 0, iter = 0;
+  std::vector<double> lam;
+  while (true) {
+    ++iter;
+    for (; ks < k; ++ks) {
+      auto t0 = std::chrono::steady_clock::now();
+      sigma(sb, plan_, row(B, ks), row(S, ks));
+      sync();
+      sigma_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    // subspace matrix h_ij = b_i . sigma_j
+    std::vector<double> h((size_t)k * k);
+    for (int j = 0; j < k; ++j)
+      cuda_check(dev::launch_gram(B, k, row(S, j), 1, n, n, work, red + 0, stream_), "gram"),
+          cuda_check(cudaMemcpyAsync(h.data() + (size_t)j * k, red, k * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+                     "d2h");
+    sync();
+    // symmetrise as the reference does (lower triangle of b_i . sigma_j)
+    std::vector<double> hs((size_t)k * k);
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j <= i; ++j) hs[(size_t)i * k + j] = hs[(size_t)j * k + i] = h[(size_t)j * k + i];
+    // subspace eigenproblem on the GPU (batched Jacobi, one matrix)
+    cuda_check(cudaMemcpyAsync(hmat, hs.data(), hs.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
+    int64_t ho[2] = {0, 0};
+    cuda_check(cudaMemcpyAsync(offs, ho, sizeof(ho), cudaMemcpyHostToDevice, stream_), "h2d");
+    cuda_check(cudaMemcpyAsync(dims, &k, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d");
+    cuda_check(dev::launch_jacobi(hmat, offs, dims, hw, offs + 1, hvec, offs, status, 1, k, stream_), "subspace eig");
+    std::vector<double> alpha((size_t)k * k);
+    lam.assign(k, 0.0);
+    int st = 0;
+    cuda_check(cudaMemcpyAsync(lam.data(), hw, k * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    cuda_check(cudaMemcpyAsync(alpha.data(), hvec, alpha.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    cuda_check(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
+    if (st < 0) throw std::runtime_error("subspace eigensolver did not converge");
+    // Ritz vectors: b'_j = sum_i alpha_ij b_i (same for sigma)
+    cuda_check(cudaMemcpyAsync(hmat, alpha.data(), alpha.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
+    cuda_check(dev::launch_combine(B, k, n, n, hmat, k, T, n, stream_), "ritz b");
+    std::swap(B, T);
+    cuda_check(dev::launch_combine(S, k, n, n, hmat, k, T, n, stream_), "ritz s");
+    std::swap(S, T);
+    auto resid = [&](int i) {
+      cuda_check(cudaMemcpyAsync(r, row(S, i), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy");
+      cuda_check(dev::launch_axpy(-lam[i], row(B, i), r, n, stream_), "axpy");
+    };
+    for (int i = 0; i < converged; ++i) {
+      resid(i);
+      if (dot(r, r) > p.tol) {
+        converged = i;
+        break;
+      }
+    }
+    resid(converged);
+    const double rnorm = dot(r, r);
+    {  // Olsen preconditioner (linear.C:50-60)
+      cuda_check(cudaMemcpyAsync(c0, row(B, converged), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy");
+      cuda_check(dev::launch_precondition(c0, diag, lam[converged], n, stream_), "precond");
+      const double num = dot(c0, r), den = dot(row(B, converged), c0);
+      cuda_check(dev::launch_axpy(-num / den, row(B, converged), r, n, stream_), "olsen");
+      cuda_check(dev::launch_precondition(r, diag, lam[converged], n, stream_), "precond");
+    }
+    if (rnorm < p.tol) {
+      ++converged;
+      if (converged == nroots) break;
+    } else {
+      if (k >= p.deflation_max) {
+        k = p.deflation_min;
+        ks = std::min(ks, k);
+      }
+      for (int j = 0; j < k; ++j) {
+        cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(r, r)), r, n, stream_), "scale");
+        cuda_check(dev::launch_axpy(-dot(r, row(B, j)), row(B, j), r, n, stream_), "gs");
+      }
+      cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(r, r)), r, n, stream_), "scale");
+      cuda_check(cudaMemcpyAsync(row(B, k), r, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "append");
+      ++k;
+    }
+    if (iter >= p.max_iter) break;
+  }
+  energies.assign(lam.begin(), lam.begin() + nroots);
+  if (waves_) free(waves_);
+  waves_ = alloc((int64_t)nroots * n);
+  cuda_check(cudaMemcpyAsync(waves_, B, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "waves");
+  wave_n_ = n;
+  nwaves_ = nroots;
+  for (double* q : {diag, B, S, T, r, c0, work, red, hmat, hvec, hw}) free(q);
+  cudaFreeAsync(offs, stream_);
+  cudaFreeAsync(dims, stream_);
+  cudaFreeAsync(status, stream_);
+  sync();
+  return iter;
+}
+
+// ------------------------------------------------------------------ density
+
+void GpuEngine::density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) {
+  const Block& B = left ? *sb.L : *sb.R;
+  const int nq = B.si.size();
+  std::vector<int64_t> off(nq);
+  int64_t tot = 0;
+  int maxn = 0;
+  dm_dims_.assign(nq, 0);
+  for (int q = 0; q < nq; ++q) {
+    off[q] = tot;
+    dm_dims_[q] = B.si.states[q];
+    tot += (int64_t)B.si.states[q] * B.si.states[q];
+    maxn = std::max(maxn, B.si.states[q]);
+  }
+  double* rho = alloc(tot);
+  cuda_check(cudaMemsetAsync(rho, 0, std::max<int64_t>(tot, 1) * sizeof(double), stream_), "memset");
+  // rho(q) = sum_r w_r sum_sectors psi psi^T (or psi^T psi for the right block)
+  std::vector<dev::GemmUnit> units;
+  std::vector<dev::GemmItem> items;
+  std::vector<dev::GemmTask> tasks;
+  for (int q = 0; q < nq; ++q) {
+    dev::GemmUnit u{};
+    u.c_buf = 1;
+    u.c_off = off[q];
+    u.ldc = B.si.states[q];
+    u.m = u.n = B.si.states[q];
+    u.beta_one = 0;
+    u.ibeg = (int)items.size();
+    for (int rr = 0; rr < nwaves_; ++rr) {
+      const double w = rr < (int)weights.size() ? weights[rr] : 1.0 / nwaves_;
+      for (const auto& S : sb.sectors) {
+        if ((left ? S.lq : S.rq) != q) continue;
+        dev::GemmItem g{};
+        g.a_buf = g.b_buf = 0;
+        g.a_off = g.b_off = (int64_t)rr * wave_n_ + S.offset;
+        g.lda = g.ldb = S.cols;
+        if (left) {
+          g.ta = 0;
+          g.tb = 1;
+          g.k = S.cols;
+        } else {
+          g.ta = 1;
+          g.tb = 0;
+          g.k = S.rows;
+        }
+        g.alpha = w;
+        items.push_back(g);
+      }
+    }
+    u.iend = (int)items.size();
+    units.push_back(u);
+  }
+  for (int u = 0; u < (int)units.size(); ++u) add_tasks(tasks, u, units[u].m, units[u].n);
+  DevArray<dev::GemmUnit> du;
+  DevArray<dev::GemmItem> di;
+  DevArray<dev::GemmTask> dt;
+  du.upload(units, stream_);
+  di.upload(items, stream_);
+  dt.upload(tasks, stream_);
+  dev::Bufs bufs{};
+  bufs.p[0] = waves_;
+  bufs.p[1] = rho;
+  cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "density");
+  // eigen-decomposition of every sector (diagonalise_dm)
+  if (dm_vecs_) free(dm_vecs_);
+  dm_vecs_ = alloc(tot);
+  dm_off_ = off;
+  double* w = alloc(std::max<int64_t>(B.si.total_states(), 1));
+  std::vector<int64_t> woff(nq);
+  int64_t wt = 0;
+  for (int q = 0; q < nq; ++q) {
+    woff[q] = wt;
+    wt += B.si.states[q];
+  }
+  DevArray<int64_t> doff, dwoff;
+  DevArray<int> ddims, dstat;
+  doff.upload(off, stream_);
+  dwoff.upload(woff, stream_);
+  ddims.upload(dm_dims_, stream_);
+  dstat.upload(std::vector<int>(nq, 0), stream_);
+  cuda_check(dev::launch_jacobi(rho, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, maxn, stream_),
+             "density eig");
+  std::vector<double> hw(wt);
+  std::vector<int> st(nq);
+  cuda_check(cudaMemcpyAsync(hw.data(), w, wt * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+  cuda_check(cudaMemcpyAsync(st.data(), dstat.d, nq * sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
+  sync();
+  for (int q = 0; q < nq; ++q)
+    if (st[q] < 0) throw std::runtime_error("density-matrix eigensolver did not converge");
+  spec.eig.assign(nq, {});
+  for (int q = 0; q < nq; ++q) spec.eig[q].assign(hw.begin() + woff[q], hw.begin() + woff[q] + B.si.states[q]);
+  du.release(stream_);
+  di.release(stream_);
+  dt.release(stream_);
+  doff.release(stream_);
+  dwoff.release(stream_);
+  ddims.release(stream_);
+  dstat.release(stream_);
+  free(rho);
+  free(w);
+  sync();
+}
+
+void GpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {
+  const int nq = (int)kept.size();
+  rot_off_.assign(nq, 0);
+  rot_kept_.assign(nq, 0);
+  rot_rows_.assign(nq, 0);
+  int64_t tot = 0;
+  std::vector<dev::GatherUnit> units;
+  std::vector<int> cols;
+  for (int q = 0; q < nq; ++q) {
+    rot_off_[q] = tot;
+    rot_kept_[q] = (int)kept[q].size();
+    rot_rows_[q] = dm_dims_[q];
+    dev::GatherUnit g{};
+    g.u_off = tot;
+    g.v_off = dm_off_[q];
+    g.n = dm_dims_[q];
+    g.m = rot_kept_[q];
+    g.c_off = (int)cols.size();
+    for (int c : kept[q]) cols.push_back(c);
+    if (g.m > 0) units.push_back(g);
+    tot += (int64_t)dm_dims_[q] * rot_kept_[q];
+  }
+  if (rot_) free(rot_);
+  rot_ = alloc(tot);
+  DevArray<dev::GatherUnit> du;
+  DevArray<int> dc;
+  du.upload(units, stream_);
+  dc.upload(cols, stream_);
+  cuda_check(dev::launch_gather_cols(dm_vecs_, rot_, du.d, dc.d, (int)units.size(), stream_), "gather");
+  du.release(stream_);
+  dc.release(stream_);
+  sync();
+}
+
+void GpuEngine::set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) {
+  const int nq = (int)kept.size();
+  rot_off_.assign(nq, 0);
+  rot_kept_ = kept;
+  rot_rows_.assign(nq, 0);
+  int64_t tot = 0;
+  for (int q = 0; q < nq; ++q) {
+    rot_off_[q] = tot;
+    rot_rows_[q] = kept[q] > 0 ? (int)(rot[q].size() / kept[q]) : 0;
+    tot += (int64_t)rot[q].size();
+  }
+  std::vector<double> h(std::max<int64_t>(tot, 1));
+  for (int q = 0; q < nq; ++q) std::copy(rot[q].begin(), rot[q].end(), h.begin() + rot_off_[q]);
+  if (rot_) free(rot_);
+  rot_ = alloc(tot);
+  cuda_check(cudaMemcpyAsync(rot_, h.data(), tot * sizeof(double), cudaMemcpyHostToDevice, stream_), "rot");
+  sync();
+}
+
+// O'(b',k') = U_b^T O(b,k) U_k in two grouped-GEMM launches per chunk of
+// operators (renormalise_transform, BaseOperator.C:341-363; MatrixRotate,
+// MatrixBLAS.C:553-572).
+void GpuEngine::renormalise(Block& small, const Block& big) {
+  double* dst = arena(small);
+  const double* src = arena(big);
+  const int64_t chunk_limit = 64ll << 20;  // scratch elements per chunk (512 MB)
+  std::vector<dev::GemmUnit> ua, ub;
+  std::vector<dev::GemmItem> ia, ib;
+  int64_t scratch = 0;
+  double* tmp = nullptr;
+  auto flush = [&]() {
+    if (ua.empty()) return;
+    std::vector<dev::GemmTask> ta, tb;
+    for (int u = 0; u < (int)ua.size(); ++u) add_tasks(ta, u, ua[u].m, ua[u].n);
+    for (int u = 0; u < (int)ub.size(); ++u) add_tasks(tb, u, ub[u].m, ub[u].n);
+    tmp = alloc(scratch);
+    DevArray<dev::GemmUnit> dua, dub;
+    DevArray<dev::GemmItem> dia, dib;
+    DevArray<dev::GemmTask> dta, dtb;
+    dua.upload(ua, stream_);
+    dub.upload(ub, stream_);
+    dia.upload(ia, stream_);
+    dib.upload(ib, stream_);
+    dta.upload(ta, stream_);
+    dtb.upload(tb, stream_);
+    dev::Bufs bufs{};
+    bufs.p[0] = const_cast<double*>(src);
+    bufs.p[1] = dst;
+    bufs.p[2] = rot_;
+    bufs.p[3] = tmp;
+    cuda_check(dev::launch_gemm(bufs, dua.d, dia.d, dta.d, (int)ta.size(), stream_), "rotate A");
+    cuda_check(dev::launch_gemm(bufs, dub.d, dib.d, dtb.d, (int)tb.size(), stream_), "rotate B");
+    for (auto* a : {&dua, &dub}) a->release(stream_);
+    for (auto* a : {&dia, &dib}) a->release(stream_);
+    for (auto* a : {&dta, &dtb}) a->release(stream_);
+    free(tmp);
+    ua.clear();
+    ub.clear();
+    ia.clear();
+    ib.clear();
+    scratch = 0;
+  };
+  cuda_check(cudaMemsetAsync(dst, 0, std::max<int64_t>(small.ops.arena, 1) * sizeof(double), stream_), "memset");
+  for (const auto& kv : small.ops.ops) {
+    const OpEntry& se = kv.second;
+    const OpLayout& SL = small.ops.layouts[se.layout];
+    const OpEntry& be = big.ops.at(kv.first);
+    const OpLayout& BL = big.ops.layouts[be.layout];
+    for (const OpBlock& sbk : SL.blocks) {
+      const int b = big.si.find(small.si.quanta[sbk.bra]);
+      const int k = big.si.find(small.si.quanta[sbk.ket]);
+      const int bi = BL.find(b, k);
+      if (bi < 0) continue;
+      const OpBlock& bb = BL.blocks[bi];
+      const int mb = rot_kept_[b], mk = rot_kept_[k];
+      // T = O U_k
+      dev::GemmUnit u{};
+      u.c_buf = 3;
+      u.c_off = scratch;
+      u.ldc = mk;
+      u.m = bb.rows;
+      u.n = mk;
+      u.beta_one = 0;
+      u.ibeg = (int)ia.size();
+      dev::GemmItem g{};
+      g.a_buf = 0;
+      g.a_off = be.base + bb.offset;
+      g.lda = bb.cols;
+      g.ta = 0;
+      g.b_buf = 2;
+      g.b_off = rot_off_[k];
+      g.ldb = mk;
+      g.tb = 0;
+      g.k = bb.cols;
+      g.alpha = 1.0;
+      ia.push_back(g);
+      u.iend = (int)ia.size();
+      ua.push_back(u);
+      // O' = U_b^T T
+      dev::GemmUnit v{};
+      v.c_buf = 1;
+      v.c_off = se.base + sbk.offset;
+      v.ldc = sbk.cols;
+      v.m = mb;
+      v.n = mk;
+      v.beta_one = 0;
+      v.ibeg = (int)ib.size();
+      dev::GemmItem h{};
+      h.a_buf = 2;
+      h.a_off = rot_off_[b];
+      h.lda = mb;
+      h.ta = 1;
+      h.b_buf = 3;
+      h.b_off = scratch;
+      h.ldb = mk;
+      h.tb = 0;
+      h.k = bb.rows;
+      h.alpha = 1.0;
+      ib.push_back(h);
+      v.iend = (int)ib.size();
+      ub.push_back(v);
+      scratch += (int64_t)bb.rows * mk;
+      if (scratch > chunk_limit) flush();
+    }
+  }
+  flush();
+  // keep host copies for single-site blocks (never renormalised in practice)
+  sync();
+}
+
+}  // namespace bgpu

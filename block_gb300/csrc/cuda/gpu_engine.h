@@ -1,0 +1,114 @@
+// CUDA engine of the sweep hot path: operator arenas in HBM, host-compiled
+// work lists, FP64 grouped-GEMM sigma, GPU Davidson, density matrix,
+// batched Jacobi eigensolver and U^T O U renormalisation.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <stdexcept>
+#include <set>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../host/sweep.h"
+#include "kernels.cuh"
+
+namespace bgpu {
+
+enum class Precision : int { FP64 = 0, BF16X3 = 1, FP16X2 = 2 };
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+void cuda_check(cudaError_t e, const char* what);
+
+// Device array of trivially-copyable descriptors.
+template <class T>
+struct DevArray {
+  T* d = nullptr;
+  size_t n = 0;
+  void upload(const std::vector<T>& h, cudaStream_t s);
+  void release(cudaStream_t s);
+};
+
+// Compiled sigma = H psi work lists of one superblock.
+struct SigmaPlan {
+  DevArray<dev::GemmUnit> u1, u2;
+  DevArray<dev::GemmItem> i1, i2;
+  DevArray<dev::GemmTask> t1, t2;
+  DevArray<dev::DiagUnit> du;
+  DevArray<dev::DiagItem> di;
+  double* scratch = nullptr;  // stage-1 intermediates
+  int64_t scratch_elems = 0;
+  double flops = 0.0;         // FP64-equivalent flops of one sigma
+  double bytes = 0.0;         // algorithmic bytes of one sigma (operator blocks + psi + sigma)
+  int64_t n = 0;
+  double ecore = 0.0;
+  int nstage1_units = 0, nstage2_units = 0, nitems = 0;
+};
+
+class GpuEngine : public Engine {
+ public:
+  explicit GpuEngine(int device = 0);
+  ~GpuEngine() override;
+  std::string name() const override { return "cuda"; }
+  void create_block(Block& b) override;
+  void release_block(Block& b) override;
+  void upload_block(Block& b, const std::vector<double>& arena) override;
+  void download_block(const Block& b, std::vector<double>& arena) override;
+  void build_block(Block& big, const Block& a, const Block& b,
+                   const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) override;
+  int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) override;
+  void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
+  void select_rotation(const std::vector<std::vector<int>>& kept) override;
+  void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
+  void renormalise(Block& small, const Block& big) override;
+
+  // pieces used by the C ABI, the tests and the bench
+  void plan_sigma(const Superblock& sb, SigmaPlan& plan);
+  void free_plan(SigmaPlan& plan);
+  // device pointers, stream-ordered on stream()
+  void sigma(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d);
+  void hdiag(const Superblock& sb, const SigmaPlan& plan, double* diag_d);
+  double* arena(const Block& b) const;
+  cudaStream_t stream() const { return stream_; }
+  double* alloc(int64_t elems);
+  void free(double* p);
+  void sync();
+  // last Davidson wavefunctions (device, nroots x n)
+  const double* waves() const { return waves_; }
+  int64_t wave_size() const { return wave_n_; }
+  Precision precision = Precision::FP64;
+  double sigma_seconds = 0.0;
+  long sigma_calls = 0;
+  double sigma_flops = 0.0;
+
+ private:
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  struct DevBlock {
+    double* d = nullptr;
+    int64_t n = 0;
+    std::vector<double> host;  // dot blocks keep a host copy (their 1x1 blocks fold into factors)
+    bool dot = false;
+  };
+  std::map<int, DevBlock> blocks_;
+  int next_handle_ = 0;
+  // current superblock plan (solve)
+  SigmaPlan plan_;
+  bool have_plan_ = false;
+  double* waves_ = nullptr;
+  int64_t wave_n_ = 0;
+  int nwaves_ = 0;
+  // density / rotation state
+  double* dm_vecs_ = nullptr;
+  std::vector<int64_t> dm_off_;
+  std::vector<int> dm_dims_;
+  double* rot_ = nullptr;
+  std::vector<int64_t> rot_off_;
+  std::vector<int> rot_kept_, rot_rows_;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+};
+
+}  // namespace bgpu

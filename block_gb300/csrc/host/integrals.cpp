@@ -344,6 +344,29 @@ Config parse_config(const std::string& path) {
   return parse_config_text(ss.str(), dir);
 }
 
+Integrals load_integrals(Config& c) {
+  Integrals I0;
+  const std::string key = "synthetic:";
+  std::string o = c.orbitals;
+  const auto pos = o.find(key);
+  if (pos != std::string::npos) {
+    std::string spec = o.substr(pos + key.size());
+    for (auto& ch : spec)
+      if (ch == ':') ch = ' ';
+    std::istringstream is(spec);
+    int norb = 0, nelec = 0, nchol = 0, d2h = 0;
+    unsigned long long seed = 0;
+    is >> norb >> nelec >> nchol >> seed >> d2h;
+    if (norb <= 0) throw std::runtime_error("bad synthetic spec " + o);
+    I0 = synthetic_hamiltonian(norb, nelec, nchol, seed, d2h != 0);
+    if (d2h) c.sym = "d2h";
+  } else {
+    I0 = read_fcidump(o);
+  }
+  if (c.nelec < 0) c.nelec = I0.nelec;
+  return reorder(I0, orbital_order(I0, c.reorder));
+}
+
 void make_default_schedule(Config& c) {
   // the reference's ladder (Schedule.C:13-98): M steps and sweeps per step
   const int defM[] = {50, 100, 250, 500, 1000, 2000, 3000, 4000, 5000, 6000, 7000, 8000, 9000, 10000};

@@ -83,6 +83,10 @@ struct Config {
 };
 
 Config parse_config(const std::string& path);
+// Integrals named by `orbitals`: an FCIDUMP path, or a generated Hamiltonian
+// `synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h 0|1>`; reordered as the
+// configuration asks.
+Integrals load_integrals(Config& c);
 Config parse_config_text(const std::string& text, const std::string& base_dir);
 // The reference's default schedule (Schedule.C generateDefaultSchedule) for
 // `schedule default` with startM/maxM.

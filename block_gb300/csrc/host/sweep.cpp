@@ -264,6 +264,35 @@ void SweepDriver::warmup() {
   }
 }
 
+void SweepDriver::warmup_left(int upto) {
+  const int M = C_.schedule.front().M;
+  for (int q = 1; q <= upto; ++q) {
+    Block& sys = left_block(q - 1);
+    std::vector<int> own;
+    for (int i = 0; i <= q; ++i) own.push_back(i);
+    CatalogSpec spec = renorm_spec(own, q + 1, loop_is_left(q + 1));
+    Block big = make_enlarged(sys, q, /*dot_on_right=*/true, spec);
+    std::vector<int> kept = warmup_rotation(big, M, C_.seed + 6271ull * (uint64_t)q);
+    if (left_[q]) E_.release_block(*left_[q]);
+    left_[q] = renormalised(big, kept, spec);
+    E_.release_block(big);
+  }
+}
+
+Superblock SweepDriver::prepare_partition(int p, Block& L, Block& R) {
+  if (p < 1 || p > N_ - 3) throw std::runtime_error("partition out of range");
+  warmup();
+  warmup_left(p - 1);
+  std::vector<int> Ls, Rs;
+  for (int i = 0; i <= p; ++i) Ls.push_back(i);
+  for (int i = p + 1; i < N_; ++i) Rs.push_back(i);
+  const bool loopL = loop_is_left(p);
+  const std::vector<int>& loop_sites = loopL ? Ls : Rs;
+  L = make_enlarged(left_block(p - 1), p, true, sigma_spec(Ls, Rs, loopL, loop_sites));
+  R = make_enlarged(right_block(p + 2), p + 1, false, sigma_spec(Rs, Ls, !loopL, loop_sites));
+  return make_superblock(L, R);
+}
+
 // Truncation: keep the M largest density-matrix eigenvalues above 1e-13
 // (makeRotateMatrix / sort_weights / assign_matrix_by_dm,
 // renormalise.C:135-166, rotationmat.C:149-339); returns discarded weight.

@@ -106,7 +106,14 @@ class SweepDriver {
   SweepResult run();
   // pieces used by tests and the bench
   void warmup();
+  // left blocks [0..q] for q = 1..upto from seeded random rotations
+  void warmup_left(int upto);
   double sweep(bool forward, int sweep_index);
+  // Superblock of partition p (L=[0..p], R=[p+1..N-1]) built from warm-up
+  // blocks on both sides: the sector structure and operator catalogue of a
+  // mid-sweep step with bond dimension M, without any Davidson solve.
+  // L and R receive the enlarged blocks (owned by the caller).
+  Superblock prepare_partition(int p, Block& L, Block& R);
   const Integrals& integrals() const { return I_; }
   // builds the superblock of a forward step at partition p (L = [0..p])
   // using current blocks; useful for snapshots.

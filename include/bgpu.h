@@ -1,0 +1,172 @@
+/*
+ * C ABI of the GB300 sweep hot path of spin-adapted two-site DMRG.
+ *
+ * Everything is plain pointers and sizes; device memory is owned by the
+ * library; one host thread per context; calls are stream-ordered on the
+ * context's stream and return when their results are ready (host buffers)
+ * unless stated otherwise.  Every entry point returns BGPU_OK or an error
+ * code, with the message available from bgpu_last_error_string().
+ *
+ * The reference has no plugin API for this path; its call sites are
+ * internal C++ functions.  Each entry point below names the reference
+ * function whose work it replaces (file:line in sanshar/Block).
+ *
+ * Conventions shared with the reference:
+ *  - quanta are (particle number, 2S, irrep) triples; irreps are 0-based
+ *    abelian indices with XOR products (Symmetry.C:22-120);
+ *  - an operator is an SU(2) tensor stored as reduced dense blocks for every
+ *    allowed (bra quantum, ket quantum) pair, enumerated bra-major then
+ *    ket, each block row-major (SparseMatrix::allocate, BaseOperator.C:123-145;
+ *    Newmat row-major storage, MatrixBLAS.C:144); operators of a block are
+ *    laid out back to back in the order of their keys (type, i, j, 2k)
+ *    sorted ascending;
+ *  - a wavefunction is block-sparse over the (left quantum, right quantum)
+ *    sectors coupling to the target, left-major, each sector row-major
+ *    (Wavefunction::initialise, wavefunction.C:17-52).
+ */
+#ifndef BGPU_H
+#define BGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BGPU_OK 0
+#define BGPU_ERR_INVALID 1
+#define BGPU_ERR_CUDA 2
+#define BGPU_ERR_RUNTIME 3
+
+/* operator types (BaseOperator.h:35-45) */
+#define BGPU_OP_HAM 0
+#define BGPU_OP_CRE 1
+#define BGPU_OP_CRE_DES 2
+#define BGPU_OP_CRE_CRE 3
+#define BGPU_OP_CRE_DESCOMP 4
+#define BGPU_OP_DES_DESCOMP 5
+#define BGPU_OP_CRE_CRE_DESCOMP 6
+#define BGPU_OP_OVERLAP 7
+
+/* arithmetic of the sigma product */
+#define BGPU_PREC_FP64 0
+#define BGPU_PREC_BF16X3 1
+#define BGPU_PREC_FP16X2 2
+
+typedef struct bgpu_ctx bgpu_ctx;
+
+/* Context on CUDA device `device`. */
+int bgpu_create(bgpu_ctx** ctx, int device);
+int bgpu_destroy(bgpu_ctx* ctx);
+const char* bgpu_last_error_string(const bgpu_ctx* ctx);
+/* Library version string. */
+const char* bgpu_version(void);
+/* Arithmetic of sigma products (BGPU_PREC_*). */
+int bgpu_set_precision(bgpu_ctx* ctx, int precision);
+
+/*
+ * Declare a block: its state space and operator catalogue.
+ * Replaces the SpinBlock state (spinblock.h:104-259) and the operator
+ * containers Op_component / SparseMatrix::allocate (op_components.h:161-210,
+ * BaseOperator.C:123-145).
+ *   norb, orbsym[norb]: orbital irreps (0-based), group: "c1", "d2h", ...
+ *   quanta[3*nquanta]: (n, 2S, irrep) sorted ascending; states[nquanta]
+ *   op_keys[4*nops]: (type, i, j, 2k) per operator
+ *   is_dot: 1 for single-site blocks
+ * Returns a block handle and the number of doubles of its operator arena.
+ */
+int bgpu_block_define(bgpu_ctx* ctx, int norb, const int* orbsym, const char* group, int nquanta, const int* quanta,
+                      const int* states, int nops, const int* op_keys, int is_dot, int* handle,
+                      int64_t* arena_elems);
+/* Element offset of every operator of a block inside its arena (nops values,
+ * in the order the operators were declared). */
+int bgpu_block_op_offsets(bgpu_ctx* ctx, int handle, int64_t* offsets, int nops);
+/* Copy a whole operator arena in / out (host buffers, `n` doubles). */
+int bgpu_block_upload(bgpu_ctx* ctx, int handle, const double* arena, int64_t n);
+int bgpu_block_download(bgpu_ctx* ctx, int handle, double* arena, int64_t n);
+int bgpu_block_free(bgpu_ctx* ctx, int handle);
+
+/*
+ * Superblock L|R with its operator-pair list; compiles the sigma work lists.
+ * Replaces the set-up of SpinBlock::multiplyH (spinblock.C:722-789) and the
+ * opxop pair loops (opxop.C:155-285).
+ *   target[3]: (n, 2S, irrep) of the wavefunction
+ *   nterms, coef[nterms], term_ops[4*nterms] = (left op index | -1 identity,
+ *   left transpose flag, right op index | -1, right transpose flag); op
+ *   indices refer to the op_keys order of the blocks' declarations; every
+ *   term is coef * [left x right]^0 applied to psi (TensorMultiply,
+ *   operatorfunctions.C:485-537).
+ *   ecore: constant added as ecore * psi
+ * Returns a superblock handle and the number of doubles of a wavefunction.
+ */
+int bgpu_superblock_define(bgpu_ctx* ctx, int left, int right, const int* target, int nterms, const double* coef,
+                           const int* term_ops, double ecore, int* sb, int64_t* psi_elems);
+int bgpu_superblock_free(bgpu_ctx* ctx, int sb);
+/* Algorithmic work of one sigma: FP64-equivalent flops and bytes. */
+int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes);
+
+/*
+ * sigma = H psi on host buffers (copies in and out are part of the call).
+ * Replaces SpinBlock::multiplyH (spinblock.C:722-789) as called by the
+ * Davidson functor (davidson.C:19-22).
+ */
+int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma);
+/* Same on device pointers (stream-ordered, asynchronous). */
+int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev);
+/* Diagonal of H (SpinBlock::diagonalH, spinblock.C:855-899). */
+int bgpu_hdiag(bgpu_ctx* ctx, int sb, double* diag);
+/*
+ * Block Davidson for the lowest `nroots` states (Linear::block_davidson,
+ * linear.C:179-385): tol bounds the squared residual norm.  energies[nroots];
+ * vectors (nroots x psi_elems, may be NULL) receive the eigenvectors.
+ */
+int bgpu_davidson(bgpu_ctx* ctx, int sb, int nroots, double tol, int max_iter, double* energies, double* vectors,
+                  int* iterations);
+/*
+ * Reduced density matrix of the left (left=1) or right block from the last
+ * Davidson vectors with root weights[nroots] and its per-sector
+ * eigenvalues, ascending within each sector, concatenated in sector order
+ * (DensityMatrix::makedensitymatrix, density.C:27-90; diagonalise_dm,
+ * rotationmat.C:258-279).
+ */
+int bgpu_density_eig(bgpu_ctx* ctx, int sb, int left, int nroots, const double* weights, double* eigvals,
+                     int64_t n_eigvals);
+
+/*
+ * Device-memory accounting: pointer to a device buffer of `n` doubles owned
+ * by the context (for callers that drive bgpu_sigma_device).
+ */
+int bgpu_device_alloc(bgpu_ctx* ctx, int64_t n, double** ptr);
+int bgpu_device_free(bgpu_ctx* ctx, double* ptr);
+int bgpu_copy_to_device(bgpu_ctx* ctx, double* dst, const double* src, int64_t n);
+int bgpu_copy_to_host(bgpu_ctx* ctx, double* dst, const double* src, int64_t n);
+int bgpu_synchronize(bgpu_ctx* ctx);
+
+/*
+ * Superblock of the bipartition after orbital `partition` (left block
+ * [0..partition], right block [partition+1..norb-1]) for the system of a
+ * dmrg.conf, built from warm-up blocks of bond dimension M (the first
+ * schedule entry) made by seeded random rotations: the sector structure and
+ * operator catalogue of a mid-sweep step (InitBlocks / BlockAndDecimate,
+ * sweep.C:91-178) without the Davidson solves.  The superblock owns its
+ * blocks; use it with bgpu_sigma / bgpu_davidson / bgpu_hdiag.
+ */
+int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition, int* sb, int64_t* psi_elems);
+
+/*
+ * Full two-site sweep DMRG from a dmrg.conf and its FCIDUMP (the
+ * `block.spin_adapted dmrg.conf` entry, main.C:25-52 / dmrg.C:600-706), with
+ * all operator and wavefunction arithmetic on the GPU.  `orbitals` may also
+ * name a generated Hamiltonian: synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>.
+ * energies[max_roots] receive the final energies; stats[8] (may be NULL):
+ *   sweeps, sigma calls, sigma seconds, sigma flops, total seconds, max
+ *   discarded weight, last-sweep energy, number of roots.
+ */
+int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
+                  double* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BGPU_H */

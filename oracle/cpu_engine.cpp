@@ -116,13 +116,6 @@ bool view(const Block& B, const double* arena, const Operand& o, int bra, int ke
 int rank2(const Operand& o) { return o.identity ? 0 : o.key.k2; }
 bool fermion(const Operand& o) { return !o.identity && op_fermion(o.key); }
 
-// dense copy of a view (scaled)
-void dense(const View& v, std::vector<double>& out) {
-  out.assign((size_t)v.rows * v.cols, 0.0);
-  for (int r = 0; r < v.rows; ++r)
-    for (int c = 0; c < v.cols; ++c) out[(size_t)r * v.cols + c] = v.at(r, c);
-}
-
 }  // namespace
 
 // ------------------------------------------------------------- engine

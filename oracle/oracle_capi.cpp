@@ -1,1 +1,287 @@
-// placeholder
+// TEST INFRASTRUCTURE ONLY: C entry points of the CPU oracle for the Python
+// tests and the bench's CPU baseline.  Runs the oracle sweep, or stops it at
+// a chosen step and exposes that step's superblock (blocks, operator-pair
+// list, wavefunction and the oracle's sigma) so the CUDA library can be fed
+// the same inputs through its C ABI.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "cpu_engine.h"
+
+using namespace bgpu;
+
+namespace {
+struct Captured {};
+
+struct SnapBlock {
+  std::vector<int> quanta, states, keys;
+  std::vector<double> arena;
+  std::vector<OpKey> order;
+  int is_dot = 0;
+};
+
+struct Snapshot {
+  SnapBlock L, R;
+  std::vector<double> coef;
+  std::vector<int> ops;
+  std::vector<double> psi, sigma, diag;
+  int target[3] = {0, 0, 0};
+  double ecore = 0.0;
+  double energy = 0.0;
+  std::vector<int> orbsym;
+  std::string group;
+  double sigma_seconds = 0.0;
+  int threads = 1;
+};
+
+SnapBlock snap_block(const Block& b, oracle::CpuEngine& e) {
+  SnapBlock s;
+  for (int q = 0; q < b.si.size(); ++q) {
+    s.quanta.push_back(b.si.quanta[q].n);
+    s.quanta.push_back(b.si.quanta[q].s2);
+    s.quanta.push_back(b.si.quanta[q].irrep);
+    s.states.push_back(b.si.states[q]);
+  }
+  for (const auto& kv : b.ops.ops) {
+    s.order.push_back(kv.first);
+    s.keys.push_back((int)kv.first.type);
+    s.keys.push_back(kv.first.i);
+    s.keys.push_back(kv.first.j);
+    s.keys.push_back(kv.first.k2);
+  }
+  s.arena = e.arena(b);
+  s.is_dot = b.is_dot ? 1 : 0;
+  return s;
+}
+
+int index_of(const SnapBlock& s, const Operand& o) {
+  if (o.identity) return -1;
+  for (size_t i = 0; i < s.order.size(); ++i)
+    if (s.order[i] == o.key) return (int)i;
+  return -2;
+}
+}  // namespace
+
+extern "C" {
+
+int oracle_run(const char* conf, int threads, int verbose, double* energies, int max_roots, double* stats) {
+  try {
+    auto t0 = std::chrono::steady_clock::now();
+    Config c = parse_config(conf);
+    Integrals I = load_integrals(c);
+    oracle::CpuEngine eng(threads);
+    DriverOptions opt;
+    opt.verbose = verbose;
+    SweepResult r;
+    {
+      SweepDriver drv(I, c, eng, opt);
+      r = drv.run();
+    }
+    for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
+    if (stats) {
+      stats[0] = r.sweeps;
+      stats[1] = (double)eng.sigma_calls;
+      stats[2] = eng.sigma_seconds;
+      stats[3] = 0.0;
+      stats[4] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      stats[5] = r.discarded;
+      stats[6] = r.sweep_energies.empty() ? 0.0 : r.sweep_energies.back();
+      stats[7] = (double)r.energies.size();
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_run: %s\n", e.what());
+    return 1;
+  }
+}
+
+// Run `conf` and capture the superblock of step (sweep, pos); nullptr on error.
+void* oracle_snapshot(const char* conf, int sweep, int pos, int threads) {
+  auto snap = std::make_unique<Snapshot>();
+  try {
+    Config c = parse_config(conf);
+    Integrals I = load_integrals(c);
+    oracle::CpuEngine eng(threads);
+    DriverOptions opt;
+    snap->orbsym = I.orbsym;
+    snap->group = c.sym;
+    snap->threads = eng.threads;
+    opt.on_step = [&](const Superblock& sb, int s, int p) {
+      if (s != sweep || p != pos) return;
+      snap->L = snap_block(*sb.L, eng);
+      snap->R = snap_block(*sb.R, eng);
+      for (const auto& t : sb.terms) {
+        snap->coef.push_back(t.coef);
+        snap->ops.push_back(index_of(snap->L, t.l));
+        snap->ops.push_back(t.l.trans ? 1 : 0);
+        snap->ops.push_back(index_of(snap->R, t.r));
+        snap->ops.push_back(t.r.trans ? 1 : 0);
+      }
+      snap->psi = eng.wavefunctions().at(0);
+      snap->sigma.assign(sb.size, 0.0);
+      auto t0 = std::chrono::steady_clock::now();
+      eng.sigma(sb, snap->psi.data(), snap->sigma.data());
+      snap->sigma_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      snap->diag.assign(sb.size, 0.0);
+      eng.hdiag(sb, snap->diag.data());
+      snap->target[0] = sb.target.n;
+      snap->target[1] = sb.target.s2;
+      snap->target[2] = sb.target.irrep;
+      snap->ecore = sb.ecore;
+      double e = 0;
+      for (size_t i = 0; i < snap->psi.size(); ++i) e += snap->psi[i] * snap->sigma[i];
+      snap->energy = e;
+      throw Captured{};
+    };
+    try {
+      SweepDriver drv(I, c, eng, opt);
+      drv.run();
+    } catch (const Captured&) {
+      return snap.release();
+    }
+    std::fprintf(stderr, "oracle_snapshot: step (%d,%d) not reached\n", sweep, pos);
+    return nullptr;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_snapshot: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+void oracle_snapshot_free(void* h) { delete static_cast<Snapshot*>(h); }
+
+// sizes: [0]=nquanta L, [1]=nops L, [2]=arena L, [3]=nquanta R, [4]=nops R,
+// [5]=arena R, [6]=nterms, [7]=psi size, [8]=norb, [9]=L is dot, [10]=R is dot
+void oracle_snapshot_sizes(void* h, int64_t* out) {
+  auto* s = static_cast<Snapshot*>(h);
+  out[0] = (int64_t)s->L.states.size();
+  out[1] = (int64_t)s->L.order.size();
+  out[2] = (int64_t)s->L.arena.size();
+  out[3] = (int64_t)s->R.states.size();
+  out[4] = (int64_t)s->R.order.size();
+  out[5] = (int64_t)s->R.arena.size();
+  out[6] = (int64_t)s->coef.size();
+  out[7] = (int64_t)s->psi.size();
+  out[8] = (int64_t)s->orbsym.size();
+  out[9] = s->L.is_dot;
+  out[10] = s->R.is_dot;
+}
+
+void oracle_snapshot_block(void* h, int which, int* quanta, int* states, int* keys, double* arena) {
+  auto* s = static_cast<Snapshot*>(h);
+  const SnapBlock& b = which == 0 ? s->L : s->R;
+  std::memcpy(quanta, b.quanta.data(), b.quanta.size() * sizeof(int));
+  std::memcpy(states, b.states.data(), b.states.size() * sizeof(int));
+  std::memcpy(keys, b.keys.data(), b.keys.size() * sizeof(int));
+  std::memcpy(arena, b.arena.data(), b.arena.size() * sizeof(double));
+}
+
+// misc[0..2] target, misc[3] ecore, misc[4] energy <psi|H|psi>, misc[5] oracle sigma seconds, misc[6] threads
+void oracle_snapshot_data(void* h, double* coef, int* ops, double* psi, double* sigma, double* diag, int* orbsym,
+                          double* misc) {
+  auto* s = static_cast<Snapshot*>(h);
+  std::memcpy(coef, s->coef.data(), s->coef.size() * sizeof(double));
+  std::memcpy(ops, s->ops.data(), s->ops.size() * sizeof(int));
+  std::memcpy(psi, s->psi.data(), s->psi.size() * sizeof(double));
+  std::memcpy(sigma, s->sigma.data(), s->sigma.size() * sizeof(double));
+  std::memcpy(diag, s->diag.data(), s->diag.size() * sizeof(double));
+  std::memcpy(orbsym, s->orbsym.data(), s->orbsym.size() * sizeof(int));
+  misc[0] = s->target[0];
+  misc[1] = s->target[1];
+  misc[2] = s->target[2];
+  misc[3] = s->ecore;
+  misc[4] = s->energy;
+  misc[5] = s->sigma_seconds;
+  misc[6] = s->threads;
+}
+
+const char* oracle_snapshot_group(void* h) { return static_cast<Snapshot*>(h)->group.c_str(); }
+
+// Time `reps` oracle sigma products on the captured superblock with `threads`
+// threads (CPU baseline of the bench); returns seconds per product.
+double oracle_time_sigma(const char* conf, int sweep, int pos, int threads, int reps) {
+  double per = -1.0;
+  try {
+    Config c = parse_config(conf);
+    Integrals I = load_integrals(c);
+    oracle::CpuEngine eng(threads);
+    DriverOptions opt;
+    opt.on_step = [&](const Superblock& sb, int s, int p) {
+      if (s != sweep || p != pos) return;
+      std::vector<double> psi = eng.wavefunctions().at(0), out(sb.size);
+      auto t0 = std::chrono::steady_clock::now();
+      for (int r = 0; r < reps; ++r) eng.sigma(sb, psi.data(), out.data());
+      per = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() / reps;
+      throw Captured{};
+    };
+    try {
+      SweepDriver drv(I, c, eng, opt);
+      drv.run();
+    } catch (const Captured&) {
+    }
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_time_sigma: %s\n", e.what());
+  }
+  return per;
+}
+
+}  // extern "C"
+
+extern "C" {
+// Superblock of `partition` built from seeded warm-up blocks (same
+// construction as bgpu_prepare_superblock) captured as a snapshot whose psi
+// is a seeded random unit vector.
+void* oracle_prepare(const char* conf, int partition, int threads) {
+  auto snap = std::make_unique<Snapshot>();
+  try {
+    Config c = parse_config(conf);
+    Integrals I = load_integrals(c);
+    oracle::CpuEngine eng(threads);
+    snap->orbsym = I.orbsym;
+    snap->group = c.sym;
+    snap->threads = eng.threads;
+    SweepDriver drv(I, c, eng);
+    Block L, R;
+    Superblock sb = drv.prepare_partition(partition, L, R);
+    sb.L = &L;
+    sb.R = &R;
+    snap->L = snap_block(L, eng);
+    snap->R = snap_block(R, eng);
+    for (const auto& t : sb.terms) {
+      snap->coef.push_back(t.coef);
+      snap->ops.push_back(index_of(snap->L, t.l));
+      snap->ops.push_back(t.l.trans ? 1 : 0);
+      snap->ops.push_back(index_of(snap->R, t.r));
+      snap->ops.push_back(t.r.trans ? 1 : 0);
+    }
+    Rng rng(c.seed + 99991);
+    snap->psi.resize(sb.size);
+    double nrm = 0;
+    for (auto& x : snap->psi) {
+      x = rng.normal();
+      nrm += x * x;
+    }
+    for (auto& x : snap->psi) x /= std::sqrt(nrm);
+    snap->sigma.assign(sb.size, 0.0);
+    auto t0 = std::chrono::steady_clock::now();
+    eng.sigma(sb, snap->psi.data(), snap->sigma.data());
+    snap->sigma_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    snap->diag.assign(sb.size, 0.0);
+    eng.hdiag(sb, snap->diag.data());
+    snap->target[0] = sb.target.n;
+    snap->target[1] = sb.target.s2;
+    snap->target[2] = sb.target.irrep;
+    snap->ecore = sb.ecore;
+    double e = 0;
+    for (size_t i = 0; i < snap->psi.size(); ++i) e += snap->psi[i] * snap->sigma[i];
+    snap->energy = e;
+    eng.release_block(L);
+    eng.release_block(R);
+    return snap.release();
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_prepare: %s\n", e.what());
+    return nullptr;
+  }
+}
+}  // extern "C"

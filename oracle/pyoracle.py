@@ -1,0 +1,110 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes access to the CPU oracle (liboracle.so).
+
+Used by tests/ and by bench.py's CPU-baseline leg; never by block_gb300.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+EXE = os.path.join(HERE, "_build", "dmrg_oracle")
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "-j", str(min(16, os.cpu_count() or 4))], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        DP = ctypes.POINTER(ctypes.c_double)
+        L.oracle_run.restype = I
+        L.oracle_run.argtypes = [ctypes.c_char_p, I, I, DP, I, DP]
+        L.oracle_snapshot.restype = P
+        L.oracle_snapshot.argtypes = [ctypes.c_char_p, I, I, I]
+        L.oracle_prepare.restype = P
+        L.oracle_prepare.argtypes = [ctypes.c_char_p, I, I]
+        L.oracle_snapshot_free.argtypes = [P]
+        L.oracle_snapshot_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_snapshot_block.argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), DP]
+        L.oracle_snapshot_data.argtypes = [P, DP, ctypes.POINTER(I), DP, DP, DP, ctypes.POINTER(I), DP]
+        L.oracle_snapshot_group.restype = ctypes.c_char_p
+        L.oracle_snapshot_group.argtypes = [P]
+        L.oracle_time_sigma.restype = D
+        L.oracle_time_sigma.argtypes = [ctypes.c_char_p, I, I, I, I]
+        _lib = L
+    return _lib
+
+
+def run(conf, threads=0, verbose=0, max_roots=32):
+    L = lib()
+    e = np.zeros(max_roots)
+    st = np.zeros(8)
+    rc = L.oracle_run(conf.encode(), threads, verbose, e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), max_roots,
+                      st.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    if rc != 0:
+        raise RuntimeError("oracle run failed for " + conf)
+    n = int(st[7])
+    return e[:n].copy(), dict(sweeps=int(st[0]), sigma_calls=int(st[1]), sigma_seconds=st[2], seconds=st[4],
+                              discarded=st[5], last_sweep_energy=st[6])
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def _unpack(L, h):
+    if not h:
+        raise RuntimeError("oracle snapshot failed")
+    sz = np.zeros(11, dtype=np.int64)
+    L.oracle_snapshot_sizes(h, sz.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    snap = {}
+    for which, (nq, nops, na) in ((0, sz[0:3]), (1, sz[3:6])):
+        q = np.zeros(3 * nq, dtype=np.int32)
+        s = np.zeros(nq, dtype=np.int32)
+        k = np.zeros(4 * nops, dtype=np.int32)
+        a = np.zeros(na, dtype=np.float64)
+        L.oracle_snapshot_block(h, which, _ptr(q, ctypes.c_int), _ptr(s, ctypes.c_int), _ptr(k, ctypes.c_int),
+                                _ptr(a, ctypes.c_double))
+        snap["L" if which == 0 else "R"] = dict(quanta=q.reshape(-1, 3), states=s, keys=k.reshape(-1, 4), arena=a,
+                                                is_dot=int(sz[9 + which]))
+    nt, n, norb = int(sz[6]), int(sz[7]), int(sz[8])
+    coef = np.zeros(nt)
+    ops = np.zeros(4 * nt, dtype=np.int32)
+    psi = np.zeros(n)
+    sig = np.zeros(n)
+    diag = np.zeros(n)
+    orbsym = np.zeros(norb, dtype=np.int32)
+    misc = np.zeros(8)
+    L.oracle_snapshot_data(h, _ptr(coef, ctypes.c_double), _ptr(ops, ctypes.c_int), _ptr(psi, ctypes.c_double),
+                           _ptr(sig, ctypes.c_double), _ptr(diag, ctypes.c_double), _ptr(orbsym, ctypes.c_int),
+                           _ptr(misc, ctypes.c_double))
+    snap.update(coef=coef, ops=ops.reshape(-1, 4), psi=psi, sigma=sig, diag=diag, orbsym=orbsym,
+                target=misc[0:3].astype(np.int32), ecore=misc[3], energy=misc[4], sigma_seconds=misc[5],
+                threads=int(misc[6]), group=L.oracle_snapshot_group(h).decode())
+    L.oracle_snapshot_free(h)
+    return snap
+
+
+def snapshot(conf, sweep, pos, threads=0):
+    """Superblock of step (sweep, pos) of an oracle run, with psi = root 0."""
+    L = lib()
+    return _unpack(L, L.oracle_snapshot(conf.encode(), sweep, pos, threads))
+
+
+def prepare(conf, partition, threads=0):
+    """Superblock built from seeded warm-up blocks (see bgpu_prepare_superblock)."""
+    L = lib()
+    return _unpack(L, L.oracle_prepare(conf.encode(), partition, threads))
+
+
+def time_sigma(conf, sweep, pos, threads=0, reps=3):
+    return lib().oracle_time_sigma(conf.encode(), sweep, pos, threads, reps)

@@ -1,0 +1,46 @@
+"""Writes the dmrg.conf inputs of the benchmark configurations.
+
+hubbard12: open 12-site Hubbard chain, t=1, U=4, half filling (FCIDUMP
+written here).  syn24 / syn30 / syn30_d2h / syn40: seeded synthetic
+Cholesky Hamiltonians generated inside the library from the `orbitals
+synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>` spec; syn8 / syn8_d2h are
+small members of the same family used for FCI cross-checks.
+"""
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def hubbard_fcidump(path, n=12, t=1.0, u=4.0):
+    with open(path, "w") as f:
+        f.write(" &FCI NORB=%d,NELEC=%d,MS2=0,\n  ORBSYM=%s\n  ISYM=1\n &END\n" % (n, n, ",".join(["1"] * n)))
+        for i in range(1, n + 1):
+            f.write("%20.12f %4d %4d %4d %4d\n" % (u, i, i, i, i))
+        for i in range(1, n):
+            f.write("%20.12f %4d %4d %4d %4d\n" % (-t, i + 1, i, 0, 0))
+        f.write("%20.12f %4d %4d %4d %4d\n" % (0.0, 0, 0, 0, 0))
+
+
+CONFS = {
+    "hubbard12": ("FCIDUMP", "nelec 12\nspin 0\nschedule\n0 50 1e-8 0\n2 100 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn8": ("synthetic:8:8:16:8:0", "nelec 8\nspin 0\nschedule\n0 200 1e-12 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn8_d2h": ("synthetic:8:8:16:8:1", "nelec 8\nspin 0\nschedule\n0 200 1e-12 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn24": ("synthetic:24:24:48:24:0", "nelec 24\nspin 0\nschedule\n0 500 1e-8 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn30": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn30_d2h": ("synthetic:30:30:60:30:1", "nelec 30\nspin 0\nschedule\n0 1500 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn40": ("synthetic:40:40:80:40:0", "nelec 40\nspin 0\nnroots 3\nweights 0.333333333333 0.333333333333 0.333333333334\nschedule\n0 4000 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
+}
+
+
+def main():
+    for name, (orb, body) in CONFS.items():
+        d = os.path.join(HERE, name)
+        os.makedirs(d, exist_ok=True)
+        if orb == "FCIDUMP":
+            hubbard_fcidump(os.path.join(d, "FCIDUMP"))
+        with open(os.path.join(d, "dmrg.conf"), "w") as f:
+            f.write(body + "orbitals %s\n" % orb)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,55 @@
+"""Regenerates the golden fixtures of this directory from the reference tree.
+
+Copies the FCIDUMP inputs of the reference's energy tests (data files only)
+and records the expected energies its test scripts check:
+  dmrg_tests/runtest:12,23,30 (test_energy.py tolerance 1e-6) and
+  pydmrg/tests/test_dmrg_simple.py:34 (10 decimal places).
+Run in a container that has the reference mounted; the GPU machine only reads
+the committed copies.
+"""
+import hashlib
+import json
+import os
+import shutil
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CASES = {
+    # name: (source FCIDUMP, conf body, expected energies, citation)
+    "hubbard": ("dmrg_tests/hubbard/FCIDUMP",
+                "nelec 8\nspin 0\nhf_occ integral\nschedule\n0 50 1.0e-6 0\n4 150 1e-6 0\n6 200 1e-6 0\n8 200 1e-8 0\nend\n"
+                "maxiter 30\nsweep_tol 1e-9\nnroots 2\nweights 0.5 0.5\n",
+                [-6.56819216], "dmrg_tests/runtest:30"),
+    "pydmrg_fcidump1": ("pydmrg/tests/FCIDUMP-1",
+                        "nelec 4\nspin 0\nirrep 1\nhf_occ integral\nschedule\n0 20 1.0e-6 0\n8 50 1e-8 0\n18 100 1e-8 0\nend\n"
+                        "maxiter 30\nsweep_tol 1e-8\nsym d2h\n",
+                        [-17.10516373008], "pydmrg/tests/test_dmrg_simple.py:34"),
+    "c2_d2h": ("dmrg_tests/c2_d2h/FCIDUMP",
+               "nelec 8\nspin 0\nirrep 1\nhf_occ integral\nschedule\n0 50 1.0e-6 0\n4 150 1e-6 0\n6 400 1e-6 0\n8 400 1e-10 0\nend\n"
+               "maxiter 12\nsweep_tol 1e-9\nsym d2h\nnroots 2\nweights 0.5 0.5\n",
+               [-75.4844085040, -74.9778423596], "dmrg_tests/runtest:12"),
+    "h2o_nosym": ("dmrg_tests/h2o_nosym/FCIDUMP",
+                  "nelec 10\nspin 0\nirrep 1\nhf_occ integral\nschedule default\nstartM 100\nmaxM 300\nsweep_tol tight\n",
+                  [-76.11460447], "dmrg_tests/runtest:23"),
+}
+
+
+def main():
+    meta = {}
+    for name, (src, conf, energies, cite) in CASES.items():
+        d = os.path.join(HERE, name)
+        os.makedirs(d, exist_ok=True)
+        shutil.copyfile(os.path.join(REF, src), os.path.join(d, "FCIDUMP"))
+        with open(os.path.join(d, "dmrg.conf"), "w") as f:
+            f.write(conf + "orbitals FCIDUMP\n")
+        with open(os.path.join(d, "FCIDUMP"), "rb") as f:
+            sha = hashlib.sha256(f.read()).hexdigest()
+        meta[name] = dict(energies=energies, source=src, cited=cite, sha256=sha, tolerance=1e-6)
+    with open(os.path.join(HERE, "golden.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
