@@ -46,6 +46,8 @@ _SIGS = {
     "bgpu_sigma": (_I, [_P, _I, _DP, _DP]),
     "bgpu_sigma_device": (_I, [_P, _I, _P, _P]),
     "bgpu_hdiag": (_I, [_P, _I, _DP]),
+    "bgpu_sigma_timed": (_I, [_P, _I, _P, _P, _I, _DP]),
+    "bgpu_superblock_launches": (_I, [_P, _I, _IP]),
     "bgpu_davidson": (_I, [_P, _I, _I, _D, _I, _DP, _DP, _IP]),
     "bgpu_density_eig": (_I, [_P, _I, _I, _I, _DP, _DP, _I64]),
     "bgpu_device_alloc": (_I, [_P, _I64, ctypes.POINTER(_P)]),
@@ -180,6 +182,17 @@ class Context:
 
     def sigma_device(self, sb, psi_ptr, out_ptr):
         self._check(self.lib.bgpu_sigma_device(self.h, sb, _P(psi_ptr), _P(out_ptr)))
+
+    def sigma_timed(self, sb, psi_ptr, out_ptr, reps):
+        """Device-timed products: (total ms, stage-1 ms, stage-2 ms) summed over reps."""
+        ms = np.zeros(3)
+        self._check(self.lib.bgpu_sigma_timed(self.h, sb, _P(psi_ptr), _P(out_ptr), reps, _dp(ms)))
+        return ms
+
+    def superblock_launches(self, sb):
+        n = _I()
+        self._check(self.lib.bgpu_superblock_launches(self.h, sb, ctypes.byref(n)))
+        return n.value
 
     def hdiag(self, sb, n):
         out = np.empty(n, dtype=np.float64)

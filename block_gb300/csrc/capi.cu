@@ -280,6 +280,24 @@ int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
   });
 }
 
+int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi, double* sigma, int reps, double* ms) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && psi && sigma && ms && reps > 0, "bad arguments");
+    float t[3] = {0, 0, 0};
+    ctx->eng->sigma_timed(it->second->sb, it->second->plan, psi, sigma, reps, t);
+    for (int i = 0; i < 3; ++i) ms[i] = t[i];
+  });
+}
+
+int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && launches, "bad arguments");
+    *launches = ctx->eng->sigma_launches(it->second->plan);
+  });
+}
+
 int bgpu_hdiag(bgpu_ctx* ctx, int sb, double* diag) {
   return guarded(ctx, [&] {
     auto it = ctx->sbs.find(sb);

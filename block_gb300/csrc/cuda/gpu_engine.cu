@@ -478,6 +478,43 @@ void GpuEngine::sigma(const Superblock& sb, const SigmaPlan& p, const double* ps
   ++sigma_calls;
 }
 
+int GpuEngine::sigma_launches(const SigmaPlan& p) const {
+  return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
+}
+
+void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out, int reps,
+                            float* ms) {
+  dev::Bufs bufs{};
+  bufs.p[0] = arena(*sb.L);
+  bufs.p[1] = arena(*sb.R);
+  bufs.p[2] = const_cast<double*>(psi);
+  bufs.p[3] = out;
+  bufs.p[4] = p.scratch;
+  cudaEvent_t e[4];
+  for (auto& x : e) cuda_check(cudaEventCreate(&x), "event");
+  ms[0] = ms[1] = ms[2] = 0.f;
+  for (int r = 0; r < reps; ++r) {
+    cuda_check(cudaEventRecord(e[0], stream_), "record");
+    cuda_check(dev::launch_gemm(bufs, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "sigma stage 1");
+    cuda_check(cudaEventRecord(e[1], stream_), "record");
+    cuda_check(dev::launch_gemm(bufs, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "sigma stage 2");
+    cuda_check(cudaEventRecord(e[2], stream_), "record");
+    if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
+    cuda_check(cudaEventRecord(e[3], stream_), "record");
+    cuda_check(cudaEventSynchronize(e[3]), "sync");
+    float a, b, c;
+    cudaEventElapsedTime(&a, e[0], e[3]);
+    cudaEventElapsedTime(&b, e[0], e[1]);
+    cudaEventElapsedTime(&c, e[1], e[2]);
+    ms[0] += a;
+    ms[1] += b;
+    ms[2] += c;
+    sigma_flops += p.flops;
+    ++sigma_calls;
+  }
+  for (auto& x : e) cudaEventDestroy(x);
+}
+
 void GpuEngine::hdiag(const Superblock& sb, const SigmaPlan& p, double* d) {
   dev::Bufs bufs{};
   bufs.p[0] = arena(*sb.L);

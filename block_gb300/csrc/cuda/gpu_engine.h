@@ -71,6 +71,10 @@ class GpuEngine : public Engine {
   // device pointers, stream-ordered on stream()
   void sigma(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d);
   void hdiag(const Superblock& sb, const SigmaPlan& plan, double* diag_d);
+  // reps products timed by events on stream(): ms[0] total, ms[1] stage 1, ms[2] stage 2
+  void sigma_timed(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d, int reps,
+                   float* ms);
+  int sigma_launches(const SigmaPlan& plan) const;
   double* arena(const Block& b) const;
   cudaStream_t stream() const { return stream_; }
   double* alloc(int64_t elems);

@@ -104,6 +104,8 @@ int bgpu_superblock_define(bgpu_ctx* ctx, int left, int right, const int* target
 int bgpu_superblock_free(bgpu_ctx* ctx, int sb);
 /* Algorithmic work of one sigma: FP64-equivalent flops and bytes. */
 int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes);
+/* Kernel launches of one sigma product. */
+int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);
 
 /*
  * sigma = H psi on host buffers (copies in and out are part of the call).
@@ -113,6 +115,12 @@ int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes);
 int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma);
 /* Same on device pointers (stream-ordered, asynchronous). */
 int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev);
+/*
+ * `reps` back-to-back sigma products on device buffers timed with CUDA
+ * events on the context's stream; ms[0] = total, ms[1] = first GEMM stage,
+ * ms[2] = second GEMM stage (all summed over the repetitions).
+ */
+int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev, int reps, double* ms);
 /* Diagonal of H (SpinBlock::diagonalH, spinblock.C:855-899). */
 int bgpu_hdiag(bgpu_ctx* ctx, int sb, double* diag);
 /*

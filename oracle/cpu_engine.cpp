@@ -213,6 +213,7 @@ void CpuEngine::sigma(const Superblock& sb, const double* psi, double* out) {
   const int J = sb.target.s2;
   const int nth = threads;
   std::vector<std::vector<double>> part(nth, std::vector<double>(sb.size, 0.0));
+  std::vector<double> fl(nth, 0.0);
 #pragma omp parallel num_threads(nth)
   {
     int tid = 0;
@@ -241,6 +242,7 @@ void CpuEngine::sigma(const Superblock& sb, const double* psi, double* out) {
               std::memcpy(m.data(), psi + S.offset, sizeof(double) * mr * mc);
             } else {
               dgemm(va.trans, false, mr, mc, S.rows, va.scale, va.p, va.ld, psi + S.offset, S.cols, 0.0, m.data(), mc);
+              fl[tid] += 2.0 * mr * mc * S.rows;
             }
             for (int rQ = 0; rQ < nR; ++rQ) {
               const int vs = sec[(size_t)lQ * nR + rQ];
@@ -259,11 +261,14 @@ void CpuEngine::sigma(const Superblock& sb, const double* psi, double* out) {
                 // V += f * m * B(rQ,rQ')^T
                 dgemm(false, !vb.trans, mr, SV.cols, mc, f * vb.scale, m.data(), mc, vb.p, vb.ld, 1.0, V + SV.offset,
                       SV.cols);
+                fl[tid] += 2.0 * mr * SV.cols * mc;
               }
             }
           }
     }
   }
+  last_sigma_flops = 0.0;
+  for (int t = 0; t < nth; ++t) last_sigma_flops += fl[t];
   std::fill(out, out + sb.size, 0.0);
   for (int t = 0; t < nth; ++t)
     for (int64_t i = 0; i < sb.size; ++i) out[i] += part[t][i];

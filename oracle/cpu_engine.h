@@ -43,6 +43,7 @@ class CpuEngine : public Engine {
   void set_wavefunctions(const std::vector<std::vector<double>>& w) { waves_ = w; }
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
+  double last_sigma_flops = 0.0;  // GEMM flops of the last sigma (2mnk per product)
   int threads = 1;
 
  private:

@@ -33,6 +33,7 @@ struct Snapshot {
   std::vector<int> orbsym;
   std::string group;
   double sigma_seconds = 0.0;
+  double sigma_flops = 0.0;
   int threads = 1;
 };
 
@@ -124,6 +125,7 @@ void* oracle_snapshot(const char* conf, int sweep, int pos, int threads) {
       auto t0 = std::chrono::steady_clock::now();
       eng.sigma(sb, snap->psi.data(), snap->sigma.data());
       snap->sigma_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      snap->sigma_flops = eng.last_sigma_flops;
       snap->diag.assign(sb.size, 0.0);
       eng.hdiag(sb, snap->diag.data());
       snap->target[0] = sb.target.n;
@@ -177,7 +179,8 @@ void oracle_snapshot_block(void* h, int which, int* quanta, int* states, int* ke
   std::memcpy(arena, b.arena.data(), b.arena.size() * sizeof(double));
 }
 
-// misc[0..2] target, misc[3] ecore, misc[4] energy <psi|H|psi>, misc[5] oracle sigma seconds, misc[6] threads
+// misc[0..2] target, misc[3] ecore, misc[4] energy <psi|H|psi>, misc[5] oracle sigma seconds,
+// misc[6] threads, misc[7] oracle sigma GEMM flops
 void oracle_snapshot_data(void* h, double* coef, int* ops, double* psi, double* sigma, double* diag, int* orbsym,
                           double* misc) {
   auto* s = static_cast<Snapshot*>(h);
@@ -194,6 +197,7 @@ void oracle_snapshot_data(void* h, double* coef, int* ops, double* psi, double* 
   misc[4] = s->energy;
   misc[5] = s->sigma_seconds;
   misc[6] = s->threads;
+  misc[7] = s->sigma_flops;
 }
 
 const char* oracle_snapshot_group(void* h) { return static_cast<Snapshot*>(h)->group.c_str(); }
@@ -232,7 +236,7 @@ extern "C" {
 // Superblock of `partition` built from seeded warm-up blocks (same
 // construction as bgpu_prepare_superblock) captured as a snapshot whose psi
 // is a seeded random unit vector.
-void* oracle_prepare(const char* conf, int partition, int threads) {
+void* oracle_prepare(const char* conf, int partition, int threads, int reps) {
   auto snap = std::make_unique<Snapshot>();
   try {
     Config c = parse_config(conf);
@@ -264,9 +268,11 @@ void* oracle_prepare(const char* conf, int partition, int threads) {
     }
     for (auto& x : snap->psi) x /= std::sqrt(nrm);
     snap->sigma.assign(sb.size, 0.0);
+    if (reps < 1) reps = 1;
     auto t0 = std::chrono::steady_clock::now();
-    eng.sigma(sb, snap->psi.data(), snap->sigma.data());
-    snap->sigma_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int r = 0; r < reps; ++r) eng.sigma(sb, snap->psi.data(), snap->sigma.data());
+    snap->sigma_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() / reps;
+    snap->sigma_flops = eng.last_sigma_flops;
     snap->diag.assign(sb.size, 0.0);
     eng.hdiag(sb, snap->diag.data());
     snap->target[0] = sb.target.n;
