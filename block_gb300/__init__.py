@@ -48,6 +48,7 @@ _SIGS = {
     "bgpu_hdiag": (_I, [_P, _I, _DP]),
     "bgpu_sigma_timed": (_I, [_P, _I, _P, _P, _I, _DP]),
     "bgpu_superblock_launches": (_I, [_P, _I, _IP]),
+    "bgpu_sigma_noalloc": (_I, [_P, _I, _P, _P]),
     "bgpu_davidson": (_I, [_P, _I, _I, _D, _I, _DP, _DP, _IP]),
     "bgpu_density_eig": (_I, [_P, _I, _I, _I, _DP, _DP, _I64]),
     "bgpu_device_alloc": (_I, [_P, _I64, ctypes.POINTER(_P)]),
@@ -188,6 +189,11 @@ class Context:
         ms = np.zeros(3)
         self._check(self.lib.bgpu_sigma_timed(self.h, sb, _P(psi_ptr), _P(out_ptr), reps, _dp(ms)))
         return ms
+
+    def sigma_noalloc(self, sb, psi_ptr, out_ptr):
+        """sigma on device buffers using only the library's fixed device
+        array for intermediates (no device allocation during the call)."""
+        self._check(self.lib.bgpu_sigma_noalloc(self.h, sb, _P(psi_ptr), _P(out_ptr)))
 
     def superblock_launches(self, sb):
         n = _I()

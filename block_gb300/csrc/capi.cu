@@ -4,6 +4,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 
 #include "../../include/bgpu.h"
@@ -431,3 +432,64 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free sigma (bgpu_sigma_noalloc).  The stage-1 intermediates go
+// to a fixed device array instead of the superblock's scratch buffer.  Host
+// code only ever sees the array's name as a host-side stand-in, never as a
+// device address: its device address is looked up once per device with
+// cudaGetSymbolAddress (with that device current) and passed to the kernels.
+// ---------------------------------------------------------------------------
+namespace {
+static __device__ __align__(256) double g_noalloc_scratch[BGPU_NOALLOC_SCRATCH_DOUBLES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device` (set-up on first use).
+cudaError_t noalloc_scratch(int device, double** out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) return e;
+    if (cur != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+    double* p = nullptr;
+    e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (cur != device) cudaSetDevice(cur);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[device] = p;
+  }
+  *out = g_noalloc_ptr[device];
+  return cudaSuccess;
+}
+}  // namespace
+
+extern "C" int bgpu_sigma_noalloc(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && psi && sigma, "bad arguments");
+    const SigmaPlan& plan = it->second->plan;
+    if (plan.scratch_elems > (int64_t)BGPU_NOALLOC_SCRATCH_DOUBLES)
+      throw std::invalid_argument("bgpu_sigma_noalloc: superblock needs " + std::to_string(plan.scratch_elems) +
+                                  " doubles of intermediates, more than the fixed " +
+                                  std::to_string((long long)BGPU_NOALLOC_SCRATCH_DOUBLES) +
+                                  "; use bgpu_sigma_device");
+    double* scratch = nullptr;
+    cuda_check(noalloc_scratch(ctx->device, &scratch), "noalloc scratch address");
+    const Superblock& s = it->second->sb;
+    dev::Bufs bufs{};
+    bufs.p[0] = ctx->eng->arena(*s.L);
+    bufs.p[1] = ctx->eng->arena(*s.R);
+    bufs.p[2] = const_cast<double*>(psi);
+    bufs.p[3] = sigma;
+    bufs.p[4] = scratch;
+    cudaStream_t st = ctx->eng->stream();
+    cuda_check(dev::launch_gemm(bufs, plan.u1.d, plan.i1.d, plan.t1.d, (int)plan.t1.n, st), "sigma stage 1");
+    cuda_check(dev::launch_gemm(bufs, plan.u2.d, plan.i2.d, plan.t2.d, (int)plan.t2.n, st), "sigma stage 2");
+    if (plan.ecore != 0.0) cuda_check(dev::launch_axpy(plan.ecore, psi, sigma, plan.n, st), "ecore");
+  });
+}

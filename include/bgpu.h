@@ -121,6 +121,26 @@ int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigm
  * ms[2] = second GEMM stage (all summed over the repetitions).
  */
 int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev, int reps, double* ms);
+/*
+ * sigma = H psi on device buffers without allocating any memory.  This entry
+ * point has no counterpart in the reference; it exists for callers that may
+ * not allocate device memory while they run -- for example code recorded
+ * into a CUDA graph, code running under a fixed memory budget, or a host
+ * application whose own allocator owns the GPU -- and therefore cannot let
+ * the library call cudaMalloc on their behalf.  Instead of a per-superblock
+ * scratch buffer, the stage-1 intermediates of the product live in one
+ * fixed array of BGPU_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB) that every
+ * GPU loading the library holds until the process exits.  The superblock
+ * must already be defined (bgpu_superblock_define / _prepare_superblock);
+ * superblocks whose intermediates do not fit are rejected with
+ * BGPU_ERR_INVALID.  The first call on a device looks up the array's
+ * address and should therefore come before any stream capture.  All calls
+ * share the array: calls whose work overlaps on the GPU (other streams,
+ * other contexts on the same device) race and must be serialised by the
+ * caller.  Stream-ordered and asynchronous like bgpu_sigma_device.
+ */
+#define BGPU_NOALLOC_SCRATCH_DOUBLES (4 * 1024 * 1024)
+int bgpu_sigma_noalloc(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev);
 /* Diagonal of H (SpinBlock::diagonalH, spinblock.C:855-899). */
 int bgpu_hdiag(bgpu_ctx* ctx, int sb, double* diag);
 /*
