@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--partition", type=int, default=11)
     ap.add_argument("--cpu-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="open the CUDA profiler range around the device-timed steps only")
     return ap.parse_args()
 
 
@@ -196,7 +198,11 @@ def run_ours(a):
         dist.barrier()
     ctx.synchronize()
     with ClockSampler(local) as clk:
+        if a.profile:
+            ctx.profiler_start()
         ms = ctx.sigma_timed(sb, x, y, a.steps)
+        if a.profile:
+            ctx.profiler_stop()
         # end-to-end through the host-buffer C ABI call (H2D psi, D2H sigma per step)
         t0 = time.perf_counter()
         for _ in range(a.steps):

@@ -56,6 +56,8 @@ _SIGS = {
     "bgpu_copy_to_device": (_I, [_P, _P, _DP, _I64]),
     "bgpu_copy_to_host": (_I, [_P, _DP, _P, _I64]),
     "bgpu_synchronize": (_I, [_P]),
+    "bgpu_profiler_start": (_I, [_P]),
+    "bgpu_profiler_stop": (_I, [_P]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
 }
@@ -235,6 +237,12 @@ class Context:
         out = np.empty(n, dtype=np.float64)
         self._check(self.lib.bgpu_copy_to_host(self.h, _dp(out), _P(src), n))
         return out
+
+    def profiler_start(self):
+        self._check(self.lib.bgpu_profiler_start(self.h))
+
+    def profiler_stop(self):
+        self._check(self.lib.bgpu_profiler_stop(self.h))
 
     def synchronize(self):
         self._check(self.lib.bgpu_synchronize(self.h))

@@ -1,5 +1,7 @@
 // extern "C" boundary of the library (declarations and reference mapping in
 // include/bgpu.h).
+#include <cuda_profiler_api.h>
+
 #include <chrono>
 #include <cstring>
 #include <map>
@@ -376,6 +378,20 @@ int bgpu_copy_to_host(bgpu_ctx* ctx, double* dst, const double* src, int64_t n) 
 }
 int bgpu_synchronize(bgpu_ctx* ctx) {
   return guarded(ctx, [&] { ctx->eng->sync(); });
+}
+
+int bgpu_profiler_start(bgpu_ctx* ctx) {
+  return guarded(ctx, [&] {
+    ctx->eng->sync();
+    cuda_check(cudaProfilerStart(), "cudaProfilerStart");
+  });
+}
+
+int bgpu_profiler_stop(bgpu_ctx* ctx) {
+  return guarded(ctx, [&] {
+    ctx->eng->sync();
+    cuda_check(cudaProfilerStop(), "cudaProfilerStop");
+  });
 }
 
 int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition, int* sbh, int64_t* psi_elems) {

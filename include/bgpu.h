@@ -169,6 +169,11 @@ int bgpu_device_free(bgpu_ctx* ctx, double* ptr);
 int bgpu_copy_to_device(bgpu_ctx* ctx, double* dst, const double* src, int64_t n);
 int bgpu_copy_to_host(bgpu_ctx* ctx, double* dst, const double* src, int64_t n);
 int bgpu_synchronize(bgpu_ctx* ctx);
+/* Start / stop the CUDA profiler's collection range (cudaProfilerStart/Stop),
+ * so that a profiler run with collection off at start sees only the calls in
+ * between. */
+int bgpu_profiler_start(bgpu_ctx* ctx);
+int bgpu_profiler_stop(bgpu_ctx* ctx);
 
 /*
  * Superblock of the bipartition after orbital `partition` (left block

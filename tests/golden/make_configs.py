@@ -26,6 +26,7 @@ CONFS = {
     "syn8": ("synthetic:8:8:16:8:0", "nelec 8\nspin 0\nschedule\n0 200 1e-12 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
     "syn8_d2h": ("synthetic:8:8:16:8:1", "nelec 8\nspin 0\nschedule\n0 200 1e-12 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
     "syn24": ("synthetic:24:24:48:24:0", "nelec 24\nspin 0\nschedule\n0 500 1e-8 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn24_m250": ("synthetic:24:24:48:24:0", "nelec 24\nspin 0\nschedule\n0 250 1e-8 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_d2h": ("synthetic:30:30:60:30:1", "nelec 30\nspin 0\nschedule\n0 1500 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn40": ("synthetic:40:40:80:40:0", "nelec 40\nspin 0\nnroots 3\nweights 0.333333333333 0.333333333333 0.333333333334\nschedule\n0 4000 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
