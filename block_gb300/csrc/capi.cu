@@ -103,7 +103,7 @@ const char* bgpu_last_error_string(const bgpu_ctx* ctx) { return ctx ? ctx->err.
 
 int bgpu_set_precision(bgpu_ctx* ctx, int p) {
   return guarded(ctx, [&] {
-    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_FP16X2, "unknown precision");
+    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6, "unknown precision");
     need(ctx->eng != nullptr, "no device");
     ctx->eng->precision = (Precision)p;
   });

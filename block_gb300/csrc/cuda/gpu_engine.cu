@@ -76,6 +76,12 @@ void GpuEngine::create_block(Block& b) {
 }
 
 void GpuEngine::release_block(Block& b) {
+  auto sl = slices_.find(b.handle);
+  if (sl != slices_.end()) {
+    for (auto* p : sl->second.s)
+      if (p) cudaFreeAsync(p, stream_);
+    slices_.erase(sl);
+  }
   auto it = blocks_.find(b.handle);
   if (it != blocks_.end()) {
     free(it->second.d);
@@ -452,6 +458,12 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
 }
 
 void GpuEngine::free_plan(SigmaPlan& p) {
+  for (int i = 0; i < 3; ++i) {
+    if (p.psi_s[i]) cudaFreeAsync(p.psi_s[i], stream_);
+    if (p.mid_s[i]) cudaFreeAsync(p.mid_s[i], stream_);
+    p.psi_s[i] = p.mid_s[i] = nullptr;
+  }
+  p.ns = 0;
   p.u1.release(stream_);
   p.u2.release(stream_);
   p.i1.release(stream_);
@@ -478,6 +490,66 @@ void GpuEngine::sigma(const Superblock& sb, const SigmaPlan& p, const double* ps
   ++sigma_calls;
 }
 
+const GpuEngine::Slices& GpuEngine::block_slices(const Block& b, int ns) {
+  Slices& sl = slices_[b.handle];
+  if (sl.ns >= ns) return sl;
+  for (auto*& p : sl.s)
+    if (p) {
+      cudaFreeAsync(p, stream_);
+      p = nullptr;
+    }
+  const DevBlock& d = blocks_.at(b.handle);
+  for (int i = 0; i < ns; ++i)
+    cuda_check(cudaMallocAsync((void**)&sl.s[i], std::max<int64_t>(d.n, 1) * sizeof(__nv_bfloat16), stream_),
+               "slices");
+  cuda_check(dev::launch_slices(d.d, d.n, ns, sl.s[0], sl.s[1], ns > 2 ? sl.s[2] : nullptr, stream_), "slice op");
+  sl.ns = ns;
+  return sl;
+}
+
+// Split-precision sigma: the FP64 plan's work lists, executed by the bf16
+// tensor-core kernel; operator arenas are sliced once per block, psi per call,
+// stage-1 intermediates are written directly as slices.
+void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const double* psi, double* out) {
+  const Slices& Ls = block_slices(*sb.L, ns);
+  const Slices& Rs = block_slices(*sb.R, ns);
+  if (p.ns < ns) {
+    for (int i = 0; i < 3; ++i) {
+      if (p.psi_s[i]) cudaFreeAsync(p.psi_s[i], stream_);
+      if (p.mid_s[i]) cudaFreeAsync(p.mid_s[i], stream_);
+      p.psi_s[i] = p.mid_s[i] = nullptr;
+    }
+    for (int i = 0; i < ns; ++i) {
+      cuda_check(cudaMallocAsync((void**)&p.psi_s[i], std::max<int64_t>(p.n, 1) * 2, stream_), "psi slices");
+      cuda_check(cudaMallocAsync((void**)&p.mid_s[i], std::max<int64_t>(p.scratch_elems, 1) * 2, stream_),
+                 "mid slices");
+    }
+    p.ns = ns;
+  }
+  cuda_check(dev::launch_slices(psi, p.n, ns, p.psi_s[0], p.psi_s[1], ns > 2 ? p.psi_s[2] : nullptr, stream_),
+             "slice psi");
+  dev::SplitBufs b{};
+  for (int i = 0; i < ns; ++i) {
+    b.s[0][i] = Ls.s[i];
+    b.s[1][i] = Rs.s[i];
+    b.s[2][i] = p.psi_s[i];
+    b.s[4][i] = p.mid_s[i];
+    b.out16[4][i] = p.mid_s[i];
+  }
+  b.out64[3] = out;
+  cuda_check(dev::launch_gemm_split(ns, b, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "split stage 1");
+  cuda_check(dev::launch_gemm_split(ns, b, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "split stage 2");
+  if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
+  sigma_flops += p.flops;
+  ++sigma_calls;
+}
+
+void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
+  const int ns = precision_slices(precision);
+  if (ns) sigma_split(sb, p, ns, psi, out);
+  else sigma(sb, p, psi, out);
+}
+
 int GpuEngine::sigma_launches(const SigmaPlan& p) const {
   return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
 }
@@ -493,6 +565,23 @@ void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const doub
   cudaEvent_t e[4];
   for (auto& x : e) cuda_check(cudaEventCreate(&x), "event");
   ms[0] = ms[1] = ms[2] = 0.f;
+  const int ns = precision_slices(precision);
+  if (ns) {
+    SigmaPlan& pm = const_cast<SigmaPlan&>(p);
+    sigma_split(sb, pm, ns, psi, out);  // slices operators and buffers outside the timed region
+    sync();
+    for (int r = 0; r < reps; ++r) {
+      cuda_check(cudaEventRecord(e[0], stream_), "record");
+      sigma_split(sb, pm, ns, psi, out);
+      cuda_check(cudaEventRecord(e[3], stream_), "record");
+      cuda_check(cudaEventSynchronize(e[3]), "sync");
+      float a;
+      cudaEventElapsedTime(&a, e[0], e[3]);
+      ms[0] += a;
+    }
+    for (auto& x : e) cudaEventDestroy(x);
+    return;
+  }
   for (int r = 0; r < reps; ++r) {
     cuda_check(cudaEventRecord(e[0], stream_), "record");
     cuda_check(dev::launch_gemm(bufs, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "sigma stage 1");
@@ -591,9 +680,17 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     ++iter;
     for (; ks < k; ++ks) {
       auto t0 = std::chrono::steady_clock::now();
-      sigma(sb, plan_, row(B, ks), row(S, ks));
+      sigma_any(sb, plan_, row(B, ks), row(S, ks));
       sync();
-      sigma_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      sigma_seconds += dt;
+      if (precision_slices(precision)) {
+        split_seconds += dt;
+        ++split_calls;
+      } else {
+        fp64_seconds += dt;
+        ++fp64_calls;
+      }
     }
     // subspace matrix h_ij = b_i . sigma_j
     std::vector<double> h((size_t)k * k);
@@ -665,6 +762,19 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     if (iter >= p.max_iter) break;
   }
   energies.assign(lam.begin(), lam.begin() + nroots);
+  if (precision_slices(precision)) {
+    // defect correction: energies of the split-precision Ritz vectors from one
+    // FP64 product each (Rayleigh quotient, second order in the vector error)
+    for (int rr = 0; rr < nroots; ++rr) {
+      auto t0 = std::chrono::steady_clock::now();
+      sigma(sb, plan_, row(B, rr), r);
+      energies[rr] = dot(row(B, rr), r);
+      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      sigma_seconds += dt;
+      fp64_seconds += dt;
+      ++fp64_calls;
+    }
+  }
   if (waves_) free(waves_);
   waves_ = alloc((int64_t)nroots * n);
   cuda_check(cudaMemcpyAsync(waves_, B, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "waves");

@@ -12,11 +12,13 @@
 #include <vector>
 
 #include "../host/sweep.h"
+#include "k_split.cuh"
 #include "kernels.cuh"
 
 namespace bgpu {
 
-enum class Precision : int { FP64 = 0, BF16X3 = 1, FP16X2 = 2 };
+enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2 };
+inline int precision_slices(Precision p) { return p == Precision::BF16X3 ? 2 : p == Precision::BF16X6 ? 3 : 0; }
 
 struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
@@ -46,6 +48,10 @@ struct SigmaPlan {
   int64_t n = 0;
   double ecore = 0.0;
   int nstage1_units = 0, nstage2_units = 0, nitems = 0;
+  // split-precision buffers (allocated on first split-precision product)
+  int ns = 0;
+  __nv_bfloat16* psi_s[3] = {nullptr, nullptr, nullptr};
+  __nv_bfloat16* mid_s[3] = {nullptr, nullptr, nullptr};
 };
 
 class GpuEngine : public Engine {
@@ -70,6 +76,10 @@ class GpuEngine : public Engine {
   void free_plan(SigmaPlan& plan);
   // device pointers, stream-ordered on stream()
   void sigma(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d);
+  // split-precision product with `ns` bf16 slices (2 or 3)
+  void sigma_split(const Superblock& sb, SigmaPlan& plan, int ns, const double* psi_d, double* out_d);
+  // product at the engine's current precision
+  void sigma_any(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d);
   void hdiag(const Superblock& sb, const SigmaPlan& plan, double* diag_d);
   // reps products timed by events on stream(): ms[0] total, ms[1] stage 1, ms[2] stage 2
   void sigma_timed(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d, int reps,
@@ -87,8 +97,16 @@ class GpuEngine : public Engine {
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
   double sigma_flops = 0.0;
+  long split_calls = 0, fp64_calls = 0;
+  double split_seconds = 0.0, fp64_seconds = 0.0;
 
  private:
+  struct Slices {
+    int ns = 0;
+    __nv_bfloat16* s[3] = {nullptr, nullptr, nullptr};
+  };
+  const Slices& block_slices(const Block& b, int ns);
+  std::map<int, Slices> slices_;
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   struct DevBlock {

@@ -48,10 +48,15 @@ extern "C" {
 #define BGPU_OP_CRE_CRE_DESCOMP 6
 #define BGPU_OP_OVERLAP 7
 
-/* arithmetic of the sigma product */
+/* arithmetic of the sigma product: FP64, or bf16 slices on the tensor cores
+ * with FP32 accumulation -- 2 slices / 3 products per logical product
+ * (BF16X3) or 3 slices / 6 products (BF16X6).  With a split precision,
+ * bgpu_davidson and bgpu_run_dmrg iterate with split-precision sigma and
+ * refine every converged root's energy with one FP64 sigma (Rayleigh
+ * quotient against the FP64 Hamiltonian). */
 #define BGPU_PREC_FP64 0
 #define BGPU_PREC_BF16X3 1
-#define BGPU_PREC_FP16X2 2
+#define BGPU_PREC_BF16X6 2
 
 typedef struct bgpu_ctx bgpu_ctx;
 
