@@ -6,7 +6,10 @@ the middle bond of the synthetic 24-orbital / 24-electron Cholesky
 Hamiltonian (48 vectors, seed 24, S=0, C1), with left and right blocks
 renormalised to M=500 multiplets from seeded warm-up rotations.  The metric
 is FP64-equivalent sigma TFLOP/s (the algorithmic flop count of every sector
-GEMM, counted by the library's schedule compiler).
+GEMM, counted by the library's schedule compiler).  The headline arithmetic
+is the split-precision path (bf16 slices on the tensor cores, "bf16x3");
+the line also carries the plain FP64 path's sigma time and a Davidson solve
+of the same superblock in both arithmetics (time and energy difference).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
                   [--precision fp64|bf16x3] [--conf PATH --partition P]
@@ -36,7 +39,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "bf16x6"])
+    ap.add_argument("--no-davidson", action="store_true", help="skip the FP64-vs-split Davidson comparison")
     ap.add_argument("--conf", default=DEFAULT_CONF)
     ap.add_argument("--partition", type=int, default=11)
     ap.add_argument("--cpu-reps", type=int, default=3)
@@ -141,10 +145,21 @@ def cpu_baseline(conf, partition, reps):
     return snap
 
 
+def conf_M(conf):
+    with open(conf) as f:
+        lines = [l.split() for l in f if l.strip()]
+    for i, t in enumerate(lines):
+        if t[0].lower() == "schedule" and i + 1 < len(lines):
+            return int(lines[i + 1][1])
+    return None
+
+
 def config_dict(conf, partition, n, prec, arena_mb):
+    M = conf_M(conf)
     return {"workload": "sigma = H psi at the middle bond (L=[0..%d]) of the synthetic 24-orbital/24-electron "
-                        "Cholesky Hamiltonian (48 vectors, seed 24, S=0, C1), blocks renormalised to M=500" % partition,
-            "conf": os.path.relpath(conf, ROOT), "norb": 24, "nelec": 24, "M": 500, "partition": partition,
+                        "Cholesky Hamiltonian (48 vectors, seed 24, S=0, C1), blocks renormalised to M=%s"
+                        % (partition, M),
+            "conf": os.path.relpath(conf, ROOT), "norb": 24, "nelec": 24, "M": M, "partition": partition,
             "psi_elems": n, "precision": prec,
             "l2": "inputs larger than L2: operator arenas %.0f MB per step" % arena_mb}
 
@@ -221,11 +236,12 @@ def run_ours(a):
         t_e2e_step = t_e2e / a.steps
     value = world * flops / t_step / 1e12
     e2e = world * flops / t_e2e_step / 1e12
-    kern_ms = (ms[1] + ms[2]) / a.steps
+    split = a.precision != "fp64"
+    kern_ms = (ms[1] if split else ms[1] + ms[2]) / a.steps
     achieved = flops / (kern_ms * 1e-3) / 1e12
     peaks = measured_peaks()
-    fp64 = fp64_peak_tflops() if a.precision == "fp64" else None
-    if a.precision == "fp64":
+    fp64 = fp64_peak_tflops()
+    if not split:
         roof = {"bound": "tensor", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
                 "frac": (achieved / fp64) if fp64 else None, "traffic": None,
                 "kernel": "gemm_fp64_kernel (sigma stages 1+2)",
@@ -234,24 +250,56 @@ def run_ours(a):
                 "algorithmic_bytes_per_step": nbytes}
     else:
         pk = peaks.get("bf16_tflops", 1900.0)
+        prods = 3 if a.precision == "bf16x3" else 6
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
-                "traffic": None, "peak_source": "bf16_tflops of measured" if peaks else "fallback"}
+                "traffic": None, "kernel": "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)",
+                "peak_source": ("bf16_tflops of measured" if peaks else "fallback 1900"),
+                "products_per_logical_product": prods,
+                "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
+                "fp64_peak_tflops_in_run": fp64, "algorithmic_bytes_per_step": nbytes}
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else a.precision, "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else "bf16 slices, f32 accumulate",
+            "data": "synthetic",
             "config": config_dict(a.conf, a.partition, n, a.precision, nbytes / 1e6),
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
             "gpu_launches": launches * a.steps, "clocks": clocks, "roofline": roof,
-            "sigma_flops_per_step": flops, "stage_ms_per_step": [ms[1] / a.steps, ms[2] / a.steps]}
+            "sigma_flops_per_step": flops, "kernel_ms_per_step": [ms[1] / a.steps, ms[2] / a.steps]}
+    if split:
+        # plain FP64 path on the same superblock and input
+        ctx.set_precision("fp64")
+        ref64 = ctx.sigma(sb, psi)
+        ms64 = ctx.sigma_timed(sb, x, y, 2)
+        ctx.set_precision(a.precision)
+        sp = ctx.sigma(sb, psi)
+        line["fp64_path"] = {"ms_per_step": ms64[0] / 2, "tflops": flops / (ms64[0] / 2e3) / 1e12,
+                             "speedup_of_split": (ms64[0] / 2) / (ms[0] / a.steps),
+                             "split_sigma_rel_err": float(np.linalg.norm(sp - ref64) / np.linalg.norm(ref64))}
+    if not a.no_davidson:
+        # Davidson solve of the superblock (tol 1e-8 on the squared residual, as
+        # in the schedule): plain FP64 vs split precision with FP64 refinement
+        out = {}
+        for prec in (["fp64", a.precision] if split else ["fp64"]):
+            ctx.set_precision(prec)
+            t0 = time.perf_counter()
+            e, _, it = ctx.davidson(sb, n, nroots=1, tol=1e-8)
+            out[prec] = {"seconds": time.perf_counter() - t0, "iterations": it, "energy": float(e[0])}
+        ctx.set_precision(a.precision)
+        if split:
+            out["dE_split_minus_fp64"] = out[a.precision]["energy"] - out["fp64"]["energy"]
+            out["speedup"] = out["fp64"]["seconds"] / out[a.precision]["seconds"]
+        line["davidson"] = out
     if rank == 0 and not a.no_cpu_baseline:
         threads = os.cpu_count() or 1
         snap = cpu_baseline(a.conf, a.partition, a.cpu_reps)
+        ctx.set_precision("fp64")
         err = float(np.linalg.norm(ctx.sigma(sb, snap["psi"]) - snap["sigma"]) / np.linalg.norm(snap["sigma"]))
+        ctx.set_precision(a.precision)
         line["cpu_baseline"] = {"value": flops / snap["sigma_seconds"] / 1e12, "unit": "TFLOP/s", "cores": threads,
                                 "kind": "port",
                                 "sample": "%d sigma products of the same superblock on the CPU oracle (OpenMP over "
                                           "operator pairs, per-thread sigma copies)" % a.cpu_reps}
-        line["sigma_rel_err_vs_oracle"] = err
+        line["fp64_sigma_rel_err_vs_oracle"] = err
     ctx.device_free(x)
     ctx.device_free(y)
     ctx.close()

@@ -269,7 +269,7 @@ int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
     auto& r = *it->second;
     const int64_t n = r.sb.size;
     cuda_check(cudaMemcpyAsync(r.psi, psi, n * sizeof(double), cudaMemcpyHostToDevice, ctx->eng->stream()), "h2d");
-    ctx->eng->sigma(r.sb, r.plan, r.psi, r.sig);
+    ctx->eng->sigma_any(r.sb, r.plan, r.psi, r.sig);
     cuda_check(cudaMemcpyAsync(sigma, r.sig, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->eng->stream()), "d2h");
     ctx->eng->sync();
   });
@@ -279,7 +279,7 @@ int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
   return guarded(ctx, [&] {
     auto it = ctx->sbs.find(sb);
     need(it != ctx->sbs.end() && psi && sigma, "bad arguments");
-    ctx->eng->sigma(it->second->sb, it->second->plan, psi, sigma);
+    ctx->eng->sigma_any(it->second->sb, it->second->plan, psi, sigma);
   });
 }
 

@@ -460,10 +460,15 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
 void GpuEngine::free_plan(SigmaPlan& p) {
   for (int i = 0; i < 3; ++i) {
     if (p.psi_s[i]) cudaFreeAsync(p.psi_s[i], stream_);
-    if (p.mid_s[i]) cudaFreeAsync(p.mid_s[i], stream_);
-    p.psi_s[i] = p.mid_s[i] = nullptr;
+    p.psi_s[i] = nullptr;
   }
   p.ns = 0;
+  p.fi.release(stream_);
+  p.ft.release(stream_);
+  p.ftile.release(stream_);
+  if (p.partials) cudaFreeAsync(p.partials, stream_);
+  p.partials = nullptr;
+  p.fused = false;
   p.u1.release(stream_);
   p.u2.release(stream_);
   p.i1.release(stream_);
@@ -507,38 +512,156 @@ const GpuEngine::Slices& GpuEngine::block_slices(const Block& b, int ns) {
   return sl;
 }
 
-// Split-precision sigma: the FP64 plan's work lists, executed by the bf16
-// tensor-core kernel; operator arenas are sliced once per block, psi per call,
-// stage-1 intermediates are written directly as slices.
-void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const double* psi, double* out) {
+// Work lists of the fused split-precision kernel: the same couplings as
+// plan_sigma, grouped by output sector; every 64 x 64 tile of a sector gets
+// its coupling list cut into chunks of similar cost (one thread block each)
+// and a fixed-order reduction of the chunks' partial tiles.
+void GpuEngine::plan_fused(const Superblock& sb, SigmaPlan& plan) {
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const int nL = L.si.size(), nR = R.si.size();
+  std::vector<int> sec((size_t)nL * nR, -1);
+  for (int s = 0; s < (int)sb.sectors.size(); ++s) sec[(size_t)sb.sectors[s].lq * nR + sb.sectors[s].rq] = s;
+  const int J = sb.target.s2;
+  std::vector<std::vector<dev::FusedItem>> per(sb.sectors.size());
+  for (const PairTerm& t : sb.terms) {
+    const int kL = rank2(t.l), kR = rank2(t.r);
+    const bool fR = fermion(t.r);
+    for (int lQ = 0; lQ < nL; ++lQ)
+      for (int rQp = 0; rQp < nR; ++rQp)
+        for (int lQp = 0; lQp < nL; ++lQp) {
+          const int cs = sec[(size_t)lQp * nR + rQp];
+          if (cs < 0) continue;
+          HostView va = hview(L, t.l, lQ, lQp);
+          if (!va.ok) continue;
+          const auto& C = sb.sectors[cs];
+          for (int rQ = 0; rQ < nR; ++rQ) {
+            const int vs = sec[(size_t)lQ * nR + rQ];
+            if (vs < 0) continue;
+            HostView vb = hview(R, t.r, rQ, rQp);
+            if (!vb.ok) continue;
+            double f = t.coef * ninej(L.si.quanta[lQp].s2, R.si.quanta[rQp].s2, J, kL, kR, 0, L.si.quanta[lQ].s2,
+                                      R.si.quanta[rQ].s2, J);
+            if (fR && is_fermion(L.si.quanta[lQp])) f = -f;
+            if (f == 0.0) continue;
+            dev::FusedItem it{};
+            it.n1 = C.cols;
+            it.k1 = C.rows;
+            it.c_off = C.offset;
+            it.ldc = C.cols;
+            if (va.identity && vb.identity) throw std::runtime_error("identity x identity pair term");
+            if (va.identity) {
+              it.kind = dev::kFusedLIdent;
+              it.a_off = C.offset;  // psi(lQ, rQ') with lQ' = lQ
+              it.lda = C.cols;
+              it.b_off = vb.off;
+              it.ldb = vb.ld;
+              it.tb = vb.trans;
+              it.alpha = (float)(f * vb.scale);
+            } else if (vb.identity) {
+              it.kind = dev::kFusedRIdent;
+              it.a_off = va.off;
+              it.lda = va.ld;
+              it.ta = va.trans;
+              it.alpha = (float)(f * va.scale);
+            } else {
+              it.kind = dev::kFusedFull;
+              it.a_off = va.off;
+              it.lda = va.ld;
+              it.ta = va.trans;
+              it.b_off = vb.off;
+              it.ldb = vb.ld;
+              it.tb = vb.trans;
+              it.alpha = (float)(f * va.scale * vb.scale);
+            }
+            per[vs].push_back(it);
+          }
+        }
+  }
+  auto cost = [](const dev::FusedItem& it) {
+    const double n1 = ((it.n1 + 15) / 16) * 16.0, k1 = ((it.k1 + 15) / 16) * 16.0;
+    double c = 2048.0;
+    if (it.kind != dev::kFusedLIdent) c += k1 * (it.kind == dev::kFusedRIdent ? 64.0 : n1);
+    if (it.kind != dev::kFusedRIdent) c += n1 * 64.0;
+    return c;
+  };
+  double total = 0.0;
+  std::vector<double> sec_cost(sb.sectors.size(), 0.0);
+  for (size_t s = 0; s < per.size(); ++s) {
+    for (auto& it : per[s]) sec_cost[s] += cost(it);
+    const auto& S = sb.sectors[s];
+    total += sec_cost[s] * ((S.rows + 63) / 64) * ((S.cols + 63) / 64);
+  }
+  const double chunk = std::max(total / (152.0 * 12.0), 64.0 * 1024.0);
+  std::vector<dev::FusedItem> items;
+  std::vector<dev::FusedTask> tasks;
+  std::vector<dev::FusedTile> tiles;
+  for (size_t s = 0; s < per.size(); ++s) {
+    const auto& S = sb.sectors[s];
+    const int ib = (int)items.size();
+    for (auto& it : per[s]) items.push_back(it);
+    const int ie = (int)items.size();
+    for (int tm = 0; tm < (S.rows + 63) / 64; ++tm)
+      for (int tn = 0; tn < (S.cols + 63) / 64; ++tn) {
+        dev::FusedTile tl{};
+        tl.s_off = S.offset;
+        tl.lds = S.cols;
+        tl.m = S.rows;
+        tl.n = S.cols;
+        tl.tm = tm;
+        tl.tn = tn;
+        tl.pbeg = (int)tasks.size();
+        int a = ib;
+        while (a < ie) {
+          double acc = 0.0;
+          int b = a;
+          while (b < ie && (acc < chunk || b == a)) acc += cost(items[b++]);
+          tasks.push_back({S.rows, S.cols, tm, tn, a, b});
+          a = b;
+        }
+        tl.pend = (int)tasks.size();
+        tiles.push_back(tl);
+      }
+  }
+  plan.fi.upload(items, stream_);
+  plan.ft.upload(tasks, stream_);
+  plan.ftile.upload(tiles, stream_);
+  cuda_check(cudaMallocAsync((void**)&plan.partials, std::max<size_t>(tasks.size(), 1) * 4096 * sizeof(float), stream_),
+             "partials");
+  plan.fused = true;
+  sync();
+}
+
+// Split-precision sigma with the fused two-stage kernel: operator arenas
+// are sliced once per block, psi per call.
+void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const double* psi, double* out,
+                            cudaEvent_t* marks) {
+  if (!p.fused) plan_fused(sb, p);
   const Slices& Ls = block_slices(*sb.L, ns);
   const Slices& Rs = block_slices(*sb.R, ns);
   if (p.ns < ns) {
     for (int i = 0; i < 3; ++i) {
       if (p.psi_s[i]) cudaFreeAsync(p.psi_s[i], stream_);
-      if (p.mid_s[i]) cudaFreeAsync(p.mid_s[i], stream_);
-      p.psi_s[i] = p.mid_s[i] = nullptr;
+      p.psi_s[i] = nullptr;
     }
-    for (int i = 0; i < ns; ++i) {
+    for (int i = 0; i < ns; ++i)
       cuda_check(cudaMallocAsync((void**)&p.psi_s[i], std::max<int64_t>(p.n, 1) * 2, stream_), "psi slices");
-      cuda_check(cudaMallocAsync((void**)&p.mid_s[i], std::max<int64_t>(p.scratch_elems, 1) * 2, stream_),
-                 "mid slices");
-    }
     p.ns = ns;
   }
   cuda_check(dev::launch_slices(psi, p.n, ns, p.psi_s[0], p.psi_s[1], ns > 2 ? p.psi_s[2] : nullptr, stream_),
              "slice psi");
-  dev::SplitBufs b{};
-  for (int i = 0; i < ns; ++i) {
-    b.s[0][i] = Ls.s[i];
-    b.s[1][i] = Rs.s[i];
-    b.s[2][i] = p.psi_s[i];
-    b.s[4][i] = p.mid_s[i];
-    b.out16[4][i] = p.mid_s[i];
+  dev::FusedBufs fb{};
+  for (int i = 0; i < 3; ++i) {
+    fb.L[i] = Ls.s[i];
+    fb.R[i] = Rs.s[i];
+    fb.psi[i] = p.psi_s[i];
   }
-  b.out64[3] = out;
-  cuda_check(dev::launch_gemm_split(ns, b, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "split stage 1");
-  cuda_check(dev::launch_gemm_split(ns, b, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "split stage 2");
+  fb.psi64 = psi;
+  fb.partials = p.partials;
+  if (marks) cuda_check(cudaEventRecord(marks[0], stream_), "record");
+  cuda_check(dev::launch_fused_sigma(ns, fb, p.fi.d, p.ft.d, (int)p.ft.n, stream_), "fused sigma");
+  if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");
+  cuda_check(dev::launch_fused_reduce(fb, p.ftile.d, (int)p.ftile.n, out, stream_), "fused reduce");
   if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
   sigma_flops += p.flops;
   ++sigma_calls;
@@ -551,6 +674,7 @@ void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi,
 }
 
 int GpuEngine::sigma_launches(const SigmaPlan& p) const {
+  if (precision_slices(precision)) return 3 + (p.ecore != 0.0 ? 1 : 0);  // slice psi, fused, reduce (+ecore)
   return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
 }
 
@@ -572,12 +696,15 @@ void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const doub
     sync();
     for (int r = 0; r < reps; ++r) {
       cuda_check(cudaEventRecord(e[0], stream_), "record");
-      sigma_split(sb, pm, ns, psi, out);
+      sigma_split(sb, pm, ns, psi, out, e + 1);
       cuda_check(cudaEventRecord(e[3], stream_), "record");
       cuda_check(cudaEventSynchronize(e[3]), "sync");
-      float a;
+      float a, b;
       cudaEventElapsedTime(&a, e[0], e[3]);
+      cudaEventElapsedTime(&b, e[1], e[2]);
       ms[0] += a;
+      ms[1] += b;  // fused two-stage kernel alone
+      ms[2] += a - b;
     }
     for (auto& x : e) cudaEventDestroy(x);
     return;

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../host/sweep.h"
+#include "k_fused.cuh"
 #include "k_split.cuh"
 #include "kernels.cuh"
 
@@ -48,10 +49,14 @@ struct SigmaPlan {
   int64_t n = 0;
   double ecore = 0.0;
   int nstage1_units = 0, nstage2_units = 0, nitems = 0;
-  // split-precision buffers (allocated on first split-precision product)
+  // split-precision fused work lists and buffers (built on first use)
+  bool fused = false;
+  DevArray<dev::FusedItem> fi;
+  DevArray<dev::FusedTask> ft;
+  DevArray<dev::FusedTile> ftile;
+  float* partials = nullptr;
   int ns = 0;
   __nv_bfloat16* psi_s[3] = {nullptr, nullptr, nullptr};
-  __nv_bfloat16* mid_s[3] = {nullptr, nullptr, nullptr};
 };
 
 class GpuEngine : public Engine {
@@ -77,7 +82,9 @@ class GpuEngine : public Engine {
   // device pointers, stream-ordered on stream()
   void sigma(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d);
   // split-precision product with `ns` bf16 slices (2 or 3)
-  void sigma_split(const Superblock& sb, SigmaPlan& plan, int ns, const double* psi_d, double* out_d);
+  void sigma_split(const Superblock& sb, SigmaPlan& plan, int ns, const double* psi_d, double* out_d,
+                   cudaEvent_t* marks = nullptr);
+  void plan_fused(const Superblock& sb, SigmaPlan& plan);
   // product at the engine's current precision
   void sigma_any(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d);
   void hdiag(const Superblock& sb, const SigmaPlan& plan, double* diag_d);

@@ -113,7 +113,8 @@ int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes);
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);
 
 /*
- * sigma = H psi on host buffers (copies in and out are part of the call).
+ * sigma = H psi on host buffers (copies in and out are part of the call), in
+ * the context's precision (bgpu_set_precision).
  * Replaces SpinBlock::multiplyH (spinblock.C:722-789) as called by the
  * Davidson functor (davidson.C:19-22).
  */
@@ -122,8 +123,10 @@ int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma);
 int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev);
 /*
  * `reps` back-to-back sigma products on device buffers timed with CUDA
- * events on the context's stream; ms[0] = total, ms[1] = first GEMM stage,
- * ms[2] = second GEMM stage (all summed over the repetitions).
+ * events on the context's stream; ms[0] = total.  FP64: ms[1] = first GEMM
+ * stage, ms[2] = second stage.  Split precision: ms[1] = the fused two-stage
+ * tensor-core kernel, ms[2] = the rest (psi slicing, partial-tile
+ * reduction).  All summed over the repetitions.
  */
 int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev, int reps, double* ms);
 /*

@@ -17,18 +17,21 @@ int main(int argc, char** argv) {
     return 2;
   }
   int threads = 0, verbose = 0;
-  std::string reorder_override;
+  std::string reorder_override, write_dump;
   for (int i = 2; i < argc; ++i) {
     if (!std::strcmp(argv[i], "--threads") && i + 1 < argc) threads = std::atoi(argv[++i]);
     else if (!std::strcmp(argv[i], "--verbose") && i + 1 < argc) verbose = std::atoi(argv[++i]);
     else if (!std::strcmp(argv[i], "--noreorder")) reorder_override = "noreorder";
+    else if (!std::strcmp(argv[i], "--write-fcidump") && i + 1 < argc) write_dump = argv[++i];
   }
   try {
     Config c = parse_config(argv[1]);
     if (!reorder_override.empty()) c.reorder = reorder_override;
-    Integrals I0 = read_fcidump(c.orbitals);
-    if (c.nelec < 0) c.nelec = I0.nelec;
-    Integrals I = reorder(I0, orbital_order(I0, c.reorder));
+    Integrals I = load_integrals(c);
+    if (!write_dump.empty()) {  // integrals in the orbital order used by the sweep
+      write_fcidump(I, write_dump);
+      return 0;
+    }
     oracle::CpuEngine eng(threads);
     DriverOptions opt;
     opt.verbose = verbose;
