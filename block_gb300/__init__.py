@@ -16,7 +16,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libblockgb300.so")
 
 OP = dict(HAM=0, CRE=1, CRE_DES=2, CRE_CRE=3, CRE_DESCOMP=4, DES_DESCOMP=5, CRE_CRE_DESCOMP=6, OVERLAP=7)
-PREC = dict(fp64=0, bf16x3=1, bf16x6=2)
+PREC = dict(fp64=0, bf16x3=1, bf16x6=2, bf16x3tc=3)
 
 _lib = None
 
@@ -58,6 +58,7 @@ _SIGS = {
     "bgpu_synchronize": (_I, [_P]),
     "bgpu_profiler_start": (_I, [_P]),
     "bgpu_profiler_stop": (_I, [_P]),
+    "bgpu_tc_tile": (_I, [_P, _P, _P, _P, _I, _I, _I]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
 }
@@ -91,6 +92,18 @@ def _ip(a):
 
 def _dp(a):
     return a.ctypes.data_as(_DP)
+
+
+def pack_kmajor(x):
+    """Rows x k matrix (rows % 8 == 0, k % 16 == 0) as K-chunks of 64 columns,
+    each in the K-major core-matrix order of the tensor-core kernels."""
+    r, k = x.shape
+    out = np.zeros(r * k, dtype=x.dtype)
+    for c in range(0, k, 64):
+        w = min(64, k - c)
+        blk = x[:, c:c + w].reshape(r // 8, 8, w // 8, 8).transpose(2, 0, 1, 3)  # [k/8][r/8][8][8]
+        out[r * c:r * c + r * w] = blk.reshape(-1)
+    return out
 
 
 class Context:
@@ -244,15 +257,32 @@ class Context:
     def profiler_stop(self):
         self._check(self.lib.bgpu_profiler_stop(self.h))
 
+    def tc_tile(self, a_bits, b_bits, packed=False):
+        """d = a * b^T on one tcgen05 tile; a (128 x k) and b (n x k) are
+        uint16 arrays of bf16 bit patterns, d is float32 (128 x n).  With
+        packed=True the operands are staged through the K-chunk core-matrix
+        packing and bulk copies."""
+        a = np.ascontiguousarray(a_bits, dtype=np.uint16)
+        b = np.ascontiguousarray(b_bits, dtype=np.uint16)
+        n, k = b.shape
+        if a.shape != (128, k):
+            raise ValueError("a must be 128 x k")
+        if packed:
+            a, b = pack_kmajor(a), pack_kmajor(b)
+        d = np.zeros((128, n), dtype=np.float32)
+        self._check(self.lib.bgpu_tc_tile(self.h, a.ctypes.data, b.ctypes.data, d.ctypes.data, n, k, int(packed)))
+        return d
+
     def synchronize(self):
         self._check(self.lib.bgpu_synchronize(self.h))
 
     # ---- full sweep (block.spin_adapted dmrg.conf)
     def run_dmrg(self, conf_path, verbose=0, max_roots=32):
         e = np.zeros(max_roots, dtype=np.float64)
-        st = np.zeros(8, dtype=np.float64)
+        st = np.zeros(12, dtype=np.float64)
         self._check(self.lib.bgpu_run_dmrg(self.h, conf_path.encode(), verbose, _dp(e), max_roots, _dp(st)))
         nroots = int(st[7])
         stats = dict(sweeps=int(st[0]), sigma_calls=int(st[1]), sigma_seconds=st[2], sigma_flops=st[3],
-                     seconds=st[4], discarded=st[5], last_sweep_energy=st[6])
+                     seconds=st[4], discarded=st[5], last_sweep_energy=st[6], build_seconds=st[8],
+                     solve_seconds=st[9], density_seconds=st[10], renorm_seconds=st[11])
         return e[:nroots].copy(), stats

@@ -55,7 +55,8 @@ def build(verbose=False, jobs=None):
             if l.strip():
                 print(l, file=sys.stderr)
     tmp = LIB + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs])
+    libdir = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcusolver", "-Xlinker", "-rpath", "-Xlinker", libdir])
     os.replace(tmp, LIB)
     return LIB
 

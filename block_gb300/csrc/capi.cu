@@ -11,6 +11,7 @@
 
 #include "../../include/bgpu.h"
 #include "cuda/gpu_engine.h"
+#include "cuda/k_tc.cuh"
 #include "host/sweep.h"
 
 using namespace bgpu;
@@ -103,7 +104,8 @@ const char* bgpu_last_error_string(const bgpu_ctx* ctx) { return ctx ? ctx->err.
 
 int bgpu_set_precision(bgpu_ctx* ctx, int p) {
   return guarded(ctx, [&] {
-    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6, "unknown precision");
+    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6 || p == BGPU_PREC_BF16X3_TC,
+         "unknown precision");
     need(ctx->eng != nullptr, "no device");
     ctx->eng->precision = (Precision)p;
   });
@@ -394,6 +396,34 @@ int bgpu_profiler_stop(bgpu_ctx* ctx) {
   });
 }
 
+int bgpu_tc_tile(bgpu_ctx* ctx, const uint16_t* a, const uint16_t* b, float* d, int n, int k, int packed) {
+  return guarded(ctx, [&] {
+    if (n < 16 || n > 256 || n % 16 || k < 16 || k > (packed ? 256 : 64) || k % 16)
+      throw std::runtime_error("bgpu_tc_tile: need 16 <= n <= 256 and 16 <= k <= 64 (256 packed), multiples of 16");
+    cudaStream_t s = ctx->eng->stream();
+    __nv_bfloat16 *da = nullptr, *db = nullptr;
+    float* dd = nullptr;
+    int* st = nullptr;
+    cuda_check(cudaMallocAsync((void**)&da, (size_t)128 * k * 2, s), "alloc");
+    cuda_check(cudaMallocAsync((void**)&db, (size_t)n * k * 2, s), "alloc");
+    cuda_check(cudaMallocAsync((void**)&dd, (size_t)128 * n * 4, s), "alloc");
+    cuda_check(cudaMallocAsync((void**)&st, sizeof(int), s), "alloc");
+    cuda_check(cudaMemsetAsync(st, 0, sizeof(int), s), "memset");
+    cuda_check(cudaMemcpyAsync(da, a, (size_t)128 * k * 2, cudaMemcpyHostToDevice, s), "h2d");
+    cuda_check(cudaMemcpyAsync(db, b, (size_t)n * k * 2, cudaMemcpyHostToDevice, s), "h2d");
+    if (packed)
+      cuda_check(dev::launch_tc_tile_bulk(da, db, dd, n, k, st, s), "tc tile bulk");
+    else
+      cuda_check(dev::launch_tc_tile(da, db, dd, n, k, st, s), "tc tile");
+    int hst = 0;
+    cuda_check(cudaMemcpyAsync(d, dd, (size_t)128 * n * 4, cudaMemcpyDeviceToHost, s), "d2h");
+    cuda_check(cudaMemcpyAsync(&hst, st, sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
+    for (void* p : {(void*)da, (void*)db, (void*)dd, (void*)st}) cudaFreeAsync(p, s);
+    ctx->eng->sync();
+    if (hst) throw std::runtime_error("bgpu_tc_tile: MMA completion wait ran out");
+  });
+}
+
 int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition, int* sbh, int64_t* psi_elems) {
   return guarded(ctx, [&] {
     need(conf_path && sbh && psi_elems, "null argument");
@@ -443,6 +473,10 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
       stats[5] = r.discarded;
       stats[6] = r.sweep_energies.empty() ? 0.0 : r.sweep_energies.back();
       stats[7] = (double)r.energies.size();
+      stats[8] = r.build_seconds;
+      stats[9] = r.solve_seconds;
+      stats[10] = r.density_seconds;
+      stats[11] = r.renorm_seconds;
     }
   });
 }

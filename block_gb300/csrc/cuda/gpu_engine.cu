@@ -10,6 +10,13 @@
 
 #include "../host/dense.h"
 
+#include <set>
+#include <unordered_map>
+
+#include "../host/parallel.h"
+
+#include <cusolverDn.h>
+
 namespace bgpu {
 
 void cuda_check(cudaError_t e, const char* what) {
@@ -40,6 +47,10 @@ GpuEngine::GpuEngine(int device) : device_(device) {
   cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   cuda_check(cudaEventCreate(&ev0_), "event");
   cuda_check(cudaEventCreate(&ev1_), "event");
+  cuda_check(cudaMalloc((void**)&tc_status_, sizeof(int)), "alloc status");
+  cuda_check(cudaMemset(tc_status_, 0, sizeof(int)), "memset status");
+  cuda_check(cudaMallocHost((void**)&tc_status_host_, sizeof(int)), "alloc status");
+  *tc_status_host_ = 0;
 }
 
 GpuEngine::~GpuEngine() {
@@ -49,9 +60,14 @@ GpuEngine::~GpuEngine() {
   if (waves_) cudaFreeAsync(waves_, stream_);
   if (dm_vecs_) cudaFreeAsync(dm_vecs_, stream_);
   if (rot_) cudaFreeAsync(rot_, stream_);
+  if (solver_work_) cudaFreeAsync(solver_work_, stream_);
+  if (solver_info_) cudaFreeAsync(solver_info_, stream_);
   cudaStreamSynchronize(stream_);
+  if (solver_) cusolverDnDestroy((cusolverDnHandle_t)solver_);
   cudaEventDestroy(ev0_);
   cudaEventDestroy(ev1_);
+  cudaFree(tc_status_);
+  cudaFreeHost(tc_status_host_);
   cudaStreamDestroy(stream_);
 }
 
@@ -64,7 +80,14 @@ double* GpuEngine::alloc(int64_t elems) {
 void GpuEngine::free(double* p) {
   if (p) cudaFreeAsync(p, stream_);
 }
-void GpuEngine::sync() { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
+void GpuEngine::sync() {
+  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  if (*tc_status_host_) {
+    *tc_status_host_ = 0;
+    cudaMemset(tc_status_, 0, sizeof(int));
+    throw std::runtime_error("tensor-core sigma: a pipeline wait ran out (results discarded)");
+  }
+}
 
 void GpuEngine::create_block(Block& b) {
   b.handle = next_handle_++;
@@ -153,6 +176,62 @@ HostView hview(const Block& B, const Operand& o, int bra, int ket) {
 inline int rank2(const Operand& o) { return o.identity ? 0 : o.key.k2; }
 inline bool fermion(const Operand& o) { return !o.identity && op_fermion(o.key); }
 
+// (bra, ket) pairs of the blocks of an operand view
+void view_pairs(const Block& B, const Operand& o, std::vector<std::pair<int, int>>& out) {
+  out.clear();
+  if (o.identity) {
+    for (int q = 0; q < B.si.size(); ++q) out.push_back({q, q});
+    return;
+  }
+  const OpLayout& L = B.ops.layout_of(o.key);
+  for (const OpBlock& b : L.blocks) out.push_back(o.trans ? std::make_pair(b.ket, b.bra) : std::make_pair(b.bra, b.ket));
+}
+
+// One TensorMultiply coupling of a pair term (operatorfunctions.C:506-533):
+// sigma(lQ, rQ) += f * A(lQ, lQ') psi(lQ', rQ') B(rQ, rQ')^T
+struct Coupling {
+  int lQ, lQp, rQ, rQp, cs, vs;
+  HostView va, vb;
+  double f;
+};
+
+// Enumerates the couplings of `t`, driven by the operator's own block list.
+template <class F>
+void for_each_coupling(const Superblock& sb, const PairTerm& t, const std::vector<std::vector<std::pair<int, int>>>& by_l,
+                       F&& fn) {
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const int J = sb.target.s2;
+  const int kL = t.l.identity ? 0 : t.l.key.k2, kR = t.r.identity ? 0 : t.r.key.k2;
+  const bool fR = !t.r.identity && op_fermion(t.r.key);
+  std::vector<std::pair<int, int>> lp;
+  view_pairs(L, t.l, lp);
+  for (auto& pr : lp) {
+    const int lQ = pr.first, lQp = pr.second;
+    HostView va = hview(L, t.l, lQ, lQp);
+    if (!va.ok) continue;
+    for (auto& cp : by_l[lQp]) {
+      const int rQp = cp.first, cs = cp.second;
+      for (auto& vp : by_l[lQ]) {
+        const int rQ = vp.first, vs = vp.second;
+        HostView vb = hview(R, t.r, rQ, rQp);
+        if (!vb.ok) continue;
+        double f = t.coef * ninej(L.si.quanta[lQp].s2, R.si.quanta[rQp].s2, J, kL, kR, 0, L.si.quanta[lQ].s2,
+                                  R.si.quanta[rQ].s2, J);
+        if (fR && is_fermion(L.si.quanta[lQp])) f = -f;
+        if (f == 0.0) continue;
+        fn(Coupling{lQ, lQp, rQ, rQp, cs, vs, va, vb, f});
+      }
+    }
+  }
+}
+
+std::vector<std::vector<std::pair<int, int>>> sectors_by_left(const Superblock& sb) {
+  std::vector<std::vector<std::pair<int, int>>> by_l(sb.L->si.size());
+  for (int s = 0; s < (int)sb.sectors.size(); ++s) by_l[sb.sectors[s].lq].push_back({sb.sectors[s].rq, s});
+  return by_l;
+}
+
 void add_tasks(std::vector<dev::GemmTask>& t, int unit, int m, int n) {
   for (int a = 0; a < (m + 63) / 64; ++a)
     for (int b = 0; b < (n + 63) / 64; ++b) t.push_back({unit, a, b});
@@ -170,57 +249,82 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
   const bool b_scalar = !a_scalar;  // if both are dots, b folds
   if (b_scalar && !db.dot) throw std::runtime_error("build_block: one sub-block must be a single site");
   const DevBlock& dsc = a_scalar ? da : db;
-  const Block& sblk = a_scalar ? a : b;
-  std::vector<dev::CopyUnit> units;
-  std::vector<dev::CopyItem> items;
-  for (const auto& rec : recipes) {
-    const OpKey& tk = rec.first;
+  // per recipe: rectangles keyed by (target block, row part, column part)
+  struct Rect {
+    int64_t key;
+    dev::CopyUnit u;
+    std::vector<dev::CopyItem> items;
+  };
+  std::vector<std::vector<Rect>> per(recipes.size());
+  parallel_for((int)recipes.size(), [&](int ri) {
+    const OpKey& tk = recipes[ri].first;
     const OpEntry& te = big.ops.at(tk);
     const OpLayout& TL = big.ops.layouts[te.layout];
     const int kC = tk.k2;
-    for (const OpBlock& tb : TL.blocks) {
-      const Quantum& Q = big.si.quanta[tb.bra];
-      const Quantum& Qp = big.si.quanta[tb.ket];
-      for (const SectorPart& pr : big.si.parts[tb.bra])
-        for (const SectorPart& pc : big.si.parts[tb.ket]) {
-          const int ibeg = (int)items.size();
-          for (const BuildTerm& t : rec.second) {
-            HostView va = hview(a, t.a, pr.lq, pc.lq);
-            if (!va.ok) continue;
-            HostView vb = hview(b, t.b, pr.rq, pc.rq);
-            if (!vb.ok) continue;
-            double f = t.coef * ninej(a.si.quanta[pc.lq].s2, b.si.quanta[pc.rq].s2, Qp.s2, rank2(t.a), rank2(t.b), kC,
-                                      a.si.quanta[pr.lq].s2, b.si.quanta[pr.rq].s2, Q.s2);
-            if (fermion(t.b) && is_fermion(a.si.quanta[pc.lq])) f = -f;
-            if (f == 0.0) continue;
-            const HostView& vs = a_scalar ? va : vb;  // single-site factor
-            const HostView& vg = a_scalar ? vb : va;  // factor copied from HBM
-            double sv = 1.0;
-            if (!vs.identity) sv = vs.scale * dsc.host[vs.off];  // 1x1 block
-            (void)sblk;
-            f *= sv;
-            if (f == 0.0) continue;
-            dev::CopyItem it;
-            it.alpha = f * (vg.identity ? 1.0 : vg.scale);
-            it.trans = vg.trans ? 1 : 0;
-            it.lds = vg.ld;
-            it.s_off = vg.off;
-            it.s_buf = vg.identity ? -1 : (a_scalar ? 1 : 0);
-            it.pad = 0;
-            items.push_back(it);
-          }
-          if ((int)items.size() == ibeg) continue;
-          dev::CopyUnit u;
-          u.c_off = te.base + tb.offset + (int64_t)pr.offset * tb.cols + pc.offset;
-          u.ldc = tb.cols;
-          u.m = pr.size;
-          u.n = pc.size;
-          u.ibeg = ibeg;
-          u.iend = (int)items.size();
-          units.push_back(u);
+    std::unordered_map<int64_t, int> where;
+    std::vector<Rect>& rects = per[ri];
+    std::vector<std::pair<int, int>> ap, bp;
+    for (const BuildTerm& t : recipes[ri].second) {
+      view_pairs(a, t.a, ap);
+      view_pairs(b, t.b, bp);
+      for (auto& x : ap)
+        for (auto& y : bp) {
+          const auto& rows = big.si.parts_of(x.first, y.first);
+          const auto& cols = big.si.parts_of(x.second, y.second);
+          for (auto& rp : rows)
+            for (auto& cp : cols) {
+              const int tbi = TL.find(rp.first, cp.first);
+              if (tbi < 0) continue;
+              const OpBlock& tb = TL.blocks[tbi];
+              const SectorPart& pr = big.si.parts[rp.first][rp.second];
+              const SectorPart& pc = big.si.parts[cp.first][cp.second];
+              HostView va = hview(a, t.a, pr.lq, pc.lq);
+              HostView vb = hview(b, t.b, pr.rq, pc.rq);
+              if (!va.ok || !vb.ok) continue;
+              double f = t.coef * ninej(a.si.quanta[pc.lq].s2, b.si.quanta[pc.rq].s2, big.si.quanta[tb.ket].s2,
+                                        rank2(t.a), rank2(t.b), kC, a.si.quanta[pr.lq].s2, b.si.quanta[pr.rq].s2,
+                                        big.si.quanta[tb.bra].s2);
+              if (fermion(t.b) && is_fermion(a.si.quanta[pc.lq])) f = -f;
+              if (f == 0.0) continue;
+              const HostView& vs = a_scalar ? va : vb;  // single-site factor
+              const HostView& vg = a_scalar ? vb : va;  // factor copied from HBM
+              if (!vs.identity) f *= vs.scale * dsc.host[vs.off];  // 1x1 block
+              if (f == 0.0) continue;
+              dev::CopyItem it{};
+              it.alpha = f * (vg.identity ? 1.0 : vg.scale);
+              it.trans = vg.trans ? 1 : 0;
+              it.lds = vg.ld;
+              it.s_off = vg.off;
+              it.s_buf = vg.identity ? -1 : (a_scalar ? 1 : 0);
+              const int64_t key = ((int64_t)tbi << 32) | ((int64_t)rp.second << 16) | (int64_t)cp.second;
+              auto w = where.find(key);
+              if (w == where.end()) {
+                Rect r;
+                r.key = key;
+                r.u.c_off = te.base + tb.offset + (int64_t)pr.offset * tb.cols + pc.offset;
+                r.u.ldc = tb.cols;
+                r.u.m = pr.size;
+                r.u.n = pc.size;
+                where.emplace(key, (int)rects.size());
+                rects.push_back(std::move(r));
+                rects.back().items.push_back(it);
+              } else {
+                rects[w->second].items.push_back(it);
+              }
+            }
         }
     }
-  }
+  });
+  std::vector<dev::CopyUnit> units;
+  std::vector<dev::CopyItem> items;
+  for (auto& rv : per)
+    for (auto& r : rv) {
+      dev::CopyUnit u = r.u;
+      u.ibeg = (int)items.size();
+      items.insert(items.end(), r.items.begin(), r.items.end());
+      u.iend = (int)items.size();
+      units.push_back(u);
+    }
   DevBlock& dt = blocks_.at(big.handle);
   cuda_check(cudaMemsetAsync(dt.d, 0, (size_t)std::max<int64_t>(dt.n, 1) * sizeof(double), stream_), "memset");
   DevArray<dev::CopyUnit> du;
@@ -251,133 +355,100 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
 void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   const Block& L = *sb.L;
   const Block& R = *sb.R;
-  const int nL = L.si.size(), nR = R.si.size();
-  std::vector<int> sec((size_t)nL * nR, -1);
-  for (int s = 0; s < (int)sb.sectors.size(); ++s) sec[(size_t)sb.sectors[s].lq * nR + sb.sectors[s].rq] = s;
   const int J = sb.target.s2;
+  const auto by_l = sectors_by_left(sb);
   // buffers: 0 = L arena, 1 = R arena, 2 = psi, 3 = sigma, 4 = scratch
   std::vector<dev::GemmUnit> u1;
   std::vector<dev::GemmItem> i1;
   std::vector<std::vector<dev::GemmItem>> per_sector(sb.sectors.size());
   int64_t scratch = 0;
   double flops = 0.0, bytes = 0.0;
-  std::map<std::pair<int, int64_t>, bool> touched;  // (buf, off) of operator blocks read
-  auto touch = [&](int buf, int64_t off, int64_t elems) {
-    if (touched.emplace(std::make_pair(buf, off), true).second) bytes += 8.0 * elems;
-  };
+  std::set<std::pair<int, OpKey>> used;
   for (const PairTerm& t : sb.terms) {
-    const int kL = rank2(t.l), kR = rank2(t.r);
-    const bool fR = fermion(t.r);
-    for (int lQ = 0; lQ < nL; ++lQ)
-      for (int rQp = 0; rQp < nR; ++rQp)
-        for (int lQp = 0; lQp < nL; ++lQp) {
-          const int cs = sec[(size_t)lQp * nR + rQp];
-          if (cs < 0) continue;
-          HostView va = hview(L, t.l, lQ, lQp);
-          if (!va.ok) continue;
-          const auto& S = sb.sectors[cs];
-          // collect stage-2 partners
-          struct P { int vs; HostView vb; double f; };
-          std::vector<P> parts;
-          for (int rQ = 0; rQ < nR; ++rQ) {
-            const int vs = sec[(size_t)lQ * nR + rQ];
-            if (vs < 0) continue;
-            HostView vb = hview(R, t.r, rQ, rQp);
-            if (!vb.ok) continue;
-            double f = t.coef * ninej(L.si.quanta[lQp].s2, R.si.quanta[rQp].s2, J, kL, kR, 0, L.si.quanta[lQ].s2,
-                                      R.si.quanta[rQ].s2, J);
-            if (fR && is_fermion(L.si.quanta[lQp])) f = -f;
-            if (f == 0.0) continue;
-            parts.push_back({vs, vb, f});
-          }
-          if (parts.empty()) continue;
-          const int mr = L.si.states[lQ], mc = R.si.states[rQp];
-          if (va.identity) {
-            // L identity: sigma(lQ,rQ) += f psi(lQ,rQ') B^T
-            for (auto& pt : parts) {
-              const auto& SV = sb.sectors[pt.vs];
-              dev::GemmItem g{};
-              g.a_buf = 2;
-              g.a_off = S.offset;
-              g.lda = S.cols;
-              g.ta = 0;
-              if (pt.vb.identity) throw std::runtime_error("identity x identity pair term");
-              g.b_buf = 1;
-              g.b_off = pt.vb.off;
-              g.ldb = pt.vb.ld;
-              g.tb = pt.vb.trans ? 0 : 1;
-              g.k = mc;
-              g.alpha = pt.f * pt.vb.scale;
-              per_sector[pt.vs].push_back(g);
-              flops += 2.0 * SV.rows * SV.cols * mc;
-              touch(1, pt.vb.off, (int64_t)pt.vb.rows * pt.vb.cols);
-            }
-            continue;
-          }
-          touch(0, va.off, (int64_t)va.rows * va.cols);
-          bool r_identity = parts.size() == 1 && parts[0].vb.identity;
-          if (r_identity) {
-            // R identity: sigma(lQ,rQ') += f s_L A psi(lQ',rQ')
-            auto& pt = parts[0];
-            dev::GemmItem g{};
-            g.a_buf = 0;
-            g.a_off = va.off;
-            g.lda = va.ld;
-            g.ta = va.trans ? 1 : 0;
-            g.b_buf = 2;
-            g.b_off = S.offset;
-            g.ldb = S.cols;
-            g.tb = 0;
-            g.k = S.rows;
-            g.alpha = pt.f * va.scale;
-            per_sector[pt.vs].push_back(g);
-            flops += 2.0 * mr * mc * S.rows;
-            continue;
-          }
-          // stage 1: M = s_L A psi
-          dev::GemmUnit u{};
-          u.c_buf = 4;
-          u.c_off = scratch;
-          u.ldc = mc;
-          u.m = mr;
-          u.n = mc;
-          u.beta_one = 0;
-          u.ibeg = (int)i1.size();
-          dev::GemmItem g{};
-          g.a_buf = 0;
-          g.a_off = va.off;
-          g.lda = va.ld;
-          g.ta = va.trans ? 1 : 0;
-          g.b_buf = 2;
-          g.b_off = S.offset;
-          g.ldb = S.cols;
-          g.tb = 0;
-          g.k = S.rows;
-          g.alpha = va.scale;
-          i1.push_back(g);
-          u.iend = (int)i1.size();
-          u1.push_back(u);
-          flops += 2.0 * mr * mc * S.rows;
-          for (auto& pt : parts) {
-            const auto& SV = sb.sectors[pt.vs];
-            dev::GemmItem h{};
-            h.a_buf = 4;
-            h.a_off = scratch;
-            h.lda = mc;
-            h.ta = 0;
-            if (pt.vb.identity) throw std::runtime_error("unexpected identity partner");
-            h.b_buf = 1;
-            h.b_off = pt.vb.off;
-            h.ldb = pt.vb.ld;
-            h.tb = pt.vb.trans ? 0 : 1;
-            h.k = mc;
-            h.alpha = pt.f * pt.vb.scale;
-            per_sector[pt.vs].push_back(h);
-            flops += 2.0 * SV.rows * SV.cols * mc;
-            touch(1, pt.vb.off, (int64_t)pt.vb.rows * pt.vb.cols);
-          }
-          scratch += (int64_t)mr * mc;
-        }
+    if (!t.l.identity && used.insert({0, t.l.key}).second) bytes += 8.0 * L.ops.layout_of(t.l.key).size;
+    if (!t.r.identity && used.insert({1, t.r.key}).second) bytes += 8.0 * R.ops.layout_of(t.r.key).size;
+    // group the couplings of a term by (lQ, lQ', rQ'): one stage-1 product each
+    int cur_l = -1, cur_lp = -1, cur_rp = -1;
+    int64_t cur_m = -1;
+    for_each_coupling(sb, t, by_l, [&](const Coupling& c) {
+      const auto& S = sb.sectors[c.cs];
+      const auto& SV = sb.sectors[c.vs];
+      const int mr = L.si.states[c.lQ], mc = R.si.states[c.rQp];
+      if (c.va.identity && c.vb.identity) throw std::runtime_error("identity x identity pair term");
+      if (c.va.identity) {
+        // L identity: sigma(lQ,rQ) += f psi(lQ,rQ') B^T
+        dev::GemmItem g{};
+        g.a_buf = 2;
+        g.a_off = S.offset;
+        g.lda = S.cols;
+        g.b_buf = 1;
+        g.b_off = c.vb.off;
+        g.ldb = c.vb.ld;
+        g.tb = c.vb.trans ? 0 : 1;
+        g.k = mc;
+        g.alpha = c.f * c.vb.scale;
+        per_sector[c.vs].push_back(g);
+        flops += 2.0 * SV.rows * SV.cols * mc;
+        return;
+      }
+      if (c.vb.identity) {
+        // R identity: sigma(lQ,rQ') += f s_L A psi(lQ',rQ')
+        dev::GemmItem g{};
+        g.a_buf = 0;
+        g.a_off = c.va.off;
+        g.lda = c.va.ld;
+        g.ta = c.va.trans ? 1 : 0;
+        g.b_buf = 2;
+        g.b_off = S.offset;
+        g.ldb = S.cols;
+        g.k = S.rows;
+        g.alpha = c.f * c.va.scale;
+        per_sector[c.vs].push_back(g);
+        flops += 2.0 * mr * mc * S.rows;
+        return;
+      }
+      if (!(c.lQ == cur_l && c.lQp == cur_lp && c.rQp == cur_rp)) {
+        // stage 1: M = s_L A psi
+        dev::GemmUnit u{};
+        u.c_buf = 4;
+        u.c_off = scratch;
+        u.ldc = mc;
+        u.m = mr;
+        u.n = mc;
+        u.ibeg = (int)i1.size();
+        dev::GemmItem g{};
+        g.a_buf = 0;
+        g.a_off = c.va.off;
+        g.lda = c.va.ld;
+        g.ta = c.va.trans ? 1 : 0;
+        g.b_buf = 2;
+        g.b_off = S.offset;
+        g.ldb = S.cols;
+        g.k = S.rows;
+        g.alpha = c.va.scale;
+        i1.push_back(g);
+        u.iend = (int)i1.size();
+        u1.push_back(u);
+        flops += 2.0 * mr * mc * S.rows;
+        cur_l = c.lQ;
+        cur_lp = c.lQp;
+        cur_rp = c.rQp;
+        cur_m = scratch;
+        scratch += (int64_t)mr * mc;
+      }
+      dev::GemmItem h{};
+      h.a_buf = 4;
+      h.a_off = cur_m;
+      h.lda = mc;
+      h.b_buf = 1;
+      h.b_off = c.vb.off;
+      h.ldb = c.vb.ld;
+      h.tb = c.vb.trans ? 0 : 1;
+      h.k = mc;
+      h.alpha = c.f * c.vb.scale;
+      per_sector[c.vs].push_back(h);
+      flops += 2.0 * SV.rows * SV.cols * mc;
+    });
   }
   std::vector<dev::GemmUnit> u2;
   std::vector<dev::GemmItem> i2;
@@ -469,6 +540,22 @@ void GpuEngine::free_plan(SigmaPlan& p) {
   if (p.partials) cudaFreeAsync(p.partials, stream_);
   p.partials = nullptr;
   p.fused = false;
+  for (int i = 0; i < dev::kTcPools; ++i) {
+    if (p.tc_hi[i]) cudaFreeAsync(p.tc_hi[i], stream_);
+    if (p.tc_lo[i]) cudaFreeAsync(p.tc_lo[i], stream_);
+    p.tc_hi[i] = p.tc_lo[i] = nullptr;
+    p.tc_pool_elems[i] = 0;
+  }
+  p.tc_psi_pack.release(stream_);
+  p.tc_i1.release(stream_);
+  p.tc_i2.release(stream_);
+  p.tc_t1.release(stream_);
+  p.tc_t2.release(stream_);
+  p.tc_tiles.release(stream_);
+  p.tc_slots.release(stream_);
+  if (p.tc_partials) cudaFreeAsync(p.tc_partials, stream_);
+  p.tc_partials = nullptr;
+  p.tc = false;
   p.u1.release(stream_);
   p.u2.release(stream_);
   p.i1.release(stream_);
@@ -517,67 +604,49 @@ const GpuEngine::Slices& GpuEngine::block_slices(const Block& b, int ns) {
 // its coupling list cut into chunks of similar cost (one thread block each)
 // and a fixed-order reduction of the chunks' partial tiles.
 void GpuEngine::plan_fused(const Superblock& sb, SigmaPlan& plan) {
-  const Block& L = *sb.L;
-  const Block& R = *sb.R;
-  const int nL = L.si.size(), nR = R.si.size();
-  std::vector<int> sec((size_t)nL * nR, -1);
-  for (int s = 0; s < (int)sb.sectors.size(); ++s) sec[(size_t)sb.sectors[s].lq * nR + sb.sectors[s].rq] = s;
-  const int J = sb.target.s2;
+  const auto by_l = sectors_by_left(sb);
+  std::vector<std::vector<std::vector<dev::FusedItem>>> per_t(sb.terms.size());
+  parallel_for((int)sb.terms.size(), [&](int ti) {
+    auto& per = per_t[ti];
+    per.assign(sb.sectors.size(), {});
+    for_each_coupling(sb, sb.terms[ti], by_l, [&](const Coupling& c) {
+      const auto& C = sb.sectors[c.cs];
+      dev::FusedItem it{};
+      it.n1 = C.cols;
+      it.k1 = C.rows;
+      it.c_off = C.offset;
+      it.ldc = C.cols;
+      if (c.va.identity && c.vb.identity) throw std::runtime_error("identity x identity pair term");
+      if (c.va.identity) {
+        it.kind = dev::kFusedLIdent;
+        it.a_off = C.offset;  // psi(lQ, rQ') with lQ' = lQ
+        it.lda = C.cols;
+        it.b_off = c.vb.off;
+        it.ldb = c.vb.ld;
+        it.tb = c.vb.trans;
+        it.alpha = (float)(c.f * c.vb.scale);
+      } else if (c.vb.identity) {
+        it.kind = dev::kFusedRIdent;
+        it.a_off = c.va.off;
+        it.lda = c.va.ld;
+        it.ta = c.va.trans;
+        it.alpha = (float)(c.f * c.va.scale);
+      } else {
+        it.kind = dev::kFusedFull;
+        it.a_off = c.va.off;
+        it.lda = c.va.ld;
+        it.ta = c.va.trans;
+        it.b_off = c.vb.off;
+        it.ldb = c.vb.ld;
+        it.tb = c.vb.trans;
+        it.alpha = (float)(c.f * c.va.scale * c.vb.scale);
+      }
+      per[c.vs].push_back(it);
+    });
+  });
   std::vector<std::vector<dev::FusedItem>> per(sb.sectors.size());
-  for (const PairTerm& t : sb.terms) {
-    const int kL = rank2(t.l), kR = rank2(t.r);
-    const bool fR = fermion(t.r);
-    for (int lQ = 0; lQ < nL; ++lQ)
-      for (int rQp = 0; rQp < nR; ++rQp)
-        for (int lQp = 0; lQp < nL; ++lQp) {
-          const int cs = sec[(size_t)lQp * nR + rQp];
-          if (cs < 0) continue;
-          HostView va = hview(L, t.l, lQ, lQp);
-          if (!va.ok) continue;
-          const auto& C = sb.sectors[cs];
-          for (int rQ = 0; rQ < nR; ++rQ) {
-            const int vs = sec[(size_t)lQ * nR + rQ];
-            if (vs < 0) continue;
-            HostView vb = hview(R, t.r, rQ, rQp);
-            if (!vb.ok) continue;
-            double f = t.coef * ninej(L.si.quanta[lQp].s2, R.si.quanta[rQp].s2, J, kL, kR, 0, L.si.quanta[lQ].s2,
-                                      R.si.quanta[rQ].s2, J);
-            if (fR && is_fermion(L.si.quanta[lQp])) f = -f;
-            if (f == 0.0) continue;
-            dev::FusedItem it{};
-            it.n1 = C.cols;
-            it.k1 = C.rows;
-            it.c_off = C.offset;
-            it.ldc = C.cols;
-            if (va.identity && vb.identity) throw std::runtime_error("identity x identity pair term");
-            if (va.identity) {
-              it.kind = dev::kFusedLIdent;
-              it.a_off = C.offset;  // psi(lQ, rQ') with lQ' = lQ
-              it.lda = C.cols;
-              it.b_off = vb.off;
-              it.ldb = vb.ld;
-              it.tb = vb.trans;
-              it.alpha = (float)(f * vb.scale);
-            } else if (vb.identity) {
-              it.kind = dev::kFusedRIdent;
-              it.a_off = va.off;
-              it.lda = va.ld;
-              it.ta = va.trans;
-              it.alpha = (float)(f * va.scale);
-            } else {
-              it.kind = dev::kFusedFull;
-              it.a_off = va.off;
-              it.lda = va.ld;
-              it.ta = va.trans;
-              it.b_off = vb.off;
-              it.ldb = vb.ld;
-              it.tb = vb.trans;
-              it.alpha = (float)(f * va.scale * vb.scale);
-            }
-            per[vs].push_back(it);
-          }
-        }
-  }
+  for (auto& pt : per_t)
+    for (size_t s2 = 0; s2 < pt.size(); ++s2) per[s2].insert(per[s2].end(), pt[s2].begin(), pt[s2].end());
   auto cost = [](const dev::FusedItem& it) {
     const double n1 = ((it.n1 + 15) / 16) * 16.0, k1 = ((it.k1 + 15) / 16) * 16.0;
     double c = 2048.0;
@@ -667,13 +736,296 @@ void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const do
   ++sigma_calls;
 }
 
+// Tensor-core plan.  Stage-1 products S = s_L A psi (one per (term, lQ, lQ',
+// rQ') as in plan_sigma) become phase-1 tasks writing S as packed bf16
+// (hi, lo) operands; every sigma sector tile then sums its items
+// alpha * X * Y^T (X = S, psi or an L operator; Y = an R operator or psi^T)
+// in phase 2, in the same order as the FP64 plan.
+void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
+  using namespace dev;
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const auto by_l = sectors_by_left(sb);
+  const int nsec = (int)sb.sectors.size();
+  std::vector<std::vector<Coupling>> per_t(sb.terms.size());
+  parallel_for((int)sb.terms.size(), [&](int ti) {
+    for_each_coupling(sb, sb.terms[ti], by_l, [&](const Coupling& c) { per_t[ti].push_back(c); });
+  });
+  int64_t pool_n[kTcPools] = {0, 0, 0, 0, 0};
+  // (rows_p, kp) of every packed operand, by pool and offset: every item is
+  // checked against its tile below, so that no bulk copy leaves its operand
+  std::unordered_map<int64_t, std::pair<int, int>> dims[kTcPools];
+  std::vector<TcPack> ops_packs, psi_packs;
+  std::unordered_map<int64_t, int64_t> lmap, rmap;
+  auto pack_view = [&](int pool, const HostView& v, std::unordered_map<int64_t, int64_t>& m) -> int64_t {
+    const int64_t key = v.off * 2 + (v.trans ? 1 : 0);
+    auto it = m.find(key);
+    if (it != m.end()) return it->second;
+    TcPack p{};
+    p.src_off = v.off;
+    p.ld = v.ld;
+    p.rows_v = v.rows;
+    p.cols_v = v.cols;
+    p.rows_p = tc_round8(v.rows);
+    p.kp = tc_round16(v.cols);
+    p.trans = v.trans ? 1 : 0;
+    p.src = (uint8_t)pool;  // 0: L arena, 1: R arena
+    p.pool = (uint8_t)pool;
+    p.dst_off = pool_n[pool];
+    pool_n[pool] += (int64_t)p.rows_p * p.kp;
+    dims[pool][p.dst_off] = {p.rows_p, p.kp};
+    ops_packs.push_back(p);
+    m.emplace(key, p.dst_off);
+    return p.dst_off;
+  };
+  std::vector<int64_t> psi_off(nsec), psit_off(nsec);
+  for (int s = 0; s < nsec; ++s) {
+    const auto& S = sb.sectors[s];
+    TcPack a{};
+    a.src = 2;
+    a.pool = kTcPoolPsi;
+    a.src_off = S.offset;
+    a.ld = S.cols;
+    a.rows_v = S.rows;
+    a.cols_v = S.cols;
+    a.rows_p = tc_round8(S.rows);
+    a.kp = tc_round16(S.cols);
+    a.dst_off = psi_off[s] = pool_n[kTcPoolPsi];
+    pool_n[kTcPoolPsi] += (int64_t)a.rows_p * a.kp;
+    dims[kTcPoolPsi][a.dst_off] = {a.rows_p, a.kp};
+    psi_packs.push_back(a);
+    TcPack t = a;
+    t.pool = kTcPoolPsiT;
+    t.trans = 1;
+    t.rows_v = S.cols;
+    t.cols_v = S.rows;
+    t.rows_p = tc_round8(S.cols);
+    t.kp = tc_round16(S.rows);
+    t.dst_off = psit_off[s] = pool_n[kTcPoolPsiT];
+    pool_n[kTcPoolPsiT] += (int64_t)t.rows_p * t.kp;
+    dims[kTcPoolPsiT][t.dst_off] = {t.rows_p, t.kp};
+    psi_packs.push_back(t);
+  }
+  std::vector<TcItem> i1;
+  std::vector<TcTask> t1;
+  std::vector<std::vector<TcItem>> per_sector(nsec);
+  double mma = 0.0;
+  for (auto& cl : per_t) {
+    int cur_l = -1, cur_lp = -1, cur_rp = -1, cur_kp = 0;
+    int64_t cur_s = -1;
+    for (const Coupling& c : cl) {
+      if (c.va.identity && c.vb.identity) throw std::runtime_error("identity x identity pair term");
+      TcItem it{};
+      if (c.va.identity) {  // sigma(lQ,rQ) += f psi(lQ,rQ') B^T
+        it.a_pool = kTcPoolPsi;
+        it.a_off = psi_off[c.cs];
+        it.b_pool = kTcPoolR;
+        it.b_off = pack_view(1, c.vb, rmap);
+        it.kp = tc_round16(R.si.states[c.rQp]);
+        it.alpha = (float)(c.f * c.vb.scale);
+        per_sector[c.vs].push_back(it);
+        continue;
+      }
+      if (c.vb.identity) {  // sigma(lQ,rQ') += f s_L A psi(lQ',rQ')
+        it.a_pool = kTcPoolL;
+        it.a_off = pack_view(0, c.va, lmap);
+        it.b_pool = kTcPoolPsiT;
+        it.b_off = psit_off[c.cs];
+        it.kp = tc_round16(L.si.states[c.lQp]);
+        it.alpha = (float)(c.f * c.va.scale);
+        per_sector[c.vs].push_back(it);
+        continue;
+      }
+      if (!(c.lQ == cur_l && c.lQp == cur_lp && c.rQp == cur_rp)) {
+        const int mr = L.si.states[c.lQ], mc = R.si.states[c.rQp], k1 = L.si.states[c.lQp];
+        const int rows_p = tc_round8(mr), skp = tc_round16(mc);
+        cur_s = pool_n[kTcPoolS];
+        pool_n[kTcPoolS] += (int64_t)rows_p * skp;
+        dims[kTcPoolS][cur_s] = {rows_p, skp};
+        TcItem a{};
+        a.a_pool = kTcPoolL;
+        a.a_off = pack_view(0, c.va, lmap);
+        a.b_pool = kTcPoolPsiT;
+        a.b_off = psit_off[c.cs];
+        a.kp = tc_round16(k1);
+        a.alpha = (float)c.va.scale;
+        const int idx = (int)i1.size();
+        i1.push_back(a);
+        for (int tm = 0; tm < (mr + 127) / 128; ++tm)
+          for (int tn = 0; tn < (mc + 127) / 128; ++tn) {
+            TcTask t{};
+            t.a_rows = rows_p;
+            t.b_rows = tc_round8(mc);
+            t.tm = tm;
+            t.tn = tn;
+            t.ibeg = idx;
+            t.iend = idx + 1;
+            t.out_off = cur_s;
+            t.out_kp = skp;
+            t1.push_back(t);
+            mma += 3.0 * 2.0 * 128 * tc_round16(std::min(128, t.b_rows - 128 * tn)) * a.kp;
+          }
+        cur_l = c.lQ;
+        cur_lp = c.lQp;
+        cur_rp = c.rQp;
+        cur_kp = skp;
+      }
+      it.a_pool = kTcPoolS;
+      it.a_off = cur_s;
+      it.b_pool = kTcPoolR;
+      it.b_off = pack_view(1, c.vb, rmap);
+      it.kp = cur_kp;
+      it.alpha = (float)(c.f * c.vb.scale);
+      per_sector[c.vs].push_back(it);
+    }
+  }
+  // phase 2: sector tiles, items split into tasks of similar cost
+  std::vector<TcItem> i2;
+  std::vector<TcTask> t2;
+  std::vector<TcTile> tiles;
+  std::vector<int64_t> slots;
+  int64_t partial_n = 0;
+  double total = 0.0;
+  for (int s = 0; s < nsec; ++s) {
+    const auto& S = sb.sectors[s];
+    for (const TcItem& it : per_sector[s]) total += (it.kp + 64.0) * ((S.rows + 127) / 128) * ((S.cols + 127) / 128);
+  }
+  const double chunk = std::max(total / (152.0 * 4.0), 4096.0);
+  struct Pending {
+    TcTask t;
+    double cost;
+  };
+  std::vector<Pending> pend;
+  for (int s = 0; s < nsec; ++s) {
+    const auto& S = sb.sectors[s];
+    const int ib = (int)i2.size();
+    i2.insert(i2.end(), per_sector[s].begin(), per_sector[s].end());
+    const int ie = (int)i2.size();
+    const int rows_p = tc_round8(S.rows), cols_p = tc_round8(S.cols);
+    for (int tm = 0; tm < (S.rows + 127) / 128; ++tm)
+      for (int tn = 0; tn < (S.cols + 127) / 128; ++tn) {
+        const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(128, cols_p - 128 * tn);
+        TcTile tl{};
+        tl.s_off = S.offset;
+        tl.lds = S.cols;
+        tl.h = std::min(128, S.rows - 128 * tm);
+        tl.w = std::min(128, S.cols - 128 * tn);
+        tl.r0 = 128 * tm;
+        tl.c0 = 128 * tn;
+        tl.pad = hb;  // row stride of the partial slots
+        tl.pbeg = (int)slots.size();
+        int a = ib;
+        while (a < ie) {
+          double acc = 0.0;
+          int e = a;
+          while (e < ie && (acc < chunk || e == a)) acc += i2[e++].kp + 64.0;
+          TcTask t{};
+          t.a_rows = rows_p;
+          t.b_rows = cols_p;
+          t.tm = tm;
+          t.tn = tn;
+          t.ibeg = a;
+          t.iend = e;
+          t.out_off = partial_n;
+          slots.push_back(partial_n);
+          partial_n += (int64_t)ha * hb;
+          pend.push_back({t, acc});
+          for (int x = a; x < e; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
+          a = e;
+        }
+        tl.pend = (int)slots.size();
+        tiles.push_back(tl);
+      }
+  }
+  auto check = [&](const TcTask& t, const std::vector<TcItem>& items) {
+    for (int x = t.ibeg; x < t.iend; ++x) {
+      const TcItem& it = items[x];
+      const auto a = dims[it.a_pool].find(it.a_off);
+      const auto b = dims[it.b_pool].find(it.b_off);
+      if (a == dims[it.a_pool].end() || b == dims[it.b_pool].end() || a->second.first != t.a_rows ||
+          b->second.first != t.b_rows || a->second.second != it.kp || b->second.second != it.kp ||
+          128 * t.tm >= t.a_rows || 128 * t.tn >= t.b_rows)
+        throw std::runtime_error("tensor-core plan: operand shape does not match its tile");
+    }
+  };
+  for (const TcTask& t : t1) {
+    check(t, i1);
+    const auto sdim = dims[kTcPoolS].find(t.out_off);
+    if (sdim == dims[kTcPoolS].end() || sdim->second.first != t.a_rows || sdim->second.second != t.out_kp ||
+        128 * t.tn >= t.out_kp)
+      throw std::runtime_error("tensor-core plan: stage-1 output does not match its tile");
+  }
+  for (const Pending& p : pend) check(p.t, i2);
+  std::stable_sort(pend.begin(), pend.end(), [](const Pending& x, const Pending& y) { return x.cost > y.cost; });
+  for (auto& p : pend) t2.push_back(p.t);
+  // buffers
+  for (int i = 0; i < kTcPools; ++i) {
+    plan.tc_pool_elems[i] = pool_n[i];
+    const size_t bytes = (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16);
+    cuda_check(cudaMallocAsync((void**)&plan.tc_hi[i], bytes, stream_), "tc pool");
+    cuda_check(cudaMallocAsync((void**)&plan.tc_lo[i], bytes, stream_), "tc pool");
+  }
+  cuda_check(cudaMallocAsync((void**)&plan.tc_partials, (size_t)std::max<int64_t>(partial_n, 1) * sizeof(float2),
+                             stream_),
+             "tc partials");
+  plan.tc_psi_pack.upload(psi_packs, stream_);
+  plan.tc_i1.upload(i1, stream_);
+  plan.tc_t1.upload(t1, stream_);
+  plan.tc_i2.upload(i2, stream_);
+  plan.tc_t2.upload(t2, stream_);
+  plan.tc_tiles.upload(tiles, stream_);
+  plan.tc_slots.upload(slots, stream_);
+  plan.tc_mma_flops = mma;
+  // operator blocks are packed once per plan
+  DevArray<TcPack> dops;
+  dops.upload(ops_packs, stream_);
+  TcBufs b{};
+  b.src[0] = arena(L);
+  b.src[1] = arena(R);
+  for (int i = 0; i < kTcPools; ++i) {
+    b.hi[i] = plan.tc_hi[i];
+    b.lo[i] = plan.tc_lo[i];
+  }
+  cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
+  dops.release(stream_);
+  plan.tc = true;
+  sync();
+}
+
+void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, double* out, cudaEvent_t* marks) {
+  if (!p.tc) plan_tc(sb, p);
+  dev::TcBufs b{};
+  b.src[0] = arena(*sb.L);
+  b.src[1] = arena(*sb.R);
+  b.src[2] = psi;
+  for (int i = 0; i < dev::kTcPools; ++i) {
+    b.hi[i] = p.tc_hi[i];
+    b.lo[i] = p.tc_lo[i];
+  }
+  b.partials = p.tc_partials;
+  b.status = tc_status_;
+  constexpr uint64_t kWaitLimitNs = 1000000000ull;
+  cuda_check(dev::launch_tc_pack(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tc pack psi");
+  if (marks) cuda_check(cudaEventRecord(marks[0], stream_), "record");
+  cuda_check(dev::launch_tc_sigma(1, b, p.tc_i1.d, p.tc_t1.d, (int)p.tc_t1.n, kWaitLimitNs, stream_), "tc phase 1");
+  cuda_check(dev::launch_tc_sigma(2, b, p.tc_i2.d, p.tc_t2.d, (int)p.tc_t2.n, kWaitLimitNs, stream_), "tc phase 2");
+  if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");
+  cuda_check(dev::launch_tc_reduce(b, p.tc_tiles.d, p.tc_slots.d, (int)p.tc_tiles.n, out, stream_), "tc reduce");
+  if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
+  cuda_check(cudaMemcpyAsync(tc_status_host_, tc_status_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "status");
+  sigma_flops += p.flops;
+  ++sigma_calls;
+}
+
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
   const int ns = precision_slices(precision);
-  if (ns) sigma_split(sb, p, ns, psi, out);
+  if (precision == Precision::BF16X3_TC) sigma_tc(sb, p, psi, out);
+  else if (ns) sigma_split(sb, p, ns, psi, out);
   else sigma(sb, p, psi, out);
 }
 
 int GpuEngine::sigma_launches(const SigmaPlan& p) const {
+  if (precision == Precision::BF16X3_TC) return 4 + (p.ecore != 0.0 ? 1 : 0);  // pack psi, phase 1, phase 2, reduce
   if (precision_slices(precision)) return 3 + (p.ecore != 0.0 ? 1 : 0);  // slice psi, fused, reduce (+ecore)
   return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
 }
@@ -692,21 +1044,26 @@ void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const doub
   const int ns = precision_slices(precision);
   if (ns) {
     SigmaPlan& pm = const_cast<SigmaPlan&>(p);
-    sigma_split(sb, pm, ns, psi, out);  // slices operators and buffers outside the timed region
+    auto call = [&](cudaEvent_t* marks) {
+      if (precision == Precision::BF16X3_TC) sigma_tc(sb, pm, psi, out, marks);
+      else sigma_split(sb, pm, ns, psi, out, marks);
+    };
+    call(nullptr);  // slices / packs operators and buffers outside the timed region
     sync();
     for (int r = 0; r < reps; ++r) {
       cuda_check(cudaEventRecord(e[0], stream_), "record");
-      sigma_split(sb, pm, ns, psi, out, e + 1);
+      call(e + 1);
       cuda_check(cudaEventRecord(e[3], stream_), "record");
       cuda_check(cudaEventSynchronize(e[3]), "sync");
       float a, b;
       cudaEventElapsedTime(&a, e[0], e[3]);
       cudaEventElapsedTime(&b, e[1], e[2]);
       ms[0] += a;
-      ms[1] += b;  // fused two-stage kernel alone
+      ms[1] += b;  // tensor-core kernels alone
       ms[2] += a - b;
     }
     for (auto& x : e) cudaEventDestroy(x);
+    sync();
     return;
   }
   for (int r = 0; r < reps; ++r) {
@@ -878,9 +1235,12 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
         k = p.deflation_min;
         ks = std::min(ks, k);
       }
-      for (int j = 0; j < k; ++j) {
-        cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(r, r)), r, n, stream_), "scale");
-        cuda_check(dev::launch_axpy(-dot(r, row(B, j)), row(B, j), r, n, stream_), "gs");
+      // classical Gram-Schmidt applied twice against the whole basis (the
+      // reference orthogonalises one basis vector at a time; same span and
+      // normalised result, without a host round trip per basis vector)
+      for (int pass = 0; pass < 2; ++pass) {
+        cuda_check(dev::launch_gram(B, k, r, 1, n, n, work, red, stream_), "gs coefficients");
+        cuda_check(dev::launch_project_out(B, k, n, n, red, r, stream_), "gs");
       }
       cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(r, r)), r, n, stream_), "scale");
       cuda_check(cudaMemcpyAsync(row(B, k), r, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "append");
@@ -979,32 +1339,87 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   bufs.p[0] = waves_;
   bufs.p[1] = rho;
   cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "density");
-  // eigen-decomposition of every sector (diagonalise_dm)
+  // eigen-decomposition of every sector (diagonalise_dm): sectors up to
+  // kJacobiMax states in one batched Jacobi launch, larger ones with the
+  // dense divide-and-conquer solver (eigenvectors column-major)
+  constexpr int kJacobiMax = 48;
   if (dm_vecs_) free(dm_vecs_);
   dm_vecs_ = alloc(tot);
   dm_off_ = off;
+  dm_colmajor_.assign(nq, 0);
   double* w = alloc(std::max<int64_t>(B.si.total_states(), 1));
   std::vector<int64_t> woff(nq);
   int64_t wt = 0;
+  std::vector<int> small_dims(nq, 0), large;
+  int small_max = 0;
   for (int q = 0; q < nq; ++q) {
     woff[q] = wt;
     wt += B.si.states[q];
+    if (dm_dims_[q] > kJacobiMax) {
+      large.push_back(q);
+      dm_colmajor_[q] = 1;
+    } else {
+      small_dims[q] = dm_dims_[q];
+      small_max = std::max(small_max, dm_dims_[q]);
+    }
   }
   DevArray<int64_t> doff, dwoff;
   DevArray<int> ddims, dstat;
   doff.upload(off, stream_);
   dwoff.upload(woff, stream_);
-  ddims.upload(dm_dims_, stream_);
+  ddims.upload(small_dims, stream_);
   dstat.upload(std::vector<int>(nq, 0), stream_);
-  cuda_check(dev::launch_jacobi(rho, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, maxn, stream_),
-             "density eig");
+  if (small_max > 0)
+    cuda_check(dev::launch_jacobi(rho, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, small_max, stream_),
+               "density eig");
+  if (!large.empty()) {
+    auto h = (cusolverDnHandle_t)solver_;
+    if (!h) {
+      if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnCreate failed");
+      solver_ = h;
+    }
+    if (cusolverDnSetStream(h, stream_) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnSetStream");
+    int need = 0;
+    for (int q : large) {
+      int lw = 0;
+      if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, dm_dims_[q],
+                                      dm_vecs_ + off[q], dm_dims_[q], w + woff[q], &lw) != CUSOLVER_STATUS_SUCCESS)
+        throw std::runtime_error("syevd buffer size");
+      need = std::max(need, lw);
+    }
+    if (need > solver_lwork_) {
+      if (solver_work_) free(solver_work_);
+      solver_work_ = alloc(need);
+      solver_lwork_ = need;
+    }
+    if ((int)large.size() > solver_ninfo_) {
+      if (solver_info_) cudaFreeAsync(solver_info_, stream_);
+      cuda_check(cudaMallocAsync((void**)&solver_info_, large.size() * sizeof(int), stream_), "alloc info");
+      solver_ninfo_ = (int)large.size();
+    }
+    for (size_t i = 0; i < large.size(); ++i) {
+      const int q = large[i];
+      const int n = dm_dims_[q];
+      cuda_check(cudaMemcpyAsync(dm_vecs_ + off[q], rho + off[q], (size_t)n * n * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, stream_),
+                 "copy rho");
+      if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, dm_vecs_ + off[q], n, w + woff[q],
+                           solver_work_, (int)solver_lwork_, solver_info_ + i) != CUSOLVER_STATUS_SUCCESS)
+        throw std::runtime_error("syevd launch failed");
+    }
+  }
   std::vector<double> hw(wt);
-  std::vector<int> st(nq);
+  std::vector<int> st(nq), info(large.size());
   cuda_check(cudaMemcpyAsync(hw.data(), w, wt * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
   cuda_check(cudaMemcpyAsync(st.data(), dstat.d, nq * sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
+  if (!large.empty())
+    cuda_check(cudaMemcpyAsync(info.data(), solver_info_, large.size() * sizeof(int), cudaMemcpyDeviceToHost, stream_),
+               "d2h");
   sync();
   for (int q = 0; q < nq; ++q)
     if (st[q] < 0) throw std::runtime_error("density-matrix eigensolver did not converge");
+  for (int x : info)
+    if (x != 0) throw std::runtime_error("density-matrix dense eigensolver failed");
   spec.eig.assign(nq, {});
   for (int q = 0; q < nq; ++q) spec.eig[q].assign(hw.begin() + woff[q], hw.begin() + woff[q] + B.si.states[q]);
   du.release(stream_);
@@ -1034,6 +1449,7 @@ void GpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {
     dev::GatherUnit g{};
     g.u_off = tot;
     g.v_off = dm_off_[q];
+    g.colmajor = dm_colmajor_.empty() ? 0 : dm_colmajor_[q];
     g.n = dm_dims_[q];
     g.m = rot_kept_[q];
     g.c_off = (int)cols.size();

@@ -14,12 +14,18 @@
 #include "../host/sweep.h"
 #include "k_fused.cuh"
 #include "k_split.cuh"
+#include "k_tc.cuh"
 #include "kernels.cuh"
 
 namespace bgpu {
 
-enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2 };
-inline int precision_slices(Precision p) { return p == Precision::BF16X3 ? 2 : p == Precision::BF16X6 ? 3 : 0; }
+// FP64, or split precision: bf16 slices on the tensor cores with f32
+// accumulation (BF16X3 / BF16X6: warp-level MMA kernel with 2 / 3 slices;
+// BF16X3_TC: tcgen05 / TMEM kernels with 2 slices)
+enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2, BF16X3_TC = 3 };
+inline int precision_slices(Precision p) {
+  return (p == Precision::BF16X3 || p == Precision::BF16X3_TC) ? 2 : p == Precision::BF16X6 ? 3 : 0;
+}
 
 struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
@@ -57,6 +63,20 @@ struct SigmaPlan {
   float* partials = nullptr;
   int ns = 0;
   __nv_bfloat16* psi_s[3] = {nullptr, nullptr, nullptr};
+  // tensor-core (tcgen05) split-precision work lists and packed operand
+  // pools (built on first use): L / R operator blocks packed once, psi and
+  // psi^T packed per product, S = stage-1 products written by phase 1
+  bool tc = false;
+  __nv_bfloat16* tc_hi[dev::kTcPools] = {};
+  __nv_bfloat16* tc_lo[dev::kTcPools] = {};
+  int64_t tc_pool_elems[dev::kTcPools] = {};
+  DevArray<dev::TcPack> tc_psi_pack;
+  DevArray<dev::TcItem> tc_i1, tc_i2;
+  DevArray<dev::TcTask> tc_t1, tc_t2;
+  DevArray<dev::TcTile> tc_tiles;
+  DevArray<int64_t> tc_slots;
+  float2* tc_partials = nullptr;
+  double tc_mma_flops = 0.0;  // tensor-core flops issued per product (3 bf16 products per logical one)
 };
 
 class GpuEngine : public Engine {
@@ -85,6 +105,10 @@ class GpuEngine : public Engine {
   void sigma_split(const Superblock& sb, SigmaPlan& plan, int ns, const double* psi_d, double* out_d,
                    cudaEvent_t* marks = nullptr);
   void plan_fused(const Superblock& sb, SigmaPlan& plan);
+  // split-precision product on tcgen05 (pack psi, phase 1, phase 2, reduce)
+  void plan_tc(const Superblock& sb, SigmaPlan& plan);
+  void sigma_tc(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d,
+                cudaEvent_t* marks = nullptr);
   // product at the engine's current precision
   void sigma_any(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d);
   void hdiag(const Superblock& sb, const SigmaPlan& plan, double* diag_d);
@@ -134,10 +158,20 @@ class GpuEngine : public Engine {
   double* dm_vecs_ = nullptr;
   std::vector<int64_t> dm_off_;
   std::vector<int> dm_dims_;
+  std::vector<char> dm_colmajor_;  // sector eigenvectors stored column-major (dense solver)
+  // dense symmetric eigensolver for the large density-matrix sectors
+  void* solver_ = nullptr;  // cusolverDnHandle_t
+  double* solver_work_ = nullptr;
+  int64_t solver_lwork_ = 0;
+  int* solver_info_ = nullptr;
+  int solver_ninfo_ = 0;
   double* rot_ = nullptr;
   std::vector<int64_t> rot_off_;
   std::vector<int> rot_kept_, rot_rows_;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  // pipeline-wait status of the tensor-core kernels (device flag, pinned copy)
+  int* tc_status_ = nullptr;
+  int* tc_status_host_ = nullptr;
 };
 
 }  // namespace bgpu

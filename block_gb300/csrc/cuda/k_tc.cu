@@ -1,0 +1,527 @@
+// tcgen05 building blocks: a single-tile GEMM used to check the operand
+// layout, descriptors and TMEM read-back against a host product.
+#include "k_tc.cuh"
+#include "tc.cuh"
+
+namespace bgpu {
+namespace dev {
+
+using namespace tc;
+
+// D (128 x N, row-major f32) = A (128 x K, row-major bf16) * B (N x K, row-major bf16)^T
+__global__ void __launch_bounds__(128) tc_tile_kernel(const __nv_bfloat16* __restrict__ A,
+                                                       const __nv_bfloat16* __restrict__ B, float* __restrict__ D,
+                                                       int N, int K, int* status) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tbase;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + 128 * K * 2;
+  if (warp == 0) {
+    tmem_alloc(&tbase, 256);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  for (int idx = tid; idx < 128 * K; idx += 128)
+    *(__nv_bfloat16*)(sA + kmajor_off(idx / K, idx % K, 128)) = A[idx];
+  for (int idx = tid; idx < N * K; idx += 128) *(__nv_bfloat16*)(sB + kmajor_off(idx / K, idx % K, N)) = B[idx];
+  fence_async_smem();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t d = tbase;
+  if (tid == 0) {
+    const uint32_t idesc = idesc_bf16(128, N);
+    for (int j = 0; j < K / 16; ++j) {
+      const uint64_t ad = smem_desc(smem_u32(sA) + j * 2 * 128 * 16, 128 * 16, 128);
+      const uint64_t bd = smem_desc(smem_u32(sB) + j * 2 * N * 16, N * 16, 128);
+      mma_bf16(d, ad, bd, idesc, j > 0 ? 1u : 0u);
+    }
+    mma_commit(&bar);
+  }
+  __syncwarp();
+  bool ok = mbar_wait_bounded(&bar, 0, 1000000000ull);
+  ok = __syncthreads_and(ok) != 0;
+  fence_after_sync();
+  if (ok) {
+    const int row = warp * 32 + (tid & 31);
+    for (int c = 0; c < N; c += 16) {
+      float v[16];
+      tmem_ld16(d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) D[(int64_t)row * N + c + i] = v[i];
+    }
+  } else {
+    if (tid == 0) atomicExch(status, 1);
+    mbar_wait_bounded(&bar, 0, 1000000000ull);  // let the MMAs drain before freeing TMEM
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tbase, 256);
+}
+
+// Same product with both operands pre-packed in global memory as K-chunks of
+// 64 columns in the K-major core-matrix order (chunk c of a R-row operand at
+// element R * 64 * c), each chunk moved to shared memory by one bulk copy.
+__global__ void __launch_bounds__(128) tc_tile_bulk_kernel(const __nv_bfloat16* __restrict__ Ap,
+                                                            const __nv_bfloat16* __restrict__ Bp,
+                                                            float* __restrict__ D, int N, int K, int* status) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t full, done;
+  __shared__ uint32_t tbase;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  uint8_t* sA = smem;              // 128 x 64
+  uint8_t* sB = smem + 128 * 128;  // N x 64
+  if (warp == 0) {
+    tmem_alloc(&tbase, 256);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(&full, 1);
+    mbar_init(&done, 1);
+    mbar_fence_init();
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t d = tbase;
+  bool ok = true;
+  if (tid == 0) {
+    const uint32_t idesc = idesc_bf16(128, N);
+    const int nck = (K + 63) / 64;
+    for (int c = 0; c < nck && ok; ++c) {
+      const int w = min(64, K - 64 * c);
+      mbar_expect_tx(&full, (uint32_t)(128 + N) * w * 2);
+      bulk_g2s(sA, Ap + (int64_t)128 * 64 * c, 128 * w * 2, &full);
+      bulk_g2s(sB, Bp + (int64_t)N * 64 * c, N * w * 2, &full);
+      ok = mbar_wait_bounded(&full, c & 1, 1000000000ull);
+      if (!ok) break;
+      fence_after_sync();
+      for (int j = 0; j < w / 16; ++j) {
+        const uint64_t ad = smem_desc(smem_u32(sA) + j * 2 * 128 * 16, 128 * 16, 128);
+        const uint64_t bd = smem_desc(smem_u32(sB) + j * 2 * N * 16, N * 16, 128);
+        mma_bf16(d, ad, bd, idesc, (c > 0 || j > 0) ? 1u : 0u);
+      }
+      mma_commit(&done);
+      ok = mbar_wait_bounded(&done, c & 1, 1000000000ull);  // stage reused by the next chunk
+    }
+    if (!ok) atomicExch(status, 1);
+  }
+  ok = __syncthreads_and(ok) != 0;
+  fence_after_sync();
+  if (ok) {
+    const int row = warp * 32 + (tid & 31);
+    for (int c = 0; c < N; c += 16) {
+      float v[16];
+      tmem_ld16(d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) D[(int64_t)row * N + c + i] = v[i];
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tbase, 256);
+}
+
+cudaError_t launch_tc_tile_bulk(const __nv_bfloat16* Ap, const __nv_bfloat16* Bp, float* D, int N, int K,
+                                int* status, cudaStream_t s) {
+  if (N < 16 || N > 256 || N % 16 || K < 16 || K > 256 || K % 16) return cudaErrorInvalidValue;
+  const size_t smem = 200 * 1024;  // operands use (128 + N) * 128 bytes
+  cudaError_t e = cudaFuncSetAttribute(tc_tile_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tc_tile_bulk_kernel<<<1, 128, smem, s>>>(Ap, Bp, D, N, K, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_tile(const __nv_bfloat16* A, const __nv_bfloat16* B, float* D, int N, int K, int* status,
+                           cudaStream_t s) {
+  if (N < 16 || N > 256 || N % 16 || K < 16 || K > 64 || K % 16) return cudaErrorInvalidValue;
+  // the operands need (128 + N) * K * 2 bytes; the allocation is larger so
+  // that every address the descriptors can form stays inside it
+  const size_t smem = 200 * 1024;
+  cudaError_t e = cudaFuncSetAttribute(tc_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tc_tile_kernel<<<1, 128, smem, s>>>(A, B, D, N, K, status);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- sigma
+
+// p[i] for a small kernel-parameter array, by selects (dynamic indexing
+// would copy the parameter block to local memory)
+template <class T, int N>
+__device__ __forceinline__ T pick(const T (&p)[N], int i) {
+  T r = p[0];
+#pragma unroll
+  for (int k = 1; k < N; ++k)
+    if (i == k) r = p[k];
+  return r;
+}
+
+// Packs FP64 blocks into split bf16 operands.  Each thread writes one
+// 16-byte core-matrix row (8 consecutive K values of one operand row) of the
+// hi and lo pools; for transposed views consecutive threads take consecutive
+// rows so that the FP64 reads stay coalesced.
+__global__ void __launch_bounds__(256) tc_pack_kernel(TcBufs b, const TcPack* __restrict__ units) {
+  const TcPack u = units[blockIdx.x];
+  const double* src = pick(b.src, u.src) + u.src_off;
+  __nv_bfloat16* hi = pick(b.hi, u.pool) + u.dst_off;
+  __nv_bfloat16* lo = pick(b.lo, u.pool) + u.dst_off;
+  const int kg = u.kp >> 3;
+  const int64_t total = (int64_t)u.rows_p * kg;
+  for (int64_t g = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.y * blockDim.x) {
+    int r, k0;
+    if (u.trans) {
+      r = (int)(g % u.rows_p);
+      k0 = (int)(g / u.rows_p) * 8;
+    } else {
+      r = (int)(g / kg);
+      k0 = (int)(g % kg) * 8;
+    }
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int k = k0 + e;
+      double x = 0.0;
+      if (r < u.rows_v && k < u.cols_v) x = u.trans ? src[(int64_t)k * u.ld + r] : src[(int64_t)r * u.ld + k];
+      const __nv_bfloat16 xh = __double2bfloat16(x);
+      const __nv_bfloat16 xl = __double2bfloat16(x - (double)__bfloat162float(xh));
+      const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+      if (e & 1) {
+        hw[e >> 1] |= bh << 16;
+        lw[e >> 1] |= bl << 16;
+      } else {
+        hw[e >> 1] = bh;
+        lw[e >> 1] = bl;
+      }
+    }
+    const int t = r >> 7, c = k0 >> 6;
+    const int rest = u.rows_p - 128 * t;
+    const int h = rest < 128 ? rest : 128;
+    const int64_t off = tc_block_off(u.rows_p, u.kp, t, c) + (kmajor_off(r & 127, k0 & 63, h) >> 1);
+    *(uint4*)(hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *(uint4*)(lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
+cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cudaStream_t s) {
+  if (nunits > 0) tc_pack_kernel<<<dim3(nunits, 4), 256, 0, s>>>(b, units);
+  return cudaGetLastError();
+}
+
+namespace {
+
+constexpr int kTcStages = 3;
+constexpr uint32_t kTcOperandBytes = 128 * 64 * 2;  // one slice of one operand block
+constexpr uint32_t kTcStageBytes = 4 * kTcOperandBytes;
+constexpr int kTcThreads = 320;  // warps 0-7 epilogue, 8 bulk-copy producer, 9 MMA issuer
+constexpr int kTcSmem = kTcStages * kTcStageBytes;
+
+struct TcShared {
+  uint64_t full[kTcStages], empty[kTcStages], acc_full[2], acc_empty[2], drain;
+  uint32_t tbase;
+  int abort_flag;
+};
+
+// bounded wait that also gives up when another role gave up
+__device__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* status, uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort_flag) return false;
+    if (globaltimer_ns() - t0 > limit_ns) {
+      *abort_flag = 1;
+      atomicExch(status, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+// hi + lo += x, with the rounding error of the sum kept in lo (TwoSum)
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bp = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+}  // namespace
+
+// Grouped split-precision GEMM over packed operands on tcgen05: per K=16
+// step three MMAs (hi*hi + hi*lo + lo*hi) into an f32 TMEM accumulator
+// (two accumulators alternate between items), operand blocks streamed by
+// bulk copies through a 3-stage shared-memory ring.
+template <int PHASE>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_sigma_kernel(TcBufs b, const TcItem* __restrict__ items, const TcTask* __restrict__ tasks, uint64_t limit_ns) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ TcShared sh;
+  const TcTask T = tasks[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int h_a = min(128, T.a_rows - 128 * T.tm);
+  const int h_b = min(128, T.b_rows - 128 * T.tn);
+  const int N = (h_b + 15) & ~15;
+  if (warp == 9) {
+    tmem_alloc(&sh.tbase, 256);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kTcStages; ++i) {
+      mbar_init(&sh.full[i], 1);
+      mbar_init(&sh.empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&sh.acc_full[i], 1);
+      mbar_init(&sh.acc_empty[i], 8);
+    }
+    mbar_init(&sh.drain, 1);
+    sh.abort_flag = 0;
+    mbar_fence_init();
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = sh.tbase;
+  volatile int* abort_flag = &sh.abort_flag;
+
+  if (warp == 8) {
+    // ---- producer: one thread streams the operand blocks of every item
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      int last_par[kTcStages];
+      for (int i = 0; i < kTcStages; ++i) last_par[i] = -1;
+      bool ok = true;
+      for (int i = T.ibeg; i < T.iend && ok; ++i) {
+        const TcItem it = items[i];
+        const __nv_bfloat16* ah = pick(b.hi, it.a_pool) + it.a_off;
+        const __nv_bfloat16* al = pick(b.lo, it.a_pool) + it.a_off;
+        const __nv_bfloat16* bh = pick(b.hi, it.b_pool) + it.b_off;
+        const __nv_bfloat16* bl = pick(b.lo, it.b_pool) + it.b_off;
+        const int nck = (it.kp + 63) >> 6;
+        for (int c = 0; c < nck; ++c) {
+          if (!tc_wait(&sh.empty[s], ph ^ 1u, abort_flag, b.status, limit_ns)) {
+            ok = false;
+            break;
+          }
+          const int w = min(64, it.kp - 64 * c);
+          const int64_t ao = tc_block_off(T.a_rows, it.kp, T.tm, c);
+          const int64_t bo = tc_block_off(T.b_rows, it.kp, T.tn, c);
+          const uint32_t abytes = (uint32_t)h_a * w * 2, bbytes = (uint32_t)h_b * w * 2;
+          uint8_t* st = smem + s * kTcStageBytes;
+          mbar_expect_tx(&sh.full[s], 2 * (abytes + bbytes));
+          bulk_g2s(st, ah + ao, abytes, &sh.full[s]);
+          bulk_g2s(st + kTcOperandBytes, al + ao, abytes, &sh.full[s]);
+          bulk_g2s(st + 2 * kTcOperandBytes, bh + bo, bbytes, &sh.full[s]);
+          bulk_g2s(st + 3 * kTcOperandBytes, bl + bo, bbytes, &sh.full[s]);
+          last_par[s] = (int)ph;
+          if (++s == kTcStages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+      }
+      if (!ok) {
+        // copies already issued still land in shared memory: wait for them
+        for (int i = 0; i < kTcStages; ++i)
+          if (last_par[i] >= 0) mbar_wait_bounded(&sh.full[i], (uint32_t)last_par[i], limit_ns);
+      }
+    }
+  } else if (warp == 9) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(128, N);
+      int s = 0, ab = 0;
+      uint32_t ph = 0, aph = 0;
+      bool ok = true;
+      for (int i = T.ibeg; i < T.iend && ok; ++i) {
+        const int kp = items[i].kp;
+        if (!tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns)) break;
+        fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)ab * 128u;
+        const int nck = (kp + 63) >> 6;
+        for (int c = 0; c < nck; ++c) {
+          if (!tc_wait(&sh.full[s], ph, abort_flag, b.status, limit_ns)) {
+            ok = false;
+            break;
+          }
+          fence_after_sync();
+          const int w = min(64, kp - 64 * c);
+          const uint32_t sa = smem_u32(smem + s * kTcStageBytes);
+          for (int j = 0; j < w / 16; ++j) {
+            const uint32_t ao = (uint32_t)(32 * j * h_a), bo = (uint32_t)(32 * j * h_b);
+            const uint64_t a_hi = smem_desc(sa + ao, h_a * 16, 128);
+            const uint64_t a_lo = smem_desc(sa + kTcOperandBytes + ao, h_a * 16, 128);
+            const uint64_t b_hi = smem_desc(sa + 2 * kTcOperandBytes + bo, h_b * 16, 128);
+            const uint64_t b_lo = smem_desc(sa + 3 * kTcOperandBytes + bo, h_b * 16, 128);
+            mma_bf16(d, a_hi, b_hi, idesc, (c > 0 || j > 0) ? 1u : 0u);
+            mma_bf16(d, a_hi, b_lo, idesc, 1u);
+            mma_bf16(d, a_lo, b_hi, idesc, 1u);
+          }
+          mma_commit(&sh.empty[s]);
+          if (++s == kTcStages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (!ok) break;
+        mma_commit(&sh.acc_full[ab]);
+        ab ^= 1;
+        if (ab == 0) aph ^= 1u;
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue: warp w owns TMEM lanes 32 (w % 4).. and columns 64 (w / 4)..
+    const int q = warp & 3, half = warp >> 2;
+    const int row = 32 * q + lane;
+    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    if (PHASE == 2) {
+      float vh[64], vl[64];
+#pragma unroll
+      for (int e = 0; e < 64; ++e) vh[e] = vl[e] = 0.f;
+      int ab = 0;
+      uint32_t aph = 0;
+      for (int i = T.ibeg; i < T.iend; ++i) {
+        const float alpha = items[i].alpha;
+        const bool ok = tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns);
+        if (!__all_sync(0xffffffffu, ok)) break;  // TMEM loads below need the whole warp
+        fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)ab * 128u + (uint32_t)half * 64u + lane_base;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          if (half * 64 + g * 16 < N) {
+            float v[16];
+            tmem_ld16(d + (uint32_t)(g * 16), v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) two_sum_acc(vh[g * 16 + e], vl[g * 16 + e], __fmul_rn(alpha, v[e]));
+          }
+        }
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
+        ab ^= 1;
+        if (ab == 0) aph ^= 1u;
+      }
+      if (!*abort_flag && row < h_a) {
+        float2* out = b.partials + T.out_off + (int64_t)row * h_b;
+#pragma unroll
+        for (int e = 0; e < 64; ++e) {
+          const int col = half * 64 + e;
+          if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+        }
+      }
+    } else {
+      // phase 1: one item; S tile written as a packed operand (rows of this
+      // tile, K columns 128 tn.. of S)
+      const bool ok = T.iend > T.ibeg && tc_wait(&sh.acc_full[0], 0, abort_flag, b.status, limit_ns);
+      if (__all_sync(0xffffffffu, ok)) {
+        fence_after_sync();
+        const float alpha = items[T.ibeg].alpha;
+        const int ncols = min(128, T.out_kp - 128 * T.tn);
+        const uint32_t d = tmem + (uint32_t)half * 64u + lane_base;
+        __nv_bfloat16* shi = b.hi[kTcPoolS] + T.out_off;
+        __nv_bfloat16* slo = b.lo[kTcPoolS] + T.out_off;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const int c0 = half * 64 + g * 16;
+          if (c0 < ncols) {
+            float v[16];
+            if (c0 < N) {
+              tmem_ld16(d + (uint32_t)(g * 16), v);
+            } else {
+#pragma unroll
+              for (int e = 0; e < 16; ++e) v[e] = 0.f;
+            }
+            if (row < h_a) {
+#pragma unroll
+              for (int hv = 0; hv < 2; ++hv) {
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                  const int col = c0 + 8 * hv + e;
+                  const float x = col < h_b ? __fmul_rn(alpha, v[8 * hv + e]) : 0.f;
+                  __nv_bfloat16 xh, xl;
+                  split_bf16(x, xh, xl);
+                  const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+                  if (e & 1) {
+                    hw[e >> 1] |= bh << 16;
+                    lw[e >> 1] |= bl << 16;
+                  } else {
+                    hw[e >> 1] = bh;
+                    lw[e >> 1] = bl;
+                  }
+                }
+                const int C = 128 * T.tn + c0 + 8 * hv;  // S column
+                const int64_t off =
+                    tc_block_off(T.a_rows, T.out_kp, T.tm, C >> 6) + (kmajor_off(row, C & 63, h_a) >> 1);
+                *(uint4*)(shi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *(uint4*)(slo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+              }
+            }
+          }
+        }
+      }
+      fence_before_sync();
+    }
+  }
+  __syncthreads();
+  if (warp == 9) {
+    // every MMA of this block has completed before TMEM is released
+    if (lane == 0) {
+      mma_commit(&sh.drain);
+      mbar_wait_bounded(&sh.drain, 0, limit_ns);
+    }
+    __syncwarp();
+    fence_after_sync();
+    tmem_dealloc(tmem, 256);
+  }
+}
+
+cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, int ntasks,
+                            uint64_t limit_ns, cudaStream_t s) {
+  if (ntasks <= 0) return cudaGetLastError();
+  if (phase == 1) {
+    cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e != cudaSuccess) return e;
+    tc_sigma_kernel<1><<<ntasks, kTcThreads, kTcSmem, s>>>(b, items, tasks, limit_ns);
+  } else if (phase == 2) {
+    cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e != cudaSuccess) return e;
+    tc_sigma_kernel<2><<<ntasks, kTcThreads, kTcSmem, s>>>(b, items, tasks, limit_ns);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) tc_reduce_kernel(const float2* __restrict__ partials,
+                                                         const TcTile* __restrict__ tiles,
+                                                         const int64_t* __restrict__ slots, double* __restrict__ sigma) {
+  const TcTile t = tiles[blockIdx.x];
+  const int n = t.h * t.w;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    double acc = 0.0;
+    const int r = e / t.w, c = e % t.w;
+    for (int p = t.pbeg; p < t.pend; ++p) {
+      const float2 v = partials[slots[p] + (int64_t)r * t.pad + c];  // slots are h_a x h_b, row stride pad
+      acc += (double)v.x + (double)v.y;
+    }
+    sigma[t.s_off + (int64_t)(t.r0 + r) * t.lds + t.c0 + c] = acc;
+  }
+}
+
+cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
+                             cudaStream_t s) {
+  if (ntiles > 0) tc_reduce_kernel<<<ntiles, 256, 0, s>>>(b.partials, tiles, slots, sigma);
+  return cudaGetLastError();
+}
+
+}  // namespace dev
+}  // namespace bgpu

@@ -1,0 +1,94 @@
+// Tensor-core (tcgen05 / TMEM) kernels of the split-precision path.
+#pragma once
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace bgpu {
+namespace dev {
+
+// One 128 x N tile: D = A * B^T with A (128 x K) and B (N x K) row-major
+// bf16, D row-major f32; 16 <= N <= 256 and 16 <= K <= 64, both multiples of
+// 16.  status is set to 1 if the MMA completion wait ran out.
+cudaError_t launch_tc_tile(const __nv_bfloat16* A, const __nv_bfloat16* B, float* D, int N, int K, int* status,
+                           cudaStream_t s);
+
+// Same product from operands pre-packed as K-chunks of 64 columns in the
+// K-major core-matrix order (chunk c of an R-row operand starts at element
+// R * 64 * c), moved by bulk copies; 16 <= K <= 256, multiple of 16.
+cudaError_t launch_tc_tile_bulk(const __nv_bfloat16* Ap, const __nv_bfloat16* Bp, float* D, int N, int K,
+                                int* status, cudaStream_t s);
+
+// ---------------------------------------------------------------- sigma
+//
+// Packed operand: `rows` (multiple of 8) x `kp` (multiple of 16) bf16 values
+// (hi and lo slices in two pools with the same offsets), cut into row tiles
+// of 128 and K-chunks of 64; block (row tile t, chunk c) is contiguous, starts
+// at element tc_block_off(rows, kp, t, c) and holds its h x w values in the
+// K-major core-matrix order (byte (j/8)*h*16 + (i/8)*128 + (i%8)*16 + (j%8)*2).
+// Rows beyond the operand's own rows and columns beyond its own K are zero.
+__host__ __device__ inline int64_t tc_block_off(int rows, int kp, int t, int c) {
+  const int rest = rows - 128 * t;
+  const int h = rest < 128 ? rest : 128;
+  return (int64_t)128 * t * kp + (int64_t)h * 64 * c;
+}
+__host__ __device__ inline int tc_round8(int x) { return (x + 7) & ~7; }
+__host__ __device__ inline int tc_round16(int x) { return (x + 15) & ~15; }
+
+enum : int { kTcPoolL = 0, kTcPoolR = 1, kTcPoolPsi = 2, kTcPoolPsiT = 3, kTcPoolS = 4, kTcPools = 5 };
+
+// One packed operand filled from an FP64 block: view element (r, k) is
+// src[src_off + (trans ? k * ld + r : r * ld + k)] for r < rows_v, k < cols_v.
+struct TcPack {
+  int64_t src_off, dst_off;
+  int32_t ld, rows_v, cols_v, rows_p, kp;
+  uint8_t src, pool, trans, pad;
+};
+
+// out (+)= alpha * A * B^T over K = kp, A and B packed operands
+struct TcItem {
+  int64_t a_off, b_off;
+  int32_t kp;
+  uint8_t a_pool, b_pool;
+  uint16_t pad;
+  float alpha;
+};
+
+// One thread block: output tile (tm, tn) -- rows 128 tm.. of the A operands,
+// rows 128 tn.. of the B operands -- and the items [ibeg, iend).
+//   phase 1 (one item): writes alpha * A B^T as the packed S operand at
+//     out_off of pool S (rows a_rows, K out_kp);
+//   phase 2: sum of the items, compensated (hi, lo) f32 pairs for the
+//     h_a x h_b valid part of the tile, written at partials + out_off.
+struct TcTask {
+  int32_t a_rows, b_rows;
+  int32_t tm, tn;
+  int32_t ibeg, iend;
+  int64_t out_off;
+  int32_t out_kp, pad;
+};
+
+// sigma tile (rows r0.., cols c0.., h x w) = sum of the partial slots
+// slots[pbeg..pend) (each with row stride pad, the tile's padded width)
+struct TcTile {
+  int64_t s_off;
+  int32_t lds, h, w, r0, c0, pbeg, pend, pad;
+};
+
+struct TcBufs {
+  const double* src[3];  // FP64 sources of packing: L arena, R arena, psi
+  __nv_bfloat16* hi[kTcPools];
+  __nv_bfloat16* lo[kTcPools];
+  float2* partials;
+  int* status;  // set to 1 when a pipeline wait ran out
+};
+
+cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cudaStream_t s);
+// phase 1 or 2; limit_ns bounds every pipeline wait
+cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, int ntasks,
+                            uint64_t limit_ns, cudaStream_t s);
+cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
+                             cudaStream_t s);
+
+}  // namespace dev
+}  // namespace bgpu

@@ -238,6 +238,27 @@ cudaError_t launch_combine(const double* X, int k, int64_t n, int64_t ld, const 
   return cudaGetLastError();
 }
 
+__global__ void project_out_kernel(const double* __restrict__ X, int k, int64_t n, int64_t ld,
+                                   const double* __restrict__ coef, double* __restrict__ r) {
+  __shared__ double c[kMaxGram];
+  if (threadIdx.x < kMaxGram) c[threadIdx.x] = threadIdx.x < k ? coef[threadIdx.x] : 0.0;
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    double s = 0.0;
+    for (int i = 0; i < k; ++i) s = fma(c[i], X[(int64_t)i * ld + t], s);
+    r[t] -= s;
+  }
+}
+
+cudaError_t launch_project_out(const double* X, int k, int64_t n, int64_t ld, const double* coef, double* r,
+                               cudaStream_t s) {
+  if (k > kMaxGram) return cudaErrorInvalidValue;
+  if (k <= 0 || n <= 0) return cudaSuccess;
+  project_out_kernel<<<kGramBlocks * 2, 256, 0, s>>>(X, k, n, ld, coef, r);
+  return cudaGetLastError();
+}
+
 __global__ void axpy_kernel(double a, const double* __restrict__ x, double* __restrict__ y, int64_t n) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) y[t] = fma(a, x[t], y[t]);
@@ -463,7 +484,8 @@ __global__ void gather_cols_kernel(const double* __restrict__ V, double* __restr
   const int64_t total = (int64_t)u.n * u.m;
   for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
     const int r = (int)(e / u.m), c = (int)(e % u.m);
-    U[u.u_off + e] = V[u.v_off + (int64_t)r * u.n + cols[u.c_off + c]];
+    const int64_t col = cols[u.c_off + c];
+    U[u.u_off + e] = u.colmajor ? V[u.v_off + col * u.n + r] : V[u.v_off + (int64_t)r * u.n + col];
   }
 }
 

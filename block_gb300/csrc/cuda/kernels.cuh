@@ -94,6 +94,10 @@ cudaError_t launch_gram(const double* X, int nx, const double* Y, int ny, int64_
 // out_row r = sum_i coef[i*k + r] * X_i, for r < k   (basis rotation)
 cudaError_t launch_combine(const double* X, int k, int64_t n, int64_t ld, const double* coef, int kout, double* Y,
                            int64_t ldy, cudaStream_t s);
+// r -= sum_i coef[i] * X_i for the k rows X_i (stride ld); coef is device
+// memory (for instance the output of launch_gram), so no host round trip
+cudaError_t launch_project_out(const double* X, int k, int64_t n, int64_t ld, const double* coef, double* r,
+                               cudaStream_t s);
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s);
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t s);
 // r_i /= (e - d_i) where |e - d_i| > 1e-12
@@ -109,10 +113,12 @@ cudaError_t launch_jacobi(double* A, const int64_t* a_off, const int* dims, doub
                           const int64_t* v_off, int* status, int nmat, int max_n, cudaStream_t s);
 
 // U columns gathered from eigenvector matrices: for each (sector) entry,
-// U[u_off + r*m + c] = V[v_off + r*n + col[c_off + c]]
+// U[u_off + r*m + c] = V[v_off + r*n + col[c_off + c]] (eigenvectors as
+// columns of a row-major matrix), or V[v_off + col[c_off + c]*n + r] when
+// colmajor is set
 struct GatherUnit {
   int64_t u_off, v_off;
-  int32_t n, m, c_off, pad;
+  int32_t n, m, c_off, colmajor;
 };
 cudaError_t launch_gather_cols(const double* V, double* U, const GatherUnit* units, const int* cols, int nunits,
                                cudaStream_t s);

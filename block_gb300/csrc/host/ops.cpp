@@ -62,6 +62,10 @@ Quantum op_dq(const OpKey& k, const std::vector<int>& orbsym) {
 OpLayout make_layout(const StateInfo& si, const Quantum& dq, const PointGroup& g) {
   OpLayout L;
   L.dq = dq;
+  L.nq = si.size();
+  L.index.assign((size_t)L.nq * L.nq, -1);
+  L.by_ket.assign(L.nq, {});
+  L.by_bra.assign(L.nq, {});
   for (int b = 0; b < si.size(); ++b)
     for (int k = 0; k < si.size(); ++k) {
       if (!quantum_allowed(si.quanta[b], si.quanta[k], dq, g)) continue;
@@ -71,7 +75,9 @@ OpLayout make_layout(const StateInfo& si, const Quantum& dq, const PointGroup& g
       blk.rows = si.states[b];
       blk.cols = si.states[k];
       blk.offset = L.size;
-      L.index[{b, k}] = (int)L.blocks.size();
+      L.index[(size_t)b * L.nq + k] = (int)L.blocks.size();
+      L.by_ket[k].push_back((int)L.blocks.size());
+      L.by_bra[b].push_back((int)L.blocks.size());
       L.blocks.push_back(blk);
       L.size += (int64_t)blk.rows * blk.cols;
     }

@@ -80,12 +80,12 @@ struct OpBlock {
 struct OpLayout {
   Quantum dq;
   std::vector<OpBlock> blocks;
-  std::map<std::pair<int, int>, int> index;  // (bra, ket) -> block
+  int nq = 0;               // quanta of the block's state space
+  std::vector<int> index;   // bra * nq + ket -> block, -1 if not allowed
+  std::vector<std::vector<int>> by_ket;  // ket -> blocks with that ket
+  std::vector<std::vector<int>> by_bra;  // bra -> blocks with that bra
   int64_t size = 0;
-  int find(int bra, int ket) const {
-    auto it = index.find({bra, ket});
-    return it == index.end() ? -1 : it->second;
-  }
+  int find(int bra, int ket) const { return index[(size_t)bra * nq + ket]; }
 };
 
 OpLayout make_layout(const StateInfo& si, const Quantum& dq, const PointGroup& g);

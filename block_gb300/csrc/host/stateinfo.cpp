@@ -54,6 +54,9 @@ StateInfo product_stateinfo(const StateInfo& a, const StateInfo& b, const PointG
   out.quanta = qs;
   out.states.assign(qs.size(), 0);
   out.parts.assign(qs.size(), {});
+  out.nleft = a.size();
+  out.nright = b.size();
+  out.part_index.assign((size_t)out.nleft * out.nright, {});
   for (auto& u : unc) {
     int c = out.find(u.q);
     SectorPart p;
@@ -61,7 +64,7 @@ StateInfo product_stateinfo(const StateInfo& a, const StateInfo& b, const PointG
     p.rq = u.rq;
     p.offset = out.states[c];
     p.size = u.size;
-    out.part_of[{u.lq, u.rq}] = {c, (int)out.parts[c].size()};
+    out.part_index[(size_t)u.lq * out.nright + u.rq].push_back({c, (int)out.parts[c].size()});
     out.parts[c].push_back(p);
     out.states[c] += u.size;
   }

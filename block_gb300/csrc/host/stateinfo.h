@@ -28,8 +28,13 @@ struct StateInfo {
   std::vector<int> states;      // number of multiplets per quantum
   // product blocks only: composition of every sector
   std::vector<std::vector<SectorPart>> parts;
-  // (lq, rq) -> (sector, part index) for product blocks
-  std::map<std::pair<int, int>, std::pair<int, int>> part_of;
+  // (lq, rq) -> every (sector, part index) it forms (one per coupled total
+  // spin that is kept), dense over left x right quanta
+  int nleft = 0, nright = 0;
+  std::vector<std::vector<std::pair<int, int>>> part_index;
+  const std::vector<std::pair<int, int>>& parts_of(int lq, int rq) const {
+    return part_index[(size_t)lq * nright + rq];
+  }
 
   int size() const { return (int)quanta.size(); }
   long total_states() const;

@@ -2,7 +2,6 @@
 
 #include <cmath>
 #include <cstdlib>
-#include <mutex>
 #include <stdexcept>
 #include <unordered_map>
 
@@ -133,33 +132,19 @@ double ninej_norm(int a, int b, int c, int d, int e, int f, int g, int h, int i)
   return std::pow((g + 1) * (h + 1) * (c + 1) * (f + 1), 0.5) * nine_j(a, b, c, d, e, f, g, h, i);
 }
 
-namespace {
-struct NinejCache {
-  std::mutex mu;
-  std::unordered_map<uint64_t, double> map;
-};
-NinejCache& cache() {
-  static NinejCache c;
-  return c;
-}
-}  // namespace
-
 double ninej(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
-  // all arguments are small non-negative 2j values; pack 7 bits each
+  // all arguments are small non-negative 2j values; pack 7 bits each.  Each
+  // thread keeps its own memo table (no locking on the hot host loops).
   auto ok = [](int x) { return x >= 0 && x < 128; };
   if (!(ok(a) && ok(b) && ok(c) && ok(d) && ok(e) && ok(f) && ok(g) && ok(h) && ok(i)))
     return ninej_norm(a, b, c, d, e, f, g, h, i);
   uint64_t key = 0;
   for (int x : {a, b, c, d, e, f, g, h, i}) key = (key << 7) | (uint64_t)x;
-  auto& C = cache();
-  {
-    std::lock_guard<std::mutex> lk(C.mu);
-    auto it = C.map.find(key);
-    if (it != C.map.end()) return it->second;
-  }
+  thread_local std::unordered_map<uint64_t, double> memo;
+  auto it = memo.find(key);
+  if (it != memo.end()) return it->second;
   const double v = ninej_norm(a, b, c, d, e, f, g, h, i);
-  std::lock_guard<std::mutex> lk(C.mu);
-  C.map.emplace(key, v);
+  memo.emplace(key, v);
   return v;
 }
 

@@ -343,9 +343,14 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
     keepspec = renorm_spec(Rs, p, !loop_is_left(p - 1));
     merge(specR, keepspec);
   }
+  using clk = std::chrono::steady_clock;
+  auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+  auto t0 = clk::now();
   Block L = make_enlarged(left_block(p - 1), p, true, specL);
   Block R = make_enlarged(right_block(p + 2), p + 1, false, specR);
   Superblock sb = make_superblock(L, R);
+  phase_.build_seconds += secs(t0);
+  t0 = clk::now();
   DavidsonParams dp;
   dp.nroots = C_.nroots;
   dp.tol = se.davidson_tol;
@@ -353,13 +358,17 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   dp.deflation_max = C_.deflation_max;
   dp.seed = C_.seed + 104729ull * (uint64_t)(sweep_index * N_ + p);
   const int iters = E_.solve(sb, dp, energies);
+  phase_.solve_seconds += secs(t0);
   if (opt_.on_step) opt_.on_step(sb, sweep_index, p);
+  t0 = clk::now();
   DensitySpectrum spec;
   E_.density(sb, forward, C_.weights, spec);
   std::vector<std::vector<int>> kept_idx;
   std::vector<int> kept;
   const double disc = choose_kept(spec, se.M, kept_idx, kept);
   E_.select_rotation(kept_idx);
+  phase_.density_seconds += secs(t0);
+  t0 = clk::now();
   if (forward) {
     if (left_[p]) E_.release_block(*left_[p]);
     left_[p] = renormalised(L, kept, keepspec);
@@ -367,6 +376,7 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
     if (right_[p + 1]) E_.release_block(*right_[p + 1]);
     right_[p + 1] = renormalised(R, kept, keepspec);
   }
+  phase_.renorm_seconds += secs(t0);
   log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f  disc=%.3e\n", forward ? "fwd" : "bwd", p,
       L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], disc);
   E_.release_block(L);
@@ -405,13 +415,18 @@ SweepResult SweepDriver::run() {
     const double e = sweep(forward, s);
     res.sweep_energies.push_back(e);
     res.sweeps = s + 1;
-    log(1, "sweep %d (%s) M=%d  E=%.12f  dE=%.3e  maxdisc=%.3e\n", s, forward ? "fwd" : "bwd", C_.entry(s).M, e,
-        e - eprev, last_discarded_);
+    log(1, "sweep %d (%s) M=%d  E=%.12f  dE=%.3e  maxdisc=%.3e  [build %.2fs solve %.2fs density %.2fs renorm %.2fs]\n",
+        s, forward ? "fwd" : "bwd", C_.entry(s).M, e, e - eprev, last_discarded_, phase_.build_seconds,
+        phase_.solve_seconds, phase_.density_seconds, phase_.renorm_seconds);
     if (s >= last_sched && std::fabs(e - eprev) <= C_.sweep_tol) break;
     eprev = e;
   }
   res.energies = last_energies_;
   res.discarded = last_discarded_;
+  res.build_seconds = phase_.build_seconds;
+  res.solve_seconds = phase_.solve_seconds;
+  res.density_seconds = phase_.density_seconds;
+  res.renorm_seconds = phase_.renorm_seconds;
   return res;
 }
 

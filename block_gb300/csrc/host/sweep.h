@@ -91,6 +91,10 @@ struct SweepResult {
   int sweeps = 0;
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
+  // wall seconds per phase of the block steps: enlarged-block builds and
+  // superblock set-up, Davidson solve, density matrix + rotation choice,
+  // renormalisation
+  double build_seconds = 0.0, solve_seconds = 0.0, density_seconds = 0.0, renorm_seconds = 0.0;
 };
 
 struct DriverOptions {
@@ -148,6 +152,7 @@ class SweepDriver {
   int cur_M_ = 0;
   std::vector<double> last_energies_;
   double last_discarded_ = 0.0;
+  SweepResult phase_;  // accumulates the per-phase wall times
 };
 
 }  // namespace bgpu

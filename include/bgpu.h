@@ -50,13 +50,16 @@ extern "C" {
 
 /* arithmetic of the sigma product: FP64, or bf16 slices on the tensor cores
  * with FP32 accumulation -- 2 slices / 3 products per logical product
- * (BF16X3) or 3 slices / 6 products (BF16X6).  With a split precision,
+ * (BF16X3) or 3 slices / 6 products (BF16X6) with warp-level MMAs, or
+ * 2 slices / 3 products on tcgen05 with TMEM accumulators and bulk-copy
+ * staged operands (BF16X3_TC).  With a split precision,
  * bgpu_davidson and bgpu_run_dmrg iterate with split-precision sigma and
  * refine every converged root's energy with one FP64 sigma (Rayleigh
  * quotient against the FP64 Hamiltonian). */
 #define BGPU_PREC_FP64 0
 #define BGPU_PREC_BF16X3 1
 #define BGPU_PREC_BF16X6 2
+#define BGPU_PREC_BF16X3_TC 3
 
 typedef struct bgpu_ctx bgpu_ctx;
 
@@ -182,6 +185,15 @@ int bgpu_synchronize(bgpu_ctx* ctx);
  * between. */
 int bgpu_profiler_start(bgpu_ctx* ctx);
 int bgpu_profiler_stop(bgpu_ctx* ctx);
+/* Tensor-core self-check (no reference counterpart): one 128 x n tile
+ * d = a * b^T on tcgen05 with a TMEM accumulator, d row-major f32.  With
+ * packed = 0, a (128 x k) and b (n x k) are row-major bf16 bit patterns
+ * (16 <= k <= 64); with packed = 1 they are K-chunks of 64 columns in the
+ * K-major core-matrix order (chunk c of an r-row operand at element
+ * r * 64 * c; element (i, j) of a chunk at byte (j/8)*r*16 + (i/8)*128 +
+ * (i%8)*16 + (j%8)*2), moved by bulk copies (16 <= k <= 256).
+ * 16 <= n <= 256; n and k multiples of 16. */
+int bgpu_tc_tile(bgpu_ctx* ctx, const uint16_t* a, const uint16_t* b, float* d, int n, int k, int packed);
 
 /*
  * Superblock of the bipartition after orbital `partition` (left block
@@ -199,9 +211,11 @@ int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition,
  * `block.spin_adapted dmrg.conf` entry, main.C:25-52 / dmrg.C:600-706), with
  * all operator and wavefunction arithmetic on the GPU.  `orbitals` may also
  * name a generated Hamiltonian: synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>.
- * energies[max_roots] receive the final energies; stats[8] (may be NULL):
+ * energies[max_roots] receive the final energies; stats[12] (may be NULL):
  *   sweeps, sigma calls, sigma seconds, sigma flops, total seconds, max
- *   discarded weight, last-sweep energy, number of roots.
+ *   discarded weight, last-sweep energy, number of roots, then wall seconds
+ *   of the block-build, Davidson, density/rotation and renormalisation
+ *   phases.
  */
 int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
                   double* stats);

@@ -18,7 +18,7 @@ from test_gpu_sigma import SNAPS, load
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"bf16x3": 1e-4, "bf16x6": 5e-6}
+TOL = {"bf16x3": 1e-4, "bf16x6": 5e-6, "bf16x3tc": 1e-4}
 
 with open(os.path.join(GOLDEN, "golden.json")) as f:
     GOLD = json.load(f)
@@ -30,7 +30,7 @@ def split_ctx(gpu_ctx):
     gpu_ctx.set_precision("fp64")
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "bf16x6"])
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16x6", "bf16x3tc"])
 @pytest.mark.parametrize("name,sweep,pos", SNAPS)
 def test_split_sigma_accuracy(split_ctx, oracle, prec, name, sweep, pos):
     snap = oracle.snapshot(conf(name), sweep, pos)
@@ -46,19 +46,21 @@ def test_split_sigma_accuracy(split_ctx, oracle, prec, name, sweep, pos):
     assert err <= TOL[prec], (prec, name, err)
 
 
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x3tc"])
 @pytest.mark.parametrize("name,sweep,pos", SNAPS[:3])
-def test_split_davidson_refined_energy(split_ctx, oracle, name, sweep, pos):
+def test_split_davidson_refined_energy(split_ctx, oracle, prec, name, sweep, pos):
     snap = oracle.snapshot(conf(name), sweep, pos)
     sb, n = load(split_ctx, snap)
     e64, _, _ = split_ctx.davidson(sb, n, nroots=1, tol=1e-12)
-    split_ctx.set_precision("bf16x6")
+    split_ctx.set_precision(prec)
     e, _, _ = split_ctx.davidson(sb, n, nroots=1, tol=1e-9)
     assert abs(e[0] - e64[0]) <= 1e-8, (e[0], e64[0])
 
 
+@pytest.mark.parametrize("prec", ["bf16x6", "bf16x3tc"])
 @pytest.mark.parametrize("name", ["hubbard", "c2_d2h"])
-def test_split_sweep_golden(split_ctx, name):
-    split_ctx.set_precision("bf16x6")
+def test_split_sweep_golden(split_ctx, prec, name):
+    split_ctx.set_precision(prec)
     e, st = split_ctx.run_dmrg(conf(name))
     for got, ref in zip(e, GOLD[name]["energies"]):
         assert abs(got - ref) <= GOLD[name]["tolerance"], (name, got, ref)
