@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "bf16x6"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc"])
     ap.add_argument("--no-davidson", action="store_true", help="skip the FP64-vs-split Davidson comparison")
     ap.add_argument("--conf", default=DEFAULT_CONF)
     ap.add_argument("--partition", type=int, default=11)
@@ -250,9 +250,11 @@ def run_ours(a):
                 "algorithmic_bytes_per_step": nbytes}
     else:
         pk = peaks.get("bf16_tflops", 1900.0)
-        prods = 3 if a.precision == "bf16x3" else 6
+        prods = 6 if a.precision == "bf16x6" else 3
+        kname = ("tc_sigma_kernel<1>+<2> (tcgen05/TMEM two-phase sector GEMMs, bf16 slices)"
+                 if a.precision == "bf16x3tc" else "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)")
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
-                "traffic": None, "kernel": "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)",
+                "traffic": None, "kernel": kname,
                 "peak_source": ("bf16_tflops of measured" if peaks else "fallback 1900"),
                 "products_per_logical_product": prods,
                 "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
