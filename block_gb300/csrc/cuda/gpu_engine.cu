@@ -10,6 +10,7 @@
 
 #include "../host/dense.h"
 
+#include <queue>
 #include <set>
 #include <unordered_map>
 
@@ -130,6 +131,11 @@ void GpuEngine::download_block(const Block& b, std::vector<double>& a) {
 
 double* GpuEngine::arena(const Block& b) const { return blocks_.at(b.handle).d; }
 
+int GpuEngine::sm_count() {
+  if (sm_count_ <= 0) cuda_check(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "sm count");
+  return sm_count_;
+}
+
 // ------------------------------------------------------------------ views
 
 namespace {
@@ -230,6 +236,34 @@ std::vector<std::vector<std::pair<int, int>>> sectors_by_left(const Superblock& 
   std::vector<std::vector<std::pair<int, int>>> by_l(sb.L->si.size());
   for (int s = 0; s < (int)sb.sectors.size(); ++s) by_l[sb.sectors[s].lq].push_back({sb.sectors[s].rq, s});
   return by_l;
+}
+
+// Longest-processing-time assignment of tasks to `nblocks` persistent
+// blocks; block j runs order[ranges[j].x .. ranges[j].y), in task order.
+void schedule_lpt(const std::vector<double>& cost, int nblocks, std::vector<int>& order, std::vector<int2>& ranges) {
+  const int n = (int)cost.size();
+  nblocks = std::max(1, std::min(nblocks, n));
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<std::vector<int>> per(nblocks);
+  std::priority_queue<std::pair<double, int>, std::vector<std::pair<double, int>>, std::greater<>> load;
+  for (int j = 0; j < nblocks; ++j) load.push({0.0, j});
+  for (int i : idx) {
+    auto [l, j] = load.top();
+    load.pop();
+    per[j].push_back(i);
+    load.push({l + cost[i], j});
+  }
+  order.clear();
+  ranges.clear();
+  if (n == 0) return;
+  for (auto& v : per) {
+    std::sort(v.begin(), v.end());
+    const int b = (int)order.size();
+    order.insert(order.end(), v.begin(), v.end());
+    ranges.push_back(make_int2(b, (int)order.size()));
+  }
 }
 
 void add_tasks(std::vector<dev::GemmTask>& t, int unit, int m, int n) {
@@ -551,6 +585,10 @@ void GpuEngine::free_plan(SigmaPlan& p) {
   p.tc_i2.release(stream_);
   p.tc_t1.release(stream_);
   p.tc_t2.release(stream_);
+  p.tc_o1.release(stream_);
+  p.tc_o2.release(stream_);
+  p.tc_r1.release(stream_);
+  p.tc_r2.release(stream_);
   p.tc_tiles.release(stream_);
   p.tc_slots.release(stream_);
   if (p.tc_partials) cudaFreeAsync(p.tc_partials, stream_);
@@ -879,23 +917,26 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       per_sector[c.vs].push_back(it);
     }
   }
-  // phase 2: sector tiles, items split into tasks of similar cost
+  // phase 2: sector tiles; a tile whose items cost more than a block's fair
+  // share is split into several tasks summed by the reduce kernel, every
+  // other tile is one task writing its FP64 result directly
+  const int nsm = sm_count();
+  auto item_cost = [](const TcItem& it, int hb) { return 400.0 + (double)it.kp * tc_round16(hb) / 8.0; };
   std::vector<TcItem> i2;
   std::vector<TcTask> t2;
+  std::vector<double> c2;
   std::vector<TcTile> tiles;
   std::vector<int64_t> slots;
   int64_t partial_n = 0;
   double total = 0.0;
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
-    for (const TcItem& it : per_sector[s]) total += (it.kp + 64.0) * ((S.rows + 127) / 128) * ((S.cols + 127) / 128);
+    for (int tn = 0; tn < (S.cols + 127) / 128; ++tn) {
+      const int hb = std::min(128, tc_round8(S.cols) - 128 * tn);
+      for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
+    }
   }
-  const double chunk = std::max(total / (152.0 * 4.0), 4096.0);
-  struct Pending {
-    TcTask t;
-    double cost;
-  };
-  std::vector<Pending> pend;
+  const double chunk = std::max(total / (2.0 * nsm), 20000.0);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     const int ib = (int)i2.size();
@@ -905,38 +946,58 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     for (int tm = 0; tm < (S.rows + 127) / 128; ++tm)
       for (int tn = 0; tn < (S.cols + 127) / 128; ++tn) {
         const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(128, cols_p - 128 * tn);
+        double tile_cost = 0.0;
+        for (int x = ib; x < ie; ++x) tile_cost += item_cost(i2[x], hb);
+        TcTask t{};
+        t.a_rows = rows_p;
+        t.b_rows = cols_p;
+        t.tm = tm;
+        t.tn = tn;
+        t.valid_rows = std::min(128, S.rows - 128 * tm);
+        t.valid_cols = std::min(128, S.cols - 128 * tn);
+        for (int x = ib; x < ie; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
+        if (tile_cost <= chunk || ie - ib <= 1) {
+          t.ibeg = ib;
+          t.iend = ie;
+          t.direct = 1;
+          t.out_off = S.offset;
+          t.out_kp = S.cols;
+          t2.push_back(t);
+          c2.push_back(tile_cost);
+          continue;
+        }
         TcTile tl{};
         tl.s_off = S.offset;
         tl.lds = S.cols;
-        tl.h = std::min(128, S.rows - 128 * tm);
-        tl.w = std::min(128, S.cols - 128 * tn);
+        tl.h = t.valid_rows;
+        tl.w = t.valid_cols;
         tl.r0 = 128 * tm;
         tl.c0 = 128 * tn;
         tl.pad = hb;  // row stride of the partial slots
         tl.pbeg = (int)slots.size();
-        int a = ib;
-        while (a < ie) {
+        int x0 = ib;
+        while (x0 < ie) {
           double acc = 0.0;
-          int e = a;
-          while (e < ie && (acc < chunk || e == a)) acc += i2[e++].kp + 64.0;
-          TcTask t{};
-          t.a_rows = rows_p;
-          t.b_rows = cols_p;
-          t.tm = tm;
-          t.tn = tn;
-          t.ibeg = a;
-          t.iend = e;
-          t.out_off = partial_n;
+          int x1 = x0;
+          while (x1 < ie && (acc < chunk || x1 == x0)) acc += item_cost(i2[x1++], hb);
+          TcTask u = t;
+          u.ibeg = x0;
+          u.iend = x1;
+          u.direct = 0;
+          u.out_off = partial_n;
           slots.push_back(partial_n);
           partial_n += (int64_t)ha * hb;
-          pend.push_back({t, acc});
-          for (int x = a; x < e; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
-          a = e;
+          t2.push_back(u);
+          c2.push_back(acc);
+          x0 = x1;
         }
         tl.pend = (int)slots.size();
         tiles.push_back(tl);
       }
   }
+  std::vector<double> c1;
+  for (const TcTask& t : t1)
+    c1.push_back(item_cost(i1[t.ibeg], std::min(128, t.b_rows - 128 * t.tn)) + 200.0);
   auto check = [&](const TcTask& t, const std::vector<TcItem>& items) {
     for (int x = t.ibeg; x < t.iend; ++x) {
       const TcItem& it = items[x];
@@ -955,9 +1016,16 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         128 * t.tn >= t.out_kp)
       throw std::runtime_error("tensor-core plan: stage-1 output does not match its tile");
   }
-  for (const Pending& p : pend) check(p.t, i2);
-  std::stable_sort(pend.begin(), pend.end(), [](const Pending& x, const Pending& y) { return x.cost > y.cost; });
-  for (auto& p : pend) t2.push_back(p.t);
+  for (const TcTask& t : t2) {
+    check(t, i2);
+    if (t.direct && (t.valid_rows > std::min(128, t.a_rows - 128 * t.tm) ||
+                     t.valid_cols > std::min(128, t.b_rows - 128 * t.tn)))
+      throw std::runtime_error("tensor-core plan: output tile larger than its operands");
+  }
+  std::vector<int> o1, o2;
+  std::vector<int2> r1, r2;
+  schedule_lpt(c1, nsm, o1, r1);
+  schedule_lpt(c2, nsm, o2, r2);
   // buffers
   for (int i = 0; i < kTcPools; ++i) {
     plan.tc_pool_elems[i] = pool_n[i];
@@ -973,6 +1041,10 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   plan.tc_t1.upload(t1, stream_);
   plan.tc_i2.upload(i2, stream_);
   plan.tc_t2.upload(t2, stream_);
+  plan.tc_o1.upload(o1, stream_);
+  plan.tc_o2.upload(o2, stream_);
+  plan.tc_r1.upload(r1, stream_);
+  plan.tc_r2.upload(r2, stream_);
   plan.tc_tiles.upload(tiles, stream_);
   plan.tc_slots.upload(slots, stream_);
   plan.tc_mma_flops = mma;
@@ -1007,8 +1079,12 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   constexpr uint64_t kWaitLimitNs = 1000000000ull;
   cuda_check(dev::launch_tc_pack(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tc pack psi");
   if (marks) cuda_check(cudaEventRecord(marks[0], stream_), "record");
-  cuda_check(dev::launch_tc_sigma(1, b, p.tc_i1.d, p.tc_t1.d, (int)p.tc_t1.n, kWaitLimitNs, stream_), "tc phase 1");
-  cuda_check(dev::launch_tc_sigma(2, b, p.tc_i2.d, p.tc_t2.d, (int)p.tc_t2.n, kWaitLimitNs, stream_), "tc phase 2");
+  cuda_check(dev::launch_tc_sigma(1, b, p.tc_i1.d, p.tc_t1.d, p.tc_o1.d, p.tc_r1.d, (int)p.tc_r1.n, out,
+                                  kWaitLimitNs, stream_),
+             "tc phase 1");
+  cuda_check(dev::launch_tc_sigma(2, b, p.tc_i2.d, p.tc_t2.d, p.tc_o2.d, p.tc_r2.d, (int)p.tc_r2.n, out,
+                                  kWaitLimitNs, stream_),
+             "tc phase 2");
   if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");
   cuda_check(dev::launch_tc_reduce(b, p.tc_tiles.d, p.tc_slots.d, (int)p.tc_tiles.n, out, stream_), "tc reduce");
   if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");

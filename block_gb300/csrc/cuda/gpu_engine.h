@@ -73,6 +73,8 @@ struct SigmaPlan {
   DevArray<dev::TcPack> tc_psi_pack;
   DevArray<dev::TcItem> tc_i1, tc_i2;
   DevArray<dev::TcTask> tc_t1, tc_t2;
+  DevArray<int> tc_o1, tc_o2;    // task order per persistent block
+  DevArray<int2> tc_r1, tc_r2;   // per block: range in the order
   DevArray<dev::TcTile> tc_tiles;
   DevArray<int64_t> tc_slots;
   float2* tc_partials = nullptr;
@@ -117,6 +119,7 @@ class GpuEngine : public Engine {
                    float* ms);
   int sigma_launches(const SigmaPlan& plan) const;
   double* arena(const Block& b) const;
+  int sm_count();
   cudaStream_t stream() const { return stream_; }
   double* alloc(int64_t elems);
   void free(double* p);
@@ -171,6 +174,7 @@ class GpuEngine : public Engine {
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   // pipeline-wait status of the tensor-core kernels (device flag, pinned copy)
   int* tc_status_ = nullptr;
+  int sm_count_ = 0;
   int* tc_status_host_ = nullptr;
 };
 

@@ -254,19 +254,20 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }  // namespace
 
 // Grouped split-precision GEMM over packed operands on tcgen05: per K=16
-// step three MMAs (hi*hi + hi*lo + lo*hi) into an f32 TMEM accumulator
-// (two accumulators alternate between items), operand blocks streamed by
-// bulk copies through a 3-stage shared-memory ring.
+// step three MMAs (hi*hi + hi*lo + lo*hi) into an f32 TMEM accumulator (two
+// accumulators alternate between items), operand blocks streamed by bulk
+// copies through a 3-stage shared-memory ring.  Persistent: block j walks
+// the tasks order[ranges[j].x .. ranges[j].y) and the pipeline runs across
+// task boundaries.
 template <int PHASE>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    tc_sigma_kernel(TcBufs b, const TcItem* __restrict__ items, const TcTask* __restrict__ tasks, uint64_t limit_ns) {
+    tc_sigma_kernel(TcBufs b, const TcItem* __restrict__ items, const TcTask* __restrict__ tasks,
+                    const int* __restrict__ order, const int2* __restrict__ ranges, double* __restrict__ sigma,
+                    uint64_t limit_ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ TcShared sh;
-  const TcTask T = tasks[blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int h_a = min(128, T.a_rows - 128 * T.tm);
-  const int h_b = min(128, T.b_rows - 128 * T.tn);
-  const int N = (h_b + 15) & ~15;
+  const int2 rg = ranges[blockIdx.x];
   if (warp == 9) {
     tmem_alloc(&sh.tbase, 256);
     tmem_relinquish();
@@ -298,32 +299,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       int last_par[kTcStages];
       for (int i = 0; i < kTcStages; ++i) last_par[i] = -1;
       bool ok = true;
-      for (int i = T.ibeg; i < T.iend && ok; ++i) {
-        const TcItem it = items[i];
-        const __nv_bfloat16* ah = pick(b.hi, it.a_pool) + it.a_off;
-        const __nv_bfloat16* al = pick(b.lo, it.a_pool) + it.a_off;
-        const __nv_bfloat16* bh = pick(b.hi, it.b_pool) + it.b_off;
-        const __nv_bfloat16* bl = pick(b.lo, it.b_pool) + it.b_off;
-        const int nck = (it.kp + 63) >> 6;
-        for (int c = 0; c < nck; ++c) {
-          if (!tc_wait(&sh.empty[s], ph ^ 1u, abort_flag, b.status, limit_ns)) {
-            ok = false;
-            break;
-          }
-          const int w = min(64, it.kp - 64 * c);
-          const int64_t ao = tc_block_off(T.a_rows, it.kp, T.tm, c);
-          const int64_t bo = tc_block_off(T.b_rows, it.kp, T.tn, c);
-          const uint32_t abytes = (uint32_t)h_a * w * 2, bbytes = (uint32_t)h_b * w * 2;
-          uint8_t* st = smem + s * kTcStageBytes;
-          mbar_expect_tx(&sh.full[s], 2 * (abytes + bbytes));
-          bulk_g2s(st, ah + ao, abytes, &sh.full[s]);
-          bulk_g2s(st + kTcOperandBytes, al + ao, abytes, &sh.full[s]);
-          bulk_g2s(st + 2 * kTcOperandBytes, bh + bo, bbytes, &sh.full[s]);
-          bulk_g2s(st + 3 * kTcOperandBytes, bl + bo, bbytes, &sh.full[s]);
-          last_par[s] = (int)ph;
-          if (++s == kTcStages) {
-            s = 0;
-            ph ^= 1u;
+      for (int tk = rg.x; tk < rg.y && ok; ++tk) {
+        const TcTask T = tasks[order[tk]];
+        const int h_a = min(128, T.a_rows - 128 * T.tm);
+        const int h_b = min(128, T.b_rows - 128 * T.tn);
+        for (int i = T.ibeg; i < T.iend && ok; ++i) {
+          const TcItem it = items[i];
+          const __nv_bfloat16* ah = pick(b.hi, it.a_pool) + it.a_off;
+          const __nv_bfloat16* al = pick(b.lo, it.a_pool) + it.a_off;
+          const __nv_bfloat16* bh = pick(b.hi, it.b_pool) + it.b_off;
+          const __nv_bfloat16* bl = pick(b.lo, it.b_pool) + it.b_off;
+          const int nck = (it.kp + 63) >> 6;
+          for (int c = 0; c < nck; ++c) {
+            if (!tc_wait(&sh.empty[s], ph ^ 1u, abort_flag, b.status, limit_ns)) {
+              ok = false;
+              break;
+            }
+            const int w = min(64, it.kp - 64 * c);
+            const int64_t ao = tc_block_off(T.a_rows, it.kp, T.tm, c);
+            const int64_t bo = tc_block_off(T.b_rows, it.kp, T.tn, c);
+            const uint32_t abytes = (uint32_t)h_a * w * 2, bbytes = (uint32_t)h_b * w * 2;
+            uint8_t* st = smem + s * kTcStageBytes;
+            mbar_expect_tx(&sh.full[s], 2 * (abytes + bbytes));
+            bulk_g2s(st, ah + ao, abytes, &sh.full[s]);
+            bulk_g2s(st + kTcOperandBytes, al + ao, abytes, &sh.full[s]);
+            bulk_g2s(st + 2 * kTcOperandBytes, bh + bo, bbytes, &sh.full[s]);
+            bulk_g2s(st + 3 * kTcOperandBytes, bl + bo, bbytes, &sh.full[s]);
+            last_par[s] = (int)ph;
+            if (++s == kTcStages) {
+              s = 0;
+              ph ^= 1u;
+            }
           }
         }
       }
@@ -336,44 +342,52 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   } else if (warp == 9) {
     // ---- MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(128, N);
       int s = 0, ab = 0;
       uint32_t ph = 0, aph = 0;
       bool ok = true;
-      for (int i = T.ibeg; i < T.iend && ok; ++i) {
-        const int kp = items[i].kp;
-        if (!tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns)) break;
-        fence_after_sync();
-        const uint32_t d = tmem + (uint32_t)ab * 128u;
-        const int nck = (kp + 63) >> 6;
-        for (int c = 0; c < nck; ++c) {
-          if (!tc_wait(&sh.full[s], ph, abort_flag, b.status, limit_ns)) {
+      for (int tk = rg.x; tk < rg.y && ok; ++tk) {
+        const TcTask T = tasks[order[tk]];
+        const int h_a = min(128, T.a_rows - 128 * T.tm);
+        const int h_b = min(128, T.b_rows - 128 * T.tn);
+        const uint32_t idesc = idesc_bf16(128, (h_b + 15) & ~15);
+        for (int i = T.ibeg; i < T.iend && ok; ++i) {
+          const int kp = items[i].kp;
+          if (!tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns)) {
             ok = false;
             break;
           }
           fence_after_sync();
-          const int w = min(64, kp - 64 * c);
-          const uint32_t sa = smem_u32(smem + s * kTcStageBytes);
-          for (int j = 0; j < w / 16; ++j) {
-            const uint32_t ao = (uint32_t)(32 * j * h_a), bo = (uint32_t)(32 * j * h_b);
-            const uint64_t a_hi = smem_desc(sa + ao, h_a * 16, 128);
-            const uint64_t a_lo = smem_desc(sa + kTcOperandBytes + ao, h_a * 16, 128);
-            const uint64_t b_hi = smem_desc(sa + 2 * kTcOperandBytes + bo, h_b * 16, 128);
-            const uint64_t b_lo = smem_desc(sa + 3 * kTcOperandBytes + bo, h_b * 16, 128);
-            mma_bf16(d, a_hi, b_hi, idesc, (c > 0 || j > 0) ? 1u : 0u);
-            mma_bf16(d, a_hi, b_lo, idesc, 1u);
-            mma_bf16(d, a_lo, b_hi, idesc, 1u);
+          const uint32_t d = tmem + (uint32_t)ab * 128u;
+          const int nck = (kp + 63) >> 6;
+          for (int c = 0; c < nck; ++c) {
+            if (!tc_wait(&sh.full[s], ph, abort_flag, b.status, limit_ns)) {
+              ok = false;
+              break;
+            }
+            fence_after_sync();
+            const int w = min(64, kp - 64 * c);
+            const uint32_t sa = smem_u32(smem + s * kTcStageBytes);
+            for (int j = 0; j < w / 16; ++j) {
+              const uint32_t ao = (uint32_t)(32 * j * h_a), bo = (uint32_t)(32 * j * h_b);
+              const uint64_t a_hi = smem_desc(sa + ao, h_a * 16, 128);
+              const uint64_t a_lo = smem_desc(sa + kTcOperandBytes + ao, h_a * 16, 128);
+              const uint64_t b_hi = smem_desc(sa + 2 * kTcOperandBytes + bo, h_b * 16, 128);
+              const uint64_t b_lo = smem_desc(sa + 3 * kTcOperandBytes + bo, h_b * 16, 128);
+              mma_bf16(d, a_hi, b_hi, idesc, (c > 0 || j > 0) ? 1u : 0u);
+              mma_bf16(d, a_hi, b_lo, idesc, 1u);
+              mma_bf16(d, a_lo, b_hi, idesc, 1u);
+            }
+            mma_commit(&sh.empty[s]);
+            if (++s == kTcStages) {
+              s = 0;
+              ph ^= 1u;
+            }
           }
-          mma_commit(&sh.empty[s]);
-          if (++s == kTcStages) {
-            s = 0;
-            ph ^= 1u;
-          }
+          if (!ok) break;
+          mma_commit(&sh.acc_full[ab]);
+          ab ^= 1;
+          if (ab == 0) aph ^= 1u;
         }
-        if (!ok) break;
-        mma_commit(&sh.acc_full[ab]);
-        ab ^= 1;
-        if (ab == 0) aph ^= 1u;
       }
     }
     __syncwarp();
@@ -382,93 +396,113 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int q = warp & 3, half = warp >> 2;
     const int row = 32 * q + lane;
     const uint32_t lane_base = (uint32_t)(32 * q) << 16;
-    if (PHASE == 2) {
-      float vh[64], vl[64];
+    int ab = 0;
+    uint32_t aph = 0;
+    bool ok = true;
+    for (int tk = rg.x; tk < rg.y && ok; ++tk) {
+      const TcTask T = tasks[order[tk]];
+      const int h_a = min(128, T.a_rows - 128 * T.tm);
+      const int h_b = min(128, T.b_rows - 128 * T.tn);
+      const int N = (h_b + 15) & ~15;
+      if (PHASE == 2) {
+        float vh[64], vl[64];
 #pragma unroll
-      for (int e = 0; e < 64; ++e) vh[e] = vl[e] = 0.f;
-      int ab = 0;
-      uint32_t aph = 0;
-      for (int i = T.ibeg; i < T.iend; ++i) {
-        const float alpha = items[i].alpha;
-        const bool ok = tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns);
-        if (!__all_sync(0xffffffffu, ok)) break;  // TMEM loads below need the whole warp
+        for (int e = 0; e < 64; ++e) vh[e] = vl[e] = 0.f;
+        for (int i = T.ibeg; i < T.iend; ++i) {
+          const float alpha = items[i].alpha;
+          ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
+          if (!ok) break;  // TMEM loads below need the whole warp
+          fence_after_sync();
+          const uint32_t d = tmem + (uint32_t)ab * 128u + (uint32_t)half * 64u + lane_base;
+#pragma unroll
+          for (int g = 0; g < 4; ++g) {
+            if (half * 64 + g * 16 < N) {
+              float v[16];
+              tmem_ld16(d + (uint32_t)(g * 16), v);
+#pragma unroll
+              for (int e = 0; e < 16; ++e) two_sum_acc(vh[g * 16 + e], vl[g * 16 + e], __fmul_rn(alpha, v[e]));
+            }
+          }
+          fence_before_sync();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
+          ab ^= 1;
+          if (ab == 0) aph ^= 1u;
+        }
+        if (!ok) break;
+        if (T.direct) {
+          // the whole tile in this task: FP64 result straight into sigma
+          if (row < T.valid_rows) {
+            double* out = sigma + T.out_off + (int64_t)(128 * T.tm + row) * T.out_kp + 128 * T.tn;
+#pragma unroll
+            for (int e = 0; e < 64; ++e) {
+              const int col = half * 64 + e;
+              if (col < T.valid_cols) out[col] = (double)vh[e] + (double)vl[e];
+            }
+          }
+        } else if (row < h_a) {
+          float2* out = b.partials + T.out_off + (int64_t)row * h_b;
+#pragma unroll
+          for (int e = 0; e < 64; ++e) {
+            const int col = half * 64 + e;
+            if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+          }
+        }
+      } else {
+        // phase 1: one item; S tile written as a packed operand (rows of this
+        // tile, K columns 128 tn.. of S)
+        ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
+        if (!ok) break;
         fence_after_sync();
+        const float alpha = items[T.ibeg].alpha;
+        const int ncols = min(128, T.out_kp - 128 * T.tn);
         const uint32_t d = tmem + (uint32_t)ab * 128u + (uint32_t)half * 64u + lane_base;
+        __nv_bfloat16* shi = b.hi[kTcPoolS] + T.out_off;
+        __nv_bfloat16* slo = b.lo[kTcPoolS] + T.out_off;
+        float v[64];
 #pragma unroll
         for (int g = 0; g < 4; ++g) {
           if (half * 64 + g * 16 < N) {
-            float v[16];
-            tmem_ld16(d + (uint32_t)(g * 16), v);
+            tmem_ld16(d + (uint32_t)(g * 16), v + 16 * g);
+          } else {
 #pragma unroll
-            for (int e = 0; e < 16; ++e) two_sum_acc(vh[g * 16 + e], vl[g * 16 + e], __fmul_rn(alpha, v[e]));
+            for (int e = 0; e < 16; ++e) v[16 * g + e] = 0.f;
           }
         }
+        // accumulator read: the MMA issuer may reuse it
         fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
         ab ^= 1;
         if (ab == 0) aph ^= 1u;
-      }
-      if (!*abort_flag && row < h_a) {
-        float2* out = b.partials + T.out_off + (int64_t)row * h_b;
+        if (row < h_a) {
 #pragma unroll
-        for (int e = 0; e < 64; ++e) {
-          const int col = half * 64 + e;
-          if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
-        }
-      }
-    } else {
-      // phase 1: one item; S tile written as a packed operand (rows of this
-      // tile, K columns 128 tn.. of S)
-      const bool ok = T.iend > T.ibeg && tc_wait(&sh.acc_full[0], 0, abort_flag, b.status, limit_ns);
-      if (__all_sync(0xffffffffu, ok)) {
-        fence_after_sync();
-        const float alpha = items[T.ibeg].alpha;
-        const int ncols = min(128, T.out_kp - 128 * T.tn);
-        const uint32_t d = tmem + (uint32_t)half * 64u + lane_base;
-        __nv_bfloat16* shi = b.hi[kTcPoolS] + T.out_off;
-        __nv_bfloat16* slo = b.lo[kTcPoolS] + T.out_off;
+          for (int g8 = 0; g8 < 8; ++g8) {
+            const int c0 = half * 64 + 8 * g8;
+            if (c0 < ncols) {
+              uint32_t hw[4], lw[4];
 #pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          const int c0 = half * 64 + g * 16;
-          if (c0 < ncols) {
-            float v[16];
-            if (c0 < N) {
-              tmem_ld16(d + (uint32_t)(g * 16), v);
-            } else {
-#pragma unroll
-              for (int e = 0; e < 16; ++e) v[e] = 0.f;
-            }
-            if (row < h_a) {
-#pragma unroll
-              for (int hv = 0; hv < 2; ++hv) {
-                uint32_t hw[4], lw[4];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                  const int col = c0 + 8 * hv + e;
-                  const float x = col < h_b ? __fmul_rn(alpha, v[8 * hv + e]) : 0.f;
-                  __nv_bfloat16 xh, xl;
-                  split_bf16(x, xh, xl);
-                  const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
-                  if (e & 1) {
-                    hw[e >> 1] |= bh << 16;
-                    lw[e >> 1] |= bl << 16;
-                  } else {
-                    hw[e >> 1] = bh;
-                    lw[e >> 1] = bl;
-                  }
+              for (int e = 0; e < 8; ++e) {
+                const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
+                __nv_bfloat16 xh, xl;
+                split_bf16(x, xh, xl);
+                const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+                if (e & 1) {
+                  hw[e >> 1] |= bh << 16;
+                  lw[e >> 1] |= bl << 16;
+                } else {
+                  hw[e >> 1] = bh;
+                  lw[e >> 1] = bl;
                 }
-                const int C = 128 * T.tn + c0 + 8 * hv;  // S column
-                const int64_t off =
-                    tc_block_off(T.a_rows, T.out_kp, T.tm, C >> 6) + (kmajor_off(row, C & 63, h_a) >> 1);
-                *(uint4*)(shi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                *(uint4*)(slo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
               }
+              const int C = 128 * T.tn + c0;  // S column
+              const int64_t off = tc_block_off(T.a_rows, T.out_kp, T.tm, C >> 6) + (kmajor_off(row, C & 63, h_a) >> 1);
+              *(uint4*)(shi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+              *(uint4*)(slo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
           }
         }
       }
-      fence_before_sync();
     }
   }
   __syncthreads();
@@ -484,17 +518,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
-cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, int ntasks,
-                            uint64_t limit_ns, cudaStream_t s) {
-  if (ntasks <= 0) return cudaGetLastError();
+cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, const int* order,
+                            const int2* ranges, int nblocks, double* sigma, uint64_t limit_ns, cudaStream_t s) {
+  if (nblocks <= 0) return cudaGetLastError();
   if (phase == 1) {
     cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     if (e != cudaSuccess) return e;
-    tc_sigma_kernel<1><<<ntasks, kTcThreads, kTcSmem, s>>>(b, items, tasks, limit_ns);
+    tc_sigma_kernel<1><<<nblocks, kTcThreads, kTcSmem, s>>>(b, items, tasks, order, ranges, sigma, limit_ns);
   } else if (phase == 2) {
     cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     if (e != cudaSuccess) return e;
-    tc_sigma_kernel<2><<<ntasks, kTcThreads, kTcSmem, s>>>(b, items, tasks, limit_ns);
+    tc_sigma_kernel<2><<<nblocks, kTcThreads, kTcSmem, s>>>(b, items, tasks, order, ranges, sigma, limit_ns);
   } else {
     return cudaErrorInvalidValue;
   }

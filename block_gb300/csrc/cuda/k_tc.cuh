@@ -54,18 +54,21 @@ struct TcItem {
   float alpha;
 };
 
-// One thread block: output tile (tm, tn) -- rows 128 tm.. of the A operands,
-// rows 128 tn.. of the B operands -- and the items [ibeg, iend).
+// One task: output tile (tm, tn) -- rows 128 tm.. of the A operands, rows
+// 128 tn.. of the B operands -- and the items [ibeg, iend).
 //   phase 1 (one item): writes alpha * A B^T as the packed S operand at
 //     out_off of pool S (rows a_rows, K out_kp);
-//   phase 2: sum of the items, compensated (hi, lo) f32 pairs for the
-//     h_a x h_b valid part of the tile, written at partials + out_off.
+//   phase 2: sum of the items with a compensated (hi, lo) f32 accumulation;
+//     direct: the FP64 tile (valid_rows x valid_cols) goes to sigma at
+//     out_off + (128 tm + r) * out_kp + 128 tn + c; otherwise the h_a x h_b
+//     (hi, lo) pairs go to partials + out_off for the reduce kernel.
 struct TcTask {
   int32_t a_rows, b_rows;
   int32_t tm, tn;
   int32_t ibeg, iend;
   int64_t out_off;
-  int32_t out_kp, pad;
+  int32_t out_kp, direct;
+  int32_t valid_rows, valid_cols;
 };
 
 // sigma tile (rows r0.., cols c0.., h x w) = sum of the partial slots
@@ -84,9 +87,10 @@ struct TcBufs {
 };
 
 cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cudaStream_t s);
-// phase 1 or 2; limit_ns bounds every pipeline wait
-cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, int ntasks,
-                            uint64_t limit_ns, cudaStream_t s);
+// phase 1 or 2 on nblocks persistent blocks: block j runs the tasks
+// order[ranges[j].x .. ranges[j].y); limit_ns bounds every pipeline wait
+cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, const int* order,
+                            const int2* ranges, int nblocks, double* sigma, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
                              cudaStream_t s);
 
