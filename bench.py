@@ -258,7 +258,13 @@ def run_ours(a):
                 "peak_source": ("bf16_tflops of measured" if peaks else "fallback 1900"),
                 "products_per_logical_product": prods,
                 "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
+                "note_issued": "3 (6) bf16 products per logical FP64 product, without tile padding",
                 "fp64_peak_tflops_in_run": fp64, "algorithmic_bytes_per_step": nbytes}
+    if a.precision == "bf16x3tc":
+        info = ctx.superblock_info(sb)
+        roof["tc_mma_issued_tflops"] = info["tc_mma_flops"] / (kern_ms * 1e-3) / 1e12
+        roof["tc_mma_issued_frac"] = roof["tc_mma_issued_tflops"] / roof["peak"]
+        roof["tc_plan"] = {k: v for k, v in info.items() if k.startswith("tc_")}
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else "bf16 slices, f32 accumulate",

@@ -59,6 +59,7 @@ _SIGS = {
     "bgpu_profiler_start": (_I, [_P]),
     "bgpu_profiler_stop": (_I, [_P]),
     "bgpu_tc_tile": (_I, [_P, _P, _P, _P, _I, _I, _I]),
+    "bgpu_superblock_info": (_I, [_P, _I, _DP, _I]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
 }
@@ -257,6 +258,16 @@ class Context:
     def profiler_stop(self):
         self._check(self.lib.bgpu_profiler_stop(self.h))
 
+    INFO_KEYS = ("flops", "bytes", "tc_mma_flops", "tc_phase1_tasks", "tc_phase2_tasks", "tc_phase2_items",
+                 "tc_phase2_stage1_items", "tc_split_tiles", "tc_pool_L", "tc_pool_R", "tc_pool_psi",
+                 "tc_pool_S", "fp64_stage1_units", "fp64_items")
+
+    def superblock_info(self, sb):
+        """Work-list statistics of one sigma (see bgpu_superblock_info)."""
+        v = np.zeros(len(self.INFO_KEYS))
+        self._check(self.lib.bgpu_superblock_info(self.h, sb, _dp(v), len(v)))
+        return dict(zip(self.INFO_KEYS, v.tolist()))
+
     def tc_tile(self, a_bits, b_bits, packed=False):
         """d = a * b^T on one tcgen05 tile; a (128 x k) and b (n x k) are
         uint16 arrays of bf16 bit patterns, d is float32 (128 x n).  With
@@ -279,10 +290,11 @@ class Context:
     # ---- full sweep (block.spin_adapted dmrg.conf)
     def run_dmrg(self, conf_path, verbose=0, max_roots=32):
         e = np.zeros(max_roots, dtype=np.float64)
-        st = np.zeros(12, dtype=np.float64)
+        st = np.zeros(13, dtype=np.float64)
         self._check(self.lib.bgpu_run_dmrg(self.h, conf_path.encode(), verbose, _dp(e), max_roots, _dp(st)))
         nroots = int(st[7])
         stats = dict(sweeps=int(st[0]), sigma_calls=int(st[1]), sigma_seconds=st[2], sigma_flops=st[3],
                      seconds=st[4], discarded=st[5], last_sweep_energy=st[6], build_seconds=st[8],
-                     solve_seconds=st[9], density_seconds=st[10], renorm_seconds=st[11])
+                     solve_seconds=st[9], density_seconds=st[10], renorm_seconds=st[11],
+                     plan_seconds=st[12])
         return e[:nroots].copy(), stats

@@ -295,6 +295,31 @@ int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi, double* sigma, in
   });
 }
 
+int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && info && n >= 0, "bad arguments");
+    auto& r = *it->second;
+    if (!r.plan.tc) ctx->eng->plan_tc(r.sb, r.plan);
+    const SigmaPlan& p = r.plan;
+    const double v[14] = {p.flops,
+                          p.bytes,
+                          p.tc_mma_flops,
+                          (double)p.tc_stats[0],
+                          (double)p.tc_stats[1],
+                          (double)p.tc_stats[2],
+                          (double)p.tc_stats[3],
+                          (double)p.tc_stats[4],
+                          (double)p.tc_pool_elems[dev::kTcPoolL],
+                          (double)p.tc_pool_elems[dev::kTcPoolR],
+                          (double)p.tc_pool_elems[dev::kTcPoolPsi],
+                          (double)p.tc_pool_elems[dev::kTcPoolS],
+                          (double)p.nstage1_units,
+                          (double)p.nitems};
+    for (int i = 0; i < n; ++i) info[i] = i < 14 ? v[i] : 0.0;
+  });
+}
+
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches) {
   return guarded(ctx, [&] {
     auto it = ctx->sbs.find(sb);
@@ -456,7 +481,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     Integrals I = load_integrals(c);
     DriverOptions opt;
     opt.verbose = verbose;
-    const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops;
+    const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops, p0 = ctx->eng->plan_seconds;
     const long c0 = ctx->eng->sigma_calls;
     SweepResult r;
     {
@@ -477,6 +502,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
       stats[9] = r.solve_seconds;
       stats[10] = r.density_seconds;
       stats[11] = r.renorm_seconds;
+      stats[12] = ctx->eng->plan_seconds - p0;
     }
   });
 }

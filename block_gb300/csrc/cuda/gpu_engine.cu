@@ -238,6 +238,14 @@ std::vector<std::vector<std::pair<int, int>>> sectors_by_left(const Superblock& 
   return by_l;
 }
 
+// adds the wall time of its scope to a counter
+struct PlanTimer {
+  double& acc;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit PlanTimer(double& a) : acc(a) {}
+  ~PlanTimer() { acc += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
 // Longest-processing-time assignment of tasks to `nblocks` persistent
 // blocks; block j runs order[ranges[j].x .. ranges[j].y), in task order.
 void schedule_lpt(const std::vector<double>& cost, int nblocks, std::vector<int>& order, std::vector<int2>& ranges) {
@@ -387,6 +395,7 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
 // plus direct products for pairs with one identity factor.  Every output
 // sector is owned by one unit (no atomics).
 void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
+  PlanTimer timer_(plan_seconds);
   const Block& L = *sb.L;
   const Block& R = *sb.R;
   const int J = sb.target.s2;
@@ -642,6 +651,7 @@ const GpuEngine::Slices& GpuEngine::block_slices(const Block& b, int ns) {
 // its coupling list cut into chunks of similar cost (one thread block each)
 // and a fixed-order reduction of the chunks' partial tiles.
 void GpuEngine::plan_fused(const Superblock& sb, SigmaPlan& plan) {
+  PlanTimer timer_(plan_seconds);
   const auto by_l = sectors_by_left(sb);
   std::vector<std::vector<std::vector<dev::FusedItem>>> per_t(sb.terms.size());
   parallel_for((int)sb.terms.size(), [&](int ti) {
@@ -780,6 +790,7 @@ void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const do
 // alpha * X * Y^T (X = S, psi or an L operator; Y = an R operator or psi^T)
 // in phase 2, in the same order as the FP64 plan.
 void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
+  PlanTimer timer_(plan_seconds);
   using namespace dev;
   const Block& L = *sb.L;
   const Block& R = *sb.R;
@@ -936,7 +947,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
     }
   }
-  const double chunk = std::max(total / (2.0 * nsm), 20000.0);
+  const double chunk = std::max(total / nsm, 20000.0);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     const int ib = (int)i2.size();
@@ -1048,6 +1059,12 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   plan.tc_tiles.upload(tiles, stream_);
   plan.tc_slots.upload(slots, stream_);
   plan.tc_mma_flops = mma;
+  {
+    int64_t full = 0;
+    for (const TcItem& it : i2) full += it.a_pool == kTcPoolS ? 1 : 0;
+    const int64_t st[5] = {(int64_t)t1.size(), (int64_t)t2.size(), (int64_t)i2.size(), full, (int64_t)tiles.size()};
+    for (int i = 0; i < 5; ++i) plan.tc_stats[i] = st[i];
+  }
   // operator blocks are packed once per plan
   DevArray<TcPack> dops;
   dops.upload(ops_packs, stream_);

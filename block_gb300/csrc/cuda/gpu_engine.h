@@ -79,6 +79,9 @@ struct SigmaPlan {
   DevArray<int64_t> tc_slots;
   float2* tc_partials = nullptr;
   double tc_mma_flops = 0.0;  // tensor-core flops issued per product (3 bf16 products per logical one)
+  // plan statistics: phase-1 tasks, phase-2 tasks, phase-2 items, phase-2
+  // items reading a stage-1 product, split tiles
+  int64_t tc_stats[5] = {};
 };
 
 class GpuEngine : public Engine {
@@ -133,6 +136,7 @@ class GpuEngine : public Engine {
   double sigma_flops = 0.0;
   long split_calls = 0, fp64_calls = 0;
   double split_seconds = 0.0, fp64_seconds = 0.0;
+  double plan_seconds = 0.0;  // host time compiling sigma work lists
 
  private:
   struct Slices {

@@ -220,6 +220,7 @@ constexpr uint32_t kTcOperandBytes = 128 * 64 * 2;  // one slice of one operand 
 constexpr uint32_t kTcStageBytes = 4 * kTcOperandBytes;
 constexpr int kTcThreads = 320;  // warps 0-7 epilogue, 8 bulk-copy producer, 9 MMA issuer
 constexpr int kTcSmem = kTcStages * kTcStageBytes;
+constexpr int kTcGroup = 8;  // phase-2 items summed in f32 before the compensated fold
 
 struct TcShared {
   uint64_t full[kTcStages], empty[kTcStages], acc_full[2], acc_empty[2], drain;
@@ -268,8 +269,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __shared__ TcShared sh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int2 rg = ranges[blockIdx.x];
+  // TMEM: accumulators at columns 0 and 128, phase-2 (hi, lo) sums at 256, 384
   if (warp == 9) {
-    tmem_alloc(&sh.tbase, 256);
+    tmem_alloc(&sh.tbase, 512);
     tmem_relinquish();
   }
   if (tid == 0) {
@@ -405,9 +407,62 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const int h_b = min(128, T.b_rows - 128 * T.tn);
       const int N = (h_b + 15) & ~15;
       if (PHASE == 2) {
-        float vh[64], vl[64];
+        // items are summed in f32 registers in groups of kTcGroup; each group
+        // sum is folded into the compensated (hi, lo) pair kept in TMEM
+        // columns 256.. (hi) and 384.. (lo)
+        float acc[64];
 #pragma unroll
-        for (int e = 0; e < 64; ++e) vh[e] = vl[e] = 0.f;
+        for (int e = 0; e < 64; ++e) acc[e] = 0.f;
+        int gi = 0;
+        bool first = true;
+        const uint32_t vh_t = tmem + 256u + (uint32_t)half * 64u + lane_base;
+        const uint32_t vl_t = tmem + 384u + (uint32_t)half * 64u + lane_base;
+        // add the pending group (if add) and either keep the pair in TMEM or
+        // write the result (last)
+        auto flush = [&](bool add, bool last) {
+#pragma unroll
+          for (int g = 0; g < 4; ++g) {
+            if (half * 64 + g * 16 < N) {
+              float vh[16], vl[16];
+              if (first) {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                  vh[e] = add ? acc[16 * g + e] : 0.f;
+                  vl[e] = 0.f;
+                }
+              } else {
+                tmem_ld16(vh_t + (uint32_t)(16 * g), vh);
+                tmem_ld16(vl_t + (uint32_t)(16 * g), vl);
+                if (add) {
+#pragma unroll
+                  for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], acc[16 * g + e]);
+                }
+              }
+              if (!last) {
+                tmem_st16(vh_t + (uint32_t)(16 * g), vh);
+                tmem_st16(vl_t + (uint32_t)(16 * g), vl);
+              } else if (T.direct) {
+                // the whole tile in this task: FP64 result straight into sigma
+                if (row < T.valid_rows) {
+                  double* out = sigma + T.out_off + (int64_t)(128 * T.tm + row) * T.out_kp + 128 * T.tn;
+#pragma unroll
+                  for (int e = 0; e < 16; ++e) {
+                    const int col = half * 64 + 16 * g + e;
+                    if (col < T.valid_cols) out[col] = (double)vh[e] + (double)vl[e];
+                  }
+                }
+              } else if (row < h_a) {
+                float2* out = b.partials + T.out_off + (int64_t)row * h_b;
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                  const int col = half * 64 + 16 * g + e;
+                  if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                }
+              }
+            }
+          }
+          first = false;
+        };
         for (int i = T.ibeg; i < T.iend; ++i) {
           const float alpha = items[i].alpha;
           ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
@@ -419,8 +474,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (half * 64 + g * 16 < N) {
               float v[16];
               tmem_ld16(d + (uint32_t)(g * 16), v);
+              if (gi == 0) {
 #pragma unroll
-              for (int e = 0; e < 16; ++e) two_sum_acc(vh[g * 16 + e], vl[g * 16 + e], __fmul_rn(alpha, v[e]));
+                for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmul_rn(alpha, v[e]);
+              } else {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmaf_rn(alpha, v[e], acc[g * 16 + e]);
+              }
             }
           }
           fence_before_sync();
@@ -428,26 +488,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
           ab ^= 1;
           if (ab == 0) aph ^= 1u;
+          if (++gi == kTcGroup && i + 1 < T.iend) {
+            flush(true, false);
+            gi = 0;
+          }
         }
         if (!ok) break;
-        if (T.direct) {
-          // the whole tile in this task: FP64 result straight into sigma
-          if (row < T.valid_rows) {
-            double* out = sigma + T.out_off + (int64_t)(128 * T.tm + row) * T.out_kp + 128 * T.tn;
-#pragma unroll
-            for (int e = 0; e < 64; ++e) {
-              const int col = half * 64 + e;
-              if (col < T.valid_cols) out[col] = (double)vh[e] + (double)vl[e];
-            }
-          }
-        } else if (row < h_a) {
-          float2* out = b.partials + T.out_off + (int64_t)row * h_b;
-#pragma unroll
-          for (int e = 0; e < 64; ++e) {
-            const int col = half * 64 + e;
-            if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
-          }
-        }
+        flush(gi > 0, true);
       } else {
         // phase 1: one item; S tile written as a packed operand (rows of this
         // tile, K columns 128 tn.. of S)
@@ -514,7 +561,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     __syncwarp();
     fence_after_sync();
-    tmem_dealloc(tmem, 256);
+    tmem_dealloc(tmem, 512);
   }
 }
 
@@ -540,7 +587,7 @@ __global__ void __launch_bounds__(256) tc_reduce_kernel(const float2* __restrict
                                                          const int64_t* __restrict__ slots, double* __restrict__ sigma) {
   const TcTile t = tiles[blockIdx.x];
   const int n = t.h * t.w;
-  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+  for (int e = blockIdx.y * blockDim.x + threadIdx.x; e < n; e += gridDim.y * blockDim.x) {
     double acc = 0.0;
     const int r = e / t.w, c = e % t.w;
     for (int p = t.pbeg; p < t.pend; ++p) {
@@ -553,7 +600,7 @@ __global__ void __launch_bounds__(256) tc_reduce_kernel(const float2* __restrict
 
 cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
                              cudaStream_t s) {
-  if (ntiles > 0) tc_reduce_kernel<<<ntiles, 256, 0, s>>>(b.partials, tiles, slots, sigma);
+  if (ntiles > 0) tc_reduce_kernel<<<dim3(ntiles, 16), 256, 0, s>>>(b.partials, tiles, slots, sigma);
   return cudaGetLastError();
 }
 

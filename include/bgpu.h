@@ -112,6 +112,14 @@ int bgpu_superblock_define(bgpu_ctx* ctx, int left, int right, const int* target
 int bgpu_superblock_free(bgpu_ctx* ctx, int sb);
 /* Algorithmic work of one sigma: FP64-equivalent flops and bytes. */
 int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes);
+/* Work-list statistics of one sigma (no reference counterpart), info[n]:
+ *   FP64-equivalent flops, algorithmic bytes, tensor-core flops issued by the
+ *   tcgen05 path (3 bf16 products, padded tiles), phase-1 tasks, phase-2
+ *   tasks, phase-2 items, phase-2 items reading a stage-1 product, split
+ *   tiles, packed elements of the L-operator / R-operator / psi / stage-1
+ *   pools, FP64 stage-1 units, FP64 items.  Builds the tensor-core plan if
+ *   needed. */
+int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n);
 /* Kernel launches of one sigma product. */
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);
 
@@ -211,11 +219,12 @@ int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition,
  * `block.spin_adapted dmrg.conf` entry, main.C:25-52 / dmrg.C:600-706), with
  * all operator and wavefunction arithmetic on the GPU.  `orbitals` may also
  * name a generated Hamiltonian: synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>.
- * energies[max_roots] receive the final energies; stats[12] (may be NULL):
+ * energies[max_roots] receive the final energies; stats[13] (may be NULL):
  *   sweeps, sigma calls, sigma seconds, sigma flops, total seconds, max
  *   discarded weight, last-sweep energy, number of roots, then wall seconds
  *   of the block-build, Davidson, density/rotation and renormalisation
- *   phases.
+ *   phases, and the host seconds spent compiling sigma work lists (part of
+ *   the Davidson phase).
  */
 int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
                   double* stats);
