@@ -590,12 +590,8 @@ void GpuEngine::free_plan(SigmaPlan& p) {
     p.tc_pool_elems[i] = 0;
   }
   p.tc_psi_pack.release(stream_);
-  p.tc_i1.release(stream_);
-  p.tc_i2.release(stream_);
-  p.tc_t1.release(stream_);
-  p.tc_t2.release(stream_);
-  p.tc_o1.release(stream_);
-  p.tc_o2.release(stream_);
+  p.tc_w1.release(stream_);
+  p.tc_w2.release(stream_);
   p.tc_r1.release(stream_);
   p.tc_r2.release(stream_);
   p.tc_tiles.release(stream_);
@@ -818,6 +814,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     p.rows_p = tc_round8(v.rows);
     p.kp = tc_round16(v.cols);
     p.trans = v.trans ? 1 : 0;
+    p.rt = pool == kTcPoolL ? kTcRowsA : kTcRowsB;  // L blocks are A operands, R blocks B operands
     p.src = (uint8_t)pool;  // 0: L arena, 1: R arena
     p.pool = (uint8_t)pool;
     p.dst_off = pool_n[pool];
@@ -839,6 +836,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     a.cols_v = S.cols;
     a.rows_p = tc_round8(S.rows);
     a.kp = tc_round16(S.cols);
+    a.rt = kTcRowsA;
     a.dst_off = psi_off[s] = pool_n[kTcPoolPsi];
     pool_n[kTcPoolPsi] += (int64_t)a.rows_p * a.kp;
     dims[kTcPoolPsi][a.dst_off] = {a.rows_p, a.kp};
@@ -850,6 +848,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     t.cols_v = S.rows;
     t.rows_p = tc_round8(S.cols);
     t.kp = tc_round16(S.rows);
+    t.rt = kTcRowsB;
     t.dst_off = psit_off[s] = pool_n[kTcPoolPsiT];
     pool_n[kTcPoolPsiT] += (int64_t)t.rows_p * t.kp;
     dims[kTcPoolPsiT][t.dst_off] = {t.rows_p, t.kp};
@@ -901,7 +900,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         const int idx = (int)i1.size();
         i1.push_back(a);
         for (int tm = 0; tm < (mr + 127) / 128; ++tm)
-          for (int tn = 0; tn < (mc + 127) / 128; ++tn) {
+          for (int tn = 0; tn < (mc + kTcRowsB - 1) / kTcRowsB; ++tn) {
             TcTask t{};
             t.a_rows = rows_p;
             t.b_rows = tc_round8(mc);
@@ -912,7 +911,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
             t.out_off = cur_s;
             t.out_kp = skp;
             t1.push_back(t);
-            mma += 3.0 * 2.0 * 128 * tc_round16(std::min(128, t.b_rows - 128 * tn)) * a.kp;
+            mma += 3.0 * 2.0 * 128 * tc_round16(std::min(kTcRowsB, t.b_rows - kTcRowsB * tn)) * a.kp;
           }
         cur_l = c.lQ;
         cur_lp = c.lQp;
@@ -942,12 +941,12 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   double total = 0.0;
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
-    for (int tn = 0; tn < (S.cols + 127) / 128; ++tn) {
-      const int hb = std::min(128, tc_round8(S.cols) - 128 * tn);
+    for (int tn = 0; tn < (S.cols + kTcRowsB - 1) / kTcRowsB; ++tn) {
+      const int hb = std::min(kTcRowsB, tc_round8(S.cols) - kTcRowsB * tn);
       for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
     }
   }
-  const double chunk = std::max(total / nsm, 20000.0);
+  const double chunk = std::max(total / (3.0 * nsm), 20000.0);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     const int ib = (int)i2.size();
@@ -955,8 +954,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     const int ie = (int)i2.size();
     const int rows_p = tc_round8(S.rows), cols_p = tc_round8(S.cols);
     for (int tm = 0; tm < (S.rows + 127) / 128; ++tm)
-      for (int tn = 0; tn < (S.cols + 127) / 128; ++tn) {
-        const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(128, cols_p - 128 * tn);
+      for (int tn = 0; tn < (S.cols + kTcRowsB - 1) / kTcRowsB; ++tn) {
+        const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(kTcRowsB, cols_p - kTcRowsB * tn);
         double tile_cost = 0.0;
         for (int x = ib; x < ie; ++x) tile_cost += item_cost(i2[x], hb);
         TcTask t{};
@@ -965,7 +964,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         t.tm = tm;
         t.tn = tn;
         t.valid_rows = std::min(128, S.rows - 128 * tm);
-        t.valid_cols = std::min(128, S.cols - 128 * tn);
+        t.valid_cols = std::min(kTcRowsB, S.cols - kTcRowsB * tn);
         for (int x = ib; x < ie; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
         if (tile_cost <= chunk || ie - ib <= 1) {
           t.ibeg = ib;
@@ -983,7 +982,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         tl.h = t.valid_rows;
         tl.w = t.valid_cols;
         tl.r0 = 128 * tm;
-        tl.c0 = 128 * tn;
+        tl.c0 = kTcRowsB * tn;
         tl.pad = hb;  // row stride of the partial slots
         tl.pbeg = (int)slots.size();
         int x0 = ib;
@@ -1008,7 +1007,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   }
   std::vector<double> c1;
   for (const TcTask& t : t1)
-    c1.push_back(item_cost(i1[t.ibeg], std::min(128, t.b_rows - 128 * t.tn)) + 200.0);
+    c1.push_back(item_cost(i1[t.ibeg], std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn)) + 200.0);
   auto check = [&](const TcTask& t, const std::vector<TcItem>& items) {
     for (int x = t.ibeg; x < t.iend; ++x) {
       const TcItem& it = items[x];
@@ -1016,7 +1015,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       const auto b = dims[it.b_pool].find(it.b_off);
       if (a == dims[it.a_pool].end() || b == dims[it.b_pool].end() || a->second.first != t.a_rows ||
           b->second.first != t.b_rows || a->second.second != it.kp || b->second.second != it.kp ||
-          128 * t.tm >= t.a_rows || 128 * t.tn >= t.b_rows)
+          128 * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows)
         throw std::runtime_error("tensor-core plan: operand shape does not match its tile");
     }
   };
@@ -1024,13 +1023,13 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     check(t, i1);
     const auto sdim = dims[kTcPoolS].find(t.out_off);
     if (sdim == dims[kTcPoolS].end() || sdim->second.first != t.a_rows || sdim->second.second != t.out_kp ||
-        128 * t.tn >= t.out_kp)
+        kTcRowsB * t.tn >= t.out_kp)
       throw std::runtime_error("tensor-core plan: stage-1 output does not match its tile");
   }
   for (const TcTask& t : t2) {
     check(t, i2);
     if (t.direct && (t.valid_rows > std::min(128, t.a_rows - 128 * t.tm) ||
-                     t.valid_cols > std::min(128, t.b_rows - 128 * t.tn)))
+                     t.valid_cols > std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn)))
       throw std::runtime_error("tensor-core plan: output tile larger than its operands");
   }
   std::vector<int> o1, o2;
@@ -1048,14 +1047,63 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
                              stream_),
              "tc partials");
   plan.tc_psi_pack.upload(psi_packs, stream_);
-  plan.tc_i1.upload(i1, stream_);
-  plan.tc_t1.upload(t1, stream_);
-  plan.tc_i2.upload(i2, stream_);
-  plan.tc_t2.upload(t2, stream_);
-  plan.tc_o1.upload(o1, stream_);
-  plan.tc_o2.upload(o2, stream_);
-  plan.tc_r1.upload(r1, stream_);
-  plan.tc_r2.upload(r2, stream_);
+  // flatten every block's tasks into its stream of work records
+  auto flatten = [&](int phase, const std::vector<TcTask>& tasks, const std::vector<TcItem>& items,
+                     const std::vector<int>& order, const std::vector<int2>& ranges, std::vector<TcWork>& w,
+                     std::vector<int2>& wr) {
+    w.clear();
+    wr.clear();
+    for (const int2& rg : ranges) {
+      const int wb = (int)w.size();
+      for (int k = rg.x; k < rg.y; ++k) {
+        const TcTask& T = tasks[order[k]];
+        TcWork base{};
+        base.h_a = (int16_t)std::min(kTcRowsA, T.a_rows - kTcRowsA * T.tm);
+        base.h_b = (int16_t)std::min(kTcRowsB, T.b_rows - kTcRowsB * T.tn);
+        base.valid_rows = (int16_t)T.valid_rows;
+        base.valid_cols = (int16_t)T.valid_cols;
+        if (phase == 1) {
+          base.out_base = T.out_off + (int64_t)kTcRowsA * T.tm * T.out_kp;
+          base.out_ld = T.out_kp;
+          base.col0 = kTcRowsB * T.tn;
+        } else if (T.direct) {
+          base.out_base = T.out_off + (int64_t)kTcRowsA * T.tm * T.out_kp + kTcRowsB * T.tn;
+          base.out_ld = T.out_kp;
+        } else {
+          base.out_base = T.out_off;
+          base.out_ld = base.h_b;
+        }
+        const uint8_t f0 = (uint8_t)(T.direct ? kTcDirect : 0);
+        if (T.ibeg == T.iend) {
+          TcWork x = base;
+          x.flags = (uint8_t)(f0 | kTcFirst | kTcLast | kTcEmpty);
+          w.push_back(x);
+          continue;
+        }
+        for (int i = T.ibeg; i < T.iend; ++i) {
+          const TcItem& it = items[i];
+          TcWork x = base;
+          x.a_base = it.a_off + (int64_t)kTcRowsA * T.tm * it.kp;
+          x.b_base = it.b_off + (int64_t)kTcRowsB * T.tn * it.kp;
+          x.kp = it.kp;
+          x.alpha = it.alpha;
+          x.a_pool = it.a_pool;
+          x.b_pool = it.b_pool;
+          x.flags = (uint8_t)(f0 | (i == T.ibeg ? kTcFirst : 0) | (i + 1 == T.iend ? kTcLast : 0));
+          w.push_back(x);
+        }
+      }
+      wr.push_back(make_int2(wb, (int)w.size()));
+    }
+  };
+  std::vector<TcWork> w1, w2;
+  std::vector<int2> wr1, wr2;
+  flatten(1, t1, i1, o1, r1, w1, wr1);
+  flatten(2, t2, i2, o2, r2, w2, wr2);
+  plan.tc_w1.upload(w1, stream_);
+  plan.tc_w2.upload(w2, stream_);
+  plan.tc_r1.upload(wr1, stream_);
+  plan.tc_r2.upload(wr2, stream_);
   plan.tc_tiles.upload(tiles, stream_);
   plan.tc_slots.upload(slots, stream_);
   plan.tc_mma_flops = mma;
@@ -1096,11 +1144,9 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   constexpr uint64_t kWaitLimitNs = 1000000000ull;
   cuda_check(dev::launch_tc_pack(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tc pack psi");
   if (marks) cuda_check(cudaEventRecord(marks[0], stream_), "record");
-  cuda_check(dev::launch_tc_sigma(1, b, p.tc_i1.d, p.tc_t1.d, p.tc_o1.d, p.tc_r1.d, (int)p.tc_r1.n, out,
-                                  kWaitLimitNs, stream_),
+  cuda_check(dev::launch_tc_sigma(1, b, p.tc_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
              "tc phase 1");
-  cuda_check(dev::launch_tc_sigma(2, b, p.tc_i2.d, p.tc_t2.d, p.tc_o2.d, p.tc_r2.d, (int)p.tc_r2.n, out,
-                                  kWaitLimitNs, stream_),
+  cuda_check(dev::launch_tc_sigma(2, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
              "tc phase 2");
   if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");
   cuda_check(dev::launch_tc_reduce(b, p.tc_tiles.d, p.tc_slots.d, (int)p.tc_tiles.n, out, stream_), "tc reduce");

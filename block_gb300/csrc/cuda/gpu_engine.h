@@ -71,10 +71,8 @@ struct SigmaPlan {
   __nv_bfloat16* tc_lo[dev::kTcPools] = {};
   int64_t tc_pool_elems[dev::kTcPools] = {};
   DevArray<dev::TcPack> tc_psi_pack;
-  DevArray<dev::TcItem> tc_i1, tc_i2;
-  DevArray<dev::TcTask> tc_t1, tc_t2;
-  DevArray<int> tc_o1, tc_o2;    // task order per persistent block
-  DevArray<int2> tc_r1, tc_r2;   // per block: range in the order
+  DevArray<dev::TcWork> tc_w1, tc_w2;  // work records of phases 1 and 2, grouped by block
+  DevArray<int2> tc_r1, tc_r2;         // per persistent block: its range of records
   DevArray<dev::TcTile> tc_tiles;
   DevArray<int64_t> tc_slots;
   float2* tc_partials = nullptr;

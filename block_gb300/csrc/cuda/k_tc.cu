@@ -199,10 +199,10 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(TcBufs b, const TcPack* __
         lw[e >> 1] = bl;
       }
     }
-    const int t = r >> 7, c = k0 >> 6;
-    const int rest = u.rows_p - 128 * t;
-    const int h = rest < 128 ? rest : 128;
-    const int64_t off = tc_block_off(u.rows_p, u.kp, t, c) + (kmajor_off(r & 127, k0 & 63, h) >> 1);
+    const int t = r / u.rt, c = k0 / kTcKC;
+    const int rest = u.rows_p - u.rt * t;
+    const int h = rest < u.rt ? rest : u.rt;
+    const int64_t off = tc_block_off(u.rows_p, u.kp, t, c, u.rt) + (kmajor_off(r - u.rt * t, k0 % kTcKC, h) >> 1);
     *(uint4*)(hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *(uint4*)(lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
@@ -215,15 +215,18 @@ cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cud
 
 namespace {
 
-constexpr int kTcStages = 3;
-constexpr uint32_t kTcOperandBytes = 128 * 64 * 2;  // one slice of one operand block
-constexpr uint32_t kTcStageBytes = 4 * kTcOperandBytes;
+constexpr int kTcStages = 8;
+constexpr uint32_t kTcABytes = kTcRowsA * kTcKC * 2;  // one slice of an A block
+constexpr uint32_t kTcBBytes = kTcRowsB * kTcKC * 2;  // one slice of a B block
+constexpr uint32_t kTcStageBytes = 2 * kTcABytes + 2 * kTcBBytes;
 constexpr int kTcThreads = 320;  // warps 0-7 epilogue, 8 bulk-copy producer, 9 MMA issuer
 constexpr int kTcSmem = kTcStages * kTcStageBytes;
-constexpr int kTcGroup = 8;  // phase-2 items summed in f32 before the compensated fold
+constexpr int kTcAcc = 4;     // accumulators of 64 TMEM columns
+constexpr int kTcGroup = 8;   // phase-2 items summed in f32 before the compensated fold
+constexpr uint32_t kTcVh = 256, kTcVl = 320;  // TMEM columns of the compensated sums
 
 struct TcShared {
-  uint64_t full[kTcStages], empty[kTcStages], acc_full[2], acc_empty[2], drain;
+  uint64_t full[kTcStages], empty[kTcStages], acc_full[kTcAcc], acc_empty[kTcAcc], drain;
   uint32_t tbase;
   int abort_flag;
 };
@@ -254,22 +257,41 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 
 }  // namespace
 
+// A warp's batch of up to 32 work records: lane l holds record base + l.
+struct WorkRegs {
+  int4 q[4];
+};
+__device__ __forceinline__ void load_work(const TcWork* __restrict__ w, int idx, int end, WorkRegs& r) {
+  if (idx < end) {
+    const int4* p = reinterpret_cast<const int4*>(w + idx);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.q[i] = __ldg(p + i);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r.q[i] = make_int4(0, 0, 0, 0);
+  }
+}
+__device__ __forceinline__ int64_t shfl64(int lo, int hi, int j) {
+  const uint32_t l = (uint32_t)__shfl_sync(0xffffffffu, lo, j), h = (uint32_t)__shfl_sync(0xffffffffu, hi, j);
+  return (int64_t)(((uint64_t)h << 32) | l);
+}
+__device__ __forceinline__ int shfl32(int v, int j) { return __shfl_sync(0xffffffffu, v, j); }
+
 // Grouped split-precision GEMM over packed operands on tcgen05: per K=16
-// step three MMAs (hi*hi + hi*lo + lo*hi) into an f32 TMEM accumulator (two
-// accumulators alternate between items), operand blocks streamed by bulk
-// copies through a 3-stage shared-memory ring.  Persistent: block j walks
-// the tasks order[ranges[j].x .. ranges[j].y) and the pipeline runs across
-// task boundaries.
+// step three MMAs (hi*hi + hi*lo + lo*hi) into an f32 TMEM accumulator of
+// 128 x 64 (four accumulators rotate between items), operand blocks streamed
+// by bulk copies through an 8-stage shared-memory ring.  Persistent: block j
+// walks the work records [ranges[j].x, ranges[j].y), each role loading them
+// 32 at a time, and the pipeline runs across task boundaries.
 template <int PHASE>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    tc_sigma_kernel(TcBufs b, const TcItem* __restrict__ items, const TcTask* __restrict__ tasks,
-                    const int* __restrict__ order, const int2* __restrict__ ranges, double* __restrict__ sigma,
-                    uint64_t limit_ns) {
+    tc_sigma_kernel(TcBufs b, const TcWork* __restrict__ work, const int2* __restrict__ ranges,
+                    double* __restrict__ sigma, uint64_t limit_ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ TcShared sh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int2 rg = ranges[blockIdx.x];
-  // TMEM: accumulators at columns 0 and 128, phase-2 (hi, lo) sums at 256, 384
+  // TMEM: accumulators at columns 0, 64, 128, 192; phase-2 (hi, lo) sums at 256, 320
   if (warp == 9) {
     tmem_alloc(&sh.tbase, 512);
     tmem_relinquish();
@@ -279,7 +301,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(&sh.full[i], 1);
       mbar_init(&sh.empty[i], 1);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kTcAcc; ++i) {
       mbar_init(&sh.acc_full[i], 1);
       mbar_init(&sh.acc_empty[i], 8);
     }
@@ -294,39 +316,43 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   volatile int* abort_flag = &sh.abort_flag;
 
   if (warp == 8) {
-    // ---- producer: one thread streams the operand blocks of every item
-    if (lane == 0) {
-      int s = 0;
-      uint32_t ph = 0;
-      int last_par[kTcStages];
-      for (int i = 0; i < kTcStages; ++i) last_par[i] = -1;
-      bool ok = true;
-      for (int tk = rg.x; tk < rg.y && ok; ++tk) {
-        const TcTask T = tasks[order[tk]];
-        const int h_a = min(128, T.a_rows - 128 * T.tm);
-        const int h_b = min(128, T.b_rows - 128 * T.tn);
-        for (int i = T.ibeg; i < T.iend && ok; ++i) {
-          const TcItem it = items[i];
-          const __nv_bfloat16* ah = pick(b.hi, it.a_pool) + it.a_off;
-          const __nv_bfloat16* al = pick(b.lo, it.a_pool) + it.a_off;
-          const __nv_bfloat16* bh = pick(b.hi, it.b_pool) + it.b_off;
-          const __nv_bfloat16* bl = pick(b.lo, it.b_pool) + it.b_off;
-          const int nck = (it.kp + 63) >> 6;
+    // ---- producer: lane 0 streams the operand blocks of every item
+    int s = 0;
+    uint32_t ph = 0;
+    int last_par[kTcStages];
+    for (int i = 0; i < kTcStages; ++i) last_par[i] = -1;
+    bool ok = true;
+    for (int base = rg.x; base < rg.y && ok; base += 32) {
+      WorkRegs r;
+      load_work(work, base + lane, rg.y, r);
+      const int cnt = min(32, rg.y - base);
+      for (int j = 0; j < cnt && ok; ++j) {
+        const int64_t a_base = shfl64(r.q[0].x, r.q[0].y, j);
+        const int64_t b_base = shfl64(r.q[0].z, r.q[0].w, j);
+        const int kp = shfl32(r.q[1].z, j);
+        const int hw = shfl32(r.q[2].x, j);
+        const int pf = shfl32(r.q[3].x, j);
+        if (lane == 0 && !((pf >> 16) & kTcEmpty)) {
+          const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
+          const __nv_bfloat16* ah = pick(b.hi, pf & 0xff) + a_base;
+          const __nv_bfloat16* al = pick(b.lo, pf & 0xff) + a_base;
+          const __nv_bfloat16* bh = pick(b.hi, (pf >> 8) & 0xff) + b_base;
+          const __nv_bfloat16* bl = pick(b.lo, (pf >> 8) & 0xff) + b_base;
+          const int nck = (kp + kTcKC - 1) / kTcKC;
           for (int c = 0; c < nck; ++c) {
             if (!tc_wait(&sh.empty[s], ph ^ 1u, abort_flag, b.status, limit_ns)) {
               ok = false;
               break;
             }
-            const int w = min(64, it.kp - 64 * c);
-            const int64_t ao = tc_block_off(T.a_rows, it.kp, T.tm, c);
-            const int64_t bo = tc_block_off(T.b_rows, it.kp, T.tn, c);
+            const int w = min(kTcKC, kp - kTcKC * c);
+            const int64_t ao = (int64_t)h_a * kTcKC * c, bo = (int64_t)h_b * kTcKC * c;
             const uint32_t abytes = (uint32_t)h_a * w * 2, bbytes = (uint32_t)h_b * w * 2;
             uint8_t* st = smem + s * kTcStageBytes;
             mbar_expect_tx(&sh.full[s], 2 * (abytes + bbytes));
             bulk_g2s(st, ah + ao, abytes, &sh.full[s]);
-            bulk_g2s(st + kTcOperandBytes, al + ao, abytes, &sh.full[s]);
-            bulk_g2s(st + 2 * kTcOperandBytes, bh + bo, bbytes, &sh.full[s]);
-            bulk_g2s(st + 3 * kTcOperandBytes, bl + bo, bbytes, &sh.full[s]);
+            bulk_g2s(st + kTcABytes, al + ao, abytes, &sh.full[s]);
+            bulk_g2s(st + 2 * kTcABytes, bh + bo, bbytes, &sh.full[s]);
+            bulk_g2s(st + 2 * kTcABytes + kTcBBytes, bl + bo, bbytes, &sh.full[s]);
             last_par[s] = (int)ph;
             if (++s == kTcStages) {
               s = 0;
@@ -334,218 +360,237 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
           }
         }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       }
-      if (!ok) {
-        // copies already issued still land in shared memory: wait for them
-        for (int i = 0; i < kTcStages; ++i)
-          if (last_par[i] >= 0) mbar_wait_bounded(&sh.full[i], (uint32_t)last_par[i], limit_ns);
-      }
+    }
+    if (lane == 0 && !ok) {
+      // copies already issued still land in shared memory: wait for them
+      for (int i = 0; i < kTcStages; ++i)
+        if (last_par[i] >= 0) mbar_wait_bounded(&sh.full[i], (uint32_t)last_par[i], limit_ns);
     }
   } else if (warp == 9) {
-    // ---- MMA issuer
-    if (lane == 0) {
-      int s = 0, ab = 0;
-      uint32_t ph = 0, aph = 0;
-      bool ok = true;
-      for (int tk = rg.x; tk < rg.y && ok; ++tk) {
-        const TcTask T = tasks[order[tk]];
-        const int h_a = min(128, T.a_rows - 128 * T.tm);
-        const int h_b = min(128, T.b_rows - 128 * T.tn);
-        const uint32_t idesc = idesc_bf16(128, (h_b + 15) & ~15);
-        for (int i = T.ibeg; i < T.iend && ok; ++i) {
-          const int kp = items[i].kp;
-          if (!tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns)) {
-            ok = false;
-            break;
-          }
-          fence_after_sync();
-          const uint32_t d = tmem + (uint32_t)ab * 128u;
-          const int nck = (kp + 63) >> 6;
-          for (int c = 0; c < nck; ++c) {
-            if (!tc_wait(&sh.full[s], ph, abort_flag, b.status, limit_ns)) {
-              ok = false;
-              break;
-            }
+    // ---- MMA issuer (lane 0)
+    int s = 0, ab = 0;
+    uint32_t ph = 0, aph = 0;
+    bool ok = true;
+    for (int base = rg.x; base < rg.y && ok; base += 32) {
+      WorkRegs r;
+      load_work(work, base + lane, rg.y, r);
+      const int cnt = min(32, rg.y - base);
+      for (int j = 0; j < cnt && ok; ++j) {
+        const int kp = shfl32(r.q[1].z, j);
+        const int hw = shfl32(r.q[2].x, j);
+        const int pf = shfl32(r.q[3].x, j);
+        if (lane == 0 && !((pf >> 16) & kTcEmpty)) {
+          const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
+          const uint32_t idesc = idesc_bf16(128, (h_b + 15) & ~15);
+          if (!tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns)) ok = false;
+          if (ok) {
             fence_after_sync();
-            const int w = min(64, kp - 64 * c);
-            const uint32_t sa = smem_u32(smem + s * kTcStageBytes);
-            for (int j = 0; j < w / 16; ++j) {
-              const uint32_t ao = (uint32_t)(32 * j * h_a), bo = (uint32_t)(32 * j * h_b);
-              const uint64_t a_hi = smem_desc(sa + ao, h_a * 16, 128);
-              const uint64_t a_lo = smem_desc(sa + kTcOperandBytes + ao, h_a * 16, 128);
-              const uint64_t b_hi = smem_desc(sa + 2 * kTcOperandBytes + bo, h_b * 16, 128);
-              const uint64_t b_lo = smem_desc(sa + 3 * kTcOperandBytes + bo, h_b * 16, 128);
-              mma_bf16(d, a_hi, b_hi, idesc, (c > 0 || j > 0) ? 1u : 0u);
-              mma_bf16(d, a_hi, b_lo, idesc, 1u);
-              mma_bf16(d, a_lo, b_hi, idesc, 1u);
+            const uint32_t d = tmem + (uint32_t)ab * 64u;
+            const int nck = (kp + kTcKC - 1) / kTcKC;
+            for (int c = 0; c < nck; ++c) {
+              if (!tc_wait(&sh.full[s], ph, abort_flag, b.status, limit_ns)) {
+                ok = false;
+                break;
+              }
+              fence_after_sync();
+              const int w = min(kTcKC, kp - kTcKC * c);
+              const uint32_t sa = smem_u32(smem + s * kTcStageBytes);
+              for (int jj = 0; jj < w / 16; ++jj) {
+                const uint32_t ao = (uint32_t)(32 * jj * h_a), bo = (uint32_t)(32 * jj * h_b);
+                const uint64_t a_hi = smem_desc(sa + ao, h_a * 16, 128);
+                const uint64_t a_lo = smem_desc(sa + kTcABytes + ao, h_a * 16, 128);
+                const uint64_t b_hi = smem_desc(sa + 2 * kTcABytes + bo, h_b * 16, 128);
+                const uint64_t b_lo = smem_desc(sa + 2 * kTcABytes + kTcBBytes + bo, h_b * 16, 128);
+                mma_bf16(d, a_hi, b_hi, idesc, (c > 0 || jj > 0) ? 1u : 0u);
+                mma_bf16(d, a_hi, b_lo, idesc, 1u);
+                mma_bf16(d, a_lo, b_hi, idesc, 1u);
+              }
+              mma_commit(&sh.empty[s]);
+              if (++s == kTcStages) {
+                s = 0;
+                ph ^= 1u;
+              }
             }
-            mma_commit(&sh.empty[s]);
-            if (++s == kTcStages) {
-              s = 0;
-              ph ^= 1u;
+            if (ok) {
+              mma_commit(&sh.acc_full[ab]);
+              if (++ab == kTcAcc) {
+                ab = 0;
+                aph ^= 1u;
+              }
             }
           }
-          if (!ok) break;
-          mma_commit(&sh.acc_full[ab]);
-          ab ^= 1;
-          if (ab == 0) aph ^= 1u;
         }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       }
     }
-    __syncwarp();
   } else {
-    // ---- epilogue: warp w owns TMEM lanes 32 (w % 4).. and columns 64 (w / 4)..
+    // ---- epilogue: warp w owns TMEM lanes 32 (w % 4).. and columns 32 (w / 4)..
     const int q = warp & 3, half = warp >> 2;
     const int row = 32 * q + lane;
     const uint32_t lane_base = (uint32_t)(32 * q) << 16;
     int ab = 0;
     uint32_t aph = 0;
     bool ok = true;
-    for (int tk = rg.x; tk < rg.y && ok; ++tk) {
-      const TcTask T = tasks[order[tk]];
-      const int h_a = min(128, T.a_rows - 128 * T.tm);
-      const int h_b = min(128, T.b_rows - 128 * T.tn);
-      const int N = (h_b + 15) & ~15;
-      if (PHASE == 2) {
-        // items are summed in f32 registers in groups of kTcGroup; each group
-        // sum is folded into the compensated (hi, lo) pair kept in TMEM
-        // columns 256.. (hi) and 384.. (lo)
-        float acc[64];
+    // phase-2 state of the current task
+    float acc[32];
 #pragma unroll
-        for (int e = 0; e < 64; ++e) acc[e] = 0.f;
-        int gi = 0;
-        bool first = true;
-        const uint32_t vh_t = tmem + 256u + (uint32_t)half * 64u + lane_base;
-        const uint32_t vl_t = tmem + 384u + (uint32_t)half * 64u + lane_base;
-        // add the pending group (if add) and either keep the pair in TMEM or
-        // write the result (last)
-        auto flush = [&](bool add, bool last) {
+    for (int e = 0; e < 32; ++e) acc[e] = 0.f;
+    int gi = 0;
+    bool first = true;
+    const uint32_t vh_t = tmem + kTcVh + (uint32_t)half * 32u + lane_base;
+    const uint32_t vl_t = tmem + kTcVl + (uint32_t)half * 32u + lane_base;
+    for (int base = rg.x; base < rg.y && ok; base += 32) {
+      WorkRegs r;
+      load_work(work, base + lane, rg.y, r);
+      const int cnt = min(32, rg.y - base);
+      for (int j = 0; j < cnt && ok; ++j) {
+        const float alpha = __int_as_float(shfl32(r.q[1].w, j));
+        const int hw = shfl32(r.q[2].x, j);
+        const int pf = shfl32(r.q[3].x, j);
+        const int flags = (pf >> 16) & 0xff;
+        const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
+        const int N = (h_b + 15) & ~15;
+        const int64_t out_base = shfl64(r.q[1].x, r.q[1].y, j);
+        const int vrc = shfl32(r.q[2].y, j);
+        const int out_ld = shfl32(r.q[2].z, j);
+        const int col0 = shfl32(r.q[2].w, j);
+        if (PHASE == 2) {
+          if (flags & kTcFirst) {
+            gi = 0;
+            first = true;
+          }
+          if (!(flags & kTcEmpty)) {
+            ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
+            if (!ok) break;  // TMEM loads below need the whole warp
+            fence_after_sync();
+            const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
 #pragma unroll
-          for (int g = 0; g < 4; ++g) {
-            if (half * 64 + g * 16 < N) {
-              float vh[16], vl[16];
-              if (first) {
+            for (int g = 0; g < 2; ++g) {
+              if (half * 32 + g * 16 < N) {
+                float v[16];
+                tmem_ld16(d + (uint32_t)(g * 16), v);
+                if (gi == 0) {
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                  vh[e] = add ? acc[16 * g + e] : 0.f;
-                  vl[e] = 0.f;
-                }
-              } else {
-                tmem_ld16(vh_t + (uint32_t)(16 * g), vh);
-                tmem_ld16(vl_t + (uint32_t)(16 * g), vl);
-                if (add) {
+                  for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmul_rn(alpha, v[e]);
+                } else {
 #pragma unroll
-                  for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], acc[16 * g + e]);
+                  for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmaf_rn(alpha, v[e], acc[g * 16 + e]);
                 }
               }
-              if (!last) {
-                tmem_st16(vh_t + (uint32_t)(16 * g), vh);
-                tmem_st16(vl_t + (uint32_t)(16 * g), vl);
-              } else if (T.direct) {
-                // the whole tile in this task: FP64 result straight into sigma
-                if (row < T.valid_rows) {
-                  double* out = sigma + T.out_off + (int64_t)(128 * T.tm + row) * T.out_kp + 128 * T.tn;
+            }
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
+            if (++ab == kTcAcc) {
+              ab = 0;
+              aph ^= 1u;
+            }
+            ++gi;
+          }
+          const bool last = (flags & kTcLast) != 0;
+          if (last || gi == kTcGroup) {
+            // fold the pending group into the compensated pair; on the
+            // task's last item write the result
+            const bool add = gi > 0;
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+              if (half * 32 + g * 16 < N) {
+                float vh[16], vl[16];
+                if (first) {
 #pragma unroll
                   for (int e = 0; e < 16; ++e) {
-                    const int col = half * 64 + 16 * g + e;
-                    if (col < T.valid_cols) out[col] = (double)vh[e] + (double)vl[e];
+                    vh[e] = add ? acc[16 * g + e] : 0.f;
+                    vl[e] = 0.f;
+                  }
+                } else {
+                  tmem_ld16(vh_t + (uint32_t)(16 * g), vh);
+                  tmem_ld16(vl_t + (uint32_t)(16 * g), vl);
+                  if (add) {
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], acc[16 * g + e]);
                   }
                 }
-              } else if (row < h_a) {
-                float2* out = b.partials + T.out_off + (int64_t)row * h_b;
+                if (!last) {
+                  tmem_st16(vh_t + (uint32_t)(16 * g), vh);
+                  tmem_st16(vl_t + (uint32_t)(16 * g), vl);
+                } else if (flags & kTcDirect) {
+                  const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
+                  if (row < vrows) {
+                    double* out = sigma + out_base + (int64_t)row * out_ld;
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                  const int col = half * 64 + 16 * g + e;
-                  if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                    for (int e = 0; e < 16; ++e) {
+                      const int col = half * 32 + 16 * g + e;
+                      if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
+                    }
+                  }
+                } else if (row < h_a) {
+                  float2* out = b.partials + out_base + (int64_t)row * h_b;
+#pragma unroll
+                  for (int e = 0; e < 16; ++e) {
+                    const int col = half * 32 + 16 * g + e;
+                    if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                  }
                 }
               }
             }
+            first = false;
+            gi = 0;
           }
-          first = false;
-        };
-        for (int i = T.ibeg; i < T.iend; ++i) {
-          const float alpha = items[i].alpha;
+        } else {
+          // phase 1: one item per task; S tile written as a packed operand
+          // (rows of this tile, K columns col0.. of S)
           ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
-          if (!ok) break;  // TMEM loads below need the whole warp
+          if (!ok) break;
           fence_after_sync();
-          const uint32_t d = tmem + (uint32_t)ab * 128u + (uint32_t)half * 64u + lane_base;
+          const int ncols = min(kTcRowsB, out_ld - col0);
+          const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
+          float v[32];
 #pragma unroll
-          for (int g = 0; g < 4; ++g) {
-            if (half * 64 + g * 16 < N) {
-              float v[16];
-              tmem_ld16(d + (uint32_t)(g * 16), v);
-              if (gi == 0) {
+          for (int g = 0; g < 2; ++g) {
+            if (half * 32 + g * 16 < N) {
+              tmem_ld16(d + (uint32_t)(g * 16), v + 16 * g);
+            } else {
 #pragma unroll
-                for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmul_rn(alpha, v[e]);
-              } else {
-#pragma unroll
-                for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmaf_rn(alpha, v[e], acc[g * 16 + e]);
-              }
+              for (int e = 0; e < 16; ++e) v[16 * g + e] = 0.f;
             }
           }
+          // accumulator read: the MMA issuer may reuse it
           fence_before_sync();
           __syncwarp();
           if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
-          ab ^= 1;
-          if (ab == 0) aph ^= 1u;
-          if (++gi == kTcGroup && i + 1 < T.iend) {
-            flush(true, false);
-            gi = 0;
+          if (++ab == kTcAcc) {
+            ab = 0;
+            aph ^= 1u;
           }
-        }
-        if (!ok) break;
-        flush(gi > 0, true);
-      } else {
-        // phase 1: one item; S tile written as a packed operand (rows of this
-        // tile, K columns 128 tn.. of S)
-        ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
-        if (!ok) break;
-        fence_after_sync();
-        const float alpha = items[T.ibeg].alpha;
-        const int ncols = min(128, T.out_kp - 128 * T.tn);
-        const uint32_t d = tmem + (uint32_t)ab * 128u + (uint32_t)half * 64u + lane_base;
-        __nv_bfloat16* shi = b.hi[kTcPoolS] + T.out_off;
-        __nv_bfloat16* slo = b.lo[kTcPoolS] + T.out_off;
-        float v[64];
+          if (row < h_a) {
+            __nv_bfloat16* shi = b.hi[kTcPoolS] + out_base;
+            __nv_bfloat16* slo = b.lo[kTcPoolS] + out_base;
 #pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          if (half * 64 + g * 16 < N) {
-            tmem_ld16(d + (uint32_t)(g * 16), v + 16 * g);
-          } else {
+            for (int g8 = 0; g8 < 4; ++g8) {
+              const int c0 = half * 32 + 8 * g8;
+              if (c0 < ncols) {
+                uint32_t hw4[4], lw4[4];
 #pragma unroll
-            for (int e = 0; e < 16; ++e) v[16 * g + e] = 0.f;
-          }
-        }
-        // accumulator read: the MMA issuer may reuse it
-        fence_before_sync();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
-        ab ^= 1;
-        if (ab == 0) aph ^= 1u;
-        if (row < h_a) {
-#pragma unroll
-          for (int g8 = 0; g8 < 8; ++g8) {
-            const int c0 = half * 64 + 8 * g8;
-            if (c0 < ncols) {
-              uint32_t hw[4], lw[4];
-#pragma unroll
-              for (int e = 0; e < 8; ++e) {
-                const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
-                __nv_bfloat16 xh, xl;
-                split_bf16(x, xh, xl);
-                const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
-                if (e & 1) {
-                  hw[e >> 1] |= bh << 16;
-                  lw[e >> 1] |= bl << 16;
-                } else {
-                  hw[e >> 1] = bh;
-                  lw[e >> 1] = bl;
+                for (int e = 0; e < 8; ++e) {
+                  const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
+                  __nv_bfloat16 xh, xl;
+                  split_bf16(x, xh, xl);
+                  const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+                  if (e & 1) {
+                    hw4[e >> 1] |= bh << 16;
+                    lw4[e >> 1] |= bl << 16;
+                  } else {
+                    hw4[e >> 1] = bh;
+                    lw4[e >> 1] = bl;
+                  }
                 }
+                const int C = col0 + c0;  // S column
+                const int64_t off = (int64_t)h_a * kTcKC * (C / kTcKC) + (kmajor_off(row, C % kTcKC, h_a) >> 1);
+                *(uint4*)(shi + off) = make_uint4(hw4[0], hw4[1], hw4[2], hw4[3]);
+                *(uint4*)(slo + off) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
               }
-              const int C = 128 * T.tn + c0;  // S column
-              const int64_t off = tc_block_off(T.a_rows, T.out_kp, T.tm, C >> 6) + (kmajor_off(row, C & 63, h_a) >> 1);
-              *(uint4*)(shi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-              *(uint4*)(slo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
           }
         }
@@ -565,17 +610,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
-cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, const int* order,
-                            const int2* ranges, int nblocks, double* sigma, uint64_t limit_ns, cudaStream_t s) {
+cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
+                            double* sigma, uint64_t limit_ns, cudaStream_t s) {
   if (nblocks <= 0) return cudaGetLastError();
   if (phase == 1) {
     cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     if (e != cudaSuccess) return e;
-    tc_sigma_kernel<1><<<nblocks, kTcThreads, kTcSmem, s>>>(b, items, tasks, order, ranges, sigma, limit_ns);
+    tc_sigma_kernel<1><<<nblocks, kTcThreads, kTcSmem, s>>>(b, work, ranges, sigma, limit_ns);
   } else if (phase == 2) {
     cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     if (e != cudaSuccess) return e;
-    tc_sigma_kernel<2><<<nblocks, kTcThreads, kTcSmem, s>>>(b, items, tasks, order, ranges, sigma, limit_ns);
+    tc_sigma_kernel<2><<<nblocks, kTcThreads, kTcSmem, s>>>(b, work, ranges, sigma, limit_ns);
   } else {
     return cudaErrorInvalidValue;
   }

@@ -23,14 +23,19 @@ cudaError_t launch_tc_tile_bulk(const __nv_bfloat16* Ap, const __nv_bfloat16* Bp
 //
 // Packed operand: `rows` (multiple of 8) x `kp` (multiple of 16) bf16 values
 // (hi and lo slices in two pools with the same offsets), cut into row tiles
-// of 128 and K-chunks of 64; block (row tile t, chunk c) is contiguous, starts
-// at element tc_block_off(rows, kp, t, c) and holds its h x w values in the
-// K-major core-matrix order (byte (j/8)*h*16 + (i/8)*128 + (i%8)*16 + (j%8)*2).
-// Rows beyond the operand's own rows and columns beyond its own K are zero.
-__host__ __device__ inline int64_t tc_block_off(int rows, int kp, int t, int c) {
-  const int rest = rows - 128 * t;
-  const int h = rest < 128 ? rest : 128;
-  return (int64_t)128 * t * kp + (int64_t)h * 64 * c;
+// of `rt` rows (128 for operands in the A role, 64 for the B role) and
+// K-chunks of kTcKC columns; block (row tile t, chunk c) is contiguous,
+// starts at element tc_block_off(rows, kp, t, c, rt) and holds its h x w
+// values in the K-major core-matrix order (byte (j/8)*h*16 + (i/8)*128 +
+// (i%8)*16 + (j%8)*2).  Rows beyond the operand's own rows and columns beyond
+// its own K are zero.
+constexpr int kTcKC = 32;
+constexpr int kTcRowsA = 128;  // output tile rows (MMA M)
+constexpr int kTcRowsB = 64;   // output tile columns (MMA N at most)
+__host__ __device__ inline int64_t tc_block_off(int rows, int kp, int t, int c, int rt) {
+  const int rest = rows - rt * t;
+  const int h = rest < rt ? rest : rt;
+  return (int64_t)rt * t * kp + (int64_t)h * kTcKC * c;
 }
 __host__ __device__ inline int tc_round8(int x) { return (x + 7) & ~7; }
 __host__ __device__ inline int tc_round16(int x) { return (x + 15) & ~15; }
@@ -38,10 +43,11 @@ __host__ __device__ inline int tc_round16(int x) { return (x + 15) & ~15; }
 enum : int { kTcPoolL = 0, kTcPoolR = 1, kTcPoolPsi = 2, kTcPoolPsiT = 3, kTcPoolS = 4, kTcPools = 5 };
 
 // One packed operand filled from an FP64 block: view element (r, k) is
-// src[src_off + (trans ? k * ld + r : r * ld + k)] for r < rows_v, k < cols_v.
+// src[src_off + (trans ? k * ld + r : r * ld + k)] for r < rows_v, k < cols_v;
+// row tiles of rt rows.
 struct TcPack {
   int64_t src_off, dst_off;
-  int32_t ld, rows_v, cols_v, rows_p, kp;
+  int32_t ld, rows_v, cols_v, rows_p, kp, rt;
   uint8_t src, pool, trans, pad;
 };
 
@@ -55,12 +61,12 @@ struct TcItem {
 };
 
 // One task: output tile (tm, tn) -- rows 128 tm.. of the A operands, rows
-// 128 tn.. of the B operands -- and the items [ibeg, iend).
+// 64 tn.. of the B operands -- and the items [ibeg, iend).
 //   phase 1 (one item): writes alpha * A B^T as the packed S operand at
 //     out_off of pool S (rows a_rows, K out_kp);
 //   phase 2: sum of the items with a compensated (hi, lo) f32 accumulation;
 //     direct: the FP64 tile (valid_rows x valid_cols) goes to sigma at
-//     out_off + (128 tm + r) * out_kp + 128 tn + c; otherwise the h_a x h_b
+//     out_off + (128 tm + r) * out_kp + 64 tn + c; otherwise the h_a x h_b
 //     (hi, lo) pairs go to partials + out_off for the reduce kernel.
 struct TcTask {
   int32_t a_rows, b_rows;
@@ -78,6 +84,27 @@ struct TcTile {
   int32_t lds, h, w, r0, c0, pbeg, pend, pad;
 };
 
+// One item as the persistent kernel streams it (64 bytes): the items of a
+// block's tasks, flattened in processing order, each carrying what the
+// producer, MMA and epilogue roles need, so that a warp loads 32 of them
+// with one coalesced access and no role chases task -> item pointers.
+//   a_base / b_base: element offsets of the row tile (128 rows of A, 64 of B)
+//   out_base: phase 1: S row-tile base (element, pool S); phase 2 direct:
+//     sigma element of tile (0, 0); phase 2 partial: partial slot (float2)
+//   out_ld: phase 1: kp of S; phase 2 direct: sigma row stride; partial: h_b
+//   col0: phase 1: S column of tile column 0
+enum : uint32_t { kTcFirst = 1, kTcLast = 2, kTcDirect = 4, kTcEmpty = 8 };
+struct __align__(16) TcWork {
+  int64_t a_base, b_base, out_base;
+  int32_t kp;
+  float alpha;
+  int16_t h_a, h_b, valid_rows, valid_cols;
+  int32_t out_ld, col0;
+  uint8_t a_pool, b_pool, flags, pad;
+  int32_t pad2[3];
+};
+static_assert(sizeof(TcWork) == 64, "TcWork is 64 bytes");
+
 struct TcBufs {
   const double* src[3];  // FP64 sources of packing: L arena, R arena, psi
   __nv_bfloat16* hi[kTcPools];
@@ -87,10 +114,10 @@ struct TcBufs {
 };
 
 cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cudaStream_t s);
-// phase 1 or 2 on nblocks persistent blocks: block j runs the tasks
-// order[ranges[j].x .. ranges[j].y); limit_ns bounds every pipeline wait
-cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcItem* items, const TcTask* tasks, const int* order,
-                            const int2* ranges, int nblocks, double* sigma, uint64_t limit_ns, cudaStream_t s);
+// phase 1 or 2 on nblocks persistent blocks: block j runs the work records
+// work[ranges[j].x .. ranges[j].y); limit_ns bounds every pipeline wait
+cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
+                            double* sigma, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
                              cudaStream_t s);
 
