@@ -466,17 +466,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!ok) break;  // TMEM loads below need the whole warp
             fence_after_sync();
             const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
+            const int ng = min(2, max(0, (N - half * 32) >> 4));  // 16-column groups present
+            if (ng > 0) {
+              float v[32];
+              if (ng == 2) tmem_ld32(d, v);
+              else tmem_ld16(d, v);
 #pragma unroll
-            for (int g = 0; g < 2; ++g) {
-              if (half * 32 + g * 16 < N) {
-                float v[16];
-                tmem_ld16(d + (uint32_t)(g * 16), v);
-                if (gi == 0) {
+              for (int g = 0; g < 2; ++g) {
+                if (g < ng) {
+                  if (gi == 0) {
 #pragma unroll
-                  for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmul_rn(alpha, v[e]);
-                } else {
+                    for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmul_rn(alpha, v[g * 16 + e]);
+                  } else {
 #pragma unroll
-                  for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmaf_rn(alpha, v[e], acc[g * 16 + e]);
+                    for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmaf_rn(alpha, v[g * 16 + e], acc[g * 16 + e]);
+                  }
                 }
               }
             }
@@ -505,8 +509,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     vl[e] = 0.f;
                   }
                 } else {
-                  tmem_ld16(vh_t + (uint32_t)(16 * g), vh);
-                  tmem_ld16(vl_t + (uint32_t)(16 * g), vl);
+                  tmem_ld16x2(vh_t + (uint32_t)(16 * g), vl_t + (uint32_t)(16 * g), vh, vl);
                   if (add) {
 #pragma unroll
                     for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], acc[16 * g + e]);
@@ -547,15 +550,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const int ncols = min(kTcRowsB, out_ld - col0);
           const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
           float v[32];
+          const int ng = min(2, max(0, (N - half * 32) >> 4));  // 16-column groups present
 #pragma unroll
-          for (int g = 0; g < 2; ++g) {
-            if (half * 32 + g * 16 < N) {
-              tmem_ld16(d + (uint32_t)(g * 16), v + 16 * g);
-            } else {
-#pragma unroll
-              for (int e = 0; e < 16; ++e) v[16 * g + e] = 0.f;
-            }
-          }
+          for (int e = 0; e < 32; ++e) v[e] = 0.f;
+          if (ng == 2) tmem_ld32(d, v);
+          else if (ng == 1) tmem_ld16(d, v);
           // accumulator read: the MMA issuer may reuse it
           fence_before_sync();
           __syncwarp();
