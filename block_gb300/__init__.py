@@ -60,6 +60,7 @@ _SIGS = {
     "bgpu_profiler_stop": (_I, [_P]),
     "bgpu_tc_tile": (_I, [_P, _P, _P, _P, _I, _I, _I]),
     "bgpu_superblock_info": (_I, [_P, _I, _DP, _I]),
+    "bgpu_set_refine_window": (_I, [_P, ctypes.c_double]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
 }
@@ -261,6 +262,10 @@ class Context:
     INFO_KEYS = ("flops", "bytes", "tc_mma_flops", "tc_phase1_tasks", "tc_phase2_tasks", "tc_phase2_items",
                  "tc_phase2_stage1_items", "tc_split_tiles", "tc_pool_L", "tc_pool_R", "tc_pool_psi",
                  "tc_pool_S", "fp64_stage1_units", "fp64_items")
+
+    def set_refine_window(self, eh):
+        """FP64 energy refinement window of split-precision sweeps (Eh)."""
+        self._check(self.lib.bgpu_set_refine_window(self.h, float(eh)))
 
     def superblock_info(self, sb):
         """Work-list statistics of one sigma (see bgpu_superblock_info)."""

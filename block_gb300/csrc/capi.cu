@@ -20,6 +20,7 @@ struct bgpu_ctx {
   std::unique_ptr<GpuEngine> eng;
   std::string err;
   int device = 0;
+  double refine_window = 1e-3;  // Eh; see bgpu_set_refine_window
   struct BlockRec {
     Block b;
     std::vector<OpKey> decl;  // declaration order
@@ -101,6 +102,13 @@ int bgpu_destroy(bgpu_ctx* ctx) {
 }
 
 const char* bgpu_last_error_string(const bgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bgpu_set_refine_window(bgpu_ctx* ctx, double eh) {
+  return guarded(ctx, [&] {
+    need(eh >= 0.0, "refine window must be >= 0");
+    ctx->refine_window = eh;
+  });
+}
 
 int bgpu_set_precision(bgpu_ctx* ctx, int p) {
   return guarded(ctx, [&] {
@@ -481,6 +489,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     Integrals I = load_integrals(c);
     DriverOptions opt;
     opt.verbose = verbose;
+    if (precision_slices(ctx->eng->precision)) opt.refine_window = ctx->refine_window;
     const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops, p0 = ctx->eng->plan_seconds;
     const long c0 = ctx->eng->sigma_calls;
     SweepResult r;

@@ -1388,30 +1388,47 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     if (iter >= p.max_iter) break;
   }
   energies.assign(lam.begin(), lam.begin() + nroots);
-  if (precision_slices(precision)) {
-    // defect correction: energies of the split-precision Ritz vectors from one
-    // FP64 product each (Rayleigh quotient, second order in the vector error)
-    for (int rr = 0; rr < nroots; ++rr) {
-      auto t0 = std::chrono::steady_clock::now();
-      sigma(sb, plan_, row(B, rr), r);
-      energies[rr] = dot(row(B, rr), r);
-      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-      sigma_seconds += dt;
-      fp64_seconds += dt;
-      ++fp64_calls;
-    }
-  }
   if (waves_) free(waves_);
   waves_ = alloc((int64_t)nroots * n);
   cuda_check(cudaMemcpyAsync(waves_, B, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "waves");
   wave_n_ = n;
   nwaves_ = nroots;
+  if (precision_slices(precision) && !p.defer_refine) refine(sb, energies);
   for (double* q : {diag, B, S, T, r, c0, work, red, hmat, hvec, hw}) free(q);
   cudaFreeAsync(offs, stream_);
   cudaFreeAsync(dims, stream_);
   cudaFreeAsync(status, stream_);
   sync();
   return iter;
+}
+
+// Defect correction: energies of the split-precision Ritz vectors from one
+// FP64 product each (Rayleigh quotient, second order in the vector error).
+bool GpuEngine::refine(const Superblock& sb, std::vector<double>& energies) {
+  if (!precision_slices(precision) || !have_plan_ || !waves_) return false;
+  const int64_t n = wave_n_;
+  double* r = alloc(n);
+  double* work = alloc((int64_t)dev::kGramBlocks);
+  double* red = alloc(8);
+  for (int rr = 0; rr < nwaves_ && rr < (int)energies.size(); ++rr) {
+    auto t0 = std::chrono::steady_clock::now();
+    const double* b = waves_ + (int64_t)rr * n;
+    sigma(sb, plan_, b, r);
+    cuda_check(dev::launch_gram(b, 1, r, 1, n, n, work, red, stream_), "dot");
+    double h;
+    cuda_check(cudaMemcpyAsync(&h, red, sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
+    energies[rr] = h;
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    sigma_seconds += dt;
+    fp64_seconds += dt;
+    ++fp64_calls;
+  }
+  free(r);
+  free(work);
+  free(red);
+  sync();
+  return true;
 }
 
 // ------------------------------------------------------------------ density

@@ -94,6 +94,7 @@ class GpuEngine : public Engine {
   void build_block(Block& big, const Block& a, const Block& b,
                    const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) override;
   int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) override;
+  bool refine(const Superblock& sb, std::vector<double>& energies) override;
   void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;

@@ -357,7 +357,20 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   dp.deflation_min = C_.deflation_min;
   dp.deflation_max = C_.deflation_max;
   dp.seed = C_.seed + 104729ull * (uint64_t)(sweep_index * N_ + p);
+  dp.defer_refine = opt_.refine_window > 0.0;
   const int iters = E_.solve(sb, dp, energies);
+  char prec_tag[64] = "";
+  if (dp.defer_refine && !energies.empty()) {
+    const bool last_step = forward ? (p == N_ - 3) : (p == 1);
+    const double e_unrefined = energies[0];
+    if (last_step || e_unrefined <= sweep_best_unrefined_ + opt_.refine_window) {
+      if (E_.refine(sb, energies))
+        std::snprintf(prec_tag, sizeof(prec_tag), " (refined; unrefined %+.3e)", e_unrefined - energies[0]);
+    } else {
+      std::snprintf(prec_tag, sizeof(prec_tag), " (unrefined)");
+    }
+    sweep_best_unrefined_ = std::min(sweep_best_unrefined_, e_unrefined);
+  }
   phase_.solve_seconds += secs(t0);
   if (opt_.on_step) opt_.on_step(sb, sweep_index, p);
   t0 = clk::now();
@@ -377,8 +390,9 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
     right_[p + 1] = renormalised(R, kept, keepspec);
   }
   phase_.renorm_seconds += secs(t0);
-  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f  disc=%.3e\n", forward ? "fwd" : "bwd", p,
-      L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], disc);
+  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f%s  disc=%.3e\n", forward ? "fwd" : "bwd", p,
+      L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], prec_tag,
+      disc);
   E_.release_block(L);
   E_.release_block(R);
   return disc;
@@ -388,6 +402,7 @@ double SweepDriver::sweep(bool forward, int sweep_index) {
   std::vector<double> best;
   double emin = std::numeric_limits<double>::infinity();
   double maxdisc = 0.0;
+  sweep_best_unrefined_ = std::numeric_limits<double>::infinity();
   auto one = [&](int p) {
     std::vector<double> e;
     maxdisc = std::max(maxdisc, step(forward, p, sweep_index, e));

@@ -49,6 +49,9 @@ struct DavidsonParams {
   int max_iter = 200;
   int deflation_min = 2, deflation_max = 20;
   uint64_t seed = 1;
+  // engines that iterate in a split precision: leave the FP64 Rayleigh-quotient
+  // refinement of the energies to a later refine() call
+  bool defer_refine = false;
 };
 
 // Density-matrix spectrum of the block being renormalised: per sector of
@@ -72,6 +75,13 @@ class Engine {
   // Davidson on the superblock; energies of the converged roots.  The
   // wavefunctions stay inside the engine.
   virtual int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) = 0;
+  // FP64 Rayleigh quotients of the last solve's vectors (no-op for engines
+  // that solve in FP64); returns true if the energies changed precision
+  virtual bool refine(const Superblock& sb, std::vector<double>& energies) {
+    (void)sb;
+    (void)energies;
+    return false;
+  }
   // reduced density matrix of the left (forward) or right (backward) block
   // from the engine's current wavefunctions and its eigen-decomposition.
   virtual void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) = 0;
@@ -99,6 +109,10 @@ struct SweepResult {
 
 struct DriverOptions {
   int verbose = 0;
+  // > 0: defer the FP64 energy refinement of split-precision solves and
+  // refine only steps whose unrefined lowest energy is within this many Eh
+  // of the sweep's lowest so far, and every sweep's last step
+  double refine_window = 0.0;
   // optional hooks for tests: called after each superblock solve
   std::function<void(const Superblock&, int sweep, int step)> on_step;
 };
@@ -153,6 +167,7 @@ class SweepDriver {
   std::vector<double> last_energies_;
   double last_discarded_ = 0.0;
   SweepResult phase_;  // accumulates the per-phase wall times
+  double sweep_best_unrefined_ = 0.0;
 };
 
 }  // namespace bgpu

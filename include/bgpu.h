@@ -71,6 +71,12 @@ const char* bgpu_last_error_string(const bgpu_ctx* ctx);
 const char* bgpu_version(void);
 /* Arithmetic of sigma products (BGPU_PREC_*). */
 int bgpu_set_precision(bgpu_ctx* ctx, int precision);
+/* Split-precision sweeps (no reference counterpart): bgpu_run_dmrg refines
+ * a step's energies with FP64 Rayleigh quotients only when its unrefined
+ * lowest energy is within `eh` of the lowest one seen so far in the sweep,
+ * and always at the last step of every sweep (so that sweep and final
+ * energies are FP64-refined).  0 refines every step.  Default 1e-3 Eh. */
+int bgpu_set_refine_window(bgpu_ctx* ctx, double eh);
 
 /*
  * Declare a block: its state space and operator catalogue.
