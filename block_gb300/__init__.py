@@ -61,6 +61,7 @@ _SIGS = {
     "bgpu_tc_tile": (_I, [_P, _P, _P, _P, _I, _I, _I]),
     "bgpu_superblock_info": (_I, [_P, _I, _DP, _I]),
     "bgpu_set_refine_window": (_I, [_P, ctypes.c_double]),
+    "bgpu_tc_wait_selftest": (_I, [_P, ctypes.c_double, _IP, _IP, _DP]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
 }
@@ -262,6 +263,15 @@ class Context:
     INFO_KEYS = ("flops", "bytes", "tc_mma_flops", "tc_phase1_tasks", "tc_phase2_tasks", "tc_phase2_items",
                  "tc_phase2_stage1_items", "tc_split_tiles", "tc_pool_L", "tc_pool_R", "tc_pool_psi",
                  "tc_pool_S", "fp64_stage1_units", "fp64_items")
+
+    def tc_wait_selftest(self, limit_ms=20.0):
+        """Bounded mbarrier wait on a barrier nothing arrives at: returns
+        (gave_up, status, waited_ms)."""
+        g = np.zeros(1, dtype=np.int32)
+        st = np.zeros(1, dtype=np.int32)
+        w = np.zeros(1)
+        self._check(self.lib.bgpu_tc_wait_selftest(self.h, float(limit_ms), _ip(g), _ip(st), _dp(w)))
+        return int(g[0]), int(st[0]), float(w[0])
 
     def set_refine_window(self, eh):
         """FP64 energy refinement window of split-precision sweeps (Eh)."""

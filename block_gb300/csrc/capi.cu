@@ -303,6 +303,27 @@ int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi, double* sigma, in
   });
 }
 
+int bgpu_tc_wait_selftest(bgpu_ctx* ctx, double limit_ms, int* gave_up, int* status, double* waited_ms) {
+  return guarded(ctx, [&] {
+    need(limit_ms > 0 && limit_ms <= 1000 && gave_up && status && waited_ms, "bad arguments");
+    cudaStream_t s = ctx->eng->stream();
+    int* st = nullptr;
+    unsigned long long* out = nullptr;
+    cuda_check(cudaMallocAsync((void**)&st, sizeof(int), s), "alloc");
+    cuda_check(cudaMallocAsync((void**)&out, 2 * sizeof(unsigned long long), s), "alloc");
+    cuda_check(cudaMemsetAsync(st, 0, sizeof(int), s), "memset");
+    cuda_check(dev::launch_tc_wait_selftest(st, out, (uint64_t)(limit_ms * 1e6), s), "wait selftest");
+    unsigned long long h[2] = {0, 0};
+    cuda_check(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s), "d2h");
+    cuda_check(cudaMemcpyAsync(status, st, sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
+    cudaFreeAsync(st, s);
+    cudaFreeAsync(out, s);
+    ctx->eng->sync();
+    *gave_up = (int)h[0];
+    *waited_ms = (double)h[1] * 1e-6;
+  });
+}
+
 int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
   return guarded(ctx, [&] {
     auto it = ctx->sbs.find(sb);

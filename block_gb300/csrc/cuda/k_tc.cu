@@ -648,5 +648,30 @@ cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t
   return cudaGetLastError();
 }
 
+// Waits on an mbarrier that nothing arrives at, through the same bounded
+// wait the sigma kernels use; the wait must give up after limit_ns and set
+// *status.  out[0] = 1 if the wait reported failure, out[1] = elapsed ns.
+__global__ void tc_wait_selftest_kernel(int* status, unsigned long long* out, uint64_t limit_ns) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint64_t t0 = globaltimer_ns();
+    const bool ok = tc_wait(&bar, 0, &abort_flag, status, limit_ns);
+    out[0] = ok ? 0ull : 1ull;
+    out[1] = globaltimer_ns() - t0;
+  }
+}
+
+cudaError_t launch_tc_wait_selftest(int* status, unsigned long long* out, uint64_t limit_ns, cudaStream_t s) {
+  tc_wait_selftest_kernel<<<1, 32, 0, s>>>(status, out, limit_ns);
+  return cudaGetLastError();
+}
+
 }  // namespace dev
 }  // namespace bgpu

@@ -118,6 +118,10 @@ cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cud
 // work[ranges[j].x .. ranges[j].y); limit_ns bounds every pipeline wait
 cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
                             double* sigma, uint64_t limit_ns, cudaStream_t s);
+// Bounded-wait self-check: one thread waits, with the sigma kernels' wait,
+// on an mbarrier that nothing arrives at; out[0] = 1 when the wait gave up,
+// out[1] = nanoseconds waited; *status is set by the wait.
+cudaError_t launch_tc_wait_selftest(int* status, unsigned long long* out, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
                              cudaStream_t s);
 

@@ -118,6 +118,12 @@ int bgpu_superblock_define(bgpu_ctx* ctx, int left, int right, const int* target
 int bgpu_superblock_free(bgpu_ctx* ctx, int sb);
 /* Algorithmic work of one sigma: FP64-equivalent flops and bytes. */
 int bgpu_superblock_work(bgpu_ctx* ctx, int sb, double* flops, double* bytes);
+/* Bounded-wait self-check of the tensor-core kernels (no reference
+ * counterpart): one GPU thread waits, with the kernels' own bounded mbarrier
+ * wait, on a barrier that nothing arrives at, for limit_ms (0 < limit_ms <=
+ * 1000).  gave_up = 1 when the wait returned failure, status = the status
+ * word the wait sets, waited_ms = time spent waiting. */
+int bgpu_tc_wait_selftest(bgpu_ctx* ctx, double limit_ms, int* gave_up, int* status, double* waited_ms);
 /* Work-list statistics of one sigma (no reference counterpart), info[n]:
  *   FP64-equivalent flops, algorithmic bytes, tensor-core flops issued by the
  *   tcgen05 path (3 bf16 products, padded tiles), phase-1 tasks, phase-2

@@ -25,3 +25,16 @@ def test_tc_tile_matches_host_product(gpu_ctx, n, k, packed):
     # f32 accumulation of k exact bf16 x bf16 products
     err = np.abs(d - ref).max() / np.abs(ref).max()
     assert err < 1e-6, err
+
+
+def test_bounded_wait_gives_up_and_reports(gpu_ctx):
+    """The pipeline wait of the tensor-core kernels, on a barrier nothing
+    arrives at, returns failure after its limit and sets the status word
+    (the host-side check that turns it into an error); the context stays
+    usable afterwards."""
+    gave_up, status, waited = gpu_ctx.tc_wait_selftest(20.0)
+    assert gave_up == 1 and status == 1
+    assert 19.0 <= waited < 1000.0, waited
+    a_bits = np.zeros((128, 16), dtype=np.uint16)
+    b_bits = np.zeros((16, 16), dtype=np.uint16)
+    assert np.all(gpu_ctx.tc_tile(a_bits, b_bits) == 0.0)
