@@ -154,12 +154,30 @@ def conf_M(conf):
     return None
 
 
+def conf_model(conf):
+    """(norb, nelec, nchol, seed, group) of a dmrg.conf whose orbitals line
+    names a generated Hamiltonian, else None."""
+    for line in open(conf):
+        t = line.split()
+        if len(t) >= 2 and t[0] == "orbitals" and t[1].startswith("synthetic:"):
+            f = t[1].split(":")
+            return int(f[1]), int(f[2]), int(f[3]), int(f[4]), ("D2h" if len(f) > 5 and f[5] == "1" else "C1")
+    return None
+
+
 def config_dict(conf, partition, n, prec, arena_mb):
     M = conf_M(conf)
-    return {"workload": "sigma = H psi at the middle bond (L=[0..%d]) of the synthetic 24-orbital/24-electron "
-                        "Cholesky Hamiltonian (48 vectors, seed 24, S=0, C1), blocks renormalised to M=%s"
-                        % (partition, M),
-            "conf": os.path.relpath(conf, ROOT), "norb": 24, "nelec": 24, "M": M, "partition": partition,
+    model = conf_model(conf)
+    if model:
+        norb, nelec, nchol, seed, grp = model
+        what = ("the synthetic %d-orbital/%d-electron Cholesky Hamiltonian (%d vectors, seed %d, S=0, %s)"
+                % (norb, nelec, nchol, seed, grp))
+    else:
+        norb = nelec = None
+        what = "the Hamiltonian of %s" % os.path.relpath(conf, ROOT)
+    return {"workload": "sigma = H psi at the middle bond (L=[0..%d]) of %s, blocks renormalised to M=%s"
+                        % (partition, what, M),
+            "conf": os.path.relpath(conf, ROOT), "norb": norb, "nelec": nelec, "M": M, "partition": partition,
             "psi_elems": n, "precision": prec,
             "l2": "inputs larger than L2: operator arenas %.0f MB per step" % arena_mb}
 

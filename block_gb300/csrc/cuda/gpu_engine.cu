@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
@@ -584,9 +585,8 @@ void GpuEngine::free_plan(SigmaPlan& p) {
   p.partials = nullptr;
   p.fused = false;
   for (int i = 0; i < dev::kTcPools; ++i) {
-    if (p.tc_hi[i]) cudaFreeAsync(p.tc_hi[i], stream_);
-    if (p.tc_lo[i]) cudaFreeAsync(p.tc_lo[i], stream_);
-    p.tc_hi[i] = p.tc_lo[i] = nullptr;
+    if (p.tc_pool[i]) cudaFreeAsync(p.tc_pool[i], stream_);
+    p.tc_pool[i] = nullptr;
     p.tc_pool_elems[i] = 0;
   }
   p.tc_psi_pack.release(stream_);
@@ -818,7 +818,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     p.src = (uint8_t)pool;  // 0: L arena, 1: R arena
     p.pool = (uint8_t)pool;
     p.dst_off = pool_n[pool];
-    pool_n[pool] += (int64_t)p.rows_p * p.kp;
+    pool_n[pool] += 2 * (int64_t)p.rows_p * p.kp;  // hi and lo
     dims[pool][p.dst_off] = {p.rows_p, p.kp};
     ops_packs.push_back(p);
     m.emplace(key, p.dst_off);
@@ -838,7 +838,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     a.kp = tc_round16(S.cols);
     a.rt = kTcRowsA;
     a.dst_off = psi_off[s] = pool_n[kTcPoolPsi];
-    pool_n[kTcPoolPsi] += (int64_t)a.rows_p * a.kp;
+    pool_n[kTcPoolPsi] += 2 * (int64_t)a.rows_p * a.kp;
     dims[kTcPoolPsi][a.dst_off] = {a.rows_p, a.kp};
     psi_packs.push_back(a);
     TcPack t = a;
@@ -850,12 +850,13 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     t.kp = tc_round16(S.rows);
     t.rt = kTcRowsB;
     t.dst_off = psit_off[s] = pool_n[kTcPoolPsiT];
-    pool_n[kTcPoolPsiT] += (int64_t)t.rows_p * t.kp;
+    pool_n[kTcPoolPsiT] += 2 * (int64_t)t.rows_p * t.kp;
     dims[kTcPoolPsiT][t.dst_off] = {t.rows_p, t.kp};
     psi_packs.push_back(t);
   }
   std::vector<TcItem> i1;
   std::vector<TcTask> t1;
+  std::unordered_map<int64_t, int> s_unit_item;  // S offset -> its phase-1 item
   std::vector<std::vector<TcItem>> per_sector(nsec);
   double mma = 0.0;
   for (auto& cl : per_t) {
@@ -888,7 +889,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         const int mr = L.si.states[c.lQ], mc = R.si.states[c.rQp], k1 = L.si.states[c.lQp];
         const int rows_p = tc_round8(mr), skp = tc_round16(mc);
         cur_s = pool_n[kTcPoolS];
-        pool_n[kTcPoolS] += (int64_t)rows_p * skp;
+        pool_n[kTcPoolS] += 2 * (int64_t)rows_p * skp;
+        s_unit_item[cur_s] = (int)i1.size();
         dims[kTcPoolS][cur_s] = {rows_p, skp};
         TcItem a{};
         a.a_pool = kTcPoolL;
@@ -926,6 +928,24 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       it.alpha = (float)(c.f * c.vb.scale);
       per_sector[c.vs].push_back(it);
     }
+  }
+  // alpha of a stage-1 product read by exactly one item moves into phase 1,
+  // so that such items (alpha = 1) can share a tensor-core accumulator
+  {
+    std::unordered_map<int64_t, int> consumers;
+    for (auto& v : per_sector)
+      for (const TcItem& it : v)
+        if (it.a_pool == kTcPoolS) ++consumers[it.a_off];
+    for (auto& v : per_sector)
+      for (TcItem& it : v)
+        if (it.a_pool == kTcPoolS && consumers[it.a_off] == 1) {
+          TcItem& u = i1[s_unit_item.at(it.a_off)];
+          u.alpha = (float)((double)u.alpha * (double)it.alpha);
+          it.alpha = 1.0f;
+        }
+    // items with alpha = 1 first, so that they form long accumulation runs
+    for (auto& v : per_sector)
+      std::stable_partition(v.begin(), v.end(), [](const TcItem& it) { return it.alpha == 1.0f; });
   }
   // phase 2: sector tiles; a tile whose items cost more than a block's fair
   // share is split into several tasks summed by the reduce kernel, every
@@ -1040,14 +1060,22 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   for (int i = 0; i < kTcPools; ++i) {
     plan.tc_pool_elems[i] = pool_n[i];
     const size_t bytes = (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16);
-    cuda_check(cudaMallocAsync((void**)&plan.tc_hi[i], bytes, stream_), "tc pool");
-    cuda_check(cudaMallocAsync((void**)&plan.tc_lo[i], bytes, stream_), "tc pool");
+    cuda_check(cudaMallocAsync((void**)&plan.tc_pool[i], bytes, stream_), "tc pool");
   }
   cuda_check(cudaMallocAsync((void**)&plan.tc_partials, (size_t)std::max<int64_t>(partial_n, 1) * sizeof(float2),
                              stream_),
              "tc partials");
   plan.tc_psi_pack.upload(psi_packs, stream_);
-  // flatten every block's tasks into its stream of work records
+  // flatten every block's tasks into its stream of work records; within a
+  // task, runs of items with alpha = 1 form accumulation groups of at most
+  // kGroupItems items and kGroupK summed K (f32 accumulation length)
+  // BGPU_TC_GROUP overrides the item limit (tuning)
+  static const int kGroupItems = [] {
+    const char* e = std::getenv("BGPU_TC_GROUP");
+    const int v = e ? std::atoi(e) : 0;
+    return v > 0 ? v : 16;
+  }();
+  constexpr int kGroupK = 1024;
   auto flatten = [&](int phase, const std::vector<TcTask>& tasks, const std::vector<TcItem>& items,
                      const std::vector<int>& order, const std::vector<int2>& ranges, std::vector<TcWork>& w,
                      std::vector<int2>& wr) {
@@ -1063,7 +1091,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         base.valid_rows = (int16_t)T.valid_rows;
         base.valid_cols = (int16_t)T.valid_cols;
         if (phase == 1) {
-          base.out_base = T.out_off + (int64_t)kTcRowsA * T.tm * T.out_kp;
+          base.out_base = T.out_off + 2 * (int64_t)kTcRowsA * T.tm * T.out_kp;
           base.out_ld = T.out_kp;
           base.col0 = kTcRowsB * T.tn;
         } else if (T.direct) {
@@ -1080,16 +1108,28 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           w.push_back(x);
           continue;
         }
+        int gn = 0, gk = 0;  // items and K in the open group
         for (int i = T.ibeg; i < T.iend; ++i) {
           const TcItem& it = items[i];
           TcWork x = base;
-          x.a_base = it.a_off + (int64_t)kTcRowsA * T.tm * it.kp;
-          x.b_base = it.b_off + (int64_t)kTcRowsB * T.tn * it.kp;
+          x.a_base = it.a_off + 2 * (int64_t)kTcRowsA * T.tm * it.kp;
+          x.b_base = it.b_off + 2 * (int64_t)kTcRowsB * T.tn * it.kp;
           x.kp = it.kp;
           x.alpha = it.alpha;
           x.a_pool = it.a_pool;
           x.b_pool = it.b_pool;
-          x.flags = (uint8_t)(f0 | (i == T.ibeg ? kTcFirst : 0) | (i + 1 == T.iend ? kTcLast : 0));
+          uint32_t f = f0 | (i == T.ibeg ? kTcFirst : 0) | (i + 1 == T.iend ? kTcLast : 0);
+          const bool foldable = phase == 2 && it.alpha == 1.0f;
+          if (gn == 0) f |= kTcGStart;
+          ++gn;
+          gk += it.kp;
+          const bool next_joins = foldable && i + 1 < T.iend && items[i + 1].alpha == 1.0f && gn < kGroupItems &&
+                                  gk + items[i + 1].kp <= kGroupK;
+          if (!next_joins) {
+            f |= kTcGEnd;
+            gn = gk = 0;
+          }
+          x.flags = (uint8_t)f;
           w.push_back(x);
         }
       }
@@ -1120,8 +1160,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   b.src[0] = arena(L);
   b.src[1] = arena(R);
   for (int i = 0; i < kTcPools; ++i) {
-    b.hi[i] = plan.tc_hi[i];
-    b.lo[i] = plan.tc_lo[i];
+    b.pool[i] = plan.tc_pool[i];
   }
   cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
   dops.release(stream_);
@@ -1136,8 +1175,7 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   b.src[1] = arena(*sb.R);
   b.src[2] = psi;
   for (int i = 0; i < dev::kTcPools; ++i) {
-    b.hi[i] = p.tc_hi[i];
-    b.lo[i] = p.tc_lo[i];
+    b.pool[i] = p.tc_pool[i];
   }
   b.partials = p.tc_partials;
   b.status = tc_status_;

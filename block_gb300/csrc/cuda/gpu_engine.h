@@ -67,8 +67,7 @@ struct SigmaPlan {
   // pools (built on first use): L / R operator blocks packed once, psi and
   // psi^T packed per product, S = stage-1 products written by phase 1
   bool tc = false;
-  __nv_bfloat16* tc_hi[dev::kTcPools] = {};
-  __nv_bfloat16* tc_lo[dev::kTcPools] = {};
+  __nv_bfloat16* tc_pool[dev::kTcPools] = {};  // packed operands, hi and lo per block
   int64_t tc_pool_elems[dev::kTcPools] = {};
   DevArray<dev::TcPack> tc_psi_pack;
   DevArray<dev::TcWork> tc_w1, tc_w2;  // work records of phases 1 and 2, grouped by block

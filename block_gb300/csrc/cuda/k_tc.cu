@@ -164,13 +164,12 @@ __device__ __forceinline__ T pick(const T (&p)[N], int i) {
 
 // Packs FP64 blocks into split bf16 operands.  Each thread writes one
 // 16-byte core-matrix row (8 consecutive K values of one operand row) of the
-// hi and lo pools; for transposed views consecutive threads take consecutive
-// rows so that the FP64 reads stay coalesced.
+// hi and of the lo slice; for transposed views consecutive threads take
+// consecutive rows so that the FP64 reads stay coalesced.
 __global__ void __launch_bounds__(256) tc_pack_kernel(TcBufs b, const TcPack* __restrict__ units) {
   const TcPack u = units[blockIdx.x];
   const double* src = pick(b.src, u.src) + u.src_off;
-  __nv_bfloat16* hi = pick(b.hi, u.pool) + u.dst_off;
-  __nv_bfloat16* lo = pick(b.lo, u.pool) + u.dst_off;
+  __nv_bfloat16* dst = pick(b.pool, u.pool) + u.dst_off;
   const int kg = u.kp >> 3;
   const int64_t total = (int64_t)u.rows_p * kg;
   for (int64_t g = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.y * blockDim.x) {
@@ -202,9 +201,10 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(TcBufs b, const TcPack* __
     const int t = r / u.rt, c = k0 / kTcKC;
     const int rest = u.rows_p - u.rt * t;
     const int h = rest < u.rt ? rest : u.rt;
-    const int64_t off = tc_block_off(u.rows_p, u.kp, t, c, u.rt) + (kmajor_off(r - u.rt * t, k0 % kTcKC, h) >> 1);
-    *(uint4*)(hi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-    *(uint4*)(lo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+    const int w = min(kTcKC, u.kp - kTcKC * c);
+    const int64_t off = 2 * tc_block_off(u.rows_p, u.kp, t, c, u.rt) + (kmajor_off(r - u.rt * t, k0 % kTcKC, h) >> 1);
+    *(uint4*)(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *(uint4*)(dst + off + (int64_t)h * w) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
 }
 
@@ -215,18 +215,15 @@ cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cud
 
 namespace {
 
-constexpr int kTcStages = 8;
-constexpr uint32_t kTcABytes = kTcRowsA * kTcKC * 2;  // one slice of an A block
-constexpr uint32_t kTcBBytes = kTcRowsB * kTcKC * 2;  // one slice of a B block
-constexpr uint32_t kTcStageBytes = 2 * kTcABytes + 2 * kTcBBytes;
+constexpr int kTcSlots = 8;  // stages of the operand ring
+// one stage holds the largest piece: A (128 rows) and B (64 rows) x 32 columns, hi and lo
+constexpr uint32_t kTcStageBytes = 2u * (kTcRowsA + kTcRowsB) * kTcKC * 2;
 constexpr int kTcThreads = 320;  // warps 0-7 epilogue, 8 bulk-copy producer, 9 MMA issuer
-constexpr int kTcSmem = kTcStages * kTcStageBytes;
-constexpr int kTcAcc = 4;     // accumulators of 64 TMEM columns
-constexpr int kTcGroup = 8;   // phase-2 items summed in f32 before the compensated fold
-constexpr uint32_t kTcVh = 256, kTcVl = 320;  // TMEM columns of the compensated sums
+constexpr int kTcSmem = kTcSlots * kTcStageBytes;
+constexpr int kTcAcc = 8;        // accumulators of 64 TMEM columns
 
 struct TcShared {
-  uint64_t full[kTcStages], empty[kTcStages], acc_full[kTcAcc], acc_empty[kTcAcc], drain;
+  uint64_t full[kTcSlots], empty[kTcSlots], acc_full[kTcAcc], acc_empty[kTcAcc], drain;
   uint32_t tbase;
   int abort_flag;
 };
@@ -279,10 +276,12 @@ __device__ __forceinline__ int shfl32(int v, int j) { return __shfl_sync(0xfffff
 
 // Grouped split-precision GEMM over packed operands on tcgen05: per K=16
 // step three MMAs (hi*hi + hi*lo + lo*hi) into an f32 TMEM accumulator of
-// 128 x 64 (four accumulators rotate between items), operand blocks streamed
-// by bulk copies through an 8-stage shared-memory ring.  Persistent: block j
-// walks the work records [ranges[j].x, ranges[j].y), each role loading them
-// 32 at a time, and the pipeline runs across task boundaries.
+// 128 x 64; the items of an accumulation group share the accumulator, eight
+// accumulators rotate between groups.  Operand pieces are streamed by bulk
+// copies through an 8-stage shared-memory ring.  Persistent: block j walks the work records [ranges[j].x,
+// ranges[j].y), each role loading them 32 at a time, and the pipeline runs
+// across task boundaries.  The epilogue folds each group sum into a
+// compensated (hi, lo) f32 pair held in registers.
 template <int PHASE>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_sigma_kernel(TcBufs b, const TcWork* __restrict__ work, const int2* __restrict__ ranges,
@@ -291,13 +290,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __shared__ TcShared sh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int2 rg = ranges[blockIdx.x];
-  // TMEM: accumulators at columns 0, 64, 128, 192; phase-2 (hi, lo) sums at 256, 320
+  // TMEM: eight accumulators of 64 columns
   if (warp == 9) {
     tmem_alloc(&sh.tbase, 512);
     tmem_relinquish();
   }
   if (tid == 0) {
-    for (int i = 0; i < kTcStages; ++i) {
+    for (int i = 0; i < kTcSlots; ++i) {
       mbar_init(&sh.full[i], 1);
       mbar_init(&sh.empty[i], 1);
     }
@@ -316,11 +315,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   volatile int* abort_flag = &sh.abort_flag;
 
   if (warp == 8) {
-    // ---- producer: lane 0 streams the operand blocks of every item
-    int s = 0;
-    uint32_t ph = 0;
-    int last_par[kTcStages];
-    for (int i = 0; i < kTcStages; ++i) last_par[i] = -1;
+    // ---- producer: lane 0 streams the operand pieces (one K-chunk of one
+    // item: A hi, A lo, B hi, B lo) of every item through the stages
+    uint32_t k = 0;  // pieces issued
     bool ok = true;
     for (int base = rg.x; base < rg.y && ok; base += 32) {
       WorkRegs r;
@@ -334,30 +331,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int pf = shfl32(r.q[3].x, j);
         if (lane == 0 && !((pf >> 16) & kTcEmpty)) {
           const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
-          const __nv_bfloat16* ah = pick(b.hi, pf & 0xff) + a_base;
-          const __nv_bfloat16* al = pick(b.lo, pf & 0xff) + a_base;
-          const __nv_bfloat16* bh = pick(b.hi, (pf >> 8) & 0xff) + b_base;
-          const __nv_bfloat16* bl = pick(b.lo, (pf >> 8) & 0xff) + b_base;
+          const __nv_bfloat16* pa = pick(b.pool, pf & 0xff) + a_base;
+          const __nv_bfloat16* pb = pick(b.pool, (pf >> 8) & 0xff) + b_base;
           const int nck = (kp + kTcKC - 1) / kTcKC;
-          for (int c = 0; c < nck; ++c) {
-            if (!tc_wait(&sh.empty[s], ph ^ 1u, abort_flag, b.status, limit_ns)) {
+          for (int c = 0; c < nck; ++c, ++k) {
+            const int w = min(kTcKC, kp - kTcKC * c);
+            const uint32_t abytes = 2u * h_a * w * 2, bbytes = 2u * h_b * w * 2;
+            const int slot = (int)(k % kTcSlots);
+            if (!tc_wait(&sh.empty[slot], ((k / kTcSlots) & 1u) ^ 1u, abort_flag, b.status, limit_ns)) {
               ok = false;
               break;
             }
-            const int w = min(kTcKC, kp - kTcKC * c);
-            const int64_t ao = (int64_t)h_a * kTcKC * c, bo = (int64_t)h_b * kTcKC * c;
-            const uint32_t abytes = (uint32_t)h_a * w * 2, bbytes = (uint32_t)h_b * w * 2;
-            uint8_t* st = smem + s * kTcStageBytes;
-            mbar_expect_tx(&sh.full[s], 2 * (abytes + bbytes));
-            bulk_g2s(st, ah + ao, abytes, &sh.full[s]);
-            bulk_g2s(st + kTcABytes, al + ao, abytes, &sh.full[s]);
-            bulk_g2s(st + 2 * kTcABytes, bh + bo, bbytes, &sh.full[s]);
-            bulk_g2s(st + 2 * kTcABytes + kTcBBytes, bl + bo, bbytes, &sh.full[s]);
-            last_par[s] = (int)ph;
-            if (++s == kTcStages) {
-              s = 0;
-              ph ^= 1u;
-            }
+            uint8_t* dst = smem + slot * kTcStageBytes;
+            mbar_expect_tx(&sh.full[slot], abytes + bbytes);
+            bulk_g2s(dst, pa + 2 * (int64_t)h_a * kTcKC * c, abytes, &sh.full[slot]);
+            bulk_g2s(dst + abytes, pb + 2 * (int64_t)h_b * kTcKC * c, bbytes, &sh.full[slot]);
           }
         }
         ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -365,13 +353,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     if (lane == 0 && !ok) {
       // copies already issued still land in shared memory: wait for them
-      for (int i = 0; i < kTcStages; ++i)
-        if (last_par[i] >= 0) mbar_wait_bounded(&sh.full[i], (uint32_t)last_par[i], limit_ns);
+      for (uint32_t i = (k > kTcSlots ? k - kTcSlots : 0); i < k; ++i)
+        mbar_wait_bounded(&sh.full[i % kTcSlots], (i / kTcSlots) & 1u, limit_ns);
     }
   } else if (warp == 9) {
     // ---- MMA issuer (lane 0)
-    int s = 0, ab = 0;
-    uint32_t ph = 0, aph = 0;
+    uint32_t k = 0;
+    int ab = 0;
+    uint32_t aph = 0;
     bool ok = true;
     for (int base = rg.x; base < rg.y && ok; base += 32) {
       WorkRegs r;
@@ -381,39 +370,42 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int kp = shfl32(r.q[1].z, j);
         const int hw = shfl32(r.q[2].x, j);
         const int pf = shfl32(r.q[3].x, j);
-        if (lane == 0 && !((pf >> 16) & kTcEmpty)) {
+        const int flags = (pf >> 16) & 0xff;
+        if (lane == 0 && !(flags & kTcEmpty)) {
           const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
           const uint32_t idesc = idesc_bf16(128, (h_b + 15) & ~15);
-          if (!tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns)) ok = false;
+          if ((flags & kTcGStart) &&
+              !tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns))
+            ok = false;
           if (ok) {
             fence_after_sync();
             const uint32_t d = tmem + (uint32_t)ab * 64u;
             const int nck = (kp + kTcKC - 1) / kTcKC;
-            for (int c = 0; c < nck; ++c) {
-              if (!tc_wait(&sh.full[s], ph, abort_flag, b.status, limit_ns)) {
+            for (int c = 0; c < nck; ++c, ++k) {
+              const int w = min(kTcKC, kp - kTcKC * c);
+              const uint32_t abytes = 2u * h_a * w * 2;
+              const int slot = (int)(k % kTcSlots);
+              if (!tc_wait(&sh.full[slot], (k / kTcSlots) & 1u, abort_flag, b.status, limit_ns)) {
                 ok = false;
                 break;
               }
               fence_after_sync();
-              const int w = min(kTcKC, kp - kTcKC * c);
-              const uint32_t sa = smem_u32(smem + s * kTcStageBytes);
+              const uint32_t sa = smem_u32(smem + slot * kTcStageBytes);
+              const uint32_t a_lo = (uint32_t)h_a * w * 2, b0 = abytes, b_lo = abytes + (uint32_t)h_b * w * 2;
               for (int jj = 0; jj < w / 16; ++jj) {
                 const uint32_t ao = (uint32_t)(32 * jj * h_a), bo = (uint32_t)(32 * jj * h_b);
-                const uint64_t a_hi = smem_desc(sa + ao, h_a * 16, 128);
-                const uint64_t a_lo = smem_desc(sa + kTcABytes + ao, h_a * 16, 128);
-                const uint64_t b_hi = smem_desc(sa + 2 * kTcABytes + bo, h_b * 16, 128);
-                const uint64_t b_lo = smem_desc(sa + 2 * kTcABytes + kTcBBytes + bo, h_b * 16, 128);
-                mma_bf16(d, a_hi, b_hi, idesc, (c > 0 || jj > 0) ? 1u : 0u);
-                mma_bf16(d, a_hi, b_lo, idesc, 1u);
-                mma_bf16(d, a_lo, b_hi, idesc, 1u);
+                const uint64_t dah = smem_desc(sa + ao, h_a * 16, 128);
+                const uint64_t dal = smem_desc(sa + a_lo + ao, h_a * 16, 128);
+                const uint64_t dbh = smem_desc(sa + b0 + bo, h_b * 16, 128);
+                const uint64_t dbl = smem_desc(sa + b_lo + bo, h_b * 16, 128);
+                const uint32_t acc = ((flags & kTcGStart) && c == 0 && jj == 0) ? 0u : 1u;
+                mma_bf16(d, dah, dbh, idesc, acc);
+                mma_bf16(d, dah, dbl, idesc, 1u);
+                mma_bf16(d, dal, dbh, idesc, 1u);
               }
-              mma_commit(&sh.empty[s]);
-              if (++s == kTcStages) {
-                s = 0;
-                ph ^= 1u;
-              }
+              mma_commit(&sh.empty[slot]);
             }
-            if (ok) {
+            if (ok && (flags & kTcGEnd)) {
               mma_commit(&sh.acc_full[ab]);
               if (++ab == kTcAcc) {
                 ab = 0;
@@ -433,124 +425,36 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     int ab = 0;
     uint32_t aph = 0;
     bool ok = true;
-    // phase-2 state of the current task
-    float acc[32];
+    float vh[32], vl[32];
 #pragma unroll
-    for (int e = 0; e < 32; ++e) acc[e] = 0.f;
-    int gi = 0;
-    bool first = true;
-    const uint32_t vh_t = tmem + kTcVh + (uint32_t)half * 32u + lane_base;
-    const uint32_t vl_t = tmem + kTcVl + (uint32_t)half * 32u + lane_base;
+    for (int e = 0; e < 32; ++e) vh[e] = vl[e] = 0.f;
     for (int base = rg.x; base < rg.y && ok; base += 32) {
       WorkRegs r;
       load_work(work, base + lane, rg.y, r);
       const int cnt = min(32, rg.y - base);
       for (int j = 0; j < cnt && ok; ++j) {
-        const float alpha = __int_as_float(shfl32(r.q[1].w, j));
-        const int hw = shfl32(r.q[2].x, j);
         const int pf = shfl32(r.q[3].x, j);
         const int flags = (pf >> 16) & 0xff;
+        if (!(flags & (kTcFirst | kTcLast | kTcGEnd))) continue;
+        const float alpha = __int_as_float(shfl32(r.q[1].w, j));
+        const int hw = shfl32(r.q[2].x, j);
         const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
         const int N = (h_b + 15) & ~15;
+        const int ng = min(2, max(0, (N - half * 32) >> 4));  // 16-column groups of this warp
         const int64_t out_base = shfl64(r.q[1].x, r.q[1].y, j);
         const int vrc = shfl32(r.q[2].y, j);
         const int out_ld = shfl32(r.q[2].z, j);
         const int col0 = shfl32(r.q[2].w, j);
-        if (PHASE == 2) {
-          if (flags & kTcFirst) {
-            gi = 0;
-            first = true;
-          }
-          if (!(flags & kTcEmpty)) {
-            ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
-            if (!ok) break;  // TMEM loads below need the whole warp
-            fence_after_sync();
-            const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
-            const int ng = min(2, max(0, (N - half * 32) >> 4));  // 16-column groups present
-            if (ng > 0) {
-              float v[32];
-              if (ng == 2) tmem_ld32(d, v);
-              else tmem_ld16(d, v);
+        if (PHASE == 2 && (flags & kTcFirst)) {
 #pragma unroll
-              for (int g = 0; g < 2; ++g) {
-                if (g < ng) {
-                  if (gi == 0) {
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmul_rn(alpha, v[g * 16 + e]);
-                  } else {
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) acc[g * 16 + e] = __fmaf_rn(alpha, v[g * 16 + e], acc[g * 16 + e]);
-                  }
-                }
-              }
-            }
-            fence_before_sync();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
-            if (++ab == kTcAcc) {
-              ab = 0;
-              aph ^= 1u;
-            }
-            ++gi;
-          }
-          const bool last = (flags & kTcLast) != 0;
-          if (last || gi == kTcGroup) {
-            // fold the pending group into the compensated pair; on the
-            // task's last item write the result
-            const bool add = gi > 0;
-#pragma unroll
-            for (int g = 0; g < 2; ++g) {
-              if (half * 32 + g * 16 < N) {
-                float vh[16], vl[16];
-                if (first) {
-#pragma unroll
-                  for (int e = 0; e < 16; ++e) {
-                    vh[e] = add ? acc[16 * g + e] : 0.f;
-                    vl[e] = 0.f;
-                  }
-                } else {
-                  tmem_ld16x2(vh_t + (uint32_t)(16 * g), vl_t + (uint32_t)(16 * g), vh, vl);
-                  if (add) {
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], acc[16 * g + e]);
-                  }
-                }
-                if (!last) {
-                  tmem_st16(vh_t + (uint32_t)(16 * g), vh);
-                  tmem_st16(vl_t + (uint32_t)(16 * g), vl);
-                } else if (flags & kTcDirect) {
-                  const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
-                  if (row < vrows) {
-                    double* out = sigma + out_base + (int64_t)row * out_ld;
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                      const int col = half * 32 + 16 * g + e;
-                      if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
-                    }
-                  }
-                } else if (row < h_a) {
-                  float2* out = b.partials + out_base + (int64_t)row * h_b;
-#pragma unroll
-                  for (int e = 0; e < 16; ++e) {
-                    const int col = half * 32 + 16 * g + e;
-                    if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
-                  }
-                }
-              }
-            }
-            first = false;
-            gi = 0;
-          }
-        } else {
-          // phase 1: one item per task; S tile written as a packed operand
-          // (rows of this tile, K columns col0.. of S)
+          for (int e = 0; e < 32; ++e) vh[e] = vl[e] = 0.f;
+        }
+        float v[32];
+        if ((flags & kTcGEnd) && !(flags & kTcEmpty)) {
           ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
-          if (!ok) break;
+          if (!ok) break;  // TMEM loads below need the whole warp
           fence_after_sync();
-          const int ncols = min(kTcRowsB, out_ld - col0);
           const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
-          float v[32];
-          const int ng = min(2, max(0, (N - half * 32) >> 4));  // 16-column groups present
 #pragma unroll
           for (int e = 0; e < 32; ++e) v[e] = 0.f;
           if (ng == 2) tmem_ld32(d, v);
@@ -563,33 +467,61 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             ab = 0;
             aph ^= 1u;
           }
-          if (row < h_a) {
-            __nv_bfloat16* shi = b.hi[kTcPoolS] + out_base;
-            __nv_bfloat16* slo = b.lo[kTcPoolS] + out_base;
+          if (PHASE == 2) {
 #pragma unroll
-            for (int g8 = 0; g8 < 4; ++g8) {
-              const int c0 = half * 32 + 8 * g8;
-              if (c0 < ncols) {
-                uint32_t hw4[4], lw4[4];
+            for (int e = 0; e < 32; ++e) two_sum_acc(vh[e], vl[e], __fmul_rn(alpha, v[e]));
+          }
+        }
+        if (PHASE == 2) {
+          if (flags & kTcLast) {
+            if (flags & kTcDirect) {
+              const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
+              if (row < vrows) {
+                double* out = sigma + out_base + (int64_t)row * out_ld;
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                  const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
-                  __nv_bfloat16 xh, xl;
-                  split_bf16(x, xh, xl);
-                  const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
-                  if (e & 1) {
-                    hw4[e >> 1] |= bh << 16;
-                    lw4[e >> 1] |= bl << 16;
-                  } else {
-                    hw4[e >> 1] = bh;
-                    lw4[e >> 1] = bl;
-                  }
+                for (int e = 0; e < 32; ++e) {
+                  const int col = half * 32 + e;
+                  if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
                 }
-                const int C = col0 + c0;  // S column
-                const int64_t off = (int64_t)h_a * kTcKC * (C / kTcKC) + (kmajor_off(row, C % kTcKC, h_a) >> 1);
-                *(uint4*)(shi + off) = make_uint4(hw4[0], hw4[1], hw4[2], hw4[3]);
-                *(uint4*)(slo + off) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
               }
+            } else if (row < h_a) {
+              float2* out = b.partials + out_base + (int64_t)row * h_b;
+#pragma unroll
+              for (int e = 0; e < 32; ++e) {
+                const int col = half * 32 + e;
+                if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+              }
+            }
+          }
+        } else if ((flags & kTcGEnd) && row < h_a) {
+          // phase 1: S tile written as a packed operand (rows of this tile,
+          // K columns col0.. of S)
+          const int ncols = min(kTcRowsB, out_ld - col0);
+          __nv_bfloat16* sp = b.pool[kTcPoolS] + out_base;
+#pragma unroll
+          for (int g8 = 0; g8 < 4; ++g8) {
+            const int c0 = half * 32 + 8 * g8;
+            if (c0 < ncols) {
+              uint32_t hw4[4], lw4[4];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
+                __nv_bfloat16 xh, xl;
+                split_bf16(x, xh, xl);
+                const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+                if (e & 1) {
+                  hw4[e >> 1] |= bh << 16;
+                  lw4[e >> 1] |= bl << 16;
+                } else {
+                  hw4[e >> 1] = bh;
+                  lw4[e >> 1] = bl;
+                }
+              }
+              const int C = col0 + c0;  // S column
+              const int cc = C / kTcKC, wc = min(kTcKC, out_ld - kTcKC * cc);
+              const int64_t off = 2 * (int64_t)h_a * kTcKC * cc + (kmajor_off(row, C % kTcKC, h_a) >> 1);
+              *(uint4*)(sp + off) = make_uint4(hw4[0], hw4[1], hw4[2], hw4[3]);
+              *(uint4*)(sp + off + (int64_t)h_a * wc) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
             }
           }
         }

@@ -21,14 +21,15 @@ cudaError_t launch_tc_tile_bulk(const __nv_bfloat16* Ap, const __nv_bfloat16* Bp
 
 // ---------------------------------------------------------------- sigma
 //
-// Packed operand: `rows` (multiple of 8) x `kp` (multiple of 16) bf16 values
-// (hi and lo slices in two pools with the same offsets), cut into row tiles
-// of `rt` rows (128 for operands in the A role, 64 for the B role) and
-// K-chunks of kTcKC columns; block (row tile t, chunk c) is contiguous,
-// starts at element tc_block_off(rows, kp, t, c, rt) and holds its h x w
-// values in the K-major core-matrix order (byte (j/8)*h*16 + (i/8)*128 +
-// (i%8)*16 + (j%8)*2).  Rows beyond the operand's own rows and columns beyond
-// its own K are zero.
+// Packed operand: `rows` (multiple of 8) x `kp` (multiple of 16) values split
+// into bf16 hi = bf16(x) and lo = bf16(x - hi), cut into row tiles of `rt`
+// rows (128 for operands in the MMA A role, 64 for the B role) and K-chunks
+// of kTcKC columns.  Block (row tile t, chunk c), h rows x w columns, starts
+// at element 2 * tc_block_off(rows, kp, t, c, rt) of its pool and holds the
+// h x w hi values followed by the h x w lo values, each in the K-major
+// core-matrix order (byte (j/8)*h*16 + (i/8)*128 + (i%8)*16 + (j%8)*2), so
+// that one bulk copy moves both slices.  Rows beyond the operand's own rows
+// and columns beyond its own K are zero.
 constexpr int kTcKC = 32;
 constexpr int kTcRowsA = 128;  // output tile rows (MMA M)
 constexpr int kTcRowsB = 64;   // output tile columns (MMA N at most)
@@ -44,14 +45,14 @@ enum : int { kTcPoolL = 0, kTcPoolR = 1, kTcPoolPsi = 2, kTcPoolPsiT = 3, kTcPoo
 
 // One packed operand filled from an FP64 block: view element (r, k) is
 // src[src_off + (trans ? k * ld + r : r * ld + k)] for r < rows_v, k < cols_v;
-// row tiles of rt rows.
+// row tiles of rt rows; dst_off in elements of the pool.
 struct TcPack {
   int64_t src_off, dst_off;
   int32_t ld, rows_v, cols_v, rows_p, kp, rt;
   uint8_t src, pool, trans, pad;
 };
 
-// out (+)= alpha * A * B^T over K = kp, A and B packed operands
+// out (+)= alpha * A * B^T over K = kp, A and B packed operands (host plan)
 struct TcItem {
   int64_t a_off, b_off;
   int32_t kp;
@@ -60,8 +61,8 @@ struct TcItem {
   float alpha;
 };
 
-// One task: output tile (tm, tn) -- rows 128 tm.. of the A operands, rows
-// 64 tn.. of the B operands -- and the items [ibeg, iend).
+// One task of the host plan: output tile (tm, tn) -- rows 128 tm.. of the A
+// operands, rows 64 tn.. of the B operands -- and the items [ibeg, iend).
 //   phase 1 (one item): writes alpha * A B^T as the packed S operand at
 //     out_off of pool S (rows a_rows, K out_kp);
 //   phase 2: sum of the items with a compensated (hi, lo) f32 accumulation;
@@ -88,12 +89,22 @@ struct TcTile {
 // block's tasks, flattened in processing order, each carrying what the
 // producer, MMA and epilogue roles need, so that a warp loads 32 of them
 // with one coalesced access and no role chases task -> item pointers.
-//   a_base / b_base: element offsets of the row tile (128 rows of A, 64 of B)
-//   out_base: phase 1: S row-tile base (element, pool S); phase 2 direct:
-//     sigma element of tile (0, 0); phase 2 partial: partial slot (float2)
+//   a_base / b_base: pool elements of the row tile (128 rows of A, 64 of B)
+//   out_base: phase 1: S row-tile base (pool S); phase 2 direct: sigma
+//     element of tile (0, 0); phase 2 partial: partial slot (float2)
 //   out_ld: phase 1: kp of S; phase 2 direct: sigma row stride; partial: h_b
 //   col0: phase 1: S column of tile column 0
-enum : uint32_t { kTcFirst = 1, kTcLast = 2, kTcDirect = 4, kTcEmpty = 8 };
+// Consecutive items of a task form accumulation groups (kTcGStart ..
+// kTcGEnd) summed by the tensor core in one TMEM accumulator; alpha is
+// applied to the group sum (groups of several items have alpha = 1).
+enum : uint32_t {
+  kTcFirst = 1,    // first record of a task
+  kTcLast = 2,     // last record of a task: write the result
+  kTcDirect = 4,   // phase 2: result straight into sigma
+  kTcEmpty = 8,    // task without items (writes zeros)
+  kTcGStart = 16,  // first item of an accumulation group
+  kTcGEnd = 32     // last item of an accumulation group
+};
 struct __align__(16) TcWork {
   int64_t a_base, b_base, out_base;
   int32_t kp;
@@ -107,8 +118,7 @@ static_assert(sizeof(TcWork) == 64, "TcWork is 64 bytes");
 
 struct TcBufs {
   const double* src[3];  // FP64 sources of packing: L arena, R arena, psi
-  __nv_bfloat16* hi[kTcPools];
-  __nv_bfloat16* lo[kTcPools];
+  __nv_bfloat16* pool[kTcPools];
   float2* partials;
   int* status;  // set to 1 when a pipeline wait ran out
 };
