@@ -966,7 +966,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
     }
   }
-  const double chunk = std::max(total / (3.0 * nsm), 20000.0);
+  const double chunk = std::max(total / (6.0 * nsm), 20000.0);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     const int ib = (int)i2.size();
@@ -1054,8 +1054,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   }
   std::vector<int> o1, o2;
   std::vector<int2> r1, r2;
-  schedule_lpt(c1, nsm, o1, r1);
-  schedule_lpt(c2, nsm, o2, r2);
+  // two persistent blocks per SM (each kernel block runs its own pipeline)
+  schedule_lpt(c1, 2 * nsm, o1, r1);
+  schedule_lpt(c2, 2 * nsm, o2, r2);
   // buffers
   for (int i = 0; i < kTcPools; ++i) {
     plan.tc_pool_elems[i] = pool_n[i];

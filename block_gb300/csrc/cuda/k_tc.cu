@@ -215,12 +215,16 @@ cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cud
 
 namespace {
 
-constexpr int kTcSlots = 8;  // stages of the operand ring
+// Two independent blocks per SM, each with its own pipeline.
+constexpr int kTcSlots = 4;  // stages of the operand ring
 // one stage holds the largest piece: A (128 rows) and B (64 rows) x 32 columns, hi and lo
 constexpr uint32_t kTcStageBytes = 2u * (kTcRowsA + kTcRowsB) * kTcKC * 2;
-constexpr int kTcThreads = 320;  // warps 0-7 epilogue, 8 bulk-copy producer, 9 MMA issuer
+constexpr int kTcThreads = 192;  // warps 0-3 epilogue, 4 bulk-copy producer, 5 MMA issuer
+constexpr int kTcProducer = 4, kTcIssuer = 5;
 constexpr int kTcSmem = kTcSlots * kTcStageBytes;
-constexpr int kTcAcc = 8;        // accumulators of 64 TMEM columns
+constexpr int kTcAcc = 2;        // accumulators of 64 TMEM columns
+constexpr uint32_t kTcVh = 128, kTcVl = 192;  // TMEM columns of the compensated (hi, lo) sums
+constexpr uint32_t kTcTmemCols = 256;
 
 struct TcShared {
   uint64_t full[kTcSlots], empty[kTcSlots], acc_full[kTcAcc], acc_empty[kTcAcc], drain;
@@ -283,16 +287,16 @@ __device__ __forceinline__ int shfl32(int v, int j) { return __shfl_sync(0xfffff
 // across task boundaries.  The epilogue folds each group sum into a
 // compensated (hi, lo) f32 pair held in registers.
 template <int PHASE>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 2)
     tc_sigma_kernel(TcBufs b, const TcWork* __restrict__ work, const int2* __restrict__ ranges,
                     double* __restrict__ sigma, uint64_t limit_ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ TcShared sh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int2 rg = ranges[blockIdx.x];
-  // TMEM: eight accumulators of 64 columns
-  if (warp == 9) {
-    tmem_alloc(&sh.tbase, 512);
+  // TMEM: two accumulators of 64 columns, then the phase-2 (hi, lo) sums
+  if (warp == kTcIssuer) {
+    tmem_alloc(&sh.tbase, kTcTmemCols);
     tmem_relinquish();
   }
   if (tid == 0) {
@@ -302,7 +306,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     for (int i = 0; i < kTcAcc; ++i) {
       mbar_init(&sh.acc_full[i], 1);
-      mbar_init(&sh.acc_empty[i], 8);
+      mbar_init(&sh.acc_empty[i], 4);
     }
     mbar_init(&sh.drain, 1);
     sh.abort_flag = 0;
@@ -314,7 +318,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = sh.tbase;
   volatile int* abort_flag = &sh.abort_flag;
 
-  if (warp == 8) {
+  if (warp == kTcProducer) {
     // ---- producer: lane 0 streams the operand pieces (one K-chunk of one
     // item: A hi, A lo, B hi, B lo) of every item through the stages
     uint32_t k = 0;  // pieces issued
@@ -356,7 +360,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       for (uint32_t i = (k > kTcSlots ? k - kTcSlots : 0); i < k; ++i)
         mbar_wait_bounded(&sh.full[i % kTcSlots], (i / kTcSlots) & 1u, limit_ns);
     }
-  } else if (warp == 9) {
+  } else if (warp == kTcIssuer) {
     // ---- MMA issuer (lane 0)
     uint32_t k = 0;
     int ab = 0;
@@ -418,16 +422,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
     }
   } else {
-    // ---- epilogue: warp w owns TMEM lanes 32 (w % 4).. and columns 32 (w / 4)..
-    const int q = warp & 3, half = warp >> 2;
-    const int row = 32 * q + lane;
-    const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+    // ---- epilogue: warp w owns TMEM lanes 32 w.., all 64 columns
+    const int row = 32 * warp + lane;
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    const uint32_t vh_t = tmem + kTcVh + lane_base, vl_t = tmem + kTcVl + lane_base;
     int ab = 0;
     uint32_t aph = 0;
-    bool ok = true;
-    float vh[32], vl[32];
-#pragma unroll
-    for (int e = 0; e < 32; ++e) vh[e] = vl[e] = 0.f;
+    bool ok = true, first = true;
     for (int base = rg.x; base < rg.y && ok; base += 32) {
       WorkRegs r;
       load_work(work, base + lane, rg.y, r);
@@ -439,26 +440,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const float alpha = __int_as_float(shfl32(r.q[1].w, j));
         const int hw = shfl32(r.q[2].x, j);
         const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
-        const int N = (h_b + 15) & ~15;
-        const int ng = min(2, max(0, (N - half * 32) >> 4));  // 16-column groups of this warp
+        const int ng = ((h_b + 15) & ~15) >> 4;  // 16-column groups of the accumulator
         const int64_t out_base = shfl64(r.q[1].x, r.q[1].y, j);
         const int vrc = shfl32(r.q[2].y, j);
         const int out_ld = shfl32(r.q[2].z, j);
         const int col0 = shfl32(r.q[2].w, j);
-        if (PHASE == 2 && (flags & kTcFirst)) {
-#pragma unroll
-          for (int e = 0; e < 32; ++e) vh[e] = vl[e] = 0.f;
-        }
-        float v[32];
-        if ((flags & kTcGEnd) && !(flags & kTcEmpty)) {
+        if (flags & kTcFirst) first = true;
+        float v[64];
+        const bool have = (flags & kTcGEnd) && !(flags & kTcEmpty);
+        if (have) {
           ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
           if (!ok) break;  // TMEM loads below need the whole warp
           fence_after_sync();
-          const uint32_t d = tmem + (uint32_t)ab * 64u + (uint32_t)half * 32u + lane_base;
+          const uint32_t d = tmem + (uint32_t)ab * 64u + lane_base;
 #pragma unroll
-          for (int e = 0; e < 32; ++e) v[e] = 0.f;
-          if (ng == 2) tmem_ld32(d, v);
-          else if (ng == 1) tmem_ld16(d, v);
+          for (int e = 0; e < 64; ++e) v[e] = 0.f;
+          if (ng > 2) {
+            tmem_ld32(d, v);
+            if (ng == 4) tmem_ld32(d + 32u, v + 32);
+            else tmem_ld16(d + 32u, v + 32);
+          } else if (ng == 2) {
+            tmem_ld32(d, v);
+          } else if (ng == 1) {
+            tmem_ld16(d, v);
+          }
           // accumulator read: the MMA issuer may reuse it
           fence_before_sync();
           __syncwarp();
@@ -467,40 +472,59 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             ab = 0;
             aph ^= 1u;
           }
-          if (PHASE == 2) {
-#pragma unroll
-            for (int e = 0; e < 32; ++e) two_sum_acc(vh[e], vl[e], __fmul_rn(alpha, v[e]));
-          }
         }
         if (PHASE == 2) {
-          if (flags & kTcLast) {
-            if (flags & kTcDirect) {
-              const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
-              if (row < vrows) {
-                double* out = sigma + out_base + (int64_t)row * out_ld;
+          const bool last = (flags & kTcLast) != 0;
+          if (!have && !last) continue;
 #pragma unroll
-                for (int e = 0; e < 32; ++e) {
-                  const int col = half * 32 + e;
-                  if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
+          for (int g = 0; g < 4; ++g) {
+            if (g < ng) {
+              float vh[16], vl[16];
+              if (first) {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                  vh[e] = have ? __fmul_rn(alpha, v[16 * g + e]) : 0.f;
+                  vl[e] = 0.f;
+                }
+              } else {
+                tmem_ld16x2(vh_t + (uint32_t)(16 * g), vl_t + (uint32_t)(16 * g), vh, vl);
+                if (have) {
+#pragma unroll
+                  for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], __fmul_rn(alpha, v[16 * g + e]));
                 }
               }
-            } else if (row < h_a) {
-              float2* out = b.partials + out_base + (int64_t)row * h_b;
+              if (!last) {
+                tmem_st16(vh_t + (uint32_t)(16 * g), vh);
+                tmem_st16(vl_t + (uint32_t)(16 * g), vl);
+              } else if (flags & kTcDirect) {
+                const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
+                if (row < vrows) {
+                  double* out = sigma + out_base + (int64_t)row * out_ld;
 #pragma unroll
-              for (int e = 0; e < 32; ++e) {
-                const int col = half * 32 + e;
-                if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                  for (int e = 0; e < 16; ++e) {
+                    const int col = 16 * g + e;
+                    if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
+                  }
+                }
+              } else if (row < h_a) {
+                float2* out = b.partials + out_base + (int64_t)row * h_b;
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                  const int col = 16 * g + e;
+                  if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                }
               }
             }
           }
-        } else if ((flags & kTcGEnd) && row < h_a) {
+          first = false;
+        } else if (have && row < h_a) {
           // phase 1: S tile written as a packed operand (rows of this tile,
           // K columns col0.. of S)
           const int ncols = min(kTcRowsB, out_ld - col0);
           __nv_bfloat16* sp = b.pool[kTcPoolS] + out_base;
 #pragma unroll
-          for (int g8 = 0; g8 < 4; ++g8) {
-            const int c0 = half * 32 + 8 * g8;
+          for (int g8 = 0; g8 < 8; ++g8) {
+            const int c0 = 8 * g8;
             if (c0 < ncols) {
               uint32_t hw4[4], lw4[4];
 #pragma unroll
@@ -529,7 +553,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
   }
   __syncthreads();
-  if (warp == 9) {
+  if (warp == kTcIssuer) {
     // every MMA of this block has completed before TMEM is released
     if (lane == 0) {
       mma_commit(&sh.drain);
@@ -537,7 +561,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     __syncwarp();
     fence_after_sync();
-    tmem_dealloc(tmem, 512);
+    tmem_dealloc(tmem, kTcTmemCols);
   }
 }
 
