@@ -249,28 +249,56 @@ struct PlanTimer {
 
 // Longest-processing-time assignment of tasks to `nblocks` persistent
 // blocks; block j runs order[ranges[j].x .. ranges[j].y), in task order.
-void schedule_lpt(const std::vector<double>& cost, int nblocks, std::vector<int>& order, std::vector<int2>& ranges) {
+// Tasks with the same bundle id (contiguous in task order; for instance the
+// column tiles of one row of an output sector, which read the same A
+// operands) stay together on one block, consecutive, unless a bundle costs
+// more than a block's fair share, in which case it is cut into pieces of at
+// most that share.
+void schedule_lpt(const std::vector<double>& cost, const std::vector<int64_t>& bundle, int nblocks,
+                  std::vector<int>& order, std::vector<int2>& ranges) {
   const int n = (int)cost.size();
-  nblocks = std::max(1, std::min(nblocks, n));
-  std::vector<int> idx(n);
-  for (int i = 0; i < n; ++i) idx[i] = i;
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  std::vector<std::vector<int>> per(nblocks);
-  std::priority_queue<std::pair<double, int>, std::vector<std::pair<double, int>>, std::greater<>> load;
-  for (int j = 0; j < nblocks; ++j) load.push({0.0, j});
-  for (int i : idx) {
-    auto [l, j] = load.top();
-    load.pop();
-    per[j].push_back(i);
-    load.push({l + cost[i], j});
-  }
   order.clear();
   ranges.clear();
   if (n == 0) return;
+  nblocks = std::max(1, std::min(nblocks, n));
+  double total = 0.0;
+  for (double c : cost) total += c;
+  const double share = total / nblocks;
+  // units: contiguous task ranges
+  std::vector<std::pair<int, int>> units;
+  std::vector<double> ucost;
+  int b0 = 0;
+  double acc = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const bool split = i > b0 && (bundle[i] != bundle[i - 1] || acc + cost[i] > share);
+    if (split) {
+      units.push_back({b0, i});
+      ucost.push_back(acc);
+      b0 = i;
+      acc = 0.0;
+    }
+    acc += cost[i];
+  }
+  units.push_back({b0, n});
+  ucost.push_back(acc);
+  std::vector<int> idx(units.size());
+  for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return ucost[a] > ucost[b]; });
+  nblocks = std::max(1, std::min(nblocks, (int)units.size()));
+  std::vector<std::vector<int>> per(nblocks);
+  std::priority_queue<std::pair<double, int>, std::vector<std::pair<double, int>>, std::greater<>> load;
+  for (int j = 0; j < nblocks; ++j) load.push({0.0, j});
+  for (int u : idx) {
+    auto [l, j] = load.top();
+    load.pop();
+    per[j].push_back(u);
+    load.push({l + ucost[u], j});
+  }
   for (auto& v : per) {
     std::sort(v.begin(), v.end());
     const int b = (int)order.size();
-    order.insert(order.end(), v.begin(), v.end());
+    for (int u : v)
+      for (int i = units[u].first; i < units[u].second; ++i) order.push_back(i);
     ranges.push_back(make_int2(b, (int)order.size()));
   }
 }
@@ -856,6 +884,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   }
   std::vector<TcItem> i1;
   std::vector<TcTask> t1;
+  std::vector<int64_t> bundle1, bundle2;  // tasks reading the same A row tile
   std::unordered_map<int64_t, int> s_unit_item;  // S offset -> its phase-1 item
   std::vector<std::vector<TcItem>> per_sector(nsec);
   double mma = 0.0;
@@ -913,6 +942,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
             t.out_off = cur_s;
             t.out_kp = skp;
             t1.push_back(t);
+            bundle1.push_back((cur_s << 8) | tm);
             mma += 3.0 * 2.0 * 128 * tc_round16(std::min(kTcRowsB, t.b_rows - kTcRowsB * tn)) * a.kp;
           }
         cur_l = c.lQ;
@@ -994,6 +1024,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           t.out_kp = S.cols;
           t2.push_back(t);
           c2.push_back(tile_cost);
+          bundle2.push_back(((int64_t)s << 8) | tm);
           continue;
         }
         TcTile tl{};
@@ -1019,6 +1050,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           partial_n += (int64_t)ha * hb;
           t2.push_back(u);
           c2.push_back(acc);
+          bundle2.push_back(-(int64_t)t2.size());  // pieces of a split tile spread over blocks
           x0 = x1;
         }
         tl.pend = (int)slots.size();
@@ -1055,8 +1087,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   std::vector<int> o1, o2;
   std::vector<int2> r1, r2;
   // two persistent blocks per SM (each kernel block runs its own pipeline)
-  schedule_lpt(c1, 2 * nsm, o1, r1);
-  schedule_lpt(c2, 2 * nsm, o2, r2);
+  schedule_lpt(c1, bundle1, 2 * nsm, o1, r1);
+  schedule_lpt(c2, bundle2, 2 * nsm, o2, r2);
   // buffers
   for (int i = 0; i < kTcPools; ++i) {
     plan.tc_pool_elems[i] = pool_n[i];
