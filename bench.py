@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc"])
+    ap.add_argument("--precision", default="bf16x3tc", choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc"])
     ap.add_argument("--no-davidson", action="store_true", help="skip the FP64-vs-split Davidson comparison")
     ap.add_argument("--conf", default=DEFAULT_CONF)
     ap.add_argument("--partition", type=int, default=11)
@@ -126,6 +126,11 @@ def fp64_peak_tflops():
         return 2.0 * n ** 3 / (best * 1e-3) / 1e12
     except Exception:
         return None
+
+
+# DRAM bytes (read + write) of the tensor-core kernels per sigma, from one ncu
+# capture of this bench's own command (profiles/tc_sigma_bf16x3tc_syn24_m500.md)
+NCU_TRAFFIC = {("tests/golden/syn24/dmrg.conf", 11, "bf16x3tc"): 3.279e9}
 
 
 def measured_peaks():
@@ -271,8 +276,11 @@ def run_ours(a):
         prods = 6 if a.precision == "bf16x6" else 3
         kname = ("tc_sigma_kernel<1>+<2> (tcgen05/TMEM two-phase sector GEMMs, bf16 slices)"
                  if a.precision == "bf16x3tc" else "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)")
+        traffic = NCU_TRAFFIC.get((os.path.relpath(a.conf, ROOT), a.partition, a.precision))
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
-                "traffic": None, "kernel": kname,
+                "traffic": traffic, "traffic_unit": "bytes per sigma (both tensor-core kernels, ncu)",
+                "hbm_time_of_traffic_ms": (traffic / (peaks.get("hbm_gbs", 6800.0) * 1e9) * 1e3) if traffic else None,
+                "kernel": kname,
                 "peak_source": ("bf16_tflops of measured" if peaks else "fallback 1900"),
                 "products_per_logical_product": prods,
                 "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
