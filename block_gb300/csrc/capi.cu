@@ -596,6 +596,7 @@ extern "C" int bgpu_sigma_noalloc(bgpu_ctx* ctx, int sb, const double* psi, doub
     cudaStream_t st = ctx->eng->stream();
     cuda_check(dev::launch_gemm(bufs, plan.u1.d, plan.i1.d, plan.t1.d, (int)plan.t1.n, st), "sigma stage 1");
     cuda_check(dev::launch_gemm(bufs, plan.u2.d, plan.i2.d, plan.t2.d, (int)plan.t2.n, st), "sigma stage 2");
+    cuda_check(dev::launch_copy(bufs, sigma, plan.ru.d, plan.ri.d, (int)plan.ru.n, st), "sigma stage-2 partial sums");
     if (plan.ecore != 0.0) cuda_check(dev::launch_axpy(plan.ecore, psi, sigma, plan.n, st), "ecore");
   });
 }

@@ -522,23 +522,81 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
       flops += 2.0 * SV.rows * SV.cols * mc;
     });
   }
+  // stage 2: one unit per sector; a sector whose 64x64 tiles carry more K
+  // than a fair share of the FP64 pipe is split along its item list into
+  // units writing partial sectors after the stage-1 intermediates, summed
+  // into sigma in a fixed order by the build-copy kernel
   std::vector<dev::GemmUnit> u2;
   std::vector<dev::GemmItem> i2;
   std::vector<dev::GemmTask> t1, t2;
+  std::vector<dev::CopyUnit> ru;
+  std::vector<dev::CopyItem> ri;
+  double tile_k_total = 0.0;
   for (size_t s = 0; s < sb.sectors.size(); ++s) {
     const auto& S = sb.sectors[s];
-    dev::GemmUnit u{};
-    u.c_buf = 3;
-    u.c_off = S.offset;
-    u.ldc = S.cols;
-    u.m = S.rows;
-    u.n = S.cols;
-    u.beta_one = 0;
-    u.ibeg = (int)i2.size();
-    for (auto& g : per_sector[s]) i2.push_back(g);
-    u.iend = (int)i2.size();
-    u2.push_back(u);
+    double k = 0.0;
+    for (auto& g : per_sector[s]) k += g.k;
+    tile_k_total += k * ((S.rows + 63) / 64) * ((S.cols + 63) / 64);
   }
+  const double tile_k_share = std::max(tile_k_total / (4.0 * sm_count()), 4096.0);
+  int64_t partial = scratch;  // partial sectors follow the stage-1 intermediates
+  for (size_t s = 0; s < sb.sectors.size(); ++s) {
+    const auto& S = sb.sectors[s];
+    const auto& items = per_sector[s];
+    double k = 0.0;
+    for (auto& g : items) k += g.k;
+    const int ntiles = ((S.rows + 63) / 64) * ((S.cols + 63) / 64);
+    const int nchunks = std::max(1, std::min((int)items.size(), (int)std::ceil(k * ntiles / tile_k_share / ntiles)));
+    if (nchunks <= 1) {
+      dev::GemmUnit u{};
+      u.c_buf = 3;
+      u.c_off = S.offset;
+      u.ldc = S.cols;
+      u.m = S.rows;
+      u.n = S.cols;
+      u.beta_one = 0;
+      u.ibeg = (int)i2.size();
+      for (auto& g : items) i2.push_back(g);
+      u.iend = (int)i2.size();
+      u2.push_back(u);
+      continue;
+    }
+    dev::CopyUnit cu{};
+    cu.c_off = S.offset;
+    cu.ldc = S.cols;
+    cu.m = S.rows;
+    cu.n = S.cols;
+    cu.ibeg = (int)ri.size();
+    const double per = k / nchunks;
+    size_t a = 0;
+    for (int c = 0; c < nchunks && a < items.size(); ++c) {
+      size_t e = a;
+      double acc = 0.0;
+      while (e < items.size() && (acc < per || e == a || c == nchunks - 1)) acc += items[e++].k;
+      dev::GemmUnit u{};
+      u.c_buf = 4;
+      u.c_off = partial;
+      u.ldc = S.cols;
+      u.m = S.rows;
+      u.n = S.cols;
+      u.beta_one = 0;
+      u.ibeg = (int)i2.size();
+      for (size_t x = a; x < e; ++x) i2.push_back(items[x]);
+      u.iend = (int)i2.size();
+      u2.push_back(u);
+      dev::CopyItem ci{};
+      ci.s_off = partial;
+      ci.lds = S.cols;
+      ci.s_buf = 4;
+      ci.alpha = 1.0;
+      ri.push_back(ci);
+      partial += (int64_t)S.rows * S.cols;
+      a = e;
+    }
+    cu.iend = (int)ri.size();
+    ru.push_back(cu);
+  }
+  scratch = partial;
   for (int u = 0; u < (int)u1.size(); ++u) add_tasks(t1, u, u1[u].m, u1[u].n);
   // heavier output tiles first
   std::vector<std::pair<double, int>> cost;
@@ -555,6 +613,8 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   plan.u2.upload(u2, stream_);
   plan.i2.upload(i2, stream_);
   plan.t2.upload(t2, stream_);
+  plan.ru.upload(ru, stream_);
+  plan.ri.upload(ri, stream_);
   plan.scratch_elems = scratch;
   plan.scratch = alloc(scratch);
   plan.flops = flops;
@@ -635,6 +695,8 @@ void GpuEngine::free_plan(SigmaPlan& p) {
   p.t2.release(stream_);
   p.du.release(stream_);
   p.di.release(stream_);
+  p.ru.release(stream_);
+  p.ri.release(stream_);
   free(p.scratch);
   p.scratch = nullptr;
 }
@@ -648,6 +710,7 @@ void GpuEngine::sigma(const Superblock& sb, const SigmaPlan& p, const double* ps
   bufs.p[4] = p.scratch;
   cuda_check(dev::launch_gemm(bufs, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "sigma stage 1");
   cuda_check(dev::launch_gemm(bufs, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "sigma stage 2");
+  cuda_check(dev::launch_copy(bufs, out, p.ru.d, p.ri.d, (int)p.ru.n, stream_), "sigma stage-2 partial sums");
   if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
   sigma_flops += p.flops;
   ++sigma_calls;
@@ -1237,7 +1300,7 @@ void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi,
 int GpuEngine::sigma_launches(const SigmaPlan& p) const {
   if (precision == Precision::BF16X3_TC) return 4 + (p.ecore != 0.0 ? 1 : 0);  // pack psi, phase 1, phase 2, reduce
   if (precision_slices(precision)) return 3 + (p.ecore != 0.0 ? 1 : 0);  // slice psi, fused, reduce (+ecore)
-  return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
+  return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ru.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
 }
 
 void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out, int reps,
@@ -1281,6 +1344,7 @@ void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const doub
     cuda_check(dev::launch_gemm(bufs, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "sigma stage 1");
     cuda_check(cudaEventRecord(e[1], stream_), "record");
     cuda_check(dev::launch_gemm(bufs, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "sigma stage 2");
+    cuda_check(dev::launch_copy(bufs, out, p.ru.d, p.ri.d, (int)p.ru.n, stream_), "sigma stage-2 partial sums");
     cuda_check(cudaEventRecord(e[2], stream_), "record");
     if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
     cuda_check(cudaEventRecord(e[3], stream_), "record");

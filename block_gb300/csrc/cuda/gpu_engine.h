@@ -48,7 +48,9 @@ struct SigmaPlan {
   DevArray<dev::GemmTask> t1, t2;
   DevArray<dev::DiagUnit> du;
   DevArray<dev::DiagItem> di;
-  double* scratch = nullptr;  // stage-1 intermediates
+  DevArray<dev::CopyUnit> ru;  // FP64 sum of split stage-2 partial sectors into sigma
+  DevArray<dev::CopyItem> ri;
+  double* scratch = nullptr;  // stage-1 intermediates, then split stage-2 partial sectors
   int64_t scratch_elems = 0;
   double flops = 0.0;         // FP64-equivalent flops of one sigma
   double bytes = 0.0;         // algorithmic bytes of one sigma (operator blocks + psi + sigma)
