@@ -61,6 +61,7 @@ _SIGS = {
     "bgpu_tc_tile": (_I, [_P, _P, _P, _P, _I, _I, _I]),
     "bgpu_superblock_info": (_I, [_P, _I, _DP, _I]),
     "bgpu_set_refine_window": (_I, [_P, ctypes.c_double]),
+    "bgpu_set_guess": (_I, [_P, _I]),
     "bgpu_tc_wait_selftest": (_I, [_P, ctypes.c_double, _IP, _IP, _DP]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
@@ -272,6 +273,11 @@ class Context:
         w = np.zeros(1)
         self._check(self.lib.bgpu_tc_wait_selftest(self.h, float(limit_ms), _ip(g), _ip(st), _dp(w)))
         return int(g[0]), int(st[0]), float(w[0])
+
+    def set_guess(self, transform=True):
+        """Davidson start of run_dmrg steps: transformed previous wavefunction
+        (True) or unit vectors (False)."""
+        self._check(self.lib.bgpu_set_guess(self.h, int(bool(transform))))
 
     def set_refine_window(self, eh):
         """FP64 energy refinement window of split-precision sweeps (Eh)."""

@@ -21,6 +21,7 @@ struct bgpu_ctx {
   std::string err;
   int device = 0;
   double refine_window = 1e-3;  // Eh; see bgpu_set_refine_window
+  bool transform_guess = true;  // see bgpu_set_guess
   struct BlockRec {
     Block b;
     std::vector<OpKey> decl;  // declaration order
@@ -102,6 +103,10 @@ int bgpu_destroy(bgpu_ctx* ctx) {
 }
 
 const char* bgpu_last_error_string(const bgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bgpu_set_guess(bgpu_ctx* ctx, int transform) {
+  return guarded(ctx, [&] { ctx->transform_guess = transform != 0; });
+}
 
 int bgpu_set_refine_window(bgpu_ctx* ctx, double eh) {
   return guarded(ctx, [&] {
@@ -511,6 +516,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     DriverOptions opt;
     opt.verbose = verbose;
     if (precision_slices(ctx->eng->precision)) opt.refine_window = ctx->refine_window;
+    opt.transform_guess = ctx->transform_guess;
     const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops, p0 = ctx->eng->plan_seconds;
     const long c0 = ctx->eng->sigma_calls;
     SweepResult r;

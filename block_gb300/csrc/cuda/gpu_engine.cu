@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -62,6 +63,9 @@ GpuEngine::~GpuEngine() {
   if (waves_) cudaFreeAsync(waves_, stream_);
   if (dm_vecs_) cudaFreeAsync(dm_vecs_, stream_);
   if (rot_) cudaFreeAsync(rot_, stream_);
+  for (auto& kv : block_rot_)
+    if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
+  if (guess_) cudaFreeAsync(guess_, stream_);
   if (solver_work_) cudaFreeAsync(solver_work_, stream_);
   if (solver_info_) cudaFreeAsync(solver_info_, stream_);
   cudaStreamSynchronize(stream_);
@@ -111,6 +115,11 @@ void GpuEngine::release_block(Block& b) {
   if (it != blocks_.end()) {
     free(it->second.d);
     blocks_.erase(it);
+  }
+  auto rr = block_rot_.find(b.handle);
+  if (rr != block_rot_.end()) {
+    free(rr->second.d);
+    block_rot_.erase(rr);
   }
   b.handle = -1;
 }
@@ -1410,7 +1419,11 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   std::partial_sort(order.begin(), order.begin() + nroots, order.end(),
                     [&](int64_t a, int64_t b) { return hd[a] < hd[b]; });
   Rng rng(p.seed);
-  {
+  if (p.use_guess && guess_ && guess_n_ == n && nguess_ >= nroots) {
+    // transformed previous wavefunctions (orthonormalised below)
+    cuda_check(cudaMemcpyAsync(B, guess_, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
+               "guess");
+  } else {
     std::vector<double> g((size_t)nroots * n);
     for (int rr = 0; rr < nroots; ++rr) {
       for (int64_t i = 0; i < n; ++i) g[(size_t)rr * n + i] = 1e-3 * (rng.uniform() - 0.5);
@@ -1564,6 +1577,293 @@ bool GpuEngine::refine(const Superblock& sb, std::vector<double>& energies) {
   free(red);
   sync();
   return true;
+}
+
+// Guess transform (GuessWave::transform_previous_wavefunction with
+// TransformLeftBlock / onedot_shufflesysdot / TransformRightBlock,
+// guess_wavefunction.C:17-53, 434-486, 526-620) of the last solve's vectors
+// into the state space of `sb`:
+//   forward (previous step p-1, this step p):
+//     phi[a, r]   = U^T psi           U: rotation that made B_L(p-1)
+//     chi[(a d) J_L, b] = sum_{J_R} W(a, d, b; J_L, J_R) phi[a, (d b) J_R]
+//     guess[., e] = chi V^T           V: rotation that made B_R(p+1), e in dot(p+1) x B_R(p+2)
+//   backward (previous step p+1, this step p): the mirror image, with
+//     phi = psi V, the recoupling ((a d) J_L, r) -> (a, (d r) J_R) and
+//     guess = U chi.
+// W = (-1)^{(j_a + j_d + j_b + J)/2} sqrt((2J_L+1)(2J_R+1)) {j_a j_d J_L; j_b J J_R}
+// is the recoupling coefficient of three spins (no fermion signs: the site
+// order does not change).  Stages are grouped FP64 GEMMs and one build-copy.
+bool GpuEngine::transform_guess(const GuessInput& g, const Superblock& sb) {
+  if (!waves_ || nwaves_ < 1 || !g.rotated || !g.expanded || !g.dot) return false;
+  auto ri = block_rot_.find(g.rotated->handle);
+  auto ei = block_rot_.find(g.expanded->handle);
+  if (ri == block_rot_.end() || ei == block_rot_.end()) return false;
+  const RotRecord& rot = ri->second;  // U (forward) / V (backward)
+  const RotRecord& exp = ei->second;  // V (forward) / U (backward)
+  int64_t old_n = 0;
+  for (const auto& S : g.old_sectors) old_n = std::max<int64_t>(old_n, S.offset + (int64_t)S.rows * S.cols);
+  if (old_n != wave_n_) return false;
+  const StateInfo& newL = sb.L->si;
+  const StateInfo& newR = sb.R->si;
+  const int J = sb.target.s2;
+  // the rotations must belong to the state spaces they are applied to
+  const StateInfo& rot_big = g.forward ? g.old_L : g.old_R;
+  const StateInfo& exp_big = g.forward ? newR : newL;
+  if ((int)rot.n.size() != rot_big.size() || (int)exp.n.size() != exp_big.size()) return false;
+  for (int q = 0; q < rot_big.size(); ++q)
+    if (rot.m[q] > 0 && rot.n[q] != rot_big.states[q]) return false;
+  for (int q = 0; q < exp_big.size(); ++q)
+    if (exp.m[q] > 0 && exp.n[q] != exp_big.states[q]) return false;
+  if (!g.forward && !(g.old_L.is_product() && newR.is_product())) return false;
+  if (g.forward && !(g.old_R.is_product() && newL.is_product())) return false;
+  auto W = [&](int ja, int jd, int jb, int jl, int jr) {
+    const int ph = (ja + jd + jb + J) / 2;
+    return ((ph & 1) ? -1.0 : 1.0) * std::sqrt((double)(jl + 1) * (jr + 1)) * six_j(ja, jd, jl, jb, J, jr);
+  };
+  // stage A: phi per old sector
+  std::map<std::pair<int, int>, std::pair<int64_t, int>> phi;  // (row q, col q) -> (offset, cols)
+  std::vector<dev::GemmUnit> ua;
+  std::vector<dev::GemmItem> ia;
+  int64_t phi_n = 0;
+  for (const auto& S : g.old_sectors) {
+    dev::GemmUnit u{};
+    dev::GemmItem it{};
+    u.c_buf = 3;
+    u.beta_one = 0;
+    it.alpha = 1.0;
+    if (g.forward) {
+      const int a = rot.small_of_big[S.lq];
+      if (a < 0) continue;
+      const int m = rot.m[S.lq];
+      u.m = m;
+      u.n = S.cols;
+      u.ldc = S.cols;
+      it.a_buf = 0;  // U^T
+      it.a_off = rot.off[S.lq];
+      it.lda = m;
+      it.ta = 1;
+      it.b_buf = 2;  // psi
+      it.b_off = S.offset;
+      it.ldb = S.cols;
+      it.k = S.rows;
+      phi[{a, S.rq}] = {phi_n, S.cols};
+    } else {
+      const int r = rot.small_of_big[S.rq];
+      if (r < 0) continue;
+      const int m = rot.m[S.rq];
+      u.m = S.rows;
+      u.n = m;
+      u.ldc = m;
+      it.a_buf = 2;  // psi
+      it.a_off = S.offset;
+      it.lda = S.cols;
+      it.b_buf = 0;  // V
+      it.b_off = rot.off[S.rq];
+      it.ldb = m;
+      it.k = S.cols;
+      phi[{S.lq, r}] = {phi_n, m};
+    }
+    u.c_off = phi_n;
+    u.ibeg = (int)ia.size();
+    ia.push_back(it);
+    u.iend = (int)ia.size();
+    ua.push_back(u);
+    phi_n += (int64_t)u.m * u.n;
+  }
+  // stage B (chi, scaled copies) and stage C (GEMM into the new sectors)
+  std::vector<dev::CopyUnit> ub;
+  std::vector<dev::CopyItem> ib;
+  std::vector<dev::GemmUnit> uc;
+  std::vector<dev::GemmItem> ic;
+  int64_t chi_n = 0;
+  for (const auto& S : sb.sectors) {
+    if (g.forward) {
+      const int b = exp.small_of_big[S.rq];  // B_R(p+1) quantum behind the new right sector
+      if (b < 0) continue;
+      const int mb = exp.m[S.rq];
+      const int64_t chi0 = chi_n;
+      chi_n += (int64_t)S.rows * mb;
+      bool any = false;
+      for (const SectorPart& pt : newL.parts[S.lq]) {  // (a in B_L(p-1), d in dot(p))
+        dev::CopyUnit cu{};
+        cu.c_off = chi0 + (int64_t)pt.offset * mb;
+        cu.ldc = mb;
+        cu.m = pt.size;
+        cu.n = mb;
+        cu.ibeg = (int)ib.size();
+        const int ja = g.old_L.quanta[rot.big_of_small[pt.lq]].s2;
+        const int jd = g.dot->quanta[pt.rq].s2;
+        const int jb = g.expanded->si.quanta[b].s2;
+        for (const auto& jp : g.old_R.parts_of(pt.rq, b)) {  // old right quantum J_R with part (d, b)
+          auto f = phi.find({pt.lq, jp.first});
+          if (f == phi.end()) continue;
+          const double c = W(ja, jd, jb, newL.quanta[S.lq].s2, g.old_R.quanta[jp.first].s2);
+          if (c == 0.0) continue;
+          dev::CopyItem ci{};
+          ci.s_buf = 3;
+          ci.s_off = f->second.first + g.old_R.parts[jp.first][jp.second].offset;
+          ci.lds = f->second.second;
+          ci.alpha = c;
+          ib.push_back(ci);
+        }
+        cu.iend = (int)ib.size();
+        ub.push_back(cu);  // also when empty: the rectangle is zero-filled
+        any = any || cu.iend > cu.ibeg;
+      }
+      if (!any) continue;
+      dev::GemmUnit u{};
+      u.c_buf = 5;
+      u.c_off = S.offset;
+      u.ldc = S.cols;
+      u.m = S.rows;
+      u.n = S.cols;
+      u.beta_one = 0;
+      u.ibeg = (int)ic.size();
+      dev::GemmItem it{};
+      it.alpha = 1.0;
+      it.a_buf = 4;  // chi
+      it.a_off = chi0;
+      it.lda = mb;
+      it.b_buf = 1;  // V^T
+      it.b_off = exp.off[S.rq];
+      it.ldb = mb;
+      it.tb = 1;
+      it.k = mb;
+      ic.push_back(it);
+      u.iend = (int)ic.size();
+      uc.push_back(u);
+    } else {
+      const int a = exp.small_of_big[S.lq];  // B_L(p) quantum behind the new left sector
+      if (a < 0) continue;
+      const int ma = exp.m[S.lq];
+      const int64_t chi0 = chi_n;
+      chi_n += (int64_t)ma * S.cols;
+      bool any = false;
+      for (const SectorPart& pt : newR.parts[S.rq]) {  // (d in dot(p+1), r in B_R(p+2))
+        dev::CopyUnit cu{};
+        cu.c_off = chi0 + pt.offset;
+        cu.ldc = S.cols;
+        cu.m = ma;
+        cu.n = pt.size;
+        cu.ibeg = (int)ib.size();
+        const int ja = g.expanded->si.quanta[a].s2;
+        const int jd = g.dot->quanta[pt.lq].s2;
+        const int jr = g.old_R.quanta[rot.big_of_small[pt.rq]].s2;
+        for (const auto& jp : g.old_L.parts_of(a, pt.lq)) {  // old left quantum J_L with part (a, d)
+          auto f = phi.find({jp.first, pt.rq});
+          if (f == phi.end()) continue;
+          const double c = W(ja, jd, jr, g.old_L.quanta[jp.first].s2, newR.quanta[S.rq].s2);
+          if (c == 0.0) continue;
+          dev::CopyItem ci{};
+          ci.s_buf = 3;
+          ci.s_off = f->second.first + (int64_t)g.old_L.parts[jp.first][jp.second].offset * f->second.second;
+          ci.lds = f->second.second;
+          ci.alpha = c;
+          ib.push_back(ci);
+        }
+        cu.iend = (int)ib.size();
+        ub.push_back(cu);
+        any = any || cu.iend > cu.ibeg;
+      }
+      if (!any) continue;
+      dev::GemmUnit u{};
+      u.c_buf = 5;
+      u.c_off = S.offset;
+      u.ldc = S.cols;
+      u.m = S.rows;
+      u.n = S.cols;
+      u.beta_one = 0;
+      u.ibeg = (int)ic.size();
+      dev::GemmItem it{};
+      it.alpha = 1.0;
+      it.a_buf = 1;  // U
+      it.a_off = exp.off[S.lq];
+      it.lda = ma;
+      it.b_buf = 4;  // chi
+      it.b_off = chi0;
+      it.ldb = S.cols;
+      it.k = ma;
+      ic.push_back(it);
+      u.iend = (int)ic.size();
+      uc.push_back(u);
+    }
+  }
+  if (uc.empty()) return false;
+  std::vector<dev::GemmTask> ta, tc;
+  for (int u = 0; u < (int)ua.size(); ++u) add_tasks(ta, u, ua[u].m, ua[u].n);
+  for (int u = 0; u < (int)uc.size(); ++u) add_tasks(tc, u, uc[u].m, uc[u].n);
+  DevArray<dev::GemmUnit> dua, duc;
+  DevArray<dev::GemmItem> dia, dic;
+  DevArray<dev::GemmTask> dta, dtc;
+  DevArray<dev::CopyUnit> dub;
+  DevArray<dev::CopyItem> dib;
+  dua.upload(ua, stream_);
+  dia.upload(ia, stream_);
+  dta.upload(ta, stream_);
+  dub.upload(ub, stream_);
+  dib.upload(ib, stream_);
+  duc.upload(uc, stream_);
+  dic.upload(ic, stream_);
+  dtc.upload(tc, stream_);
+  double* phi_d = alloc(phi_n);
+  double* chi_d = alloc(chi_n);
+  const int nr = nwaves_;
+  if (guess_) free(guess_);
+  guess_ = alloc((int64_t)nr * sb.size);
+  cuda_check(cudaMemsetAsync(guess_, 0, (size_t)nr * sb.size * sizeof(double), stream_), "memset guess");
+  cuda_check(cudaMemsetAsync(chi_d, 0, (size_t)std::max<int64_t>(chi_n, 1) * sizeof(double), stream_), "memset chi");
+  for (int r = 0; r < nr; ++r) {
+    dev::Bufs bufs{};
+    bufs.p[0] = rot.d;
+    bufs.p[1] = exp.d;
+    bufs.p[2] = waves_ + (int64_t)r * wave_n_;
+    bufs.p[3] = phi_d;
+    bufs.p[4] = chi_d;
+    bufs.p[5] = guess_ + (int64_t)r * sb.size;
+    cuda_check(dev::launch_gemm(bufs, dua.d, dia.d, dta.d, (int)ta.size(), stream_), "guess stage A");
+    cuda_check(dev::launch_copy(bufs, chi_d, dub.d, dib.d, (int)ub.size(), stream_), "guess stage B");
+    cuda_check(dev::launch_gemm(bufs, duc.d, dic.d, dtc.d, (int)tc.size(), stream_), "guess stage C");
+  }
+  free(phi_d);
+  free(chi_d);
+  for (auto* a : {&dua, &duc}) a->release(stream_);
+  for (auto* a : {&dia, &dic}) a->release(stream_);
+  for (auto* a : {&dta, &dtc}) a->release(stream_);
+  dub.release(stream_);
+  dib.release(stream_);
+  // usable only if every root keeps a sizeable norm
+  double* work = alloc((int64_t)dev::kGramBlocks);
+  double* red = alloc(8);
+  bool ok = true;
+  for (int r = 0; r < nr && ok; ++r) {
+    const double* x = guess_ + (int64_t)r * sb.size;
+    cuda_check(dev::launch_gram(x, 1, x, 1, sb.size, sb.size, work, red, stream_), "guess norm");
+    double h = 0.0;
+    cuda_check(cudaMemcpyAsync(&h, red, sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
+    ok = std::isfinite(h) && h > 1e-4;
+  }
+  free(work);
+  free(red);
+  guess_n_ = sb.size;
+  nguess_ = ok ? nr : 0;
+  sync();
+  return ok;
+}
+
+std::string GpuEngine::step_stats() {
+  char buf[160];
+  std::snprintf(buf, sizeof(buf), "  [split sigma %ld x %.4fs, fp64 sigma %ld x %.4fs]", split_calls - last_split_calls_,
+                split_calls > last_split_calls_ ? (split_seconds - last_split_seconds_) / (split_calls - last_split_calls_)
+                                                : 0.0,
+                fp64_calls - last_fp64_calls_,
+                fp64_calls > last_fp64_calls_ ? (fp64_seconds - last_fp64_seconds_) / (fp64_calls - last_fp64_calls_)
+                                              : 0.0);
+  last_split_seconds_ = split_seconds;
+  last_fp64_seconds_ = fp64_seconds;
+  last_split_calls_ = split_calls;
+  last_fp64_calls_ = fp64_calls;
+  return buf;
 }
 
 // ------------------------------------------------------------------ density
@@ -1886,7 +2186,32 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
     }
   }
   flush();
-  // keep host copies for single-site blocks (never renormalised in practice)
+  // keep the rotation with the block (guess transform of later steps)
+  {
+    RotRecord rec;
+    const int nq = (int)rot_kept_.size();
+    rec.off = rot_off_;
+    rec.n = rot_rows_;
+    rec.m = rot_kept_;
+    rec.small_of_big.assign(nq, -1);
+    int64_t tot = 0;
+    for (int q = 0; q < nq; ++q) {
+      tot = std::max<int64_t>(tot, rot_off_[q] + (int64_t)rot_rows_[q] * rot_kept_[q]);
+      if (rot_kept_[q] > 0) {
+        rec.small_of_big[q] = (int)rec.big_of_small.size();
+        rec.big_of_small.push_back(q);
+      }
+    }
+    if (nq == big.si.size() && (int)rec.big_of_small.size() == small.si.size()) {
+      rec.d = alloc(tot);
+      cuda_check(cudaMemcpyAsync(rec.d, rot_, std::max<int64_t>(tot, 1) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 stream_),
+                 "keep rotation");
+      auto old = block_rot_.find(small.handle);
+      if (old != block_rot_.end()) free(old->second.d);
+      block_rot_[small.handle] = std::move(rec);
+    }
+  }
   sync();
 }
 

@@ -96,6 +96,8 @@ class GpuEngine : public Engine {
                    const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) override;
   int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) override;
   bool refine(const Superblock& sb, std::vector<double>& energies) override;
+  bool transform_guess(const GuessInput& g, const Superblock& sb) override;
+  std::string step_stats() override;
   void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
@@ -137,6 +139,9 @@ class GpuEngine : public Engine {
   long split_calls = 0, fp64_calls = 0;
   double split_seconds = 0.0, fp64_seconds = 0.0;
   double plan_seconds = 0.0;  // host time compiling sigma work lists
+  // counters at the previous step_stats() call
+  double last_split_seconds_ = 0.0, last_fp64_seconds_ = 0.0;
+  long last_split_calls_ = 0, last_fp64_calls_ = 0;
 
  private:
   struct Slices {
@@ -176,6 +181,17 @@ class GpuEngine : public Engine {
   std::vector<int64_t> rot_off_;
   std::vector<int> rot_kept_, rot_rows_;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  // rotation that made each renormalised block (big-block quantum q: n[q] x m[q]
+  // row-major at off[q]), kept for the wavefunction guess transform
+  struct RotRecord {
+    double* d = nullptr;
+    std::vector<int64_t> off;
+    std::vector<int> n, m, small_of_big, big_of_small;
+  };
+  std::map<int, RotRecord> block_rot_;
+  double* guess_ = nullptr;  // transformed guess vectors (nguess_ x guess_n_)
+  int64_t guess_n_ = 0;
+  int nguess_ = 0;
   // pipeline-wait status of the tensor-core kernels (device flag, pinned copy)
   int* tc_status_ = nullptr;
   int sm_count_ = 0;

@@ -358,6 +358,17 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   dp.deflation_max = C_.deflation_max;
   dp.seed = C_.seed + 104729ull * (uint64_t)(sweep_index * N_ + p);
   dp.defer_refine = opt_.refine_window > 0.0;
+  if (opt_.transform_guess && prev_.valid && prev_.forward == forward && prev_.p == (forward ? p - 1 : p + 1)) {
+    GuessInput g;
+    g.forward = forward;
+    g.old_L = prev_.L;
+    g.old_R = prev_.R;
+    g.old_sectors = prev_.sectors;
+    g.rotated = forward ? left_[p - 1].get() : right_[p + 2].get();
+    g.expanded = forward ? right_[p + 1].get() : left_[p].get();
+    g.dot = forward ? &dots_[p]->si : &dots_[p + 1]->si;
+    if (g.rotated && g.expanded) dp.use_guess = E_.transform_guess(g, sb);
+  }
   const int iters = E_.solve(sb, dp, energies);
   char prec_tag[64] = "";
   if (dp.defer_refine && !energies.empty()) {
@@ -390,9 +401,15 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
     right_[p + 1] = renormalised(R, kept, keepspec);
   }
   phase_.renorm_seconds += secs(t0);
-  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f%s  disc=%.3e\n", forward ? "fwd" : "bwd", p,
+  prev_.valid = true;
+  prev_.forward = forward;
+  prev_.p = p;
+  prev_.L = L.si;
+  prev_.R = R.si;
+  prev_.sectors = sb.sectors;
+  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f%s  disc=%.3e%s\n", forward ? "fwd" : "bwd", p,
       L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], prec_tag,
-      disc);
+      disc, E_.step_stats().c_str());
   E_.release_block(L);
   E_.release_block(R);
   return disc;

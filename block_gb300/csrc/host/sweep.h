@@ -52,6 +52,26 @@ struct DavidsonParams {
   // engines that iterate in a split precision: leave the FP64 Rayleigh-quotient
   // refinement of the energies to a later refine() call
   bool defer_refine = false;
+  // start from the engine's transformed guess (transform_guess) instead of
+  // unit vectors on the lowest diagonal elements
+  bool use_guess = false;
+};
+
+// The previous block step of the same sweep direction, for the wavefunction
+// guess transform (GuessWave::transform_previous_wavefunction,
+// guess_wavefunction.C:526-620): its enlarged blocks' state spaces and psi
+// sectors, the block renormalised at that step (B_L(p-1) in a forward sweep,
+// B_R(p+2) in a backward one), the block re-expanded through the rotation
+// that made it (B_R(p+1) forward, B_L(p) backward) and the single site
+// shared by the old right (forward) or left (backward) enlarged block and the
+// new left (forward) or right (backward) one.
+struct GuessInput {
+  bool forward = true;
+  StateInfo old_L, old_R;
+  std::vector<Superblock::Sector> old_sectors;
+  const Block* rotated = nullptr;
+  const Block* expanded = nullptr;
+  const StateInfo* dot = nullptr;
 };
 
 // Density-matrix spectrum of the block being renormalised: per sector of
@@ -75,6 +95,16 @@ class Engine {
   // Davidson on the superblock; energies of the converged roots.  The
   // wavefunctions stay inside the engine.
   virtual int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) = 0;
+  // prepares a guess for the next solve on `sb` by transforming the last
+  // solve's vectors; false if the engine cannot (the solve then starts from
+  // unit vectors)
+  virtual bool transform_guess(const GuessInput& g, const Superblock& sb) {
+    (void)g;
+    (void)sb;
+    return false;
+  }
+  // engine-specific timing of the last block step, for verbose logs
+  virtual std::string step_stats() { return std::string(); }
   // FP64 Rayleigh quotients of the last solve's vectors (no-op for engines
   // that solve in FP64); returns true if the energies changed precision
   virtual bool refine(const Superblock& sb, std::vector<double>& energies) {
@@ -113,6 +143,9 @@ struct DriverOptions {
   // refine only steps whose unrefined lowest energy is within this many Eh
   // of the sweep's lowest so far, and every sweep's last step
   double refine_window = 0.0;
+  // transform the previous step's wavefunction into the next step's guess
+  // (TRANSFORM guess); off: unit-vector guesses (BASIC guess) at every step
+  bool transform_guess = false;
   // optional hooks for tests: called after each superblock solve
   std::function<void(const Superblock&, int sweep, int step)> on_step;
 };
@@ -167,6 +200,13 @@ class SweepDriver {
   std::vector<double> last_energies_;
   double last_discarded_ = 0.0;
   SweepResult phase_;  // accumulates the per-phase wall times
+  // previous block step (guess transform)
+  struct PrevStep {
+    bool valid = false, forward = true;
+    int p = -1;
+    StateInfo L, R;
+    std::vector<Superblock::Sector> sectors;
+  } prev_;
   double sweep_best_unrefined_ = 0.0;
 };
 

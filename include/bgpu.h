@@ -77,6 +77,13 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
  * and always at the last step of every sweep (so that sweep and final
  * energies are FP64-refined).  0 refines every step.  Default 1e-3 Eh. */
 int bgpu_set_refine_window(bgpu_ctx* ctx, double eh);
+/* Davidson start of bgpu_run_dmrg's block steps: transform = 1 (default)
+ * transforms the previous step's wavefunction into the next step's state
+ * space when the two steps are consecutive in one sweep direction
+ * (TRANSFORM guess, guess_wavefunction.C:526-620), otherwise and with
+ * transform = 0 unit vectors on the lowest diagonal elements (BASIC guess,
+ * guess_wavefunction.C:258-273). */
+int bgpu_set_guess(bgpu_ctx* ctx, int transform);
 
 /*
  * Declare a block: its state space and operator catalogue.

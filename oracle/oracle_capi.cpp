@@ -32,7 +32,7 @@ struct Snapshot {
   double energy = 0.0;
   std::vector<int> orbsym;
   std::string group;
-  double sigma_seconds = 0.0;
+  double sigma_seconds = 0.0, sigma_seconds_1t = 0.0;
   double sigma_flops = 0.0;
   int threads = 1;
 };
@@ -180,7 +180,7 @@ void oracle_snapshot_block(void* h, int which, int* quanta, int* states, int* ke
 }
 
 // misc[0..2] target, misc[3] ecore, misc[4] energy <psi|H|psi>, misc[5] oracle sigma seconds,
-// misc[6] threads, misc[7] oracle sigma GEMM flops
+// misc[6] threads, misc[7] oracle sigma GEMM flops, misc[8] one-thread sigma seconds (0 if not timed)
 void oracle_snapshot_data(void* h, double* coef, int* ops, double* psi, double* sigma, double* diag, int* orbsym,
                           double* misc) {
   auto* s = static_cast<Snapshot*>(h);
@@ -198,6 +198,7 @@ void oracle_snapshot_data(void* h, double* coef, int* ops, double* psi, double* 
   misc[5] = s->sigma_seconds;
   misc[6] = s->threads;
   misc[7] = s->sigma_flops;
+  misc[8] = s->sigma_seconds_1t;
 }
 
 const char* oracle_snapshot_group(void* h) { return static_cast<Snapshot*>(h)->group.c_str(); }
@@ -236,7 +237,7 @@ extern "C" {
 // Superblock of `partition` built from seeded warm-up blocks (same
 // construction as bgpu_prepare_superblock) captured as a snapshot whose psi
 // is a seeded random unit vector.
-void* oracle_prepare(const char* conf, int partition, int threads, int reps) {
+void* oracle_prepare(const char* conf, int partition, int threads, int reps, int time_single) {
   auto snap = std::make_unique<Snapshot>();
   try {
     Config c = parse_config(conf);
@@ -273,6 +274,16 @@ void* oracle_prepare(const char* conf, int partition, int threads, int reps) {
     for (int r = 0; r < reps; ++r) eng.sigma(sb, snap->psi.data(), snap->sigma.data());
     snap->sigma_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() / reps;
     snap->sigma_flops = eng.last_sigma_flops;
+    if (time_single) {
+      // the same product on one thread
+      const int nt = eng.threads;
+      eng.threads = 1;
+      std::vector<double> tmp(sb.size, 0.0);
+      t0 = std::chrono::steady_clock::now();
+      eng.sigma(sb, snap->psi.data(), tmp.data());
+      snap->sigma_seconds_1t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      eng.threads = nt;
+    }
     snap->diag.assign(sb.size, 0.0);
     eng.hdiag(sb, snap->diag.data());
     snap->target[0] = sb.target.n;

@@ -31,7 +31,7 @@ def lib():
         L.oracle_snapshot.restype = P
         L.oracle_snapshot.argtypes = [ctypes.c_char_p, I, I, I]
         L.oracle_prepare.restype = P
-        L.oracle_prepare.argtypes = [ctypes.c_char_p, I, I, I]
+        L.oracle_prepare.argtypes = [ctypes.c_char_p, I, I, I, I]
         L.oracle_snapshot_free.argtypes = [P]
         L.oracle_snapshot_sizes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
         L.oracle_snapshot_block.argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), DP]
@@ -83,13 +83,14 @@ def _unpack(L, h):
     sig = np.zeros(n)
     diag = np.zeros(n)
     orbsym = np.zeros(norb, dtype=np.int32)
-    misc = np.zeros(8)
+    misc = np.zeros(9)
     L.oracle_snapshot_data(h, _ptr(coef, ctypes.c_double), _ptr(ops, ctypes.c_int), _ptr(psi, ctypes.c_double),
                            _ptr(sig, ctypes.c_double), _ptr(diag, ctypes.c_double), _ptr(orbsym, ctypes.c_int),
                            _ptr(misc, ctypes.c_double))
     snap.update(coef=coef, ops=ops.reshape(-1, 4), psi=psi, sigma=sig, diag=diag, orbsym=orbsym,
                 target=misc[0:3].astype(np.int32), ecore=misc[3], energy=misc[4], sigma_seconds=misc[5],
-                threads=int(misc[6]), flops=misc[7], group=L.oracle_snapshot_group(h).decode())
+                threads=int(misc[6]), flops=misc[7], sigma_seconds_1t=misc[8],
+                group=L.oracle_snapshot_group(h).decode())
     L.oracle_snapshot_free(h)
     return snap
 
@@ -100,11 +101,12 @@ def snapshot(conf, sweep, pos, threads=0):
     return _unpack(L, L.oracle_snapshot(conf.encode(), sweep, pos, threads))
 
 
-def prepare(conf, partition, threads=0, reps=1):
+def prepare(conf, partition, threads=0, reps=1, time_single=False):
     """Superblock built from seeded warm-up blocks (see bgpu_prepare_superblock);
-    the oracle sigma is timed over `reps` products (seconds per product)."""
+    the oracle sigma is timed over `reps` products (seconds per product), and
+    with time_single also once on one thread (sigma_seconds_1t)."""
     L = lib()
-    return _unpack(L, L.oracle_prepare(conf.encode(), partition, threads, reps))
+    return _unpack(L, L.oracle_prepare(conf.encode(), partition, threads, reps, int(bool(time_single))))
 
 
 def time_sigma(conf, sweep, pos, threads=0, reps=3):
