@@ -248,6 +248,14 @@ std::vector<std::vector<std::pair<int, int>>> sectors_by_left(const Superblock& 
   return by_l;
 }
 
+double env_double(const char* name, double dflt) {
+  const char* e = std::getenv(name);
+  if (!e || !*e) return dflt;
+  char* end = nullptr;
+  const double v = std::strtod(e, &end);
+  return (end && end != e && v > 0) ? v : dflt;
+}
+
 // adds the wall time of its scope to a counter
 struct PlanTimer {
   double& acc;
@@ -1053,7 +1061,11 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   // share is split into several tasks summed by the reduce kernel, every
   // other tile is one task writing its FP64 result directly
   const int nsm = sm_count();
-  auto item_cost = [](const TcItem& it, int hb) { return 400.0 + (double)it.kp * tc_round16(hb) / 8.0; };
+  // cost model of the LPT assignment (tuning: BGPU_TC_ITEM_COST = fixed cost of
+  // an item, BGPU_TC_SPLIT = phase-2 pieces per block)
+  static const double kItemFixed = env_double("BGPU_TC_ITEM_COST", 400.0);
+  static const double kSplit = env_double("BGPU_TC_SPLIT", 3.0);
+  auto item_cost = [](const TcItem& it, int hb) { return kItemFixed + (double)it.kp * tc_round16(hb) / 8.0; };
   std::vector<TcItem> i2;
   std::vector<TcTask> t2;
   std::vector<double> c2;
@@ -1068,7 +1080,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
     }
   }
-  const double chunk = std::max(total / (6.0 * nsm), 20000.0);
+  const double chunk = std::max(total / (2.0 * kSplit * nsm), 20000.0);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     const int ib = (int)i2.size();
