@@ -1,0 +1,49 @@
+"""Wavefunction guess transform between consecutive block steps
+(GuessWave::transform_previous_wavefunction, guess_wavefunction.C:526-620):
+the transformed guess starts each Davidson closer to its solution, so a
+sweep needs fewer sigma products, and converges to the same energies as
+sweeps started from unit vectors."""
+import json
+import os
+
+import pytest
+
+from conftest import GOLDEN, conf
+
+pytestmark = pytest.mark.gpu
+
+with open(os.path.join(GOLDEN, "golden.json")) as f:
+    GOLD = json.load(f)
+
+
+@pytest.fixture
+def guess_ctx(gpu_ctx):
+    yield gpu_ctx
+    gpu_ctx.set_guess(True)
+    gpu_ctx.set_precision("fp64")
+
+
+@pytest.mark.parametrize("name", ["syn8", "c2_d2h"])
+def test_transform_guess_fewer_products_same_energy(guess_ctx, name):
+    guess_ctx.set_guess(False)
+    e0, st0 = guess_ctx.run_dmrg(conf(name))
+    guess_ctx.set_guess(True)
+    e1, st1 = guess_ctx.run_dmrg(conf(name))
+    # syn8 at M=200 keeps every state (exact); c2_d2h truncates, and the two
+    # starts may pick slightly different truncations (reference tolerance)
+    tol = 1e-8 if name == "syn8" else 1e-6
+    for a, b in zip(e0, e1):
+        assert abs(a - b) <= tol, (name, a, b)
+    assert st1["sigma_calls"] < st0["sigma_calls"], (st1["sigma_calls"], st0["sigma_calls"])
+    if name in GOLD:
+        for got, ref in zip(e1, GOLD[name]["energies"]):
+            assert abs(got - ref) <= GOLD[name]["tolerance"]
+
+
+def test_transform_guess_split_precision(guess_ctx):
+    """Split-precision sweeps with the transformed guess keep the reference's
+    golden energy (FP64-refined)."""
+    guess_ctx.set_precision("bf16x3tc")
+    e, st = guess_ctx.run_dmrg(conf("hubbard"))
+    for got, ref in zip(e, GOLD["hubbard"]["energies"]):
+        assert abs(got - ref) <= GOLD["hubbard"]["tolerance"], (got, ref)
