@@ -22,6 +22,7 @@ struct bgpu_ctx {
   int device = 0;
   double refine_window = 1e-3;  // Eh; see bgpu_set_refine_window
   bool transform_guess = true;  // see bgpu_set_guess
+  int deferred_steps = 4;        // see bgpu_set_refine_window
   struct BlockRec {
     Block b;
     std::vector<OpKey> decl;  // declaration order
@@ -515,7 +516,10 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     Integrals I = load_integrals(c);
     DriverOptions opt;
     opt.verbose = verbose;
-    if (precision_slices(ctx->eng->precision)) opt.refine_window = ctx->refine_window;
+    if (precision_slices(ctx->eng->precision)) {
+      opt.refine_window = ctx->refine_window;
+      opt.deferred_steps = ctx->deferred_steps;
+    }
     opt.transform_guess = ctx->transform_guess;
     const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops, p0 = ctx->eng->plan_seconds;
     const long c0 = ctx->eng->sigma_calls;

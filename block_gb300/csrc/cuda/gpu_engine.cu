@@ -65,6 +65,8 @@ GpuEngine::~GpuEngine() {
   if (rot_) cudaFreeAsync(rot_, stream_);
   for (auto& kv : block_rot_)
     if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
+  for (auto& kv : parked_)
+    if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
   if (guess_) cudaFreeAsync(guess_, stream_);
   if (solver_work_) cudaFreeAsync(solver_work_, stream_);
   if (solver_info_) cudaFreeAsync(solver_info_, stream_);
@@ -1861,6 +1863,61 @@ bool GpuEngine::transform_guess(const GuessInput& g, const Superblock& sb) {
   nguess_ = ok ? nr : 0;
   sync();
   return ok;
+}
+
+int GpuEngine::park_vectors() {
+  if (!precision_slices(precision) || !waves_ || nwaves_ < 1) return -1;
+  Parked pk;
+  pk.nroots = nwaves_;
+  pk.n = wave_n_;
+  pk.d = alloc((int64_t)nwaves_ * wave_n_);
+  cuda_check(cudaMemcpyAsync(pk.d, waves_, (size_t)nwaves_ * wave_n_ * sizeof(double), cudaMemcpyDeviceToDevice,
+                             stream_),
+             "park vectors");
+  const int id = next_parked_++;
+  parked_[id] = pk;
+  return id;
+}
+
+// FP64 Rayleigh quotients of parked vectors, with a temporary FP64 plan of
+// their superblock (whose blocks the caller kept alive).
+bool GpuEngine::refine_parked(int id, const Superblock& sb, std::vector<double>& energies) {
+  auto it = parked_.find(id);
+  if (it == parked_.end() || it->second.n != sb.size) return false;
+  const Parked& pk = it->second;
+  SigmaPlan plan;
+  plan_sigma(sb, plan);
+  double* r = alloc(pk.n);
+  double* work = alloc((int64_t)dev::kGramBlocks);
+  double* red = alloc(8);
+  energies.assign(pk.nroots, 0.0);
+  for (int rr = 0; rr < pk.nroots; ++rr) {
+    auto t0 = std::chrono::steady_clock::now();
+    const double* b = pk.d + (int64_t)rr * pk.n;
+    sigma(sb, plan, b, r);
+    cuda_check(dev::launch_gram(b, 1, r, 1, pk.n, pk.n, work, red, stream_), "dot");
+    double h;
+    cuda_check(cudaMemcpyAsync(&h, red, sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
+    energies[rr] = h;
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    sigma_seconds += dt;
+    fp64_seconds += dt;
+    ++fp64_calls;
+  }
+  free(r);
+  free(work);
+  free(red);
+  free_plan(plan);
+  sync();
+  return true;
+}
+
+void GpuEngine::drop_parked(int id) {
+  auto it = parked_.find(id);
+  if (it == parked_.end()) return;
+  free(it->second.d);
+  parked_.erase(it);
 }
 
 std::string GpuEngine::step_stats() {

@@ -97,6 +97,9 @@ class GpuEngine : public Engine {
   int solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) override;
   bool refine(const Superblock& sb, std::vector<double>& energies) override;
   bool transform_guess(const GuessInput& g, const Superblock& sb) override;
+  int park_vectors() override;
+  bool refine_parked(int id, const Superblock& sb, std::vector<double>& energies) override;
+  void drop_parked(int id) override;
   std::string step_stats() override;
   void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
@@ -189,6 +192,13 @@ class GpuEngine : public Engine {
     std::vector<int> n, m, small_of_big, big_of_small;
   };
   std::map<int, RotRecord> block_rot_;
+  struct Parked {
+    double* d = nullptr;
+    int nroots = 0;
+    int64_t n = 0;
+  };
+  std::map<int, Parked> parked_;  // vectors kept for deferred energy refinement
+  int next_parked_ = 0;
   double* guess_ = nullptr;  // transformed guess vectors (nguess_ x guess_n_)
   int64_t guess_n_ = 0;
   int nguess_ = 0;

@@ -371,16 +371,26 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   }
   const int iters = E_.solve(sb, dp, energies);
   char prec_tag[64] = "";
+  int parked = -1;
+  double e_unrefined = 0.0;
   if (dp.defer_refine && !energies.empty()) {
     const bool last_step = forward ? (p == N_ - 3) : (p == 1);
-    const double e_unrefined = energies[0];
-    if (last_step || e_unrefined <= sweep_best_unrefined_ + opt_.refine_window) {
+    e_unrefined = energies[0];
+    sweep_best_unrefined_ = std::min(sweep_best_unrefined_, e_unrefined);
+    settle_candidates(false);  // steps now too far above the lowest one are dropped
+    const bool qualifies = e_unrefined <= sweep_best_unrefined_ + opt_.refine_window;
+    if (!last_step && qualifies && opt_.deferred_steps > 0) parked = E_.park_vectors();
+    if (parked >= 0) {
+      std::snprintf(prec_tag, sizeof(prec_tag), " (unrefined; refinement deferred)");
+    } else if (last_step || qualifies) {
       if (E_.refine(sb, energies))
         std::snprintf(prec_tag, sizeof(prec_tag), " (refined; unrefined %+.3e)", e_unrefined - energies[0]);
+      note_refined(energies);
     } else {
       std::snprintf(prec_tag, sizeof(prec_tag), " (unrefined)");
     }
-    sweep_best_unrefined_ = std::min(sweep_best_unrefined_, e_unrefined);
+  } else {
+    note_refined(energies);
   }
   phase_.solve_seconds += secs(t0);
   if (opt_.on_step) opt_.on_step(sb, sweep_index, p);
@@ -410,31 +420,86 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f%s  disc=%.3e%s\n", forward ? "fwd" : "bwd", p,
       L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], prec_tag,
       disc, E_.step_stats().c_str());
-  E_.release_block(L);
-  E_.release_block(R);
+  if (parked >= 0) {
+    // keep the step's enlarged blocks for a refinement at the end of the sweep
+    auto c = std::make_unique<Candidate>();
+    c->L = std::make_unique<Block>(std::move(L));
+    c->R = std::make_unique<Block>(std::move(R));
+    c->sb = std::move(sb);
+    c->sb.L = c->L.get();
+    c->sb.R = c->R.get();
+    c->parked = parked;
+    c->p = p;
+    c->e_unrefined = e_unrefined;
+    cands_.push_back(std::move(c));
+    while ((int)cands_.size() > opt_.deferred_steps) {
+      // over the limit: refine the highest one now
+      size_t hi = 0;
+      for (size_t i = 1; i < cands_.size(); ++i)
+        if (cands_[i]->e_unrefined > cands_[hi]->e_unrefined) hi = i;
+      refine_candidate(*cands_[hi]);
+      drop_candidate(cands_[hi]);
+      cands_.erase(cands_.begin() + hi);
+    }
+  } else {
+    E_.release_block(L);
+    E_.release_block(R);
+  }
   return disc;
 }
 
+void SweepDriver::note_refined(const std::vector<double>& e) {
+  if (!e.empty() && e[0] < sweep_refined_min_) {
+    sweep_refined_min_ = e[0];
+    sweep_refined_best_ = e;
+  }
+}
+
+void SweepDriver::refine_candidate(Candidate& c) {
+  std::vector<double> e(C_.nroots, 0.0);
+  if (E_.refine_parked(c.parked, c.sb, e)) {
+    log(1, "  refined p=%2d  E=%.12f (unrefined %+.3e)\n", c.p, e[0], c.e_unrefined - e[0]);
+    note_refined(e);
+  }
+}
+
+void SweepDriver::drop_candidate(std::unique_ptr<Candidate>& c) {
+  E_.drop_parked(c->parked);
+  E_.release_block(*c->L);
+  E_.release_block(*c->R);
+  c.reset();
+}
+
+// Drops the deferred steps whose unrefined energy is more than the window
+// above the sweep's lowest; at the end of the sweep refines the others.
+void SweepDriver::settle_candidates(bool end_of_sweep) {
+  for (auto& c : cands_) {
+    if (!c) continue;
+    const bool near = c->e_unrefined <= sweep_best_unrefined_ + opt_.refine_window;
+    if (end_of_sweep && near) refine_candidate(*c);
+    if (end_of_sweep || !near) drop_candidate(c);
+  }
+  cands_.erase(std::remove(cands_.begin(), cands_.end(), nullptr), cands_.end());
+}
+
 double SweepDriver::sweep(bool forward, int sweep_index) {
-  std::vector<double> best;
-  double emin = std::numeric_limits<double>::infinity();
   double maxdisc = 0.0;
   sweep_best_unrefined_ = std::numeric_limits<double>::infinity();
+  sweep_refined_min_ = std::numeric_limits<double>::infinity();
+  sweep_refined_best_.clear();
   auto one = [&](int p) {
     std::vector<double> e;
     maxdisc = std::max(maxdisc, step(forward, p, sweep_index, e));
-    if (!e.empty() && e[0] < emin) {
-      emin = e[0];
-      best = e;
-    }
-    last_energies_ = e;
+    last_energies_ = e;  // the last step of a sweep is always refined
   };
   if (forward)
     for (int p = 1; p <= N_ - 3; ++p) one(p);
   else
     for (int p = N_ - 3; p >= 1; --p) one(p);
+  settle_candidates(true);
   last_discarded_ = maxdisc;
-  return emin;
+  // sweep energy: the lowest refined step energy (Sweep::do_one, sweep.C:436-453)
+  return sweep_refined_min_;
 }
 
 SweepResult SweepDriver::run() {

@@ -103,6 +103,17 @@ class Engine {
     (void)sb;
     return false;
   }
+  // keeps a copy of the last solve's vectors for a later refine_parked();
+  // returns an id, or -1 if the engine does not defer refinements
+  virtual int park_vectors() { return -1; }
+  // FP64 Rayleigh quotients of parked vectors on their superblock
+  virtual bool refine_parked(int id, const Superblock& sb, std::vector<double>& energies) {
+    (void)id;
+    (void)sb;
+    (void)energies;
+    return false;
+  }
+  virtual void drop_parked(int id) { (void)id; }
   // engine-specific timing of the last block step, for verbose logs
   virtual std::string step_stats() { return std::string(); }
   // FP64 Rayleigh quotients of the last solve's vectors (no-op for engines
@@ -143,6 +154,11 @@ struct DriverOptions {
   // refine only steps whose unrefined lowest energy is within this many Eh
   // of the sweep's lowest so far, and every sweep's last step
   double refine_window = 0.0;
+  // with refine_window: keep up to this many steps (their enlarged blocks and
+  // vectors) whose refinement may still be needed and refine, at the end of
+  // the sweep, only those within the window of the sweep's lowest unrefined
+  // energy; 0 refines each qualifying step at once
+  int deferred_steps = 0;
   // transform the previous step's wavefunction into the next step's guess
   // (TRANSFORM guess); off: unit-vector guesses (BASIC guess) at every step
   bool transform_guess = false;
@@ -208,6 +224,21 @@ class SweepDriver {
     std::vector<Superblock::Sector> sectors;
   } prev_;
   double sweep_best_unrefined_ = 0.0;
+  // steps whose FP64 refinement is deferred (their blocks stay alive)
+  struct Candidate {
+    std::unique_ptr<Block> L, R;
+    Superblock sb;
+    int parked = -1;
+    int p = 0;
+    double e_unrefined = 0.0;
+  };
+  std::vector<std::unique_ptr<Candidate>> cands_;
+  double sweep_refined_min_ = 0.0;
+  std::vector<double> sweep_refined_best_;
+  void note_refined(const std::vector<double>& e);
+  void refine_candidate(Candidate& c);
+  void drop_candidate(std::unique_ptr<Candidate>& c);
+  void settle_candidates(bool end_of_sweep);
 };
 
 }  // namespace bgpu

@@ -75,7 +75,10 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
  * a step's energies with FP64 Rayleigh quotients only when its unrefined
  * lowest energy is within `eh` of the lowest one seen so far in the sweep,
  * and always at the last step of every sweep (so that sweep and final
- * energies are FP64-refined).  0 refines every step.  Default 1e-3 Eh. */
+ * energies are FP64-refined).  Qualifying steps are kept (their enlarged
+ * blocks and vectors, at most 4 at a time) and refined at the end of the
+ * sweep only if they are still within `eh` of the sweep's lowest unrefined
+ * energy.  0 refines every step.  Default 1e-3 Eh. */
 int bgpu_set_refine_window(bgpu_ctx* ctx, double eh);
 /* Davidson start of bgpu_run_dmrg's block steps: transform = 1 (default)
  * transforms the previous step's wavefunction into the next step's state
