@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16x3tc", choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc"])
+    ap.add_argument("--precision", default="bf16x3tc", choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc", "fp16x2tc"])
     ap.add_argument("--no-davidson", action="store_true", help="skip the FP64-vs-split Davidson comparison")
     ap.add_argument("--conf", default=DEFAULT_CONF)
     ap.add_argument("--partition", type=int, default=11)
@@ -275,7 +275,8 @@ def run_ours(a):
         pk = peaks.get("bf16_tflops", 1900.0)
         prods = 6 if a.precision == "bf16x6" else 3
         kname = ("tc_sigma_kernel<1>+<2> (tcgen05/TMEM two-phase sector GEMMs, bf16 slices)"
-                 if a.precision == "bf16x3tc" else "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)")
+                 if a.precision in ("bf16x3tc", "fp16x2tc")
+                 else "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)")
         traffic = NCU_TRAFFIC.get((os.path.relpath(a.conf, ROOT), a.partition, a.precision))
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
                 "traffic": traffic, "traffic_unit": "bytes per sigma (both tensor-core kernels, ncu)",
@@ -286,14 +287,16 @@ def run_ours(a):
                 "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
                 "note_issued": "3 (6) bf16 products per logical FP64 product, without tile padding",
                 "fp64_peak_tflops_in_run": fp64, "algorithmic_bytes_per_step": nbytes}
-    if a.precision == "bf16x3tc":
+    if a.precision in ("bf16x3tc", "fp16x2tc"):
         info = ctx.superblock_info(sb)
         roof["tc_mma_issued_tflops"] = info["tc_mma_flops"] / (kern_ms * 1e-3) / 1e12
         roof["tc_mma_issued_frac"] = roof["tc_mma_issued_tflops"] / roof["peak"]
         roof["tc_plan"] = {k: v for k, v in info.items() if k.startswith("tc_")}
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if a.precision == "fp64" else "bf16 slices, f32 accumulate",
+            "vs_baseline": None,
+            "dtype": {"fp64": "f64", "fp16x2tc": "fp16 slices, f32 accumulate"}.get(a.precision,
+                                                                                     "bf16 slices, f32 accumulate"),
             "data": "synthetic",
             "config": config_dict(a.conf, a.partition, n, a.precision, nbytes / 1e6),
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},

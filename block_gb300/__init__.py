@@ -16,7 +16,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libblockgb300.so")
 
 OP = dict(HAM=0, CRE=1, CRE_DES=2, CRE_CRE=3, CRE_DESCOMP=4, DES_DESCOMP=5, CRE_CRE_DESCOMP=6, OVERLAP=7)
-PREC = dict(fp64=0, bf16x3=1, bf16x6=2, bf16x3tc=3)
+PREC = dict(fp64=0, bf16x3=1, bf16x6=2, bf16x3tc=3, fp16x2tc=4)
 
 _lib = None
 

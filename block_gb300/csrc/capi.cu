@@ -118,7 +118,8 @@ int bgpu_set_refine_window(bgpu_ctx* ctx, double eh) {
 
 int bgpu_set_precision(bgpu_ctx* ctx, int p) {
   return guarded(ctx, [&] {
-    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6 || p == BGPU_PREC_BF16X3_TC,
+    need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6 || p == BGPU_PREC_BF16X3_TC ||
+             p == BGPU_PREC_FP16X2_TC,
          "unknown precision");
     need(ctx->eng != nullptr, "no device");
     ctx->eng->precision = (Precision)p;

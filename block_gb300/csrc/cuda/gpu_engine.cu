@@ -679,18 +679,7 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   sync();
 }
 
-void GpuEngine::free_plan(SigmaPlan& p) {
-  for (int i = 0; i < 3; ++i) {
-    if (p.psi_s[i]) cudaFreeAsync(p.psi_s[i], stream_);
-    p.psi_s[i] = nullptr;
-  }
-  p.ns = 0;
-  p.fi.release(stream_);
-  p.ft.release(stream_);
-  p.ftile.release(stream_);
-  if (p.partials) cudaFreeAsync(p.partials, stream_);
-  p.partials = nullptr;
-  p.fused = false;
+void GpuEngine::free_tc(SigmaPlan& p) {
   for (int i = 0; i < dev::kTcPools; ++i) {
     if (p.tc_pool[i]) cudaFreeAsync(p.tc_pool[i], stream_);
     p.tc_pool[i] = nullptr;
@@ -706,6 +695,21 @@ void GpuEngine::free_plan(SigmaPlan& p) {
   if (p.tc_partials) cudaFreeAsync(p.tc_partials, stream_);
   p.tc_partials = nullptr;
   p.tc = false;
+}
+
+void GpuEngine::free_plan(SigmaPlan& p) {
+  for (int i = 0; i < 3; ++i) {
+    if (p.psi_s[i]) cudaFreeAsync(p.psi_s[i], stream_);
+    p.psi_s[i] = nullptr;
+  }
+  p.ns = 0;
+  p.fi.release(stream_);
+  p.ft.release(stream_);
+  p.ftile.release(stream_);
+  if (p.partials) cudaFreeAsync(p.partials, stream_);
+  p.partials = nullptr;
+  p.fused = false;
+  free_tc(p);
   p.u1.release(stream_);
   p.u2.release(stream_);
   p.i1.release(stream_);
@@ -1281,6 +1285,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   for (int i = 0; i < kTcPools; ++i) {
     b.pool[i] = plan.tc_pool[i];
   }
+  b.fp16 = precision == Precision::FP16X2_TC ? 1 : 0;
+  plan.tc_fp16 = b.fp16 != 0;
   cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
   dops.release(stream_);
   plan.tc = true;
@@ -1288,6 +1294,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
 }
 
 void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, double* out, cudaEvent_t* marks) {
+  const bool fp16 = precision == Precision::FP16X2_TC;
+  if (p.tc && p.tc_fp16 != fp16) free_tc(p);  // operators packed in the other format
   if (!p.tc) plan_tc(sb, p);
   dev::TcBufs b{};
   b.src[0] = arena(*sb.L);
@@ -1298,6 +1306,7 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   }
   b.partials = p.tc_partials;
   b.status = tc_status_;
+  b.fp16 = fp16 ? 1 : 0;
   constexpr uint64_t kWaitLimitNs = 1000000000ull;
   cuda_check(dev::launch_tc_pack(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tc pack psi");
   if (marks) cuda_check(cudaEventRecord(marks[0], stream_), "record");
@@ -1315,13 +1324,13 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
 
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
   const int ns = precision_slices(precision);
-  if (precision == Precision::BF16X3_TC) sigma_tc(sb, p, psi, out);
+  if (precision_tc(precision)) sigma_tc(sb, p, psi, out);
   else if (ns) sigma_split(sb, p, ns, psi, out);
   else sigma(sb, p, psi, out);
 }
 
 int GpuEngine::sigma_launches(const SigmaPlan& p) const {
-  if (precision == Precision::BF16X3_TC) return 4 + (p.ecore != 0.0 ? 1 : 0);  // pack psi, phase 1, phase 2, reduce
+  if (precision_tc(precision)) return 4 + (p.ecore != 0.0 ? 1 : 0);  // pack psi, phase 1, phase 2, reduce
   if (precision_slices(precision)) return 3 + (p.ecore != 0.0 ? 1 : 0);  // slice psi, fused, reduce (+ecore)
   return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ru.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
 }
@@ -1341,7 +1350,7 @@ void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const doub
   if (ns) {
     SigmaPlan& pm = const_cast<SigmaPlan&>(p);
     auto call = [&](cudaEvent_t* marks) {
-      if (precision == Precision::BF16X3_TC) sigma_tc(sb, pm, psi, out, marks);
+      if (precision_tc(precision)) sigma_tc(sb, pm, psi, out, marks);
       else sigma_split(sb, pm, ns, psi, out, marks);
     };
     call(nullptr);  // slices / packs operators and buffers outside the timed region

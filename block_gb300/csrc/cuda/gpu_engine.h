@@ -22,10 +22,14 @@ namespace bgpu {
 // FP64, or split precision: bf16 slices on the tensor cores with f32
 // accumulation (BF16X3 / BF16X6: warp-level MMA kernel with 2 / 3 slices;
 // BF16X3_TC: tcgen05 / TMEM kernels with 2 slices)
-enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2, BF16X3_TC = 3 };
+// (FP16X2_TC: the tcgen05 kernels with 2 fp16 slices, 3 products)
+enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2, BF16X3_TC = 3, FP16X2_TC = 4 };
 inline int precision_slices(Precision p) {
-  return (p == Precision::BF16X3 || p == Precision::BF16X3_TC) ? 2 : p == Precision::BF16X6 ? 3 : 0;
+  return (p == Precision::BF16X3 || p == Precision::BF16X3_TC || p == Precision::FP16X2_TC) ? 2
+         : p == Precision::BF16X6                                                        ? 3
+                                                                                         : 0;
 }
+inline bool precision_tc(Precision p) { return p == Precision::BF16X3_TC || p == Precision::FP16X2_TC; }
 
 struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
@@ -69,6 +73,7 @@ struct SigmaPlan {
   // pools (built on first use): L / R operator blocks packed once, psi and
   // psi^T packed per product, S = stage-1 products written by phase 1
   bool tc = false;
+  bool tc_fp16 = false;  // slices of the packed pools are fp16 (else bf16)
   __nv_bfloat16* tc_pool[dev::kTcPools] = {};  // packed operands, hi and lo per block
   int64_t tc_pool_elems[dev::kTcPools] = {};
   DevArray<dev::TcPack> tc_psi_pack;
@@ -109,6 +114,7 @@ class GpuEngine : public Engine {
   // pieces used by the C ABI, the tests and the bench
   void plan_sigma(const Superblock& sb, SigmaPlan& plan);
   void free_plan(SigmaPlan& plan);
+  void free_tc(SigmaPlan& plan);  // tensor-core lists and pools only
   // device pointers, stream-ordered on stream()
   void sigma(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d);
   // split-precision product with `ns` bf16 slices (2 or 3)

@@ -187,9 +187,8 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(TcBufs b, const TcPack* __
       const int k = k0 + e;
       double x = 0.0;
       if (r < u.rows_v && k < u.cols_v) x = u.trans ? src[(int64_t)k * u.ld + r] : src[(int64_t)r * u.ld + k];
-      const __nv_bfloat16 xh = __double2bfloat16(x);
-      const __nv_bfloat16 xl = __double2bfloat16(x - (double)__bfloat162float(xh));
-      const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+      uint32_t bh, bl;
+      split16(x, b.fp16 != 0, bh, bl);
       if (e & 1) {
         hw[e >> 1] |= bh << 16;
         lw[e >> 1] |= bl << 16;
@@ -377,7 +376,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const int flags = (pf >> 16) & 0xff;
         if (lane == 0 && !(flags & kTcEmpty)) {
           const int h_a = hw & 0xffff, h_b = (hw >> 16) & 0xffff;
-          const uint32_t idesc = idesc_bf16(128, (h_b + 15) & ~15);
+          const uint32_t idesc = b.fp16 ? idesc_f16(128, (h_b + 15) & ~15) : idesc_bf16(128, (h_b + 15) & ~15);
           if ((flags & kTcGStart) &&
               !tc_wait(&sh.acc_empty[ab], aph ^ 1u, abort_flag, b.status, limit_ns))
             ok = false;
@@ -530,9 +529,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 #pragma unroll
               for (int e = 0; e < 8; ++e) {
                 const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
-                __nv_bfloat16 xh, xl;
-                split_bf16(x, xh, xl);
-                const uint32_t bh = __bfloat16_as_ushort(xh), bl = __bfloat16_as_ushort(xl);
+                uint32_t bh, bl;
+                split16(x, b.fp16 != 0, bh, bl);
                 if (e & 1) {
                   hw4[e >> 1] |= bh << 16;
                   lw4[e >> 1] |= bl << 16;

@@ -121,6 +121,7 @@ struct TcBufs {
   __nv_bfloat16* pool[kTcPools];
   float2* partials;
   int* status;  // set to 1 when a pipeline wait ran out
+  int fp16;     // slices are fp16 (else bf16)
 };
 
 cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cudaStream_t s);

@@ -12,6 +12,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace bgpu {
@@ -44,6 +45,36 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
          | (1u << 10)                     // B format bf16
          | ((uint32_t)(N >> 3) << 17)     // N / 8
          | ((uint32_t)(M >> 4) << 24);    // M / 16
+}
+
+// same with fp16 A and B
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// 16-bit slices: x ~= hi + lo with hi = round(x), lo = round(x - hi) in bf16
+// (8-bit significand, f32 range) or fp16 (11-bit significand, range +-65504)
+__device__ __forceinline__ void split16(float x, bool fp16, uint32_t& hi, uint32_t& lo) {
+  if (fp16) {
+    const __half h = __float2half_rn(x);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__float2half_rn(x - __half2float(h)));
+  } else {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    hi = __bfloat16_as_ushort(h);
+    lo = __bfloat16_as_ushort(__float2bfloat16_rn(x - __bfloat162float(h)));
+  }
+}
+__device__ __forceinline__ void split16(double x, bool fp16, uint32_t& hi, uint32_t& lo) {
+  if (fp16) {
+    const __half h = __double2half(x);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__double2half(x - (double)__half2float(h)));
+  } else {
+    const __nv_bfloat16 h = __double2bfloat16(x);
+    hi = __bfloat16_as_ushort(h);
+    lo = __bfloat16_as_ushort(__double2bfloat16(x - (double)__bfloat162float(h)));
+  }
 }
 
 // ---- TMEM ----

@@ -52,7 +52,9 @@ extern "C" {
  * with FP32 accumulation -- 2 slices / 3 products per logical product
  * (BF16X3) or 3 slices / 6 products (BF16X6) with warp-level MMAs, or
  * 2 slices / 3 products on tcgen05 with TMEM accumulators and bulk-copy
- * staged operands (BF16X3_TC).  With a split precision,
+ * staged operands (BF16X3_TC), or the same kernels with 2 fp16 slices
+ * (11-bit significands, values within +-65504; FP16X2_TC).  With a split
+ * precision,
  * bgpu_davidson and bgpu_run_dmrg iterate with split-precision sigma and
  * refine every converged root's energy with one FP64 sigma (Rayleigh
  * quotient against the FP64 Hamiltonian). */
@@ -60,6 +62,7 @@ extern "C" {
 #define BGPU_PREC_BF16X3 1
 #define BGPU_PREC_BF16X6 2
 #define BGPU_PREC_BF16X3_TC 3
+#define BGPU_PREC_FP16X2_TC 4
 
 typedef struct bgpu_ctx bgpu_ctx;
 

@@ -18,7 +18,7 @@ from test_gpu_sigma import SNAPS, load
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"bf16x3": 1e-4, "bf16x6": 5e-6, "bf16x3tc": 1e-4}
+TOL = {"bf16x3": 1e-4, "bf16x6": 5e-6, "bf16x3tc": 1e-4, "fp16x2tc": 1e-4}
 
 with open(os.path.join(GOLDEN, "golden.json")) as f:
     GOLD = json.load(f)
@@ -30,7 +30,7 @@ def split_ctx(gpu_ctx):
     gpu_ctx.set_precision("fp64")
 
 
-@pytest.mark.parametrize("prec", ["bf16x3", "bf16x6", "bf16x3tc"])
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16x6", "bf16x3tc", "fp16x2tc"])
 @pytest.mark.parametrize("name,sweep,pos", SNAPS)
 def test_split_sigma_accuracy(split_ctx, oracle, prec, name, sweep, pos):
     snap = oracle.snapshot(conf(name), sweep, pos)
