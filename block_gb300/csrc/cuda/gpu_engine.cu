@@ -258,6 +258,20 @@ double env_double(const char* name, double dflt) {
   return (end && end != e && v > 0) ? v : dflt;
 }
 
+// Prints the host time of the stages of a plan compiler (BGPU_PLAN_TIMING=1).
+struct PlanLaps {
+  const char* name;
+  bool on = env_double("BGPU_PLAN_TIMING", 0.0) > 0.5;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void lap(const char* what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[plan %s] %-24s %8.1f ms\n", name, what,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 // adds the wall time of its scope to a counter
 struct PlanTimer {
   double& acc;
@@ -444,6 +458,7 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
 // sector is owned by one unit (no atomics).
 void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   PlanTimer timer_(plan_seconds);
+  PlanLaps laps{"fp64"};
   const Block& L = *sb.L;
   const Block& R = *sb.R;
   const int J = sb.target.s2;
@@ -541,6 +556,7 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
       flops += 2.0 * SV.rows * SV.cols * mc;
     });
   }
+  laps.lap("stage-1 and items");
   // stage 2: one unit per sector; a sector whose 64x64 tiles carry more K
   // than a fair share of the FP64 pipe is split along its item list into
   // units writing partial sectors after the stage-1 intermediates, summed
@@ -626,6 +642,7 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   }
   std::stable_sort(cost.begin(), cost.end());
   for (auto& c : cost) add_tasks(t2, c.second, u2[c.second].m, u2[c.second].n);
+  laps.lap("stage-2 units");
   plan.u1.upload(u1, stream_);
   plan.i1.upload(i1, stream_);
   plan.t1.upload(t1, stream_);
@@ -643,6 +660,7 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   plan.nstage1_units = (int)u1.size();
   plan.nstage2_units = (int)u2.size();
   plan.nitems = (int)(i1.size() + i2.size());
+  laps.lap("uploads");
   // diagonal work list (diagonalH, spinblock.C:855-899)
   std::vector<dev::DiagUnit> du;
   std::vector<dev::DiagItem> di;
@@ -674,6 +692,7 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
     u.iend = (int)di.size();
     du.push_back(u);
   }
+  laps.lap("diagonal lists");
   plan.du.upload(du, stream_);
   plan.di.upload(di, stream_);
   sync();
@@ -901,6 +920,7 @@ void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const do
 // in phase 2, in the same order as the FP64 plan.
 void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   PlanTimer timer_(plan_seconds);
+  PlanLaps laps{"tc"};
   using namespace dev;
   const Block& L = *sb.L;
   const Block& R = *sb.R;
@@ -910,16 +930,19 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   parallel_for((int)sb.terms.size(), [&](int ti) {
     for_each_coupling(sb, sb.terms[ti], by_l, [&](const Coupling& c) { per_t[ti].push_back(c); });
   });
+  laps.lap("couplings");
   int64_t pool_n[kTcPools] = {0, 0, 0, 0, 0};
-  // (rows_p, kp) of every packed operand, by pool and offset: every item is
-  // checked against its tile below, so that no bulk copy leaves its operand
-  std::unordered_map<int64_t, std::pair<int, int>> dims[kTcPools];
+  // Every item is checked against the packed operands it reads (rows and K
+  // of its output sector), so that no bulk copy can leave its operand.
+  auto fail = []() { throw std::runtime_error("tensor-core plan: operand shape does not match its sector"); };
   std::vector<TcPack> ops_packs, psi_packs;
-  std::unordered_map<int64_t, int64_t> lmap, rmap;
-  auto pack_view = [&](int pool, const HostView& v, std::unordered_map<int64_t, int64_t>& m) -> int64_t {
+  std::unordered_map<int64_t, int> lmap, rmap;  // (block offset, transposed) -> index in ops_packs
+  lmap.reserve(1 << 16);
+  rmap.reserve(1 << 16);
+  auto pack_view = [&](int pool, const HostView& v, std::unordered_map<int64_t, int>& m) -> TcPack {
     const int64_t key = v.off * 2 + (v.trans ? 1 : 0);
     auto it = m.find(key);
-    if (it != m.end()) return it->second;
+    if (it != m.end()) return ops_packs[it->second];
     TcPack p{};
     p.src_off = v.off;
     p.ld = v.ld;
@@ -933,10 +956,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     p.pool = (uint8_t)pool;
     p.dst_off = pool_n[pool];
     pool_n[pool] += 2 * (int64_t)p.rows_p * p.kp;  // hi and lo
-    dims[pool][p.dst_off] = {p.rows_p, p.kp};
+    m.emplace(key, (int)ops_packs.size());
     ops_packs.push_back(p);
-    m.emplace(key, p.dst_off);
-    return p.dst_off;
+    return p;
   };
   std::vector<int64_t> psi_off(nsec), psit_off(nsec);
   for (int s = 0; s < nsec; ++s) {
@@ -953,7 +975,6 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     a.rt = kTcRowsA;
     a.dst_off = psi_off[s] = pool_n[kTcPoolPsi];
     pool_n[kTcPoolPsi] += 2 * (int64_t)a.rows_p * a.kp;
-    dims[kTcPoolPsi][a.dst_off] = {a.rows_p, a.kp};
     psi_packs.push_back(a);
     TcPack t = a;
     t.pool = kTcPoolPsiT;
@@ -965,39 +986,52 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     t.rt = kTcRowsB;
     t.dst_off = psit_off[s] = pool_n[kTcPoolPsiT];
     pool_n[kTcPoolPsiT] += 2 * (int64_t)t.rows_p * t.kp;
-    dims[kTcPoolPsiT][t.dst_off] = {t.rows_p, t.kp};
     psi_packs.push_back(t);
   }
   std::vector<TcItem> i1;
   std::vector<TcTask> t1;
   std::vector<int64_t> bundle1, bundle2;  // tasks reading the same A row tile
-  std::unordered_map<int64_t, int> s_unit_item;  // S offset -> its phase-1 item
   std::vector<std::vector<TcItem>> per_sector(nsec);
+  std::vector<std::vector<int>> per_sector_s(nsec);  // phase-1 item of a stage-1 operand, else -1
   double mma = 0.0;
   for (auto& cl : per_t) {
-    int cur_l = -1, cur_lp = -1, cur_rp = -1, cur_kp = 0;
+    int cur_l = -1, cur_lp = -1, cur_rp = -1, cur_kp = 0, cur_item = -1;
     int64_t cur_s = -1;
     for (const Coupling& c : cl) {
       if (c.va.identity && c.vb.identity) throw std::runtime_error("identity x identity pair term");
+      const auto& SV = sb.sectors[c.vs];
+      const int out_rows_p = tc_round8(SV.rows), out_cols_p = tc_round8(SV.cols);
       TcItem it{};
       if (c.va.identity) {  // sigma(lQ,rQ) += f psi(lQ,rQ') B^T
+        const TcPack pb = pack_view(1, c.vb, rmap);
         it.a_pool = kTcPoolPsi;
         it.a_off = psi_off[c.cs];
         it.b_pool = kTcPoolR;
-        it.b_off = pack_view(1, c.vb, rmap);
+        it.b_off = pb.dst_off;
         it.kp = tc_round16(R.si.states[c.rQp]);
         it.alpha = (float)(c.f * c.vb.scale);
+        const auto& C = sb.sectors[c.cs];
+        if (tc_round8(C.rows) != out_rows_p || tc_round16(C.cols) != it.kp || pb.rows_p != out_cols_p ||
+            pb.kp != it.kp)
+          fail();
         per_sector[c.vs].push_back(it);
+        per_sector_s[c.vs].push_back(-1);
         continue;
       }
       if (c.vb.identity) {  // sigma(lQ,rQ') += f s_L A psi(lQ',rQ')
+        const TcPack pa = pack_view(0, c.va, lmap);
         it.a_pool = kTcPoolL;
-        it.a_off = pack_view(0, c.va, lmap);
+        it.a_off = pa.dst_off;
         it.b_pool = kTcPoolPsiT;
         it.b_off = psit_off[c.cs];
         it.kp = tc_round16(L.si.states[c.lQp]);
         it.alpha = (float)(c.f * c.va.scale);
+        const auto& C = sb.sectors[c.cs];
+        if (pa.rows_p != out_rows_p || pa.kp != it.kp || tc_round8(C.cols) != out_cols_p ||
+            tc_round16(C.rows) != it.kp)
+          fail();
         per_sector[c.vs].push_back(it);
+        per_sector_s[c.vs].push_back(-1);
         continue;
       }
       if (!(c.lQ == cur_l && c.lQp == cur_lp && c.rQp == cur_rp)) {
@@ -1005,15 +1039,18 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         const int rows_p = tc_round8(mr), skp = tc_round16(mc);
         cur_s = pool_n[kTcPoolS];
         pool_n[kTcPoolS] += 2 * (int64_t)rows_p * skp;
-        s_unit_item[cur_s] = (int)i1.size();
-        dims[kTcPoolS][cur_s] = {rows_p, skp};
+        const TcPack pa = pack_view(0, c.va, lmap);
         TcItem a{};
         a.a_pool = kTcPoolL;
-        a.a_off = pack_view(0, c.va, lmap);
+        a.a_off = pa.dst_off;
         a.b_pool = kTcPoolPsiT;
         a.b_off = psit_off[c.cs];
         a.kp = tc_round16(k1);
         a.alpha = (float)c.va.scale;
+        const auto& C = sb.sectors[c.cs];
+        if (pa.rows_p != rows_p || pa.kp != a.kp || tc_round8(C.cols) != tc_round8(mc) ||
+            tc_round16(C.rows) != a.kp)
+          fail();
         const int idx = (int)i1.size();
         i1.push_back(a);
         for (int tm = 0; tm < (mr + 127) / 128; ++tm)
@@ -1035,34 +1072,44 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         cur_lp = c.lQp;
         cur_rp = c.rQp;
         cur_kp = skp;
+        cur_item = idx;
+        if (rows_p != out_rows_p) fail();
       }
+      const TcPack pb = pack_view(1, c.vb, rmap);
       it.a_pool = kTcPoolS;
       it.a_off = cur_s;
       it.b_pool = kTcPoolR;
-      it.b_off = pack_view(1, c.vb, rmap);
+      it.b_off = pb.dst_off;
       it.kp = cur_kp;
       it.alpha = (float)(c.f * c.vb.scale);
+      if (pb.rows_p != out_cols_p || pb.kp != it.kp) fail();
       per_sector[c.vs].push_back(it);
+      per_sector_s[c.vs].push_back(cur_item);
     }
   }
+  laps.lap("items");
   // alpha of a stage-1 product read by exactly one item moves into phase 1,
   // so that such items (alpha = 1) can share a tensor-core accumulator
   {
-    std::unordered_map<int64_t, int> consumers;
-    for (auto& v : per_sector)
-      for (const TcItem& it : v)
-        if (it.a_pool == kTcPoolS) ++consumers[it.a_off];
-    for (auto& v : per_sector)
-      for (TcItem& it : v)
-        if (it.a_pool == kTcPoolS && consumers[it.a_off] == 1) {
-          TcItem& u = i1[s_unit_item.at(it.a_off)];
-          u.alpha = (float)((double)u.alpha * (double)it.alpha);
-          it.alpha = 1.0f;
+    std::vector<int> consumers(i1.size(), 0);
+    for (auto& v : per_sector_s)
+      for (int u : v)
+        if (u >= 0) ++consumers[u];
+    for (int s = 0; s < nsec; ++s) {
+      auto& v = per_sector[s];
+      const auto& us = per_sector_s[s];
+      for (size_t k = 0; k < v.size(); ++k)
+        if (us[k] >= 0 && consumers[us[k]] == 1) {
+          TcItem& u = i1[us[k]];
+          u.alpha = (float)((double)u.alpha * (double)v[k].alpha);
+          v[k].alpha = 1.0f;
         }
+    }
     // items with alpha = 1 first, so that they form long accumulation runs
     for (auto& v : per_sector)
       std::stable_partition(v.begin(), v.end(), [](const TcItem& it) { return it.alpha == 1.0f; });
   }
+  laps.lap("alpha folding");
   // phase 2: sector tiles; a tile whose items cost more than a block's fair
   // share is split into several tasks summed by the reduce kernel, every
   // other tile is one task writing its FP64 result directly
@@ -1150,35 +1197,23 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   std::vector<double> c1;
   for (const TcTask& t : t1)
     c1.push_back(item_cost(i1[t.ibeg], std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn)) + 200.0);
-  auto check = [&](const TcTask& t, const std::vector<TcItem>& items) {
-    for (int x = t.ibeg; x < t.iend; ++x) {
-      const TcItem& it = items[x];
-      const auto a = dims[it.a_pool].find(it.a_off);
-      const auto b = dims[it.b_pool].find(it.b_off);
-      if (a == dims[it.a_pool].end() || b == dims[it.b_pool].end() || a->second.first != t.a_rows ||
-          b->second.first != t.b_rows || a->second.second != it.kp || b->second.second != it.kp ||
-          128 * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows)
-        throw std::runtime_error("tensor-core plan: operand shape does not match its tile");
-    }
-  };
-  for (const TcTask& t : t1) {
-    check(t, i1);
-    const auto sdim = dims[kTcPoolS].find(t.out_off);
-    if (sdim == dims[kTcPoolS].end() || sdim->second.first != t.a_rows || sdim->second.second != t.out_kp ||
-        kTcRowsB * t.tn >= t.out_kp)
-      throw std::runtime_error("tensor-core plan: stage-1 output does not match its tile");
-  }
-  for (const TcTask& t : t2) {
-    check(t, i2);
-    if (t.direct && (t.valid_rows > std::min(128, t.a_rows - 128 * t.tm) ||
-                     t.valid_cols > std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn)))
-      throw std::runtime_error("tensor-core plan: output tile larger than its operands");
-  }
+  laps.lap("phase-2 tasks");
+  // tiles inside their operands (item shapes were checked against their
+  // sectors above)
+  for (const TcTask& t : t1)
+    if (kTcRowsA * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows || kTcRowsB * t.tn >= t.out_kp) fail();
+  for (const TcTask& t : t2)
+    if (kTcRowsA * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows ||
+        (t.direct && (t.valid_rows > std::min(kTcRowsA, t.a_rows - kTcRowsA * t.tm) ||
+                      t.valid_cols > std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn))))
+      fail();
+  laps.lap("checks");
   std::vector<int> o1, o2;
   std::vector<int2> r1, r2;
   // two persistent blocks per SM (each kernel block runs its own pipeline)
   schedule_lpt(c1, bundle1, 2 * nsm, o1, r1);
   schedule_lpt(c2, bundle2, 2 * nsm, o2, r2);
+  laps.lap("schedule");
   // buffers
   for (int i = 0; i < kTcPools; ++i) {
     plan.tc_pool_elems[i] = pool_n[i];
@@ -1276,6 +1311,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     const int64_t st[5] = {(int64_t)t1.size(), (int64_t)t2.size(), (int64_t)i2.size(), full, (int64_t)tiles.size()};
     for (int i = 0; i < 5; ++i) plan.tc_stats[i] = st[i];
   }
+  laps.lap("flatten + upload");
   // operator blocks are packed once per plan
   DevArray<TcPack> dops;
   dops.upload(ops_packs, stream_);
@@ -1291,6 +1327,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   dops.release(stream_);
   plan.tc = true;
   sync();
+  laps.lap("pack operators");
 }
 
 void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, double* out, cudaEvent_t* marks) {
