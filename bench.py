@@ -321,6 +321,14 @@ def run_ours(a):
             t0 = time.perf_counter()
             e, _, it = ctx.davidson(sb, n, nroots=1, tol=1e-8)
             out[prec] = {"seconds": time.perf_counter() - t0, "iterations": it, "energy": float(e[0])}
+            out[prec]["graph_launches"] = ctx.davidson_graph_launches()
+        # the same solve with the iteration's launches issued one by one
+        # instead of as one captured CUDA graph per iteration
+        ctx.set_davidson_graph(False)
+        t0 = time.perf_counter()
+        e, _, it = ctx.davidson(sb, n, nroots=1, tol=1e-8)
+        out[a.precision]["seconds_without_graph"] = time.perf_counter() - t0
+        ctx.set_davidson_graph(True)
         ctx.set_precision(a.precision)
         if split:
             out["dE_split_minus_fp64"] = out[a.precision]["energy"] - out["fp64"]["energy"]

@@ -62,6 +62,8 @@ _SIGS = {
     "bgpu_superblock_info": (_I, [_P, _I, _DP, _I]),
     "bgpu_set_refine_window": (_I, [_P, ctypes.c_double]),
     "bgpu_set_guess": (_I, [_P, _I]),
+    "bgpu_set_davidson_graph": (_I, [_P, _I]),
+    "bgpu_davidson_graph_launches": (_I, [_P, _I64P]),
     "bgpu_tc_wait_selftest": (_I, [_P, ctypes.c_double, _IP, _IP, _DP]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
@@ -278,6 +280,17 @@ class Context:
         """Davidson start of run_dmrg steps: transformed previous wavefunction
         (True) or unit vectors (False)."""
         self._check(self.lib.bgpu_set_guess(self.h, int(bool(transform))))
+
+    def set_davidson_graph(self, on=True):
+        """Davidson iterations as launches of a captured CUDA graph (True) or
+        as the same launches issued one by one (False)."""
+        self._check(self.lib.bgpu_set_davidson_graph(self.h, int(bool(on))))
+
+    def davidson_graph_launches(self):
+        """Graph launches of the last Davidson solve."""
+        v = _I64()
+        self._check(self.lib.bgpu_davidson_graph_launches(self.h, ctypes.byref(v)))
+        return v.value
 
     def set_refine_window(self, eh):
         """FP64 energy refinement window of split-precision sweeps (Eh)."""

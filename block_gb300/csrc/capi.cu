@@ -109,6 +109,20 @@ int bgpu_set_guess(bgpu_ctx* ctx, int transform) {
   return guarded(ctx, [&] { ctx->transform_guess = transform != 0; });
 }
 
+int bgpu_set_davidson_graph(bgpu_ctx* ctx, int on) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    ctx->eng->dav_graph = on != 0;
+  });
+}
+
+int bgpu_davidson_graph_launches(bgpu_ctx* ctx, int64_t* launches) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr && launches, "bad arguments");
+    *launches = ctx->eng->dav_graph_launches_;
+  });
+}
+
 int bgpu_set_refine_window(bgpu_ctx* ctx, double eh) {
   return guarded(ctx, [&] {
     need(eh >= 0.0, "refine window must be >= 0");

@@ -54,6 +54,9 @@ GpuEngine::GpuEngine(int device) : device_(device) {
   cuda_check(cudaMemset(tc_status_, 0, sizeof(int)), "memset status");
   cuda_check(cudaMallocHost((void**)&tc_status_host_, sizeof(int)), "alloc status");
   *tc_status_host_ = 0;
+  cuda_check(cudaMallocHost((void**)&dav_host_, sizeof(dev::DavCtl)), "alloc davidson header");
+  const char* g = std::getenv("BGPU_DAVIDSON_GRAPH");
+  dav_graph = !(g && g[0] == '0');
 }
 
 GpuEngine::~GpuEngine() {
@@ -76,6 +79,7 @@ GpuEngine::~GpuEngine() {
   cudaEventDestroy(ev1_);
   cudaFree(tc_status_);
   cudaFreeHost(tc_status_host_);
+  cudaFreeHost(dav_host_);
   cudaStreamDestroy(stream_);
 }
 
@@ -1441,8 +1445,21 @@ void GpuEngine::hdiag(const Superblock& sb, const SigmaPlan& p, double* d) {
 
 // ------------------------------------------------------------------ Davidson
 
-// Linear::block_davidson (linear.C:179-385) with vectors and all O(n) work
-// on the GPU; the host only steers with the small subspace quantities.
+// Linear::block_davidson (linear.C:179-385) with the vectors, every O(n)
+// pass and every steering scalar on the GPU.  The first iteration's sigma
+// vectors and subspace matrix are formed eagerly; every later iteration is
+// one launch of a captured CUDA graph (the sigma of the newest basis vector,
+// its subspace row, the subspace eigenproblem, Ritz rotation, residual with
+// Olsen correction, convergence / deflation decisions, Gram-Schmidt and the
+// append), after which the host reads a 296-byte header to stop the loop.
+// dav_graph = false (BGPU_DAVIDSON_GRAPH=0) issues the same launches without
+// capture.
+//
+// After a Ritz rotation the basis diagonalises the projected Hamiltonian, so
+// the subspace matrix of the next iteration is diag(Ritz values) bordered by
+// the row of the new vector (b_new . sigma_j), instead of the reference's
+// full recomputation of b_i . sigma_j: the same matrix up to rounding, at
+// O(k n) instead of O(k^2 n) memory traffic per iteration.
 int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) {
   if (have_plan_) free_plan(plan_);
   plan_sigma(sb, plan_);
@@ -1451,24 +1468,39 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   const int nroots = p.nroots;
   if (n < nroots) throw std::runtime_error("superblock smaller than number of roots");
   const int kmax = std::max(p.deflation_max, nroots) + 1;
-  if (kmax > 32) throw std::runtime_error("Davidson subspace larger than 32 vectors");
-  double* diag = alloc(n);
-  double* B = alloc((int64_t)kmax * n);
-  double* S = alloc((int64_t)kmax * n);
-  double* T = alloc((int64_t)kmax * n);
-  double* r = alloc(n);
-  double* c0 = alloc(n);
-  double* work = alloc((int64_t)dev::kGramBlocks * 32);
-  double* red = alloc(64);
-  double* hmat = alloc(32 * 32);
-  double* hvec = alloc(32 * 32);
-  double* hw = alloc(32);
-  int64_t* offs = nullptr;
-  int* dims = nullptr;
-  int* status = nullptr;
-  cuda_check(cudaMallocAsync((void**)&offs, 2 * sizeof(int64_t), stream_), "alloc");
-  cuda_check(cudaMallocAsync((void**)&dims, sizeof(int), stream_), "alloc");
-  cuda_check(cudaMallocAsync((void**)&status, sizeof(int), stream_), "alloc");
+  if (kmax > dev::kDavMax) throw std::runtime_error("Davidson subspace larger than 32 vectors");
+  if (p.deflation_min < nroots || p.deflation_min >= p.deflation_max)
+    throw std::runtime_error("Davidson deflation sizes must satisfy nroots <= min < max");
+  // buffers and graphs of this solve, released on every exit
+  struct Scope {
+    GpuEngine& e;
+    std::vector<double*> bufs;
+    dev::DavCtl* ctl = nullptr;
+    cudaGraphExec_t gx[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    ~Scope() {
+      cudaStreamSynchronize(e.stream_);
+      for (auto& g : gx)
+        if (g) cudaGraphExecDestroy(g);
+      for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+      for (double* q : bufs) e.free(q);
+      if (ctl) cudaFreeAsync(ctl, e.stream_);
+    }
+  } sc{*this};
+  auto buf = [&](int64_t elems) {
+    sc.bufs.push_back(alloc(elems));
+    return sc.bufs.back();
+  };
+  double* diag = buf(n);
+  double* B = buf((int64_t)kmax * n);
+  double* S = buf((int64_t)kmax * n);
+  double* r = buf(n);
+  double* y = buf(n);
+  double* work = buf((int64_t)dev::kDavBlocks * dev::kDavMax);
+  double* red = buf(dev::kDavMax);
+  cuda_check(cudaMallocAsync((void**)&sc.ctl, sizeof(dev::DavCtl), stream_), "alloc");
+  for (auto& x : sc.ev) cuda_check(cudaEventCreate(&x), "event");
   hdiag(sb, plan_, diag);
   std::vector<double> hd(n);
   cuda_check(cudaMemcpyAsync(hd.data(), diag, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h diag");
@@ -1492,120 +1524,126 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     cuda_check(cudaMemcpyAsync(B, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "guess");
     sync();
   }
-  auto dot = [&](const double* x, const double* y) {
-    cuda_check(dev::launch_gram(x, 1, y, 1, n, n, work, red, stream_), "dot");
-    double h;
-    cuda_check(cudaMemcpyAsync(&h, red, sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
-    sync();
-    return h;
-  };
   auto row = [&](double* M, int i) { return M + (int64_t)i * n; };
+  auto dots = [&](const double* X, int nx, const double* v, double* out) {
+    cuda_check(dev::launch_gram(X, nx, v, 1, n, n, work, red, stream_), "dot");
+    cuda_check(cudaMemcpyAsync(out, red, nx * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
+  };
   for (int i = 0; i < nroots; ++i) {
-    for (int j = 0; j < i; ++j) cuda_check(dev::launch_axpy(-dot(row(B, j), row(B, i)), row(B, j), row(B, i), n, stream_), "gs");
-    cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(row(B, i), row(B, i))), row(B, i), n, stream_), "norm");
+    double h;
+    for (int j = 0; j < i; ++j) {
+      dots(row(B, j), 1, row(B, i), &h);
+      cuda_check(dev::launch_axpy(-h, row(B, j), row(B, i), n, stream_), "gs");
+    }
+    dots(row(B, i), 1, row(B, i), &h);
+    cuda_check(dev::launch_scale(1.0 / std::sqrt(h), row(B, i), n, stream_), "norm");
   }
-  int k = nroots, ks = 0;  // basis size, number of sigma vectors
-  int converged = 0, iter = 0;
-  std::vector<double> lam;
-  while (true) {
-    ++iter;
-    for (; ks < k; ++ks) {
-      auto t0 = std::chrono::steady_clock::now();
-      sigma_any(sb, plan_, row(B, ks), row(S, ks));
-      sync();
-      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-      sigma_seconds += dt;
-      if (precision_slices(precision)) {
-        split_seconds += dt;
-        ++split_calls;
-      } else {
-        fp64_seconds += dt;
-        ++fp64_calls;
-      }
-    }
-    // subspace matrix h_ij = b_i . sigma_j
-    std::vector<double> h((size_t)k * k);
-    for (int j = 0; j < k; ++j)
-      cuda_check(dev::launch_gram(B, k, row(S, j), 1, n, n, work, red + 0, stream_), "gram"),
-          cuda_check(cudaMemcpyAsync(h.data() + (size_t)j * k, red, k * sizeof(double), cudaMemcpyDeviceToHost, stream_),
-                     "d2h");
-    sync();
-    // symmetrise as the reference does (lower triangle of b_i . sigma_j)
-    std::vector<double> hs((size_t)k * k);
-    for (int i = 0; i < k; ++i)
-      for (int j = 0; j <= i; ++j) hs[(size_t)i * k + j] = hs[(size_t)j * k + i] = h[(size_t)j * k + i];
-    // subspace eigenproblem on the GPU (batched Jacobi, one matrix)
-    cuda_check(cudaMemcpyAsync(hmat, hs.data(), hs.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
-    int64_t ho[2] = {0, 0};
-    cuda_check(cudaMemcpyAsync(offs, ho, sizeof(ho), cudaMemcpyHostToDevice, stream_), "h2d");
-    cuda_check(cudaMemcpyAsync(dims, &k, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d");
-    cuda_check(dev::launch_jacobi(hmat, offs, dims, hw, offs + 1, hvec, offs, status, 1, k, stream_), "subspace eig");
-    std::vector<double> alpha((size_t)k * k);
-    lam.assign(k, 0.0);
-    int st = 0;
-    cuda_check(cudaMemcpyAsync(lam.data(), hw, k * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
-    cuda_check(cudaMemcpyAsync(alpha.data(), hvec, alpha.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
-    cuda_check(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
-    sync();
-    if (st < 0) throw std::runtime_error("subspace eigensolver did not converge");
-    // Ritz vectors: b'_j = sum_i alpha_ij b_i (same for sigma)
-    cuda_check(cudaMemcpyAsync(hmat, alpha.data(), alpha.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
-    cuda_check(dev::launch_combine(B, k, n, n, hmat, k, T, n, stream_), "ritz b");
-    std::swap(B, T);
-    cuda_check(dev::launch_combine(S, k, n, n, hmat, k, T, n, stream_), "ritz s");
-    std::swap(S, T);
-    auto resid = [&](int i) {
-      cuda_check(cudaMemcpyAsync(r, row(S, i), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy");
-      cuda_check(dev::launch_axpy(-lam[i], row(B, i), r, n, stream_), "axpy");
-    };
-    for (int i = 0; i < converged; ++i) {
-      resid(i);
-      if (dot(r, r) > p.tol) {
-        converged = i;
-        break;
-      }
-    }
-    resid(converged);
-    const double rnorm = dot(r, r);
-    {  // Olsen preconditioner (linear.C:50-60)
-      cuda_check(cudaMemcpyAsync(c0, row(B, converged), n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy");
-      cuda_check(dev::launch_precondition(c0, diag, lam[converged], n, stream_), "precond");
-      const double num = dot(c0, r), den = dot(row(B, converged), c0);
-      cuda_check(dev::launch_axpy(-num / den, row(B, converged), r, n, stream_), "olsen");
-      cuda_check(dev::launch_precondition(r, diag, lam[converged], n, stream_), "precond");
-    }
-    if (rnorm < p.tol) {
-      ++converged;
-      if (converged == nroots) break;
+  auto count_sigma = [&](double dt) {
+    sigma_seconds += dt;
+    if (precision_slices(precision)) {
+      split_seconds += dt;
+      ++split_calls;
     } else {
-      if (k >= p.deflation_max) {
-        k = p.deflation_min;
-        ks = std::min(ks, k);
-      }
-      // classical Gram-Schmidt applied twice against the whole basis (the
-      // reference orthogonalises one basis vector at a time; same span and
-      // normalised result, without a host round trip per basis vector)
-      for (int pass = 0; pass < 2; ++pass) {
-        cuda_check(dev::launch_gram(B, k, r, 1, n, n, work, red, stream_), "gs coefficients");
-        cuda_check(dev::launch_project_out(B, k, n, n, red, r, stream_), "gs");
-      }
-      cuda_check(dev::launch_scale(1.0 / std::sqrt(dot(r, r)), r, n, stream_), "scale");
-      cuda_check(cudaMemcpyAsync(row(B, k), r, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "append");
-      ++k;
+      fp64_seconds += dt;
+      ++fp64_calls;
     }
-    if (iter >= p.max_iter) break;
+  };
+  // first iteration: sigma of every start vector, whole subspace matrix
+  // h_ij = b_i . sigma_j (j <= i, symmetrised as linear.C:268-272)
+  for (int i = 0; i < nroots; ++i) {
+    auto t0 = std::chrono::steady_clock::now();
+    sigma_any(sb, plan_, row(B, i), row(S, i));
+    sync();
+    count_sigma(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
   }
-  energies.assign(lam.begin(), lam.begin() + nroots);
+  dev::DavCtl c0{};
+  {
+    std::vector<double> col(nroots);
+    for (int j = 0; j < nroots; ++j) {
+      dots(B, nroots, row(S, j), col.data());  // b_i . sigma_j
+      for (int i = j; i < nroots; ++i) c0.h[i * nroots + j] = c0.h[j * nroots + i] = col[i];
+    }
+  }
+  c0.k = nroots;
+  c0.mode = 2;
+  cuda_check(cudaMemcpyAsync(sc.ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice, stream_), "h2d ctl");
+  sync();
+  dev::DavBufs db{B, S, r, diag, y, work, sc.ctl, n, nroots, p.deflation_min, p.deflation_max, p.tol};
+  // one iteration; with_sigma: the newest basis vector (left in r) has no sigma yet
+  // (event records inside a capture become external event nodes; outside a
+  // capture the external flag is refused)
+  auto enqueue = [&](bool with_sigma, bool capturing) {
+    const unsigned rec = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if (with_sigma) {
+      cuda_check(cudaEventRecordWithFlags(sc.ev[0], stream_, rec), "record");
+      sigma_any(sb, plan_, r, y);
+      cuda_check(cudaEventRecordWithFlags(sc.ev[1], stream_, rec), "record");
+      cuda_check(dev::launch_dav_new_row(db, stream_), "davidson row");
+    }
+    cuda_check(dev::launch_dav_update(db, stream_), "davidson update");
+    cuda_check(cudaMemcpyAsync(dav_host_, sc.ctl, dev::kDavHeaderBytes, cudaMemcpyDeviceToHost, stream_), "d2h ctl");
+  };
+  const bool use_graph = dav_graph;
+  auto capture = [&](bool with_sigma) {
+    const double f0 = sigma_flops;
+    const long c0n = sigma_calls;
+    cudaGraph_t g = nullptr;
+    cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed), "begin capture");
+    try {
+      enqueue(with_sigma, true);
+    } catch (...) {
+      cudaStreamEndCapture(stream_, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    cuda_check(cudaStreamEndCapture(stream_, &g), "end capture");
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    cuda_check(e, "instantiate");
+    sigma_flops = f0;  // the captured launches ran nothing
+    sigma_calls = c0n;
+    return x;
+  };
+  bool with_sigma = false;
+  int iter = 0;
+  dav_graph_launches_ = 0;
+  while (true) {
+    const int w = with_sigma ? 1 : 0;
+    auto t0 = std::chrono::steady_clock::now();
+    if (use_graph) {
+      if (!sc.gx[w]) sc.gx[w] = capture(with_sigma);
+      cuda_check(cudaGraphLaunch(sc.gx[w], stream_), "graph launch");
+      ++dav_graph_launches_;
+      if (with_sigma) {
+        sigma_flops += plan_.flops;
+        ++sigma_calls;
+      }
+    } else {
+      enqueue(with_sigma, false);
+    }
+    sync();
+    if (with_sigma) {
+      float ms = 0.f;
+      double dt;
+      if (cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]) == cudaSuccess) dt = ms * 1e-3;
+      else dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      count_sigma(dt);
+    }
+    const dev::DavCtl& h = *dav_host_;
+    if (h.status < 0) throw std::runtime_error("subspace eigensolver did not converge");
+    iter = h.iter;
+    if (h.done || iter >= p.max_iter) break;
+    with_sigma = h.expand != 0;
+  }
+  energies.assign(dav_host_->lam, dav_host_->lam + nroots);
   if (waves_) free(waves_);
   waves_ = alloc((int64_t)nroots * n);
   cuda_check(cudaMemcpyAsync(waves_, B, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "waves");
   wave_n_ = n;
   nwaves_ = nroots;
   if (precision_slices(precision) && !p.defer_refine) refine(sb, energies);
-  for (double* q : {diag, B, S, T, r, c0, work, red, hmat, hvec, hw}) free(q);
-  cudaFreeAsync(offs, stream_);
-  cudaFreeAsync(dims, stream_);
-  cudaFreeAsync(status, stream_);
   sync();
   return iter;
 }

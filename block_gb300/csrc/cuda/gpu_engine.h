@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../host/sweep.h"
+#include "k_dav.cuh"
 #include "k_fused.cuh"
 #include "k_split.cuh"
 #include "k_tc.cuh"
@@ -212,6 +213,14 @@ class GpuEngine : public Engine {
   int* tc_status_ = nullptr;
   int sm_count_ = 0;
   int* tc_status_host_ = nullptr;
+  // header of the Davidson control record, read back after every iteration
+  dev::DavCtl* dav_host_ = nullptr;
+
+ public:
+  // Davidson iterations as launches of a captured CUDA graph (else the same
+  // launches issued one by one); graph launches of the last solve
+  bool dav_graph = true;
+  long dav_graph_launches_ = 0;
 };
 
 }  // namespace bgpu

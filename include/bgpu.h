@@ -90,6 +90,17 @@ int bgpu_set_refine_window(bgpu_ctx* ctx, double eh);
  * transform = 0 unit vectors on the lowest diagonal elements (BASIC guess,
  * guess_wavefunction.C:258-273). */
 int bgpu_set_guess(bgpu_ctx* ctx, int transform);
+/* Davidson iterations (bgpu_davidson, bgpu_run_dmrg) as launches of a
+ * captured CUDA graph: on = 1 (default, unless the environment sets
+ * BGPU_DAVIDSON_GRAPH=0) captures one iteration (the sigma of the newest
+ * basis vector, subspace eigenproblem, Ritz rotation, Olsen residual,
+ * convergence and deflation decisions, Gram-Schmidt) once per solve and
+ * launches it per iteration; on = 0 issues the same launches one by one.
+ * Results are identical.  No reference counterpart (the reference steps
+ * Linear::block_davidson, linear.C:179-385, on the host). */
+int bgpu_set_davidson_graph(bgpu_ctx* ctx, int on);
+/* Graph launches of the last Davidson solve (0 when it ran without capture). */
+int bgpu_davidson_graph_launches(bgpu_ctx* ctx, int64_t* launches);
 
 /*
  * Declare a block: its state space and operator catalogue.

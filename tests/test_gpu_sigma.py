@@ -60,3 +60,36 @@ def test_davidson_matches_dense(gpu_ctx, oracle, name, sweep, pos):
     assert snap["energy"] >= w[0] - 1e-10
     r = gpu_ctx.sigma(sb, v[0]) - e[0] * v[0]
     assert np.dot(r, r) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16x3tc"])
+def test_davidson_graph_roots(gpu_ctx, oracle, prec):
+    """Three roots through the device-resident Davidson: the captured-graph
+    iteration and the same launches issued one by one give identical
+    energies and iteration counts, and the roots match dense
+    diagonalisation (the split path after its FP64 Rayleigh refinement)."""
+    snap = oracle.snapshot(conf("hubbard"), 1, 3)
+    sb, n = load(gpu_ctx, snap)
+    H = np.empty((n, n))
+    eye = np.eye(n)
+    gpu_ctx.set_precision("fp64")
+    for j in range(n):
+        H[:, j] = gpu_ctx.sigma(sb, eye[j])
+    w = np.linalg.eigvalsh(0.5 * (H + H.T))
+    gpu_ctx.set_precision(prec)
+    try:
+        out = {}
+        for graph in (True, False):
+            gpu_ctx.set_davidson_graph(graph)
+            e, v, it = gpu_ctx.davidson(sb, n, nroots=3, tol=1e-12 if prec == "fp64" else 1e-9, vectors=True)
+            out[graph] = (e, v, it, gpu_ctx.davidson_graph_launches())
+        assert out[True][3] > 0 and out[False][3] == 0
+        assert out[True][2] == out[False][2]
+        assert np.array_equal(out[True][0], out[False][0])
+        assert np.array_equal(out[True][1], out[False][1])
+        e = out[True][0]
+        tol = 1e-9 if prec == "fp64" else 1e-8
+        assert np.max(np.abs(e - w[:3])) <= tol, (e, w[:3])
+    finally:
+        gpu_ctx.set_davidson_graph(True)
+        gpu_ctx.set_precision("fp64")
