@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--partition", type=int, default=11)
     ap.add_argument("--cpu-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="default schedule knobs instead of the autotuner's (tensor-core paths)")
+    ap.add_argument("--no-schedules", action="store_true",
+                    help="skip the per-sector-launch baseline and default-knob comparison")
     ap.add_argument("--profile", action="store_true",
                     help="open the CUDA profiler range around the device-timed steps only")
     return ap.parse_args()
@@ -222,6 +226,11 @@ def run_ours(a):
         dist.init_process_group("nccl")
     ctx = block_gb300.Context(local)
     ctx.set_precision(a.precision)
+    tc_path = a.precision in ("bf16x3tc", "fp16x2tc")
+    if tc_path and not a.no_autotune:
+        # schedule knobs chosen by timing candidates on the first product
+        # (untimed warm-up), keyed on the sector-size histogram
+        ctx.set_autotune(True)
     sb, n = ctx.prepare_superblock(a.conf, a.partition)
     flops, nbytes = ctx.superblock_work(sb)
     launches = ctx.superblock_launches(sb)
@@ -287,7 +296,7 @@ def run_ours(a):
                 "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
                 "note_issued": "3 (6) bf16 products per logical FP64 product, without tile padding",
                 "fp64_peak_tflops_in_run": fp64, "algorithmic_bytes_per_step": nbytes}
-    if a.precision in ("bf16x3tc", "fp16x2tc"):
+    if tc_path:
         info = ctx.superblock_info(sb)
         roof["tc_mma_issued_tflops"] = info["tc_mma_flops"] / (kern_ms * 1e-3) / 1e12
         roof["tc_mma_issued_frac"] = roof["tc_mma_issued_tflops"] / roof["peak"]
@@ -302,6 +311,31 @@ def run_ours(a):
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
             "gpu_launches": launches * a.steps, "clocks": clocks, "roofline": roof,
             "sigma_flops_per_step": flops, "kernel_ms_per_step": [ms[1] / a.steps, ms[2] / a.steps]}
+    if tc_path and not a.no_schedules:
+        # one persistent launch per phase against the per-sector-launch
+        # baseline (one launch per sector, one block per tile), and the
+        # autotuned knobs against the defaults
+        sched = {"autotuned": not a.no_autotune,
+                 "knobs": {k: info[k] for k in ("tc_item_cost", "tc_split", "tc_group")},
+                 "launches_per_sigma": info["launches"], "ms_per_sigma": t_step * 1e3}
+        reps = max(2, min(a.steps, 5))
+        ctx.set_autotune(False)
+        ctx.set_tc_schedule(True)
+        ms_ps = ctx.sigma_timed(sb, x, y, reps)
+        sched["per_sector"] = {"ms_per_sigma": ms_ps[0] / reps,
+                               "launches_per_sigma": ctx.superblock_info(sb)["launches"],
+                               "slowdown_vs_persistent": (ms_ps[0] / reps) / (t_step * 1e3)}
+        ctx.set_tc_schedule(False)
+        ms_d = ctx.sigma_timed(sb, x, y, reps)
+        info_d = ctx.superblock_info(sb)
+        sched["default_knobs"] = {"ms_per_sigma": ms_d[0] / reps,
+                                  "knobs": {k: info_d[k] for k in ("tc_item_cost", "tc_split", "tc_group")}}
+        if not a.no_autotune:
+            ctx.set_autotune(True)
+            ctx.sigma_timed(sb, x, y, 1)  # cached knobs back on the plan
+            tuned, cached, secs = ctx.autotune_stats()
+            sched["tuning"] = {"histograms_tuned": tuned, "seconds": secs}
+        line["schedules"] = sched
     if split:
         # plain FP64 path on the same superblock and input
         ctx.set_precision("fp64")

@@ -63,6 +63,9 @@ _SIGS = {
     "bgpu_set_refine_window": (_I, [_P, ctypes.c_double]),
     "bgpu_set_guess": (_I, [_P, _I]),
     "bgpu_set_davidson_graph": (_I, [_P, _I]),
+    "bgpu_set_tc_schedule": (_I, [_P, _I]),
+    "bgpu_set_autotune": (_I, [_P, _I, _CP]),
+    "bgpu_autotune_stats": (_I, [_P, _I64P, _I64P, _DP]),
     "bgpu_davidson_graph_launches": (_I, [_P, _I64P]),
     "bgpu_tc_wait_selftest": (_I, [_P, ctypes.c_double, _IP, _IP, _DP]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
@@ -265,7 +268,8 @@ class Context:
 
     INFO_KEYS = ("flops", "bytes", "tc_mma_flops", "tc_phase1_tasks", "tc_phase2_tasks", "tc_phase2_items",
                  "tc_phase2_stage1_items", "tc_split_tiles", "tc_pool_L", "tc_pool_R", "tc_pool_psi",
-                 "tc_pool_S", "fp64_stage1_units", "fp64_items")
+                 "tc_pool_S", "fp64_stage1_units", "fp64_items", "tc_item_cost", "tc_split", "tc_group",
+                 "tc_per_sector", "tc_tuned", "launches")
 
     def tc_wait_selftest(self, limit_ms=20.0):
         """Bounded mbarrier wait on a barrier nothing arrives at: returns
@@ -285,6 +289,23 @@ class Context:
         """Davidson iterations as launches of a captured CUDA graph (True) or
         as the same launches issued one by one (False)."""
         self._check(self.lib.bgpu_set_davidson_graph(self.h, int(bool(on))))
+
+    def set_tc_schedule(self, per_sector=False):
+        """Tensor-core sigma as two persistent launches (False) or as the
+        per-sector baseline, one launch per sector (True)."""
+        self._check(self.lib.bgpu_set_tc_schedule(self.h, int(bool(per_sector))))
+
+    def set_autotune(self, on=True, cache_path=None):
+        """Autotuner of the persistent tensor-core schedule, keyed on the
+        sector-size histogram; cache_path: text file of tuned knobs."""
+        self._check(self.lib.bgpu_set_autotune(self.h, int(bool(on)),
+                                               cache_path.encode() if cache_path else None))
+
+    def autotune_stats(self):
+        """(histograms tuned, histograms cached, seconds spent tuning)."""
+        a, b, c = _I64(), _I64(), ctypes.c_double()
+        self._check(self.lib.bgpu_autotune_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
 
     def davidson_graph_launches(self):
         """Graph launches of the last Davidson solve."""

@@ -116,6 +116,31 @@ int bgpu_set_davidson_graph(bgpu_ctx* ctx, int on) {
   });
 }
 
+int bgpu_set_tc_schedule(bgpu_ctx* ctx, int mode) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    need(mode == 0 || mode == 1, "schedule mode must be 0 (persistent) or 1 (per sector)");
+    ctx->eng->tc_schedule_mode = mode;
+  });
+}
+
+int bgpu_set_autotune(bgpu_ctx* ctx, int on, const char* cache_path) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    ctx->eng->tc_autotune = on != 0;
+    if (cache_path) ctx->eng->load_tune_cache(cache_path);
+  });
+}
+
+int bgpu_autotune_stats(bgpu_ctx* ctx, int64_t* keys_tuned, int64_t* keys_cached, double* seconds) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    if (keys_tuned) *keys_tuned = ctx->eng->tune_runs;
+    if (keys_cached) *keys_cached = (int64_t)ctx->eng->tune_cache.size();
+    if (seconds) *seconds = ctx->eng->tune_seconds;
+  });
+}
+
 int bgpu_davidson_graph_launches(bgpu_ctx* ctx, int64_t* launches) {
   return guarded(ctx, [&] {
     need(ctx->eng != nullptr && launches, "bad arguments");
@@ -352,7 +377,7 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
     auto& r = *it->second;
     if (!r.plan.tc) ctx->eng->plan_tc(r.sb, r.plan);
     const SigmaPlan& p = r.plan;
-    const double v[14] = {p.flops,
+    const double v[20] = {p.flops,
                           p.bytes,
                           p.tc_mma_flops,
                           (double)p.tc_stats[0],
@@ -365,8 +390,14 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
                           (double)p.tc_pool_elems[dev::kTcPoolPsi],
                           (double)p.tc_pool_elems[dev::kTcPoolS],
                           (double)p.nstage1_units,
-                          (double)p.nitems};
-    for (int i = 0; i < n; ++i) info[i] = i < 14 ? v[i] : 0.0;
+                          (double)p.nitems,
+                          p.tc_knobs.item_cost,
+                          p.tc_knobs.split,
+                          (double)p.tc_knobs.group,
+                          (double)p.tc_knobs.per_sector,
+                          p.tc_tuned ? 1.0 : 0.0,
+                          (double)ctx->eng->sigma_launches(p)};
+    for (int i = 0; i < n; ++i) info[i] = i < 20 ? v[i] : 0.0;
   });
 }
 

@@ -57,6 +57,10 @@ GpuEngine::GpuEngine(int device) : device_(device) {
   cuda_check(cudaMallocHost((void**)&dav_host_, sizeof(dev::DavCtl)), "alloc davidson header");
   const char* g = std::getenv("BGPU_DAVIDSON_GRAPH");
   dav_graph = !(g && g[0] == '0');
+  const char* at = std::getenv("BGPU_AUTOTUNE");
+  tc_autotune = at && at[0] == '1';
+  const char* tcp = std::getenv("BGPU_TUNE_CACHE");
+  if (tcp && *tcp) load_tune_cache(tcp);
 }
 
 GpuEngine::~GpuEngine() {
@@ -717,6 +721,11 @@ void GpuEngine::free_tc(SigmaPlan& p) {
   p.tc_slots.release(stream_);
   if (p.tc_partials) cudaFreeAsync(p.tc_partials, stream_);
   p.tc_partials = nullptr;
+  p.tc_partial_cap = 0;
+  p.tc_host.reset();
+  p.tc_l1.clear();
+  p.tc_l2.clear();
+  p.tc_tuned = false;
   p.tc = false;
 }
 
@@ -922,6 +931,17 @@ void GpuEngine::sigma_split(const Superblock& sb, SigmaPlan& p, int ns, const do
 // (hi, lo) operands; every sigma sector tile then sums its items
 // alpha * X * Y^T (X = S, psi or an L operator; Y = an R operator or psi^T)
 // in phase 2, in the same order as the FP64 plan.
+// Host side of a tensor-core plan: phase-1 items and tasks (with the psi
+// sector each task reads), and the phase-2 items of every sigma sector.
+struct TcHostPlan {
+  std::vector<dev::TcItem> i1;
+  std::vector<dev::TcTask> t1;
+  std::vector<int> sec1;
+  std::vector<int64_t> bundle1;
+  std::vector<std::vector<dev::TcItem>> per_sector;
+  double mma1 = 0.0;  // tensor-core flops of phase 1
+};
+
 void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   PlanTimer timer_(plan_seconds);
   PlanLaps laps{"tc"};
@@ -994,7 +1014,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   }
   std::vector<TcItem> i1;
   std::vector<TcTask> t1;
-  std::vector<int64_t> bundle1, bundle2;  // tasks reading the same A row tile
+  std::vector<int> sec1;          // psi sector read by each phase-1 task
+  std::vector<int64_t> bundle1;  // tasks reading the same A row tile
   std::vector<std::vector<TcItem>> per_sector(nsec);
   std::vector<std::vector<int>> per_sector_s(nsec);  // phase-1 item of a stage-1 operand, else -1
   double mma = 0.0;
@@ -1069,6 +1090,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
             t.out_off = cur_s;
             t.out_kp = skp;
             t1.push_back(t);
+            sec1.push_back(c.cs);
             bundle1.push_back((cur_s << 8) | tm);
             mma += 3.0 * 2.0 * 128 * tc_round16(std::min(kTcRowsB, t.b_rows - kTcRowsB * tn)) * a.kp;
           }
@@ -1114,18 +1136,81 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       std::stable_partition(v.begin(), v.end(), [](const TcItem& it) { return it.alpha == 1.0f; });
   }
   laps.lap("alpha folding");
-  // phase 2: sector tiles; a tile whose items cost more than a block's fair
-  // share is split into several tasks summed by the reduce kernel, every
-  // other tile is one task writing its FP64 result directly
+  // the item lists stay on the host, so that the device work lists can be
+  // rebuilt for other schedule knobs (autotuner, per-sector baseline)
+  auto host = std::make_shared<TcHostPlan>();
+  host->i1 = std::move(i1);
+  host->t1 = std::move(t1);
+  host->sec1 = std::move(sec1);
+  host->bundle1 = std::move(bundle1);
+  host->per_sector = std::move(per_sector);
+  host->mma1 = mma;
+  plan.tc_host = host;
+  for (int i = 0; i < kTcPools; ++i) {
+    plan.tc_pool_elems[i] = pool_n[i];
+    const size_t bytes = (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16);
+    cuda_check(cudaMallocAsync((void**)&plan.tc_pool[i], bytes, stream_), "tc pool");
+  }
+  plan.tc_psi_pack.upload(psi_packs, stream_);
+  // operator blocks are packed once per plan
+  DevArray<TcPack> dops;
+  dops.upload(ops_packs, stream_);
+  TcBufs b{};
+  b.src[0] = arena(L);
+  b.src[1] = arena(R);
+  for (int i = 0; i < kTcPools; ++i) {
+    b.pool[i] = plan.tc_pool[i];
+  }
+  b.fp16 = precision == Precision::FP16X2_TC ? 1 : 0;
+  plan.tc_fp16 = b.fp16 != 0;
+  cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
+  dops.release(stream_);
+  laps.lap("pools + pack operators");
+  TcKnobs kn = tc_default_knobs();
+  kn.per_sector = tc_schedule_mode == 1 ? 1 : 0;
+  plan.tc_tuned = false;
+  schedule_tc(sb, plan, kn);
+  plan.tc = true;
+  sync();
+  laps.lap("schedule");
+}
+
+TcKnobs GpuEngine::tc_default_knobs() const {
+  // defaults measured near-optimal on the 24-orbital M=500 superblock;
+  // BGPU_TC_ITEM_COST, BGPU_TC_SPLIT and BGPU_TC_GROUP override them
+  TcKnobs k;
+  k.item_cost = env_double("BGPU_TC_ITEM_COST", 400.0);
+  k.split = env_double("BGPU_TC_SPLIT", 3.0);
+  k.group = (int)env_double("BGPU_TC_GROUP", 16.0);
+  return k;
+}
+
+// Phase-2 tasks, cost model, block assignment and flattened work records of
+// a tensor-core plan for one set of knobs.  Persistent schedule: two blocks
+// per SM, longest-processing-time assignment; tiles costing more than
+// total / (2 split SMs) are cut into pieces summed by the reduce kernel.
+// Per-sector schedule (baseline): no cut tiles, one block per task, one
+// launch per psi sector (phase 1) and per sigma sector (phase 2).
+void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs& kn) {
+  PlanTimer timer_(plan_seconds);
+  PlanLaps laps{"tc schedule"};
+  using namespace dev;
+  const TcHostPlan& H = *plan.tc_host;
+  const auto& i1 = H.i1;
+  const auto& t1 = H.t1;
+  const auto& per_sector = H.per_sector;
+  const int nsec = (int)sb.sectors.size();
   const int nsm = sm_count();
-  // cost model of the LPT assignment (tuning: BGPU_TC_ITEM_COST = fixed cost of
-  // an item, BGPU_TC_SPLIT = phase-2 pieces per block)
-  static const double kItemFixed = env_double("BGPU_TC_ITEM_COST", 400.0);
-  static const double kSplit = env_double("BGPU_TC_SPLIT", 3.0);
-  auto item_cost = [](const TcItem& it, int hb) { return kItemFixed + (double)it.kp * tc_round16(hb) / 8.0; };
+  const bool seq = kn.per_sector != 0;
+  const double item_fixed = kn.item_cost;
+  auto item_cost = [&](const TcItem& it, int hb) { return item_fixed + (double)it.kp * tc_round16(hb) / 8.0; };
+  auto fail = []() { throw std::runtime_error("tensor-core plan: operand shape does not match its sector"); };
+  double mma = H.mma1;
   std::vector<TcItem> i2;
   std::vector<TcTask> t2;
   std::vector<double> c2;
+  std::vector<int> sec2;
+  std::vector<int64_t> bundle2;
   std::vector<TcTile> tiles;
   std::vector<int64_t> slots;
   int64_t partial_n = 0;
@@ -1137,7 +1222,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
     }
   }
-  const double chunk = std::max(total / (2.0 * kSplit * nsm), 20000.0);
+  const double chunk = seq ? 1e300 : std::max(total / (2.0 * kn.split * nsm), 20000.0);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     const int ib = (int)i2.size();
@@ -1165,6 +1250,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           t.out_kp = S.cols;
           t2.push_back(t);
           c2.push_back(tile_cost);
+          sec2.push_back(s);
           bundle2.push_back(((int64_t)s << 8) | tm);
           continue;
         }
@@ -1191,6 +1277,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           partial_n += (int64_t)ha * hb;
           t2.push_back(u);
           c2.push_back(acc);
+          sec2.push_back(s);
           bundle2.push_back(-(int64_t)t2.size());  // pieces of a split tile spread over blocks
           x0 = x1;
         }
@@ -1203,7 +1290,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     c1.push_back(item_cost(i1[t.ibeg], std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn)) + 200.0);
   laps.lap("phase-2 tasks");
   // tiles inside their operands (item shapes were checked against their
-  // sectors above)
+  // sectors when the items were made)
   for (const TcTask& t : t1)
     if (kTcRowsA * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows || kTcRowsB * t.tn >= t.out_kp) fail();
   for (const TcTask& t : t2)
@@ -1211,32 +1298,39 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         (t.direct && (t.valid_rows > std::min(kTcRowsA, t.a_rows - kTcRowsA * t.tm) ||
                       t.valid_cols > std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn))))
       fail();
-  laps.lap("checks");
   std::vector<int> o1, o2;
-  std::vector<int2> r1, r2;
-  // two persistent blocks per SM (each kernel block runs its own pipeline)
-  schedule_lpt(c1, bundle1, 2 * nsm, o1, r1);
-  schedule_lpt(c2, bundle2, 2 * nsm, o2, r2);
-  laps.lap("schedule");
-  // buffers
-  for (int i = 0; i < kTcPools; ++i) {
-    plan.tc_pool_elems[i] = pool_n[i];
-    const size_t bytes = (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16);
-    cuda_check(cudaMallocAsync((void**)&plan.tc_pool[i], bytes, stream_), "tc pool");
+  std::vector<int2> r1, r2, l1, l2;
+  if (!seq) {
+    // two persistent blocks per SM (each kernel block runs its own pipeline)
+    schedule_lpt(c1, H.bundle1, 2 * nsm, o1, r1);
+    schedule_lpt(c2, bundle2, 2 * nsm, o2, r2);
+  } else {
+    // one block per task, tasks grouped by sector, one launch per group
+    auto by_sector = [](const std::vector<int>& sec, std::vector<int>& o, std::vector<int2>& r,
+                        std::vector<int2>& l) {
+      o.resize(sec.size());
+      for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
+      std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return sec[a] < sec[b]; });
+      for (size_t i = 0; i < o.size(); ++i) {
+        r.push_back(make_int2((int)i, (int)i + 1));
+        if (i == 0 || sec[o[i]] != sec[o[i - 1]]) l.push_back(make_int2((int)i, 0));
+        ++l.back().y;
+      }
+    };
+    by_sector(H.sec1, o1, r1, l1);
+    by_sector(sec2, o2, r2, l2);
   }
-  cuda_check(cudaMallocAsync((void**)&plan.tc_partials, (size_t)std::max<int64_t>(partial_n, 1) * sizeof(float2),
-                             stream_),
-             "tc partials");
-  plan.tc_psi_pack.upload(psi_packs, stream_);
+  laps.lap("assignment");
+  if (partial_n > plan.tc_partial_cap || !plan.tc_partials) {
+    if (plan.tc_partials) cudaFreeAsync(plan.tc_partials, stream_);
+    plan.tc_partial_cap = std::max<int64_t>(partial_n, 1);
+    cuda_check(cudaMallocAsync((void**)&plan.tc_partials, (size_t)plan.tc_partial_cap * sizeof(float2), stream_),
+               "tc partials");
+  }
   // flatten every block's tasks into its stream of work records; within a
   // task, runs of items with alpha = 1 form accumulation groups of at most
-  // kGroupItems items and kGroupK summed K (f32 accumulation length)
-  // BGPU_TC_GROUP overrides the item limit (tuning)
-  static const int kGroupItems = [] {
-    const char* e = std::getenv("BGPU_TC_GROUP");
-    const int v = e ? std::atoi(e) : 0;
-    return v > 0 ? v : 16;
-  }();
+  // kn.group items and kGroupK summed K (f32 accumulation length)
+  const int group_items = std::max(1, kn.group);
   constexpr int kGroupK = 1024;
   auto flatten = [&](int phase, const std::vector<TcTask>& tasks, const std::vector<TcItem>& items,
                      const std::vector<int>& order, const std::vector<int2>& ranges, std::vector<TcWork>& w,
@@ -1285,7 +1379,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           if (gn == 0) f |= kTcGStart;
           ++gn;
           gk += it.kp;
-          const bool next_joins = foldable && i + 1 < T.iend && items[i + 1].alpha == 1.0f && gn < kGroupItems &&
+          const bool next_joins = foldable && i + 1 < T.iend && items[i + 1].alpha == 1.0f && gn < group_items &&
                                   gk + items[i + 1].kp <= kGroupK;
           if (!next_joins) {
             f |= kTcGEnd;
@@ -1302,6 +1396,10 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   std::vector<int2> wr1, wr2;
   flatten(1, t1, i1, o1, r1, w1, wr1);
   flatten(2, t2, i2, o2, r2, w2, wr2);
+  for (auto* d : {&plan.tc_w1, &plan.tc_w2}) d->release(stream_);
+  for (auto* d : {&plan.tc_r1, &plan.tc_r2}) d->release(stream_);
+  plan.tc_tiles.release(stream_);
+  plan.tc_slots.release(stream_);
   plan.tc_w1.upload(w1, stream_);
   plan.tc_w2.upload(w2, stream_);
   plan.tc_r1.upload(wr1, stream_);
@@ -1309,6 +1407,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   plan.tc_tiles.upload(tiles, stream_);
   plan.tc_slots.upload(slots, stream_);
   plan.tc_mma_flops = mma;
+  plan.tc_l1 = std::move(l1);
+  plan.tc_l2 = std::move(l2);
+  plan.tc_knobs = kn;
   {
     int64_t full = 0;
     for (const TcItem& it : i2) full += it.a_pool == kTcPoolS ? 1 : 0;
@@ -1316,28 +1417,124 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     for (int i = 0; i < 5; ++i) plan.tc_stats[i] = st[i];
   }
   laps.lap("flatten + upload");
-  // operator blocks are packed once per plan
-  DevArray<TcPack> dops;
-  dops.upload(ops_packs, stream_);
-  TcBufs b{};
-  b.src[0] = arena(L);
-  b.src[1] = arena(R);
-  for (int i = 0; i < kTcPools; ++i) {
-    b.pool[i] = plan.tc_pool[i];
+}
+
+// Autotuner key: slice format, octave of the plan's tensor-core work and the
+// histogram of psi-sector shapes (octaves of rows and columns, octave of the
+// count per bin), so that superblocks with the same sector structure share
+// their tuned knobs.
+std::string GpuEngine::tc_tune_key(const Superblock& sb, const SigmaPlan& p) const {
+  auto oct = [](double x) {
+    int b = 0;
+    while (x >= 2.0 && b < 80) {
+      x *= 0.5;
+      ++b;
+    }
+    return b;
+  };
+  std::map<std::pair<int, int>, int> hist;
+  for (const auto& S : sb.sectors) ++hist[{oct(S.rows), oct(S.cols)}];
+  std::string k = std::string(p.tc_fp16 ? "fp16" : "bf16") + "/w" + std::to_string(oct(p.tc_mma_flops));
+  for (const auto& h : hist)
+    k += "/" + std::to_string(h.first.first) + "x" + std::to_string(h.first.second) + ":" + std::to_string(oct(h.second));
+  return k;
+}
+
+// Coordinate search over the schedule knobs (LPT item cost, phase-2 split,
+// accumulation group), each candidate timed by CUDA events over three
+// products on the plan's own operators; a candidate replaces the best one
+// when it is at least 2 % faster.  Keys seen before reuse their knobs.
+void GpuEngine::autotune_tc(const Superblock& sb, SigmaPlan& p) {
+  p.tc_tuned = true;  // also stops sigma_tc from re-entering
+  const std::string key = tc_tune_key(sb, p);
+  auto it = tune_cache.find(key);
+  if (it != tune_cache.end()) {
+    TcKnobs k = it->second;
+    k.per_sector = 0;
+    if (!(k == p.tc_knobs)) schedule_tc(sb, p, k);
+    return;
   }
-  b.fp16 = precision == Precision::FP16X2_TC ? 1 : 0;
-  plan.tc_fp16 = b.fp16 != 0;
-  cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
-  dops.release(stream_);
-  plan.tc = true;
+  const auto t0 = std::chrono::steady_clock::now();
+  const double f0 = sigma_flops;
+  const long c0 = sigma_calls;
+  double* x = alloc(p.n);
+  double* y = alloc(p.n);
+  cuda_check(dev::launch_fill(x, 1.0 / std::sqrt((double)std::max<int64_t>(p.n, 1)), p.n, stream_), "fill");
+  cudaEvent_t e[2];
+  for (auto& v : e) cuda_check(cudaEventCreate(&v), "event");
+  auto measure = [&]() {
+    sigma_tc(sb, p, x, y);
+    cuda_check(cudaEventRecord(e[0], stream_), "record");
+    for (int r = 0; r < 3; ++r) sigma_tc(sb, p, x, y);
+    cuda_check(cudaEventRecord(e[1], stream_), "record");
+    sync();
+    float ms = 0.f;
+    cuda_check(cudaEventElapsedTime(&ms, e[0], e[1]), "elapsed");
+    return (double)ms;
+  };
+  TcKnobs best = p.tc_knobs;
+  best.per_sector = 0;
+  if (!(best == p.tc_knobs)) schedule_tc(sb, p, best);
+  double tbest = measure();
+  const double costs[] = {150.0, 400.0, 1000.0};
+  const double splits[] = {1.5, 3.0, 6.0};
+  const int groups[] = {8, 16, 32};
+  for (int axis = 0; axis < 3; ++axis)
+    for (int v = 0; v < 3; ++v) {
+      TcKnobs c = best;
+      if (axis == 0) c.item_cost = costs[v];
+      if (axis == 1) c.split = splits[v];
+      if (axis == 2) c.group = groups[v];
+      if (c == best) continue;
+      schedule_tc(sb, p, c);
+      const double t = measure();
+      if (t < 0.98 * tbest) {
+        best = c;
+        tbest = t;
+      }
+    }
+  if (!(best == p.tc_knobs)) schedule_tc(sb, p, best);
+  for (auto& v : e) cudaEventDestroy(v);
+  free(x);
+  free(y);
   sync();
-  laps.lap("pack operators");
+  sigma_flops = f0;
+  sigma_calls = c0;
+  tune_cache[key] = best;
+  if (!tune_cache_path.empty()) {
+    if (FILE* f = std::fopen(tune_cache_path.c_str(), "a")) {
+      std::fprintf(f, "%s %.17g %.17g %d\n", key.c_str(), best.item_cost, best.split, best.group);
+      std::fclose(f);
+    }
+  }
+  ++tune_runs;
+  tune_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void GpuEngine::load_tune_cache(const std::string& path) {
+  tune_cache_path = path;
+  if (path.empty()) return;
+  FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return;
+  char key[4096];
+  TcKnobs k;
+  while (std::fscanf(f, "%4095s %lf %lf %d", key, &k.item_cost, &k.split, &k.group) == 4) {
+    if (k.item_cost > 0 && k.split > 0 && k.group > 0) tune_cache[key] = k;
+  }
+  std::fclose(f);
 }
 
 void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, double* out, cudaEvent_t* marks) {
   const bool fp16 = precision == Precision::FP16X2_TC;
   if (p.tc && p.tc_fp16 != fp16) free_tc(p);  // operators packed in the other format
   if (!p.tc) plan_tc(sb, p);
+  if (p.tc_knobs.per_sector != (tc_schedule_mode == 1 ? 1 : 0)) {
+    TcKnobs k = tc_default_knobs();
+    k.per_sector = tc_schedule_mode == 1 ? 1 : 0;
+    schedule_tc(sb, p, k);
+    p.tc_tuned = false;
+  }
+  if (tc_autotune && !p.tc_knobs.per_sector && !p.tc_tuned) autotune_tc(sb, p);
   dev::TcBufs b{};
   b.src[0] = arena(*sb.L);
   b.src[1] = arena(*sb.R);
@@ -1351,10 +1548,21 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   constexpr uint64_t kWaitLimitNs = 1000000000ull;
   cuda_check(dev::launch_tc_pack(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tc pack psi");
   if (marks) cuda_check(cudaEventRecord(marks[0], stream_), "record");
-  cuda_check(dev::launch_tc_sigma(1, b, p.tc_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
-             "tc phase 1");
-  cuda_check(dev::launch_tc_sigma(2, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
-             "tc phase 2");
+  if (p.tc_knobs.per_sector) {
+    // baseline: one launch per psi sector (phase 1) and per sigma sector
+    // (phase 2), one block per task
+    for (const int2& g : p.tc_l1)
+      cuda_check(dev::launch_tc_sigma(1, b, p.tc_w1.d, p.tc_r1.d + g.x, g.y, out, kWaitLimitNs, stream_),
+                 "tc phase 1");
+    for (const int2& g : p.tc_l2)
+      cuda_check(dev::launch_tc_sigma(2, b, p.tc_w2.d, p.tc_r2.d + g.x, g.y, out, kWaitLimitNs, stream_),
+                 "tc phase 2");
+  } else {
+    cuda_check(dev::launch_tc_sigma(1, b, p.tc_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
+               "tc phase 1");
+    cuda_check(dev::launch_tc_sigma(2, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
+               "tc phase 2");
+  }
   if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");
   cuda_check(dev::launch_tc_reduce(b, p.tc_tiles.d, p.tc_slots.d, (int)p.tc_tiles.n, out, stream_), "tc reduce");
   if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
@@ -1371,7 +1579,10 @@ void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi,
 }
 
 int GpuEngine::sigma_launches(const SigmaPlan& p) const {
-  if (precision_tc(precision)) return 4 + (p.ecore != 0.0 ? 1 : 0);  // pack psi, phase 1, phase 2, reduce
+  if (precision_tc(precision)) {  // pack psi, phase 1, phase 2, reduce of split tiles
+    const int phases = (p.tc && p.tc_knobs.per_sector) ? (int)(p.tc_l1.size() + p.tc_l2.size()) : 2;
+    return 1 + phases + (p.tc && p.tc_tiles.n == 0 ? 0 : 1) + (p.ecore != 0.0 ? 1 : 0);
+  }
   if (precision_slices(precision)) return 3 + (p.ecore != 0.0 ? 1 : 0);  // slice psi, fused, reduce (+ecore)
   return (p.t1.n ? 1 : 0) + (p.t2.n ? 1 : 0) + (p.ru.n ? 1 : 0) + (p.ecore != 0.0 ? 1 : 0);
 }

@@ -46,6 +46,19 @@ struct DevArray {
   void release(cudaStream_t s);
 };
 
+// Knobs of the tensor-core work-list schedule (the tile shapes follow the
+// sectors: 128-row A tiles and up to 64-column B tiles, cut to each sector).
+struct TcKnobs {
+  double item_cost = 400.0;  // LPT cost of an item on top of its K x N work
+  double split = 3.0;        // phase-2 pieces per persistent block (tile splitting)
+  int group = 16;            // items per tensor-core accumulation group
+  int per_sector = 0;        // 1: one launch per sector, one block per task (baseline)
+  bool operator==(const TcKnobs& o) const {
+    return item_cost == o.item_cost && split == o.split && group == o.group && per_sector == o.per_sector;
+  }
+};
+struct TcHostPlan;  // item lists of a tensor-core plan, kept for rescheduling
+
 // Compiled sigma = H psi work lists of one superblock.
 struct SigmaPlan {
   DevArray<dev::GemmUnit> u1, u2;
@@ -87,6 +100,11 @@ struct SigmaPlan {
   // plan statistics: phase-1 tasks, phase-2 tasks, phase-2 items, phase-2
   // items reading a stage-1 product, split tiles
   int64_t tc_stats[5] = {};
+  std::shared_ptr<TcHostPlan> tc_host;
+  TcKnobs tc_knobs;                // knobs of the current schedule
+  bool tc_tuned = false;           // knobs chosen by the autotuner
+  std::vector<int2> tc_l1, tc_l2;  // per-sector launches: (first block range, blocks)
+  int64_t tc_partial_cap = 0;      // float2 capacity of tc_partials
 };
 
 class GpuEngine : public Engine {
@@ -126,6 +144,22 @@ class GpuEngine : public Engine {
   void plan_tc(const Superblock& sb, SigmaPlan& plan);
   void sigma_tc(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d,
                 cudaEvent_t* marks = nullptr);
+  // (re)builds the device work lists of a tensor-core plan for the knobs
+  void schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs& knobs);
+  // chooses the knobs of a tensor-core plan by timing candidate schedules;
+  // the choice is cached under the superblock's sector-size histogram
+  void autotune_tc(const Superblock& sb, SigmaPlan& plan);
+  std::string tc_tune_key(const Superblock& sb, const SigmaPlan& plan) const;
+  TcKnobs tc_default_knobs() const;
+  // tensor-core schedule of new plans: 0 persistent blocks (LPT), 1 one
+  // launch per sector (baseline); autotune: tune the knobs of persistent plans
+  int tc_schedule_mode = 0;
+  bool tc_autotune = false;
+  std::map<std::string, TcKnobs> tune_cache;
+  std::string tune_cache_path;  // file the cache is read from and appended to
+  void load_tune_cache(const std::string& path);
+  double tune_seconds = 0.0;    // time spent tuning
+  long tune_runs = 0;           // keys tuned
   // product at the engine's current precision
   void sigma_any(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d);
   void hdiag(const Superblock& sb, const SigmaPlan& plan, double* diag_d);

@@ -101,6 +101,24 @@ int bgpu_set_guess(bgpu_ctx* ctx, int transform);
 int bgpu_set_davidson_graph(bgpu_ctx* ctx, int on);
 /* Graph launches of the last Davidson solve (0 when it ran without capture). */
 int bgpu_davidson_graph_launches(bgpu_ctx* ctx, int64_t* launches);
+/* Work-list schedule of the tensor-core sigma (no reference counterpart; the
+ * reference calls one DGEMM per sector pair, operatorfunctions.C:515,530):
+ * mode 0 (default) runs every sigma as two persistent launches (two blocks
+ * per SM, longest-processing-time assignment of the sector tiles); mode 1 is
+ * the per-sector baseline: one launch per psi sector (stage-1 products) and
+ * per sigma sector (stage-2 tiles), one block per tile.  Applies to the next
+ * product of every superblock. */
+int bgpu_set_tc_schedule(bgpu_ctx* ctx, int mode);
+/* Autotuner of the persistent tensor-core schedule (no reference
+ * counterpart): on = 1 times candidate knobs (cost model of the block
+ * assignment, splitting of heavy tiles, accumulation group length) on the
+ * first product of every superblock whose sector-size histogram was not seen
+ * before and keeps the fastest; superblocks with a known histogram reuse its
+ * knobs.  cache_path (may be NULL) is a text file the tuned knobs are read
+ * from and appended to. */
+int bgpu_set_autotune(bgpu_ctx* ctx, int on, const char* cache_path);
+/* Histograms tuned by this context, histograms in the cache, seconds spent tuning. */
+int bgpu_autotune_stats(bgpu_ctx* ctx, int64_t* keys_tuned, int64_t* keys_cached, double* seconds);
 
 /*
  * Declare a block: its state space and operator catalogue.
@@ -153,8 +171,10 @@ int bgpu_tc_wait_selftest(bgpu_ctx* ctx, double limit_ms, int* gave_up, int* sta
  *   tcgen05 path (3 bf16 products, padded tiles), phase-1 tasks, phase-2
  *   tasks, phase-2 items, phase-2 items reading a stage-1 product, split
  *   tiles, packed elements of the L-operator / R-operator / psi / stage-1
- *   pools, FP64 stage-1 units, FP64 items.  Builds the tensor-core plan if
- *   needed. */
+ *   pools, FP64 stage-1 units, FP64 items, the schedule knobs (item cost,
+ *   split, group, per-sector flag, 1 when chosen by the autotuner) and the
+ *   launches of one sigma at the current precision.  Builds the tensor-core
+ *   plan if needed. */
 int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n);
 /* Kernel launches of one sigma product. */
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);
