@@ -77,6 +77,8 @@ GpuEngine::~GpuEngine() {
   if (guess_) cudaFreeAsync(guess_, stream_);
   if (solver_work_) cudaFreeAsync(solver_work_, stream_);
   if (solver_info_) cudaFreeAsync(solver_info_, stream_);
+  for (auto* q : pool_cache_)
+    if (q) cudaFreeAsync(q, stream_);
   cudaStreamSynchronize(stream_);
   if (solver_) cusolverDnDestroy((cusolverDnHandle_t)solver_);
   cudaEventDestroy(ev0_);
@@ -366,6 +368,8 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
     int64_t key;
     dev::CopyUnit u;
     std::vector<dev::CopyItem> items;
+    int64_t block_off;  // arena offset of the operator block
+    int r0, c0;         // rectangle origin inside the block
   };
   std::vector<std::vector<Rect>> per(recipes.size());
   parallel_for((int)recipes.size(), [&](int ri) {
@@ -417,6 +421,9 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
                 r.u.ldc = tb.cols;
                 r.u.m = pr.size;
                 r.u.n = pc.size;
+                r.block_off = te.base + tb.offset;
+                r.r0 = pr.offset;
+                r.c0 = pc.offset;
                 where.emplace(key, (int)rects.size());
                 rects.push_back(std::move(r));
                 rects.back().items.push_back(it);
@@ -429,6 +436,8 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
   });
   std::vector<dev::CopyUnit> units;
   std::vector<dev::CopyItem> items;
+  DevBlock& dt = blocks_.at(big.handle);
+  dt.nz.clear();
   for (auto& rv : per)
     for (auto& r : rv) {
       dev::CopyUnit u = r.u;
@@ -436,8 +445,8 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
       items.insert(items.end(), r.items.begin(), r.items.end());
       u.iend = (int)items.size();
       units.push_back(u);
+      dt.nz[r.block_off].push_back({r.r0, r.c0, r.u.m, r.u.n});
     }
-  DevBlock& dt = blocks_.at(big.handle);
   cuda_check(cudaMemsetAsync(dt.d, 0, (size_t)std::max<int64_t>(dt.n, 1) * sizeof(double), stream_), "memset");
   DevArray<dev::CopyUnit> du;
   DevArray<dev::CopyItem> di;
@@ -660,7 +669,7 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   plan.ru.upload(ru, stream_);
   plan.ri.upload(ri, stream_);
   plan.scratch_elems = scratch;
-  plan.scratch = alloc(scratch);
+  plan.scratch = nullptr;  // allocated by the first FP64 product
   plan.flops = flops;
   plan.bytes = bytes + 2.0 * 8.0 * sb.size;
   plan.n = sb.size;
@@ -700,17 +709,27 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
     u.iend = (int)di.size();
     du.push_back(u);
   }
+  std::vector<dev::GemmTask> dtask;
+  for (int u = 0; u < (int)du.size(); ++u) add_tasks(dtask, u, du[u].rows, du[u].cols);
   laps.lap("diagonal lists");
   plan.du.upload(du, stream_);
   plan.di.upload(di, stream_);
+  plan.dtask.upload(dtask, stream_);
   sync();
 }
 
 void GpuEngine::free_tc(SigmaPlan& p) {
   for (int i = 0; i < dev::kTcPools; ++i) {
-    if (p.tc_pool[i]) cudaFreeAsync(p.tc_pool[i], stream_);
+    if (p.tc_pool[i] && p.reuse_pools) {
+      if (pool_cache_[i]) cudaFreeAsync(pool_cache_[i], stream_);
+      pool_cache_[i] = p.tc_pool[i];
+      pool_cache_cap_[i] = p.tc_pool_cap[i];
+    } else if (p.tc_pool[i]) {
+      cudaFreeAsync(p.tc_pool[i], stream_);
+    }
     p.tc_pool[i] = nullptr;
     p.tc_pool_elems[i] = 0;
+    p.tc_pool_cap[i] = 0;
   }
   p.tc_psi_pack.release(stream_);
   p.tc_w1.release(stream_);
@@ -750,6 +769,7 @@ void GpuEngine::free_plan(SigmaPlan& p) {
   p.t2.release(stream_);
   p.du.release(stream_);
   p.di.release(stream_);
+  p.dtask.release(stream_);
   p.ru.release(stream_);
   p.ri.release(stream_);
   free(p.scratch);
@@ -757,6 +777,7 @@ void GpuEngine::free_plan(SigmaPlan& p) {
 }
 
 void GpuEngine::sigma(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out) {
+  if (!p.scratch) p.scratch = alloc(p.scratch_elems);
   dev::Bufs bufs{};
   bufs.p[0] = arena(*sb.L);
   bufs.p[1] = arena(*sb.R);
@@ -1149,7 +1170,22 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   for (int i = 0; i < kTcPools; ++i) {
     plan.tc_pool_elems[i] = pool_n[i];
     const size_t bytes = (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16);
-    cuda_check(cudaMallocAsync((void**)&plan.tc_pool[i], bytes, stream_), "tc pool");
+    if (plan.reuse_pools && pool_cache_[i] && pool_cache_cap_[i] >= bytes) {
+      plan.tc_pool[i] = pool_cache_[i];
+      plan.tc_pool_cap[i] = pool_cache_cap_[i];
+      pool_cache_[i] = nullptr;
+      pool_cache_cap_[i] = 0;
+      continue;
+    }
+    if (plan.reuse_pools && pool_cache_[i]) {
+      cudaFreeAsync(pool_cache_[i], stream_);
+      pool_cache_[i] = nullptr;
+      pool_cache_cap_[i] = 0;
+    }
+    // pools handed from solve to solve get 1/8 slack for the next superblock
+    const size_t cap = plan.reuse_pools ? bytes + bytes / 8 : bytes;
+    cuda_check(cudaMallocAsync((void**)&plan.tc_pool[i], cap, stream_), "tc pool");
+    plan.tc_pool_cap[i] = cap;
   }
   plan.tc_psi_pack.upload(psi_packs, stream_);
   // operator blocks are packed once per plan
@@ -1332,13 +1368,25 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   // kn.group items and kGroupK summed K (f32 accumulation length)
   const int group_items = std::max(1, kn.group);
   constexpr int kGroupK = 1024;
+  // blocks are flattened in parallel, each into its own slice of records
   auto flatten = [&](int phase, const std::vector<TcTask>& tasks, const std::vector<TcItem>& items,
                      const std::vector<int>& order, const std::vector<int2>& ranges, std::vector<TcWork>& w,
                      std::vector<int2>& wr) {
-    w.clear();
-    wr.clear();
-    for (const int2& rg : ranges) {
-      const int wb = (int)w.size();
+    wr.assign(ranges.size(), make_int2(0, 0));
+    int64_t nrec = 0;
+    for (size_t j = 0; j < ranges.size(); ++j) {
+      wr[j].x = (int)nrec;
+      for (int k = ranges[j].x; k < ranges[j].y; ++k) {
+        const TcTask& T = tasks[order[k]];
+        nrec += std::max(1, T.iend - T.ibeg);
+      }
+      wr[j].y = (int)nrec;
+    }
+    if (nrec > INT32_MAX) throw std::runtime_error("tensor-core plan: too many work records");
+    w.assign(nrec, TcWork{});
+    parallel_for((int)ranges.size(), [&](int j) {
+      const int2& rg = ranges[j];
+      int64_t pos = wr[j].x;
       for (int k = rg.x; k < rg.y; ++k) {
         const TcTask& T = tasks[order[k]];
         TcWork base{};
@@ -1361,7 +1409,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
         if (T.ibeg == T.iend) {
           TcWork x = base;
           x.flags = (uint8_t)(f0 | kTcFirst | kTcLast | kTcEmpty);
-          w.push_back(x);
+          w[pos++] = x;
           continue;
         }
         int gn = 0, gk = 0;  // items and K in the open group
@@ -1386,11 +1434,10 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
             gn = gk = 0;
           }
           x.flags = (uint8_t)f;
-          w.push_back(x);
+          w[pos++] = x;
         }
       }
-      wr.push_back(make_int2(wb, (int)w.size()));
-    }
+    });
   };
   std::vector<TcWork> w1, w2;
   std::vector<int2> wr1, wr2;
@@ -1589,6 +1636,7 @@ int GpuEngine::sigma_launches(const SigmaPlan& p) const {
 
 void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out, int reps,
                             float* ms) {
+  if (!precision_slices(precision) && !p.scratch) p.scratch = alloc(p.scratch_elems);
   dev::Bufs bufs{};
   bufs.p[0] = arena(*sb.L);
   bufs.p[1] = arena(*sb.R);
@@ -1651,7 +1699,7 @@ void GpuEngine::hdiag(const Superblock& sb, const SigmaPlan& p, double* d) {
   bufs.p[0] = arena(*sb.L);
   bufs.p[1] = arena(*sb.R);
   cuda_check(dev::launch_fill(d, sb.ecore, sb.size, stream_), "fill");
-  cuda_check(dev::launch_diag(bufs, d, p.du.d, p.di.d, (int)p.du.n, stream_), "hdiag");
+  cuda_check(dev::launch_diag_tiles(bufs, d, p.du.d, p.di.d, p.dtask.d, (int)p.dtask.n, stream_), "hdiag");
 }
 
 // ------------------------------------------------------------------ Davidson
@@ -1673,6 +1721,7 @@ void GpuEngine::hdiag(const Superblock& sb, const SigmaPlan& p, double* d) {
 // O(k n) instead of O(k^2 n) memory traffic per iteration.
 int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) {
   if (have_plan_) free_plan(plan_);
+  plan_.reuse_pools = true;
   plan_sigma(sb, plan_);
   have_plan_ = true;
   const int64_t n = sb.size;
@@ -1712,21 +1761,23 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   double* red = buf(dev::kDavMax);
   cuda_check(cudaMallocAsync((void**)&sc.ctl, sizeof(dev::DavCtl), stream_), "alloc");
   for (auto& x : sc.ev) cuda_check(cudaEventCreate(&x), "event");
+  PlanLaps laps{"davidson"};
+  laps.lap("plan");
   hdiag(sb, plan_, diag);
-  std::vector<double> hd(n);
-  cuda_check(cudaMemcpyAsync(hd.data(), diag, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h diag");
-  sync();
-  // basic guess (as the oracle): unit vectors on the lowest diagonal + small noise
-  std::vector<int64_t> order(n);
-  for (int64_t i = 0; i < n; ++i) order[i] = i;
-  std::partial_sort(order.begin(), order.begin() + nroots, order.end(),
-                    [&](int64_t a, int64_t b) { return hd[a] < hd[b]; });
-  Rng rng(p.seed);
   if (p.use_guess && guess_ && guess_n_ == n && nguess_ >= nroots) {
     // transformed previous wavefunctions (orthonormalised below)
     cuda_check(cudaMemcpyAsync(B, guess_, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
                "guess");
   } else {
+    // basic guess (as the oracle): unit vectors on the lowest diagonal + small noise
+    std::vector<double> hd(n);
+    cuda_check(cudaMemcpyAsync(hd.data(), diag, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h diag");
+    sync();
+    std::vector<int64_t> order(n);
+    for (int64_t i = 0; i < n; ++i) order[i] = i;
+    std::partial_sort(order.begin(), order.begin() + nroots, order.end(),
+                      [&](int64_t a, int64_t b) { return hd[a] < hd[b]; });
+    Rng rng(p.seed);
     std::vector<double> g((size_t)nroots * n);
     for (int rr = 0; rr < nroots; ++rr) {
       for (int64_t i = 0; i < n; ++i) g[(size_t)rr * n + i] = 1e-3 * (rng.uniform() - 0.5);
@@ -1741,6 +1792,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     cuda_check(cudaMemcpyAsync(out, red, nx * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
     sync();
   };
+  laps.lap("diag + guess");
   for (int i = 0; i < nroots; ++i) {
     double h;
     for (int j = 0; j < i; ++j) {
@@ -1760,6 +1812,10 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
       ++fp64_calls;
     }
   };
+  if (precision_tc(precision) && !plan_.tc) {
+    plan_tc(sb, plan_);
+    laps.lap("tensor-core plan");
+  }
   // first iteration: sigma of every start vector, whole subspace matrix
   // h_ij = b_i . sigma_j (j <= i, symmetrised as linear.C:268-272)
   for (int i = 0; i < nroots; ++i) {
@@ -1780,6 +1836,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   c0.mode = 2;
   cuda_check(cudaMemcpyAsync(sc.ctl, &c0, sizeof(c0), cudaMemcpyHostToDevice, stream_), "h2d ctl");
   sync();
+  laps.lap("first sigma + subspace");
   dev::DavBufs db{B, S, r, diag, y, work, sc.ctl, n, nroots, p.deflation_min, p.deflation_max, p.tol};
   // one iteration; with_sigma: the newest basis vector (left in r) has no sigma yet
   // (event records inside a capture become external event nodes; outside a
@@ -1848,6 +1905,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     if (h.done || iter >= p.max_iter) break;
     with_sigma = h.expand != 0;
   }
+  laps.lap("iterations");
   energies.assign(dav_host_->lam, dav_host_->lam + nroots);
   if (waves_) free(waves_);
   waves_ = alloc((int64_t)nroots * n);
@@ -1903,6 +1961,7 @@ bool GpuEngine::refine(const Superblock& sb, std::vector<double>& energies) {
 // is the recoupling coefficient of three spins (no fermion signs: the site
 // order does not change).  Stages are grouped FP64 GEMMs and one build-copy.
 bool GpuEngine::transform_guess(const GuessInput& g, const Superblock& sb) {
+  PlanLaps laps{"guess"};
   if (!waves_ || nwaves_ < 1 || !g.rotated || !g.expanded || !g.dot) return false;
   auto ri = block_rot_.find(g.rotated->handle);
   auto ei = block_rot_.find(g.expanded->handle);
@@ -2157,6 +2216,7 @@ bool GpuEngine::transform_guess(const GuessInput& g, const Superblock& sb) {
   guess_n_ = sb.size;
   nguess_ = ok ? nr : 0;
   sync();
+  laps.lap("transform");
   return ok;
 }
 
@@ -2233,6 +2293,7 @@ std::string GpuEngine::step_stats() {
 // ------------------------------------------------------------------ density
 
 void GpuEngine::density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) {
+  PlanLaps laps{"density"};
   const Block& B = left ? *sb.L : *sb.R;
   const int nq = B.si.size();
   std::vector<int64_t> off(nq);
@@ -2294,6 +2355,8 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   bufs.p[0] = waves_;
   bufs.p[1] = rho;
   cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "density");
+  if (laps.on) sync();
+  laps.lap("rho gemm");
   // eigen-decomposition of every sector (diagonalise_dm): sectors up to
   // kJacobiMax states in one batched Jacobi launch, larger ones with the
   // dense divide-and-conquer solver (eigenvectors column-major)
@@ -2363,6 +2426,12 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
         throw std::runtime_error("syevd launch failed");
     }
   }
+  if (laps.on) {
+    sync();
+    char what[64];
+    std::snprintf(what, sizeof(what), "eig (%zu dense, max n %d)", large.size(), maxn);
+    laps.lap(what);
+  }
   std::vector<double> hw(wt);
   std::vector<int> st(nq), info(large.size());
   cuda_check(cudaMemcpyAsync(hw.data(), w, wt * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
@@ -2386,6 +2455,58 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   dstat.release(stream_);
   free(rho);
   free(w);
+  sync();
+}
+
+// The dense divide-and-conquer solver loads its kernels on first use of
+// each size class, which took up to seconds inside the first sweep; one
+// solve per size class (64 .. 2048 states, capped at max_n) moves that to the
+// warm-up.
+void GpuEngine::prepare_density(int max_n) {
+  PlanLaps laps{"density"};
+  auto h = (cusolverDnHandle_t)solver_;
+  if (!h) {
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnCreate failed");
+    solver_ = h;
+  }
+  if (cusolverDnSetStream(h, stream_) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnSetStream");
+  const int sizes[] = {64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048};
+  int top = 0;
+  for (int n : sizes)
+    if (n <= std::max(64, max_n)) top = n;
+  double* a = alloc((int64_t)top * top);
+  double* w = alloc(top);
+  int* info = nullptr;
+  cuda_check(cudaMallocAsync((void**)&info, sizeof(int), stream_), "alloc info");
+  for (int n : sizes) {
+    if (n > top) break;
+    // symmetric tridiagonal test matrix: 2 on the diagonal, -1 beside it
+    std::vector<double> m((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+      m[(size_t)i * n + i] = 2.0;
+      if (i + 1 < n) m[(size_t)i * n + i + 1] = m[(size_t)(i + 1) * n + i] = -1.0;
+    }
+    cuda_check(cudaMemcpyAsync(a, m.data(), m.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
+    int lw = 0;
+    if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, &lw) !=
+        CUSOLVER_STATUS_SUCCESS)
+      throw std::runtime_error("syevd buffer size");
+    if (lw > solver_lwork_) {
+      if (solver_work_) free(solver_work_);
+      solver_work_ = alloc(lw);
+      solver_lwork_ = lw;
+    }
+    if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, solver_work_,
+                         (int)solver_lwork_, info) != CUSOLVER_STATUS_SUCCESS)
+      throw std::runtime_error("syevd launch failed");
+    sync();
+    char what[48];
+    std::snprintf(what, sizeof(what), "prepare syevd n=%d", n);
+    laps.lap(what);
+  }
+  free(a);
+  free(w);
+  cudaFreeAsync(info, stream_);
   sync();
 }
 
@@ -2447,6 +2568,9 @@ void GpuEngine::set_rotation(const std::vector<std::vector<double>>& rot, const 
 // operators (renormalise_transform, BaseOperator.C:341-363; MatrixRotate,
 // MatrixBLAS.C:553-572).
 void GpuEngine::renormalise(Block& small, const Block& big) {
+  PlanLaps laps{"renormalise"};
+  double rflops = 0.0;
+  const DevBlock& dbig = blocks_.at(big.handle);
   double* dst = arena(small);
   const double* src = arena(big);
   const int64_t chunk_limit = 64ll << 20;  // scratch elements per chunk (512 MB)
@@ -2499,29 +2623,76 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
       if (bi < 0) continue;
       const OpBlock& bb = BL.blocks[bi];
       const int mb = rot_kept_[b], mk = rot_kept_[k];
-      // T = O U_k
-      dev::GemmUnit u{};
-      u.c_buf = 3;
-      u.c_off = scratch;
-      u.ldc = mk;
-      u.m = bb.rows;
-      u.n = mk;
-      u.beta_one = 0;
-      u.ibeg = (int)ia.size();
-      dev::GemmItem g{};
-      g.a_buf = 0;
-      g.a_off = be.base + bb.offset;
-      g.lda = bb.cols;
-      g.ta = 0;
-      g.b_buf = 2;
-      g.b_off = rot_off_[k];
-      g.ldb = mk;
-      g.tb = 0;
-      g.k = bb.cols;
-      g.alpha = 1.0;
-      ia.push_back(g);
-      u.iend = (int)ia.size();
-      ua.push_back(u);
+      // T = O U_k; for a built block only its nonzero rectangles take part:
+      // one unit per row band (rows without a rectangle are written as zero),
+      // one item per rectangle in column order
+      auto nzit = dbig.nz.find(be.base + bb.offset);
+      if (nzit == dbig.nz.end()) {
+        dev::GemmUnit u{};
+        u.c_buf = 3;
+        u.c_off = scratch;
+        u.ldc = mk;
+        u.m = bb.rows;
+        u.n = mk;
+        u.beta_one = 0;
+        u.ibeg = (int)ia.size();
+        dev::GemmItem g{};
+        g.a_buf = 0;
+        g.a_off = be.base + bb.offset;
+        g.lda = bb.cols;
+        g.ta = 0;
+        g.b_buf = 2;
+        g.b_off = rot_off_[k];
+        g.ldb = mk;
+        g.tb = 0;
+        g.k = bb.cols;
+        g.alpha = 1.0;
+        ia.push_back(g);
+        u.iend = (int)ia.size();
+        ua.push_back(u);
+        rflops += 2.0 * bb.rows * bb.cols * mk;
+      } else {
+        auto rects = nzit->second;  // (r0, c0, rows, cols)
+        std::sort(rects.begin(), rects.end());
+        auto band = [&](int r0, int rows) {
+          dev::GemmUnit u{};
+          u.c_buf = 3;
+          u.c_off = scratch + (int64_t)r0 * mk;
+          u.ldc = mk;
+          u.m = rows;
+          u.n = mk;
+          u.beta_one = 0;
+          u.ibeg = u.iend = (int)ia.size();
+          ua.push_back(u);
+        };
+        int next_row = 0;
+        for (size_t x = 0; x < rects.size();) {
+          const int r0 = rects[x][0], rows = rects[x][2];
+          if (r0 < next_row || r0 + rows > bb.rows) throw std::runtime_error("renormalise: overlapping rectangles");
+          if (r0 > next_row) band(next_row, r0 - next_row);
+          band(r0, rows);
+          for (; x < rects.size() && rects[x][0] == r0; ++x) {
+            if (rects[x][2] != rows || rects[x][1] + rects[x][3] > bb.cols)
+              throw std::runtime_error("renormalise: ragged rectangle band");
+            dev::GemmItem g{};
+            g.a_buf = 0;
+            g.a_off = be.base + bb.offset + (int64_t)r0 * bb.cols + rects[x][1];
+            g.lda = bb.cols;
+            g.ta = 0;
+            g.b_buf = 2;
+            g.b_off = rot_off_[k] + (int64_t)rects[x][1] * mk;
+            g.ldb = mk;
+            g.tb = 0;
+            g.k = rects[x][3];
+            g.alpha = 1.0;
+            ia.push_back(g);
+            rflops += 2.0 * rows * rects[x][3] * mk;
+          }
+          ua.back().iend = (int)ia.size();
+          next_row = r0 + rows;
+        }
+        if (next_row < bb.rows) band(next_row, bb.rows - next_row);
+      }
       // O' = U_b^T T
       dev::GemmUnit v{};
       v.c_buf = 1;
@@ -2546,10 +2717,17 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
       v.iend = (int)ib.size();
       ub.push_back(v);
       scratch += (int64_t)bb.rows * mk;
+      rflops += 2.0 * mb * mk * bb.rows;
       if (scratch > chunk_limit) flush();
     }
   }
   flush();
+  if (laps.on) {
+    sync();
+    char what[64];
+    std::snprintf(what, sizeof(what), "U^T O U %.3g flops", rflops);
+    laps.lap(what);
+  }
   // keep the rotation with the block (guess transform of later steps)
   {
     RotRecord rec;

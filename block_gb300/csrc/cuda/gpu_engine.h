@@ -4,7 +4,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <map>
+#include <unordered_map>
 #include <stdexcept>
 #include <set>
 #include <memory>
@@ -66,9 +68,12 @@ struct SigmaPlan {
   DevArray<dev::GemmTask> t1, t2;
   DevArray<dev::DiagUnit> du;
   DevArray<dev::DiagItem> di;
+  DevArray<dev::GemmTask> dtask;  // 64 x 64 tiles of the diagonal units
   DevArray<dev::CopyUnit> ru;  // FP64 sum of split stage-2 partial sectors into sigma
   DevArray<dev::CopyItem> ri;
-  double* scratch = nullptr;  // stage-1 intermediates, then split stage-2 partial sectors
+  // stage-1 intermediates, then split stage-2 partial sectors (FP64 path;
+  // allocated on the first FP64 product)
+  mutable double* scratch = nullptr;
   int64_t scratch_elems = 0;
   double flops = 0.0;         // FP64-equivalent flops of one sigma
   double bytes = 0.0;         // algorithmic bytes of one sigma (operator blocks + psi + sigma)
@@ -105,6 +110,10 @@ struct SigmaPlan {
   bool tc_tuned = false;           // knobs chosen by the autotuner
   std::vector<int2> tc_l1, tc_l2;  // per-sector launches: (first block range, blocks)
   int64_t tc_partial_cap = 0;      // float2 capacity of tc_partials
+  size_t tc_pool_cap[dev::kTcPools] = {};  // bytes of each packed pool
+  // the pools come from (and return to) the engine's pool cache: set for the
+  // plan of the sweep's consecutive solves, whose pools have similar sizes
+  bool reuse_pools = false;
 };
 
 class GpuEngine : public Engine {
@@ -125,6 +134,7 @@ class GpuEngine : public Engine {
   bool refine_parked(int id, const Superblock& sb, std::vector<double>& energies) override;
   void drop_parked(int id) override;
   std::string step_stats() override;
+  void prepare_density(int max_n) override;
   void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
@@ -201,6 +211,10 @@ class GpuEngine : public Engine {
     int64_t n = 0;
     std::vector<double> host;  // dot blocks keep a host copy (their 1x1 blocks fold into factors)
     bool dot = false;
+    // blocks built by build_block: the nonzero rectangles (row, column,
+    // rows, columns) of every operator block, keyed by the block's arena
+    // offset; everything outside them is zero
+    std::unordered_map<int64_t, std::vector<std::array<int, 4>>> nz;
   };
   std::map<int, DevBlock> blocks_;
   int next_handle_ = 0;
@@ -249,6 +263,9 @@ class GpuEngine : public Engine {
   int* tc_status_host_ = nullptr;
   // header of the Davidson control record, read back after every iteration
   dev::DavCtl* dav_host_ = nullptr;
+  // packed-operand pools of the last solve's plan, handed to the next one
+  __nv_bfloat16* pool_cache_[dev::kTcPools] = {};
+  size_t pool_cache_cap_[dev::kTcPools] = {};
 
  public:
   // Davidson iterations as launches of a captured CUDA graph (else the same

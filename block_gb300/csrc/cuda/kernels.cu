@@ -140,29 +140,77 @@ cudaError_t launch_copy(const Bufs& bufs, double* dst, const CopyUnit* units, co
 
 // Diagonal of the superblock Hamiltonian (diagonal TensorProduct /
 // TensorTrace, operatorfunctions.C:653-762).
-__global__ void __launch_bounds__(256) diag_kernel(Bufs bufs, double* __restrict__ d, const DiagUnit* __restrict__ units,
-                                                   const DiagItem* __restrict__ items) {
-  const DiagUnit u = units[blockIdx.x];
-  const int64_t total = (int64_t)u.rows * u.cols;
-  for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-    const int i = (int)(e / u.cols), j = (int)(e % u.cols);
-    double s = d[u.d_off + e];
-    for (int it = u.ibeg; it < u.iend; ++it) {
-      const DiagItem c = items[it];
-      const double a = c.a_off < 0 ? 1.0 : bufs.p[c.a_buf][c.a_off + (int64_t)i * c.a_stride];
-      const double b = c.b_off < 0 ? 1.0 : bufs.p[c.b_buf][c.b_off + (int64_t)j * c.b_stride];
-      s = fma(c.alpha * a, b, s);
+// Same sums as a GEMM: over a 64 x 64 tile of a sector, d(i, j) +=
+// sum_t (alpha_t a_t[i]) b_t[j] with the items t as the K dimension, 16
+// items at a time gathered into shared memory (the diagonals of the
+// operator blocks are strided reads), 4 x 4 outputs per thread.
+__global__ void __launch_bounds__(NT) diag_tile_kernel(Bufs bufs, double* __restrict__ d,
+                                                       const DiagUnit* __restrict__ units,
+                                                       const DiagItem* __restrict__ items,
+                                                       const GemmTask* __restrict__ tasks) {
+  __shared__ double As[TK][TM + 1];
+  __shared__ double Bs[TK][TN + 1];
+  const GemmTask task = tasks[blockIdx.x];
+  const DiagUnit u = units[task.unit];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int row0 = task.tm * TM, col0 = task.tn * TN;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+  for (int it0 = u.ibeg; it0 < u.iend; it0 += TK) {
+#pragma unroll
+    for (int r = 0; r < (TM * TK) / NT; ++r) {
+      const int e = tid + r * NT;
+      const int p = e / TM, i = e % TM;
+      const int it = it0 + p;
+      double va = 0.0, vb = 0.0;
+      if (it < u.iend) {
+        const DiagItem c = items[it];
+        if (row0 + i < u.rows)
+          va = c.alpha * (c.a_off < 0 ? 1.0 : bufs.p[c.a_buf][c.a_off + (int64_t)(row0 + i) * c.a_stride]);
+        if (col0 + i < u.cols) vb = c.b_off < 0 ? 1.0 : bufs.p[c.b_buf][c.b_off + (int64_t)(col0 + i) * c.b_stride];
+      }
+      As[p][i] = va;
+      Bs[p][i] = vb;
     }
-    d[u.d_off + e] = s;
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < TK; ++p) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[p][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[p][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gi = row0 + ty * 4 + i;
+    if (gi >= u.rows) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gj = col0 + tx * 4 + j;
+      if (gj >= u.cols) continue;
+      d[u.d_off + (int64_t)gi * u.cols + gj] += acc[i][j];
+    }
   }
 }
 
-cudaError_t launch_diag(const Bufs& bufs, double* d, const DiagUnit* units, const DiagItem* items, int nunits,
-                        cudaStream_t s) {
-  if (nunits <= 0) return cudaSuccess;
-  diag_kernel<<<nunits, 256, 0, s>>>(bufs, d, units, items);
+cudaError_t launch_diag_tiles(const Bufs& bufs, double* d, const DiagUnit* units, const DiagItem* items,
+                              const GemmTask* tasks, int ntasks, cudaStream_t s) {
+  if (ntasks <= 0) return cudaSuccess;
+  diag_tile_kernel<<<ntasks, NT, 0, s>>>(bufs, d, units, items, tasks);
   return cudaGetLastError();
 }
+
 
 // ------------------------------------------------------------------------
 // Deterministic reductions and BLAS-1 over the flat wavefunction arena

@@ -81,8 +81,10 @@ cudaError_t launch_gemm(const Bufs& bufs, const GemmUnit* units, const GemmItem*
                         int ntasks, cudaStream_t s);
 cudaError_t launch_copy(const Bufs& bufs, double* dst, const CopyUnit* units, const CopyItem* items, int nunits,
                         cudaStream_t s);
-cudaError_t launch_diag(const Bufs& bufs, double* d, const DiagUnit* units, const DiagItem* items, int nunits,
-                        cudaStream_t s);
+// d[off + i*cols + j] += sum over the unit's items, by 64 x 64 tiles of the
+// units (task.unit, task.tm, task.tn), the items as the K dimension of a GEMM
+cudaError_t launch_diag_tiles(const Bufs& bufs, double* d, const DiagUnit* units, const DiagItem* items,
+                              const GemmTask* tasks, int ntasks, cudaStream_t s);
 
 // out[i*ny + j] = sum_t x_i[t] * y_j[t] for i < nx, j < ny, vectors stored
 // row-wise with stride ld; deterministic two-pass reduction using `work`

@@ -250,6 +250,9 @@ std::unique_ptr<Block> SweepDriver::renormalised(const Block& big, const std::ve
 void SweepDriver::warmup() {
   const int M = C_.schedule.front().M;
   cur_M_ = M;
+  int maxM = M;
+  for (const auto& e : C_.schedule) maxM = std::max(maxM, e.M);
+  E_.prepare_density(maxM);
   for (int p = N_ - 2; p >= 3; --p) {
     Block& sys = right_block(p + 1);
     std::vector<int> own;
@@ -345,6 +348,7 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   }
   using clk = std::chrono::steady_clock;
   auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+  const SweepResult phase0 = phase_;
   auto t0 = clk::now();
   Block L = make_enlarged(left_block(p - 1), p, true, specL);
   Block R = make_enlarged(right_block(p + 2), p + 1, false, specR);
@@ -417,9 +421,11 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   prev_.L = L.si;
   prev_.R = R.si;
   prev_.sectors = sb.sectors;
-  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f%s  disc=%.3e%s\n", forward ? "fwd" : "bwd", p,
-      L.si.total_states(), R.si.total_states(), (long)sb.size, iters, energies.empty() ? 0.0 : energies[0], prec_tag,
-      disc, E_.step_stats().c_str());
+  log(1, "  %s p=%2d  L=%ld R=%ld psi=%ld  iters=%d  E=%.12f%s  disc=%.3e%s  [build %.3fs solve %.3fs density %.3fs renorm %.3fs]\n",
+      forward ? "fwd" : "bwd", p, L.si.total_states(), R.si.total_states(), (long)sb.size, iters,
+      energies.empty() ? 0.0 : energies[0], prec_tag, disc, E_.step_stats().c_str(),
+      phase_.build_seconds - phase0.build_seconds, phase_.solve_seconds - phase0.solve_seconds,
+      phase_.density_seconds - phase0.density_seconds, phase_.renorm_seconds - phase0.renorm_seconds);
   if (parked >= 0) {
     // keep the step's enlarged blocks for a refinement at the end of the sweep
     auto c = std::make_unique<Candidate>();

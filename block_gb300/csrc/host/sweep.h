@@ -116,6 +116,9 @@ class Engine {
   virtual void drop_parked(int id) { (void)id; }
   // engine-specific timing of the last block step, for verbose logs
   virtual std::string step_stats() { return std::string(); }
+  // loads the dense eigensolver of the density-matrix sectors for sectors of
+  // up to max_n states (called once by the warm-up, before the first sweep)
+  virtual void prepare_density(int max_n) { (void)max_n; }
   // FP64 Rayleigh quotients of the last solve's vectors (no-op for engines
   // that solve in FP64); returns true if the energies changed precision
   virtual bool refine(const Superblock& sb, std::vector<double>& energies) {
