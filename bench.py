@@ -30,6 +30,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 DEFAULT_CONF = os.path.join(ROOT, "tests", "golden", "syn24", "dmrg.conf")
+# config 1: 12-site Hubbard chain, M 50 -> 100, 4 sweeps (whole-sweep timing)
+SWEEP_CONF = os.path.join(ROOT, "tests", "golden", "hubbard12", "dmrg.conf")
 METRIC = "sigma TFLOP/s & sweep time: split-prec batched vs FP64 GPU at |dE|<=1e-6 Eh"
 
 
@@ -49,6 +51,9 @@ def parse():
                     help="default schedule knobs instead of the autotuner's (tensor-core paths)")
     ap.add_argument("--no-schedules", action="store_true",
                     help="skip the per-sector-launch baseline and default-knob comparison")
+    ap.add_argument("--no-sweeps", action="store_true", help="skip the sweep-time comparison")
+    ap.add_argument("--sweep-conf", default=SWEEP_CONF,
+                    help="dmrg.conf of the sweep-time comparison (GPU FP64, GPU split, CPU oracle)")
     ap.add_argument("--profile", action="store_true",
                     help="open the CUDA profiler range around the device-timed steps only")
     return ap.parse_args()
@@ -383,6 +388,28 @@ def run_ours(a):
                                                "unit": "TFLOP/s", "cores": 1,
                                                "sample": "1 sigma product of the same superblock, one thread"}}
         line["fp64_sigma_rel_err_vs_oracle"] = err
+    if rank == 0 and not a.no_sweeps:
+        # whole sweeps (bgpu_run_dmrg: warm-up, then the conf's sweeps) in
+        # plain FP64 and in the split precision, beside the CPU oracle's sweep
+        sw = {"conf": os.path.relpath(a.sweep_conf, ROOT)}
+        for prec in ("fp64", a.precision):
+            ctx.set_precision(prec)
+            t0 = time.perf_counter()
+            e, st = ctx.run_dmrg(a.sweep_conf)
+            sw[prec] = {"seconds": time.perf_counter() - t0, "energy": float(e[0]), "sweeps": st["sweeps"],
+                        "sigma_calls": st["sigma_calls"], "sigma_seconds": st["sigma_seconds"]}
+        ctx.set_precision(a.precision)
+        sw["dE_split_minus_fp64"] = sw[a.precision]["energy"] - sw["fp64"]["energy"]
+        if not a.no_cpu_baseline:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import pyoracle
+
+            t0 = time.perf_counter()
+            e, st = pyoracle.run(a.sweep_conf)
+            sw["cpu_oracle"] = {"seconds": time.perf_counter() - t0, "energy": float(e[0]), "sweeps": st["sweeps"],
+                                "cores": os.cpu_count() or 1}
+            sw["dE_fp64_minus_cpu"] = sw["fp64"]["energy"] - sw["cpu_oracle"]["energy"]
+        line["sweeps"] = sw
     ctx.device_free(x)
     ctx.device_free(y)
     ctx.close()

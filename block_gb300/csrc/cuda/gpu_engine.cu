@@ -12,6 +12,8 @@
 
 #include "../host/dense.h"
 
+#include <deque>
+#include <mutex>
 #include <queue>
 #include <set>
 #include <unordered_map>
@@ -26,13 +28,103 @@ void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// ------------------------------------------------------------------ staging
+//
+// A host-to-device copy from pageable memory waits for the stream, so every
+// work-list upload would stall the host until the device caught up.  Uploads
+// are therefore staged through a pinned ring buffer per stream: the data is
+// copied into the ring, the device copy is queued behind the work already on
+// the stream, and a ring region is reused only after the event recorded
+// behind its copy has completed.  The host thus compiles the next step's
+// work lists while the device still runs the current step.
+namespace {
+struct StageRing {
+  char* ring = nullptr;
+  size_t cap = 0, head = 0;
+  struct Span {
+    size_t beg, end;
+    cudaEvent_t ev;
+  };
+  std::deque<Span> inflight;
+  std::vector<cudaEvent_t> spare;
+  void drain() {
+    for (auto& sp : inflight) {
+      cudaEventSynchronize(sp.ev);
+      spare.push_back(sp.ev);
+    }
+    inflight.clear();
+  }
+};
+std::mutex g_stage_mu;
+std::map<cudaStream_t, StageRing> g_stage;
+}  // namespace
+
+cudaError_t stage_h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return cudaSuccess;
+  std::lock_guard<std::mutex> lk(g_stage_mu);
+  StageRing& st = g_stage[s];
+  const size_t need = (bytes + 255) & ~(size_t)255;
+  if (need > st.cap / 4) {  // the ring holds at least four of the largest copy
+    st.drain();
+    if (st.ring) cudaFreeHost(st.ring);
+    st.ring = nullptr;
+    st.cap = std::max<size_t>(size_t(64) << 20, 4 * need);
+    st.head = 0;
+    if (cudaMallocHost((void**)&st.ring, st.cap) != cudaSuccess) {
+      cudaGetLastError();
+      st.ring = nullptr;
+      st.cap = 0;
+      return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);  // unstaged
+    }
+  }
+  size_t p = st.head;
+  if (p + need > st.cap) p = 0;
+  // wait for the newest copy still reading [p, p + need); copies on one
+  // stream complete in order, so every older span is free as well
+  int last = -1;
+  for (int i = 0; i < (int)st.inflight.size(); ++i)
+    if (st.inflight[i].beg < p + need && p < st.inflight[i].end) last = i;
+  if (last >= 0) {
+    cudaError_t e = cudaEventSynchronize(st.inflight[last].ev);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i <= last; ++i) {
+      st.spare.push_back(st.inflight.front().ev);
+      st.inflight.pop_front();
+    }
+  }
+  std::memcpy(st.ring + p, src, bytes);
+  cudaError_t e = cudaMemcpyAsync(dst, st.ring + p, bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t ev;
+  if (!st.spare.empty()) {
+    ev = st.spare.back();
+    st.spare.pop_back();
+  } else if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+    return e;
+  }
+  if ((e = cudaEventRecord(ev, s)) != cudaSuccess) return e;
+  st.inflight.push_back({p, p + need, ev});
+  st.head = p + need;
+  return cudaSuccess;
+}
+
+void release_staging(cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_stage_mu);
+  auto it = g_stage.find(s);
+  if (it == g_stage.end()) return;
+  it->second.drain();
+  for (cudaEvent_t ev : it->second.spare) cudaEventDestroy(ev);
+  if (it->second.ring) cudaFreeHost(it->second.ring);
+  g_stage.erase(it);
+}
+
 template <class T>
 void DevArray<T>::upload(const std::vector<T>& h, cudaStream_t s) {
   release(s);
   n = h.size();
   if (n == 0) return;
   cuda_check(cudaMallocAsync((void**)&d, n * sizeof(T), s), "cudaMallocAsync(desc)");
-  cuda_check(cudaMemcpyAsync(d, h.data(), n * sizeof(T), cudaMemcpyHostToDevice, s), "upload desc");
+  cuda_check(stage_h2d(d, h.data(), n * sizeof(T), s), "upload desc");
 }
 template <class T>
 void DevArray<T>::release(cudaStream_t s) {
@@ -80,6 +172,7 @@ GpuEngine::~GpuEngine() {
   for (auto* q : pool_cache_)
     if (q) cudaFreeAsync(q, stream_);
   cudaStreamSynchronize(stream_);
+  release_staging(stream_);
   if (solver_) cusolverDnDestroy((cusolverDnHandle_t)solver_);
   cudaEventDestroy(ev0_);
   cudaEventDestroy(ev1_);
@@ -100,6 +193,13 @@ void GpuEngine::free(double* p) {
 }
 void GpuEngine::sync() {
   cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  for (auto& ev : pending_renorm_) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev.first, ev.second) == cudaSuccess) renorm_device_seconds += ms * 1e-3;
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
+  pending_renorm_.clear();
   if (*tc_status_host_) {
     *tc_status_host_ = 0;
     cudaMemset(tc_status_, 0, sizeof(int));
@@ -139,7 +239,7 @@ void GpuEngine::release_block(Block& b) {
 void GpuEngine::upload_block(Block& b, const std::vector<double>& a) {
   DevBlock& d = blocks_.at(b.handle);
   if ((int64_t)a.size() != d.n) throw std::runtime_error("upload_block: size mismatch");
-  cuda_check(cudaMemcpyAsync(d.d, a.data(), a.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "upload");
+  cuda_check(stage_h2d(d.d, a.data(), a.size() * sizeof(double), stream_), "upload");
   if (b.is_dot || d.dot) d.host = a;
   sync();
 }
@@ -461,8 +561,9 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
   if (big.is_dot) {
     dt.host.resize(dt.n);
     cuda_check(cudaMemcpyAsync(dt.host.data(), dt.d, dt.n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    sync();
   }
-  sync();
+  // otherwise stream-ordered: the host goes on planning while the copies run
 }
 
 // ------------------------------------------------------------------ sigma
@@ -715,7 +816,6 @@ void GpuEngine::plan_sigma(const Superblock& sb, SigmaPlan& plan) {
   plan.du.upload(du, stream_);
   plan.di.upload(di, stream_);
   plan.dtask.upload(dtask, stream_);
-  sync();
 }
 
 void GpuEngine::free_tc(SigmaPlan& p) {
@@ -1207,7 +1307,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   plan.tc_tuned = false;
   schedule_tc(sb, plan, kn);
   plan.tc = true;
-  sync();
+  if (laps.on) sync();
   laps.lap("schedule");
 }
 
@@ -1719,11 +1819,19 @@ void GpuEngine::hdiag(const Superblock& sb, const SigmaPlan& p, double* d) {
 // the row of the new vector (b_new . sigma_j), instead of the reference's
 // full recomputation of b_i . sigma_j: the same matrix up to rounding, at
 // O(k n) instead of O(k^2 n) memory traffic per iteration.
-int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) {
+void GpuEngine::prepare_plan(const Superblock& sb) {
   if (have_plan_) free_plan(plan_);
   plan_.reuse_pools = true;
   plan_sigma(sb, plan_);
+  if (precision_tc(precision)) plan_tc(sb, plan_);
   have_plan_ = true;
+  prepared_ = true;
+}
+
+int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<double>& energies) {
+  // work lists compiled by prepare_plan for this superblock, else now
+  if (!prepared_ || !have_plan_ || plan_.n != sb.size) prepare_plan(sb);
+  prepared_ = false;
   const int64_t n = sb.size;
   const int nroots = p.nroots;
   if (n < nroots) throw std::runtime_error("superblock smaller than number of roots");
@@ -2542,7 +2650,6 @@ void GpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {
   cuda_check(dev::launch_gather_cols(dm_vecs_, rot_, du.d, dc.d, (int)units.size(), stream_), "gather");
   du.release(stream_);
   dc.release(stream_);
-  sync();
 }
 
 void GpuEngine::set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) {
@@ -2560,8 +2667,7 @@ void GpuEngine::set_rotation(const std::vector<std::vector<double>>& rot, const 
   for (int q = 0; q < nq; ++q) std::copy(rot[q].begin(), rot[q].end(), h.begin() + rot_off_[q]);
   if (rot_) free(rot_);
   rot_ = alloc(tot);
-  cuda_check(cudaMemcpyAsync(rot_, h.data(), tot * sizeof(double), cudaMemcpyHostToDevice, stream_), "rot");
-  sync();
+  cuda_check(stage_h2d(rot_, h.data(), tot * sizeof(double), stream_), "rot");
 }
 
 // O'(b',k') = U_b^T O(b,k) U_k in two grouped-GEMM launches per chunk of
@@ -2572,6 +2678,10 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
   double rflops = 0.0;
   const DevBlock& dbig = blocks_.at(big.handle);
   double* dst = arena(small);
+  std::pair<cudaEvent_t, cudaEvent_t> ev{};
+  cuda_check(cudaEventCreate(&ev.first), "event");
+  cuda_check(cudaEventCreate(&ev.second), "event");
+  cuda_check(cudaEventRecord(ev.first, stream_), "record");
   const double* src = arena(big);
   const int64_t chunk_limit = 64ll << 20;  // scratch elements per chunk (512 MB)
   std::vector<dev::GemmUnit> ua, ub;
@@ -2754,7 +2864,11 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
       block_rot_[small.handle] = std::move(rec);
     }
   }
-  sync();
+  // stream-ordered: the host goes on with the next step's block builds and
+  // work-list compilation while the products run; their device time is
+  // read from the events at the next synchronisation
+  cuda_check(cudaEventRecord(ev.second, stream_), "record");
+  pending_renorm_.push_back(ev);
 }
 
 }  // namespace bgpu

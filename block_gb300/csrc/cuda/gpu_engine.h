@@ -38,6 +38,10 @@ struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
 void cuda_check(cudaError_t e, const char* what);
+// host-to-device copy queued on stream s without waiting for it (staged
+// through a pinned ring buffer of that stream); release_staging frees the ring
+cudaError_t stage_h2d(void* dst, const void* src, size_t bytes, cudaStream_t s);
+void release_staging(cudaStream_t s);
 
 // Device array of trivially-copyable descriptors.
 template <class T>
@@ -135,6 +139,13 @@ class GpuEngine : public Engine {
   void drop_parked(int id) override;
   std::string step_stats() override;
   void prepare_density(int max_n) override;
+  void prepare_plan(const Superblock& sb) override;
+  // (synchronises, so that every renormalisation issued so far is counted)
+  double device_renorm_seconds() override {
+    sync();
+    return renorm_device_seconds;
+  }
+  double renorm_device_seconds = 0.0;  // device time of the renormalisations (events)
   void density(const Superblock& sb, bool left, const std::vector<double>& weights, DensitySpectrum& spec) override;
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
@@ -221,6 +232,8 @@ class GpuEngine : public Engine {
   // current superblock plan (solve)
   SigmaPlan plan_;
   bool have_plan_ = false;
+  bool prepared_ = false;  // plan_ was compiled by prepare_plan for the next solve
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending_renorm_;
   double* waves_ = nullptr;
   int64_t wave_n_ = 0;
   int nwaves_ = 0;

@@ -119,6 +119,11 @@ class Engine {
   // loads the dense eigensolver of the density-matrix sectors for sectors of
   // up to max_n states (called once by the warm-up, before the first sweep)
   virtual void prepare_density(int max_n) { (void)max_n; }
+  // compiles the sigma work lists of the superblock the next solve() gets
+  // (engines that run asynchronously overlap this with device work)
+  virtual void prepare_plan(const Superblock& sb) { (void)sb; }
+  // device seconds of the renormalisations so far (< 0: not measured)
+  virtual double device_renorm_seconds() { return -1.0; }
   // FP64 Rayleigh quotients of the last solve's vectors (no-op for engines
   // that solve in FP64); returns true if the energies changed precision
   virtual bool refine(const Superblock& sb, std::vector<double>& energies) {
@@ -149,6 +154,7 @@ struct SweepResult {
   // superblock set-up, Davidson solve, density matrix + rotation choice,
   // renormalisation
   double build_seconds = 0.0, solve_seconds = 0.0, density_seconds = 0.0, renorm_seconds = 0.0;
+  double renorm_device_seconds = -1.0;  // device time of the renormalisations (< 0: not measured)
 };
 
 struct DriverOptions {

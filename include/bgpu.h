@@ -278,9 +278,10 @@ int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition,
  * energies[max_roots] receive the final energies; stats[13] (may be NULL):
  *   sweeps, sigma calls, sigma seconds, sigma flops, total seconds, max
  *   discarded weight, last-sweep energy, number of roots, then wall seconds
- *   of the block-build, Davidson, density/rotation and renormalisation
- *   phases, and the host seconds spent compiling sigma work lists (part of
- *   the Davidson phase).
+ *   of the block-build, Davidson and density/rotation phases, the device
+ *   seconds of the renormalisations (they run while the host builds and
+ *   plans the next step, so the phases overlap), and the host seconds spent
+ *   compiling sigma work lists (part of the Davidson phase).
  */
 int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
                   double* stats);
