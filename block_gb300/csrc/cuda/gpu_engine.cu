@@ -2328,6 +2328,44 @@ bool GpuEngine::transform_guess(const GuessInput& g, const Superblock& sb) {
   return ok;
 }
 
+bool GpuEngine::get_rotation_record(const Block& b, RotationRecord& r) {
+  auto it = block_rot_.find(b.handle);
+  if (it == block_rot_.end() || !it->second.d) return false;
+  const RotRecord& rec = it->second;
+  r.off = rec.off;
+  r.n = rec.n;
+  r.m = rec.m;
+  r.small_of_big = rec.small_of_big;
+  r.big_of_small = rec.big_of_small;
+  int64_t tot = 0;
+  for (size_t q = 0; q < rec.off.size(); ++q) tot = std::max<int64_t>(tot, rec.off[q] + (int64_t)rec.n[q] * rec.m[q]);
+  r.data.assign(std::max<int64_t>(tot, 1), 0.0);
+  cuda_check(cudaMemcpyAsync(r.data.data(), rec.d, r.data.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+             "d2h rotation");
+  sync();
+  return true;
+}
+
+void GpuEngine::set_rotation_record(const Block& b, const RotationRecord& r) {
+  const size_t nq = r.off.size();
+  if (r.n.size() != nq || r.m.size() != nq || r.small_of_big.size() != nq)
+    throw std::runtime_error("rotation record: inconsistent sizes");
+  for (size_t q = 0; q < nq; ++q)
+    if (r.off[q] < 0 || r.off[q] + (int64_t)r.n[q] * r.m[q] > (int64_t)r.data.size())
+      throw std::runtime_error("rotation record: sector outside its data");
+  RotRecord rec;
+  rec.off = r.off;
+  rec.n = r.n;
+  rec.m = r.m;
+  rec.small_of_big = r.small_of_big;
+  rec.big_of_small = r.big_of_small;
+  rec.d = alloc((int64_t)std::max<size_t>(r.data.size(), 1));
+  cuda_check(stage_h2d(rec.d, r.data.data(), r.data.size() * sizeof(double), stream_), "h2d rotation");
+  auto old = block_rot_.find(b.handle);
+  if (old != block_rot_.end()) free(old->second.d);
+  block_rot_[b.handle] = std::move(rec);
+}
+
 int GpuEngine::park_vectors() {
   if (!precision_slices(precision) || !waves_ || nwaves_ < 1) return -1;
   Parked pk;

@@ -140,6 +140,8 @@ class GpuEngine : public Engine {
   std::string step_stats() override;
   void prepare_density(int max_n) override;
   void prepare_plan(const Superblock& sb) override;
+  bool get_rotation_record(const Block& b, RotationRecord& r) override;
+  void set_rotation_record(const Block& b, const RotationRecord& r) override;
   // (synchronises, so that every renormalisation issued so far is counted)
   double device_renorm_seconds() override {
     sync();

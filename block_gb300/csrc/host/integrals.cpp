@@ -298,6 +298,14 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
     else if (key == "deflation_max_size" || key == "max_deflation_size") { need(1); c.deflation_max = std::stoi(tok[1]); }
     else if (key == "deflation_min_size") { need(1); c.deflation_min = std::stoi(tok[1]); }
     else if (key == "warmup") { if (tok.size() > 1) c.warmup = lower(tok[1]); }
+    else if (key == "restart" || key == "fullrestart") c.restart = true;
+    else if (key == "reset_iter" || key == "reset_iters" || key == "reset_iterations") c.reset_iter = true;
+    else if (key == "checkpoint") {
+      need(1);
+      std::string p = tok[1];
+      if (p[0] != '/' && !base_dir.empty()) p = base_dir + "/" + p;
+      c.checkpoint = p;
+    }
     else if (key == "hubbard" || key == "heisenberg" || key == "nonspinadapted" || key == "bcs" || key == "onedot")
       throw std::runtime_error("dmrg.conf keyword not supported on this path: " + key);
     else if (key == "schedule") {
@@ -327,6 +335,8 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
     c.deflation_max = std::max(c.deflation_max, c.nroots + 20);
   }
   if (c.weights.empty()) c.weights.assign(c.nroots, 1.0 / c.nroots);
+  if (c.restart && c.checkpoint.empty())
+    c.checkpoint = (base_dir.empty() ? std::string(".") : base_dir) + "/bgpu_checkpoint.bin";
   if (c.schedule_default) make_default_schedule(c);
   if (c.schedule.empty()) throw std::runtime_error("dmrg.conf: no schedule");
   if (c.maxiter < c.schedule.back().iter) c.maxiter = c.schedule.back().iter + 2;

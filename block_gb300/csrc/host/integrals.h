@@ -77,6 +77,12 @@ struct Config {
   int deflation_min = 2, deflation_max = 20;
   uint64_t seed = 12345;  // warm-up rotations and Davidson guesses
   std::string warmup = "random";
+  // sweep checkpoints (this project's restart format, host/checkpoint.h):
+  // `checkpoint <path>` writes one after every completed sweep; `restart`
+  // (or `fullrestart`) resumes from it instead of the warm-up, and
+  // `reset_iter` then starts the schedule from its first entry again
+  std::string checkpoint;
+  bool restart = false, reset_iter = false;
   // the remaining keywords are recognised and ignored (twodot_to_onedot,
   // hf_occ, onepdm/twopdm, noise columns ...)
   const ScheduleEntry& entry(int sweep) const;

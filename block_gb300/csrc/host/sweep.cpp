@@ -247,6 +247,72 @@ std::unique_ptr<Block> SweepDriver::renormalised(const Block& big, const std::ve
   return nb;
 }
 
+void SweepDriver::save_checkpoint(const std::string& path, int sweeps_done, bool next_forward, double sweep_energy,
+                                  const std::vector<double>& sweep_energies) {
+  CheckpointHeader h;
+  h.norb = N_;
+  h.nelec = target_.n;
+  h.target = target_;
+  h.nroots = C_.nroots;
+  h.fingerprint = integrals_fingerprint(I_);
+  h.sweeps_done = sweeps_done;
+  h.next_forward = next_forward ? 1 : 0;
+  h.cur_M = cur_M_;
+  h.discarded = last_discarded_;
+  h.last_sweep_energy = sweep_energy;
+  h.energies = last_energies_;
+  h.sweep_energies = sweep_energies;
+  CheckpointWriter w(path);
+  w.header(h);
+  int nb = 0;
+  std::vector<double> arena;
+  for (int side = 0; side < 2; ++side)
+    for (int p = 0; p < N_; ++p) {
+      const Block* b = side == 0 ? left_[p].get() : right_[p].get();
+      if (!b || b->handle < 0) continue;
+      E_.download_block(*b, arena);  // one block at a time on the host
+      RotationRecord rr;
+      const bool has = E_.get_rotation_record(*b, rr);
+      w.block(side, p, b->sites, b->si, b->ops, arena, has ? &rr : nullptr);
+      ++nb;
+    }
+  w.finish(nb);
+}
+
+int SweepDriver::load_checkpoint(const std::string& path, bool& next_forward, double& sweep_energy,
+                                 std::vector<double>& sweep_energies) {
+  CheckpointReader rd(path);
+  const CheckpointHeader& h = rd.header();
+  if (h.norb != N_ || h.target != target_ || h.nroots != C_.nroots)
+    throw std::runtime_error("checkpoint " + path + " was written for another system (orbitals, target or roots)");
+  if (h.fingerprint != integrals_fingerprint(I_))
+    throw std::runtime_error("checkpoint " + path + " was written for another Hamiltonian");
+  CheckpointBlock cb;
+  while (rd.next(cb)) {
+    if (cb.index < 0 || cb.index >= N_ || (cb.side != 0 && cb.side != 1))
+      throw std::runtime_error("checkpoint: block position out of range");
+    auto b = std::make_unique<Block>();
+    b->sites = cb.sites;
+    b->si = cb.si;
+    b->ops = make_opset(b->si, std::set<OpKey>(cb.keys.begin(), cb.keys.end()), I_.orbsym, g_);
+    if (b->ops.arena != (int64_t)cb.arena.size())
+      throw std::runtime_error("checkpoint: operator catalogue does not match its stored arena");
+    E_.create_block(*b);
+    E_.upload_block(*b, cb.arena);
+    if (cb.has_rot) E_.set_rotation_record(*b, cb.rot);
+    auto& slot = cb.side == 0 ? left_[cb.index] : right_[cb.index];
+    if (slot) E_.release_block(*slot);
+    slot = std::move(b);
+  }
+  cur_M_ = h.cur_M;
+  last_discarded_ = h.discarded;
+  last_energies_ = h.energies;
+  next_forward = h.next_forward != 0;
+  sweep_energy = h.last_sweep_energy;
+  sweep_energies = h.sweep_energies;
+  return h.sweeps_done;
+}
+
 void SweepDriver::warmup() {
   const int M = C_.schedule.front().M;
   cur_M_ = M;
@@ -511,11 +577,25 @@ double SweepDriver::sweep(bool forward, int sweep_index) {
 
 SweepResult SweepDriver::run() {
   SweepResult res;
-  warmup();
   double eprev = std::numeric_limits<double>::infinity();
+  int s_begin = 0;
+  bool first_forward = true;
+  if (C_.restart) {
+    // resume after the checkpoint's last sweep (dmrg.C:476-560 restarts from
+    // the saved blocks the same way); reset_iter starts the schedule over
+    int maxM = 0;
+    for (const auto& e : C_.schedule) maxM = std::max(maxM, e.M);
+    E_.prepare_density(maxM);
+    s_begin = load_checkpoint(C_.checkpoint, first_forward, eprev, res.sweep_energies);
+    if (C_.reset_iter) s_begin = 0;
+    log(1, "restart from %s: %d sweeps done, next sweep %s\n", C_.checkpoint.c_str(), s_begin,
+        first_forward ? "forward" : "backward");
+  } else {
+    warmup();
+  }
   const int last_sched = C_.schedule.back().iter;
-  for (int s = 0; s < C_.maxiter; ++s) {
-    const bool forward = (s % 2 == 0);
+  for (int s = s_begin; s < C_.maxiter; ++s) {
+    const bool forward = ((s - s_begin) % 2 == 0) == first_forward;
     const auto ts = std::chrono::steady_clock::now();
     const double r0 = E_.device_renorm_seconds();
     const double e = sweep(forward, s);
@@ -528,6 +608,12 @@ SweepResult SweepDriver::run() {
         s, forward ? "fwd" : "bwd", C_.entry(s).M, e, e - eprev, last_discarded_,
         std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count(), phase_.build_seconds,
         phase_.solve_seconds, phase_.density_seconds, phase_.renorm_seconds, E_.device_renorm_seconds() - r0);
+    if (!C_.checkpoint.empty()) {
+      const auto tc = std::chrono::steady_clock::now();
+      save_checkpoint(C_.checkpoint, s + 1, !forward, e, res.sweep_energies);
+      log(1, "checkpoint after sweep %d written to %s (%.2fs)\n", s, C_.checkpoint.c_str(),
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - tc).count());
+    }
     if (s >= last_sched && std::fabs(e - eprev) <= C_.sweep_tol) break;
     eprev = e;
   }

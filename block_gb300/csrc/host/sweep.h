@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "checkpoint.h"
 #include "integrals.h"
 #include "ops.h"
 #include "stateinfo.h"
@@ -124,6 +125,17 @@ class Engine {
   virtual void prepare_plan(const Superblock& sb) { (void)sb; }
   // device seconds of the renormalisations so far (< 0: not measured)
   virtual double device_renorm_seconds() { return -1.0; }
+  // rotation that made a renormalised block (kept by engines that transform
+  // wavefunction guesses), read and restored by checkpoints
+  virtual bool get_rotation_record(const Block& b, RotationRecord& r) {
+    (void)b;
+    (void)r;
+    return false;
+  }
+  virtual void set_rotation_record(const Block& b, const RotationRecord& r) {
+    (void)b;
+    (void)r;
+  }
   // FP64 Rayleigh quotients of the last solve's vectors (no-op for engines
   // that solve in FP64); returns true if the energies changed precision
   virtual bool refine(const Superblock& sb, std::vector<double>& energies) {
@@ -206,6 +218,11 @@ class SweepDriver {
 
  private:
   std::vector<int> warmup_rotation(Block& big, int M, uint64_t seed);
+  // checkpoint after `sweeps_done` sweeps; restore returns the sweeps done
+  void save_checkpoint(const std::string& path, int sweeps_done, bool next_forward, double sweep_energy,
+                       const std::vector<double>& sweep_energies);
+  int load_checkpoint(const std::string& path, bool& next_forward, double& sweep_energy,
+                      std::vector<double>& sweep_energies);
   std::unique_ptr<Block> renormalised(const Block& big, const std::vector<int>& kept, const CatalogSpec& spec);
   double step(bool forward, int p, int sweep_index, std::vector<double>& energies);
   Block make_dot_block(int x);
