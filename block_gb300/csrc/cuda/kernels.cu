@@ -261,52 +261,6 @@ cudaError_t launch_gram(const double* X, int nx, const double* Y, int ny, int64_
   return cudaGetLastError();
 }
 
-__global__ void combine_kernel(const double* __restrict__ X, int k, int64_t n, int64_t ld, const double* __restrict__ coef,
-                               int kout, double* __restrict__ Y, int64_t ldy) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-    double x[kMaxGram];
-#pragma unroll
-    for (int i = 0; i < kMaxGram; ++i)
-      if (i < k) x[i] = X[(int64_t)i * ld + t];
-    for (int r = 0; r < kout; ++r) {
-      double s = 0.0;
-#pragma unroll
-      for (int i = 0; i < kMaxGram; ++i)
-        if (i < k) s = fma(coef[i * kout + r], x[i], s);
-      Y[(int64_t)r * ldy + t] = s;
-    }
-  }
-}
-
-cudaError_t launch_combine(const double* X, int k, int64_t n, int64_t ld, const double* coef, int kout, double* Y,
-                           int64_t ldy, cudaStream_t s) {
-  if (k > kMaxGram) return cudaErrorInvalidValue;
-  combine_kernel<<<kGramBlocks * 2, 256, 0, s>>>(X, k, n, ld, coef, kout, Y, ldy);
-  return cudaGetLastError();
-}
-
-__global__ void project_out_kernel(const double* __restrict__ X, int k, int64_t n, int64_t ld,
-                                   const double* __restrict__ coef, double* __restrict__ r) {
-  __shared__ double c[kMaxGram];
-  if (threadIdx.x < kMaxGram) c[threadIdx.x] = threadIdx.x < k ? coef[threadIdx.x] : 0.0;
-  __syncthreads();
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-    double s = 0.0;
-    for (int i = 0; i < k; ++i) s = fma(c[i], X[(int64_t)i * ld + t], s);
-    r[t] -= s;
-  }
-}
-
-cudaError_t launch_project_out(const double* X, int k, int64_t n, int64_t ld, const double* coef, double* r,
-                               cudaStream_t s) {
-  if (k > kMaxGram) return cudaErrorInvalidValue;
-  if (k <= 0 || n <= 0) return cudaSuccess;
-  project_out_kernel<<<kGramBlocks * 2, 256, 0, s>>>(X, k, n, ld, coef, r);
-  return cudaGetLastError();
-}
-
 __global__ void axpy_kernel(double a, const double* __restrict__ x, double* __restrict__ y, int64_t n) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) y[t] = fma(a, x[t], y[t]);
@@ -318,14 +272,6 @@ __global__ void scale_kernel(double a, double* __restrict__ x, int64_t n) {
 __global__ void fill_kernel(double* __restrict__ x, double v, int64_t n) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) x[t] = v;
-}
-// Linear::precondition (linear.C:27-47)
-__global__ void precond_kernel(double* __restrict__ r, const double* __restrict__ d, double e, int64_t n) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-    const double den = e - d[t];
-    if (fabs(den) > 1e-12) r[t] /= den;
-  }
 }
 
 static int blocks_for(int64_t n) {
@@ -345,10 +291,6 @@ cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t s) {
 }
 cudaError_t launch_fill(double* x, double v, int64_t n, cudaStream_t s) {
   fill_kernel<<<blocks_for(n), 256, 0, s>>>(x, v, n);
-  return cudaGetLastError();
-}
-cudaError_t launch_precondition(double* r, const double* d, double e, int64_t n, cudaStream_t s) {
-  precond_kernel<<<blocks_for(n), 256, 0, s>>>(r, d, e, n);
   return cudaGetLastError();
 }
 

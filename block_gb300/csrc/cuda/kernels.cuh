@@ -92,18 +92,8 @@ cudaError_t launch_diag_tiles(const Bufs& bufs, double* d, const DiagUnit* units
 constexpr int kGramBlocks = 304;
 cudaError_t launch_gram(const double* X, int nx, const double* Y, int ny, int64_t n, int64_t ld, double* work,
                         double* out, cudaStream_t s);
-// Y[j] = sum_i A[i*ld_a + j] * X[i] for the rows X[i] (vectors) of a k x n block:
-// out_row r = sum_i coef[i*k + r] * X_i, for r < k   (basis rotation)
-cudaError_t launch_combine(const double* X, int k, int64_t n, int64_t ld, const double* coef, int kout, double* Y,
-                           int64_t ldy, cudaStream_t s);
-// r -= sum_i coef[i] * X_i for the k rows X_i (stride ld); coef is device
-// memory (for instance the output of launch_gram), so no host round trip
-cudaError_t launch_project_out(const double* X, int k, int64_t n, int64_t ld, const double* coef, double* r,
-                               cudaStream_t s);
 cudaError_t launch_axpy(double a, const double* x, double* y, int64_t n, cudaStream_t s);
 cudaError_t launch_scale(double a, double* x, int64_t n, cudaStream_t s);
-// r_i /= (e - d_i) where |e - d_i| > 1e-12
-cudaError_t launch_precondition(double* r, const double* d, double e, int64_t n, cudaStream_t s);
 cudaError_t launch_fill(double* x, double v, int64_t n, cudaStream_t s);
 
 // Batched symmetric eigensolver: matrices A_b (n_b x n_b, row-major at
