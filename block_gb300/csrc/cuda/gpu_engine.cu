@@ -167,13 +167,19 @@ GpuEngine::~GpuEngine() {
   for (auto& kv : parked_)
     if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
   if (guess_) cudaFreeAsync(guess_, stream_);
-  if (solver_work_) cudaFreeAsync(solver_work_, stream_);
+  for (auto& l : lanes_)
+    if (l.work) cudaFreeAsync(l.work, stream_);
   if (solver_info_) cudaFreeAsync(solver_info_, stream_);
   for (auto* q : pool_cache_)
     if (q) cudaFreeAsync(q, stream_);
   cudaStreamSynchronize(stream_);
   release_staging(stream_);
-  if (solver_) cusolverDnDestroy((cusolverDnHandle_t)solver_);
+  for (auto& l : lanes_) {
+    if (l.h) cusolverDnDestroy((cusolverDnHandle_t)l.h);
+    if (l.done) cudaEventDestroy(l.done);
+    if (l.s) cudaStreamDestroy(l.s);
+  }
+  if (fork_) cudaEventDestroy(fork_);
   cudaEventDestroy(ev0_);
   cudaEventDestroy(ev1_);
   cudaFree(tc_status_);
@@ -2537,39 +2543,49 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
     cuda_check(dev::launch_jacobi(rho, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, small_max, stream_),
                "density eig");
   if (!large.empty()) {
-    auto h = (cusolverDnHandle_t)solver_;
-    if (!h) {
-      if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnCreate failed");
-      solver_ = h;
-    }
-    if (cusolverDnSetStream(h, stream_) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnSetStream");
-    int need = 0;
-    for (int q : large) {
-      int lw = 0;
-      if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, dm_dims_[q],
-                                      dm_vecs_ + off[q], dm_dims_[q], w + woff[q], &lw) != CUSOLVER_STATUS_SUCCESS)
-        throw std::runtime_error("syevd buffer size");
-      need = std::max(need, lw);
-    }
-    if (need > solver_lwork_) {
-      if (solver_work_) free(solver_work_);
-      solver_work_ = alloc(need);
-      solver_lwork_ = need;
-    }
+    ensure_lanes();
     if ((int)large.size() > solver_ninfo_) {
       if (solver_info_) cudaFreeAsync(solver_info_, stream_);
       cuda_check(cudaMallocAsync((void**)&solver_info_, large.size() * sizeof(int), stream_), "alloc info");
       solver_ninfo_ = (int)large.size();
     }
+    // sector i goes to lane i % kSolverLanes; workspaces grow on the engine
+    // stream, before the lanes fork from it
+    int64_t need[kSolverLanes] = {};
+    for (size_t i = 0; i < large.size(); ++i) {
+      const int q = large[i];
+      int lw = 0;
+      auto h = (cusolverDnHandle_t)lanes_[i % kSolverLanes].h;
+      if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, dm_dims_[q],
+                                      dm_vecs_ + off[q], dm_dims_[q], w + woff[q], &lw) != CUSOLVER_STATUS_SUCCESS)
+        throw std::runtime_error("syevd buffer size");
+      need[i % kSolverLanes] = std::max<int64_t>(need[i % kSolverLanes], lw);
+    }
+    const int used = (int)std::min<size_t>(large.size(), kSolverLanes);
+    for (int l = 0; l < used; ++l)
+      if (need[l] > lanes_[l].lwork) {
+        if (lanes_[l].work) free(lanes_[l].work);
+        lanes_[l].work = alloc(need[l]);
+        lanes_[l].lwork = need[l];
+      }
+    for (int q : large)
+      cuda_check(cudaMemcpyAsync(dm_vecs_ + off[q], rho + off[q], (size_t)dm_dims_[q] * dm_dims_[q] * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, stream_),
+                 "copy rho");
+    cuda_check(cudaEventRecord(fork_, stream_), "fork");
+    for (int l = 0; l < used; ++l) cuda_check(cudaStreamWaitEvent(lanes_[l].s, fork_, 0), "lane wait");
     for (size_t i = 0; i < large.size(); ++i) {
       const int q = large[i];
       const int n = dm_dims_[q];
-      cuda_check(cudaMemcpyAsync(dm_vecs_ + off[q], rho + off[q], (size_t)n * n * sizeof(double),
-                                 cudaMemcpyDeviceToDevice, stream_),
-                 "copy rho");
-      if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, dm_vecs_ + off[q], n, w + woff[q],
-                           solver_work_, (int)solver_lwork_, solver_info_ + i) != CUSOLVER_STATUS_SUCCESS)
+      SolverLane& ln = lanes_[i % kSolverLanes];
+      if (cusolverDnDsyevd((cusolverDnHandle_t)ln.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                           dm_vecs_ + off[q], n, w + woff[q], ln.work, (int)ln.lwork,
+                           solver_info_ + i) != CUSOLVER_STATUS_SUCCESS)
         throw std::runtime_error("syevd launch failed");
+    }
+    for (int l = 0; l < used; ++l) {
+      cuda_check(cudaEventRecord(lanes_[l].done, lanes_[l].s), "lane done");
+      cuda_check(cudaStreamWaitEvent(stream_, lanes_[l].done, 0), "join lane");
     }
   }
   if (laps.on) {
@@ -2610,12 +2626,9 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
 // warm-up.
 void GpuEngine::prepare_density(int max_n) {
   PlanLaps laps{"density"};
-  auto h = (cusolverDnHandle_t)solver_;
-  if (!h) {
-    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnCreate failed");
-    solver_ = h;
-  }
-  if (cusolverDnSetStream(h, stream_) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnSetStream");
+  ensure_lanes();
+  SolverLane& ln = lanes_[0];
+  auto h = (cusolverDnHandle_t)ln.h;
   const int sizes[] = {64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048};
   int top = 0;
   for (int n : sizes)
@@ -2637,15 +2650,16 @@ void GpuEngine::prepare_density(int max_n) {
     if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, &lw) !=
         CUSOLVER_STATUS_SUCCESS)
       throw std::runtime_error("syevd buffer size");
-    if (lw > solver_lwork_) {
-      if (solver_work_) free(solver_work_);
-      solver_work_ = alloc(lw);
-      solver_lwork_ = lw;
+    if (lw > ln.lwork) {
+      if (ln.work) free(ln.work);
+      ln.work = alloc(lw);
+      ln.lwork = lw;
     }
-    if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, solver_work_,
-                         (int)solver_lwork_, info) != CUSOLVER_STATUS_SUCCESS)
+    sync();  // the lane stream reads what the engine stream wrote
+    if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, ln.work, (int)ln.lwork,
+                         info) != CUSOLVER_STATUS_SUCCESS)
       throw std::runtime_error("syevd launch failed");
-    sync();
+    cuda_check(cudaStreamSynchronize(ln.s), "lane sync");
     char what[48];
     std::snprintf(what, sizeof(what), "prepare syevd n=%d", n);
     laps.lap(what);
@@ -2654,6 +2668,19 @@ void GpuEngine::prepare_density(int max_n) {
   free(w);
   cudaFreeAsync(info, stream_);
   sync();
+}
+
+void GpuEngine::ensure_lanes() {
+  if (!fork_) cuda_check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "event");
+  for (auto& l : lanes_) {
+    if (l.h) continue;
+    cusolverDnHandle_t h = nullptr;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnCreate failed");
+    l.h = h;
+    cuda_check(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking), "lane stream");
+    cuda_check(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming), "event");
+    if (cusolverDnSetStream(h, l.s) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnSetStream");
+  }
 }
 
 void GpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {

@@ -245,9 +245,20 @@ class GpuEngine : public Engine {
   std::vector<int> dm_dims_;
   std::vector<char> dm_colmajor_;  // sector eigenvectors stored column-major (dense solver)
   // dense symmetric eigensolver for the large density-matrix sectors
-  void* solver_ = nullptr;  // cusolverDnHandle_t
-  double* solver_work_ = nullptr;
-  int64_t solver_lwork_ = 0;
+  // lanes of the dense solver: the large sectors of one density matrix are
+  // decomposed concurrently, each lane with its own handle, stream and
+  // workspace (the stream joins the engine stream through events)
+  struct SolverLane {
+    void* h = nullptr;  // cusolverDnHandle_t
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
+    double* work = nullptr;
+    int64_t lwork = 0;
+  };
+  static constexpr int kSolverLanes = 4;
+  SolverLane lanes_[kSolverLanes];
+  cudaEvent_t fork_ = nullptr;
+  void ensure_lanes();
   int* solver_info_ = nullptr;
   int solver_ninfo_ = 0;
   double* rot_ = nullptr;
