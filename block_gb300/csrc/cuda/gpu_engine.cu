@@ -2621,45 +2621,53 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
 }
 
 // The dense divide-and-conquer solver loads its kernels on first use of
-// each size class, which took up to seconds inside the first sweep; one
-// solve per size class (64 .. 2048 states, capped at max_n) moves that to the
-// warm-up.
+// each size class and handle, which took up to seconds inside the first
+// sweep; one solve per size class (64 .. 2048 states, up to 1.25 max_n) on
+// every solver lane moves that to the warm-up.
 void GpuEngine::prepare_density(int max_n) {
   PlanLaps laps{"density"};
   ensure_lanes();
-  SolverLane& ln = lanes_[0];
-  auto h = (cusolverDnHandle_t)ln.h;
   const int sizes[] = {64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048};
+  // sectors of a density matrix reach ~0.9 M states; size classes up to 1.25 M
   int top = 0;
   for (int n : sizes)
-    if (n <= std::max(64, max_n)) top = n;
-  double* a = alloc((int64_t)top * top);
-  double* w = alloc(top);
+    if (n <= std::max(64, max_n + max_n / 4)) top = n;
+  double* a = alloc((int64_t)kSolverLanes * top * top);
+  double* w = alloc((int64_t)kSolverLanes * top);
   int* info = nullptr;
-  cuda_check(cudaMallocAsync((void**)&info, sizeof(int), stream_), "alloc info");
+  cuda_check(cudaMallocAsync((void**)&info, kSolverLanes * sizeof(int), stream_), "alloc info");
   for (int n : sizes) {
     if (n > top) break;
-    // symmetric tridiagonal test matrix: 2 on the diagonal, -1 beside it
+    // symmetric tridiagonal test matrix: 2 on the diagonal, -1 beside it,
+    // one copy per lane (each lane's handle loads its kernels on first use)
     std::vector<double> m((size_t)n * n, 0.0);
     for (int i = 0; i < n; ++i) {
       m[(size_t)i * n + i] = 2.0;
       if (i + 1 < n) m[(size_t)i * n + i + 1] = m[(size_t)(i + 1) * n + i] = -1.0;
     }
-    cuda_check(cudaMemcpyAsync(a, m.data(), m.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
-    int lw = 0;
-    if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, &lw) !=
-        CUSOLVER_STATUS_SUCCESS)
-      throw std::runtime_error("syevd buffer size");
-    if (lw > ln.lwork) {
-      if (ln.work) free(ln.work);
-      ln.work = alloc(lw);
-      ln.lwork = lw;
+    for (int l = 0; l < kSolverLanes; ++l) {
+      SolverLane& ln = lanes_[l];
+      double* al = a + (int64_t)l * top * top;
+      cuda_check(cudaMemcpyAsync(al, m.data(), m.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
+      int lw = 0;
+      if (cusolverDnDsyevd_bufferSize((cusolverDnHandle_t)ln.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                      al, n, w + (int64_t)l * top, &lw) != CUSOLVER_STATUS_SUCCESS)
+        throw std::runtime_error("syevd buffer size");
+      if (lw > ln.lwork) {
+        if (ln.work) free(ln.work);
+        ln.work = alloc(lw);
+        ln.lwork = lw;
+      }
     }
-    sync();  // the lane stream reads what the engine stream wrote
-    if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, a, n, w, ln.work, (int)ln.lwork,
-                         info) != CUSOLVER_STATUS_SUCCESS)
-      throw std::runtime_error("syevd launch failed");
-    cuda_check(cudaStreamSynchronize(ln.s), "lane sync");
+    sync();  // the lane streams read what the engine stream wrote
+    for (int l = 0; l < kSolverLanes; ++l) {
+      SolverLane& ln = lanes_[l];
+      if (cusolverDnDsyevd((cusolverDnHandle_t)ln.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                           a + (int64_t)l * top * top, n, w + (int64_t)l * top, ln.work, (int)ln.lwork,
+                           info + l) != CUSOLVER_STATUS_SUCCESS)
+        throw std::runtime_error("syevd launch failed");
+    }
+    for (auto& ln : lanes_) cuda_check(cudaStreamSynchronize(ln.s), "lane sync");
     char what[48];
     std::snprintf(what, sizeof(what), "prepare syevd n=%d", n);
     laps.lap(what);
