@@ -61,6 +61,10 @@ std::map<cudaStream_t, StageRing> g_stage;
 
 cudaError_t stage_h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (bytes == 0) return cudaSuccess;
+  // block arenas (restarts) are copied directly: a ring for them would pin
+  // several times their size
+  constexpr size_t kStageMax = size_t(256) << 20;
+  if (bytes > kStageMax) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   std::lock_guard<std::mutex> lk(g_stage_mu);
   StageRing& st = g_stage[s];
   const size_t need = (bytes + 255) & ~(size_t)255;
