@@ -12,7 +12,13 @@ the line also carries the plain FP64 path's sigma time and a Davidson solve
 of the same superblock in both arithmetics (time and energy difference).
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-                  [--precision fp64|bf16x3] [--conf PATH --partition P]
+                  [--precision fp64|bf16x3|bf16x6|bf16x3tc|fp16x2tc] [--conf PATH --partition P]
+                  [--sweep-conf PATH --sweep-precisions fp64,split]
+
+The default run adds whole-sweep times of the 12-site Hubbard chain (GPU
+FP64, GPU split precision, CPU oracle).  The 30-orbital M=2000 sweep:
+  python bench.py --no-davidson --no-schedules --no-cpu-baseline \
+      --sweep-conf tests/golden/syn30_sweep1/dmrg.conf --sweep-precisions split
 
 With torchrun (N > 1) every rank runs an independent replica on its own GPU
 ("replicas only": the sigma of one superblock is not sharded).
@@ -54,6 +60,8 @@ def parse():
     ap.add_argument("--no-sweeps", action="store_true", help="skip the sweep-time comparison")
     ap.add_argument("--sweep-conf", default=SWEEP_CONF,
                     help="dmrg.conf of the sweep-time comparison (GPU FP64, GPU split, CPU oracle)")
+    ap.add_argument("--sweep-precisions", default="fp64,split",
+                    help="comma list of the sweep comparison's GPU arithmetics: fp64, split (the --precision path)")
     ap.add_argument("--profile", action="store_true",
                     help="open the CUDA profiler range around the device-timed steps only")
     return ap.parse_args()
@@ -392,15 +400,20 @@ def run_ours(a):
         # whole sweeps (bgpu_run_dmrg: warm-up, then the conf's sweeps) in
         # plain FP64 and in the split precision, beside the CPU oracle's sweep
         sw = {"conf": os.path.relpath(a.sweep_conf, ROOT)}
-        for prec in ("fp64", a.precision):
+        ctx.set_autotune(False)  # sweeps with the default schedule knobs, as bgpu_run_dmrg runs them
+        wanted = [p.strip() for p in a.sweep_precisions.split(",") if p.strip()]
+        for prec in [{"split": a.precision}.get(p, p) for p in wanted]:
             ctx.set_precision(prec)
             t0 = time.perf_counter()
             e, st = ctx.run_dmrg(a.sweep_conf)
             sw[prec] = {"seconds": time.perf_counter() - t0, "energy": float(e[0]), "sweeps": st["sweeps"],
-                        "sigma_calls": st["sigma_calls"], "sigma_seconds": st["sigma_seconds"]}
+                        "sigma_calls": st["sigma_calls"], "sigma_seconds": st["sigma_seconds"],
+                        "phase_seconds": {k: st[k] for k in ("build_seconds", "solve_seconds", "density_seconds",
+                                                             "renorm_seconds")}}
         ctx.set_precision(a.precision)
-        sw["dE_split_minus_fp64"] = sw[a.precision]["energy"] - sw["fp64"]["energy"]
-        if not a.no_cpu_baseline:
+        if "fp64" in sw and a.precision in sw and a.precision != "fp64":
+            sw["dE_split_minus_fp64"] = sw[a.precision]["energy"] - sw["fp64"]["energy"]
+        if not a.no_cpu_baseline and "fp64" in sw:
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import pyoracle
 
