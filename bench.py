@@ -71,6 +71,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def whole_job(flops_per_step, t_step, t_e2e_step, dist=None, device="cuda"):
+    """Replicas only: every rank ran `flops_per_step` per step; the job's
+    step time is the slowest rank's (max over ranks), and the whole-job
+    throughput counts the work of all ranks.  Returns (t_step, t_e2e_step,
+    value, e2e) with the throughputs in TFLOP/s."""
+    world = 1
+    if dist is not None:
+        import torch
+
+        world = dist.get_world_size()
+        tt = torch.tensor([t_step, t_e2e_step], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step, t_e2e_step = tt.tolist()
+    return t_step, t_e2e_step, world * flops_per_step / t_step / 1e12, world * flops_per_step / t_e2e_step / 1e12
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -271,16 +287,7 @@ def run_ours(a):
     ctx.synchronize()
     clocks = clk.summary()
     t_step = ms[0] / a.steps * 1e-3
-    if dist:
-        import torch
-
-        tt = torch.tensor([t_step, t_e2e / a.steps], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step, t_e2e_step = tt.tolist()
-    else:
-        t_e2e_step = t_e2e / a.steps
-    value = world * flops / t_step / 1e12
-    e2e = world * flops / t_e2e_step / 1e12
+    t_step, t_e2e_step, value, e2e = whole_job(flops, t_step, t_e2e / a.steps, dist)
     split = a.precision != "fp64"
     kern_ms = (ms[1] if split else ms[1] + ms[2]) / a.steps
     achieved = flops / (kern_ms * 1e-3) / 1e12
