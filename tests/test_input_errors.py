@@ -1,0 +1,58 @@
+"""Host-side failure detection on the CPU: malformed dmrg.conf inputs, a
+missing FCIDUMP, keywords of methods outside this path, and a restart
+without a checkpoint are refused with an error (the reference aborts on
+most of these, input.C; here the driver raises and the C ABI returns a
+status code).  The parser and driver are the product's own host code; the
+oracle engine runs them without a GPU."""
+import os
+
+import pytest
+
+from conftest import GOLDEN
+
+BASE = """nelec 12
+spin 0
+schedule
+0 50 1e-8 0
+end
+maxiter 2
+sweep_tol 1e-12
+noreorder
+orbitals {orb}
+"""
+FCIDUMP = os.path.join(GOLDEN, "hubbard12", "FCIDUMP")
+
+
+def run_conf(oracle, tmp_path, text):
+    p = tmp_path / "dmrg.conf"
+    p.write_text(text)
+    return oracle.run(str(p))
+
+
+def test_valid_input_runs(oracle, tmp_path):
+    e, st = run_conf(oracle, tmp_path, BASE.format(orb=FCIDUMP))
+    assert st["sweeps"] == 2 and -7.0 < e[0] < -5.0
+
+
+@pytest.mark.parametrize("text", [
+    BASE.replace("0 50 1e-8 0", "0 50 1e-8"),                 # schedule line with 3 entries
+    BASE.replace("schedule\n0 50 1e-8 0\nend\n", ""),        # no schedule
+    BASE + "hubbard\n",                                        # other Hamiltonian family
+    BASE + "onedot\n",                                         # one-site sweeps
+    BASE + "nonspinadapted\n",                                 # determinant basis
+    BASE.replace("maxiter 2", "maxiter"),                      # keyword without its value
+    BASE.replace("orbitals {orb}", "orbitals synthetic:0:0:0:0:0"),  # empty synthetic system
+], ids=["schedule-entries", "no-schedule", "hubbard", "onedot", "nonspinadapted", "no-value", "bad-synthetic"])
+def test_malformed_input_refused(oracle, tmp_path, text):
+    with pytest.raises(RuntimeError):
+        run_conf(oracle, tmp_path, text.format(orb=FCIDUMP))
+
+
+def test_missing_fcidump_refused(oracle, tmp_path):
+    with pytest.raises(RuntimeError):
+        run_conf(oracle, tmp_path, BASE.format(orb=str(tmp_path / "no_such_FCIDUMP")))
+
+
+def test_restart_without_checkpoint_refused(oracle, tmp_path):
+    with pytest.raises(RuntimeError):
+        run_conf(oracle, tmp_path, BASE.format(orb=FCIDUMP) + "restart\n")
