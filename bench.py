@@ -409,7 +409,7 @@ def run_ours(a):
         sw = {"conf": os.path.relpath(a.sweep_conf, ROOT)}
         ctx.set_autotune(False)  # sweeps with the default schedule knobs, as bgpu_run_dmrg runs them
         wanted = [p.strip() for p in a.sweep_precisions.split(",") if p.strip()]
-        for prec in [{"split": a.precision}.get(p, p) for p in wanted]:
+        for prec in dict.fromkeys({"split": a.precision}.get(p, p) for p in wanted):
             ctx.set_precision(prec)
             t0 = time.perf_counter()
             e, st = ctx.run_dmrg(a.sweep_conf)
