@@ -15,11 +15,29 @@
 namespace oracle {
 
 // ------------------------------------------------------------------ dgemm
+// Optional Fortran DGEMM of a tuned BLAS (set by oracle_use_blas after a
+// self-check); the reference links one the same way (CMakeLists.txt:31-47).
+FortranDgemm g_blas_dgemm = nullptr;
+
 // Row-major DGEMM used where the reference calls MatrixMultiply -> DGEMM
-// (MatrixBLAS.C:438-498).  Operands are packed to row-major non-transposed
-// panels, then an i-k-j loop with a 64-column tile keeps B rows in cache.
+// (MatrixBLAS.C:438-498): through the tuned BLAS when one is set (row-major
+// C = op(A) op(B) is column-major C^T = op(B)^T op(A)^T, as MatrixMultiply
+// maps it, MatrixBLAS.C:456-483), else operands are packed to row-major
+// non-transposed panels and an i-k-j loop with a 64-column tile keeps B rows
+// in cache.
 void dgemm(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
            double beta, double* C, int ldc) {
+  if (m <= 0 || n <= 0) return;
+  if (g_blas_dgemm && k > 0) {
+    const char tra = tb ? 'T' : 'N', trb = ta ? 'T' : 'N';
+    g_blas_dgemm(&tra, &trb, &n, &m, &k, &alpha, B, &ldb, A, &lda, &beta, C, &ldc);
+    return;
+  }
+  dgemm_loop(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+void dgemm_loop(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
+                int ldb, double beta, double* C, int ldc) {
   if (m <= 0 || n <= 0) return;
   if (beta != 1.0)
     for (int i = 0; i < m; ++i)

@@ -17,6 +17,14 @@ using namespace bgpu;
 // Row-major C = alpha * op(A) * op(B) + beta * C, op = transpose when t* is true.
 void dgemm(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
            double beta, double* C, int ldc);
+// the built-in loop of dgemm (used when no tuned BLAS is set)
+void dgemm_loop(bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda, const double* B,
+                int ldb, double beta, double* C, int ldc);
+// Fortran DGEMM (column-major, arguments by reference)
+typedef void (*FortranDgemm)(const char* ta, const char* tb, const int* m, const int* n, const int* k,
+                             const double* alpha, const double* a, const int* lda, const double* b, const int* ldb,
+                             const double* beta, double* c, const int* ldc);
+extern FortranDgemm g_blas_dgemm;
 
 class CpuEngine : public Engine {
  public:

@@ -6,7 +6,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <dlfcn.h>
 #include <memory>
+#include <random>
 
 #include "cpu_engine.h"
 
@@ -66,6 +68,54 @@ int index_of(const SnapBlock& s, const Operand& o) {
 }  // namespace
 
 extern "C" {
+
+// Routes the oracle's DGEMM through the Fortran DGEMM of the shared library
+// at `path` (a tuned BLAS, e.g. the OpenBLAS bundled with SciPy), single-
+// threaded (the oracle threads over operator pairs itself).  The library is
+// kept only if its products match the built-in loop to 1e-12 on transposed
+// and plain operands.  Returns 0 when the BLAS is in use, < 0 otherwise;
+// path NULL switches back to the built-in loop.
+int oracle_use_blas(const char* path) {
+  using oracle::FortranDgemm;
+  oracle::g_blas_dgemm = nullptr;
+  if (!path) return 0;
+  void* h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+  if (!h) return -1;
+  FortranDgemm f = nullptr;
+  for (const char* name : {"scipy_dgemm_", "dgemm_"})
+    if (!f) f = (FortranDgemm)dlsym(h, name);
+  if (!f) return -2;
+  typedef void (*SetThreads)(int);
+  for (const char* name : {"scipy_openblas_set_num_threads", "openblas_set_num_threads"}) {
+    SetThreads st = (SetThreads)dlsym(h, name);
+    if (st) {
+      st(1);
+      break;
+    }
+  }
+  std::mt19937_64 rng(7);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  for (int ta = 0; ta < 2; ++ta)
+    for (int tb = 0; tb < 2; ++tb) {
+      const int m = 37, n = 29, k = 41, lda = (ta ? m : k) + 3, ldb = (tb ? k : n) + 2, ldc = n + 5;
+      std::vector<double> A((size_t)(ta ? k : m) * lda), B((size_t)(tb ? n : k) * ldb), C((size_t)m * ldc), D;
+      for (auto& x : A) x = u(rng);
+      for (auto& x : B) x = u(rng);
+      for (auto& x : C) x = u(rng);
+      D = C;
+      oracle::g_blas_dgemm = f;
+      oracle::dgemm(ta, tb, m, n, k, 0.75, A.data(), lda, B.data(), ldb, 0.5, C.data(), ldc);
+      oracle::g_blas_dgemm = nullptr;
+      oracle::dgemm_loop(ta, tb, m, n, k, 0.75, A.data(), lda, B.data(), ldb, 0.5, D.data(), ldc);
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j < n; ++j)
+          if (std::fabs(C[(size_t)i * ldc + j] - D[(size_t)i * ldc + j]) >
+              1e-12 * (1.0 + std::fabs(D[(size_t)i * ldc + j])))
+            return -3;
+    }
+  oracle::g_blas_dgemm = f;
+  return 0;
+}
 
 int oracle_run(const char* conf, int threads, int verbose, double* energies, int max_roots, double* stats) {
   try {

@@ -44,6 +44,84 @@ def lib():
     return _lib
 
 
+# ---------------------------------------------------------------- BLAS
+# The reference links a tuned BLAS for its DGEMMs (CMakeLists.txt:31-47);
+# the oracle can route its DGEMM through the OpenBLAS that SciPy bundles, so
+# that the CPU baseline is not held back by the built-in loop.  A library is
+# used only after a child process has run the oracle with it and matched the
+# built-in products, so a mismatched library cannot take down the caller.
+_blas = None  # (path or None, description)
+
+
+def blas_candidates():
+    import glob
+
+    out = []
+    try:
+        import scipy
+
+        base = os.path.dirname(os.path.dirname(scipy.__file__))
+        out += sorted(glob.glob(os.path.join(base, "scipy.libs", "libscipy_openblas*.so*")))
+    except ImportError:
+        pass
+    try:
+        import scipy_openblas32
+
+        out += sorted(glob.glob(os.path.join(os.path.dirname(scipy_openblas32.__file__), "lib", "libscipy_openblas*.so*")))
+    except ImportError:
+        pass
+    return [p for p in out if "openblas64" not in os.path.basename(p)]  # 64-bit-integer builds take other symbols
+
+
+def _blas_selftest(path):
+    """Child-process check: sigma of a small superblock with the BLAS equals
+    the built-in loop's to 1e-12 (relative)."""
+    L = lib()
+    L.oracle_use_blas.restype = ctypes.c_int
+    L.oracle_use_blas.argtypes = [ctypes.c_char_p]
+    conf = os.path.join(os.path.dirname(HERE), "tests", "golden", "hubbard", "dmrg.conf")
+    ref = snapshot(conf, 1, 3)
+    if L.oracle_use_blas(path.encode()) != 0:
+        return 1
+    got = snapshot(conf, 1, 3)
+    err = np.linalg.norm(got["sigma"] - ref["sigma"]) / np.linalg.norm(ref["sigma"])
+    return 0 if err <= 1e-12 else 2
+
+
+def enable_blas():
+    """Use the first candidate BLAS that passes the child-process check;
+    returns a description of the DGEMM in use."""
+    global _blas
+    if _blas is not None:
+        return _blas[1]
+    import sys
+
+    L = lib()
+    L.oracle_use_blas.restype = ctypes.c_int
+    L.oracle_use_blas.argtypes = [ctypes.c_char_p]
+    for path in blas_candidates():
+        code = "import sys; sys.path.insert(0, %r); import pyoracle; sys.exit(pyoracle._blas_selftest(%r))" % (HERE, path)
+        try:
+            rc = subprocess.run([sys.executable, "-c", code], capture_output=True, timeout=300).returncode
+        except (OSError, subprocess.TimeoutExpired):
+            rc = -1
+        if rc == 0 and L.oracle_use_blas(path.encode()) == 0:
+            _blas = (path, "OpenBLAS bundled with SciPy (%s), one thread per operator-pair worker" % os.path.basename(path))
+            return _blas[1]
+    _blas = (None, "built-in cache-blocked loop")
+    return _blas[1]
+
+
+def disable_blas():
+    """Back to the built-in DGEMM loop."""
+    global _blas
+    L = lib()
+    L.oracle_use_blas.restype = ctypes.c_int
+    L.oracle_use_blas.argtypes = [ctypes.c_char_p]
+    L.oracle_use_blas(None)
+    _blas = None
+
+
 def run(conf, threads=0, verbose=0, max_roots=32):
     L = lib()
     e = np.zeros(max_roots)
