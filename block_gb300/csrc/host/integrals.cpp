@@ -65,15 +65,48 @@ Integrals read_fcidump(const std::string& path) {
   if (norb <= 0) throw std::runtime_error("FCIDUMP header without NORB: " + path);
   I.resize(norb);
   for (int i = 0; i < norb && i < (int)orbsym.size(); ++i) I.orbsym[i] = orbsym[i];
-  double x;
-  int i, j, k, l;
-  while (f >> x >> i >> j >> k >> l) {
+  // value i j k l per line (1-based; k = l = 0: one-electron; all 0: core
+  // energy), input.C:1421-1663; Fortran D exponents are accepted, anything
+  // else that is not five numbers with indices in 0..norb is an error
+  long lineno = 0;
+  while (std::getline(f, line)) {
+    ++lineno;
+    std::istringstream ls(line);
+    std::vector<std::string> t;
+    while (ls >> w) t.push_back(w);
+    if (t.empty() || t[0][0] == '!') continue;  // blank and comment lines (ReadMeaningfulLine)
+    auto bad = [&](const char* why) {
+      return std::runtime_error(std::string("FCIDUMP ") + path + ": " + why + " in integral line " +
+                                std::to_string(lineno) + ": " + line);
+    };
+    if (t.size() != 5) throw bad("expected value i j k l");
+    for (auto& c : t[0])
+      if (c == 'D' || c == 'd') c = 'E';
+    double x;
+    int idx[4];
+    try {
+      size_t used = 0;
+      x = std::stod(t[0], &used);
+      if (used != t[0].size()) throw std::invalid_argument("value");
+      for (int q = 0; q < 4; ++q) {
+        idx[q] = std::stoi(t[q + 1], &used);
+        if (used != t[q + 1].size()) throw std::invalid_argument("index");
+      }
+    } catch (const std::logic_error&) {
+      throw bad("unreadable number");
+    }
+    for (int q = 0; q < 4; ++q)
+      if (idx[q] < 0 || idx[q] > norb) throw bad("orbital index out of range");
+    const int i = idx[0], j = idx[1], k = idx[2], l = idx[3];
     if (i == 0 && j == 0 && k == 0 && l == 0) I.ecore = x;
     else if (k == 0 && l == 0) {
+      if (i == 0 || j == 0) throw bad("one-electron integral with orbital 0");
       I.t[(size_t)(i - 1) * norb + (j - 1)] = x;
       I.t[(size_t)(j - 1) * norb + (i - 1)] = x;
-    } else
+    } else {
+      if (i == 0 || j == 0 || k == 0 || l == 0) throw bad("two-electron integral with orbital 0");
       I.set_eri(i - 1, j - 1, k - 1, l - 1, x);
+    }
   }
   return I;
 }

@@ -56,3 +56,42 @@ def test_missing_fcidump_refused(oracle, tmp_path):
 def test_restart_without_checkpoint_refused(oracle, tmp_path):
     with pytest.raises(RuntimeError):
         run_conf(oracle, tmp_path, BASE.format(orb=FCIDUMP) + "restart\n")
+
+
+def _dump(tmp_path, name, body_lines, norb=12):
+    src = open(FCIDUMP).read().splitlines()
+    head = []
+    for l in src:
+        head.append(l)
+        if "&END" in l.upper() or l.strip() == "/":
+            break
+    p = tmp_path / name
+    p.write_text("\n".join(head + body_lines) + "\n")
+    return str(p)
+
+
+def _integral_lines():
+    lines = open(FCIDUMP).read().splitlines()
+    k = next(i for i, l in enumerate(lines) if "&END" in l.upper() or l.strip() == "/")
+    return lines[k + 1:]
+
+
+def test_fcidump_fortran_exponents_and_comments(oracle, tmp_path):
+    e_ref, _ = run_conf(oracle, tmp_path, BASE.format(orb=FCIDUMP))
+    body = ["! integrals written with Fortran D exponents"]
+    for l in _integral_lines():
+        t = l.split()
+        if len(t) == 5:
+            body.append("%.15D %s %s %s %s".replace("%.15D", "%sD+00" % repr(float(t[0]))) % tuple(t[1:]))
+    e, _ = run_conf(oracle, tmp_path, BASE.format(orb=_dump(tmp_path, "FCIDUMP_D", body)))
+    assert abs(e[0] - e_ref[0]) <= 1e-9
+
+
+@pytest.mark.parametrize("line", ["1.0 13 1 0 0", "1.0 1 1 1", "1.0x 1 1 0 0", "1.0 0 1 0 0", "1.0 1 2 0 3"],
+                         ids=["index-above-norb", "four-fields", "bad-value", "orbital-0-one-electron",
+                              "orbital-0-two-electron"])
+def test_fcidump_bad_integral_line_refused(oracle, tmp_path, line):
+    body = _integral_lines()
+    body.insert(3, line)
+    with pytest.raises(RuntimeError):
+        run_conf(oracle, tmp_path, BASE.format(orb=_dump(tmp_path, "FCIDUMP_bad", body)))
