@@ -4,8 +4,8 @@ Copies the FCIDUMP inputs of the reference's energy tests (data files only)
 and records the expected energies its test scripts check:
   dmrg_tests/runtest:12,23,30 (test_energy.py tolerance 1e-6) and
   pydmrg/tests/test_dmrg_simple.py:34 (10 decimal places).
-Run in a container that has the reference mounted; the GPU machine only reads
-the committed copies.
+Run where the reference tree is available (path as the first argument);
+the tests read only the committed copies.
 """
 import hashlib
 import json
