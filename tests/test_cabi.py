@@ -51,3 +51,32 @@ def test_errors_without_gpu_are_reported():
         assert str(e)
     else:
         raise AssertionError("context creation must fail loudly without a GPU")
+
+
+def test_plain_c_caller_builds_and_links(tmp_path):
+    """include/bgpu.h is valid C: a C program that includes it, links the
+    library and calls an entry point that needs no GPU."""
+    import shutil
+
+    import block_gb300
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        import pytest
+
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "bgpu.h"\n'
+        "int main(void) {\n"
+        "  bgpu_ctx* ctx = 0;\n"
+        "  const char* v = bgpu_version();\n"
+        "  (void)ctx;\n"
+        '  printf("%s\\n", v);\n'
+        "  return v ? 0 : 1;\n}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(block_gb300.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", str(src), "-I", os.path.join(ROOT, "include"), "-L", libdir,
+                    "-lblockgb300", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    assert "sm_103a" in out
