@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libblockgb300.so")
 
 OP = dict(HAM=0, CRE=1, CRE_DES=2, CRE_CRE=3, CRE_DESCOMP=4, DES_DESCOMP=5, CRE_CRE_DESCOMP=6, OVERLAP=7)
 PREC = dict(fp64=0, bf16x3=1, bf16x6=2, bf16x3tc=3, fp16x2tc=4)
+# BGPU_NOALLOC_SCRATCH_DOUBLES: doubles of the fixed array behind bgpu_sigma_noalloc
+NOALLOC_SCRATCH_DOUBLES = 4 * 1024 * 1024
 
 _lib = None
 
@@ -70,6 +72,16 @@ _SIGS = {
     "bgpu_tc_wait_selftest": (_I, [_P, ctypes.c_double, _IP, _IP, _DP]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
+    "bgpu_block_set_sites": (_I, [_P, _I, _I, _IP]),
+    "bgpu_block_quanta": (_I, [_P, _I, _IP, _IP, _IP]),
+    "bgpu_integrals_load": (_I, [_P, _CP, _IP, _IP]),
+    "bgpu_integrals_define": (_I, [_P, _I, _IP, _DP, _DP, _D, _IP]),
+    "bgpu_integrals_free": (_I, [_P, _I]),
+    "bgpu_build_enlarged_ops": (_I, [_P, _I, _I, _I, _IP, _I, _IP, _IP, _I64P, _IP]),
+    "bgpu_set_wavefunctions": (_I, [_P, _I, _I, _DP]),
+    "bgpu_density_download": (_I, [_P, _DP, _DP, _I64]),
+    "bgpu_renormalise": (_I, [_P, _I, _IP, _DP, _I, _IP, _IP, _I64P, _IP]),
+    "bgpu_rotation_download": (_I, [_P, _I, _DP, _I64]),
 }
 
 EXPORTED = sorted(_SIGS)
@@ -176,6 +188,79 @@ class Context:
         self._check(self.lib.bgpu_block_download(self.h, handle, _dp(out), n))
         return out
 
+    def block_set_sites(self, handle, sites):
+        sites = np.ascontiguousarray(sites, dtype=np.int32)
+        self._check(self.lib.bgpu_block_set_sites(self.h, handle, len(sites), _ip(sites)))
+
+    def block_quanta(self, handle):
+        """(quanta as an (n, 3) array of (n, 2S, irrep), states per quantum)."""
+        nq = _I(0)
+        self._check(self.lib.bgpu_block_quanta(self.h, handle, ctypes.byref(nq), None, None))
+        q = np.zeros(3 * nq.value, dtype=np.int32)
+        st = np.zeros(nq.value, dtype=np.int32)
+        self._check(self.lib.bgpu_block_quanta(self.h, handle, ctypes.byref(nq), _ip(q), _ip(st)))
+        return q.reshape(-1, 3), st
+
+    # ---- operator builds and renormalisation (TensorProduct / transform_operators boundary)
+    def integrals_load(self, conf_path):
+        """Integrals of a dmrg.conf's `orbitals`: (handle, norb)."""
+        h, n = _I(), _I()
+        self._check(self.lib.bgpu_integrals_load(self.h, conf_path.encode(), ctypes.byref(h), ctypes.byref(n)))
+        return h.value, n.value
+
+    def integrals_define(self, orbsym, h1, eri, ecore=0.0):
+        orbsym = np.ascontiguousarray(orbsym, dtype=np.int32)
+        h1 = np.ascontiguousarray(h1, dtype=np.float64).reshape(-1)
+        eri = np.ascontiguousarray(eri, dtype=np.float64).reshape(-1)
+        h = _I()
+        self._check(self.lib.bgpu_integrals_define(self.h, len(orbsym), _ip(orbsym), _dp(h1), _dp(eri), float(ecore),
+                                                   ctypes.byref(h)))
+        return h.value
+
+    def integrals_free(self, handle):
+        self._check(self.lib.bgpu_integrals_free(self.h, handle))
+
+    def build_enlarged_ops(self, integrals, left, right, op_keys, filt=None):
+        """Enlarged block left (x) right with catalogue op_keys; filt =
+        (nelec, 2S, norb) of the system or None.  Returns (handle, arena
+        doubles, quanta)."""
+        op_keys = np.ascontiguousarray(op_keys, dtype=np.int32).reshape(-1)
+        f = np.ascontiguousarray(filt, dtype=np.int32) if filt is not None else None
+        h, n, nq = _I(), _I64(), _I()
+        self._check(self.lib.bgpu_build_enlarged_ops(self.h, integrals, left, right, _ip(f) if f is not None else None,
+                                                     len(op_keys) // 4, _ip(op_keys), ctypes.byref(h),
+                                                     ctypes.byref(n), ctypes.byref(nq)))
+        return h.value, n.value, nq.value
+
+    def set_wavefunctions(self, sb, vectors):
+        v = np.ascontiguousarray(np.atleast_2d(vectors), dtype=np.float64)
+        self._check(self.lib.bgpu_set_wavefunctions(self.h, sb, v.shape[0], _dp(v)))
+
+    def density_download(self, n):
+        """(rho, eigenvectors) of the last density matrix, n doubles each."""
+        rho = np.empty(n, dtype=np.float64)
+        vec = np.empty(n, dtype=np.float64)
+        self._check(self.lib.bgpu_density_download(self.h, _dp(rho), _dp(vec), n))
+        return rho, vec
+
+    def renormalise(self, big, kept, op_keys, rotations=None):
+        """U^T big U with kept states per quantum; rotations (concatenated
+        states x kept blocks) or None for the last density's eigenvectors.
+        Returns (handle, arena doubles, quanta)."""
+        kept = np.ascontiguousarray(kept, dtype=np.int32)
+        op_keys = np.ascontiguousarray(op_keys, dtype=np.int32).reshape(-1)
+        r = np.ascontiguousarray(rotations, dtype=np.float64) if rotations is not None else None
+        h, n, nq = _I(), _I64(), _I()
+        self._check(self.lib.bgpu_renormalise(self.h, big, _ip(kept), _dp(r) if r is not None else None,
+                                              len(op_keys) // 4, _ip(op_keys), ctypes.byref(h), ctypes.byref(n),
+                                              ctypes.byref(nq)))
+        return h.value, n.value, nq.value
+
+    def rotation_download(self, small, n):
+        out = np.empty(n, dtype=np.float64)
+        self._check(self.lib.bgpu_rotation_download(self.h, small, _dp(out), n))
+        return out
+
     def superblock_define(self, left, right, target, coef, term_ops, ecore=0.0):
         target = np.ascontiguousarray(target, dtype=np.int32)
         coef = np.ascontiguousarray(coef, dtype=np.float64)
@@ -215,8 +300,9 @@ class Context:
         return ms
 
     def sigma_noalloc(self, sb, psi_ptr, out_ptr):
-        """sigma on device buffers using only the library's fixed device
-        array for intermediates (no device allocation during the call)."""
+        """FP64 sigma on device buffers using only the library's fixed device
+        array for intermediates (no device allocation during the call),
+        whatever precision the context is set to."""
         self._check(self.lib.bgpu_sigma_noalloc(self.h, sb, _P(psi_ptr), _P(out_ptr)))
 
     def superblock_launches(self, sb):
@@ -269,7 +355,7 @@ class Context:
     INFO_KEYS = ("flops", "bytes", "tc_mma_flops", "tc_phase1_tasks", "tc_phase2_tasks", "tc_phase2_items",
                  "tc_phase2_stage1_items", "tc_split_tiles", "tc_pool_L", "tc_pool_R", "tc_pool_psi",
                  "tc_pool_S", "fp64_stage1_units", "fp64_items", "tc_item_cost", "tc_split", "tc_group",
-                 "tc_per_sector", "tc_tuned", "launches")
+                 "tc_per_sector", "tc_tuned", "launches", "fp64_scratch")
 
     def tc_wait_selftest(self, limit_ms=20.0):
         """Bounded mbarrier wait on a barrier nothing arrives at: returns

@@ -27,8 +27,10 @@ struct bgpu_ctx {
     Block b;
     std::vector<OpKey> decl;  // declaration order
     std::vector<int> orbsym;
+    std::string group = "c1";
   };
   std::map<int, std::unique_ptr<BlockRec>> blocks;
+  std::map<int, std::unique_ptr<Integrals>> integrals;
   struct SbRec {
     Superblock sb;
     SigmaPlan plan;
@@ -63,6 +65,28 @@ int guarded(bgpu_ctx* ctx, F&& f) {
 }
 void need(bool c, const char* what) {
   if (!c) throw std::invalid_argument(what);
+}
+void need(bool c, const std::string& what) {
+  if (!c) throw std::invalid_argument(what);
+}
+// operator keys (type, i, j, 2k) of a C-ABI catalogue, in declaration order
+std::set<OpKey> read_keys(int nops, const int* op_keys, int norb, std::vector<OpKey>& decl) {
+  std::set<OpKey> keys;
+  decl.clear();
+  for (int o = 0; o < nops; ++o) {
+    const int t = op_keys[4 * o], i = op_keys[4 * o + 1], j = op_keys[4 * o + 2], k2 = op_keys[4 * o + 3];
+    need(t >= 0 && t <= BGPU_OP_OVERLAP, "bad operator type");
+    need(i < norb && j < norb, "orbital index out of range");
+    need(k2 >= 0 && k2 <= 4, "bad tensor rank");
+    OpKey k;
+    k.type = (OpType)t;
+    k.i = (int16_t)i;
+    k.j = (int16_t)j;
+    k.k2 = (int8_t)k2;
+    need(keys.insert(k).second, "duplicate operator key");
+    decl.push_back(k);
+  }
+  return keys;
 }
 }  // namespace
 
@@ -173,7 +197,8 @@ int bgpu_block_define(bgpu_ctx* ctx, int norb, const int* orbsym, const char* gr
     need(nquanta > 0 && nops >= 0 && (nops == 0 || op_keys), "bad sizes");
     auto rec = std::make_unique<bgpu_ctx::BlockRec>();
     rec->orbsym.assign(orbsym, orbsym + norb);
-    PointGroup g = PointGroup::from_name(group ? group : "c1");
+    rec->group = group ? group : "c1";
+    PointGroup g = PointGroup::from_name(rec->group);
     for (int q = 0; q < nquanta; ++q) {
       Quantum Q{quanta[3 * q], quanta[3 * q + 1], quanta[3 * q + 2]};
       need(Q.s2 >= 0 && Q.irrep >= 0 && Q.irrep < g.nirrep, "bad quantum");
@@ -182,19 +207,7 @@ int bgpu_block_define(bgpu_ctx* ctx, int norb, const int* orbsym, const char* gr
       rec->b.si.quanta.push_back(Q);
       rec->b.si.states.push_back(states[q]);
     }
-    std::set<OpKey> keys;
-    for (int o = 0; o < nops; ++o) {
-      const int t = op_keys[4 * o], i = op_keys[4 * o + 1], j = op_keys[4 * o + 2], k2 = op_keys[4 * o + 3];
-      need(t >= 0 && t <= BGPU_OP_OVERLAP, "bad operator type");
-      need(i < norb && j < norb, "orbital index out of range");
-      OpKey k;
-      k.type = (OpType)t;
-      k.i = (int16_t)i;
-      k.j = (int16_t)j;
-      k.k2 = (int8_t)k2;
-      need(keys.insert(k).second, "duplicate operator key");
-      rec->decl.push_back(k);
-    }
+    std::set<OpKey> keys = read_keys(nops, op_keys, norb, rec->decl);
     rec->b.ops = make_opset(rec->b.si, keys, rec->orbsym, g);
     rec->b.is_dot = is_dot != 0;
     rec->b.sites.clear();
@@ -377,7 +390,7 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
     auto& r = *it->second;
     if (!r.plan.tc) ctx->eng->plan_tc(r.sb, r.plan);
     const SigmaPlan& p = r.plan;
-    const double v[20] = {p.flops,
+    const double v[21] = {p.flops,
                           p.bytes,
                           p.tc_mma_flops,
                           (double)p.tc_stats[0],
@@ -396,8 +409,9 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
                           (double)p.tc_knobs.group,
                           (double)p.tc_knobs.per_sector,
                           p.tc_tuned ? 1.0 : 0.0,
-                          (double)ctx->eng->sigma_launches(p)};
-    for (int i = 0; i < n; ++i) info[i] = i < 20 ? v[i] : 0.0;
+                          (double)ctx->eng->sigma_launches(p),
+                          (double)p.scratch_elems};
+    for (int i = 0; i < n; ++i) info[i] = i < 21 ? v[i] : 0.0;
   });
 }
 
@@ -530,6 +544,212 @@ int bgpu_tc_tile(bgpu_ctx* ctx, const uint16_t* a, const uint16_t* b, float* d, 
   });
 }
 
+int bgpu_integrals_load(bgpu_ctx* ctx, const char* conf_path, int* handle, int* norb) {
+  return guarded(ctx, [&] {
+    need(conf_path && handle, "null argument");
+    Config c = parse_config(conf_path);
+    auto I = std::make_unique<Integrals>(load_integrals(c));
+    if (norb) *norb = I->norb;
+    *handle = ctx->next++;
+    ctx->integrals[*handle] = std::move(I);
+  });
+}
+
+int bgpu_integrals_define(bgpu_ctx* ctx, int norb, const int* orbsym, const double* h1, const double* eri, double ecore,
+                          int* handle) {
+  return guarded(ctx, [&] {
+    need(norb > 0 && orbsym && h1 && eri && handle, "null argument");
+    auto I = std::make_unique<Integrals>();
+    I->resize(norb);
+    I->orbsym.assign(orbsym, orbsym + norb);
+    I->ecore = ecore;
+    std::copy(h1, h1 + (size_t)norb * norb, I->t.begin());
+    std::copy(eri, eri + (size_t)norb * norb * norb * norb, I->v.begin());
+    *handle = ctx->next++;
+    ctx->integrals[*handle] = std::move(I);
+  });
+}
+
+int bgpu_integrals_free(bgpu_ctx* ctx, int handle) {
+  return guarded(ctx, [&] { need(ctx->integrals.erase(handle) == 1, "bad integrals handle"); });
+}
+
+int bgpu_block_set_sites(bgpu_ctx* ctx, int handle, int nsites, const int* sites) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(handle);
+    need(it != ctx->blocks.end(), "bad block");
+    need(nsites > 0 && sites, "null argument");
+    const int norb = (int)it->second->orbsym.size();
+    for (int i = 0; i < nsites; ++i) need(sites[i] >= 0 && sites[i] < norb, "site out of range");
+    it->second->b.sites.assign(sites, sites + nsites);
+  });
+}
+
+int bgpu_block_quanta(bgpu_ctx* ctx, int handle, int* nquanta, int* quanta, int* states) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(handle);
+    need(it != ctx->blocks.end() && nquanta, "bad block");
+    const StateInfo& si = it->second->b.si;
+    const int cap = *nquanta;
+    *nquanta = si.size();
+    if (!quanta && !states) return;
+    need(cap >= si.size(), "quanta buffers smaller than the block's quanta");
+    for (int q = 0; q < si.size(); ++q) {
+      if (quanta) {
+        quanta[3 * q] = si.quanta[q].n;
+        quanta[3 * q + 1] = si.quanta[q].s2;
+        quanta[3 * q + 2] = si.quanta[q].irrep;
+      }
+      if (states) states[q] = si.states[q];
+    }
+  });
+}
+
+int bgpu_build_enlarged_ops(bgpu_ctx* ctx, int integrals, int left, int right, const int* filter, int nops,
+                            const int* op_keys, int* big, int64_t* arena_elems, int* nquanta) {
+  return guarded(ctx, [&] {
+    auto ii = ctx->integrals.find(integrals);
+    need(ii != ctx->integrals.end(), "bad integrals handle");
+    auto li = ctx->blocks.find(left), ri = ctx->blocks.find(right);
+    need(li != ctx->blocks.end() && ri != ctx->blocks.end(), "bad block handle");
+    need(big && arena_elems && (nops == 0 || op_keys), "null argument");
+    const Integrals& I = *ii->second;
+    const auto& A = *li->second;
+    const auto& B = *ri->second;
+    need(!A.b.sites.empty() && !B.b.sites.empty(), "sub-blocks need their sites (bgpu_block_set_sites)");
+    need(A.b.is_dot || B.b.is_dot, "one sub-block must be a single site (is_dot)");
+    need((int)A.orbsym.size() == I.norb && A.orbsym == B.orbsym, "orbital irreps of the blocks and integrals differ");
+    need(A.group == B.group, "point groups of the sub-blocks differ");
+    auto rec = std::make_unique<bgpu_ctx::BlockRec>();
+    rec->orbsym = A.orbsym;
+    rec->group = A.group;
+    PointGroup g = PointGroup::from_name(rec->group);
+    Block& nb = rec->b;
+    nb.sites = A.b.sites;
+    nb.sites.insert(nb.sites.end(), B.b.sites.begin(), B.b.sites.end());
+    QuantumFilter qf;
+    if (filter) {
+      qf.nelec = filter[0];
+      qf.s2 = filter[1];
+      qf.norb = filter[2];
+      need(qf.norb >= (int)nb.sites.size() && qf.nelec >= 0 && qf.s2 >= 0, "bad filter");
+    }
+    nb.si = product_stateinfo(A.b.si, B.b.si, g, filter ? &qf : nullptr, (int)nb.sites.size(), nullptr);
+    need(nb.si.size() > 0, "the product keeps no quantum");
+    std::set<OpKey> keys = read_keys(nops, op_keys, I.norb, rec->decl);
+    nb.ops = make_opset(nb.si, keys, rec->orbsym, g);
+    std::vector<std::pair<OpKey, std::vector<BuildTerm>>> recipes;
+    for (const auto& kv : nb.ops.ops) {
+      recipes.push_back({kv.first, build_terms(kv.first, A.b.sites, B.b.sites, I)});
+      for (const auto& t : recipes.back().second) {
+        need(t.a.identity || A.b.ops.has(t.a.key),
+             "build of " + kv.first.str() + " needs " + t.a.key.str() + " on the left sub-block");
+        need(t.b.identity || B.b.ops.has(t.b.key),
+             "build of " + kv.first.str() + " needs " + t.b.key.str() + " on the right sub-block");
+      }
+    }
+    ctx->eng->create_block(nb);
+    ctx->eng->build_block(nb, A.b, B.b, recipes);
+    ctx->eng->sync();
+    *arena_elems = nb.ops.arena;
+    if (nquanta) *nquanta = nb.si.size();
+    *big = ctx->next++;
+    ctx->blocks[*big] = std::move(rec);
+  });
+}
+
+int bgpu_set_wavefunctions(bgpu_ctx* ctx, int sb, int nroots, const double* vectors) {
+  return guarded(ctx, [&] {
+    auto it = ctx->sbs.find(sb);
+    need(it != ctx->sbs.end() && vectors && nroots > 0, "bad arguments");
+    ctx->eng->set_waves(nroots, it->second->sb.size, vectors);
+  });
+}
+
+int bgpu_density_download(bgpu_ctx* ctx, double* rho, double* vecs, int64_t n) {
+  return guarded(ctx, [&] {
+    need(rho || vecs, "null argument");
+    std::vector<double> r, v;
+    ctx->eng->density_download(r, v);
+    need(n == (int64_t)r.size(), "buffer size must be the sum of the squared sector sizes (" +
+                                     std::to_string(r.size()) + ")");
+    if (rho) std::copy(r.begin(), r.end(), rho);
+    if (vecs) std::copy(v.begin(), v.end(), vecs);
+  });
+}
+
+int bgpu_renormalise(bgpu_ctx* ctx, int big, const int* kept, const double* rotations, int nops, const int* op_keys,
+                     int* small, int64_t* arena_elems, int* nquanta) {
+  return guarded(ctx, [&] {
+    auto bi = ctx->blocks.find(big);
+    need(bi != ctx->blocks.end(), "bad block handle");
+    need(kept && small && arena_elems && (nops == 0 || op_keys), "null argument");
+    const auto& B = *bi->second;
+    const StateInfo& si = B.b.si;
+    const int nq = si.size();
+    std::vector<int> k(kept, kept + nq);
+    int64_t total = 0;
+    for (int q = 0; q < nq; ++q) {
+      need(k[q] >= 0 && k[q] <= si.states[q], "kept states out of range");
+      total += k[q];
+    }
+    need(total > 0, "no state kept");
+    if (rotations) {
+      std::vector<std::vector<double>> rot(nq);
+      int64_t o = 0;
+      for (int q = 0; q < nq; ++q) {
+        const int64_t sz = (int64_t)si.states[q] * k[q];
+        rot[q].assign(rotations + o, rotations + o + sz);
+        o += sz;
+      }
+      ctx->eng->set_rotation(rot, k);
+    } else {
+      need(ctx->eng->density_dims() == si.states,
+           "no density matrix of this block: call bgpu_density_eig first or pass rotations");
+      std::vector<std::vector<int>> idx(nq);
+      for (int q = 0; q < nq; ++q)
+        for (int c = 0; c < k[q]; ++c) idx[q].push_back(si.states[q] - 1 - c);  // descending eigenvalues
+      ctx->eng->select_rotation(idx);
+    }
+    auto rec = std::make_unique<bgpu_ctx::BlockRec>();
+    rec->orbsym = B.orbsym;
+    rec->group = B.group;
+    PointGroup g = PointGroup::from_name(rec->group);
+    Block& nb = rec->b;
+    nb.sites = B.b.sites;
+    std::vector<int> map;
+    nb.si = truncated_stateinfo(si, k, map);
+    std::set<OpKey> keys = read_keys(nops, op_keys, (int)rec->orbsym.size(), rec->decl);
+    for (const OpKey& key : keys) need(B.b.ops.has(key), "the enlarged block has no operator " + key.str());
+    nb.ops = make_opset(nb.si, keys, rec->orbsym, g);
+    ctx->eng->create_block(nb);
+    ctx->eng->renormalise(nb, B.b);
+    ctx->eng->sync();
+    *arena_elems = nb.ops.arena;
+    if (nquanta) *nquanta = nb.si.size();
+    *small = ctx->next++;
+    ctx->blocks[*small] = std::move(rec);
+  });
+}
+
+int bgpu_rotation_download(bgpu_ctx* ctx, int small, double* rot, int64_t n) {
+  return guarded(ctx, [&] {
+    auto it = ctx->blocks.find(small);
+    need(it != ctx->blocks.end() && rot, "bad arguments");
+    RotationRecord r;
+    need(ctx->eng->get_rotation_record(it->second->b, r), "the block was not made by bgpu_renormalise");
+    int64_t tot = 0;
+    for (size_t q = 0; q < r.off.size(); ++q) tot += (int64_t)r.n[q] * r.m[q];
+    need(n == tot, "buffer size must be the sum of rows x kept over the sectors (" + std::to_string(tot) + ")");
+    int64_t o = 0;
+    for (size_t q = 0; q < r.off.size(); ++q) {
+      const int64_t sz = (int64_t)r.n[q] * r.m[q];
+      std::copy(r.data.begin() + r.off[q], r.data.begin() + r.off[q] + sz, rot + o);
+      o += sz;
+    }
+  });
+}
+
 int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition, int* sbh, int64_t* psi_elems) {
   return guarded(ctx, [&] {
     need(conf_path && sbh && psi_elems, "null argument");
@@ -644,17 +864,8 @@ extern "C" int bgpu_sigma_noalloc(bgpu_ctx* ctx, int sb, const double* psi, doub
                                   "; use bgpu_sigma_device");
     double* scratch = nullptr;
     cuda_check(noalloc_scratch(ctx->device, &scratch), "noalloc scratch address");
-    const Superblock& s = it->second->sb;
-    dev::Bufs bufs{};
-    bufs.p[0] = ctx->eng->arena(*s.L);
-    bufs.p[1] = ctx->eng->arena(*s.R);
-    bufs.p[2] = const_cast<double*>(psi);
-    bufs.p[3] = sigma;
-    bufs.p[4] = scratch;
-    cudaStream_t st = ctx->eng->stream();
-    cuda_check(dev::launch_gemm(bufs, plan.u1.d, plan.i1.d, plan.t1.d, (int)plan.t1.n, st), "sigma stage 1");
-    cuda_check(dev::launch_gemm(bufs, plan.u2.d, plan.i2.d, plan.t2.d, (int)plan.t2.n, st), "sigma stage 2");
-    cuda_check(dev::launch_copy(bufs, sigma, plan.ru.d, plan.ri.d, (int)plan.ru.n, st), "sigma stage-2 partial sums");
-    if (plan.ecore != 0.0) cuda_check(dev::launch_axpy(plan.ecore, psi, sigma, plan.n, st), "ecore");
+    // always the FP64 plan, whatever bgpu_set_precision chose: the split
+    // paths keep packed operand pools that are allocated on first use
+    ctx->eng->sigma_fp64(it->second->sb, plan, psi, sigma, scratch);
   });
 }

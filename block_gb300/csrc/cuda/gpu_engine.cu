@@ -165,6 +165,7 @@ GpuEngine::~GpuEngine() {
     if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
   if (waves_) cudaFreeAsync(waves_, stream_);
   if (dm_vecs_) cudaFreeAsync(dm_vecs_, stream_);
+  if (dm_rho_) cudaFreeAsync(dm_rho_, stream_);
   if (rot_) cudaFreeAsync(rot_, stream_);
   for (auto& kv : block_rot_)
     if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
@@ -888,12 +889,17 @@ void GpuEngine::free_plan(SigmaPlan& p) {
 
 void GpuEngine::sigma(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out) {
   if (!p.scratch) p.scratch = alloc(p.scratch_elems);
+  sigma_fp64(sb, p, psi, out, p.scratch);
+}
+
+void GpuEngine::sigma_fp64(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out,
+                           double* scratch) {
   dev::Bufs bufs{};
   bufs.p[0] = arena(*sb.L);
   bufs.p[1] = arena(*sb.R);
   bufs.p[2] = const_cast<double*>(psi);
   bufs.p[3] = out;
-  bufs.p[4] = p.scratch;
+  bufs.p[4] = scratch;
   cuda_check(dev::launch_gemm(bufs, p.u1.d, p.i1.d, p.t1.d, (int)p.t1.n, stream_), "sigma stage 1");
   cuda_check(dev::launch_gemm(bufs, p.u2.d, p.i2.d, p.t2.d, (int)p.t2.n, stream_), "sigma stage 2");
   cuda_check(dev::launch_copy(bufs, out, p.ru.d, p.ri.d, (int)p.ru.n, stream_), "sigma stage-2 partial sums");
@@ -2462,7 +2468,10 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
     tot += (int64_t)B.si.states[q] * B.si.states[q];
     maxn = std::max(maxn, B.si.states[q]);
   }
-  double* rho = alloc(tot);
+  // the matrix is kept (until the next density) for density_download
+  if (dm_rho_) free(dm_rho_);
+  dm_rho_ = alloc(tot);
+  double* rho = dm_rho_;
   cuda_check(cudaMemsetAsync(rho, 0, std::max<int64_t>(tot, 1) * sizeof(double), stream_), "memset");
   // rho(q) = sum_r w_r sum_sectors psi psi^T (or psi^T psi for the right block)
   std::vector<dev::GemmUnit> units;
@@ -2543,9 +2552,13 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   dwoff.upload(woff, stream_);
   ddims.upload(small_dims, stream_);
   dstat.upload(std::vector<int>(nq, 0), stream_);
-  if (small_max > 0)
-    cuda_check(dev::launch_jacobi(rho, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, small_max, stream_),
+  double* jac = nullptr;  // the Jacobi sweeps overwrite their matrices: a copy of rho
+  if (small_max > 0) {
+    jac = alloc(tot);
+    cuda_check(cudaMemcpyAsync(jac, rho, tot * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy rho");
+    cuda_check(dev::launch_jacobi(jac, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, small_max, stream_),
                "density eig");
+  }
   if (!large.empty()) {
     ensure_lanes();
     if ((int)large.size() > solver_ninfo_) {
@@ -2619,8 +2632,37 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   dwoff.release(stream_);
   ddims.release(stream_);
   dstat.release(stream_);
-  free(rho);
   free(w);
+  if (jac) free(jac);
+  sync();
+}
+
+void GpuEngine::density_download(std::vector<double>& rho, std::vector<double>& vecs) {
+  if (!dm_rho_ || !dm_vecs_) throw std::invalid_argument("no density matrix has been formed");
+  int64_t tot = 0;
+  for (int n : dm_dims_) tot += (int64_t)n * n;
+  rho.resize(tot);
+  vecs.resize(tot);
+  cuda_check(cudaMemcpyAsync(rho.data(), dm_rho_, tot * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h rho");
+  cuda_check(cudaMemcpyAsync(vecs.data(), dm_vecs_, tot * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h vecs");
+  sync();
+  // every sector row-major with the eigenvectors as columns
+  for (size_t q = 0; q < dm_dims_.size(); ++q) {
+    if (q >= dm_colmajor_.size() || !dm_colmajor_[q]) continue;
+    const int n = dm_dims_[q];
+    double* v = vecs.data() + dm_off_[q];
+    for (int i = 0; i < n; ++i)
+      for (int j = i + 1; j < n; ++j) std::swap(v[(int64_t)i * n + j], v[(int64_t)j * n + i]);
+  }
+}
+
+void GpuEngine::set_waves(int nroots, int64_t n, const double* host) {
+  if (nroots < 1 || n < 1) throw std::invalid_argument("set_waves: empty");
+  if (waves_) free(waves_);
+  waves_ = alloc((int64_t)nroots * n);
+  cuda_check(stage_h2d(waves_, host, (size_t)nroots * n * sizeof(double), stream_), "h2d waves");
+  wave_n_ = n;
+  nwaves_ = nroots;
   sync();
 }
 

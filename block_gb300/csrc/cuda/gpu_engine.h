@@ -159,6 +159,9 @@ class GpuEngine : public Engine {
   void free_tc(SigmaPlan& plan);  // tensor-core lists and pools only
   // device pointers, stream-ordered on stream()
   void sigma(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d);
+  // the FP64 product's launches with the stage-1 intermediates in `scratch`
+  // (plan.scratch_elems doubles), whoever owns it; counts the product
+  void sigma_fp64(const Superblock& sb, const SigmaPlan& plan, const double* psi_d, double* out_d, double* scratch);
   // split-precision product with `ns` bf16 slices (2 or 3)
   void sigma_split(const Superblock& sb, SigmaPlan& plan, int ns, const double* psi_d, double* out_d,
                    cudaEvent_t* marks = nullptr);
@@ -198,6 +201,14 @@ class GpuEngine : public Engine {
   void sync();
   // last Davidson wavefunctions (device, nroots x n)
   const double* waves() const { return waves_; }
+  // replaces them with caller vectors (host, nroots x n), e.g. for density()
+  void set_waves(int nroots, int64_t n, const double* host);
+  // the last density matrix, per sector row-major, and its eigenvectors
+  // (per sector row-major, column c = eigenvector of the c-th smallest
+  // eigenvalue); sectors back to back in quantum order
+  void density_download(std::vector<double>& rho, std::vector<double>& vecs);
+  // sector sizes of the last density matrix
+  const std::vector<int>& density_dims() const { return dm_dims_; }
   int64_t wave_size() const { return wave_n_; }
   Precision precision = Precision::FP64;
   double sigma_seconds = 0.0;
@@ -241,6 +252,7 @@ class GpuEngine : public Engine {
   int nwaves_ = 0;
   // density / rotation state
   double* dm_vecs_ = nullptr;
+  double* dm_rho_ = nullptr;
   std::vector<int64_t> dm_off_;
   std::vector<int> dm_dims_;
   std::vector<char> dm_colmajor_;  // sector eigenvectors stored column-major (dense solver)

@@ -142,6 +142,44 @@ int bgpu_block_upload(bgpu_ctx* ctx, int handle, const double* arena, int64_t n)
 int bgpu_block_download(bgpu_ctx* ctx, int handle, double* arena, int64_t n);
 int bgpu_block_free(bgpu_ctx* ctx, int handle);
 
+/* Orbitals of a block, in order (SpinBlock::sites, spinblock.h:104-259);
+ * the enlarged-block build needs them for its integral-weighted terms. */
+int bgpu_block_set_sites(bgpu_ctx* ctx, int handle, int nsites, const int* sites);
+/* State space of a block (StateInfo::quanta / quantaStates, StateInfo.h:79-206):
+ * *nquanta is the capacity of quanta[3*cap] / states[cap] on entry (both may
+ * be NULL to query the count) and the block's number of quanta on return. */
+int bgpu_block_quanta(bgpu_ctx* ctx, int handle, int* nquanta, int* quanta, int* states);
+
+/*
+ * Hamiltonian integrals read by the operator builds (Input::readorbitalsfile,
+ * input.C:1407-1681; the integral-weighted sums of the complementary
+ * operators, Operators.C:87-137, 1059-1194).  _load takes the `orbitals` of
+ * a dmrg.conf (an FCIDUMP, or synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>)
+ * reordered as the configuration asks and returns norb; _define takes
+ * h1[norb*norb] row-major and the chemist-notation eri[norb^4] with (ij|kl)
+ * at ((i*norb+j)*norb+k)*norb+l, both in the block orbitals' order.
+ */
+int bgpu_integrals_load(bgpu_ctx* ctx, const char* conf_path, int* handle, int* norb);
+int bgpu_integrals_define(bgpu_ctx* ctx, int norb, const int* orbsym, const double* h1, const double* eri, double ecore,
+                          int* handle);
+int bgpu_integrals_free(bgpu_ctx* ctx, int handle);
+
+/*
+ * Enlarged block left (x) right built on the GPU, one of the two a single
+ * site (is_dot): SpinBlock::BuildSumBlock (spinblock.C:194-260) with every
+ * operator made by TensorProduct (operatorfunctions.h:34,
+ * operatorfunctions.C:146-254) as Op::build does it (Operators.C:453-2395).
+ * Both sub-blocks must be defined with their sites and uploaded.
+ *   filter[3] = (nelec, 2S, norb) of the whole system: quanta the remaining
+ *     orbitals cannot complete to that target are dropped
+ *     (PARTICLE_SPIN_NUMBER_CONSTRAINT, StateInfo.C:123-308); NULL keeps all
+ *   op_keys[4*nops]: catalogue of the enlarged block (type, i, j, 2k)
+ * Returns the new block, the doubles of its arena and its number of quanta
+ * (read them with bgpu_block_quanta; download with bgpu_block_download).
+ */
+int bgpu_build_enlarged_ops(bgpu_ctx* ctx, int integrals, int left, int right, const int* filter, int nops,
+                            const int* op_keys, int* big, int64_t* arena_elems, int* nquanta);
+
 /*
  * Superblock L|R with its operator-pair list; compiles the sigma work lists.
  * Replaces the set-up of SpinBlock::multiplyH (spinblock.C:722-789) and the
@@ -172,9 +210,10 @@ int bgpu_tc_wait_selftest(bgpu_ctx* ctx, double limit_ms, int* gave_up, int* sta
  *   tasks, phase-2 items, phase-2 items reading a stage-1 product, split
  *   tiles, packed elements of the L-operator / R-operator / psi / stage-1
  *   pools, FP64 stage-1 units, FP64 items, the schedule knobs (item cost,
- *   split, group, per-sector flag, 1 when chosen by the autotuner) and the
- *   launches of one sigma at the current precision.  Builds the tensor-core
- *   plan if needed. */
+ *   split, group, per-sector flag, 1 when chosen by the autotuner), the
+ *   launches of one sigma at the current precision and the doubles of
+ *   stage-1 intermediates the FP64 product needs (compare with
+ *   BGPU_NOALLOC_SCRATCH_DOUBLES).  Builds the tensor-core plan if needed. */
 int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n);
 /* Kernel launches of one sigma product. */
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);
@@ -212,7 +251,11 @@ int bgpu_sigma_timed(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma
  * address and should therefore come before any stream capture.  All calls
  * share the array: calls whose work overlaps on the GPU (other streams,
  * other contexts on the same device) race and must be serialised by the
- * caller.  Stream-ordered and asynchronous like bgpu_sigma_device.
+ * caller.  Stream-ordered and asynchronous like bgpu_sigma_device.  The
+ * product is always the FP64 one, whatever bgpu_set_precision chose: the
+ * split-precision paths need packed operand pools that the library
+ * allocates on first use, so they are not available here.  Counted in the
+ * context's sigma statistics like every other product.
  */
 #define BGPU_NOALLOC_SCRATCH_DOUBLES (4 * 1024 * 1024)
 int bgpu_sigma_noalloc(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev);
@@ -234,6 +277,42 @@ int bgpu_davidson(bgpu_ctx* ctx, int sb, int nroots, double tol, int max_iter, d
  */
 int bgpu_density_eig(bgpu_ctx* ctx, int sb, int left, int nroots, const double* weights, double* eigvals,
                      int64_t n_eigvals);
+
+/*
+ * Wavefunctions the next bgpu_density_eig reads (host, nroots x psi_elems in
+ * the superblock's sector order), in place of the last Davidson vectors:
+ * the `wave_solutions` argument of DensityMatrix::makedensitymatrix
+ * (density.C:27-90).
+ */
+int bgpu_set_wavefunctions(bgpu_ctx* ctx, int sb, int nroots, const double* vectors);
+/*
+ * The last density matrix and its eigenvectors (the matrices diagonalise_dm
+ * fills, rotationmat.C:258-279): per sector of the block, back to back in
+ * quantum order, rho row-major and the eigenvectors row-major with column c
+ * the eigenvector of the c-th smallest eigenvalue.  n = sum of the squared
+ * sector sizes; either pointer may be NULL.
+ */
+int bgpu_density_download(bgpu_ctx* ctx, double* rho, double* vecs, int64_t n);
+/*
+ * Renormalised block small = U^T big U for every operator of its catalogue
+ * (SpinBlock::transform_operators, spinblock.h:253, save_load_block.C:267-319;
+ * SparseMatrix::renormalise_transform, BaseOperator.h:199-204 /
+ * BaseOperator.C:341-363; MatrixRotate, MatrixBLAS.C:553-572).
+ *   kept[nquanta of big]: states kept per quantum (0 drops the quantum)
+ *   rotations: per quantum with kept > 0, states x kept row-major, back to
+ *     back in quantum order (the rotation matrices of makeRotateMatrix,
+ *     renormalise.C:135-166); NULL takes, per quantum, the eigenvectors of
+ *     the kept[q] largest eigenvalues of the last bgpu_density_eig of this
+ *     block, in descending order, without leaving the GPU
+ *   op_keys[4*nops]: catalogue of the renormalised block (each present in big)
+ * Returns the new block, the doubles of its arena and its number of quanta.
+ */
+int bgpu_renormalise(bgpu_ctx* ctx, int big, const int* kept, const double* rotations, int nops, const int* op_keys,
+                     int* small, int64_t* arena_elems, int* nquanta);
+/* The rotation that made a block returned by bgpu_renormalise, in the layout
+ * of its `rotations` argument (n doubles): the rotation matrices a Block
+ * caller stores for its later steps (rotationmat.C:21-60). */
+int bgpu_rotation_download(bgpu_ctx* ctx, int small, double* rot, int64_t n);
 
 /*
  * Device-memory accounting: pointer to a device buffer of `n` doubles owned

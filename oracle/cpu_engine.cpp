@@ -451,6 +451,7 @@ void CpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
         dgemm(true, false, S.cols, S.cols, S.rows, w, psi, S.cols, psi, S.cols, 1.0, rho[S.rq].data(), S.cols);
     }
   }
+  dm_rho_ = rho;  // kept for the element-wise parity tests
   spec.eig.assign(nq, {});
   dm_vecs_.assign(nq, {});
   dm_dims_.assign(nq, 0);

@@ -49,6 +49,13 @@ class CpuEngine : public Engine {
   std::vector<double>& arena(Block& b) { return store_.at(b.handle); }
   const std::vector<std::vector<double>>& wavefunctions() const { return waves_; }
   void set_wavefunctions(const std::vector<std::vector<double>>& w) { waves_ = w; }
+  // the last density matrix per sector (row-major), its eigenvectors (row-major,
+  // columns in ascending eigenvalue order) and the current rotation (per big
+  // sector, rows x kept row-major)
+  const std::vector<std::vector<double>>& density_matrices() const { return dm_rho_; }
+  const std::vector<std::vector<double>>& density_vectors() const { return dm_vecs_; }
+  const std::vector<std::vector<double>>& rotation() const { return rot_; }
+  const std::vector<int>& rotation_kept() const { return rot_kept_; }
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
   double last_sigma_flops = 0.0;  // GEMM flops of the last sigma (2mnk per product)
@@ -59,6 +66,7 @@ class CpuEngine : public Engine {
   int next_handle_ = 0;
   std::vector<std::vector<double>> waves_;
   std::vector<std::vector<double>> dm_vecs_;  // eigenvectors per density-matrix sector (columns, ascending)
+  std::vector<std::vector<double>> dm_rho_;   // the density matrix per sector
   std::vector<int> dm_dims_;
   std::vector<std::vector<double>> rot_;       // per big sector: rows x kept
   std::vector<int> rot_kept_;

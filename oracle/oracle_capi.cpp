@@ -3,12 +3,15 @@
 // a chosen step and exposes that step's superblock (blocks, operator-pair
 // list, wavefunction and the oracle's sigma) so the CUDA library can be fed
 // the same inputs through its C ABI.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <dlfcn.h>
+#include <map>
 #include <memory>
 #include <random>
+#include <string>
 
 #include "cpu_engine.h"
 
@@ -351,4 +354,153 @@ void* oracle_prepare(const char* conf, int partition, int threads, int reps, int
     return nullptr;
   }
 }
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Block-level case for the element-wise parity tests of the enlarged-block
+// build, the density matrix and the renormalisation: at `partition` of a
+// configuration's warm-up chain, the system block [0..p-1], the dot p, the
+// enlarged block [0..p] built by the oracle (sigma and renormalisation
+// catalogues merged, as a forward sweep step builds it), a seeded random
+// wavefunction on the superblock [0..p] | [p+1..N-1], its left density
+// matrix with eigenvectors, the rotation keeping the M largest weights
+// (the truncation rule of the sweep) and the renormalised block U^T O U.
+// ---------------------------------------------------------------------------
+namespace {
+struct BlockCase {
+  std::map<std::string, std::vector<int>> ints;
+  std::map<std::string, std::vector<double>> reals;
+  std::string group;
+};
+
+void put_block(BlockCase& c, const std::string& name, const Block& b, oracle::CpuEngine& e, bool with_arena) {
+  SnapBlock s = snap_block(b, e);
+  c.ints[name + "_quanta"] = s.quanta;
+  c.ints[name + "_states"] = s.states;
+  c.ints[name + "_keys"] = s.keys;
+  c.ints[name + "_sites"] = b.sites;
+  if (with_arena) c.reals[name + "_arena"] = s.arena;
+}
+}  // namespace
+
+extern "C" {
+void* oracle_block_case(const char* conf, int partition, int threads) {
+  auto bc = std::make_unique<BlockCase>();
+  try {
+    Config c = parse_config(conf);
+    Integrals I = load_integrals(c);
+    oracle::CpuEngine eng(threads);
+    bc->group = c.sym;
+    SweepDriver drv(I, c, eng);
+    const int N = I.norb, p = partition;
+    Block L0, R0;
+    Superblock sb0 = drv.prepare_partition(p, L0, R0);  // warm-up chain and the environment block
+    (void)sb0;
+    std::vector<int> Ls, Rs;
+    for (int i = 0; i <= p; ++i) Ls.push_back(i);
+    for (int i = p + 1; i < N; ++i) Rs.push_back(i);
+    const bool loopL = drv.loop_is_left(p);
+    CatalogSpec specL = drv.sigma_spec(Ls, Rs, loopL, loopL ? Ls : Rs);
+    CatalogSpec keep = drv.renorm_spec(Ls, p + 1, drv.loop_is_left(p + 1));
+    drv.merge(specL, keep);
+    Block& sys = drv.left_block(p - 1);
+    Block big = drv.make_enlarged(sys, p, /*dot_on_right=*/true, specL);
+    PointGroup g = PointGroup::from_name(c.sym);
+    DotOps dot = make_dot(p, I, g);
+    Block dotb;
+    dotb.sites = {p};
+    dotb.si = dot.si;
+    dotb.ops = dot.set;
+    dotb.is_dot = true;
+    eng.create_block(dotb);
+    eng.upload_block(dotb, dot.data);
+    put_block(*bc, "sys", sys, eng, true);
+    put_block(*bc, "dot", dotb, eng, true);
+    put_block(*bc, "big", big, eng, true);
+    put_block(*bc, "env", R0, eng, false);
+    bc->ints["orbsym"] = I.orbsym;
+    int nel = c.nelec >= 0 ? c.nelec : I.nelec;
+    bc->ints["filter"] = {nel, c.spin, N};
+    Superblock sb = drv.make_superblock(big, R0);
+    bc->ints["target"] = {sb.target.n, sb.target.s2, sb.target.irrep};
+    Rng rng(c.seed + 424242);
+    std::vector<double> psi(sb.size);
+    double nrm = 0.0;
+    for (auto& x : psi) {
+      x = rng.normal();
+      nrm += x * x;
+    }
+    for (auto& x : psi) x /= std::sqrt(nrm);
+    bc->reals["psi"] = psi;
+    eng.set_wavefunctions({psi});
+    DensitySpectrum spec;
+    eng.density(sb, /*left=*/true, {1.0}, spec);
+    std::vector<double> rho, vecs, eig;
+    for (const auto& m : eng.density_matrices()) rho.insert(rho.end(), m.begin(), m.end());
+    for (const auto& m : eng.density_vectors()) vecs.insert(vecs.end(), m.begin(), m.end());
+    for (const auto& v : spec.eig) eig.insert(eig.end(), v.begin(), v.end());
+    bc->reals["rho"] = rho;
+    bc->reals["vecs"] = vecs;
+    bc->reals["eig"] = eig;
+    // the M largest weights above 1e-13, eigenvectors of a sector in descending order
+    struct W { double w; int q, i; };
+    std::vector<W> all;
+    for (int q = 0; q < (int)spec.eig.size(); ++q)
+      for (int i = 0; i < (int)spec.eig[q].size(); ++i) all.push_back({spec.eig[q][i], q, i});
+    std::stable_sort(all.begin(), all.end(), [](const W& a, const W& b) { return a.w > b.w; });
+    const int M = c.schedule.empty() ? 100 : c.schedule.front().M;
+    std::vector<std::vector<int>> kept_idx(spec.eig.size());
+    for (int t = 0; t < std::min<int>(M, (int)all.size()); ++t)
+      if (all[t].w > 1e-13) kept_idx[all[t].q].push_back(all[t].i);
+    std::vector<int> kept(spec.eig.size());
+    for (size_t q = 0; q < kept_idx.size(); ++q) {
+      std::sort(kept_idx[q].begin(), kept_idx[q].end(), std::greater<int>());
+      kept[q] = (int)kept_idx[q].size();
+    }
+    eng.select_rotation(kept_idx);
+    std::vector<double> rot;
+    for (const auto& m : eng.rotation()) rot.insert(rot.end(), m.begin(), m.end());
+    bc->ints["kept"] = kept;
+    bc->reals["rot"] = rot;
+    std::vector<int> map;
+    Block small;
+    small.sites = big.sites;
+    small.si = truncated_stateinfo(big.si, kept, map);
+    small.ops = make_opset(small.si, catalog_keys(keep), I.orbsym, g);
+    eng.create_block(small);
+    eng.renormalise(small, big);
+    put_block(*bc, "small", small, eng, true);
+    for (Block* b : {&big, &dotb, &small, &L0, &R0}) eng.release_block(*b);
+    return bc.release();
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_block_case: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+void oracle_case_free(void* h) { delete static_cast<BlockCase*>(h); }
+
+// length of a named array (-1 if absent); kind 0 = int, 1 = double
+int64_t oracle_case_len(void* h, const char* name, int kind) {
+  auto* c = static_cast<BlockCase*>(h);
+  if (kind == 0) {
+    auto it = c->ints.find(name);
+    return it == c->ints.end() ? -1 : (int64_t)it->second.size();
+  }
+  auto it = c->reals.find(name);
+  return it == c->reals.end() ? -1 : (int64_t)it->second.size();
+}
+
+void oracle_case_get(void* h, const char* name, int kind, void* out) {
+  auto* c = static_cast<BlockCase*>(h);
+  if (kind == 0) {
+    const auto& v = c->ints.at(name);
+    std::memcpy(out, v.data(), v.size() * sizeof(int));
+  } else {
+    const auto& v = c->reals.at(name);
+    std::memcpy(out, v.data(), v.size() * sizeof(double));
+  }
+}
+
+const char* oracle_case_group(void* h) { return static_cast<BlockCase*>(h)->group.c_str(); }
 }  // extern "C"

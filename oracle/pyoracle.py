@@ -189,3 +189,43 @@ def prepare(conf, partition, threads=0, reps=1, time_single=False):
 
 def time_sigma(conf, sweep, pos, threads=0, reps=3):
     return lib().oracle_time_sigma(conf.encode(), sweep, pos, threads, reps)
+
+
+def block_case(conf, partition, threads=0):
+    """Element-wise parity case at `partition` of a configuration's warm-up
+    chain (see oracle_block_case): system, dot, enlarged and renormalised
+    blocks (quanta, states, keys, sites, arenas), the environment block's
+    state space, a random wavefunction, its left density matrix with
+    eigenvalues and eigenvectors, and the kept rotation."""
+    L = lib()
+    L.oracle_block_case.restype = ctypes.c_void_p
+    L.oracle_block_case.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    L.oracle_case_len.restype = ctypes.c_int64
+    L.oracle_case_len.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+    L.oracle_case_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p]
+    L.oracle_case_free.argtypes = [ctypes.c_void_p]
+    L.oracle_case_group.restype = ctypes.c_char_p
+    L.oracle_case_group.argtypes = [ctypes.c_void_p]
+    h = L.oracle_block_case(conf.encode(), partition, threads)
+    if not h:
+        raise RuntimeError("oracle block case failed")
+    out = {"group": L.oracle_case_group(h).decode()}
+    names_i = ["orbsym", "filter", "target", "kept"]
+    names_d = ["psi", "rho", "vecs", "eig", "rot"]
+    for b in ("sys", "dot", "big", "env", "small"):
+        names_i += [b + "_quanta", b + "_states", b + "_keys", b + "_sites"]
+        names_d += [b + "_arena"]
+    for kind, names, dt in ((0, names_i, np.int32), (1, names_d, np.float64)):
+        for nm in names:
+            n = L.oracle_case_len(h, nm.encode(), kind)
+            if n < 0:
+                continue
+            a = np.zeros(n, dtype=dt)
+            if n:
+                L.oracle_case_get(h, nm.encode(), kind, a.ctypes.data)
+            out[nm] = a
+    L.oracle_case_free(h)
+    for b in ("sys", "dot", "big", "env", "small"):
+        out[b + "_quanta"] = out[b + "_quanta"].reshape(-1, 3)
+        out[b + "_keys"] = out[b + "_keys"].reshape(-1, 4)
+    return out

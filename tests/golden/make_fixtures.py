@@ -4,8 +4,9 @@ Copies the FCIDUMP inputs of the reference's energy tests (data files only)
 and records the expected energies its test scripts check:
   dmrg_tests/runtest:12,23,30 (test_energy.py tolerance 1e-6) and
   pydmrg/tests/test_dmrg_simple.py:34 (10 decimal places).
-Run where the reference tree is available (path as the first argument);
-the tests read only the committed copies.
+Run where the reference tree is available, with its path as the required
+argument (python make_fixtures.py <reference tree>); the tests read only
+the committed copies.
 """
 import hashlib
 import json
@@ -13,7 +14,6 @@ import os
 import shutil
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 CASES = {
@@ -36,12 +36,15 @@ CASES = {
 }
 
 
-def main():
+def main(argv):
+    if len(argv) != 2:
+        sys.exit("usage: python make_fixtures.py <path of the reference source tree>")
+    ref = argv[1]
     meta = {}
     for name, (src, conf, energies, cite) in CASES.items():
         d = os.path.join(HERE, name)
         os.makedirs(d, exist_ok=True)
-        shutil.copyfile(os.path.join(REF, src), os.path.join(d, "FCIDUMP"))
+        shutil.copyfile(os.path.join(ref, src), os.path.join(d, "FCIDUMP"))
         with open(os.path.join(d, "dmrg.conf"), "w") as f:
             f.write(conf + "orbitals FCIDUMP\n")
         with open(os.path.join(d, "FCIDUMP"), "rb") as f:
@@ -52,4 +55,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv)

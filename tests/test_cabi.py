@@ -80,3 +80,12 @@ def test_plain_c_caller_builds_and_links(tmp_path):
                     "-lblockgb300", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
     assert "sm_103a" in out
+
+
+def test_noalloc_limit_matches_header():
+    import block_gb300
+
+    with open(os.path.join(ROOT, "include", "bgpu.h")) as f:
+        m = re.search(r"#define\s+BGPU_NOALLOC_SCRATCH_DOUBLES\s+\((\d+)\s*\*\s*(\d+)\s*\*\s*(\d+)\)", f.read())
+    assert m, "BGPU_NOALLOC_SCRATCH_DOUBLES not found"
+    assert int(m.group(1)) * int(m.group(2)) * int(m.group(3)) == block_gb300.NOALLOC_SCRATCH_DOUBLES

@@ -3,9 +3,9 @@ superblock (synthetic 24-orbital Hamiltonian, M=500, middle bond; psi of
 255 195 elements), where no oracle product is cheap enough for a test:
 Hermiticity <phi|H psi> = <psi|H phi> and linearity
 H(a psi + b phi) = a H psi + b H phi, to 1e-11 (relative to |phi| |H psi|
-and |H(a psi + b phi)|) in FP64 and to 1e-4 in the split precision, whose
+and |H(a psi + b phi)|) in FP64 and to 2e-5 in the split precision, whose
 products carry a relative error of a few 1e-6; the split product matches the
-FP64 one to 1e-4."""
+FP64 one to 2e-5."""
 import numpy as np
 import pytest
 
@@ -35,7 +35,7 @@ def products(ctx, sb, n, prec):
     return psi, phi, a, b, hp, hf, hl
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-11), ("bf16x3tc", 1e-4)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-11), ("bf16x3tc", 2e-5)])
 def test_hermitian_and_linear(gpu_ctx, big, prec, tol):
     sb, n = big
     assert n > 200000
@@ -50,4 +50,4 @@ def test_split_matches_fp64(gpu_ctx, big):
     sb, n = big
     _, _, _, _, hp64, _, _ = products(gpu_ctx, sb, n, "fp64")
     _, _, _, _, hp, _, _ = products(gpu_ctx, sb, n, "bf16x3tc")
-    assert np.linalg.norm(hp - hp64) / np.linalg.norm(hp64) <= 1e-4
+    assert np.linalg.norm(hp - hp64) / np.linalg.norm(hp64) <= 2e-5

@@ -4,7 +4,7 @@ The per-sector baseline (one launch per psi / sigma sector, one block per
 tile) and autotuned persistent schedules compute the same products as the
 default persistent schedule: relative difference <= 1e-5 between schedules
 (only the split-tile summation order differs), each within the split
-tolerance 1e-4 of the FP64 oracle.  Tuned knobs are cached under the
+tolerance 2e-5 of the FP64 oracle.  Tuned knobs are cached under the
 superblock's sector-size histogram: a superblock with the same sectors reuses
 them without timing, also from the cache file in a new context."""
 import numpy as np
@@ -42,7 +42,7 @@ def test_per_sector_schedule_matches(tc_ctx, oracle, name, sweep, pos):
     info_b = tc_ctx.superblock_info(sb)
     assert info_a["tc_per_sector"] == 0 and info_b["tc_per_sector"] == 1
     assert info_b["launches"] > info_a["launches"]
-    assert rel(a, snap["sigma"]) <= 1e-4 and rel(b, snap["sigma"]) <= 1e-4
+    assert rel(a, snap["sigma"]) <= 2e-5 and rel(b, snap["sigma"]) <= 2e-5
     assert rel(b, a) <= 1e-5
     tc_ctx.set_tc_schedule(False)
     c = tc_ctx.sigma(sb, snap["psi"])
@@ -61,7 +61,7 @@ def test_autotune_caches_by_histogram(tc_ctx, oracle, tmp_path):
     info = tc_ctx.superblock_info(sb)
     t1, c1, secs = tc_ctx.autotune_stats()
     assert info["tc_tuned"] == 1 and t1 == t0 + 1 and c1 >= 1 and secs > 0
-    assert rel(a, snap["sigma"]) <= 1e-4
+    assert rel(a, snap["sigma"]) <= 2e-5
     # same sectors: knobs from the cache, no timing, same products
     sb2, _ = load(tc_ctx, snap)
     b = tc_ctx.sigma(sb2, snap["psi"])

@@ -2,8 +2,9 @@
 against the FP64 oracle, and split-precision Davidson / sweeps with the FP64
 Rayleigh-quotient refinement against the golden energies.
 
-Tolerances written here: relative sigma error <= 1e-4 for BF16X3 (3 products,
-16-bit operands) and <= 5e-6 for BF16X6 (6 products, FP32-level operands);
+Tolerances written here: relative sigma error <= 2e-5 for BF16X3 (3 products,
+16-bit operands; observed 2-5e-6), <= 5e-5 for FP16X2 (observed 9e-6 to 4e-5)
+and <= 5e-6 for BF16X6 (6 products, FP32-level operands);
 refined energies within 1e-8 Eh of the dense FP64 eigenvalue on small
 superblocks and within the reference's 1e-6 Eh of its golden energies for
 full sweeps."""
@@ -18,7 +19,7 @@ from test_gpu_sigma import SNAPS, load
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"bf16x3": 1e-4, "bf16x6": 5e-6, "bf16x3tc": 1e-4, "fp16x2tc": 1e-4}
+TOL = {"bf16x3": 2e-5, "bf16x6": 5e-6, "bf16x3tc": 2e-5, "fp16x2tc": 5e-5}
 
 with open(os.path.join(GOLDEN, "golden.json")) as f:
     GOLD = json.load(f)

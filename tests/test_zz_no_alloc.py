@@ -51,11 +51,34 @@ def test_noalloc_matches_device_entry_point(oracle):
             ctx.device_free(p)
 
 
+def test_noalloc_is_fp64_whatever_the_precision(oracle):
+    """The allocation-free product is the FP64 one even after a split
+    precision is chosen (its packed pools would need allocations)."""
+    import block_gb300
+
+    snap = oracle.snapshot(conf("c2_d2h"), 5, 5)
+    with block_gb300.Context(0) as ctx:
+        sb, n = _superblock(ctx, snap)
+        x, y = ctx.device_alloc(n), ctx.device_alloc(n)
+        ctx.to_device(x, snap["psi"])
+        ctx.set_precision("bf16x3tc")
+        for _ in range(2):
+            ctx.sigma_noalloc(sb, x, y)
+            ctx.synchronize()
+            got = ctx.to_host(y, n)
+            assert np.linalg.norm(got - snap["sigma"]) / np.linalg.norm(snap["sigma"]) <= 1e-12
+        ctx.device_free(x)
+        ctx.device_free(y)
+
+
 def test_noalloc_rejects_oversized_superblock():
     import block_gb300
 
     with block_gb300.Context(0) as ctx:
         sb, n = ctx.prepare_superblock(conf("syn24"), 11)
+        # the case is chosen because its FP64 intermediates exceed the array
+        need = ctx.superblock_info(sb)["fp64_scratch"]
+        assert need > block_gb300.NOALLOC_SCRATCH_DOUBLES, need
         x, y = ctx.device_alloc(n), ctx.device_alloc(n)
         with pytest.raises(block_gb300.BgpuError, match="more than the fixed"):
             ctx.sigma_noalloc(sb, x, y)
