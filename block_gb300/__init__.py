@@ -72,6 +72,10 @@ _SIGS = {
     "bgpu_tc_wait_selftest": (_I, [_P, ctypes.c_double, _IP, _IP, _DP]),
     "bgpu_prepare_superblock": (_I, [_P, _CP, _I, _IP, _I64P]),
     "bgpu_run_dmrg": (_I, [_P, _CP, _I, _DP, _I, _DP]),
+    "bgpu_set_refinement": (_I, [_P, _I]),
+    "bgpu_sweep_energies": (_I, [_P, _DP, _I, _IP]),
+    "bgpu_run_stats": (_I, [_P, _DP, _I]),
+    "bgpu_refinement_stats": (_I, [_P, _I64P, _I64P, _IP]),
     "bgpu_block_set_sites": (_I, [_P, _I, _I, _IP]),
     "bgpu_block_quanta": (_I, [_P, _I, _IP, _IP, _IP]),
     "bgpu_integrals_load": (_I, [_P, _CP, _IP, _IP]),
@@ -79,6 +83,8 @@ _SIGS = {
     "bgpu_integrals_free": (_I, [_P, _I]),
     "bgpu_build_enlarged_ops": (_I, [_P, _I, _I, _I, _IP, _I, _IP, _IP, _I64P, _IP]),
     "bgpu_set_wavefunctions": (_I, [_P, _I, _I, _DP]),
+    "bgpu_diagonalise": (_I, [_P, _I, _IP, _DP, _DP, _DP]),
+    "bgpu_set_density_noise": (_I, [_P, _D, _D, ctypes.c_uint64]),
     "bgpu_density_download": (_I, [_P, _DP, _DP, _I64]),
     "bgpu_renormalise": (_I, [_P, _I, _IP, _DP, _I, _IP, _IP, _I64P, _IP]),
     "bgpu_rotation_download": (_I, [_P, _I, _DP, _I64]),
@@ -231,6 +237,27 @@ class Context:
                                                      len(op_keys) // 4, _ip(op_keys), ctypes.byref(h),
                                                      ctypes.byref(n), ctypes.byref(nq)))
         return h.value, n.value, nq.value
+
+    def diagonalise(self, matrices, vectors=True):
+        """Eigenpairs of a list of symmetric matrices on the GPU solver:
+        [(eigenvalues ascending, eigenvectors as columns or None)]."""
+        dims = np.array([m.shape[0] for m in matrices], dtype=np.int32)
+        a = np.concatenate([np.ascontiguousarray(m, dtype=np.float64).reshape(-1) for m in matrices])
+        w = np.empty(int(dims.sum()))
+        z = np.empty(a.size) if vectors else None
+        self._check(self.lib.bgpu_diagonalise(self.h, len(dims), _ip(dims), _dp(a), _dp(w),
+                                              _dp(z) if z is not None else None))
+        out, oa, ow = [], 0, 0
+        for n in dims:
+            n = int(n)
+            out.append((w[ow:ow + n].copy(), z[oa:oa + n * n].reshape(n, n).copy() if z is not None else None))
+            oa += n * n
+            ow += n
+        return out
+
+    def set_density_noise(self, perturbative=0.0, random=0.0, seed=0):
+        """Noise of the following density_eig calls (see bgpu_set_density_noise)."""
+        self._check(self.lib.bgpu_set_density_noise(self.h, float(perturbative), float(random), int(seed)))
 
     def set_wavefunctions(self, sb, vectors):
         v = np.ascontiguousarray(np.atleast_2d(vectors), dtype=np.float64)
@@ -399,6 +426,17 @@ class Context:
         self._check(self.lib.bgpu_davidson_graph_launches(self.h, ctypes.byref(v)))
         return v.value
 
+    def set_refinement(self, mode):
+        """Split-precision solves: "defect" (FP64-residual defect correction,
+        default) or "energy" (FP64 Rayleigh quotients only)."""
+        self._check(self.lib.bgpu_set_refinement(self.h, {"energy": 0, "defect": 1}[mode]))
+
+    def refinement_stats(self):
+        """(FP64 restarts, FP64 products, last solve verified on FP64 residuals)."""
+        a, b, c = _I64(), _I64(), _I()
+        self._check(self.lib.bgpu_refinement_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, bool(c.value)
+
     def set_refine_window(self, eh):
         """FP64 energy refinement window of split-precision sweeps (Eh)."""
         self._check(self.lib.bgpu_set_refine_window(self.h, float(eh)))
@@ -438,4 +476,14 @@ class Context:
                      seconds=st[4], discarded=st[5], last_sweep_energy=st[6], build_seconds=st[8],
                      solve_seconds=st[9], density_seconds=st[10], renorm_seconds=st[11],
                      plan_seconds=st[12])
+        sw = np.zeros(256)
+        ns = _I()
+        self._check(self.lib.bgpu_sweep_energies(self.h, _dp(sw), len(sw), ctypes.byref(ns)))
+        stats["sweep_energies"] = sw[:min(ns.value, len(sw))].copy()
+        nsw = len(stats["sweep_energies"])
+        rs = np.zeros(7 + nsw)
+        self._check(self.lib.bgpu_run_stats(self.h, _dp(rs), len(rs)))
+        stats.update(split_sigma_calls=int(rs[0]), split_sigma_seconds=rs[1], fp64_sigma_calls=int(rs[2]),
+                     fp64_sigma_seconds=rs[3], defect_rounds=int(rs[4]), derived_fp64_sigma_seconds=rs[5],
+                     warmup_seconds=rs[6], sweep_seconds=rs[7:7 + nsw].copy())
         return e[:nroots].copy(), stats

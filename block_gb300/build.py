@@ -56,7 +56,7 @@ def build(verbose=False, jobs=None):
                 print(l, file=sys.stderr)
     tmp = LIB + ".tmp"
     libdir = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcusolver", "-Xlinker", "-rpath", "-Xlinker", libdir])
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-Xlinker", "-rpath", "-Xlinker", libdir])
     os.replace(tmp, LIB)
     return LIB
 

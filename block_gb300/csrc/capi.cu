@@ -21,6 +21,8 @@ struct bgpu_ctx {
   std::string err;
   int device = 0;
   double refine_window = 1e-3;  // Eh; see bgpu_set_refine_window
+  std::vector<double> sweep_energies;  // of the last bgpu_run_dmrg
+  std::vector<double> run_stats;       // see bgpu_run_stats
   bool transform_guess = true;  // see bgpu_set_guess
   int deferred_steps = 4;        // see bgpu_set_refine_window
   struct BlockRec {
@@ -28,6 +30,7 @@ struct bgpu_ctx {
     std::vector<OpKey> decl;  // declaration order
     std::vector<int> orbsym;
     std::string group = "c1";
+    bool filled = false;  // arena uploaded or computed by the library
   };
   std::map<int, std::unique_ptr<BlockRec>> blocks;
   std::map<int, std::unique_ptr<Integrals>> integrals;
@@ -39,7 +42,10 @@ struct bgpu_ctx {
     // superblocks prepared from a configuration own their blocks
     std::unique_ptr<Block> ownL, ownR;
     std::unique_ptr<SweepDriver> drv;
+    std::vector<int> orbsym;  // orbital irreps and point group (density noise)
+    std::string group = "c1";
   };
+  NoiseSpec density_noise;  // see bgpu_set_density_noise
   std::map<int, std::unique_ptr<SbRec>> sbs;
   int next = 1;
 };
@@ -179,6 +185,38 @@ int bgpu_set_refine_window(bgpu_ctx* ctx, double eh) {
   });
 }
 
+int bgpu_sweep_energies(bgpu_ctx* ctx, double* e, int cap, int* n) {
+  return guarded(ctx, [&] {
+    need(n != nullptr && (cap == 0 || e), "null argument");
+    *n = (int)ctx->sweep_energies.size();
+    for (int i = 0; i < cap && i < *n; ++i) e[i] = ctx->sweep_energies[i];
+  });
+}
+
+int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n) {
+  return guarded(ctx, [&] {
+    need(out && n >= 0, "null argument");
+    for (int i = 0; i < n; ++i) out[i] = i < (int)ctx->run_stats.size() ? ctx->run_stats[i] : 0.0;
+  });
+}
+
+int bgpu_set_refinement(bgpu_ctx* ctx, int mode) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    need(mode == 0 || mode == 1, "refinement mode must be 0 (energy only) or 1 (defect correction)");
+    ctx->eng->refine_mode = mode;
+  });
+}
+
+int bgpu_refinement_stats(bgpu_ctx* ctx, int64_t* rounds, int64_t* fp64_products, int* last_verified) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    if (rounds) *rounds = ctx->eng->defect_rounds_;
+    if (fp64_products) *fp64_products = ctx->eng->defect_fp64_sigma_;
+    if (last_verified) *last_verified = ctx->eng->last_fp64_verified_ ? 1 : 0;
+  });
+}
+
 int bgpu_set_precision(bgpu_ctx* ctx, int p) {
   return guarded(ctx, [&] {
     need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6 || p == BGPU_PREC_BF16X3_TC ||
@@ -233,6 +271,7 @@ int bgpu_block_upload(bgpu_ctx* ctx, int handle, const double* a, int64_t n) {
     need(it != ctx->blocks.end() && a, "bad block");
     need(n == it->second->b.ops.arena, "arena size mismatch");
     ctx->eng->upload_block(it->second->b, std::vector<double>(a, a + n));
+    it->second->filled = true;
   });
 }
 
@@ -303,6 +342,8 @@ int bgpu_superblock_define(bgpu_ctx* ctx, int left, int right, const int* target
     ctx->eng->plan_sigma(sb, rec->plan);
     rec->psi = ctx->eng->alloc(sb.size);
     rec->sig = ctx->eng->alloc(sb.size);
+    rec->orbsym = li->second->orbsym;
+    rec->group = li->second->group;
     *psi_elems = sb.size;
     *sbh = ctx->next++;
     ctx->sbs[*sbh] = std::move(rec);
@@ -467,10 +508,32 @@ int bgpu_density_eig(bgpu_ctx* ctx, int sb, int left, int nroots, const double* 
     need(n == B.si.total_states(), "eigenvalue buffer size must equal the block's states");
     std::vector<double> w(weights ? weights : nullptr, weights ? weights + nroots : nullptr);
     DensitySpectrum spec;
-    ctx->eng->density(it->second->sb, left != 0, w, spec);
+    NoiseSpec ns = ctx->density_noise;
+    if (ns.any()) {
+      ns.orbsym = it->second->orbsym;
+      ns.group = PointGroup::from_name(it->second->group);
+    }
+    ctx->eng->set_noise(ns);
+    try {
+      ctx->eng->density(it->second->sb, left != 0, w, spec);
+    } catch (...) {
+      ctx->eng->set_noise(NoiseSpec{});
+      throw;
+    }
+    ctx->eng->set_noise(NoiseSpec{});
     int64_t o = 0;
     for (auto& v : spec.eig)
       for (double x : v) eig[o++] = x;
+  });
+}
+
+int bgpu_set_density_noise(bgpu_ctx* ctx, double perturbative, double random, uint64_t seed) {
+  return guarded(ctx, [&] {
+    need(perturbative >= 0.0 && random >= 0.0, "noise amplitudes must be >= 0");
+    ctx->density_noise = NoiseSpec{};
+    ctx->density_noise.perturbative = perturbative;
+    ctx->density_noise.random = random;
+    ctx->density_noise.seed = seed;
   });
 }
 
@@ -617,6 +680,7 @@ int bgpu_build_enlarged_ops(bgpu_ctx* ctx, int integrals, int left, int right, c
     const auto& A = *li->second;
     const auto& B = *ri->second;
     need(!A.b.sites.empty() && !B.b.sites.empty(), "sub-blocks need their sites (bgpu_block_set_sites)");
+    need(A.filled && B.filled, "sub-blocks need their operators (bgpu_block_upload)");
     need(A.b.is_dot || B.b.is_dot, "one sub-block must be a single site (is_dot)");
     need((int)A.orbsym.size() == I.norb && A.orbsym == B.orbsym, "orbital irreps of the blocks and integrals differ");
     need(A.group == B.group, "point groups of the sub-blocks differ");
@@ -651,10 +715,55 @@ int bgpu_build_enlarged_ops(bgpu_ctx* ctx, int integrals, int left, int right, c
     ctx->eng->create_block(nb);
     ctx->eng->build_block(nb, A.b, B.b, recipes);
     ctx->eng->sync();
+    rec->filled = true;
     *arena_elems = nb.ops.arena;
     if (nquanta) *nquanta = nb.si.size();
     *big = ctx->next++;
     ctx->blocks[*big] = std::move(rec);
+  });
+}
+
+int bgpu_diagonalise(bgpu_ctx* ctx, int nmat, const int* dims, const double* a, double* eigvals, double* eigvecs) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    need(nmat > 0 && dims && a && eigvals, "null argument");
+    std::vector<int> d(dims, dims + nmat);
+    std::vector<int64_t> aoff(nmat), woff(nmat);
+    int64_t ta = 0, tw = 0;
+    for (int j = 0; j < nmat; ++j) {
+      need(d[j] >= 1 && d[j] <= dev::kEigMaxN, "matrix order out of range (1 .. 4096)");
+      aoff[j] = ta;
+      woff[j] = tw;
+      ta += (int64_t)d[j] * d[j];
+      tw += d[j];
+    }
+    GpuEngine& e = *ctx->eng;
+    double* da = e.alloc(ta);
+    double* dz = e.alloc(ta);
+    double* dw = e.alloc(tw);
+    cuda_check(cudaMemcpyAsync(da, a, ta * sizeof(double), cudaMemcpyHostToDevice, e.stream()), "h2d");
+    int* st = e.eigh_batched(d, da, aoff, /*copy_inputs=*/false, dz, aoff, dw, woff);
+    std::vector<int> hs(nmat);
+    std::vector<double> z(eigvecs ? ta : 0);
+    cuda_check(cudaMemcpyAsync(eigvals, dw, tw * sizeof(double), cudaMemcpyDeviceToHost, e.stream()), "d2h");
+    if (eigvecs) cuda_check(cudaMemcpyAsync(z.data(), dz, ta * sizeof(double), cudaMemcpyDeviceToHost, e.stream()), "d2h");
+    cuda_check(cudaMemcpyAsync(hs.data(), st, nmat * sizeof(int), cudaMemcpyDeviceToHost, e.stream()), "d2h");
+    e.sync();
+    cudaFreeAsync(st, e.stream());
+    e.free(da);
+    e.free(dz);
+    e.free(dw);
+    for (int j = 0; j < nmat; ++j)
+      if (hs[j] < 0) throw std::runtime_error("bgpu_diagonalise: QL iteration did not converge for matrix " +
+                                              std::to_string(j));
+    if (eigvecs)  // column-major per matrix -> row-major with the eigenvectors as columns
+      for (int j = 0; j < nmat; ++j) {
+        const int n = d[j];
+        const double* src = z.data() + aoff[j];
+        double* dst = eigvecs + aoff[j];
+        for (int r = 0; r < n; ++r)
+          for (int c = 0; c < n; ++c) dst[(int64_t)r * n + c] = src[(int64_t)c * n + r];
+      }
   });
 }
 
@@ -685,6 +794,7 @@ int bgpu_renormalise(bgpu_ctx* ctx, int big, const int* kept, const double* rota
     need(bi != ctx->blocks.end(), "bad block handle");
     need(kept && small && arena_elems && (nops == 0 || op_keys), "null argument");
     const auto& B = *bi->second;
+    need(B.filled, "the block has no operators yet (bgpu_block_upload or bgpu_build_enlarged_ops)");
     const StateInfo& si = B.b.si;
     const int nq = si.size();
     std::vector<int> k(kept, kept + nq);
@@ -725,6 +835,7 @@ int bgpu_renormalise(bgpu_ctx* ctx, int big, const int* kept, const double* rota
     ctx->eng->create_block(nb);
     ctx->eng->renormalise(nb, B.b);
     ctx->eng->sync();
+    rec->filled = true;
     *arena_elems = nb.ops.arena;
     if (nquanta) *nquanta = nb.si.size();
     *small = ctx->next++;
@@ -764,6 +875,8 @@ int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition,
     rec->sb.L = rec->ownL.get();
     rec->sb.R = rec->ownR.get();
     rec->drv.reset();  // warm-up blocks are no longer needed
+    rec->orbsym = I.orbsym;
+    rec->group = c.sym;
     ctx->eng->plan_sigma(rec->sb, rec->plan);
     rec->psi = ctx->eng->alloc(rec->sb.size);
     rec->sig = ctx->eng->alloc(rec->sb.size);
@@ -782,7 +895,8 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     Integrals I = load_integrals(c);
     DriverOptions opt;
     opt.verbose = verbose;
-    if (precision_slices(ctx->eng->precision)) {
+    if (precision_slices(ctx->eng->precision) && ctx->eng->refine_mode == 0) {
+      // energy-only refinement: deferred to the steps that may set the sweep energy
       opt.refine_window = ctx->refine_window;
       opt.deferred_steps = ctx->deferred_steps;
     }
@@ -790,12 +904,20 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops, p0 = ctx->eng->plan_seconds;
     const double d0 = ctx->eng->renorm_device_seconds;
     const long c0 = ctx->eng->sigma_calls;
+    GpuEngine& E = *ctx->eng;
+    const long sc0 = E.split_calls, fc0 = E.fp64_calls, dr0 = E.defect_rounds_;
+    const double ss0 = E.split_seconds, fs0 = E.fp64_seconds, dv0 = E.derived_fp64_sigma_seconds;
     SweepResult r;
     {
       SweepDriver drv(I, c, *ctx->eng, opt);
       r = drv.run();
     }
     ctx->eng->sync();  // the last renormalisation and block releases
+    ctx->sweep_energies = r.sweep_energies;
+    ctx->run_stats = {(double)(E.split_calls - sc0), E.split_seconds - ss0, (double)(E.fp64_calls - fc0),
+                      E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
+                      r.warmup_seconds};
+    for (double t : r.sweep_seconds) ctx->run_stats.push_back(t);
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {
       stats[0] = r.sweeps;

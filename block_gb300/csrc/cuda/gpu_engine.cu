@@ -1,6 +1,7 @@
 // Host side of the CUDA engine: compiles the operator algebra of a sweep
 // step into device work lists and drives the kernels of kernels.cu.
 #include "gpu_engine.h"
+#include "k_noise.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -20,7 +21,6 @@
 
 #include "../host/parallel.h"
 
-#include <cusolverDn.h>
 
 namespace bgpu {
 
@@ -172,19 +172,10 @@ GpuEngine::~GpuEngine() {
   for (auto& kv : parked_)
     if (kv.second.d) cudaFreeAsync(kv.second.d, stream_);
   if (guess_) cudaFreeAsync(guess_, stream_);
-  for (auto& l : lanes_)
-    if (l.work) cudaFreeAsync(l.work, stream_);
-  if (solver_info_) cudaFreeAsync(solver_info_, stream_);
   for (auto* q : pool_cache_)
     if (q) cudaFreeAsync(q, stream_);
   cudaStreamSynchronize(stream_);
   release_staging(stream_);
-  for (auto& l : lanes_) {
-    if (l.h) cusolverDnDestroy((cusolverDnHandle_t)l.h);
-    if (l.done) cudaEventDestroy(l.done);
-    if (l.s) cudaStreamDestroy(l.s);
-  }
-  if (fork_) cudaEventDestroy(fork_);
   cudaEventDestroy(ev0_);
   cudaEventDestroy(ev1_);
   cudaFree(tc_status_);
@@ -474,6 +465,7 @@ void GpuEngine::build_block(Block& big, const Block& a, const Block& b,
   const bool b_scalar = !a_scalar;  // if both are dots, b folds
   if (b_scalar && !db.dot) throw std::runtime_error("build_block: one sub-block must be a single site");
   const DevBlock& dsc = a_scalar ? da : db;
+  if ((int64_t)dsc.host.size() != dsc.n) throw std::runtime_error("build_block: the single-site block was never uploaded");
   // per recipe: rectangles keyed by (target block, row part, column part)
   struct Rect {
     int64_t key;
@@ -1999,46 +1991,102 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     return x;
   };
   bool with_sigma = false;
-  int iter = 0;
+  int iter = 0, total_iter = 0;
   dav_graph_launches_ = 0;
-  while (true) {
-    const int w = with_sigma ? 1 : 0;
-    auto t0 = std::chrono::steady_clock::now();
-    if (use_graph) {
-      if (!sc.gx[w]) sc.gx[w] = capture(with_sigma);
-      cuda_check(cudaGraphLaunch(sc.gx[w], stream_), "graph launch");
-      ++dav_graph_launches_;
-      if (with_sigma) {
-        sigma_flops += plan_.flops;
-        ++sigma_calls;
+  // iterations until every root converged or max_iter; returns how many of
+  // them computed a sigma (expanded the basis)
+  auto iterate = [&]() {
+    int expansions = 0;
+    with_sigma = false;
+    while (true) {
+      const int w = with_sigma ? 1 : 0;
+      auto t0 = std::chrono::steady_clock::now();
+      if (use_graph) {
+        if (!sc.gx[w]) sc.gx[w] = capture(with_sigma);
+        cuda_check(cudaGraphLaunch(sc.gx[w], stream_), "graph launch");
+        ++dav_graph_launches_;
+        if (with_sigma) {
+          sigma_flops += plan_.flops;
+          ++sigma_calls;
+        }
+      } else {
+        enqueue(with_sigma, false);
       }
-    } else {
-      enqueue(with_sigma, false);
+      sync();
+      if (with_sigma) {
+        ++expansions;
+        float ms = 0.f;
+        double dt;
+        if (cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]) == cudaSuccess) dt = ms * 1e-3;
+        else dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        count_sigma(dt);
+      }
+      const dev::DavCtl& h = *dav_host_;
+      if (h.status < 0) throw std::runtime_error("subspace eigensolver did not converge");
+      iter = h.iter;
+      if (h.done || iter >= p.max_iter) break;
+      with_sigma = h.expand != 0;
     }
-    sync();
-    if (with_sigma) {
-      float ms = 0.f;
-      double dt;
-      if (cudaEventElapsedTime(&ms, sc.ev[0], sc.ev[1]) == cudaSuccess) dt = ms * 1e-3;
-      else dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-      count_sigma(dt);
-    }
-    const dev::DavCtl& h = *dav_host_;
-    if (h.status < 0) throw std::runtime_error("subspace eigensolver did not converge");
-    iter = h.iter;
-    if (h.done || iter >= p.max_iter) break;
-    with_sigma = h.expand != 0;
-  }
+    total_iter += iter;
+    return expansions;
+  };
+  iterate();
   laps.lap("iterations");
+  // Defect correction of split-precision solves: the Ritz vectors get FP64
+  // products, the Davidson restarts from them with their exact FP64
+  // subspace matrix and residuals, and every further basis vector (a
+  // correction, small next to the vectors) gets a split-precision product.
+  // The split error then enters only through the corrections, scaled by
+  // their size, and each round shrinks the FP64 residual by about the split
+  // precision; the solve ends when a restart's FP64 residuals of every root
+  // are below tol without any new basis vector (linear.C:301-335 applied to
+  // the FP64 residual).
+  bool fp64_verified = false;
+  last_defect_rounds_ = 0;
+  if (precision_slices(precision) && refine_mode == 1) {
+    for (int round = 0; round < kDefectRounds; ++round) {
+      for (int i = 0; i < nroots; ++i) {
+        auto t0 = std::chrono::steady_clock::now();
+        sigma(sb, plan_, row(B, i), row(S, i));
+        sync();
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        sigma_seconds += dt;
+        fp64_seconds += dt;
+        ++fp64_calls;
+        ++defect_fp64_sigma_;
+      }
+      dev::DavCtl c1{};
+      std::vector<double> col(nroots);
+      for (int j = 0; j < nroots; ++j) {
+        dots(B, nroots, row(S, j), col.data());
+        for (int i = j; i < nroots; ++i) c1.h[i * nroots + j] = c1.h[j * nroots + i] = col[i];
+      }
+      c1.k = nroots;
+      c1.mode = 2;
+      cuda_check(cudaMemcpyAsync(sc.ctl, &c1, sizeof(c1), cudaMemcpyHostToDevice, stream_), "h2d ctl");
+      sync();
+      ++last_defect_rounds_;
+      ++defect_rounds_;
+      const int expansions = iterate();
+      if (expansions == 0 && dav_host_->done) {
+        fp64_verified = true;
+        break;
+      }
+    }
+    laps.lap("defect correction");
+  }
   energies.assign(dav_host_->lam, dav_host_->lam + nroots);
   if (waves_) free(waves_);
   waves_ = alloc((int64_t)nroots * n);
   cuda_check(cudaMemcpyAsync(waves_, B, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "waves");
   wave_n_ = n;
   nwaves_ = nroots;
-  if (precision_slices(precision) && !p.defer_refine) refine(sb, energies);
+  last_fp64_verified_ = fp64_verified;
+  // without a verified FP64 restart (energy-only mode, or rounds / iterations
+  // exhausted): FP64 Rayleigh quotients of the final vectors
+  if (precision_slices(precision) && !fp64_verified && (!p.defer_refine || refine_mode == 1)) refine(sb, energies);
   sync();
-  return iter;
+  return total_iter;
 }
 
 // Defect correction: energies of the split-precision Ritz vectors from one
@@ -2438,13 +2486,20 @@ void GpuEngine::drop_parked(int id) {
 }
 
 std::string GpuEngine::step_stats() {
-  char buf[160];
-  std::snprintf(buf, sizeof(buf), "  [split sigma %ld x %.4fs, fp64 sigma %ld x %.4fs]", split_calls - last_split_calls_,
+  char buf[200];
+  std::snprintf(buf, sizeof(buf), "  [split sigma %ld x %.4fs, fp64 sigma %ld x %.4fs%s]", split_calls - last_split_calls_,
                 split_calls > last_split_calls_ ? (split_seconds - last_split_seconds_) / (split_calls - last_split_calls_)
                                                 : 0.0,
                 fp64_calls - last_fp64_calls_,
                 fp64_calls > last_fp64_calls_ ? (fp64_seconds - last_fp64_seconds_) / (fp64_calls - last_fp64_calls_)
-                                              : 0.0);
+                                              : 0.0,
+                precision_slices(precision) && refine_mode == 1
+                    ? (last_fp64_verified_ ? ", FP64 residuals met tol" : ", FP64 residuals NOT verified")
+                    : "");
+  // what the step's Davidson products would have cost in FP64: every product
+  // of the step (split or FP64) at the step's measured FP64 product time
+  const long ds = split_calls - last_split_calls_, df = fp64_calls - last_fp64_calls_;
+  if (df > 0) derived_fp64_sigma_seconds += (double)(ds + df) * ((fp64_seconds - last_fp64_seconds_) / df);
   last_split_seconds_ = split_seconds;
   last_fp64_seconds_ = fp64_seconds;
   last_split_calls_ = split_calls;
@@ -2520,6 +2575,7 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   bufs.p[0] = waves_;
   bufs.p[1] = rho;
   cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "density");
+  if (noise_.any()) add_noise(sb, left, rho, off);
   if (laps.on) sync();
   laps.lap("rho gemm");
   // eigen-decomposition of every sector (diagonalise_dm): sectors up to
@@ -2559,51 +2615,19 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
     cuda_check(dev::launch_jacobi(jac, doff.d, ddims.d, w, dwoff.d, dm_vecs_, doff.d, dstat.d, nq, small_max, stream_),
                "density eig");
   }
+  int* eig_status = nullptr;
   if (!large.empty()) {
-    ensure_lanes();
-    if ((int)large.size() > solver_ninfo_) {
-      if (solver_info_) cudaFreeAsync(solver_info_, stream_);
-      cuda_check(cudaMallocAsync((void**)&solver_info_, large.size() * sizeof(int), stream_), "alloc info");
-      solver_ninfo_ = (int)large.size();
+    // the batched Householder / QL solver (k_eig.cu) on a copy of the large
+    // sectors (it overwrites its inputs); eigenvectors column-major
+    std::vector<int> dims;
+    std::vector<int64_t> aoff, zoff, wo;
+    for (int q : large) {
+      dims.push_back(dm_dims_[q]);
+      aoff.push_back(off[q]);
+      zoff.push_back(off[q]);
+      wo.push_back(woff[q]);
     }
-    // sector i goes to lane i % kSolverLanes; workspaces grow on the engine
-    // stream, before the lanes fork from it
-    int64_t need[kSolverLanes] = {};
-    for (size_t i = 0; i < large.size(); ++i) {
-      const int q = large[i];
-      int lw = 0;
-      auto h = (cusolverDnHandle_t)lanes_[i % kSolverLanes].h;
-      if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, dm_dims_[q],
-                                      dm_vecs_ + off[q], dm_dims_[q], w + woff[q], &lw) != CUSOLVER_STATUS_SUCCESS)
-        throw std::runtime_error("syevd buffer size");
-      need[i % kSolverLanes] = std::max<int64_t>(need[i % kSolverLanes], lw);
-    }
-    const int used = (int)std::min<size_t>(large.size(), kSolverLanes);
-    for (int l = 0; l < used; ++l)
-      if (need[l] > lanes_[l].lwork) {
-        if (lanes_[l].work) free(lanes_[l].work);
-        lanes_[l].work = alloc(need[l]);
-        lanes_[l].lwork = need[l];
-      }
-    for (int q : large)
-      cuda_check(cudaMemcpyAsync(dm_vecs_ + off[q], rho + off[q], (size_t)dm_dims_[q] * dm_dims_[q] * sizeof(double),
-                                 cudaMemcpyDeviceToDevice, stream_),
-                 "copy rho");
-    cuda_check(cudaEventRecord(fork_, stream_), "fork");
-    for (int l = 0; l < used; ++l) cuda_check(cudaStreamWaitEvent(lanes_[l].s, fork_, 0), "lane wait");
-    for (size_t i = 0; i < large.size(); ++i) {
-      const int q = large[i];
-      const int n = dm_dims_[q];
-      SolverLane& ln = lanes_[i % kSolverLanes];
-      if (cusolverDnDsyevd((cusolverDnHandle_t)ln.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
-                           dm_vecs_ + off[q], n, w + woff[q], ln.work, (int)ln.lwork,
-                           solver_info_ + i) != CUSOLVER_STATUS_SUCCESS)
-        throw std::runtime_error("syevd launch failed");
-    }
-    for (int l = 0; l < used; ++l) {
-      cuda_check(cudaEventRecord(lanes_[l].done, lanes_[l].s), "lane done");
-      cuda_check(cudaStreamWaitEvent(stream_, lanes_[l].done, 0), "join lane");
-    }
+    eig_status = eigh_batched(dims, rho, aoff, /*copy_inputs=*/true, dm_vecs_, zoff, w, wo);
   }
   if (laps.on) {
     sync();
@@ -2616,13 +2640,14 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   cuda_check(cudaMemcpyAsync(hw.data(), w, wt * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
   cuda_check(cudaMemcpyAsync(st.data(), dstat.d, nq * sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
   if (!large.empty())
-    cuda_check(cudaMemcpyAsync(info.data(), solver_info_, large.size() * sizeof(int), cudaMemcpyDeviceToHost, stream_),
+    cuda_check(cudaMemcpyAsync(info.data(), eig_status, large.size() * sizeof(int), cudaMemcpyDeviceToHost, stream_),
                "d2h");
   sync();
+  if (eig_status) cudaFreeAsync(eig_status, stream_);
   for (int q = 0; q < nq; ++q)
     if (st[q] < 0) throw std::runtime_error("density-matrix eigensolver did not converge");
   for (int x : info)
-    if (x != 0) throw std::runtime_error("density-matrix dense eigensolver failed");
+    if (x != 0) throw std::runtime_error("density-matrix eigensolver (QL iteration) did not converge");
   spec.eig.assign(nq, {});
   for (int q = 0; q < nq; ++q) spec.eig[q].assign(hw.begin() + woff[q], hw.begin() + woff[q] + B.si.states[q]);
   du.release(stream_);
@@ -2635,6 +2660,239 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   free(w);
   if (jac) free(jac);
   sync();
+}
+
+// Noise of the density matrix (add_onedot_noise, density.C:330-421, with
+// the single-operator TensorMultiply of operatorfunctions.C:331-404;
+// add_twodot_noise, density.C:92-165); see NoiseSpec.  Every
+// phi = (O x 1) psi (or (1 x O) psi) is one grouped FP64 GEMM unit per
+// output sector, normalised on the device, and its outer products are summed
+// into the sectors of the noise matrix N by a second grouped GEMM; the trace
+// condition and scale are applied on the device.  Operators are processed in
+// chunks of at most 64 M doubles of phi.
+void GpuEngine::add_noise(const Superblock& sb, bool left, double* rho, const std::vector<int64_t>& off) {
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const Block& B = left ? L : R;
+  const int nq = B.si.size();
+  const int nroots = std::max(nwaves_, 1);
+  const PointGroup& g = noise_.group;
+  int64_t tot = 0;
+  for (int q = 0; q < nq; ++q) tot += (int64_t)B.si.states[q] * B.si.states[q];
+  // psi sector of each (lq, rq)
+  std::vector<int> index((size_t)L.si.size() * R.si.size(), -1);
+  for (int s = 0; s < (int)sb.sectors.size(); ++s) index[(size_t)sb.sectors[s].lq * R.si.size() + sb.sectors[s].rq] = s;
+  DevArray<int64_t> doff;
+  DevArray<int> ddims;
+  doff.upload(off, stream_);
+  ddims.upload(B.si.states, stream_);
+  const int64_t chunk_limit = 64ll << 20;
+  double* scal = alloc(2);  // trace of N
+  // one chunk of wavefunctions phi_j (ranges of `phi`), each added to `target`
+  // as phi_j phi_j^T with weight alpha (after normalisation on the device)
+  struct Wave {
+    std::vector<Superblock::Sector> sec;
+    int64_t base = 0;
+  };
+  auto add_outer = [&](const std::vector<Wave>& waves, double* phi, double* target, double alpha) {
+    std::vector<dev::GemmUnit> units;
+    std::vector<dev::GemmItem> items;
+    std::vector<dev::GemmTask> tasks;
+    for (int q = 0; q < nq; ++q) {
+      dev::GemmUnit u{};
+      u.c_buf = 1;
+      u.c_off = off[q];
+      u.ldc = u.m = u.n = B.si.states[q];
+      u.beta_one = 1;
+      u.ibeg = (int)items.size();
+      for (const Wave& w : waves)
+        for (const auto& S : w.sec) {
+          if ((left ? S.lq : S.rq) != q) continue;
+          dev::GemmItem it{};
+          it.a_buf = it.b_buf = 0;
+          it.a_off = it.b_off = w.base + S.offset;
+          it.lda = it.ldb = S.cols;
+          it.ta = left ? 0 : 1;
+          it.tb = left ? 1 : 0;
+          it.k = left ? S.cols : S.rows;
+          it.alpha = alpha;
+          items.push_back(it);
+        }
+      u.iend = (int)items.size();
+      if (u.iend > u.ibeg) units.push_back(u);
+    }
+    for (int u = 0; u < (int)units.size(); ++u) add_tasks(tasks, u, units[u].m, units[u].n);
+    DevArray<dev::GemmUnit> du;
+    DevArray<dev::GemmItem> di;
+    DevArray<dev::GemmTask> dt;
+    du.upload(units, stream_);
+    di.upload(items, stream_);
+    dt.upload(tasks, stream_);
+    dev::Bufs bufs{};
+    bufs.p[0] = phi;
+    bufs.p[1] = target;
+    cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "noise outer products");
+    du.release(stream_);
+    di.release(stream_);
+    dt.release(stream_);
+  };
+  auto normalise = [&](const std::vector<Wave>& waves, double* phi, int64_t total) {
+    std::vector<longlong2> ranges;
+    for (const Wave& w : waves) {
+      int64_t sz = 0;
+      for (const auto& S : w.sec) sz += (int64_t)S.rows * S.cols;
+      ranges.push_back(make_longlong2(w.base, w.base + sz));
+    }
+    (void)total;
+    DevArray<longlong2> dr;
+    dr.upload(ranges, stream_);
+    double* nrm = alloc((int64_t)ranges.size());
+    cuda_check(dev::launch_range_norm2(phi, dr.d, (int)ranges.size(), nrm, stream_), "noise norms");
+    cuda_check(dev::launch_range_normalise(phi, dr.d, (int)ranges.size(), nrm, stream_), "noise normalise");
+    dr.release(stream_);
+    free(nrm);
+  };
+  if (noise_.perturbative > 0.0) {
+    const std::vector<NoiseOp> ops = perturbative_noise_ops(B, sb.target, noise_.orbsym, g);
+    const int J = sb.target.s2;
+    double* N = alloc(tot);
+    for (int r = 0; r < nroots; ++r) {
+      cuda_check(cudaMemsetAsync(N, 0, std::max<int64_t>(tot, 1) * sizeof(double), stream_), "memset");
+      size_t i0 = 0;
+      while (i0 < ops.size()) {
+        // the next chunk of operators and its phi layout
+        std::vector<Wave> waves;
+        std::vector<size_t> which;
+        int64_t total = 0;
+        size_t i1 = i0;
+        for (; i1 < ops.size(); ++i1) {
+          Wave w;
+          int64_t size = 0;
+          w.sec = wave_sectors(L.si, R.si, ops[i1].q, g, size);
+          if (total > 0 && total + size > chunk_limit) break;
+          w.base = total;
+          total += size;
+          waves.push_back(std::move(w));
+          which.push_back(i1);
+        }
+        i0 = i1;
+        if (total == 0) continue;
+        double* phi = alloc(total);
+        std::vector<dev::GemmUnit> units;
+        std::vector<dev::GemmItem> items;
+        std::vector<dev::GemmTask> tasks;
+        for (size_t x = 0; x < waves.size(); ++x) {
+          const NoiseOp& no = ops[which[x]];
+          const Operand o = op(no.key, no.trans);
+          const int k = no.key.k2;
+          for (const auto& S : waves[x].sec) {
+            dev::GemmUnit u{};
+            u.c_buf = 2;
+            u.c_off = waves[x].base + S.offset;
+            u.ldc = S.cols;
+            u.m = S.rows;
+            u.n = S.cols;
+            u.beta_one = 0;
+            u.ibeg = (int)items.size();
+            if (left) {
+              for (int lqp = 0; lqp < L.si.size(); ++lqp) {
+                const int s = index[(size_t)lqp * R.si.size() + S.rq];
+                if (s < 0) continue;
+                const HostView v = hview(L, o, S.lq, lqp);
+                if (!v.ok) continue;
+                const double f = ninej(L.si.quanta[lqp].s2, R.si.quanta[S.rq].s2, J, k, 0, k, L.si.quanta[S.lq].s2,
+                                       R.si.quanta[S.rq].s2, no.q.s2) *
+                                 v.scale;
+                if (f == 0.0) continue;
+                const auto& P = sb.sectors[s];
+                dev::GemmItem it{};
+                it.a_buf = 0;
+                it.a_off = v.off;
+                it.lda = v.ld;
+                it.ta = v.trans ? 1 : 0;
+                it.b_buf = 1;
+                it.b_off = (int64_t)r * wave_n_ + P.offset;
+                it.ldb = P.cols;
+                it.tb = 0;
+                it.k = P.rows;
+                it.alpha = f;
+                items.push_back(it);
+              }
+            } else {
+              for (int rqp = 0; rqp < R.si.size(); ++rqp) {
+                const int s = index[(size_t)S.lq * R.si.size() + rqp];
+                if (s < 0) continue;
+                const HostView v = hview(R, o, S.rq, rqp);
+                if (!v.ok) continue;
+                double f = ninej(L.si.quanta[S.lq].s2, R.si.quanta[rqp].s2, J, 0, k, k, L.si.quanta[S.lq].s2,
+                                 R.si.quanta[S.rq].s2, no.q.s2) *
+                           v.scale;
+                if (op_fermion(no.key) && is_fermion(L.si.quanta[S.lq])) f = -f;
+                if (f == 0.0) continue;
+                const auto& P = sb.sectors[s];
+                dev::GemmItem it{};
+                it.a_buf = 1;  // psi(lq, rq')
+                it.a_off = (int64_t)r * wave_n_ + P.offset;
+                it.lda = P.cols;
+                it.ta = 0;
+                it.b_buf = 0;  // O(rq, rq')^T
+                it.b_off = v.off;
+                it.ldb = v.ld;
+                it.tb = v.trans ? 0 : 1;
+                it.k = P.cols;
+                it.alpha = f;
+                items.push_back(it);
+              }
+            }
+            u.iend = (int)items.size();
+            units.push_back(u);  // (units without items write zeros)
+          }
+        }
+        for (int u = 0; u < (int)units.size(); ++u) add_tasks(tasks, u, units[u].m, units[u].n);
+        DevArray<dev::GemmUnit> du;
+        DevArray<dev::GemmItem> di;
+        DevArray<dev::GemmTask> dt;
+        du.upload(units, stream_);
+        di.upload(items, stream_);
+        dt.upload(tasks, stream_);
+        dev::Bufs bufs{};
+        bufs.p[0] = arena(B);
+        bufs.p[1] = waves_;
+        bufs.p[2] = phi;
+        cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "noise O psi");
+        du.release(stream_);
+        di.release(stream_);
+        dt.release(stream_);
+        normalise(waves, phi, total);
+        add_outer(waves, phi, N, 1.0);
+        free(phi);
+      }
+      cuda_check(dev::launch_block_trace(N, doff.d, ddims.d, nq, scal, stream_), "noise trace");
+      cuda_check(dev::launch_noise_update(rho, N, tot, scal, noise_.perturbative / nroots, stream_), "noise update");
+    }
+    free(N);
+  }
+  if (noise_.random > 0.0) {
+    const std::vector<Quantum> qs = random_noise_quanta(sb.target);
+    for (int r = 0; r < nroots; ++r) {
+      const uint64_t seed = noise_.seed + 0x632BE59BD9B4E019ull * (uint64_t)r;
+      for (int i = 0; i < (int)qs.size(); ++i) {
+        Wave w;
+        int64_t size = 0;
+        w.sec = wave_sectors(L.si, R.si, qs[i], g, size);
+        if (size == 0) continue;
+        double* phi = alloc(size);
+        cuda_check(dev::launch_noise_fill(phi, size, seed, i, stream_), "noise fill");
+        std::vector<Wave> one{w};
+        normalise(one, phi, size);
+        add_outer(one, phi, rho, noise_.random / nroots / (double)qs.size());
+        free(phi);
+      }
+    }
+  }
+  free(scal);
+  doff.release(stream_);
+  ddims.release(stream_);
 }
 
 void GpuEngine::density_download(std::vector<double>& rho, std::vector<double>& vecs) {
@@ -2666,75 +2924,66 @@ void GpuEngine::set_waves(int nroots, int64_t n, const double* host) {
   sync();
 }
 
-// The dense divide-and-conquer solver loads its kernels on first use of
-// each size class and handle, which took up to seconds inside the first
-// sweep; one solve per size class (64 .. 2048 states, up to 1.25 max_n) on
-// every solver lane moves that to the warm-up.
-void GpuEngine::prepare_density(int max_n) {
-  PlanLaps laps{"density"};
-  ensure_lanes();
-  const int sizes[] = {64, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048};
-  // sectors of a density matrix reach ~0.9 M states; size classes up to 1.25 M
-  int top = 0;
-  for (int n : sizes)
-    if (n <= std::max(64, max_n + max_n / 4)) top = n;
-  double* a = alloc((int64_t)kSolverLanes * top * top);
-  double* w = alloc((int64_t)kSolverLanes * top);
-  int* info = nullptr;
-  cuda_check(cudaMallocAsync((void**)&info, kSolverLanes * sizeof(int), stream_), "alloc info");
-  for (int n : sizes) {
-    if (n > top) break;
-    // symmetric tridiagonal test matrix: 2 on the diagonal, -1 beside it,
-    // one copy per lane (each lane's handle loads its kernels on first use)
-    std::vector<double> m((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i) {
-      m[(size_t)i * n + i] = 2.0;
-      if (i + 1 < n) m[(size_t)i * n + i + 1] = m[(size_t)(i + 1) * n + i] = -1.0;
-    }
-    for (int l = 0; l < kSolverLanes; ++l) {
-      SolverLane& ln = lanes_[l];
-      double* al = a + (int64_t)l * top * top;
-      cuda_check(cudaMemcpyAsync(al, m.data(), m.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "h2d");
-      int lw = 0;
-      if (cusolverDnDsyevd_bufferSize((cusolverDnHandle_t)ln.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
-                                      al, n, w + (int64_t)l * top, &lw) != CUSOLVER_STATUS_SUCCESS)
-        throw std::runtime_error("syevd buffer size");
-      if (lw > ln.lwork) {
-        if (ln.work) free(ln.work);
-        ln.work = alloc(lw);
-        ln.lwork = lw;
-      }
-    }
-    sync();  // the lane streams read what the engine stream wrote
-    for (int l = 0; l < kSolverLanes; ++l) {
-      SolverLane& ln = lanes_[l];
-      if (cusolverDnDsyevd((cusolverDnHandle_t)ln.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
-                           a + (int64_t)l * top * top, n, w + (int64_t)l * top, ln.work, (int)ln.lwork,
-                           info + l) != CUSOLVER_STATUS_SUCCESS)
-        throw std::runtime_error("syevd launch failed");
-    }
-    for (auto& ln : lanes_) cuda_check(cudaStreamSynchronize(ln.s), "lane sync");
-    char what[48];
-    std::snprintf(what, sizeof(what), "prepare syevd n=%d", n);
-    laps.lap(what);
-  }
-  free(a);
-  free(w);
-  cudaFreeAsync(info, stream_);
-  sync();
-}
+// The eigensolver of the large density-matrix sectors is the library's own
+// (eigh_batched); it needs no loading ahead of the first sweep.
+void GpuEngine::prepare_density(int max_n) { (void)max_n; }
 
-void GpuEngine::ensure_lanes() {
-  if (!fork_) cuda_check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "event");
-  for (auto& l : lanes_) {
-    if (l.h) continue;
-    cusolverDnHandle_t h = nullptr;
-    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnCreate failed");
-    l.h = h;
-    cuda_check(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking), "lane stream");
-    cuda_check(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming), "event");
-    if (cusolverDnSetStream(h, l.s) != CUSOLVER_STATUS_SUCCESS) throw std::runtime_error("cusolverDnSetStream");
+// Symmetric eigendecomposition of a batch of matrices (k_eig.cu): matrix j
+// of order dims[j] at a + a_off[j] (row-major, lower triangle read; copied
+// first when copy_inputs, else overwritten), eigenvectors column-major at
+// z + z_off[j] and eigenvalues ascending at w + w_off[j].  Stream-ordered;
+// returns a device array of per-matrix status words (< 0: the QL iteration
+// did not converge) that the caller reads and frees (cudaFreeAsync).
+int* GpuEngine::eigh_batched(const std::vector<int>& dims, double* a, const std::vector<int64_t>& a_off,
+                             bool copy_inputs, double* z, const std::vector<int64_t>& z_off, double* w,
+                             const std::vector<int64_t>& w_off) {
+  const int nj = (int)dims.size();
+  std::vector<dev::EigJob> jobs(nj);
+  int64_t work = 0;
+  int tiles = 0, ql = 0, bt = 0, max_n = 0;
+  for (int j = 0; j < nj; ++j) max_n = std::max(max_n, dims[j]);
+  if (max_n > dev::kEigMaxN)
+    throw std::runtime_error("eigensolver: matrix of order " + std::to_string(max_n) + " above the limit " +
+                             std::to_string(dev::kEigMaxN));
+  const int bt_cols = dev::eig_bt_cols(max_n);
+  for (int j = 0; j < nj; ++j) {
+    dev::EigJob& J = jobs[j];
+    const int n = dims[j];
+    J.n = n;
+    J.nt = (n + dev::kEigTile - 1) / dev::kEigTile;
+    J.z_off = z_off[j];
+    J.w_off = w_off[j];
+    J.a_off = copy_inputs ? work : a_off[j];
+    if (copy_inputs) work += (int64_t)n * n;
+    J.v_off = work;
+    work += (int64_t)n * n;
+    J.q_off = work;
+    work += (int64_t)n * n;
+    J.s_off = work;
+    work += dev::eig_scalar_elems(n);
+    J.tile0 = tiles;
+    tiles += J.nt * (J.nt + 1) / 2;
+    J.ql0 = ql;
+    ql += (n + dev::kEigQlRows - 1) / dev::kEigQlRows;
+    J.bt0 = bt;
+    bt += (n + bt_cols - 1) / bt_cols;
   }
+  double* wk = alloc(work);
+  if (copy_inputs)
+    for (int j = 0; j < nj; ++j)
+      cuda_check(cudaMemcpyAsync(wk + jobs[j].a_off, a + a_off[j], (size_t)dims[j] * dims[j] * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, stream_),
+                 "copy eigensolver input");
+  int* status = nullptr;
+  cuda_check(cudaMallocAsync((void**)&status, std::max(nj, 1) * sizeof(int), stream_), "alloc status");
+  cuda_check(cudaMemsetAsync(status, 0, std::max(nj, 1) * sizeof(int), stream_), "memset");
+  DevArray<dev::EigJob> dj;
+  dj.upload(jobs, stream_);
+  dev::EigBufs eb{copy_inputs ? wk : a, z, w, wk, status};
+  cuda_check(dev::launch_eig(eb, dj.d, nj, max_n, tiles, ql, bt, stream_), "eigensolver");
+  dj.release(stream_);
+  free(wk);
+  return status;
 }
 
 void GpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {

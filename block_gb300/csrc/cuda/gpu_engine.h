@@ -15,6 +15,7 @@
 
 #include "../host/sweep.h"
 #include "k_dav.cuh"
+#include "k_eig.cuh"
 #include "k_fused.cuh"
 #include "k_split.cuh"
 #include "k_tc.cuh"
@@ -207,16 +208,32 @@ class GpuEngine : public Engine {
   // (per sector row-major, column c = eigenvector of the c-th smallest
   // eigenvalue); sectors back to back in quantum order
   void density_download(std::vector<double>& rho, std::vector<double>& vecs);
+  // adds the noise of noise() to the density matrix rho (sectors at off)
+  void add_noise(const Superblock& sb, bool left, double* rho, const std::vector<int64_t>& off);
   // sector sizes of the last density matrix
   const std::vector<int>& density_dims() const { return dm_dims_; }
+  // batched symmetric eigendecomposition (k_eig.cu); returns a device array
+  // of per-matrix status words for the caller to read and free
+  int* eigh_batched(const std::vector<int>& dims, double* a, const std::vector<int64_t>& a_off, bool copy_inputs,
+                    double* z, const std::vector<int64_t>& z_off, double* w, const std::vector<int64_t>& w_off);
   int64_t wave_size() const { return wave_n_; }
   Precision precision = Precision::FP64;
+  // split-precision solves: 1 (default) defect correction against FP64
+  // residuals; 0 only FP64 Rayleigh quotients of the converged split vectors
+  int refine_mode = 1;
+  static constexpr int kDefectRounds = 8;  // FP64 restarts per solve at most
+  int last_defect_rounds_ = 0;             // FP64 restarts of the last solve
+  bool last_fp64_verified_ = false;        // its roots met tol on FP64 residuals
+  long defect_rounds_ = 0, defect_fp64_sigma_ = 0;  // totals over all solves
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
   double sigma_flops = 0.0;
   long split_calls = 0, fp64_calls = 0;
   double split_seconds = 0.0, fp64_seconds = 0.0;
   double plan_seconds = 0.0;  // host time compiling sigma work lists
+  // sum over block steps of (products of the step) x (its mean FP64 product
+  // time): the FP64 sigma time of the same solves, for steps with an FP64 product
+  double derived_fp64_sigma_seconds = 0.0;
   // counters at the previous step_stats() call
   double last_split_seconds_ = 0.0, last_fp64_seconds_ = 0.0;
   long last_split_calls_ = 0, last_fp64_calls_ = 0;
@@ -256,23 +273,6 @@ class GpuEngine : public Engine {
   std::vector<int64_t> dm_off_;
   std::vector<int> dm_dims_;
   std::vector<char> dm_colmajor_;  // sector eigenvectors stored column-major (dense solver)
-  // dense symmetric eigensolver for the large density-matrix sectors
-  // lanes of the dense solver: the large sectors of one density matrix are
-  // decomposed concurrently, each lane with its own handle, stream and
-  // workspace (the stream joins the engine stream through events)
-  struct SolverLane {
-    void* h = nullptr;  // cusolverDnHandle_t
-    cudaStream_t s = nullptr;
-    cudaEvent_t done = nullptr;
-    double* work = nullptr;
-    int64_t lwork = 0;
-  };
-  static constexpr int kSolverLanes = 4;
-  SolverLane lanes_[kSolverLanes];
-  cudaEvent_t fork_ = nullptr;
-  void ensure_lanes();
-  int* solver_info_ = nullptr;
-  int solver_ninfo_ = 0;
   double* rot_ = nullptr;
   std::vector<int64_t> rot_off_;
   std::vector<int> rot_kept_, rot_rows_;

@@ -360,6 +360,10 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
         c.schedule.push_back(e);
       }
     }
+    else if (key == "twodot_noise") {
+      if (tok.size() != 3) throw std::runtime_error("twodot_noise needs two numbers (amplitude, gamma)");
+      c.twodot_noise = std::stod(tok[1]);
+    }
     // other keywords (hf_occ, twodot, twodot_to_onedot, onepdm, ...) are accepted and ignored
   }
   if (!sweep_tol_set && c.sweep_tol <= 0) c.sweep_tol = 1e-5;
@@ -415,6 +419,9 @@ void make_default_schedule(Config& c) {
   const int defM[] = {50, 100, 250, 500, 1000, 2000, 3000, 4000, 5000, 6000, 7000, 8000, 9000, 10000};
   const int defIter[] = {8, 8, 8, 8, 8, 4, 4, 4, 4, 4, 4, 4, 4, 4};
   const double defTol[] = {1e-5, 1e-5, 1e-5, 1e-5, 5e-5, 5e-6, 5e-6, 5e-6, 5e-6, 5e-6, 5e-6, 5e-6, 5e-6, 5e-6};
+  // scheduled (perturbative) noise; none when twodot_noise is given
+  const double nz = c.twodot_noise > 0.0 ? 0.0 : 1.0;
+  const double defNoise[] = {1e-4, 1e-4, 1e-4, 1e-4, 5e-5, 5e-5, 5e-5, 5e-5, 5e-5, 5e-5, 5e-5, 5e-5, 5e-5, 5e-5};
   if (c.maxM <= 0) throw std::runtime_error("schedule default needs maxM");
   c.schedule.clear();
   int count = 0;
@@ -422,29 +429,29 @@ void make_default_schedule(Config& c) {
   for (int i = 0; i < 14; ++i) {
     if (!first) {
       if (c.startM == c.maxM) {
-        c.schedule.push_back({count, c.startM, 1e-5, 0.0});
+        c.schedule.push_back({count, c.startM, 1e-5, nz * 1e-4});
         count += 8;
-        c.schedule.push_back({count, c.startM, 5e-6, 0.0});
+        c.schedule.push_back({count, c.startM, 5e-6, nz * 5e-5});
         break;
       } else if (c.startM == defM[i]) {
         first = true;
-        c.schedule.push_back({count, defM[i], defTol[i], 0.0});
+        c.schedule.push_back({count, defM[i], defTol[i], nz * defNoise[i]});
         count += defIter[i];
       } else if (c.startM < defM[i]) {
         first = true;
         const int j = i > 0 ? i - 1 : 0;
-        c.schedule.push_back({count, c.startM, defTol[j], 0.0});
+        c.schedule.push_back({count, c.startM, defTol[j], nz * defNoise[j]});
         count += defIter[j];
-        c.schedule.push_back({count, defM[i], defTol[i], 0.0});
+        c.schedule.push_back({count, defM[i], defTol[i], nz * defNoise[i]});
         count += defIter[i];
       }
     } else {
       if (defM[i] >= c.maxM) {
-        c.schedule.push_back({count, c.maxM, defTol[i], 0.0});
+        c.schedule.push_back({count, c.maxM, defTol[i], nz * defNoise[i]});
         count += defIter[i];
         break;
       }
-      c.schedule.push_back({count, defM[i], defTol[i], 0.0});
+      c.schedule.push_back({count, defM[i], defTol[i], nz * defNoise[i]});
       count += defIter[i];
     }
   }

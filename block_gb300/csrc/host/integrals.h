@@ -83,6 +83,10 @@ struct Config {
   // `reset_iter` then starts the schedule from its first entry again
   std::string checkpoint;
   bool restart = false, reset_iter = false;
+  // `twodot_noise <amplitude> <gamma>`: random-wavefunction noise of that
+  // amplitude in the density matrices of the first sweep (gamma is read and
+  // not used); with `schedule default` it replaces the scheduled noise
+  double twodot_noise = 0.0;
   // the remaining keywords are recognised and ignored (twodot_to_onedot,
   // hf_occ, onepdm/twopdm, noise columns ...)
   const ScheduleEntry& entry(int sweep) const;

@@ -467,6 +467,20 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   if (opt_.on_step) opt_.on_step(sb, sweep_index, p);
   t0 = clk::now();
   DensitySpectrum spec;
+  {
+    // the schedule's (perturbative) noise, and the random noise of
+    // twodot_noise in the first sweep (DensityMatrix::makedensitymatrix,
+    // density.C:27-90, called from renormalise.C:95-104)
+    NoiseSpec ns;
+    ns.perturbative = se.noise;
+    ns.random = sweep_index == 0 ? C_.twodot_noise : 0.0;
+    ns.seed = C_.seed + 0x5851F42D4C957F2Dull * (uint64_t)(sweep_index * N_ + p + 1);
+    if (ns.any()) {
+      ns.orbsym = I_.orbsym;
+      ns.group = g_;
+    }
+    E_.set_noise(ns);
+  }
   E_.density(sb, forward, C_.weights, spec);
   std::vector<std::vector<int>> kept_idx;
   std::vector<int> kept;
@@ -577,6 +591,10 @@ double SweepDriver::sweep(bool forward, int sweep_index) {
 
 SweepResult SweepDriver::run() {
   SweepResult res;
+  struct NoiseOff {  // the engine's noise ends with the run
+    Engine& e;
+    ~NoiseOff() { e.set_noise(NoiseSpec{}); }
+  } noise_off{E_};
   double eprev = std::numeric_limits<double>::infinity();
   int s_begin = 0;
   bool first_forward = true;
@@ -591,7 +609,10 @@ SweepResult SweepDriver::run() {
     log(1, "restart from %s: %d sweeps done, next sweep %s\n", C_.checkpoint.c_str(), s_begin,
         first_forward ? "forward" : "backward");
   } else {
+    const auto tw = std::chrono::steady_clock::now();
     warmup();
+    E_.device_renorm_seconds();  // waits for the warm-up's device work
+    res.warmup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
   }
   const int last_sched = C_.schedule.back().iter;
   for (int s = s_begin; s < C_.maxiter; ++s) {
@@ -599,6 +620,8 @@ SweepResult SweepDriver::run() {
     const auto ts = std::chrono::steady_clock::now();
     const double r0 = E_.device_renorm_seconds();
     const double e = sweep(forward, s);
+    E_.device_renorm_seconds();  // the sweep's device work is part of its wall time
+    res.sweep_seconds.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count());
     res.sweep_energies.push_back(e);
     res.sweeps = s + 1;
     // phases are host wall times; the renormalisation's device work runs

@@ -81,8 +81,33 @@ struct DensitySpectrum {
   std::vector<std::vector<double>> eig;
 };
 
+// Noise added to the density matrices of the next density() calls
+// (DensityMatrix::makedensitymatrix, density.C:27-90):
+//   perturbative: add_onedot_noise (density.C:330-421): for every root,
+//     rho += noise / nroots / tr(N) * N with N = sum over the normalised
+//     (O x 1) psi (O x 1)^T psi of the renormalised block's CRE and its
+//     two-index operators (CC, CD; or DDCOMP, CDCOMP on a block without
+//     them) and their adjoints, over every total spin they couple psi to,
+//     when tr(N) > 1;
+//   random: add_twodot_noise (density.C:92-165): for every root, normalised
+//     random wavefunctions of the quanta next to the target (N +- 1, 2;
+//     2S +- 1, 2) each add noise / nroots / (number of quanta) of their
+//     outer product; values uniform in [-1, 1) from a counter-based hash of
+//     (seed, quantum, element), identical on every engine.
+struct NoiseSpec {
+  double perturbative = 0.0;
+  double random = 0.0;
+  uint64_t seed = 0;
+  std::vector<int> orbsym;  // orbital irreps (operator quanta)
+  PointGroup group;
+  bool any() const { return perturbative > 0.0 || random > 0.0; }
+};
+
 class Engine {
  public:
+  // noise of the following density() calls (none by default)
+  virtual void set_noise(const NoiseSpec& n) { noise_ = n; }
+  const NoiseSpec& noise() const { return noise_; }
   virtual ~Engine() = default;
   virtual std::string name() const = 0;
   // storage
@@ -153,11 +178,31 @@ class Engine {
   virtual void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) = 0;
   // small = rotation^T big rotation for every operator of small's catalogue
   virtual void renormalise(Block& small, const Block& big) = 0;
+
+ protected:
+  NoiseSpec noise_;
 };
+
+// Host-side pieces of the noise shared by the engines: the sectors (lq, rq,
+// rows, cols, offset) of a wavefunction with total quantum q on L x R, the
+// neighbouring quanta of the random noise, its uniform values, and the
+// operator list of the perturbative noise.
+std::vector<Superblock::Sector> wave_sectors(const StateInfo& L, const StateInfo& R, const Quantum& q,
+                                             const PointGroup& g, int64_t& size);
+std::vector<Quantum> random_noise_quanta(const Quantum& target);
+struct NoiseOp {
+  OpKey key;
+  bool trans;
+  Quantum q;  // total quantum of (O x 1) psi (or (1 x O) psi)
+};
+std::vector<NoiseOp> perturbative_noise_ops(const Block& B, const Quantum& target, const std::vector<int>& orbsym,
+                                            const PointGroup& g);
 
 struct SweepResult {
   std::vector<double> energies;         // final energy per root
   std::vector<double> sweep_energies;   // lowest root, per sweep
+  std::vector<double> sweep_seconds;    // wall time per sweep (device work included)
+  double warmup_seconds = 0.0;          // wall time of the warm-up (0 on restart)
   double discarded = 0.0;
   int sweeps = 0;
   double sigma_seconds = 0.0;

@@ -54,10 +54,9 @@ extern "C" {
  * 2 slices / 3 products on tcgen05 with TMEM accumulators and bulk-copy
  * staged operands (BF16X3_TC), or the same kernels with 2 fp16 slices
  * (11-bit significands, values within +-65504; FP16X2_TC).  With a split
- * precision,
- * bgpu_davidson and bgpu_run_dmrg iterate with split-precision sigma and
- * refine every converged root's energy with one FP64 sigma (Rayleigh
- * quotient against the FP64 Hamiltonian). */
+ * precision, bgpu_davidson and bgpu_run_dmrg iterate with split-precision
+ * sigma and then correct the roots against FP64 residuals (see
+ * bgpu_set_refinement). */
 #define BGPU_PREC_FP64 0
 #define BGPU_PREC_BF16X3 1
 #define BGPU_PREC_BF16X6 2
@@ -74,7 +73,28 @@ const char* bgpu_last_error_string(const bgpu_ctx* ctx);
 const char* bgpu_version(void);
 /* Arithmetic of sigma products (BGPU_PREC_*). */
 int bgpu_set_precision(bgpu_ctx* ctx, int precision);
-/* Split-precision sweeps (no reference counterpart): bgpu_run_dmrg refines
+/*
+ * Refinement of split-precision Davidson solves (no reference counterpart;
+ * the reference iterates in FP64 throughout, linear.C:179-385):
+ *   mode 1 (default), defect correction: after the split-precision solve
+ *     converges, its Ritz vectors get FP64 products and the Davidson
+ *     restarts from them with their FP64 subspace matrix and residuals;
+ *     further basis vectors (corrections) get split-precision products.
+ *     Rounds repeat until a restart finds every root's squared FP64
+ *     residual norm below the solve's tolerance without expanding (at most
+ *     8 rounds; otherwise the energies are FP64 Rayleigh quotients of the
+ *     final vectors).  Energies are then FP64 Ritz values and the vectors
+ *     meet the FP64 convergence test of an FP64 solve.
+ *   mode 0, energy only: one FP64 Rayleigh quotient per converged root, and
+ *     in bgpu_run_dmrg only for the steps bgpu_set_refine_window selects.
+ */
+int bgpu_set_refinement(bgpu_ctx* ctx, int mode);
+/* FP64 restarts and FP64 products spent by defect correction in this
+ * context, and whether the last solve's roots met the tolerance on FP64
+ * residuals (1) or not (0). */
+int bgpu_refinement_stats(bgpu_ctx* ctx, int64_t* rounds, int64_t* fp64_products, int* last_verified);
+/* Split-precision sweeps with energy-only refinement (bgpu_set_refinement
+ * mode 0; no reference counterpart): bgpu_run_dmrg refines
  * a step's energies with FP64 Rayleigh quotients only when its unrefined
  * lowest energy is within `eh` of the lowest one seen so far in the sweep,
  * and always at the last step of every sweep (so that sweep and final
@@ -279,6 +299,35 @@ int bgpu_density_eig(bgpu_ctx* ctx, int sb, int left, int nroots, const double* 
                      int64_t n_eigvals);
 
 /*
+ * Symmetric eigendecomposition of a batch of dense matrices (diagonalise,
+ * MatrixBLAS.h:105 / MatrixBLAS.C:381-414, which calls LAPACK DSYEV), with
+ * the library's own GPU solver (Householder tridiagonalisation, implicit QL
+ * with accumulated rotations, back-transformation; the same solver runs on
+ * every density-matrix sector above 48 states).  Matrix j has order
+ * dims[j] (1 .. 4096) and is stored row-major in a, matrices back to back;
+ * eigvals receive the eigenvalues of each matrix in ascending order and
+ * eigvecs (may be NULL) the eigenvectors, row-major per matrix with column c
+ * the eigenvector of the c-th eigenvalue.  Host buffers.
+ */
+int bgpu_diagonalise(bgpu_ctx* ctx, int nmat, const int* dims, const double* a, double* eigvals, double* eigvecs);
+/*
+ * Noise added by the following bgpu_density_eig calls (the `noise` and
+ * `additional_noise` of DensityMatrix::makedensitymatrix, density.C:27-90):
+ *   perturbative > 0: add_onedot_noise (density.C:330-421) -- for every
+ *     root, rho += perturbative / nroots / tr(N) * N when tr(N) > 1, N the
+ *     sum of the normalised outer products of (O x 1) psi (the block's CRE
+ *     and two-index operators and their adjoints, coupled to every total
+ *     spin);
+ *   random > 0: add_twodot_noise (density.C:92-165) -- for every root,
+ *     normalised random wavefunctions of the quanta next to the target each
+ *     add random / nroots / (number of quanta) of their outer product; the
+ *     values are uniform in [-1, 1) from a counter-based generator seeded
+ *     with `seed` (the same values on every run and engine).
+ * 0, 0 (the default) adds none.  bgpu_run_dmrg takes its noise from the
+ * dmrg.conf instead (schedule noise column; twodot_noise).
+ */
+int bgpu_set_density_noise(bgpu_ctx* ctx, double perturbative, double random, uint64_t seed);
+/*
  * Wavefunctions the next bgpu_density_eig reads (host, nroots x psi_elems in
  * the superblock's sector order), in place of the last Davidson vectors:
  * the `wave_solutions` argument of DensityMatrix::makedensitymatrix
@@ -364,6 +413,17 @@ int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition,
  */
 int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
                   double* stats);
+/* Arithmetic of the last bgpu_run_dmrg (no reference counterpart), out[n]:
+ * split-precision products and their seconds, FP64 products and their
+ * seconds, defect-correction rounds, the FP64 product time the same
+ * solves would have taken (every product of a block step at that step's
+ * measured FP64 product time, summed over the steps with an FP64 product),
+ * the warm-up's wall seconds, then the wall seconds of each sweep. */
+int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n);
+/* Sweep energies (lowest root per sweep, Sweep::do_one's return value,
+ * sweep.C:436-453) of the last bgpu_run_dmrg: *n = number of sweeps, up to
+ * cap of them copied to e. */
+int bgpu_sweep_energies(bgpu_ctx* ctx, double* e, int cap, int* n);
 
 #ifdef __cplusplus
 }

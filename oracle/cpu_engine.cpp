@@ -8,6 +8,7 @@
 #include <stdexcept>
 
 #include "../block_gb300/csrc/host/dense.h"
+#include "../block_gb300/csrc/host/noise_rng.h"
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -149,7 +150,15 @@ CpuEngine::CpuEngine(int t) {
 
 void CpuEngine::create_block(Block& b) {
   b.handle = next_handle_++;
-  store_[b.handle].assign(b.ops.arena, 0.0);
+  if (structure_only && !b.is_dot) store_[b.handle].clear();
+  else store_[b.handle].assign(b.ops.arena, 0.0);
+}
+
+void CpuEngine::fill_random(Block& b, uint64_t seed) {
+  std::vector<double>& a = store_.at(b.handle);
+  a.resize(b.ops.arena);
+  Rng rng(seed);
+  for (auto& x : a) x = 0.1 * rng.normal();
 }
 
 void CpuEngine::release_block(Block& b) {
@@ -159,6 +168,7 @@ void CpuEngine::release_block(Block& b) {
 
 void CpuEngine::upload_block(Block& b, const std::vector<double>& a) {
   if ((int64_t)a.size() != b.ops.arena) throw std::runtime_error("upload size mismatch");
+  if (structure_only && !b.is_dot) return;
   store_.at(b.handle) = a;
 }
 
@@ -204,6 +214,7 @@ static void tensor_product(const Block& big, const OpKey& tk, double* T, const B
 
 void CpuEngine::build_block(Block& big, const Block& a, const Block& b,
                             const std::vector<std::pair<OpKey, std::vector<BuildTerm>>>& recipes) {
+  if (structure_only) return;
   std::vector<double>& T = store_.at(big.handle);
   std::fill(T.begin(), T.end(), 0.0);
   const double* Aar = store_.at(a.handle).data();
@@ -451,6 +462,7 @@ void CpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
         dgemm(true, false, S.cols, S.cols, S.rows, w, psi, S.cols, psi, S.cols, 1.0, rho[S.rq].data(), S.cols);
     }
   }
+  if (noise_.any()) add_noise(sb, left, rho);
   dm_rho_ = rho;  // kept for the element-wise parity tests
   spec.eig.assign(nq, {});
   dm_vecs_.assign(nq, {});
@@ -461,6 +473,116 @@ void CpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
     spec.eig[q].resize(d);
     dm_vecs_[q].resize((size_t)d * d);
     jacobi_eigh(d, rho[q].data(), spec.eig[q].data(), dm_vecs_[q].data());
+  }
+}
+
+// phi = (O x 1) psi (left) or (1 x O) psi (right) onto total quantum q, in
+// the sectors `out` of L x R (single-operator TensorMultiply,
+// operatorfunctions.C:331-404, in the conventions of sigma's couplings).
+void CpuEngine::apply_one(const Superblock& sb, bool left, const Operand& o, const std::vector<double>& psi,
+                          const std::vector<Superblock::Sector>& out, int s2_out, std::vector<double>& phi) {
+  const Block& L = *sb.L;
+  const Block& R = *sb.R;
+  const Block& B = left ? L : R;
+  const std::vector<double>& ar = store_.at(B.handle);
+  const int k = o.key.k2, J = sb.target.s2;
+  std::vector<int> index((size_t)L.si.size() * R.si.size(), -1);
+  for (int s = 0; s < (int)sb.sectors.size(); ++s) index[(size_t)sb.sectors[s].lq * R.si.size() + sb.sectors[s].rq] = s;
+  std::fill(phi.begin(), phi.end(), 0.0);
+  for (const auto& S : out) {
+    double* dst = phi.data() + S.offset;
+    if (left) {
+      for (int lqp = 0; lqp < L.si.size(); ++lqp) {
+        const int s = index[(size_t)lqp * R.si.size() + S.rq];
+        if (s < 0) continue;
+        View v;
+        if (!view(L, ar.data(), o, S.lq, lqp, v)) continue;
+        const double f = ninej(L.si.quanta[lqp].s2, R.si.quanta[S.rq].s2, J, k, 0, k, L.si.quanta[S.lq].s2,
+                               R.si.quanta[S.rq].s2, s2_out) * v.scale;
+        if (f == 0.0) continue;
+        const auto& P = sb.sectors[s];
+        dgemm(v.trans, false, S.rows, S.cols, P.rows, f, v.p, v.ld, psi.data() + P.offset, P.cols, 1.0, dst, S.cols);
+      }
+    } else {
+      for (int rqp = 0; rqp < R.si.size(); ++rqp) {
+        const int s = index[(size_t)S.lq * R.si.size() + rqp];
+        if (s < 0) continue;
+        View v;
+        if (!view(R, ar.data(), o, S.rq, rqp, v)) continue;
+        double f = ninej(L.si.quanta[S.lq].s2, R.si.quanta[rqp].s2, J, 0, k, k, L.si.quanta[S.lq].s2,
+                         R.si.quanta[S.rq].s2, s2_out) * v.scale;
+        if (op_fermion(o.key) && is_fermion(L.si.quanta[S.lq])) f = -f;
+        if (f == 0.0) continue;
+        const auto& P = sb.sectors[s];
+        // psi(lq, rq') O(rq, rq')^T
+        dgemm(false, !v.trans, S.rows, S.cols, P.cols, f, psi.data() + P.offset, P.cols, v.p, v.ld, 1.0, dst, S.cols);
+      }
+    }
+  }
+}
+
+// rho(b) += alpha * phi phi^T restricted to the sectors of the block (left:
+// rows, right: columns)
+static void add_outer(bool left, const std::vector<Superblock::Sector>& sec, const double* phi, double alpha,
+                      std::vector<std::vector<double>>& rho) {
+  for (const auto& S : sec) {
+    const double* p = phi + S.offset;
+    if (left)
+      dgemm(false, true, S.rows, S.rows, S.cols, alpha, p, S.cols, p, S.cols, 1.0, rho[S.lq].data(), S.rows);
+    else
+      dgemm(true, false, S.cols, S.cols, S.rows, alpha, p, S.cols, p, S.cols, 1.0, rho[S.rq].data(), S.cols);
+  }
+}
+
+// Noise of the density matrix (add_onedot_noise, density.C:330-421;
+// add_twodot_noise, density.C:92-165); see NoiseSpec.
+void CpuEngine::add_noise(const Superblock& sb, bool left, std::vector<std::vector<double>>& rho) {
+  const Block& B = left ? *sb.L : *sb.R;
+  const int nq = B.si.size();
+  const int nroots = (int)waves_.size();
+  const PointGroup& g = noise_.group;
+  if (noise_.perturbative > 0.0) {
+    const std::vector<NoiseOp> ops = perturbative_noise_ops(B, sb.target, noise_.orbsym, g);
+    for (int r = 0; r < nroots; ++r) {
+      std::vector<std::vector<double>> nm(nq);
+      for (int q = 0; q < nq; ++q) nm[q].assign((size_t)B.si.states[q] * B.si.states[q], 0.0);
+      for (const NoiseOp& no : ops) {
+        int64_t size = 0;
+        const auto sec = wave_sectors(sb.L->si, sb.R->si, no.q, g, size);
+        if (size == 0) continue;
+        std::vector<double> phi(size);
+        apply_one(sb, left, op(no.key, no.trans), waves_[r], sec, no.q.s2, phi);
+        double nrm = 0.0;
+        for (double x : phi) nrm += x * x;
+        if (std::fabs(nrm) > 1e-15) add_outer(left, sec, phi.data(), 1.0 / nrm, nm);
+      }
+      double tr = 0.0;
+      for (int q = 0; q < nq; ++q)
+        for (int i = 0; i < B.si.states[q]; ++i) tr += nm[q][(size_t)i * B.si.states[q] + i];
+      if (tr > 1.0) {
+        const double a = noise_.perturbative / nroots / tr;
+        for (int q = 0; q < nq; ++q)
+          for (size_t e = 0; e < nm[q].size(); ++e) rho[q][e] += a * nm[q][e];
+      }
+    }
+  }
+  if (noise_.random > 0.0) {
+    const std::vector<Quantum> qs = random_noise_quanta(sb.target);
+    for (int r = 0; r < nroots; ++r)
+      for (int i = 0; i < (int)qs.size(); ++i) {
+        int64_t size = 0;
+        const auto sec = wave_sectors(sb.L->si, sb.R->si, qs[i], g, size);
+        if (size == 0) continue;
+        std::vector<double> phi(size);
+        const uint64_t seed = noise_.seed + 0x632BE59BD9B4E019ull * (uint64_t)r;
+        double nrm = 0.0;
+        for (int64_t e = 0; e < size; ++e) {
+          phi[e] = noise_uniform(seed, i, e);
+          nrm += phi[e] * phi[e];
+        }
+        if (std::fabs(nrm) > 1e-15)
+          add_outer(left, sec, phi.data(), noise_.random / nroots / (double)qs.size() / nrm, rho);
+      }
   }
 }
 
@@ -486,6 +608,7 @@ void CpuEngine::set_rotation(const std::vector<std::vector<double>>& rot, const 
 // (SparseMatrix::renormalise_transform, BaseOperator.C:341-363;
 // MatrixRotate, MatrixBLAS.C:553-572).
 void CpuEngine::renormalise(Block& small, const Block& big) {
+  if (structure_only) return;
   std::vector<double>& S = store_.at(small.handle);
   const std::vector<double>& Bg = store_.at(big.handle);
   std::vector<std::pair<const OpKey*, const OpEntry*>> list;

@@ -56,12 +56,20 @@ class CpuEngine : public Engine {
   const std::vector<std::vector<double>>& density_vectors() const { return dm_vecs_; }
   const std::vector<std::vector<double>>& rotation() const { return rot_; }
   const std::vector<int>& rotation_kept() const { return rot_kept_; }
+  // structure only: blocks keep their state spaces and catalogues but no
+  // arenas, and builds / renormalisations do no arithmetic (a superblock of
+  // the right shape for timing, filled afterwards by fill_random)
+  bool structure_only = false;
+  void fill_random(Block& b, uint64_t seed);
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
   double last_sigma_flops = 0.0;  // GEMM flops of the last sigma (2mnk per product)
   int threads = 1;
 
  private:
+  void add_noise(const Superblock& sb, bool left, std::vector<std::vector<double>>& rho);
+  void apply_one(const Superblock& sb, bool left, const Operand& o, const std::vector<double>& psi,
+                 const std::vector<Superblock::Sector>& out, int s2_out, std::vector<double>& phi);
   std::map<int, std::vector<double>> store_;
   int next_handle_ = 0;
   std::vector<std::vector<double>> waves_;

@@ -120,6 +120,14 @@ int oracle_use_blas(const char* path) {
   return 0;
 }
 
+static std::vector<double> g_last_sweep_energies;  // per sweep, lowest root, of the last oracle_run
+
+// the per-sweep energies of the last oracle_run (returns how many; copies up to cap)
+int oracle_sweep_energies(double* out, int cap) {
+  for (int i = 0; i < cap && i < (int)g_last_sweep_energies.size(); ++i) out[i] = g_last_sweep_energies[i];
+  return (int)g_last_sweep_energies.size();
+}
+
 int oracle_run(const char* conf, int threads, int verbose, double* energies, int max_roots, double* stats) {
   try {
     auto t0 = std::chrono::steady_clock::now();
@@ -133,6 +141,7 @@ int oracle_run(const char* conf, int threads, int verbose, double* energies, int
       SweepDriver drv(I, c, eng, opt);
       r = drv.run();
     }
+    g_last_sweep_energies = r.sweep_energies;
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {
       stats[0] = r.sweeps;
@@ -384,7 +393,8 @@ void put_block(BlockCase& c, const std::string& name, const Block& b, oracle::Cp
 }  // namespace
 
 extern "C" {
-void* oracle_block_case(const char* conf, int partition, int threads) {
+void* oracle_block_case(const char* conf, int partition, int threads, double noise, double random_noise,
+                        unsigned long long seed) {
   auto bc = std::make_unique<BlockCase>();
   try {
     Config c = parse_config(conf);
@@ -433,8 +443,16 @@ void* oracle_block_case(const char* conf, int partition, int threads) {
     for (auto& x : psi) x /= std::sqrt(nrm);
     bc->reals["psi"] = psi;
     eng.set_wavefunctions({psi});
+    NoiseSpec ns;
+    ns.perturbative = noise;
+    ns.random = random_noise;
+    ns.seed = seed;
+    ns.orbsym = I.orbsym;
+    ns.group = PointGroup::from_name(c.sym);
+    eng.set_noise(ns);
     DensitySpectrum spec;
     eng.density(sb, /*left=*/true, {1.0}, spec);
+    eng.set_noise(NoiseSpec{});
     std::vector<double> rho, vecs, eig;
     for (const auto& m : eng.density_matrices()) rho.insert(rho.end(), m.begin(), m.end());
     for (const auto& m : eng.density_vectors()) vecs.insert(vecs.end(), m.begin(), m.end());
@@ -503,4 +521,58 @@ void oracle_case_get(void* h, const char* name, int kind, void* out) {
 }
 
 const char* oracle_case_group(void* h) { return static_cast<BlockCase*>(h)->group.c_str(); }
+}  // extern "C"
+
+extern "C" {
+// Timing sample of the oracle sigma on the superblock of `partition` with
+// the sector structure, operator catalogue and operator-pair list of the
+// seeded warm-up chain (the superblock bgpu_prepare_superblock builds), but
+// with seeded random operator values: the warm-up's renormalisations are
+// skipped, which makes a large bond dimension preparable in seconds, and
+// sigma's cost does not depend on the values.  out[0] = FP64 flops of one
+// product, out[1] = psi elements, out[2] = operator doubles of L and R,
+// out[3] = seconds per product over `reps` products, out[4] = norm of the
+// last sigma (a checksum), out[5] = threads.  Returns 0 on success.
+int oracle_sample_sigma(const char* conf, int partition, int threads, int reps, double* out) {
+  try {
+    Config c = parse_config(conf);
+    Integrals I = load_integrals(c);
+    oracle::CpuEngine eng(threads);
+    eng.structure_only = true;
+    SweepDriver drv(I, c, eng);
+    Block L, R;
+    Superblock sb = drv.prepare_partition(partition, L, R);
+    sb.L = &L;
+    sb.R = &R;
+    eng.structure_only = false;
+    eng.fill_random(L, c.seed + 1);
+    eng.fill_random(R, c.seed + 2);
+    Rng rng(c.seed + 99991);
+    std::vector<double> psi(sb.size), sig(sb.size, 0.0);
+    double nrm = 0.0;
+    for (auto& x : psi) {
+      x = rng.normal();
+      nrm += x * x;
+    }
+    for (auto& x : psi) x /= std::sqrt(nrm);
+    if (reps < 1) reps = 1;
+    auto t0 = std::chrono::steady_clock::now();
+    for (int r = 0; r < reps; ++r) eng.sigma(sb, psi.data(), sig.data());
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() / reps;
+    double sn = 0.0;
+    for (double x : sig) sn += x * x;
+    out[0] = eng.last_sigma_flops;
+    out[1] = (double)sb.size;
+    out[2] = (double)(L.ops.arena + R.ops.arena);
+    out[3] = secs;
+    out[4] = std::sqrt(sn);
+    out[5] = eng.threads;
+    eng.release_block(L);
+    eng.release_block(R);
+    return 0;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "oracle_sample_sigma: %s\n", e.what());
+    return 1;
+  }
+}
 }  // extern "C"

@@ -131,8 +131,12 @@ def run(conf, threads=0, verbose=0, max_roots=32):
     if rc != 0:
         raise RuntimeError("oracle run failed for " + conf)
     n = int(st[7])
+    L.oracle_sweep_energies.restype = ctypes.c_int
+    L.oracle_sweep_energies.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    sw = np.zeros(256)
+    ns = L.oracle_sweep_energies(sw.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(sw))
     return e[:n].copy(), dict(sweeps=int(st[0]), sigma_calls=int(st[1]), sigma_seconds=st[2], seconds=st[4],
-                              discarded=st[5], last_sweep_energy=st[6])
+                              discarded=st[5], last_sweep_energy=st[6], sweep_energies=sw[:min(ns, 256)].copy())
 
 
 def _ptr(a, t):
@@ -191,22 +195,24 @@ def time_sigma(conf, sweep, pos, threads=0, reps=3):
     return lib().oracle_time_sigma(conf.encode(), sweep, pos, threads, reps)
 
 
-def block_case(conf, partition, threads=0):
+def block_case(conf, partition, threads=0, noise=0.0, random_noise=0.0, seed=0):
     """Element-wise parity case at `partition` of a configuration's warm-up
     chain (see oracle_block_case): system, dot, enlarged and renormalised
     blocks (quanta, states, keys, sites, arenas), the environment block's
-    state space, a random wavefunction, its left density matrix with
-    eigenvalues and eigenvectors, and the kept rotation."""
+    state space, a random wavefunction, its left density matrix (with the
+    given perturbative / random noise and seed) with eigenvalues and
+    eigenvectors, and the kept rotation."""
     L = lib()
     L.oracle_block_case.restype = ctypes.c_void_p
-    L.oracle_block_case.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    L.oracle_block_case.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_ulonglong]
     L.oracle_case_len.restype = ctypes.c_int64
     L.oracle_case_len.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
     L.oracle_case_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p]
     L.oracle_case_free.argtypes = [ctypes.c_void_p]
     L.oracle_case_group.restype = ctypes.c_char_p
     L.oracle_case_group.argtypes = [ctypes.c_void_p]
-    h = L.oracle_block_case(conf.encode(), partition, threads)
+    h = L.oracle_block_case(conf.encode(), partition, threads, float(noise), float(random_noise), int(seed))
     if not h:
         raise RuntimeError("oracle block case failed")
     out = {"group": L.oracle_case_group(h).decode()}
@@ -229,3 +235,17 @@ def block_case(conf, partition, threads=0):
         out[b + "_quanta"] = out[b + "_quanta"].reshape(-1, 3)
         out[b + "_keys"] = out[b + "_keys"].reshape(-1, 4)
     return out
+
+
+def sample_sigma(conf, partition, threads=0, reps=1):
+    """Oracle sigma timed on a superblock with the structure of `partition`'s
+    warm-up superblock and seeded random operator values (see
+    oracle_sample_sigma): dict(flops, psi, arena, seconds, norm, threads)."""
+    L = lib()
+    L.oracle_sample_sigma.restype = ctypes.c_int
+    L.oracle_sample_sigma.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_double)]
+    out = np.zeros(6)
+    if L.oracle_sample_sigma(conf.encode(), partition, threads, reps, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))):
+        raise RuntimeError("oracle sample failed for " + conf)
+    return dict(flops=out[0], psi=int(out[1]), arena=int(out[2]), seconds=out[3], norm=out[4], threads=int(out[5]))

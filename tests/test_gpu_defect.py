@@ -1,0 +1,99 @@
+"""Defect correction of split-precision Davidson solves against FP64
+residuals, and split-precision sweeps against FP64 sweeps.
+
+A split-precision solve (bf16 or fp16 slices on the tensor cores) ends only
+when its Ritz vectors, given FP64 products, meet the solve's tolerance on
+the squared FP64 residual norm |H psi - E psi|^2 without a further basis
+vector (the convergence test of linear.C:301-335 applied to the FP64
+residual).  Tolerances written here:
+  - the returned vectors' squared FP64 residual within the solve's tol;
+  - energies within 1e-10 Eh of the FP64 solve on the same superblock;
+  - sweep by sweep, split-precision sweep energies within 1e-6 Eh of the
+    FP64 GPU sweeps, on two truncating cases (discarded weights 1e-4 and
+    1e-2), and the FP64 GPU sweeps within 1e-9 Eh of the oracle's.  These
+    sweeps are far from converged, so two runs can differ by more than 1e-6
+    only because their Davidson vectors differ within the solver tolerance;
+    the cases therefore converge every step to 1e-12 and start every solve
+    from the oracle's unit-vector guess.
+"""
+import numpy as np
+import pytest
+
+from conftest import conf
+from test_gpu_sigma import SNAPS, load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def split_ctx(gpu_ctx):
+    yield gpu_ctx
+    gpu_ctx.set_precision("fp64")
+    gpu_ctx.set_refinement("defect")
+
+
+@pytest.mark.parametrize("prec", ["bf16x3tc", "fp16x2tc", "bf16x3"])
+@pytest.mark.parametrize("name,sweep,pos", SNAPS[:3])
+def test_split_davidson_meets_fp64_residual(split_ctx, oracle, prec, name, sweep, pos):
+    snap = oracle.snapshot(conf(name), sweep, pos)
+    sb, n = load(split_ctx, snap)
+    tol = 1e-10
+    e64, _, _ = split_ctx.davidson(sb, n, nroots=1, tol=tol)
+    split_ctx.set_precision(prec)
+    r0, f0, _ = split_ctx.refinement_stats()
+    e, v, _ = split_ctx.davidson(sb, n, nroots=1, tol=tol, vectors=True)
+    rounds, fp64, verified = split_ctx.refinement_stats()
+    assert verified and rounds > r0 and fp64 > f0
+    split_ctx.set_precision("fp64")
+    r = split_ctx.sigma(sb, v[0]) - e[0] * v[0]
+    assert r @ r <= tol, (prec, name, r @ r)
+    assert abs(e[0] - e64[0]) <= 1e-10, (prec, name, e[0], e64[0])
+
+
+def test_two_roots_meet_fp64_residual(split_ctx, oracle):
+    snap = oracle.snapshot(conf("c2_d2h"), 5, 5)
+    sb, n = load(split_ctx, snap)
+    tol = 1e-10
+    e64, _, _ = split_ctx.davidson(sb, n, nroots=2, tol=tol)
+    split_ctx.set_precision("bf16x3tc")
+    e, v, _ = split_ctx.davidson(sb, n, nroots=2, tol=tol, vectors=True)
+    assert split_ctx.refinement_stats()[2]
+    split_ctx.set_precision("fp64")
+    for i in range(2):
+        r = split_ctx.sigma(sb, v[i]) - e[i] * v[i]
+        assert r @ r <= tol, (i, r @ r)
+        assert abs(e[i] - e64[i]) <= 1e-10, (i, e[i], e64[i])
+
+
+def test_energy_only_refinement_mode(split_ctx, oracle):
+    """The former refinement (one FP64 Rayleigh quotient per root) stays
+    selectable; its energy is second order in the split vector's error."""
+    snap = oracle.snapshot(conf("hubbard"), 1, 3)
+    sb, n = load(split_ctx, snap)
+    e64, _, _ = split_ctx.davidson(sb, n, nroots=1, tol=1e-12)
+    split_ctx.set_precision("bf16x3tc")
+    split_ctx.set_refinement("energy")
+    r0, f0, _ = split_ctx.refinement_stats()
+    e, _, _ = split_ctx.davidson(sb, n, nroots=1, tol=1e-10)
+    assert split_ctx.refinement_stats()[:2] == (r0, f0)  # no defect-correction round
+    assert abs(e[0] - e64[0]) <= 1e-8
+
+
+@pytest.mark.parametrize("name", ["c2_d2h_m50", "syn16_m200"])
+def test_split_sweeps_track_fp64_sweeps(split_ctx, oracle, name):
+    split_ctx.set_guess(False)
+    try:
+        e64, st64 = split_ctx.run_dmrg(conf(name))
+        split_ctx.set_precision("bf16x3tc")
+        es, sts = split_ctx.run_dmrg(conf(name))
+    finally:
+        split_ctx.set_guess(True)
+    s64, ss = st64["sweep_energies"], sts["sweep_energies"]
+    assert len(s64) == len(ss) >= 4
+    for i, (a, b) in enumerate(zip(s64, ss)):
+        assert abs(a - b) <= 1e-6, (name, i, a, b)
+    for a, b in zip(e64, es):
+        assert abs(a - b) <= 1e-6, (name, a, b)
+    eo, sto = oracle.run(conf(name))
+    for i, (a, b) in enumerate(zip(s64, sto["sweep_energies"])):
+        assert abs(a - b) <= 1e-9, (name, i, a, b)
