@@ -386,7 +386,7 @@ def run_ours(a):
         # baseline (one launch per sector, one block per tile), and the
         # autotuned knobs against the defaults
         sched = {"autotuned": not a.no_autotune,
-                 "knobs": {k: info[k] for k in ("tc_item_cost", "tc_split", "tc_group")},
+                 "knobs": {k: info[k] for k in ("tc_item_cost", "tc_split", "tc_group", "tc_nb")},
                  "launches_per_sigma": info["launches"], "ms_per_sigma": t_step * 1e3}
         reps = 2
         ctx.set_autotune(False)
@@ -399,7 +399,7 @@ def run_ours(a):
         ms_d = ctx.sigma_timed(sb, x, y, reps)
         info_d = ctx.superblock_info(sb)
         sched["default_knobs"] = {"ms_per_sigma": ms_d[0] / reps,
-                                  "knobs": {k: info_d[k] for k in ("tc_item_cost", "tc_split", "tc_group")}}
+                                  "knobs": {k: info_d[k] for k in ("tc_item_cost", "tc_split", "tc_group", "tc_nb")}}
         if not a.no_autotune:
             ctx.set_autotune(True)
             ctx.sigma_timed(sb, x, y, 1)  # cached knobs back on the plan

@@ -154,6 +154,14 @@ int bgpu_set_tc_schedule(bgpu_ctx* ctx, int mode) {
   });
 }
 
+int bgpu_set_tc_tile_width(bgpu_ctx* ctx, int nb) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    need(nb == 0 || nb == dev::kTcRowsB || nb == dev::kTcRowsBWide, "tile width must be 0 (automatic), 64 or 128");
+    ctx->eng->tc_nb_mode = nb;
+  });
+}
+
 int bgpu_set_autotune(bgpu_ctx* ctx, int on, const char* cache_path) {
   return guarded(ctx, [&] {
     need(ctx->eng != nullptr, "no device");
@@ -431,7 +439,7 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
     auto& r = *it->second;
     if (!r.plan.tc) ctx->eng->plan_tc(r.sb, r.plan);
     const SigmaPlan& p = r.plan;
-    const double v[21] = {p.flops,
+    const double v[22] = {p.flops,
                           p.bytes,
                           p.tc_mma_flops,
                           (double)p.tc_stats[0],
@@ -451,8 +459,9 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
                           (double)p.tc_knobs.per_sector,
                           p.tc_tuned ? 1.0 : 0.0,
                           (double)ctx->eng->sigma_launches(p),
-                          (double)p.scratch_elems};
-    for (int i = 0; i < n; ++i) info[i] = i < 21 ? v[i] : 0.0;
+                          (double)p.scratch_elems,
+                          (double)p.tc_nb};
+    for (int i = 0; i < n; ++i) info[i] = i < 22 ? v[i] : 0.0;
   });
 }
 

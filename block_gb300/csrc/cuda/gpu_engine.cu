@@ -1071,12 +1071,33 @@ struct TcHostPlan {
   double mma1 = 0.0;  // tensor-core flops of phase 1
 };
 
+// Output-tile width of a new plan: BGPU_TC_NB or tc_nb_mode when set, else
+// 128 when most of sigma's stage-2 work lies in sectors at least 128 columns
+// wide (there a 128 x 128 tile reads each A piece once for twice the MMA
+// work), otherwise 64 (two pipelines per SM hide the per-item latency of
+// small sectors).
+int GpuEngine::tc_choose_nb(const Superblock& sb) const {
+  const int env = (int)env_double("BGPU_TC_NB", 0.0);
+  if (env == 64 || env == 128) return env;
+  if (tc_nb_mode == 64 || tc_nb_mode == 128) return tc_nb_mode;
+  double wide = 0.0, all = 0.0;
+  for (const auto& S : sb.sectors) {
+    const double w = (double)S.rows * S.cols * S.cols;
+    all += w;
+    if (S.cols >= 128) wide += w;
+  }
+  return all > 0.0 && wide >= 0.5 * all ? dev::kTcRowsBWide : dev::kTcRowsB;
+}
+
 void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   PlanTimer timer_(plan_seconds);
   PlanLaps laps{"tc"};
   using namespace dev;
   const Block& L = *sb.L;
   const Block& R = *sb.R;
+  if (!plan.tc_nb_set) plan.tc_nb = tc_choose_nb(sb);
+  if (plan.tc_nb != kTcRowsB && plan.tc_nb != kTcRowsBWide) plan.tc_nb = kTcRowsB;
+  const int nb = plan.tc_nb;
   const auto by_l = sectors_by_left(sb);
   const int nsec = (int)sb.sectors.size();
   std::vector<std::vector<Coupling>> per_t(sb.terms.size());
@@ -1104,7 +1125,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     p.rows_p = tc_round8(v.rows);
     p.kp = tc_round16(v.cols);
     p.trans = v.trans ? 1 : 0;
-    p.rt = pool == kTcPoolL ? kTcRowsA : kTcRowsB;  // L blocks are A operands, R blocks B operands
+    p.rt = pool == kTcPoolL ? kTcRowsA : nb;  // L blocks are A operands, R blocks B operands
     p.src = (uint8_t)pool;  // 0: L arena, 1: R arena
     p.pool = (uint8_t)pool;
     p.dst_off = pool_n[pool];
@@ -1136,7 +1157,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     t.cols_v = S.rows;
     t.rows_p = tc_round8(S.cols);
     t.kp = tc_round16(S.rows);
-    t.rt = kTcRowsB;
+    t.rt = nb;
     t.dst_off = psit_off[s] = pool_n[kTcPoolPsiT];
     pool_n[kTcPoolPsiT] += 2 * (int64_t)t.rows_p * t.kp;
     psi_packs.push_back(t);
@@ -1208,7 +1229,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         const int idx = (int)i1.size();
         i1.push_back(a);
         for (int tm = 0; tm < (mr + 127) / 128; ++tm)
-          for (int tn = 0; tn < (mc + kTcRowsB - 1) / kTcRowsB; ++tn) {
+          for (int tn = 0; tn < (mc + nb - 1) / nb; ++tn) {
             TcTask t{};
             t.a_rows = rows_p;
             t.b_rows = tc_round8(mc);
@@ -1221,7 +1242,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
             t1.push_back(t);
             sec1.push_back(c.cs);
             bundle1.push_back((cur_s << 8) | tm);
-            mma += 3.0 * 2.0 * 128 * tc_round16(std::min(kTcRowsB, t.b_rows - kTcRowsB * tn)) * a.kp;
+            mma += 3.0 * 2.0 * 128 * tc_round16(std::min(nb, t.b_rows - nb * tn)) * a.kp;
           }
         cur_l = c.lQ;
         cur_lp = c.lQp;
@@ -1345,6 +1366,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   const auto& per_sector = H.per_sector;
   const int nsec = (int)sb.sectors.size();
   const int nsm = sm_count();
+  const int nb = plan.tc_nb;  // fixed by the packing of the B-role pools
   const bool seq = kn.per_sector != 0;
   const double item_fixed = kn.item_cost;
   auto item_cost = [&](const TcItem& it, int hb) { return item_fixed + (double)it.kp * tc_round16(hb) / 8.0; };
@@ -1361,8 +1383,8 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   double total = 0.0;
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
-    for (int tn = 0; tn < (S.cols + kTcRowsB - 1) / kTcRowsB; ++tn) {
-      const int hb = std::min(kTcRowsB, tc_round8(S.cols) - kTcRowsB * tn);
+    for (int tn = 0; tn < (S.cols + nb - 1) / nb; ++tn) {
+      const int hb = std::min(nb, tc_round8(S.cols) - nb * tn);
       for (const TcItem& it : per_sector[s]) total += item_cost(it, hb) * ((S.rows + 127) / 128);
     }
   }
@@ -1374,8 +1396,8 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
     const int ie = (int)i2.size();
     const int rows_p = tc_round8(S.rows), cols_p = tc_round8(S.cols);
     for (int tm = 0; tm < (S.rows + 127) / 128; ++tm)
-      for (int tn = 0; tn < (S.cols + kTcRowsB - 1) / kTcRowsB; ++tn) {
-        const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(kTcRowsB, cols_p - kTcRowsB * tn);
+      for (int tn = 0; tn < (S.cols + nb - 1) / nb; ++tn) {
+        const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(nb, cols_p - nb * tn);
         double tile_cost = 0.0;
         for (int x = ib; x < ie; ++x) tile_cost += item_cost(i2[x], hb);
         TcTask t{};
@@ -1384,7 +1406,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
         t.tm = tm;
         t.tn = tn;
         t.valid_rows = std::min(128, S.rows - 128 * tm);
-        t.valid_cols = std::min(kTcRowsB, S.cols - kTcRowsB * tn);
+        t.valid_cols = std::min(nb, S.cols - nb * tn);
         for (int x = ib; x < ie; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
         if (tile_cost <= chunk || ie - ib <= 1) {
           t.ibeg = ib;
@@ -1404,7 +1426,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
         tl.h = t.valid_rows;
         tl.w = t.valid_cols;
         tl.r0 = 128 * tm;
-        tl.c0 = kTcRowsB * tn;
+        tl.c0 = nb * tn;
         tl.pad = hb;  // row stride of the partial slots
         tl.pbeg = (int)slots.size();
         int x0 = ib;
@@ -1431,23 +1453,23 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   }
   std::vector<double> c1;
   for (const TcTask& t : t1)
-    c1.push_back(item_cost(i1[t.ibeg], std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn)) + 200.0);
+    c1.push_back(item_cost(i1[t.ibeg], std::min(nb, t.b_rows - nb * t.tn)) + 200.0);
   laps.lap("phase-2 tasks");
   // tiles inside their operands (item shapes were checked against their
   // sectors when the items were made)
   for (const TcTask& t : t1)
-    if (kTcRowsA * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows || kTcRowsB * t.tn >= t.out_kp) fail();
+    if (kTcRowsA * t.tm >= t.a_rows || nb * t.tn >= t.b_rows || nb * t.tn >= t.out_kp) fail();
   for (const TcTask& t : t2)
-    if (kTcRowsA * t.tm >= t.a_rows || kTcRowsB * t.tn >= t.b_rows ||
+    if (kTcRowsA * t.tm >= t.a_rows || nb * t.tn >= t.b_rows ||
         (t.direct && (t.valid_rows > std::min(kTcRowsA, t.a_rows - kTcRowsA * t.tm) ||
-                      t.valid_cols > std::min(kTcRowsB, t.b_rows - kTcRowsB * t.tn))))
+                      t.valid_cols > std::min(nb, t.b_rows - nb * t.tn))))
       fail();
   std::vector<int> o1, o2;
   std::vector<int2> r1, r2, l1, l2;
   if (!seq) {
-    // two persistent blocks per SM (each kernel block runs its own pipeline)
-    schedule_lpt(c1, H.bundle1, 2 * nsm, o1, r1);
-    schedule_lpt(c2, bundle2, 2 * nsm, o2, r2);
+    // persistent blocks: two per SM with 64-column tiles, one with 128
+    schedule_lpt(c1, H.bundle1, tc_blocks_per_sm(nb) * nsm, o1, r1);
+    schedule_lpt(c2, bundle2, tc_blocks_per_sm(nb) * nsm, o2, r2);
   } else {
     // one block per task, tasks grouped by sector, one launch per group
     auto by_sector = [](const std::vector<int>& sec, std::vector<int>& o, std::vector<int2>& r,
@@ -1499,15 +1521,15 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
         const TcTask& T = tasks[order[k]];
         TcWork base{};
         base.h_a = (int16_t)std::min(kTcRowsA, T.a_rows - kTcRowsA * T.tm);
-        base.h_b = (int16_t)std::min(kTcRowsB, T.b_rows - kTcRowsB * T.tn);
+        base.h_b = (int16_t)std::min(nb, T.b_rows - nb * T.tn);
         base.valid_rows = (int16_t)T.valid_rows;
         base.valid_cols = (int16_t)T.valid_cols;
         if (phase == 1) {
           base.out_base = T.out_off + 2 * (int64_t)kTcRowsA * T.tm * T.out_kp;
           base.out_ld = T.out_kp;
-          base.col0 = kTcRowsB * T.tn;
+          base.col0 = nb * T.tn;
         } else if (T.direct) {
-          base.out_base = T.out_off + (int64_t)kTcRowsA * T.tm * T.out_kp + kTcRowsB * T.tn;
+          base.out_base = T.out_off + (int64_t)kTcRowsA * T.tm * T.out_kp + nb * T.tn;
           base.out_ld = T.out_kp;
         } else {
           base.out_base = T.out_off;
@@ -1525,7 +1547,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
           const TcItem& it = items[i];
           TcWork x = base;
           x.a_base = it.a_off + 2 * (int64_t)kTcRowsA * T.tm * it.kp;
-          x.b_base = it.b_off + 2 * (int64_t)kTcRowsB * T.tn * it.kp;
+          x.b_base = it.b_off + 2 * (int64_t)nb * T.tn * it.kp;
           x.kp = it.kp;
           x.alpha = it.alpha;
           x.a_pool = it.a_pool;
@@ -1565,6 +1587,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   plan.tc_l1 = std::move(l1);
   plan.tc_l2 = std::move(l2);
   plan.tc_knobs = kn;
+  plan.tc_knobs.nb = nb;
   {
     int64_t full = 0;
     for (const TcItem& it : i2) full += it.a_pool == kTcPoolS ? 1 : 0;
@@ -1589,23 +1612,34 @@ std::string GpuEngine::tc_tune_key(const Superblock& sb, const SigmaPlan& p) con
   };
   std::map<std::pair<int, int>, int> hist;
   for (const auto& S : sb.sectors) ++hist[{oct(S.rows), oct(S.cols)}];
-  std::string k = std::string(p.tc_fp16 ? "fp16" : "bf16") + "/w" + std::to_string(oct(p.tc_mma_flops));
+  std::string k = std::string(p.tc_fp16 ? "fp16" : "bf16") + "/w" + std::to_string(oct(p.flops));
   for (const auto& h : hist)
     k += "/" + std::to_string(h.first.first) + "x" + std::to_string(h.first.second) + ":" + std::to_string(oct(h.second));
   return k;
 }
 
-// Coordinate search over the schedule knobs (LPT item cost, phase-2 split,
+// Tile shape and schedule knobs: for each output-tile width (64 columns with
+// two pipelines per SM, 128 with one; the pools are packed again for each),
+// a coordinate search over the schedule knobs (LPT item cost, phase-2 split,
 // accumulation group), each candidate timed by CUDA events over three
 // products on the plan's own operators; a candidate replaces the best one
-// when it is at least 2 % faster.  Keys seen before reuse their knobs.
+// when it is at least 2 % faster.  Keys seen before reuse their choice.
 void GpuEngine::autotune_tc(const Superblock& sb, SigmaPlan& p) {
   p.tc_tuned = true;  // also stops sigma_tc from re-entering
   const std::string key = tc_tune_key(sb, p);
+  auto use_nb = [&](int nb) {
+    if (p.tc_nb == nb && p.tc) return;
+    free_tc(p);
+    p.tc_nb = nb;
+    p.tc_nb_set = true;
+    plan_tc(sb, p);
+    p.tc_tuned = true;
+  };
   auto it = tune_cache.find(key);
   if (it != tune_cache.end()) {
     TcKnobs k = it->second;
     k.per_sector = 0;
+    use_nb(k.nb);
     if (!(k == p.tc_knobs)) schedule_tc(sb, p, k);
     return;
   }
@@ -1627,27 +1661,38 @@ void GpuEngine::autotune_tc(const Superblock& sb, SigmaPlan& p) {
     cuda_check(cudaEventElapsedTime(&ms, e[0], e[1]), "elapsed");
     return (double)ms;
   };
-  TcKnobs best = p.tc_knobs;
-  best.per_sector = 0;
-  if (!(best == p.tc_knobs)) schedule_tc(sb, p, best);
-  double tbest = measure();
   const double costs[] = {150.0, 400.0, 1000.0};
   const double splits[] = {1.5, 3.0, 6.0};
   const int groups[] = {8, 16, 32};
-  for (int axis = 0; axis < 3; ++axis)
-    for (int v = 0; v < 3; ++v) {
-      TcKnobs c = best;
-      if (axis == 0) c.item_cost = costs[v];
-      if (axis == 1) c.split = splits[v];
-      if (axis == 2) c.group = groups[v];
-      if (c == best) continue;
-      schedule_tc(sb, p, c);
-      const double t = measure();
-      if (t < 0.98 * tbest) {
-        best = c;
-        tbest = t;
+  TcKnobs best;
+  double tbest = 1e300;
+  const int first_nb = p.tc_nb;
+  for (int nb : {first_nb, first_nb == dev::kTcRowsB ? dev::kTcRowsBWide : dev::kTcRowsB}) {
+    use_nb(nb);
+    TcKnobs b = p.tc_knobs;
+    b.per_sector = 0;
+    if (!(b == p.tc_knobs)) schedule_tc(sb, p, b);
+    double tb = measure();
+    for (int axis = 0; axis < 3; ++axis)
+      for (int v = 0; v < 3; ++v) {
+        TcKnobs c = b;
+        if (axis == 0) c.item_cost = costs[v];
+        if (axis == 1) c.split = splits[v];
+        if (axis == 2) c.group = groups[v];
+        if (c == b) continue;
+        schedule_tc(sb, p, c);
+        const double t = measure();
+        if (t < 0.98 * tb) {
+          b = c;
+          tb = t;
+        }
       }
+    if (tb < 0.98 * tbest || nb == first_nb) {
+      best = b;
+      tbest = tb;
     }
+  }
+  use_nb(best.nb);
   if (!(best == p.tc_knobs)) schedule_tc(sb, p, best);
   for (auto& v : e) cudaEventDestroy(v);
   free(x);
@@ -1658,7 +1703,7 @@ void GpuEngine::autotune_tc(const Superblock& sb, SigmaPlan& p) {
   tune_cache[key] = best;
   if (!tune_cache_path.empty()) {
     if (FILE* f = std::fopen(tune_cache_path.c_str(), "a")) {
-      std::fprintf(f, "%s %.17g %.17g %d\n", key.c_str(), best.item_cost, best.split, best.group);
+      std::fprintf(f, "%s %.17g %.17g %d %d\n", key.c_str(), best.item_cost, best.split, best.group, best.nb);
       std::fclose(f);
     }
   }
@@ -1671,10 +1716,14 @@ void GpuEngine::load_tune_cache(const std::string& path) {
   if (path.empty()) return;
   FILE* f = std::fopen(path.c_str(), "r");
   if (!f) return;
-  char key[4096];
-  TcKnobs k;
-  while (std::fscanf(f, "%4095s %lf %lf %d", key, &k.item_cost, &k.split, &k.group) == 4) {
-    if (k.item_cost > 0 && k.split > 0 && k.group > 0) tune_cache[key] = k;
+  char line[8192], key[4096];
+  while (std::fgets(line, sizeof(line), f)) {
+    TcKnobs k;
+    const int got = std::sscanf(line, "%4095s %lf %lf %d %d", key, &k.item_cost, &k.split, &k.group, &k.nb);
+    if (got < 4) continue;
+    if (got == 4) k.nb = dev::kTcRowsB;  // files written before the tile width was tuned
+    if (k.item_cost > 0 && k.split > 0 && k.group > 0 && (k.nb == dev::kTcRowsB || k.nb == dev::kTcRowsBWide))
+      tune_cache[key] = k;
   }
   std::fclose(f);
 }
@@ -1682,6 +1731,10 @@ void GpuEngine::load_tune_cache(const std::string& path) {
 void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, double* out, cudaEvent_t* marks) {
   const bool fp16 = precision == Precision::FP16X2_TC;
   if (p.tc && p.tc_fp16 != fp16) free_tc(p);  // operators packed in the other format
+  if (p.tc && tc_nb_mode && tc_nb_mode != p.tc_nb) {  // packed for the other tile width
+    free_tc(p);
+    p.tc_nb_set = false;
+  }
   if (!p.tc) plan_tc(sb, p);
   if (p.tc_knobs.per_sector != (tc_schedule_mode == 1 ? 1 : 0)) {
     TcKnobs k = tc_default_knobs();
@@ -1707,15 +1760,15 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
     // baseline: one launch per psi sector (phase 1) and per sigma sector
     // (phase 2), one block per task
     for (const int2& g : p.tc_l1)
-      cuda_check(dev::launch_tc_sigma(1, b, p.tc_w1.d, p.tc_r1.d + g.x, g.y, out, kWaitLimitNs, stream_),
+      cuda_check(dev::launch_tc_sigma(1, p.tc_nb, b, p.tc_w1.d, p.tc_r1.d + g.x, g.y, out, kWaitLimitNs, stream_),
                  "tc phase 1");
     for (const int2& g : p.tc_l2)
-      cuda_check(dev::launch_tc_sigma(2, b, p.tc_w2.d, p.tc_r2.d + g.x, g.y, out, kWaitLimitNs, stream_),
+      cuda_check(dev::launch_tc_sigma(2, p.tc_nb, b, p.tc_w2.d, p.tc_r2.d + g.x, g.y, out, kWaitLimitNs, stream_),
                  "tc phase 2");
   } else {
-    cuda_check(dev::launch_tc_sigma(1, b, p.tc_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
+    cuda_check(dev::launch_tc_sigma(1, p.tc_nb, b, p.tc_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
                "tc phase 1");
-    cuda_check(dev::launch_tc_sigma(2, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
+    cuda_check(dev::launch_tc_sigma(2, p.tc_nb, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
                "tc phase 2");
   }
   if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");

@@ -60,8 +60,10 @@ struct TcKnobs {
   double split = 3.0;        // phase-2 pieces per persistent block (tile splitting)
   int group = 16;            // items per tensor-core accumulation group
   int per_sector = 0;        // 1: one launch per sector, one block per task (baseline)
+  int nb = 64;               // output-tile width: 64 (two pipelines per SM) or 128 (one, wider MMAs)
   bool operator==(const TcKnobs& o) const {
-    return item_cost == o.item_cost && split == o.split && group == o.group && per_sector == o.per_sector;
+    return item_cost == o.item_cost && split == o.split && group == o.group && per_sector == o.per_sector &&
+           nb == o.nb;
   }
 };
 struct TcHostPlan;  // item lists of a tensor-core plan, kept for rescheduling
@@ -98,6 +100,8 @@ struct SigmaPlan {
   // psi^T packed per product, S = stage-1 products written by phase 1
   bool tc = false;
   bool tc_fp16 = false;  // slices of the packed pools are fp16 (else bf16)
+  int tc_nb = 64;        // output-tile width the pools were packed for (row tile of the B-role pools)
+  bool tc_nb_set = false;  // tc_nb chosen by the autotuner (else plan_tc chooses it)
   __nv_bfloat16* tc_pool[dev::kTcPools] = {};  // packed operands, hi and lo per block
   int64_t tc_pool_elems[dev::kTcPools] = {};
   DevArray<dev::TcPack> tc_psi_pack;
@@ -181,6 +185,10 @@ class GpuEngine : public Engine {
   // tensor-core schedule of new plans: 0 persistent blocks (LPT), 1 one
   // launch per sector (baseline); autotune: tune the knobs of persistent plans
   int tc_schedule_mode = 0;
+  // output-tile width of new plans: 0 chosen from the sector sizes (or by the
+  // autotuner), else 64 or 128
+  int tc_nb_mode = 0;
+  int tc_choose_nb(const Superblock& sb) const;
   bool tc_autotune = false;
   std::map<std::string, TcKnobs> tune_cache;
   std::string tune_cache_path;  // file the cache is read from and appended to

@@ -329,10 +329,27 @@ __global__ void __launch_bounds__(kQlThreads) eig_ql(EigBufs b, const EigJob* __
     __syncthreads();
     if (done) break;
     if (consumer) {
+      // the rotations of a sweep act on columns m-1 .. m-cnt in turn; the
+      // columns of eight rotations are loaded before any of them is applied
+      // (they are not written before their own rotation), so that the loads
+      // overlap instead of each waiting on the previous rotation
       const double* buf = rb + (int64_t)(batch & 1) * 2 * n;
       const int m = bm[batch & 1], cnt = bc[batch & 1];
       double zi1 = Z[(int64_t)m * n + row];
-      for (int x = 0; x < cnt; ++x) {
+      int x = 0;
+      for (; x + 8 <= cnt; x += 8) {
+        double zz[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) zz[u] = Z[(int64_t)(m - 1 - x - u) * n + row];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = m - 1 - x - u;
+          const double c = buf[2 * (x + u)], s = buf[2 * (x + u) + 1];
+          Z[(int64_t)(i + 1) * n + row] = s * zz[u] + c * zi1;
+          zi1 = c * zz[u] - s * zi1;
+        }
+      }
+      for (; x < cnt; ++x) {
         const int i = m - 1 - x;
         const double c = buf[2 * x], s = buf[2 * x + 1];
         const double zi = Z[(int64_t)i * n + row];

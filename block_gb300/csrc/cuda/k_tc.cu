@@ -214,19 +214,27 @@ cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cud
 
 namespace {
 
-// Two independent blocks per SM, each with its own pipeline.
-constexpr int kTcSlots = 4;  // stages of the operand ring
-// one stage holds the largest piece: A (128 rows) and B (64 rows) x 32 columns, hi and lo
-constexpr uint32_t kTcStageBytes = 2u * (kTcRowsA + kTcRowsB) * kTcKC * 2;
+// Pipeline shape by output-tile width NB (the B operands' row tile): with
+// NB = 64 two independent blocks share an SM (256 TMEM columns and a
+// 4-stage ring each); with NB = 128 one block owns the SM (512 TMEM
+// columns, a 6-stage ring of 32 KB stages).  One stage holds the largest
+// piece: A (128 rows) and B (NB rows) x 32 columns, hi and lo.
+template <int NB>
+struct TcCfg {
+  static constexpr int kSlots = NB == 64 ? 4 : 6;
+  static constexpr uint32_t kStageBytes = 2u * (kTcRowsA + NB) * kTcKC * 2;
+  static constexpr int kSmem = kSlots * (int)kStageBytes;
+  static constexpr uint32_t kTmemCols = 4 * NB;     // two accumulators, then the (hi, lo) sums
+  static constexpr uint32_t kVh = 2 * NB, kVl = 3 * NB;
+  static constexpr int kBlocksPerSm = NB == 64 ? 2 : 1;
+};
+constexpr int kTcMaxSlots = 6;
 constexpr int kTcThreads = 192;  // warps 0-3 epilogue, 4 bulk-copy producer, 5 MMA issuer
 constexpr int kTcProducer = 4, kTcIssuer = 5;
-constexpr int kTcSmem = kTcSlots * kTcStageBytes;
-constexpr int kTcAcc = 2;        // accumulators of 64 TMEM columns
-constexpr uint32_t kTcVh = 128, kTcVl = 192;  // TMEM columns of the compensated (hi, lo) sums
-constexpr uint32_t kTcTmemCols = 256;
+constexpr int kTcAcc = 2;        // accumulators of NB TMEM columns
 
 struct TcShared {
-  uint64_t full[kTcSlots], empty[kTcSlots], acc_full[kTcAcc], acc_empty[kTcAcc], drain;
+  uint64_t full[kTcMaxSlots], empty[kTcMaxSlots], acc_full[kTcAcc], acc_empty[kTcAcc], drain;
   uint32_t tbase;
   int abort_flag;
 };
@@ -285,17 +293,21 @@ __device__ __forceinline__ int shfl32(int v, int j) { return __shfl_sync(0xfffff
 // ranges[j].y), each role loading them 32 at a time, and the pipeline runs
 // across task boundaries.  The epilogue folds each group sum into a
 // compensated (hi, lo) f32 pair held in registers.
-template <int PHASE>
-__global__ void __launch_bounds__(kTcThreads, 2)
+template <int PHASE, int NB>
+__global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
     tc_sigma_kernel(TcBufs b, const TcWork* __restrict__ work, const int2* __restrict__ ranges,
                     double* __restrict__ sigma, uint64_t limit_ns) {
+  using Cfg = TcCfg<NB>;
+  constexpr int kTcSlots = Cfg::kSlots;
+  constexpr uint32_t kTcStageBytes = Cfg::kStageBytes;
+  constexpr uint32_t kTcVh = Cfg::kVh, kTcVl = Cfg::kVl;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ TcShared sh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int2 rg = ranges[blockIdx.x];
-  // TMEM: two accumulators of 64 columns, then the phase-2 (hi, lo) sums
+  // TMEM: two accumulators of NB columns, then the phase-2 (hi, lo) sums
   if (warp == kTcIssuer) {
-    tmem_alloc(&sh.tbase, kTcTmemCols);
+    tmem_alloc(&sh.tbase, Cfg::kTmemCols);
     tmem_relinquish();
   }
   if (tid == 0) {
@@ -382,7 +394,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             ok = false;
           if (ok) {
             fence_after_sync();
-            const uint32_t d = tmem + (uint32_t)ab * 64u;
+            const uint32_t d = tmem + (uint32_t)ab * (uint32_t)NB;
             const int nck = (kp + kTcKC - 1) / kTcKC;
             for (int c = 0; c < nck; ++c, ++k) {
               const int w = min(kTcKC, kp - kTcKC * c);
@@ -421,7 +433,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
     }
   } else {
-    // ---- epilogue: warp w owns TMEM lanes 32 w.., all 64 columns
+    // ---- epilogue: warp w owns TMEM lanes 32 w.., all NB columns, read in
+    // halves of 64 columns
     const int row = 32 * warp + lane;
     const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
     const uint32_t vh_t = tmem + kTcVh + lane_base, vl_t = tmem + kTcVl + lane_base;
@@ -445,108 +458,118 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const int out_ld = shfl32(r.q[2].z, j);
         const int col0 = shfl32(r.q[2].w, j);
         if (flags & kTcFirst) first = true;
-        float v[64];
         const bool have = (flags & kTcGEnd) && !(flags & kTcEmpty);
+        const bool last = (flags & kTcLast) != 0;
         if (have) {
           ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
           if (!ok) break;  // TMEM loads below need the whole warp
           fence_after_sync();
-          const uint32_t d = tmem + (uint32_t)ab * 64u + lane_base;
-#pragma unroll
-          for (int e = 0; e < 64; ++e) v[e] = 0.f;
-          if (ng > 2) {
-            tmem_ld32(d, v);
-            if (ng == 4) tmem_ld32(d + 32u, v + 32);
-            else tmem_ld16(d + 32u, v + 32);
-          } else if (ng == 2) {
-            tmem_ld32(d, v);
-          } else if (ng == 1) {
-            tmem_ld16(d, v);
-          }
-          // accumulator read: the MMA issuer may reuse it
-          fence_before_sync();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
-          if (++ab == kTcAcc) {
-            ab = 0;
-            aph ^= 1u;
-          }
         }
-        if (PHASE == 2) {
-          const bool last = (flags & kTcLast) != 0;
-          if (!have && !last) continue;
+        const uint32_t dacc = tmem + (uint32_t)ab * (uint32_t)NB + lane_base;
+#pragma unroll 1
+        for (int hh = 0; hh < NB / 64; ++hh) {
+          const int ngh = min(max(ng - 4 * hh, 0), 4);  // 16-column groups of this half
+          float v[64];
+          if (have) {
 #pragma unroll
-          for (int g = 0; g < 4; ++g) {
-            if (g < ng) {
-              float vh[16], vl[16];
-              if (first) {
+            for (int e = 0; e < 64; ++e) v[e] = 0.f;
+            const uint32_t d = dacc + 64u * (uint32_t)hh;
+            if (ngh > 2) {
+              tmem_ld32(d, v);
+              if (ngh == 4) tmem_ld32(d + 32u, v + 32);
+              else tmem_ld16(d + 32u, v + 32);
+            } else if (ngh == 2) {
+              tmem_ld32(d, v);
+            } else if (ngh == 1) {
+              tmem_ld16(d, v);
+            }
+            if (hh == NB / 64 - 1) {
+              // accumulator read: the MMA issuer may reuse it
+              fence_before_sync();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&sh.acc_empty[ab]);
+            }
+          }
+          if (PHASE == 2) {
+            if (!have && !last) continue;
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                  vh[e] = have ? __fmul_rn(alpha, v[16 * g + e]) : 0.f;
-                  vl[e] = 0.f;
-                }
-              } else {
-                tmem_ld16x2(vh_t + (uint32_t)(16 * g), vl_t + (uint32_t)(16 * g), vh, vl);
-                if (have) {
-#pragma unroll
-                  for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], __fmul_rn(alpha, v[16 * g + e]));
-                }
-              }
-              if (!last) {
-                tmem_st16(vh_t + (uint32_t)(16 * g), vh);
-                tmem_st16(vl_t + (uint32_t)(16 * g), vl);
-              } else if (flags & kTcDirect) {
-                const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
-                if (row < vrows) {
-                  double* out = sigma + out_base + (int64_t)row * out_ld;
+            for (int g = 0; g < 4; ++g) {
+              if (g < ngh) {
+                const int cb = 64 * hh + 16 * g;  // first column of this group
+                float vh[16], vl[16];
+                if (first) {
 #pragma unroll
                   for (int e = 0; e < 16; ++e) {
-                    const int col = 16 * g + e;
-                    if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
+                    vh[e] = have ? __fmul_rn(alpha, v[16 * g + e]) : 0.f;
+                    vl[e] = 0.f;
+                  }
+                } else {
+                  tmem_ld16x2(vh_t + (uint32_t)cb, vl_t + (uint32_t)cb, vh, vl);
+                  if (have) {
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) two_sum_acc(vh[e], vl[e], __fmul_rn(alpha, v[16 * g + e]));
                   }
                 }
-              } else if (row < h_a) {
-                float2* out = b.partials + out_base + (int64_t)row * h_b;
+                if (!last) {
+                  tmem_st16(vh_t + (uint32_t)cb, vh);
+                  tmem_st16(vl_t + (uint32_t)cb, vl);
+                } else if (flags & kTcDirect) {
+                  const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
+                  if (row < vrows) {
+                    double* out = sigma + out_base + (int64_t)row * out_ld;
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                  const int col = 16 * g + e;
-                  if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                    for (int e = 0; e < 16; ++e) {
+                      const int col = cb + e;
+                      if (col < vcols) out[col] = (double)vh[e] + (double)vl[e];
+                    }
+                  }
+                } else if (row < h_a) {
+                  float2* out = b.partials + out_base + (int64_t)row * h_b;
+#pragma unroll
+                  for (int e = 0; e < 16; ++e) {
+                    const int col = cb + e;
+                    if (col < h_b) out[col] = make_float2(vh[e], vl[e]);
+                  }
                 }
               }
             }
-          }
-          first = false;
-        } else if (have && row < h_a) {
-          // phase 1: S tile written as a packed operand (rows of this tile,
-          // K columns col0.. of S)
-          const int ncols = min(kTcRowsB, out_ld - col0);
-          __nv_bfloat16* sp = b.pool[kTcPoolS] + out_base;
+          } else if (have && row < h_a) {
+            // phase 1: S tile written as a packed operand (rows of this tile,
+            // K columns col0.. of S)
+            const int ncols = min(NB, out_ld - col0);
+            __nv_bfloat16* sp = b.pool[kTcPoolS] + out_base;
 #pragma unroll
-          for (int g8 = 0; g8 < 8; ++g8) {
-            const int c0 = 8 * g8;
-            if (c0 < ncols) {
-              uint32_t hw4[4], lw4[4];
+            for (int g8 = 0; g8 < 8; ++g8) {
+              const int c0 = 64 * hh + 8 * g8;
+              if (c0 < ncols) {
+                uint32_t hw4[4], lw4[4];
 #pragma unroll
-              for (int e = 0; e < 8; ++e) {
-                const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
-                uint32_t bh, bl;
-                split16(x, b.fp16 != 0, bh, bl);
-                if (e & 1) {
-                  hw4[e >> 1] |= bh << 16;
-                  lw4[e >> 1] |= bl << 16;
-                } else {
-                  hw4[e >> 1] = bh;
-                  lw4[e >> 1] = bl;
+                for (int e = 0; e < 8; ++e) {
+                  const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
+                  uint32_t bh, bl;
+                  split16(x, b.fp16 != 0, bh, bl);
+                  if (e & 1) {
+                    hw4[e >> 1] |= bh << 16;
+                    lw4[e >> 1] |= bl << 16;
+                  } else {
+                    hw4[e >> 1] = bh;
+                    lw4[e >> 1] = bl;
+                  }
                 }
+                const int C = col0 + c0;  // S column
+                const int cc = C / kTcKC, wc = min(kTcKC, out_ld - kTcKC * cc);
+                const int64_t off = 2 * (int64_t)h_a * kTcKC * cc + (kmajor_off(row, C % kTcKC, h_a) >> 1);
+                *(uint4*)(sp + off) = make_uint4(hw4[0], hw4[1], hw4[2], hw4[3]);
+                *(uint4*)(sp + off + (int64_t)h_a * wc) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
               }
-              const int C = col0 + c0;  // S column
-              const int cc = C / kTcKC, wc = min(kTcKC, out_ld - kTcKC * cc);
-              const int64_t off = 2 * (int64_t)h_a * kTcKC * cc + (kmajor_off(row, C % kTcKC, h_a) >> 1);
-              *(uint4*)(sp + off) = make_uint4(hw4[0], hw4[1], hw4[2], hw4[3]);
-              *(uint4*)(sp + off + (int64_t)h_a * wc) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
             }
           }
         }
+        if (have && ++ab == kTcAcc) {
+          ab = 0;
+          aph ^= 1u;
+        }
+        if (PHASE == 2 && (have || last)) first = false;
       }
     }
   }
@@ -559,26 +582,31 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     }
     __syncwarp();
     fence_after_sync();
-    tmem_dealloc(tmem, kTcTmemCols);
+    tmem_dealloc(tmem, TcCfg<NB>::kTmemCols);
   }
 }
 
-cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
-                            double* sigma, uint64_t limit_ns, cudaStream_t s) {
-  if (nblocks <= 0) return cudaGetLastError();
-  if (phase == 1) {
-    cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-    if (e != cudaSuccess) return e;
-    tc_sigma_kernel<1><<<nblocks, kTcThreads, kTcSmem, s>>>(b, work, ranges, sigma, limit_ns);
-  } else if (phase == 2) {
-    cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-    if (e != cudaSuccess) return e;
-    tc_sigma_kernel<2><<<nblocks, kTcThreads, kTcSmem, s>>>(b, work, ranges, sigma, limit_ns);
-  } else {
-    return cudaErrorInvalidValue;
-  }
+template <int PHASE, int NB>
+static cudaError_t launch_tc_sigma_nb(const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
+                                      double* sigma, uint64_t limit_ns, cudaStream_t s) {
+  constexpr int smem = TcCfg<NB>::kSmem;
+  cudaError_t e = cudaFuncSetAttribute(tc_sigma_kernel<PHASE, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  tc_sigma_kernel<PHASE, NB><<<nblocks, kTcThreads, smem, s>>>(b, work, ranges, sigma, limit_ns);
   return cudaGetLastError();
 }
+
+cudaError_t launch_tc_sigma(int phase, int nb, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
+                            double* sigma, uint64_t limit_ns, cudaStream_t s) {
+  if (nblocks <= 0) return cudaGetLastError();
+  if (phase == 1 && nb == 64) return launch_tc_sigma_nb<1, 64>(b, work, ranges, nblocks, sigma, limit_ns, s);
+  if (phase == 2 && nb == 64) return launch_tc_sigma_nb<2, 64>(b, work, ranges, nblocks, sigma, limit_ns, s);
+  if (phase == 1 && nb == 128) return launch_tc_sigma_nb<1, 128>(b, work, ranges, nblocks, sigma, limit_ns, s);
+  if (phase == 2 && nb == 128) return launch_tc_sigma_nb<2, 128>(b, work, ranges, nblocks, sigma, limit_ns, s);
+  return cudaErrorInvalidValue;
+}
+
+int tc_blocks_per_sm(int nb) { return nb == 64 ? TcCfg<64>::kBlocksPerSm : TcCfg<128>::kBlocksPerSm; }
 
 __global__ void __launch_bounds__(256) tc_reduce_kernel(const float2* __restrict__ partials,
                                                          const TcTile* __restrict__ tiles,

@@ -32,7 +32,8 @@ cudaError_t launch_tc_tile_bulk(const __nv_bfloat16* Ap, const __nv_bfloat16* Bp
 // and columns beyond its own K are zero.
 constexpr int kTcKC = 32;
 constexpr int kTcRowsA = 128;  // output tile rows (MMA M)
-constexpr int kTcRowsB = 64;   // output tile columns (MMA N at most)
+constexpr int kTcRowsB = 64;   // output tile columns (MMA N at most) of the narrow tiles
+constexpr int kTcRowsBWide = 128;  // the same for wide tiles (one pipeline per SM)
 __host__ __device__ inline int64_t tc_block_off(int rows, int kp, int t, int c, int rt) {
   const int rest = rows - rt * t;
   const int h = rest < rt ? rest : rt;
@@ -126,9 +127,13 @@ struct TcBufs {
 
 cudaError_t launch_tc_pack(const TcBufs& b, const TcPack* units, int nunits, cudaStream_t s);
 // phase 1 or 2 on nblocks persistent blocks: block j runs the work records
-// work[ranges[j].x .. ranges[j].y); limit_ns bounds every pipeline wait
-cudaError_t launch_tc_sigma(int phase, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
+// work[ranges[j].x .. ranges[j].y); nb = output-tile width (kTcRowsB or
+// kTcRowsBWide, the row tile of the B-role pools); limit_ns bounds every
+// pipeline wait
+cudaError_t launch_tc_sigma(int phase, int nb, const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks,
                             double* sigma, uint64_t limit_ns, cudaStream_t s);
+// persistent blocks per SM of the kernels with tile width nb
+int tc_blocks_per_sm(int nb);
 // Bounded-wait self-check: one thread waits, with the sigma kernels' wait,
 // on an mbarrier that nothing arrives at; out[0] = 1 when the wait gave up,
 // out[1] = nanoseconds waited; *status is set by the wait.

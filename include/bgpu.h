@@ -129,13 +129,20 @@ int bgpu_davidson_graph_launches(bgpu_ctx* ctx, int64_t* launches);
  * per sigma sector (stage-2 tiles), one block per tile.  Applies to the next
  * product of every superblock. */
 int bgpu_set_tc_schedule(bgpu_ctx* ctx, int mode);
+/* Output-tile width of the tensor-core sigma (no reference counterpart):
+ * 64 columns (two pipelines per SM, 128 x 64 MMAs) or 128 (one pipeline per
+ * SM, 128 x 128 MMAs reading each A piece once for twice the work); 0
+ * (default) chooses 128 when most of the stage-2 work lies in sectors at
+ * least 128 columns wide, or lets the autotuner choose.  Applies to the next
+ * product of every superblock (its operands are packed again). */
+int bgpu_set_tc_tile_width(bgpu_ctx* ctx, int nb);
 /* Autotuner of the persistent tensor-core schedule (no reference
- * counterpart): on = 1 times candidate knobs (cost model of the block
- * assignment, splitting of heavy tiles, accumulation group length) on the
- * first product of every superblock whose sector-size histogram was not seen
- * before and keeps the fastest; superblocks with a known histogram reuse its
- * knobs.  cache_path (may be NULL) is a text file the tuned knobs are read
- * from and appended to. */
+ * counterpart): on = 1 times candidate tile widths (64, 128 columns) and,
+ * for each, candidate knobs (cost model of the block assignment, splitting
+ * of heavy tiles, accumulation group length) on the first product of every
+ * superblock whose sector-size histogram was not seen before and keeps the
+ * fastest; superblocks with a known histogram reuse the choice.  cache_path
+ * (may be NULL) is a text file the choices are read from and appended to. */
 int bgpu_set_autotune(bgpu_ctx* ctx, int on, const char* cache_path);
 /* Histograms tuned by this context, histograms in the cache, seconds spent tuning. */
 int bgpu_autotune_stats(bgpu_ctx* ctx, int64_t* keys_tuned, int64_t* keys_cached, double* seconds);
@@ -233,7 +240,8 @@ int bgpu_tc_wait_selftest(bgpu_ctx* ctx, double limit_ms, int* gave_up, int* sta
  *   split, group, per-sector flag, 1 when chosen by the autotuner), the
  *   launches of one sigma at the current precision and the doubles of
  *   stage-1 intermediates the FP64 product needs (compare with
- *   BGPU_NOALLOC_SCRATCH_DOUBLES).  Builds the tensor-core plan if needed. */
+ *   BGPU_NOALLOC_SCRATCH_DOUBLES) and the output-tile width of the
+ *   tensor-core plan.  Builds the tensor-core plan if needed. */
 int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n);
 /* Kernel launches of one sigma product. */
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);

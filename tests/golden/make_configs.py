@@ -6,11 +6,13 @@ for one sweep; syn40_m1000, syn40 at M=1000): seeded synthetic
 Cholesky Hamiltonians generated inside the library from the `orbitals
 synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>` spec; syn8 / syn8_d2h are
 small members of the same family used for FCI cross-checks.  syn16_m200
-(16 orbitals, M=200, 4 sweeps) and c2_d2h_m50 (the c2_d2h integrals at
-M=50) truncate heavily: the split-precision sweeps are compared with the
-FP64 ones sweep by sweep on them, with Davidson converged to 1e-12 so that
-the comparison is not limited by the FP64 run's own solver tolerance.  c2_d2h_noise runs c2_d2h_m50 with
-perturbative noise in its first two sweeps and random noise in the first.
+(16 orbitals, M=200, 4 sweeps) and syn24_m250_s2 (two sweeps of the
+24-orbital system at M=250) truncate heavily: the split-precision sweeps are
+compared with the FP64 ones sweep by sweep on them, with Davidson converged
+to 1e-12 so that the comparison is not limited by the FP64 run's own solver
+tolerance.  syn16_noise
+runs syn16_m200 with perturbative noise in its first two sweeps and random
+noise in the first.
 """
 import os
 
@@ -34,11 +36,10 @@ CONFS = {
     "syn24": ("synthetic:24:24:48:24:0", "nelec 24\nspin 0\nschedule\n0 500 1e-8 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
     "syn24_m250": ("synthetic:24:24:48:24:0", "nelec 24\nspin 0\nschedule\n0 250 1e-8 0\nend\nmaxiter 6\nsweep_tol 1e-12\nnoreorder\n"),
     "syn16_m200": ("synthetic:16:16:32:16:0", "nelec 16\nspin 0\nschedule\n0 200 1e-12 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
-    "c2_d2h_m50": ("../c2_d2h/FCIDUMP", "nelec 8\nspin 0\nirrep 1\nhf_occ integral\nschedule\n0 50 1e-12 0\nend\n"
-                   "maxiter 4\nsweep_tol 1e-12\nsym d2h\nnroots 2\nweights 0.5 0.5\n"),
-    "c2_d2h_noise": ("../c2_d2h/FCIDUMP", "nelec 8\nspin 0\nirrep 1\nhf_occ integral\nschedule\n0 50 1e-8 1e-4\n"
-                     "2 50 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nsym d2h\nnroots 2\nweights 0.5 0.5\n"
-                     "twodot_noise 1e-3 0.5\n"),
+    "syn16_noise": ("synthetic:16:16:32:16:0", "nelec 16\nspin 0\nschedule\n0 200 1e-12 1e-4\n2 200 1e-12 0\nend\n"
+                    "maxiter 4\nsweep_tol 1e-12\nnoreorder\ntwodot_noise 1e-3 0.5\n"),
+    "syn24_m250_s2": ("synthetic:24:24:48:24:0", "nelec 24\nspin 0\nschedule\n0 250 1e-12 0\nend\nmaxiter 2\n"
+                      "sweep_tol 1e-12\nnoreorder\n"),
     "syn30": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_sweep1": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 1\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_d2h": ("synthetic:30:30:60:30:1", "nelec 30\nspin 0\nschedule\n0 1500 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
