@@ -76,6 +76,7 @@ _SIGS = {
     "bgpu_set_refinement": (_I, [_P, _I]),
     "bgpu_sweep_energies": (_I, [_P, _DP, _I, _IP]),
     "bgpu_run_stats": (_I, [_P, _DP, _I]),
+    "bgpu_onepdm": (_I, [_P, _I, _DP, _I]),
     "bgpu_refinement_stats": (_I, [_P, _I64P, _I64P, _IP]),
     "bgpu_block_set_sites": (_I, [_P, _I, _I, _IP]),
     "bgpu_block_quanta": (_I, [_P, _I, _IP, _IP, _IP]),
@@ -441,6 +442,13 @@ class Context:
         a, b, c = _I64(), _I64(), _I()
         self._check(self.lib.bgpu_refinement_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, bool(c.value)
+
+    def onepdm(self, root, norb):
+        """Spatial one-particle density matrix of a root from the last
+        run_dmrg with the onepdm keyword (norb x norb)."""
+        g = np.zeros((norb, norb))
+        self._check(self.lib.bgpu_onepdm(self.h, int(root), _dp(g), int(norb)))
+        return g
 
     def set_refine_window(self, eh):
         """FP64 energy refinement window of split-precision sweeps (Eh)."""

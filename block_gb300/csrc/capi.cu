@@ -23,6 +23,7 @@ struct bgpu_ctx {
   double refine_window = 1e-3;  // Eh; see bgpu_set_refine_window
   std::vector<double> sweep_energies;  // of the last bgpu_run_dmrg
   std::vector<double> run_stats;       // see bgpu_run_stats
+  std::vector<std::vector<double>> onepdm;  // of the last bgpu_run_dmrg with `onepdm`
   bool transform_guess = true;  // see bgpu_set_guess
   int deferred_steps = 4;        // see bgpu_set_refine_window
   struct BlockRec {
@@ -198,6 +199,16 @@ int bgpu_sweep_energies(bgpu_ctx* ctx, double* e, int cap, int* n) {
     need(n != nullptr && (cap == 0 || e), "null argument");
     *n = (int)ctx->sweep_energies.size();
     for (int i = 0; i < cap && i < *n; ++i) e[i] = ctx->sweep_energies[i];
+  });
+}
+
+int bgpu_onepdm(bgpu_ctx* ctx, int root, double* gamma, int norb) {
+  return guarded(ctx, [&] {
+    need(gamma != nullptr, "null argument");
+    need(root >= 0 && root < (int)ctx->onepdm.size(),
+         "no one-particle density matrix of this root (the last bgpu_run_dmrg needs the onepdm keyword)");
+    need((size_t)norb * norb == ctx->onepdm[root].size(), "norb does not match the last run");
+    std::copy(ctx->onepdm[root].begin(), ctx->onepdm[root].end(), gamma);
   });
 }
 
@@ -899,6 +910,8 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
                   double* stats) {
   return guarded(ctx, [&] {
     need(conf_path && energies && max_roots > 0, "bad arguments");
+    ctx->onepdm.clear();  // results of a run that fails are not kept
+    ctx->sweep_energies.clear();
     auto t0 = std::chrono::steady_clock::now();
     Config c = parse_config(conf_path);
     Integrals I = load_integrals(c);
@@ -923,6 +936,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     }
     ctx->eng->sync();  // the last renormalisation and block releases
     ctx->sweep_energies = r.sweep_energies;
+    ctx->onepdm = r.onepdm;
     ctx->run_stats = {(double)(E.split_calls - sc0), E.split_seconds - ss0, (double)(E.fp64_calls - fc0),
                       E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
                       r.warmup_seconds};

@@ -2142,6 +2142,42 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   return total_iter;
 }
 
+// <psi_r| T |psi_r> of single pair terms T for the last solve's vectors: one
+// FP64 product per term and root, each followed by a deterministic dot
+// product (one-particle density matrix, SweepDriver::rdm_step).
+void GpuEngine::expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) {
+  if (!waves_ || wave_n_ != sb.size) throw std::runtime_error("expectations: no wavefunction of this superblock");
+  const int64_t n = sb.size;
+  const int nt = (int)terms.size();
+  out.assign((size_t)nwaves_ * nt, 0.0);
+  if (nt == 0) return;
+  const double f0 = sigma_flops;
+  const long c0 = sigma_calls;
+  double* y = alloc(n);
+  double* work = alloc((int64_t)dev::kGramBlocks);
+  double* red = alloc((int64_t)nwaves_ * nt);
+  for (int t = 0; t < nt; ++t) {
+    Superblock one = sb;
+    one.terms.assign(1, terms[t]);
+    one.ecore = 0.0;
+    SigmaPlan p;
+    plan_sigma(one, p);
+    for (int r = 0; r < nwaves_; ++r) {
+      const double* psi = waves_ + (int64_t)r * n;
+      sigma(one, p, psi, y);
+      cuda_check(dev::launch_gram(psi, 1, y, 1, n, n, work, red + (int64_t)r * nt + t, stream_), "dot");
+    }
+    free_plan(p);
+  }
+  cuda_check(cudaMemcpyAsync(out.data(), red, out.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+  sync();
+  free(y);
+  free(work);
+  free(red);
+  sigma_flops = f0;  // density-matrix products are not sigma products of the solve
+  sigma_calls = c0;
+}
+
 // Defect correction: energies of the split-precision Ritz vectors from one
 // FP64 product each (Rayleigh quotient, second order in the vector error).
 bool GpuEngine::refine(const Superblock& sb, std::vector<double>& energies) {

@@ -157,6 +157,7 @@ class GpuEngine : public Engine {
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
   void renormalise(Block& small, const Block& big) override;
+  void expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) override;
 
   // pieces used by the C ABI, the tests and the bench
   void plan_sigma(const Superblock& sb, SigmaPlan& plan);

@@ -136,6 +136,8 @@ void write_fcidump(const Integrals& I, const std::string& path) {
 Integrals reorder(const Integrals& I, const std::vector<int>& perm) {
   Integrals O = I;
   const int n = I.norb;
+  O.order.resize(n);
+  for (int a = 0; a < n; ++a) O.order[a] = I.order.empty() ? perm[a] : I.order[perm[a]];
   for (int a = 0; a < n; ++a) {
     O.orbsym[a] = I.orbsym[perm[a]];
     for (int b = 0; b < n; ++b) O.t[(size_t)a * n + b] = I.h(perm[a], perm[b]);
@@ -332,6 +334,13 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
     else if (key == "deflation_min_size") { need(1); c.deflation_min = std::stoi(tok[1]); }
     else if (key == "warmup") { if (tok.size() > 1) c.warmup = lower(tok[1]); }
     else if (key == "restart" || key == "fullrestart") c.restart = true;
+    else if (key == "onepdm" || key == "onerdm" || key == "ordm") c.onepdm = true;
+    else if (key == "prefix" || key == "scratch") {
+      need(1);
+      std::string p = tok[1];
+      if (p[0] != '/' && !base_dir.empty()) p = base_dir + "/" + p;
+      c.prefix = p;
+    }
     else if (key == "reset_iter" || key == "reset_iters" || key == "reset_iterations") c.reset_iter = true;
     else if (key == "checkpoint") {
       need(1);
@@ -364,7 +373,7 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
       if (tok.size() != 3) throw std::runtime_error("twodot_noise needs two numbers (amplitude, gamma)");
       c.twodot_noise = std::stod(tok[1]);
     }
-    // other keywords (hf_occ, twodot, twodot_to_onedot, onepdm, ...) are accepted and ignored
+    // other keywords (hf_occ, twodot, twodot_to_onedot, twopdm, ...) are accepted and ignored
   }
   if (!sweep_tol_set && c.sweep_tol <= 0) c.sweep_tol = 1e-5;
   if (c.nroots > 1) {

@@ -20,6 +20,8 @@ struct Integrals {
   double ecore = 0.0;
   std::vector<double> t;  // norb^2
   std::vector<double> v;  // norb^4, (ij|kl) = v[((i*n+j)*n+k)*n+l]
+  // after reorder(): orbital a is orbital order[a] of the input (empty: input order)
+  std::vector<int> order;
   double h(int i, int j) const { return t[(size_t)i * norb + j]; }
   double g(int i, int j, int k, int l) const {
     return v[(((size_t)i * norb + j) * norb + k) * norb + l];
@@ -83,6 +85,11 @@ struct Config {
   // `reset_iter` then starts the schedule from its first entry again
   std::string checkpoint;
   bool restart = false, reset_iter = false;
+  // `onepdm` (or onerdm, ordm): after the sweeps, one more sweep evaluates
+  // the spin-summed spatial one-particle density matrix of every root;
+  // `prefix <dir>`: where spatial_onepdm.<r>.<r>.txt files are written
+  bool onepdm = false;
+  std::string prefix;
   // `twodot_noise <amplitude> <gamma>`: random-wavefunction noise of that
   // amplitude in the density matrices of the first sweep (gamma is read and
   // not used); with `schedule default` it replaces the scheduled noise

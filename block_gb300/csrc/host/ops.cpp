@@ -137,6 +137,7 @@ std::set<OpKey> catalog_keys(const CatalogSpec& c) {
     k.insert(ddcomp_key(a, b, 0));
     if (a != b) k.insert(ddcomp_key(a, b, 2));
   }
+  for (const OpKey& x : c.extra) k.insert(x);
   return k;
 }
 

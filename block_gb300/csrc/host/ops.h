@@ -115,6 +115,7 @@ struct CatalogSpec {
   std::vector<int> ccd_sites;                    // CCD_i for these i (outside the block)
   bool normal = false;                           // CD/CC for pairs inside the block
   std::vector<std::pair<int, int>> comp_pairs;   // CDcomp/DDcomp pairs (i >= j), outside the block
+  std::vector<OpKey> extra;                      // further operators (density-matrix evaluation)
 };
 std::set<OpKey> catalog_keys(const CatalogSpec& s);
 

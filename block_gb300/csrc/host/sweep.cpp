@@ -91,6 +91,8 @@ void SweepDriver::merge(CatalogSpec& a, const CatalogSpec& b) const {
     if (std::find(a.ccd_sites.begin(), a.ccd_sites.end(), x) == a.ccd_sites.end()) a.ccd_sites.push_back(x);
   for (auto& p : b.comp_pairs)
     if (std::find(a.comp_pairs.begin(), a.comp_pairs.end(), p) == a.comp_pairs.end()) a.comp_pairs.push_back(p);
+  for (const OpKey& k : b.extra)
+    if (std::find(a.extra.begin(), a.extra.end(), k) == a.extra.end()) a.extra.push_back(k);
 }
 
 Block SweepDriver::make_enlarged(const Block& sys, int x, bool dot_on_right, const CatalogSpec& spec) {
@@ -416,6 +418,7 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
   const SweepResult phase0 = phase_;
   auto t0 = clk::now();
+  if (rdm_pass_) rdm_extras(p, specL, specR);
   Block L = make_enlarged(left_block(p - 1), p, true, specL);
   Block R = make_enlarged(right_block(p + 2), p + 1, false, specR);
   Superblock sb = make_superblock(L, R);
@@ -463,6 +466,7 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   } else {
     note_refined(energies);
   }
+  if (rdm_pass_) rdm_step(p, sb);
   phase_.solve_seconds += secs(t0);
   if (opt_.on_step) opt_.on_step(sb, sweep_index, p);
   t0 = clk::now();
@@ -589,6 +593,98 @@ double SweepDriver::sweep(bool forward, int sweep_index) {
   return sweep_refined_min_;
 }
 
+// One-particle density matrix (modules/onepdm, onepdm.C:24-55 and its
+// compute_one_pdm_* kernels): gamma_ij = sqrt(2) <[C_i x D_j]^0> with
+// [C_i x D_j]^0 = (a+_i,up a_j,up + a+_i,dn a_j,dn) / sqrt(2).  Over one sweep
+// every element is taken once, at the step p (L = [0..p], R = [p+1..N-1]):
+//   i = p < j, and at p = 1 also i = 0 < j (operators C_i on L, D_j on R);
+//   i = j = p for 2 <= p <= N-3 (CD^0_pp on L);
+//   i, j in {0, 1} at p = 1 (CD^0 on L) and in {N-2, N-1} at p = N-3 (on R);
+// gamma is symmetric (real wavefunctions).
+void SweepDriver::rdm_extras(int p, CatalogSpec& specL, CatalogSpec& specR) const {
+  auto add = [](CatalogSpec& s, const OpKey& k) {
+    if (std::find(s.extra.begin(), s.extra.end(), k) == s.extra.end()) s.extra.push_back(k);
+  };
+  if (p == 1) {
+    add(specL, cd_key(0, 0, 0));
+    add(specL, cd_key(1, 0, 0));
+    add(specL, cd_key(1, 1, 0));
+  } else {
+    add(specL, cd_key(p, p, 0));
+  }
+  if (p == N_ - 3) {
+    add(specR, cd_key(N_ - 2, N_ - 2, 0));
+    add(specR, cd_key(N_ - 1, N_ - 2, 0));
+    add(specR, cd_key(N_ - 1, N_ - 1, 0));
+  }
+}
+
+void SweepDriver::rdm_step(int p, const Superblock& sb) {
+  const double r2 = std::sqrt(2.0);
+  std::vector<PairTerm> terms;
+  std::vector<std::pair<int, int>> at;
+  auto cross = [&](int i, int j) {
+    PairTerm t;
+    t.coef = r2;
+    t.l = op(cre_key(i));
+    t.r = op(cre_key(j), true);
+    terms.push_back(t);
+    at.push_back({i, j});
+  };
+  auto inside = [&](bool left, int a, int b) {  // a >= b
+    PairTerm t;
+    t.coef = r2;
+    if (left) {
+      t.l = op(cd_key(a, b, 0));
+      t.r = ident();
+    } else {
+      t.l = ident();
+      t.r = op(cd_key(a, b, 0));
+    }
+    terms.push_back(t);
+    at.push_back({a, b});
+  };
+  for (int j = p + 1; j < N_; ++j) cross(p, j);
+  if (p == 1) {
+    for (int j = 2; j < N_; ++j) cross(0, j);
+    inside(true, 0, 0);
+    inside(true, 1, 0);
+    inside(true, 1, 1);
+  } else {
+    inside(true, p, p);
+  }
+  if (p == N_ - 3) {
+    inside(false, N_ - 2, N_ - 2);
+    inside(false, N_ - 1, N_ - 2);
+    inside(false, N_ - 1, N_ - 1);
+  }
+  std::vector<double> v;
+  E_.expectations(sb, terms, v);
+  const int nroots = (int)(v.size() / std::max<size_t>(terms.size(), 1));
+  if ((int)rdm_.size() < nroots) rdm_.resize(nroots, std::vector<double>((size_t)N_ * N_, 0.0));
+  for (int r = 0; r < nroots; ++r)
+    for (size_t t = 0; t < terms.size(); ++t) {
+      const double g = v[(size_t)r * terms.size() + t];
+      const int i = at[t].first, j = at[t].second;
+      rdm_[r][(size_t)i * N_ + j] = g;
+      rdm_[r][(size_t)j * N_ + i] = g;
+    }
+}
+
+std::vector<std::vector<double>> SweepDriver::onepdm_sweep(bool forward, int sweep_index) {
+  if (N_ < 4) throw std::runtime_error("onepdm needs at least 4 orbitals");
+  rdm_.clear();
+  rdm_pass_ = true;
+  try {
+    sweep(forward, sweep_index);
+  } catch (...) {
+    rdm_pass_ = false;
+    throw;
+  }
+  rdm_pass_ = false;
+  return std::move(rdm_);
+}
+
 SweepResult SweepDriver::run() {
   SweepResult res;
   struct NoiseOff {  // the engine's noise ends with the run
@@ -639,6 +735,33 @@ SweepResult SweepDriver::run() {
     }
     if (s >= last_sched && std::fabs(e - eprev) <= C_.sweep_tol) break;
     eprev = e;
+  }
+  if (C_.onepdm) {
+    // one more sweep, in the next direction, with the final schedule entry
+    const int last = std::max(res.sweeps - 1, 0);
+    const bool forward = ((res.sweeps - s_begin) % 2 == 0) == first_forward;
+    const auto ts = std::chrono::steady_clock::now();
+    auto g = onepdm_sweep(forward, last);
+    res.onepdm.assign(g.size(), std::vector<double>((size_t)N_ * N_, 0.0));
+    for (size_t r = 0; r < g.size(); ++r)
+      for (int a = 0; a < N_; ++a)
+        for (int b = 0; b < N_; ++b) {
+          const int A = I_.order.empty() ? a : I_.order[a], B = I_.order.empty() ? b : I_.order[b];
+          res.onepdm[r][(size_t)A * N_ + B] = g[r][(size_t)a * N_ + b];
+        }
+    log(1, "onepdm sweep (%s): %.2fs\n", forward ? "fwd" : "bwd",
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count());
+    if (!C_.prefix.empty())
+      for (size_t r = 0; r < res.onepdm.size(); ++r) {
+        // spatial_onepdm.r.r.txt (save_onepdm_spatial_text, onepdm.C:504-528)
+        const std::string path = C_.prefix + "/spatial_onepdm." + std::to_string(r) + "." + std::to_string(r) + ".txt";
+        FILE* f = std::fopen(path.c_str(), "w");
+        if (!f) throw std::runtime_error("cannot write " + path);
+        std::fprintf(f, "%d\n", N_);
+        for (int a = 0; a < N_; ++a)
+          for (int b = 0; b < N_; ++b) std::fprintf(f, "%d %d %20.14e\n", a, b, res.onepdm[r][(size_t)a * N_ + b]);
+        std::fclose(f);
+      }
   }
   res.energies = last_energies_;
   res.discarded = last_discarded_;

@@ -178,6 +178,9 @@ class Engine {
   virtual void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) = 0;
   // small = rotation^T big rotation for every operator of small's catalogue
   virtual void renormalise(Block& small, const Block& big) = 0;
+  // expectation values <psi_r| coef * [l x r]^0 |psi_r> of single pair terms
+  // for the last solve's vectors: out[root * terms.size() + t]
+  virtual void expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) = 0;
 
  protected:
   NoiseSpec noise_;
@@ -203,6 +206,9 @@ struct SweepResult {
   std::vector<double> sweep_energies;   // lowest root, per sweep
   std::vector<double> sweep_seconds;    // wall time per sweep (device work included)
   double warmup_seconds = 0.0;          // wall time of the warm-up (0 on restart)
+  // `onepdm`: per root, the spin-summed spatial one-particle density matrix
+  // gamma_ij = sum_s <a+_is a_js> (norb x norb row-major, input orbital order)
+  std::vector<std::vector<double>> onepdm;
   double discarded = 0.0;
   int sweeps = 0;
   double sigma_seconds = 0.0;
@@ -242,6 +248,9 @@ class SweepDriver {
   // left blocks [0..q] for q = 1..upto from seeded random rotations
   void warmup_left(int upto);
   double sweep(bool forward, int sweep_index);
+  // one sweep that also evaluates the one-particle density matrix (per root,
+  // norb x norb in the sweep's orbital order)
+  std::vector<std::vector<double>> onepdm_sweep(bool forward, int sweep_index);
   // Superblock of partition p (L=[0..p], R=[p+1..N-1]) built from warm-up
   // blocks on both sides: the sector structure and operator catalogue of a
   // mid-sweep step with bond dimension M, without any Davidson solve.
@@ -305,6 +314,11 @@ class SweepDriver {
   };
   std::vector<std::unique_ptr<Candidate>> cands_;
   double sweep_refined_min_ = 0.0;
+  // density-matrix sweep: the operators each step needs and the elements
+  bool rdm_pass_ = false;
+  std::vector<std::vector<double>> rdm_;
+  void rdm_extras(int p, CatalogSpec& specL, CatalogSpec& specR) const;
+  void rdm_step(int p, const Superblock& sb);
   std::vector<double> sweep_refined_best_;
   void note_refined(const std::vector<double>& e);
   void refine_candidate(Candidate& c);

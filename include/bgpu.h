@@ -421,6 +421,14 @@ int bgpu_prepare_superblock(bgpu_ctx* ctx, const char* conf_path, int partition,
  */
 int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* energies, int max_roots,
                   double* stats);
+/* Spin-summed spatial one-particle density matrix gamma_ij =
+ * sum_s <a+_is a_js> of root `root` (norb x norb row-major, the FCIDUMP's
+ * orbital order) from the last bgpu_run_dmrg whose dmrg.conf had `onepdm`
+ * (modules/onepdm, onepdm.C:24-55; the same values as its
+ * spatial_onepdm.<root>.<root>.txt, which the run also writes under
+ * `prefix <dir>` when given).  The run evaluates it in one more sweep after
+ * the last one. */
+int bgpu_onepdm(bgpu_ctx* ctx, int root, double* gamma, int norb);
 /* Arithmetic of the last bgpu_run_dmrg (no reference counterpart), out[n]:
  * split-precision products and their seconds, FP64 products and their
  * seconds, defect-correction rounds, the FP64 product time the same

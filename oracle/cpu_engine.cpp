@@ -586,6 +586,26 @@ void CpuEngine::add_noise(const Superblock& sb, bool left, std::vector<std::vect
   }
 }
 
+// <psi_r| T |psi_r> of single pair terms: the product of one term
+// (TensorMultiply over its couplings) dotted with the wavefunction.
+void CpuEngine::expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) {
+  const int nt = (int)terms.size();
+  out.assign(waves_.size() * terms.size(), 0.0);
+  std::vector<double> y(sb.size);
+  for (int t = 0; t < nt; ++t) {
+    Superblock one = sb;
+    one.terms.assign(1, terms[t]);
+    one.ecore = 0.0;
+    for (size_t r = 0; r < waves_.size(); ++r) {
+      std::fill(y.begin(), y.end(), 0.0);
+      sigma(one, waves_[r].data(), y.data());
+      double d = 0.0;
+      for (int64_t e = 0; e < sb.size; ++e) d += waves_[r][e] * y[e];
+      out[r * terms.size() + t] = d;
+    }
+  }
+}
+
 void CpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {
   const int nq = (int)kept.size();
   rot_.assign(nq, {});

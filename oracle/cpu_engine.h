@@ -41,6 +41,7 @@ class CpuEngine : public Engine {
   void select_rotation(const std::vector<std::vector<int>>& kept) override;
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
   void renormalise(Block& small, const Block& big) override;
+  void expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) override;
 
   // pieces exposed for tests and the bench
   void sigma(const Superblock& sb, const double* psi, double* out);

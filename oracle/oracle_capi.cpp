@@ -121,6 +121,15 @@ int oracle_use_blas(const char* path) {
 }
 
 static std::vector<double> g_last_sweep_energies;  // per sweep, lowest root, of the last oracle_run
+static std::vector<std::vector<double>> g_last_onepdm;  // per root, of the last oracle_run with onepdm
+
+// the one-particle density matrix of a root of the last oracle_run (0 on success)
+int oracle_onepdm(int root, double* out, int norb) {
+  if (root < 0 || root >= (int)g_last_onepdm.size()) return 1;
+  if ((size_t)norb * norb != g_last_onepdm[root].size()) return 2;
+  std::copy(g_last_onepdm[root].begin(), g_last_onepdm[root].end(), out);
+  return 0;
+}
 
 // the per-sweep energies of the last oracle_run (returns how many; copies up to cap)
 int oracle_sweep_energies(double* out, int cap) {
@@ -129,6 +138,8 @@ int oracle_sweep_energies(double* out, int cap) {
 }
 
 int oracle_run(const char* conf, int threads, int verbose, double* energies, int max_roots, double* stats) {
+  g_last_onepdm.clear();
+  g_last_sweep_energies.clear();
   try {
     auto t0 = std::chrono::steady_clock::now();
     Config c = parse_config(conf);
@@ -142,6 +153,7 @@ int oracle_run(const char* conf, int threads, int verbose, double* energies, int
       r = drv.run();
     }
     g_last_sweep_energies = r.sweep_energies;
+    g_last_onepdm = r.onepdm;
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {
       stats[0] = r.sweeps;

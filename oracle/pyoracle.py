@@ -249,3 +249,15 @@ def sample_sigma(conf, partition, threads=0, reps=1):
     if L.oracle_sample_sigma(conf.encode(), partition, threads, reps, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))):
         raise RuntimeError("oracle sample failed for " + conf)
     return dict(flops=out[0], psi=int(out[1]), arena=int(out[2]), seconds=out[3], norm=out[4], threads=int(out[5]))
+
+
+def onepdm(root, norb):
+    """One-particle density matrix of a root from the last run() of a
+    configuration with the onepdm keyword."""
+    L = lib()
+    L.oracle_onepdm.restype = ctypes.c_int
+    L.oracle_onepdm.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    g = np.zeros((norb, norb))
+    if L.oracle_onepdm(root, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), norb):
+        raise RuntimeError("no one-particle density matrix of root %d" % root)
+    return g

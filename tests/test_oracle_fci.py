@@ -37,9 +37,11 @@ def read_fcidump(path):
     return t, v, ecore
 
 
-def fci_energies(t, v, ecore, nelec, nroots=12):
+def fci_operators(t, v, ecore, nelec):
+    """The determinant-space Hamiltonian (M_S = 0) and the spin-summed
+    excitation operators E_pq = a+_pa a_qa + a+_pb a_qb as sparse matrices."""
     n = t.shape[0]
-    na = nb = nelec // 2
+    na = nelec // 2
     strs = [sum(1 << o for o in c) for c in itertools.combinations(range(n), na)]
     idx = {s: i for i, s in enumerate(strs)}
     ns = len(strs)
@@ -87,8 +89,22 @@ def fci_energies(t, v, ecore, nelec, nroots=12):
             c = sum(v[p, q, q, s] for q in range(n))
             if c != 0:
                 H = H - 0.5 * c * E[p, s]
+    return H, E
+
+
+def fci_energies(t, v, ecore, nelec, nroots=12):
+    H, _ = fci_operators(t, v, ecore, nelec)
     w = sla.eigsh(H, k=nroots, which="SA", tol=1e-12)[0]
     return np.sort(w)
+
+
+def write_fcidump(oracle, conf, path, input_order=False):
+    """The generated integrals of a configuration, through the oracle CLI's
+    FCIDUMP writer: in the sweep's orbital order, or in the input order."""
+    exe = os.path.join(os.path.dirname(oracle.LIB), "dmrg_oracle")
+    args = [exe, conf, "--write-fcidump", path] + (["--noreorder"] if input_order else [])
+    subprocess.run(args, check=True, capture_output=True)
+    return read_fcidump(path)
 
 
 @pytest.mark.parametrize("name", ["syn8", "syn8_d2h"])
@@ -96,11 +112,7 @@ def test_dmrg_spin_sectors_are_fci_eigenvalues(oracle, name, tmp_path):
     base = os.path.join(GOLDEN, name, "dmrg.conf")
     with open(base) as f:
         body = f.read()
-    # dump the generated integrals through the oracle CLI's FCIDUMP writer
-    dump = str(tmp_path / "FCIDUMP")
-    exe = os.path.join(os.path.dirname(oracle.LIB), "dmrg_oracle")
-    subprocess.run([exe, base, "--write-fcidump", dump], check=True, capture_output=True)
-    t, v, ecore = read_fcidump(dump)
+    t, v, ecore = write_fcidump(oracle, base, str(tmp_path / "FCIDUMP"))
     w = fci_energies(t, v, ecore, 8, nroots=120)
     es = []
     for spin in (0, 2, 4):

@@ -1,0 +1,91 @@
+"""The oracle's one-particle density matrix sweep (the onepdm keyword;
+modules/onepdm/onepdm.C) against an independent determinant FCI in numpy:
+gamma_pq = <Psi|E_pq|Psi> of the FCI eigenvector whose energy the DMRG run
+reached, with E_pq the spin-summed excitation operator.
+
+Tolerances written here: the DMRG solves converge the squared residual to
+1e-12, so the wavefunction, and with it gamma, is exact to about 1e-7; the
+test allows 1e-6 elementwise and 1e-6 on the trace (the electron count).
+The cases cover C1 and D2h integrals, a singlet and a triplet (E_pq is a
+spin scalar, so the M_S = 0 member of the FCI multiplet gives the same
+gamma), a run whose orbitals the sweep reorders, with gamma reported in
+the input orbital order (save_onepdm_spatial_text, onepdm.C:504-528), and
+the two state-averaged roots of the 8-site Hubbard case with its final
+Davidson tolerance tightened to 1e-12 (one gamma per root, 2e-6: the
+second root's solve ends with a larger residual, observed 7e-7)."""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as sla
+
+from conftest import GOLDEN
+from test_oracle_fci import fci_operators, write_fcidump
+
+
+def fci_onepdm(t, v, ecore, nelec, energy, nroots=40):
+    H, E = fci_operators(t, v, ecore, nelec)
+    w, X = sla.eigsh(H, k=nroots, which="SA", tol=1e-13)
+    k = int(np.argmin(np.abs(w - energy)))
+    others = np.delete(w, k)
+    assert abs(w[k] - energy) <= 1e-8, (w[k], energy)
+    assert np.min(np.abs(others - w[k])) > 1e-6  # a non-degenerate state
+    x = X[:, k]
+    n = t.shape[0]
+    return np.array([[x @ (E[p, q] @ x) for q in range(n)] for p in range(n)])
+
+
+def read_spatial_onepdm(path):
+    with open(path) as f:
+        n = int(f.readline())
+        g = np.zeros((n, n))
+        for line in f:
+            i, j, x = line.split()
+            g[int(i), int(j)] = float(x)
+    return g
+
+
+def onepdm_conf(tmp_path, name, spin=0, reorder=False):
+    """The golden configuration with the onepdm keyword and the output
+    prefix; its FCIDUMP (if any) by absolute path; the Hubbard case's final
+    Davidson tolerance at 1e-12."""
+    d = os.path.join(GOLDEN, name)
+    body = open(os.path.join(d, "dmrg.conf")).read().replace("spin 0", "spin %d" % spin)
+    body = body.replace("orbitals FCIDUMP", "orbitals %s" % os.path.join(d, "FCIDUMP"))
+    body = body.replace("8 200 1e-8 0", "8 200 1e-12 0")
+    if reorder:
+        body = body.replace("noreorder\n", "")
+    conf = tmp_path / "dmrg.conf"
+    conf.write_text(body + "onepdm\nprefix %s\n" % tmp_path)
+    return str(conf)
+
+
+CASES = [
+    ("syn8", 0, False, 1e-6),
+    ("syn8_d2h", 0, False, 1e-6),
+    ("syn8", 2, False, 1e-6),
+    ("syn8", 0, True, 1e-6),
+    ("hubbard", 0, False, 2e-6),
+]
+
+
+@pytest.mark.parametrize("name,spin,reorder,tol", CASES)
+def test_onepdm_matches_fci(oracle, tmp_path, name, spin, reorder, tol):
+    conf = onepdm_conf(tmp_path, name, spin, reorder)
+    t, v, ecore = write_fcidump(oracle, conf, str(tmp_path / "FCIDUMP"), input_order=True)
+    e, _ = oracle.run(conf)
+    for r in range(len(e)):
+        g = oracle.onepdm(r, 8)
+        gf = fci_onepdm(t, v, ecore, 8, e[r])
+        assert np.max(np.abs(g - gf)) <= tol, (r, np.max(np.abs(g - gf)))
+        assert abs(np.trace(g) - 8) <= tol
+        assert np.array_equal(g, g.T)
+        # the text file holds the same matrix
+        gt = read_spatial_onepdm(tmp_path / ("spatial_onepdm.%d.%d.txt" % (r, r)))
+        assert np.max(np.abs(gt - g)) <= 1e-13 * np.max(np.abs(g))
+
+
+def test_onepdm_needs_the_keyword(oracle):
+    oracle.run(os.path.join(GOLDEN, "syn8", "dmrg.conf"))
+    with pytest.raises(RuntimeError):
+        oracle.onepdm(0, 8)
