@@ -77,6 +77,7 @@ _SIGS = {
     "bgpu_sweep_energies": (_I, [_P, _DP, _I, _IP]),
     "bgpu_run_stats": (_I, [_P, _DP, _I]),
     "bgpu_onepdm": (_I, [_P, _I, _DP, _I]),
+    "bgpu_transition_onepdm": (_I, [_P, _I, _I, _DP, _I]),
     "bgpu_refinement_stats": (_I, [_P, _I64P, _I64P, _IP]),
     "bgpu_block_set_sites": (_I, [_P, _I, _I, _IP]),
     "bgpu_block_quanta": (_I, [_P, _I, _IP, _IP, _IP]),
@@ -448,6 +449,13 @@ class Context:
         run_dmrg with the onepdm keyword (norb x norb)."""
         g = np.zeros((norb, norb))
         self._check(self.lib.bgpu_onepdm(self.h, int(root), _dp(g), int(norb)))
+        return g
+
+    def transition_onepdm(self, bra, ket, norb):
+        """<bra|E_ij|ket> between two roots of the last run_dmrg with the
+        onepdm (or tran_onepdm) keyword (norb x norb)."""
+        g = np.zeros((norb, norb))
+        self._check(self.lib.bgpu_transition_onepdm(self.h, int(bra), int(ket), _dp(g), int(norb)))
         return g
 
     def set_refine_window(self, eh):

@@ -24,6 +24,7 @@ struct bgpu_ctx {
   std::vector<double> sweep_energies;  // of the last bgpu_run_dmrg
   std::vector<double> run_stats;       // see bgpu_run_stats
   std::vector<std::vector<double>> onepdm;  // of the last bgpu_run_dmrg with `onepdm`
+  std::vector<std::vector<double>> tonepdm;  // per root pair (bra * nroots + ket)
   bool transform_guess = true;  // see bgpu_set_guess
   int deferred_steps = 4;        // see bgpu_set_refine_window
   struct BlockRec {
@@ -209,6 +210,18 @@ int bgpu_onepdm(bgpu_ctx* ctx, int root, double* gamma, int norb) {
          "no one-particle density matrix of this root (the last bgpu_run_dmrg needs the onepdm keyword)");
     need((size_t)norb * norb == ctx->onepdm[root].size(), "norb does not match the last run");
     std::copy(ctx->onepdm[root].begin(), ctx->onepdm[root].end(), gamma);
+  });
+}
+
+int bgpu_transition_onepdm(bgpu_ctx* ctx, int bra, int ket, double* gamma, int norb) {
+  return guarded(ctx, [&] {
+    need(gamma != nullptr, "null argument");
+    const int nr = (int)ctx->onepdm.size();
+    need(bra >= 0 && bra < nr && ket >= 0 && ket < nr,
+         "no transition density matrix of these roots (the last bgpu_run_dmrg needs the onepdm keyword)");
+    const auto& m = ctx->tonepdm[(size_t)bra * nr + ket];
+    need((size_t)norb * norb == m.size(), "norb does not match the last run");
+    std::copy(m.begin(), m.end(), gamma);
   });
 }
 
@@ -911,6 +924,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
   return guarded(ctx, [&] {
     need(conf_path && energies && max_roots > 0, "bad arguments");
     ctx->onepdm.clear();  // results of a run that fails are not kept
+    ctx->tonepdm.clear();
     ctx->sweep_energies.clear();
     auto t0 = std::chrono::steady_clock::now();
     Config c = parse_config(conf_path);
@@ -937,6 +951,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     ctx->eng->sync();  // the last renormalisation and block releases
     ctx->sweep_energies = r.sweep_energies;
     ctx->onepdm = r.onepdm;
+    ctx->tonepdm = r.transition_onepdm;
     ctx->run_stats = {(double)(E.split_calls - sc0), E.split_seconds - ss0, (double)(E.fp64_calls - fc0),
                       E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
                       r.warmup_seconds};

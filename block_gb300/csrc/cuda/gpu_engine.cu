@@ -2148,24 +2148,26 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
 void GpuEngine::expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) {
   if (!waves_ || wave_n_ != sb.size) throw std::runtime_error("expectations: no wavefunction of this superblock");
   const int64_t n = sb.size;
-  const int nt = (int)terms.size();
-  out.assign((size_t)nwaves_ * nt, 0.0);
+  const int nt = (int)terms.size(), nr = nwaves_;
+  out.assign((size_t)nr * nr * nt, 0.0);
   if (nt == 0) return;
   const double f0 = sigma_flops;
   const long c0 = sigma_calls;
   double* y = alloc(n);
   double* work = alloc((int64_t)dev::kGramBlocks);
-  double* red = alloc((int64_t)nwaves_ * nt);
+  double* red = alloc((int64_t)nr * nr * nt);
   for (int t = 0; t < nt; ++t) {
     Superblock one = sb;
     one.terms.assign(1, terms[t]);
     one.ecore = 0.0;
     SigmaPlan p;
     plan_sigma(one, p);
-    for (int r = 0; r < nwaves_; ++r) {
-      const double* psi = waves_ + (int64_t)r * n;
-      sigma(one, p, psi, y);
-      cuda_check(dev::launch_gram(psi, 1, y, 1, n, n, work, red + (int64_t)r * nt + t, stream_), "dot");
+    for (int b = 0; b < nr; ++b) {
+      sigma(one, p, waves_ + (int64_t)b * n, y);
+      for (int a = 0; a < nr; ++a)
+        cuda_check(dev::launch_gram(waves_ + (int64_t)a * n, 1, y, 1, n, n, work,
+                                    red + ((int64_t)a * nr + b) * nt + t, stream_),
+                   "dot");
     }
     free_plan(p);
   }

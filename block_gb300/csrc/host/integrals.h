@@ -89,6 +89,9 @@ struct Config {
   // the spin-summed spatial one-particle density matrix of every root;
   // `prefix <dir>`: where spatial_onepdm.<r>.<r>.txt files are written
   bool onepdm = false;
+  // `tran_onepdm`: the same sweep, and also writes the transition matrices
+  // <i|E_kl|j> (i > j) as spatial_onepdm.<i>.<j>.txt
+  bool tran_onepdm = false;
   std::string prefix;
   // `twodot_noise <amplitude> <gamma>`: random-wavefunction noise of that
   // amplitude in the density matrices of the first sweep (gamma is read and

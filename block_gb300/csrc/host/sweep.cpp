@@ -600,7 +600,9 @@ double SweepDriver::sweep(bool forward, int sweep_index) {
 //   i = p < j, and at p = 1 also i = 0 < j (operators C_i on L, D_j on R);
 //   i = j = p for 2 <= p <= N-3 (CD^0_pp on L);
 //   i, j in {0, 1} at p = 1 (CD^0 on L) and in {N-2, N-1} at p = N-3 (on R);
-// gamma is symmetric (real wavefunctions).
+// gamma of one root is symmetric (real wavefunctions); between roots a and b
+// the sweep takes the transition elements <a|E_ij|b> (tran_onepdm,
+// modules/onepdm/onepdm.C with the transition flag) from the same terms.
 void SweepDriver::rdm_extras(int p, CatalogSpec& specL, CatalogSpec& specR) const {
   auto add = [](CatalogSpec& s, const OpKey& k) {
     if (std::find(s.extra.begin(), s.extra.end(), k) == s.extra.end()) s.extra.push_back(k);
@@ -660,15 +662,17 @@ void SweepDriver::rdm_step(int p, const Superblock& sb) {
   }
   std::vector<double> v;
   E_.expectations(sb, terms, v);
-  const int nroots = (int)(v.size() / std::max<size_t>(terms.size(), 1));
-  if ((int)rdm_.size() < nroots) rdm_.resize(nroots, std::vector<double>((size_t)N_ * N_, 0.0));
-  for (int r = 0; r < nroots; ++r)
-    for (size_t t = 0; t < terms.size(); ++t) {
-      const double g = v[(size_t)r * terms.size() + t];
-      const int i = at[t].first, j = at[t].second;
-      rdm_[r][(size_t)i * N_ + j] = g;
-      rdm_[r][(size_t)j * N_ + i] = g;
-    }
+  const size_t nt = terms.size();
+  const int nr = (int)std::lround(std::sqrt((double)(v.size() / std::max<size_t>(nt, 1))));
+  if ((int)rdm_.size() < nr * nr) rdm_.resize((size_t)nr * nr, std::vector<double>((size_t)N_ * N_, 0.0));
+  // <a|E_ij|b> from the term (i, j); <a|E_ji|b> = <b|E_ij|a> (real vectors)
+  for (int a = 0; a < nr; ++a)
+    for (int b = 0; b < nr; ++b)
+      for (size_t t = 0; t < nt; ++t) {
+        const int i = at[t].first, j = at[t].second;
+        rdm_[(size_t)a * nr + b][(size_t)i * N_ + j] = v[((size_t)a * nr + b) * nt + t];
+        rdm_[(size_t)a * nr + b][(size_t)j * N_ + i] = v[((size_t)b * nr + a) * nt + t];
+      }
 }
 
 std::vector<std::vector<double>> SweepDriver::onepdm_sweep(bool forward, int sweep_index) {
@@ -742,26 +746,33 @@ SweepResult SweepDriver::run() {
     const bool forward = ((res.sweeps - s_begin) % 2 == 0) == first_forward;
     const auto ts = std::chrono::steady_clock::now();
     auto g = onepdm_sweep(forward, last);
-    res.onepdm.assign(g.size(), std::vector<double>((size_t)N_ * N_, 0.0));
+    const int nr = (int)std::lround(std::sqrt((double)g.size()));
+    res.transition_onepdm.assign(g.size(), std::vector<double>((size_t)N_ * N_, 0.0));
     for (size_t r = 0; r < g.size(); ++r)
       for (int a = 0; a < N_; ++a)
         for (int b = 0; b < N_; ++b) {
           const int A = I_.order.empty() ? a : I_.order[a], B = I_.order.empty() ? b : I_.order[b];
-          res.onepdm[r][(size_t)A * N_ + B] = g[r][(size_t)a * N_ + b];
+          res.transition_onepdm[r][(size_t)A * N_ + B] = g[r][(size_t)a * N_ + b];
         }
+    for (int r = 0; r < nr; ++r) res.onepdm.push_back(res.transition_onepdm[(size_t)r * nr + r]);
     log(1, "onepdm sweep (%s): %.2fs\n", forward ? "fwd" : "bwd",
         std::chrono::duration<double>(std::chrono::steady_clock::now() - ts).count());
     if (!C_.prefix.empty())
-      for (size_t r = 0; r < res.onepdm.size(); ++r) {
-        // spatial_onepdm.r.r.txt (save_onepdm_spatial_text, onepdm.C:504-528)
-        const std::string path = C_.prefix + "/spatial_onepdm." + std::to_string(r) + "." + std::to_string(r) + ".txt";
-        FILE* f = std::fopen(path.c_str(), "w");
-        if (!f) throw std::runtime_error("cannot write " + path);
-        std::fprintf(f, "%d\n", N_);
-        for (int a = 0; a < N_; ++a)
-          for (int b = 0; b < N_; ++b) std::fprintf(f, "%d %d %20.14e\n", a, b, res.onepdm[r][(size_t)a * N_ + b]);
-        std::fclose(f);
-      }
+      for (int i = 0; i < nr; ++i)
+        for (int j = 0; j <= i; ++j) {
+          if (i != j && !C_.tran_onepdm) continue;
+          // spatial_onepdm.i.j.txt (save_onepdm_spatial_text, onepdm.C:504-528):
+          // element (k, l) = <i|E_kl|j>
+          const std::vector<double>& m = res.transition_onepdm[(size_t)i * nr + j];
+          const std::string path =
+              C_.prefix + "/spatial_onepdm." + std::to_string(i) + "." + std::to_string(j) + ".txt";
+          FILE* f = std::fopen(path.c_str(), "w");
+          if (!f) throw std::runtime_error("cannot write " + path);
+          std::fprintf(f, "%d\n", N_);
+          for (int a = 0; a < N_; ++a)
+            for (int b = 0; b < N_; ++b) std::fprintf(f, "%d %d %20.14e\n", a, b, m[(size_t)a * N_ + b]);
+          std::fclose(f);
+        }
   }
   res.energies = last_energies_;
   res.discarded = last_discarded_;

@@ -178,8 +178,9 @@ class Engine {
   virtual void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) = 0;
   // small = rotation^T big rotation for every operator of small's catalogue
   virtual void renormalise(Block& small, const Block& big) = 0;
-  // expectation values <psi_r| coef * [l x r]^0 |psi_r> of single pair terms
-  // for the last solve's vectors: out[root * terms.size() + t]
+  // matrix elements <psi_a| coef * [l x r]^0 |psi_b> of single pair terms
+  // between the last solve's vectors (nr of them):
+  // out[(a * nr + b) * terms.size() + t]
   virtual void expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) = 0;
 
  protected:
@@ -209,6 +210,8 @@ struct SweepResult {
   // `onepdm`: per root, the spin-summed spatial one-particle density matrix
   // gamma_ij = sum_s <a+_is a_js> (norb x norb row-major, input orbital order)
   std::vector<std::vector<double>> onepdm;
+  // with it, between roots a and b (index a * nroots + b): <a|E_ij|b>
+  std::vector<std::vector<double>> transition_onepdm;
   double discarded = 0.0;
   int sweeps = 0;
   double sigma_seconds = 0.0;
@@ -248,8 +251,9 @@ class SweepDriver {
   // left blocks [0..q] for q = 1..upto from seeded random rotations
   void warmup_left(int upto);
   double sweep(bool forward, int sweep_index);
-  // one sweep that also evaluates the one-particle density matrix (per root,
-  // norb x norb in the sweep's orbital order)
+  // one sweep that also evaluates the one-particle (transition) density
+  // matrices <psi_a|E_ij|psi_b> of the roots a, b at index a * nroots + b,
+  // norb x norb in the sweep's orbital order
   std::vector<std::vector<double>> onepdm_sweep(bool forward, int sweep_index);
   // Superblock of partition p (L=[0..p], R=[p+1..N-1]) built from warm-up
   // blocks on both sides: the sector structure and operator catalogue of a

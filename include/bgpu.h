@@ -429,6 +429,13 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
  * `prefix <dir>` when given).  The run evaluates it in one more sweep after
  * the last one. */
 int bgpu_onepdm(bgpu_ctx* ctx, int root, double* gamma, int norb);
+/* Transition one-particle density matrix gamma_ij = sum_s <bra| a+_is a_js
+ * |ket> between two state-averaged roots of the same run (norb x norb
+ * row-major, the FCIDUMP's orbital order); bra == ket gives bgpu_onepdm's
+ * matrix.  The reference's `tran_onepdm` writes the same values as
+ * spatial_onepdm.<bra>.<ket>.txt (bra > ket); this run does so under
+ * `prefix <dir>` with that keyword. */
+int bgpu_transition_onepdm(bgpu_ctx* ctx, int bra, int ket, double* gamma, int norb);
 /* Arithmetic of the last bgpu_run_dmrg (no reference counterpart), out[n]:
  * split-precision products and their seconds, FP64 products and their
  * seconds, defect-correction rounds, the FP64 product time the same

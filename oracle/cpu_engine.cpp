@@ -589,19 +589,21 @@ void CpuEngine::add_noise(const Superblock& sb, bool left, std::vector<std::vect
 // <psi_r| T |psi_r> of single pair terms: the product of one term
 // (TensorMultiply over its couplings) dotted with the wavefunction.
 void CpuEngine::expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) {
-  const int nt = (int)terms.size();
-  out.assign(waves_.size() * terms.size(), 0.0);
+  const size_t nt = terms.size(), nr = waves_.size();
+  out.assign(nr * nr * nt, 0.0);
   std::vector<double> y(sb.size);
-  for (int t = 0; t < nt; ++t) {
+  for (size_t t = 0; t < nt; ++t) {
     Superblock one = sb;
     one.terms.assign(1, terms[t]);
     one.ecore = 0.0;
-    for (size_t r = 0; r < waves_.size(); ++r) {
+    for (size_t b = 0; b < nr; ++b) {
       std::fill(y.begin(), y.end(), 0.0);
-      sigma(one, waves_[r].data(), y.data());
-      double d = 0.0;
-      for (int64_t e = 0; e < sb.size; ++e) d += waves_[r][e] * y[e];
-      out[r * terms.size() + t] = d;
+      sigma(one, waves_[b].data(), y.data());
+      for (size_t a = 0; a < nr; ++a) {
+        double d = 0.0;
+        for (int64_t e = 0; e < sb.size; ++e) d += waves_[a][e] * y[e];
+        out[(a * nr + b) * nt + t] = d;
+      }
     }
   }
 }

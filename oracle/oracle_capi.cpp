@@ -122,12 +122,23 @@ int oracle_use_blas(const char* path) {
 
 static std::vector<double> g_last_sweep_energies;  // per sweep, lowest root, of the last oracle_run
 static std::vector<std::vector<double>> g_last_onepdm;  // per root, of the last oracle_run with onepdm
+static std::vector<std::vector<double>> g_last_tonepdm;  // per root pair (bra * nroots + ket)
 
 // the one-particle density matrix of a root of the last oracle_run (0 on success)
 int oracle_onepdm(int root, double* out, int norb) {
   if (root < 0 || root >= (int)g_last_onepdm.size()) return 1;
   if ((size_t)norb * norb != g_last_onepdm[root].size()) return 2;
   std::copy(g_last_onepdm[root].begin(), g_last_onepdm[root].end(), out);
+  return 0;
+}
+
+// <bra|E_ij|ket> between two roots of the last oracle_run (0 on success)
+int oracle_transition_onepdm(int bra, int ket, double* out, int norb) {
+  const int nr = (int)g_last_onepdm.size();
+  if (bra < 0 || bra >= nr || ket < 0 || ket >= nr) return 1;
+  const auto& m = g_last_tonepdm[(size_t)bra * nr + ket];
+  if ((size_t)norb * norb != m.size()) return 2;
+  std::copy(m.begin(), m.end(), out);
   return 0;
 }
 
@@ -139,6 +150,7 @@ int oracle_sweep_energies(double* out, int cap) {
 
 int oracle_run(const char* conf, int threads, int verbose, double* energies, int max_roots, double* stats) {
   g_last_onepdm.clear();
+  g_last_tonepdm.clear();
   g_last_sweep_energies.clear();
   try {
     auto t0 = std::chrono::steady_clock::now();
@@ -154,6 +166,7 @@ int oracle_run(const char* conf, int threads, int verbose, double* energies, int
     }
     g_last_sweep_energies = r.sweep_energies;
     g_last_onepdm = r.onepdm;
+    g_last_tonepdm = r.transition_onepdm;
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {
       stats[0] = r.sweeps;

@@ -261,3 +261,15 @@ def onepdm(root, norb):
     if L.oracle_onepdm(root, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), norb):
         raise RuntimeError("no one-particle density matrix of root %d" % root)
     return g
+
+
+def transition_onepdm(bra, ket, norb):
+    """<bra|E_ij|ket> between two roots of the last run() of a configuration
+    with the onepdm (or tran_onepdm) keyword."""
+    L = lib()
+    L.oracle_transition_onepdm.restype = ctypes.c_int
+    L.oracle_transition_onepdm.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    g = np.zeros((norb, norb))
+    if L.oracle_transition_onepdm(bra, ket, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), norb):
+        raise RuntimeError("no transition density matrix of roots %d, %d" % (bra, ket))
+    return g

@@ -3,7 +3,11 @@
 Copies the FCIDUMP inputs of the reference's energy tests (data files only)
 and records the expected energies its test scripts check:
   dmrg_tests/runtest:12,23,30 (test_energy.py tolerance 1e-6) and
-  pydmrg/tests/test_dmrg_simple.py:34 (10 decimal places).
+  pydmrg/tests/test_dmrg_simple.py:34 (10 decimal places);
+and copies the spatial one-particle density matrices its 1-RDM tests check
+(dmrg_tests/runtest:31,141,152-154; test_onepdm.py and
+test_transitiononepdm.py: sum of squared differences within 1e-7, the
+transition matrix up to an overall sign).
 Run where the reference tree is available, with its path as the required
 argument (python make_fixtures.py <reference tree>); the tests read only
 the committed copies.
@@ -33,6 +37,26 @@ CASES = {
     "h2o_nosym": ("dmrg_tests/h2o_nosym/FCIDUMP",
                   "nelec 10\nspin 0\nirrep 1\nhf_occ integral\nschedule default\nstartM 100\nmaxM 300\nsweep_tol tight\n",
                   [-76.11460447], "dmrg_tests/runtest:23"),
+    # h2o_transitionpdm/dmrg_onepdm.conf without its noise column and
+    # twodot_to_onedot; no energy test in runtest (energies None)
+    "h2o_c2v": ("dmrg_tests/h2o_transitionpdm/FCIDUMP",
+                "nelec 10\nspin 0\nhf_occ integral\nschedule\n0 50 1.0e-6 0\n4 150 1e-6 0\n6 200 1e-6 0\n8 500 1e-8 0\nend\n"
+                "maxiter 30\nsweep_tol 1e-9\nsym c2v\nirrep 1\nnroots 2\nweights 0.5 0.5\n",
+                None, "dmrg_tests/runtest:149-154"),
+}
+
+# case: [(source, file name here, (bra, ket), citation)]; the hubbard root-1
+# matrix comes from the transition test of the same FCIDUMP and schedule
+ONEPDM = {
+    "hubbard": [("dmrg_tests/hubbard/spat_onepdm.0.0.txt", "spat_onepdm.0.0.txt", (0, 0), "dmrg_tests/runtest:31"),
+                ("dmrg_tests/hubbard_transition_pdm/spat_onepdm.1.1.txt", "spat_onepdm.1.1.txt", (1, 1),
+                 "dmrg_tests/runtest:141")],
+    "h2o_c2v": [("dmrg_tests/h2o_transitionpdm/spat_onepdm.0.0.txt", "spat_onepdm.0.0.txt", (0, 0),
+                 "dmrg_tests/runtest:152"),
+                ("dmrg_tests/h2o_transitionpdm/spat_onepdm.1.1.txt", "spat_onepdm.1.1.txt", (1, 1),
+                 "dmrg_tests/runtest:153"),
+                ("dmrg_tests/h2o_transitionpdm/spat_onepdm.1.0.txt", "spat_onepdm.1.0.txt", (1, 0),
+                 "dmrg_tests/runtest:154")],
 }
 
 
@@ -50,6 +74,14 @@ def main(argv):
         with open(os.path.join(d, "FCIDUMP"), "rb") as f:
             sha = hashlib.sha256(f.read()).hexdigest()
         meta[name] = dict(energies=energies, source=src, cited=cite, sha256=sha, tolerance=1e-6)
+        pdms = []
+        for psrc, dst, (bra, ket), pcite in ONEPDM.get(name, []):
+            shutil.copyfile(os.path.join(ref, psrc), os.path.join(d, dst))
+            with open(os.path.join(d, dst), "rb") as f:
+                psha = hashlib.sha256(f.read()).hexdigest()
+            pdms.append(dict(file=dst, bra=bra, ket=ket, source=psrc, cited=pcite, sha256=psha, sumsq=1e-7))
+        if pdms:
+            meta[name]["onepdm"] = pdms
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1)
 

@@ -11,13 +11,18 @@ Tolerances written here:
     sweep energies differ by about 1e-7 Eh, and gamma is first order in the
     wavefunction's difference);
   - the same case in split precision (bf16x3tc with defect correction)
-    against the FP64 GPU gamma within 1e-5."""
+    against the FP64 GPU gamma within 1e-5;
+  - the reference's own 1-RDM tables (Hubbard roots 0 and 1, C2v water
+    roots 0 and 1 and <1|E_kl|0>) within its measure, a sum of squared
+    differences at most 1e-7, and the transition matrices within 1e-6 of
+    the oracle's."""
 import numpy as np
 import pytest
 
 from conftest import conf
 from test_oracle_fci import write_fcidump
-from test_oracle_onepdm import CASES, fci_onepdm, onepdm_conf, read_spatial_onepdm
+from test_oracle_onepdm import (CASES, check_golden_onepdm, fci_onepdm, golden_onepdm_cases, onepdm_conf,
+                                onepdm_golden_conf, read_spatial_onepdm)
 
 pytestmark = pytest.mark.gpu
 
@@ -69,3 +74,17 @@ def test_onepdm_needs_the_keyword(gpu_ctx):
     gpu_ctx.run_dmrg(conf("syn8"))
     with pytest.raises(block_gb300.BgpuError):
         gpu_ctx.onepdm(0, 8)
+
+
+@pytest.mark.parametrize("name,pdms", golden_onepdm_cases(), ids=lambda x: x if isinstance(x, str) else "")
+def test_onepdm_matches_reference_tables(gpu_ctx, oracle, tmp_path, name, pdms):
+    c = onepdm_golden_conf(tmp_path, name, "tran_onepdm")
+    oracle.run(c)
+    n = 8 if name == "hubbard" else 7
+    go = {(a, b): oracle.transition_onepdm(a, b, n) for a in range(2) for b in range(2)}
+    gpu_ctx.run_dmrg(c)
+    check_golden_onepdm(name, pdms, lambda a, b, m: gpu_ctx.transition_onepdm(a, b, m), tmp_path)
+    for (a, b), g in go.items():
+        gg = gpu_ctx.transition_onepdm(a, b, n)
+        d = min(np.max(np.abs(gg - g)), np.max(np.abs(gg + g)) if a != b else np.inf)
+        assert d <= 1e-6, (a, b, d)

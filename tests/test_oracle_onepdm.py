@@ -12,7 +12,14 @@ gamma), a run whose orbitals the sweep reorders, with gamma reported in
 the input orbital order (save_onepdm_spatial_text, onepdm.C:504-528), and
 the two state-averaged roots of the 8-site Hubbard case with its final
 Davidson tolerance tightened to 1e-12 (one gamma per root, 2e-6: the
-second root's solve ends with a larger residual, observed 7e-7)."""
+second root's solve ends with a larger residual, observed 7e-7).
+
+The reference's own tables pin the same sweep: its 8-site Hubbard roots 0
+and 1 and its C2v water roots 0, 1 and their transition matrix <1|E_kl|0>
+(dmrg_tests/runtest:31,141,152-154) within the reference's measure, the sum
+of squared differences at most 1e-7 (observed 8.5e-10, 1.9e-11, 8.3e-9 and
+3.4e-8 for the water matrices and the Hubbard root 0)."""
+import json
 import os
 
 import numpy as np
@@ -89,3 +96,45 @@ def test_onepdm_needs_the_keyword(oracle):
     oracle.run(os.path.join(GOLDEN, "syn8", "dmrg.conf"))
     with pytest.raises(RuntimeError):
         oracle.onepdm(0, 8)
+
+
+def golden_onepdm_cases():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        meta = json.load(f)
+    return [(name, m["onepdm"]) for name, m in meta.items() if "onepdm" in m]
+
+
+def onepdm_golden_conf(tmp_path, name, keyword):
+    d = os.path.join(GOLDEN, name)
+    body = open(os.path.join(d, "dmrg.conf")).read()
+    body = body.replace("orbitals FCIDUMP", "orbitals %s" % os.path.join(d, "FCIDUMP"))
+    conf = tmp_path / "dmrg.conf"
+    conf.write_text(body + "%s\nprefix %s\n" % (keyword, tmp_path))
+    return str(conf)
+
+
+def check_golden_onepdm(name, pdms, get, tmp_path):
+    """The reference's own 1-RDM tables (test_onepdm.py: sum of squared
+    differences within 1e-7; test_transitiononepdm.py: the same, up to an
+    overall sign of the transition matrix) against `get(bra, ket)` and the
+    files the run wrote."""
+    norb = None
+    for p in pdms:
+        gr = read_spatial_onepdm(os.path.join(GOLDEN, name, p["file"]))
+        norb = gr.shape[0]
+        g = get(p["bra"], p["ket"], norb)
+        d = min(np.sum((g - gr) ** 2), np.sum((g + gr) ** 2) if p["bra"] != p["ket"] else np.inf)
+        assert d <= p["sumsq"], (name, p["file"], d)
+        gt = read_spatial_onepdm(tmp_path / ("spatial_onepdm.%d.%d.txt" % (p["bra"], p["ket"])))
+        assert np.max(np.abs(gt - g)) <= 1e-13 * np.max(np.abs(g))
+
+
+@pytest.mark.parametrize("name,pdms", golden_onepdm_cases(), ids=lambda x: x if isinstance(x, str) else "")
+def test_onepdm_matches_reference_tables(oracle, tmp_path, name, pdms):
+    conf = onepdm_golden_conf(tmp_path, name, "tran_onepdm")
+    oracle.run(conf)
+    check_golden_onepdm(name, pdms, lambda a, b, n: oracle.transition_onepdm(a, b, n), tmp_path)
+    # bra == ket is the root's density matrix
+    for r in range(2):
+        assert np.array_equal(oracle.transition_onepdm(r, r, 8 if name == "hubbard" else 7),
+                              oracle.onepdm(r, 8 if name == "hubbard" else 7))
