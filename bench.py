@@ -435,7 +435,8 @@ def run_ours(a):
             dv[prec] = {"seconds": time.perf_counter() - t0, "iterations": it, "energy": float(e[0]),
                         "graph_launches": ctx.davidson_graph_launches()}
             if prec != "fp64":
-                dv[prec].update(defect_rounds=r1 - r0, fp64_products=f1 - f0, fp64_residual_verified=bool(ver))
+                dv[prec].update(defect_rounds=r1 - r0, fp64_products=f1 - f0, fp64_residual_verified=bool(ver),
+                                verified_on=["none", "fp64 residuals", "fp64 residual bounds"][ver])
         ctx.set_precision(a.precision)
         if split and ms64 is not None:
             if "fp64" in dv:

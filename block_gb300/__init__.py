@@ -439,10 +439,11 @@ class Context:
         self._check(self.lib.bgpu_set_refinement(self.h, {"energy": 0, "defect": 1}[mode]))
 
     def refinement_stats(self):
-        """(FP64 restarts, FP64 products, last solve verified on FP64 residuals)."""
+        """(FP64 restarts, FP64 products, how the last solve was verified:
+        0 not, 1 on FP64 residuals, 2 on FP64 residual bounds)."""
         a, b, c = _I64(), _I64(), _I()
         self._check(self.lib.bgpu_refinement_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return a.value, b.value, bool(c.value)
+        return a.value, b.value, c.value
 
     def onepdm(self, root, norb):
         """Spatial one-particle density matrix of a root from the last
@@ -502,9 +503,10 @@ class Context:
         self._check(self.lib.bgpu_sweep_energies(self.h, _dp(sw), len(sw), ctypes.byref(ns)))
         stats["sweep_energies"] = sw[:min(ns.value, len(sw))].copy()
         nsw = len(stats["sweep_energies"])
-        rs = np.zeros(7 + nsw)
+        rs = np.zeros(8 + nsw)
         self._check(self.lib.bgpu_run_stats(self.h, _dp(rs), len(rs)))
         stats.update(split_sigma_calls=int(rs[0]), split_sigma_seconds=rs[1], fp64_sigma_calls=int(rs[2]),
                      fp64_sigma_seconds=rs[3], defect_rounds=int(rs[4]), derived_fp64_sigma_seconds=rs[5],
-                     warmup_seconds=rs[6], sweep_seconds=rs[7:7 + nsw].copy())
+                     warmup_seconds=rs[6], bounded_verifications=int(rs[7]),
+                     sweep_seconds=rs[8:8 + nsw].copy())
         return e[:nroots].copy(), stats

@@ -245,7 +245,8 @@ int bgpu_refinement_stats(bgpu_ctx* ctx, int64_t* rounds, int64_t* fp64_products
     need(ctx->eng != nullptr, "no device");
     if (rounds) *rounds = ctx->eng->defect_rounds_;
     if (fp64_products) *fp64_products = ctx->eng->defect_fp64_sigma_;
-    if (last_verified) *last_verified = ctx->eng->last_fp64_verified_ ? 1 : 0;
+    if (last_verified)
+      *last_verified = ctx->eng->last_fp64_verified_ ? (ctx->eng->last_defect_bounded_ ? 2 : 1) : 0;
   });
 }
 
@@ -787,7 +788,7 @@ int bgpu_diagonalise(bgpu_ctx* ctx, int nmat, const int* dims, const double* a, 
     e.free(dz);
     e.free(dw);
     for (int j = 0; j < nmat; ++j)
-      if (hs[j] < 0) throw std::runtime_error("bgpu_diagonalise: QL iteration did not converge for matrix " +
+      if (hs[j] < 0) throw std::runtime_error("bgpu_diagonalise: tridiagonal solver did not converge for matrix " +
                                               std::to_string(j));
     if (eigvecs)  // column-major per matrix -> row-major with the eigenvectors as columns
       for (int j = 0; j < nmat; ++j) {
@@ -941,7 +942,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     const double d0 = ctx->eng->renorm_device_seconds;
     const long c0 = ctx->eng->sigma_calls;
     GpuEngine& E = *ctx->eng;
-    const long sc0 = E.split_calls, fc0 = E.fp64_calls, dr0 = E.defect_rounds_;
+    const long sc0 = E.split_calls, fc0 = E.fp64_calls, dr0 = E.defect_rounds_, db0 = E.defect_bounded_;
     const double ss0 = E.split_seconds, fs0 = E.fp64_seconds, dv0 = E.derived_fp64_sigma_seconds;
     SweepResult r;
     {
@@ -954,7 +955,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     ctx->tonepdm = r.transition_onepdm;
     ctx->run_stats = {(double)(E.split_calls - sc0), E.split_seconds - ss0, (double)(E.fp64_calls - fc0),
                       E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
-                      r.warmup_seconds};
+                      r.warmup_seconds, (double)(E.defect_bounded_ - db0)};
     for (double t : r.sweep_seconds) ctx->run_stats.push_back(t);
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {

@@ -1,6 +1,7 @@
 // Host side of the CUDA engine: compiles the operator algebra of a sweep
 // step into device work lists and drives the kernels of kernels.cu.
 #include "gpu_engine.h"
+#include "k_dc.cuh"
 #include "k_noise.cuh"
 
 #include <algorithm>
@@ -14,6 +15,7 @@
 #include "../host/dense.h"
 
 #include <deque>
+#include <functional>
 #include <mutex>
 #include <queue>
 #include <set>
@@ -1713,6 +1715,7 @@ void GpuEngine::autotune_tc(const Superblock& sb, SigmaPlan& p) {
 
 void GpuEngine::load_tune_cache(const std::string& path) {
   tune_cache_path = path;
+  tune_cache.clear();  // a cache file replaces the choices held so far
   if (path.empty()) return;
   FILE* f = std::fopen(path.c_str(), "r");
   if (!f) return;
@@ -2094,10 +2097,27 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   // precision; the solve ends when a restart's FP64 residuals of every root
   // are below tol without any new basis vector (linear.C:301-335 applied to
   // the FP64 residual).
+  //
+  // After a restart every sigma row carries a bound of its difference from
+  // the FP64 product (DavCtl::eb): 0 for the restart vectors, eps for each
+  // correction, carried through the Ritz rotations.  eps is kEpsSafety times
+  // the largest difference |S_i - H_64 x_i| seen on this superblock when the
+  // split-precision Ritz vectors x_i got their FP64 products (each a sum of
+  // split products of unit vectors).  A restart that converges after adding
+  // corrections is accepted without another FP64 product when
+  // (|r_i| + eb_i)^2 <= tol for every root: the FP64 residual of a vector
+  // sum_j y_j b_j is the subspace residual plus sum_j y_j (H_64 b_j - S_j).
   bool fp64_verified = false;
   last_defect_rounds_ = 0;
+  last_defect_bounded_ = false;
   if (precision_slices(precision) && refine_mode == 1) {
+    constexpr double kEpsSafety = 4.0;
+    double eps = 0.0;
+    double* prev = alloc((int64_t)nroots * n);  // split-precision sigma rows
     for (int round = 0; round < kDefectRounds; ++round) {
+      if (round == 0)
+        cuda_check(cudaMemcpyAsync(prev, S, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
+                   "copy sigma rows");
       for (int i = 0; i < nroots; ++i) {
         auto t0 = std::chrono::steady_clock::now();
         sigma(sb, plan_, row(B, i), row(S, i));
@@ -2108,6 +2128,15 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
         ++fp64_calls;
         ++defect_fp64_sigma_;
       }
+      if (round == 0) {
+        for (int i = 0; i < nroots; ++i) {
+          double d2;
+          cuda_check(dev::launch_axpy(-1.0, row(S, i), prev + (int64_t)i * n, n, stream_), "sigma difference");
+          dots(prev + (int64_t)i * n, 1, prev + (int64_t)i * n, &d2);
+          eps = std::max(eps, kEpsSafety * std::sqrt(std::max(d2, 0.0)));
+        }
+        last_split_eps_ = eps;
+      }
       dev::DavCtl c1{};
       std::vector<double> col(nroots);
       for (int j = 0; j < nroots; ++j) {
@@ -2116,6 +2145,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
       }
       c1.k = nroots;
       c1.mode = 2;
+      c1.eps = eps;
       cuda_check(cudaMemcpyAsync(sc.ctl, &c1, sizeof(c1), cudaMemcpyHostToDevice, stream_), "h2d ctl");
       sync();
       ++last_defect_rounds_;
@@ -2125,7 +2155,26 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
         fp64_verified = true;
         break;
       }
+      if (dav_host_->done && eps > 0.0) {
+        double rn[dev::kDavMax], eb[dev::kDavMax];
+        const dev::DavCtl* dc = sc.ctl;
+        cuda_check(cudaMemcpyAsync(rn, dc->rn, nroots * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+        cuda_check(cudaMemcpyAsync(eb, dc->eb, nroots * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+        sync();
+        bool ok = true;
+        for (int i = 0; i < nroots; ++i) {
+          const double bound = std::sqrt(std::max(rn[i], 0.0)) + eb[i];
+          ok = ok && bound * bound <= p.tol;
+        }
+        if (ok) {
+          fp64_verified = true;
+          last_defect_bounded_ = true;
+          ++defect_bounded_;
+          break;
+        }
+      }
     }
+    free(prev);
     laps.lap("defect correction");
   }
   energies.assign(dav_host_->lam, dav_host_->lam + nroots);
@@ -2585,7 +2634,9 @@ std::string GpuEngine::step_stats() {
                 fp64_calls > last_fp64_calls_ ? (fp64_seconds - last_fp64_seconds_) / (fp64_calls - last_fp64_calls_)
                                               : 0.0,
                 precision_slices(precision) && refine_mode == 1
-                    ? (last_fp64_verified_ ? ", FP64 residuals met tol" : ", FP64 residuals NOT verified")
+                    ? (last_fp64_verified_ ? (last_defect_bounded_ ? ", FP64 residual bounds met tol"
+                                                                   : ", FP64 residuals met tol")
+                                           : ", FP64 residuals NOT verified")
                     : "");
   // what the step's Davidson products would have cost in FP64: every product
   // of the step (split or FP64) at the step's measured FP64 product time
@@ -2738,7 +2789,7 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
   for (int q = 0; q < nq; ++q)
     if (st[q] < 0) throw std::runtime_error("density-matrix eigensolver did not converge");
   for (int x : info)
-    if (x != 0) throw std::runtime_error("density-matrix eigensolver (QL iteration) did not converge");
+    if (x != 0) throw std::runtime_error("density-matrix eigensolver (tridiagonal divide and conquer) did not converge");
   spec.eig.assign(nq, {});
   for (int q = 0; q < nq; ++q) spec.eig[q].assign(hw.begin() + woff[q], hw.begin() + woff[q] + B.si.states[q]);
   du.release(stream_);
@@ -3031,7 +3082,7 @@ int* GpuEngine::eigh_batched(const std::vector<int>& dims, double* a, const std:
   const int nj = (int)dims.size();
   std::vector<dev::EigJob> jobs(nj);
   int64_t work = 0;
-  int tiles = 0, ql = 0, bt = 0, max_n = 0;
+  int tiles = 0, bt = 0, max_n = 0;
   for (int j = 0; j < nj; ++j) max_n = std::max(max_n, dims[j]);
   if (max_n > dev::kEigMaxN)
     throw std::runtime_error("eigensolver: matrix of order " + std::to_string(max_n) + " above the limit " +
@@ -3054,8 +3105,6 @@ int* GpuEngine::eigh_batched(const std::vector<int>& dims, double* a, const std:
     work += dev::eig_scalar_elems(n);
     J.tile0 = tiles;
     tiles += J.nt * (J.nt + 1) / 2;
-    J.ql0 = ql;
-    ql += (n + dev::kEigQlRows - 1) / dev::kEigQlRows;
     J.bt0 = bt;
     bt += (n + bt_cols - 1) / bt_cols;
   }
@@ -3071,10 +3120,152 @@ int* GpuEngine::eigh_batched(const std::vector<int>& dims, double* a, const std:
   DevArray<dev::EigJob> dj;
   dj.upload(jobs, stream_);
   dev::EigBufs eb{copy_inputs ? wk : a, z, w, wk, status};
-  cuda_check(dev::launch_eig(eb, dj.d, nj, max_n, tiles, ql, bt, stream_), "eigensolver");
+  cuda_check(dev::launch_eig_tridiag(eb, dj.d, nj, max_n, tiles, stream_), "eigensolver tridiagonalisation");
+  tridiagonal_dc(jobs, dj.d, wk, status);
+  cuda_check(dev::launch_eig_backtransform(eb, dj.d, nj, max_n, bt, stream_), "eigensolver back-transformation");
   dj.release(stream_);
   free(wk);
   return status;
+}
+
+// Divide and conquer on the tridiagonal matrices of an eigensolver batch
+// (k_dc.cuh): the tree of every job (halves down to leaves of at most
+// kDcLeaf rows), the tears, the leaves, then the merges level by level
+// (a merge's level is its height in its tree, so that both its children are
+// done).  Each level reads back its merges' pole counts to lay out the
+// eigenvector GEMM.
+void GpuEngine::tridiagonal_dc(const std::vector<dev::EigJob>& jobs, const dev::EigJob* djobs, double* wk,
+                               int* status) {
+  std::vector<dev::DcLeaf> leaves;
+  std::vector<std::vector<dev::DcMerge>> levels;
+  std::function<int(int, int, int)> tree = [&](int job, int o, int len) -> int {
+    if (len <= dev::kDcLeaf) {
+      leaves.push_back({job, o, len, 0});
+      return 0;
+    }
+    const int n1 = len / 2;
+    const int h = 1 + std::max(tree(job, o, n1), tree(job, o + n1, len - n1));
+    if ((int)levels.size() < h) levels.resize(h);
+    dev::DcMerge m{};
+    m.job = job;
+    m.o = o;
+    m.n1 = n1;
+    m.nm = len;
+    levels[h - 1].push_back(m);
+    return h;
+  };
+  for (int j = 0; j < (int)jobs.size(); ++j) {
+    // the merges write only the diagonal blocks of Z: the rest stays zero
+    cuda_check(cudaMemsetAsync(wk + jobs[j].q_off, 0, (size_t)jobs[j].n * jobs[j].n * sizeof(double), stream_),
+               "memset Z");
+    if (jobs[j].n > 0) tree(j, 0, jobs[j].n);
+  }
+  std::vector<dev::DcMerge> all;
+  for (const auto& lv : levels) all.insert(all.end(), lv.begin(), lv.end());
+  DevArray<dev::DcMerge> dall;
+  DevArray<dev::DcLeaf> dleaves;
+  dall.upload(all, stream_);
+  dleaves.upload(leaves, stream_);
+  cuda_check(dev::launch_dc_tear(wk, djobs, dall.d, (int)all.size(), stream_), "tears");
+  cuda_check(dev::launch_dc_leaves(wk, djobs, dleaves.d, (int)leaves.size(), status, stream_), "leaves");
+  for (auto& lv : levels) {
+    int64_t slots = 0, sq = 0;
+    int max_nm = 0;
+    for (auto& m : lv) {
+      m.x_off = slots;
+      m.u_off = m.g_off = sq;
+      slots += m.nm;
+      sq += (int64_t)m.nm * m.nm;
+      max_nm = std::max(max_nm, m.nm);
+    }
+    const int nm_ = (int)lv.size();
+    DevArray<dev::DcMerge> dm;
+    dm.upload(lv, stream_);
+    // doubles: rotation values (2 per slot), U, G, per slot dk, zk, tau,
+    // zhat, per merge rho; ints: rotation columns (2 per slot), per slot
+    // col, org, per merge K, nrot (vector members first and 16-byte aligned)
+    const int64_t sq2 = (sq + 1) & ~1ll;
+    double* dbl = alloc(2 * slots + 2 * sq2 + 4 * slots + nm_);
+    int* ints = nullptr;
+    cuda_check(cudaMallocAsync((void**)&ints, (size_t)(4 * slots + 2 * nm_) * sizeof(int), stream_), "alloc");
+    dev::DcLevel L{};
+    L.merges = dm.d;
+    L.nmerges = nm_;
+    L.nslots = slots;
+    L.rot_cs = reinterpret_cast<double2*>(dbl);
+    L.U = dbl + 2 * slots;
+    L.G = L.U + sq2;
+    L.dk = L.G + sq2;
+    L.zk = L.dk + slots;
+    L.tau = L.zk + slots;
+    L.zhat = L.tau + slots;
+    L.rho = L.zhat + slots;
+    L.rot_cols = reinterpret_cast<int2*>(ints);
+    L.col = ints + 2 * slots;
+    L.org = L.col + slots;
+    L.K = L.org + slots;
+    L.nrot = L.K + nm_;
+    cuda_check(dev::launch_dc_deflate(wk, djobs, L, max_nm, stream_), "merge deflation");
+    std::vector<int> K(nm_);
+    cuda_check(cudaMemcpyAsync(K.data(), L.K, nm_ * sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h K");
+    cuda_check(dev::launch_dc_roots(wk, djobs, L, status, stream_), "merge roots");
+    sync();
+    std::vector<dev::GemmUnit> units;
+    std::vector<dev::GemmItem> items;
+    std::vector<dev::GemmTask> tasks;
+    for (int i = 0; i < nm_; ++i) {
+      if (K[i] <= 0) continue;
+      const dev::DcMerge& m = lv[i];
+      const dev::EigJob& J = jobs[m.job];
+      // Z columns [o, o+K) of rows [o, o+nm) = (G[:, 0:K) U)^T as rows:
+      // C (K x nm) = U^T (K x K, row-major view of column-major U) G^T
+      dev::GemmUnit u{};
+      u.c_buf = 2;
+      u.c_off = J.q_off + (int64_t)m.o * J.n + m.o;
+      u.ldc = J.n;
+      u.m = K[i];
+      u.n = m.nm;
+      u.beta_one = 0;
+      u.ibeg = (int)items.size();
+      dev::GemmItem it{};
+      it.a_buf = 0;
+      it.a_off = m.u_off;
+      it.lda = K[i];
+      it.ta = 0;
+      it.b_buf = 1;
+      it.b_off = m.g_off;
+      it.ldb = m.nm;
+      it.tb = 0;
+      it.k = K[i];
+      it.alpha = 1.0;
+      items.push_back(it);
+      u.iend = (int)items.size();
+      units.push_back(u);
+    }
+    for (int u = 0; u < (int)units.size(); ++u) add_tasks(tasks, u, units[u].m, units[u].n);
+    if (!tasks.empty()) {
+      DevArray<dev::GemmUnit> du;
+      DevArray<dev::GemmItem> di;
+      DevArray<dev::GemmTask> dt;
+      du.upload(units, stream_);
+      di.upload(items, stream_);
+      dt.upload(tasks, stream_);
+      dev::Bufs bufs{};
+      bufs.p[0] = L.U;
+      bufs.p[1] = L.G;
+      bufs.p[2] = wk;
+      cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)tasks.size(), stream_), "merge eigenvectors");
+      du.release(stream_);
+      di.release(stream_);
+      dt.release(stream_);
+    }
+    cuda_check(dev::launch_dc_finish(wk, djobs, L, stream_), "merge deflated columns");
+    dm.release(stream_);
+    free(dbl);
+    cudaFreeAsync(ints, stream_);
+  }
+  dall.release(stream_);
+  dleaves.release(stream_);
 }
 
 void GpuEngine::select_rotation(const std::vector<std::vector<int>>& kept) {

@@ -225,6 +225,8 @@ class GpuEngine : public Engine {
   // of per-matrix status words for the caller to read and free
   int* eigh_batched(const std::vector<int>& dims, double* a, const std::vector<int64_t>& a_off, bool copy_inputs,
                     double* z, const std::vector<int64_t>& z_off, double* w, const std::vector<int64_t>& w_off);
+  // divide and conquer on the tridiagonal matrices of an eigensolver batch
+  void tridiagonal_dc(const std::vector<dev::EigJob>& jobs, const dev::EigJob* djobs, double* wk, int* status);
   int64_t wave_size() const { return wave_n_; }
   Precision precision = Precision::FP64;
   // split-precision solves: 1 (default) defect correction against FP64
@@ -234,6 +236,11 @@ class GpuEngine : public Engine {
   int last_defect_rounds_ = 0;             // FP64 restarts of the last solve
   bool last_fp64_verified_ = false;        // its roots met tol on FP64 residuals
   long defect_rounds_ = 0, defect_fp64_sigma_ = 0;  // totals over all solves
+  // the last solve was accepted on the error bound of its corrections'
+  // sigma rows (no FP64 product after its last restart); solves so accepted
+  bool last_defect_bounded_ = false;
+  long defect_bounded_ = 0;
+  double last_split_eps_ = 0.0;  // the bound eps of one split product (last solve)
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
   double sigma_flops = 0.0;

@@ -138,6 +138,16 @@ __global__ void dav_decide_root(DavBufs b) {
   if (threadIdx.x != 0) return;
   DavCtl* c = b.ctl;
   for (int i = 0; i < c->k; ++i) c->lam[i] = c->w[i];
+  if (c->eps > 0.0) {  // the rotation X_r <- sum_i alpha[i k + r] X_i of dav_rotate
+    const int k = c->k;
+    double nb[kDavMax];
+    for (int r = 0; r < k; ++r) {
+      double s = 0.0;
+      for (int i = 0; i < k; ++i) s += fabs(c->alpha[i * k + r]) * c->eb[i];
+      nb[r] = s;
+    }
+    for (int r = 0; r < k; ++r) c->eb[r] = nb[r];
+  }
   int conv = c->conv;
   for (int i = 0; i < conv; ++i)
     if (c->rn[i] > b.tol) {
@@ -259,7 +269,10 @@ __global__ void __launch_bounds__(kNT) dav_append(DavBufs b) {
 
 __global__ void dav_finish(DavCtl* c) {
   if (threadIdx.x != 0) return;
-  if (c->expand) ++c->k;
+  if (c->expand) {
+    c->eb[c->k] = c->eps;
+    ++c->k;
+  }
   c->mode = c->expand ? 1 : 0;
 }
 

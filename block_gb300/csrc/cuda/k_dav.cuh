@@ -38,6 +38,12 @@ struct DavCtl {
   double w[kDavMax];          // eigenvalues of the subspace matrix
   double h[kDavMax * kDavMax];      // subspace matrix (leading dimension k)
   double alpha[kDavMax * kDavMax];  // its eigenvectors as columns
+  // Error bounds of the sigma rows: eb[i] >= |S_i - H_64 B_i| (FP64 product),
+  // carried through the Ritz rotations as sum_j |alpha_ji| eb_j; a vector
+  // appended while eps > 0 gets eb = eps (the bound of one split-precision
+  // product of a unit vector).  eps = 0: no bookkeeping.
+  double eb[kDavMax];
+  double eps;
 };
 constexpr size_t kDavHeaderBytes = offsetof(DavCtl, zero);
 

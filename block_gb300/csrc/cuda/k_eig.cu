@@ -9,10 +9,10 @@
 // one pass over the matrix: column k of A^(k) is formed lazily from the
 // stored column (still A^(k-1)) and the rank-2 correction of step k-1.
 //
-// The tridiagonal eigenproblem uses the implicit QL iteration with the
-// Wilkinson shift of the leading 2 x 2 block (Bowdler, Martin, Reinsch and
-// Wilkinson, "The QR and QL algorithms for symmetric matrices",
-// Numer. Math. 11 (1968) 293-306), restated here for streamed rotations.
+// The tridiagonal eigenproblem is solved by divide and conquer (k_dc.cu);
+// its leaves use the implicit QL iteration with the Wilkinson shift of the
+// leading 2 x 2 block (Bowdler, Martin, Reinsch and Wilkinson, "The QR and
+// QL algorithms for symmetric matrices", Numer. Math. 11 (1968) 293-306).
 #include <cmath>
 
 #include "k_eig.cuh"
@@ -23,7 +23,6 @@ namespace {
 
 constexpr int kHouseThreads = 256;
 constexpr int kUpdThreads = 256;
-constexpr int kQlThreads = 32 + kEigQlRows;  // producer warp + consumer warps
 constexpr int kBtThreads = 32 * kEigBtCols;
 
 __device__ __forceinline__ double warp_sum(double x) {
@@ -142,7 +141,7 @@ __global__ void __launch_bounds__(kHouseThreads) eig_house(EigBufs b, const EigJ
 __device__ __forceinline__ int find_job(const EigJob* jobs, int njobs, int bid, int which) {
   int j = 0;
   for (int q = 1; q < njobs; ++q) {
-    const int first = which == 0 ? jobs[q].tile0 : (which == 1 ? jobs[q].ql0 : jobs[q].bt0);
+    const int first = which == 0 ? jobs[q].tile0 : jobs[q].bt0;
     if (first <= bid) j = q;
   }
   return j;
@@ -223,148 +222,6 @@ __global__ void __launch_bounds__(kUpdThreads) eig_update(EigBufs b, const EigJo
   }
 }
 
-// Implicit QL with streamed rotations.  Thread 0 runs the scalar iteration
-// on d, e (shared memory) and writes each sweep's rotations to one of two
-// shared buffers; the consumer warps apply the previous sweep's rotations to
-// their rows of Z meanwhile.  One barrier per sweep.
-__global__ void __launch_bounds__(kQlThreads) eig_ql(EigBufs b, const EigJob* __restrict__ jobs, int njobs) {
-  extern __shared__ double sm[];
-  __shared__ int bm[2], bc[2], done, fail;
-  const int bid = blockIdx.x;
-  const EigJob J = jobs[find_job(jobs, njobs, bid, 1)];
-  const int n = J.n, tid = threadIdx.x;
-  const Scal S = scal(b, J);
-  double* d = sm;
-  double* e = sm + n;
-  double* rb = sm + 2 * n;  // two buffers of 2n (c, s pairs)
-  double* __restrict__ Z = b.work + J.q_off;
-  const int row = (bid - J.ql0) * kEigQlRows + (tid - 32);
-  const bool consumer = tid >= 32 && row < n;
-  for (int i = tid; i < n; i += kQlThreads) {
-    d[i] = S.d[i];
-    e[i] = S.e[i];
-  }
-  if (consumer)
-    for (int c = 0; c < n; ++c) Z[(int64_t)c * n + row] = c == row ? 1.0 : 0.0;
-  if (tid == 0) {
-    done = 0;
-    fail = 0;
-  }
-  __syncthreads();
-  // producer state; an off-diagonal element is negligible below eps times
-  // the largest |d_i| + |e_i| of the matrix (the norm-relative splitting test
-  // of the tql2 algorithm: rank-deficient density matrices have clusters of
-  // zero eigenvalues, where a test relative to the neighbouring diagonal
-  // elements never succeeds)
-  int l = 0, it = 0;
-  const double eps = 2.220446049250313e-16;
-  double tnorm = 0.0;
-  if (tid == 0)
-    for (int i = 0; i < n; ++i) tnorm = fmax(tnorm, fabs(d[i]) + fabs(e[i]));
-  const double tiny = eps * tnorm;
-  for (int batch = 0;; ++batch) {
-    if (tid == 0) {
-      double* buf = rb + (int64_t)(batch & 1) * 2 * n;
-      int m = -1, cnt = 0;
-      if (n > 0) e[n - 1] = 0.0;
-      while (l < n) {
-        m = l;
-        while (m < n - 1) {
-          if (fabs(e[m]) <= tiny) break;
-          ++m;
-        }
-        if (m == l) {
-          ++l;
-          it = 0;
-          continue;
-        }
-        if (++it > 60) {
-          fail = 1;
-          l = n;
-          m = -1;
-          break;
-        }
-        // one QL sweep of the unreduced block l..m
-        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-        double r = hypot(g, 1.0);
-        g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-        double s = 1.0, c = 1.0, p = 0.0;
-        bool early = false;
-        for (int i = m - 1; i >= l; --i) {
-          const double f = s * e[i], bb = c * e[i];
-          r = hypot(f, g);
-          e[i + 1] = r;
-          if (r == 0.0) {
-            d[i + 1] -= p;
-            e[m] = 0.0;
-            early = true;
-            break;
-          }
-          s = f / r;
-          c = g / r;
-          g = d[i + 1] - p;
-          r = (d[i] - g) * s + 2.0 * c * bb;
-          p = s * r;
-          d[i + 1] = g + p;
-          g = c * r - bb;
-          buf[2 * cnt] = c;
-          buf[2 * cnt + 1] = s;
-          ++cnt;
-        }
-        if (!early) {
-          d[l] -= p;
-          e[l] = g;
-          e[m] = 0.0;
-        }
-        if (cnt > 0) break;  // a batch to hand over
-        m = -1;              // rotations none: look again
-      }
-      if (m < 0 || cnt == 0) {
-        done = 1;
-      } else {
-        bm[batch & 1] = m;
-        bc[batch & 1] = cnt;
-      }
-    }
-    __syncthreads();
-    if (done) break;
-    if (consumer) {
-      // the rotations of a sweep act on columns m-1 .. m-cnt in turn; the
-      // columns of eight rotations are loaded before any of them is applied
-      // (they are not written before their own rotation), so that the loads
-      // overlap instead of each waiting on the previous rotation
-      const double* buf = rb + (int64_t)(batch & 1) * 2 * n;
-      const int m = bm[batch & 1], cnt = bc[batch & 1];
-      double zi1 = Z[(int64_t)m * n + row];
-      int x = 0;
-      for (; x + 8 <= cnt; x += 8) {
-        double zz[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) zz[u] = Z[(int64_t)(m - 1 - x - u) * n + row];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int i = m - 1 - x - u;
-          const double c = buf[2 * (x + u)], s = buf[2 * (x + u) + 1];
-          Z[(int64_t)(i + 1) * n + row] = s * zz[u] + c * zi1;
-          zi1 = c * zz[u] - s * zi1;
-        }
-      }
-      for (; x < cnt; ++x) {
-        const int i = m - 1 - x;
-        const double c = buf[2 * x], s = buf[2 * x + 1];
-        const double zi = Z[(int64_t)i * n + row];
-        Z[(int64_t)(i + 1) * n + row] = s * zi + c * zi1;
-        zi1 = c * zi - s * zi1;
-      }
-      Z[(int64_t)(m - cnt) * n + row] = zi1;
-    }
-  }
-  if (bid == J.ql0) {
-    for (int i = tid; i < n; i += kQlThreads) S.eu[i] = d[i];
-    if (tid == 0 && fail) b.status[find_job(jobs, njobs, bid, 1)] = -1;
-  }
-}
-
 // Back-transformation V = H_0 H_1 ... H_{n-3} Z, one eigenvector per warp in
 // shared memory, written at the rank of its eigenvalue (ascending; ties in
 // index order).
@@ -412,23 +269,26 @@ __global__ void __launch_bounds__(kBtThreads) eig_backtransform(EigBufs b, const
 
 }  // namespace
 
-cudaError_t launch_eig(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int tiles, int ql_ctas,
-                       int bt_ctas, cudaStream_t s) {
+cudaError_t launch_eig_tridiag(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int tiles,
+                               cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;
   if (max_n < 1 || max_n > kEigMaxN) return cudaErrorInvalidValue;
-  const size_t smem_ql = (size_t)6 * max_n * sizeof(double);
-  const int bt_cols = eig_bt_cols(max_n);
-  const size_t smem_bt = (size_t)(1 + bt_cols) * max_n * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(eig_ql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ql);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(eig_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bt);
-  if (e != cudaSuccess) return e;
   for (int k = 0; k <= max_n - 2 || k == 0; ++k) {
     eig_house<<<njobs, kHouseThreads, 0, s>>>(b, jobs, k);
     if (k <= max_n - 3 && tiles > 0) eig_update<<<tiles, kUpdThreads, 0, s>>>(b, jobs, njobs, k);
     if (max_n < 2) break;
   }
-  eig_ql<<<ql_ctas, kQlThreads, smem_ql, s>>>(b, jobs, njobs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eig_backtransform(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int bt_ctas,
+                                     cudaStream_t s) {
+  if (njobs <= 0) return cudaSuccess;
+  if (max_n < 1 || max_n > kEigMaxN) return cudaErrorInvalidValue;
+  const int bt_cols = eig_bt_cols(max_n);
+  const size_t smem_bt = (size_t)(1 + bt_cols) * max_n * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(eig_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bt);
+  if (e != cudaSuccess) return e;
   eig_backtransform<<<bt_ctas, kBtThreads, smem_bt, s>>>(b, jobs, njobs, bt_cols);
   return cudaGetLastError();
 }

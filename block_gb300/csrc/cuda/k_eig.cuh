@@ -12,13 +12,12 @@
 //      triangle of the trailing matrix and, in the same pass, forms the
 //      partial products A v_k of the next step (fixed-order reductions, no
 //      atomics: results are bit-reproducible).
-//   2. Implicit QL with Wilkinson shifts on the tridiagonal matrix.  Every
-//      CTA of a sector runs the (identical, sequential) scalar recurrence
-//      itself in one thread and streams each QL sweep's Givens rotations
-//      through shared memory to four warps that apply them to the CTA's own
-//      rows of Z (column-major, so a rotation of two columns is one
-//      coalesced load and store per warp).  The CTAs of a sector never wait
-//      on each other.
+//   2. Divide and conquer on the tridiagonal matrix (k_dc.cuh): leaves of at
+//      most 32 rows by the implicit QL iteration in one warp, merges by the
+//      secular equation with one warp per root and the eigenvector update as
+//      one grouped FP64 GEMM per level for all sectors.  (The QL iteration on
+//      a whole sector is a chain of O(n^2) dependent rotations in one thread,
+//      bound by FP64 latency; the merges are parallel across the GPU.)
 //   3. Back-transformation V = Q Z by the reflectors in reverse order, one
 //      warp per eigenvector held in shared memory, and the eigenpairs
 //      written in ascending eigenvalue order.
@@ -30,9 +29,8 @@ namespace bgpu {
 namespace dev {
 
 constexpr int kEigTile = 64;     // tile edge of the tridiagonalisation update
-constexpr int kEigQlRows = 128;  // rows of Z per QL CTA (four consumer warps)
 constexpr int kEigBtCols = 8;    // eigenvectors per back-transformation CTA
-constexpr int kEigMaxN = 4096;   // largest sector (shared-memory bound of the QL and back-transformation)
+constexpr int kEigMaxN = 4096;   // largest sector (shared-memory bound of the merges and back-transformation)
 
 // One symmetric matrix of the batch.  All offsets are in doubles.
 struct EigJob {
@@ -40,13 +38,11 @@ struct EigJob {
   int64_t z_off;  // output eigenvectors, n x n column-major, ascending eigenvalues
   int64_t w_off;  // output eigenvalues, ascending
   int64_t v_off;  // work: reflectors, n x n (row k = v_k)
-  int64_t q_off;  // work: Z of the QL iteration, n x n column-major
+  int64_t q_off;  // work: Z, eigenvectors of the tridiagonal matrix, n x n column-major
   int64_t s_off;  // work: d, e, tau, unsorted eigenvalues, w (2 n), partial products (2 nt n)
   int32_t n, nt;  // order, tiles per edge
   int32_t tile0;  // first CTA of this job in the update launch
-  int32_t ql0;    // first CTA of this job in the QL launch
   int32_t bt0;    // first CTA of this job in the back-transformation launch
-  int32_t pad;
 };
 // eigenvectors per back-transformation CTA for a batch whose largest order is max_n
 inline int eig_bt_cols(int max_n) { return max_n > 2048 ? kEigBtCols / 2 : kEigBtCols; }
@@ -57,8 +53,11 @@ inline int64_t eig_scalar_elems(int n) {
 }
 
 // Bufs: p[0] = A (inputs, overwritten), p[1] = Z (outputs), p[2] = w
-// (outputs), p[3] = work.  status[j] < 0: the QL iteration of job j did not
-// converge.  Stream-ordered; `jobs` is a device array.
+// (outputs), p[3] = work.  status[j] < 0: the tridiagonal solver of job j
+// did not converge (-1 a leaf's QL iteration, -2 a secular equation).
+// Stream-ordered; `jobs` is a device array.  The host runs
+// launch_eig_tridiag, the divide and conquer of k_dc.cuh on the work area's
+// d, e (unsorted eigenvalues and Z out), then launch_eig_backtransform.
 struct EigBufs {
   double* a;
   double* z;
@@ -66,8 +65,10 @@ struct EigBufs {
   double* work;
   int* status;
 };
-cudaError_t launch_eig(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int tiles, int ql_ctas,
-                       int bt_ctas, cudaStream_t s);
+cudaError_t launch_eig_tridiag(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int tiles,
+                               cudaStream_t s);
+cudaError_t launch_eig_backtransform(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int bt_ctas,
+                                     cudaStream_t s);
 
 }  // namespace dev
 }  // namespace bgpu

@@ -368,7 +368,7 @@ Superblock SweepDriver::prepare_partition(int p, Block& L, Block& R) {
 // (makeRotateMatrix / sort_weights / assign_matrix_by_dm,
 // renormalise.C:135-166, rotationmat.C:149-339); returns discarded weight.
 static double choose_kept(const DensitySpectrum& spec, int M, std::vector<std::vector<int>>& kept_idx,
-                          std::vector<int>& kept) {
+                          std::vector<int>& kept, double* cutoff = nullptr) {
   struct W { double w; int q, i; };
   std::vector<W> all;
   double norm = 0.0;
@@ -388,6 +388,10 @@ static double choose_kept(const DensitySpectrum& spec, int M, std::vector<std::v
     if (all[t].w <= 1e-13) continue;
     kept_idx[all[t].q].push_back(all[t].i);
     keptw += all[t].w;
+  }
+  if (cutoff) {  // the last kept and the first discarded weight
+    cutoff[0] = nk > 0 ? all[nk - 1].w : 0.0;
+    cutoff[1] = nk < (int)all.size() ? all[nk].w : 0.0;
   }
   for (size_t q = 0; q < kept_idx.size(); ++q) {
     // keep the eigenvectors of each sector in descending weight order
@@ -488,7 +492,14 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   E_.density(sb, forward, C_.weights, spec);
   std::vector<std::vector<int>> kept_idx;
   std::vector<int> kept;
-  const double disc = choose_kept(spec, se.M, kept_idx, kept);
+  double cut[2];
+  const double disc = choose_kept(spec, se.M, kept_idx, kept, cut);
+  if (opt_.verbose >= 3) {
+    std::string s;
+    for (size_t q = 0; q < kept.size(); ++q)
+      if (kept[q]) s += " " + std::to_string(q) + ":" + std::to_string(kept[q]);
+    log(3, "    kept%s  (cutoff %.17g | %.17g)\n", s.c_str(), cut[0], cut[1]);
+  }
   E_.select_rotation(kept_idx);
   phase_.density_seconds += secs(t0);
   t0 = clk::now();

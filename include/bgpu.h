@@ -81,17 +81,22 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
  *     restarts from them with their FP64 subspace matrix and residuals;
  *     further basis vectors (corrections) get split-precision products.
  *     Rounds repeat until a restart finds every root's squared FP64
- *     residual norm below the solve's tolerance without expanding (at most
- *     8 rounds; otherwise the energies are FP64 Rayleigh quotients of the
- *     final vectors).  Energies are then FP64 Ritz values and the vectors
- *     meet the FP64 convergence test of an FP64 solve.
+ *     residual norm below the solve's tolerance without expanding, or a
+ *     restart converges with corrections whose split-precision error bound
+ *     keeps (|r| + bound)^2 below the tolerance for every root (at most 8
+ *     rounds; otherwise the energies are FP64 Rayleigh quotients of the
+ *     final vectors).  The bound of one split product of a unit vector is 4
+ *     times the largest difference between the split and FP64 products of
+ *     the first round's Ritz vectors; it is carried through the Ritz
+ *     rotations.  Energies are then FP64 Ritz values and the vectors meet
+ *     the FP64 convergence test of an FP64 solve.
  *   mode 0, energy only: one FP64 Rayleigh quotient per converged root, and
  *     in bgpu_run_dmrg only for the steps bgpu_set_refine_window selects.
  */
 int bgpu_set_refinement(bgpu_ctx* ctx, int mode);
 /* FP64 restarts and FP64 products spent by defect correction in this
  * context, and whether the last solve's roots met the tolerance on FP64
- * residuals (1) or not (0). */
+ * residuals (1), on FP64 residual bounds (2), or not (0). */
 int bgpu_refinement_stats(bgpu_ctx* ctx, int64_t* rounds, int64_t* fp64_products, int* last_verified);
 /* Split-precision sweeps with energy-only refinement (bgpu_set_refinement
  * mode 0; no reference counterpart): bgpu_run_dmrg refines
@@ -142,7 +147,9 @@ int bgpu_set_tc_tile_width(bgpu_ctx* ctx, int nb);
  * of heavy tiles, accumulation group length) on the first product of every
  * superblock whose sector-size histogram was not seen before and keeps the
  * fastest; superblocks with a known histogram reuse the choice.  cache_path
- * (may be NULL) is a text file the choices are read from and appended to. */
+ * (may be NULL: the choices made so far are kept) is a text file the
+ * choices are read from and appended to; it replaces the choices held so
+ * far. */
 int bgpu_set_autotune(bgpu_ctx* ctx, int on, const char* cache_path);
 /* Histograms tuned by this context, histograms in the cache, seconds spent tuning. */
 int bgpu_autotune_stats(bgpu_ctx* ctx, int64_t* keys_tuned, int64_t* keys_cached, double* seconds);
@@ -441,7 +448,9 @@ int bgpu_transition_onepdm(bgpu_ctx* ctx, int bra, int ket, double* gamma, int n
  * seconds, defect-correction rounds, the FP64 product time the same
  * solves would have taken (every product of a block step at that step's
  * measured FP64 product time, summed over the steps with an FP64 product),
- * the warm-up's wall seconds, then the wall seconds of each sweep. */
+ * the warm-up's wall seconds, the solves accepted on the error bound of
+ * their corrections (no FP64 product after the last restart; see
+ * bgpu_refinement_stats), then the wall seconds of each sweep. */
 int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n);
 /* Sweep energies (lowest root per sweep, Sweep::do_one's return value,
  * sweep.C:436-453) of the last bgpu_run_dmrg: *n = number of sweeps, up to
