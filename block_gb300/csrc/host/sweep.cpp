@@ -500,6 +500,16 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
       if (kept[q]) s += " " + std::to_string(q) + ":" + std::to_string(kept[q]);
     log(3, "    kept%s  (cutoff %.17g | %.17g)\n", s.c_str(), cut[0], cut[1]);
   }
+  if (opt_.verbose >= 4)  // the whole spectrum, sector by sector
+    for (size_t q = 0; q < spec.eig.size(); ++q) {
+      std::string s;
+      char buf[32];
+      for (double x : spec.eig[q]) {
+        std::snprintf(buf, sizeof(buf), " %.10e", x);
+        s += buf;
+      }
+      log(4, "    rho[%zu]%s\n", q, s.c_str());
+    }
   E_.select_rotation(kept_idx);
   phase_.density_seconds += secs(t0);
   t0 = clk::now();
@@ -614,6 +624,12 @@ double SweepDriver::sweep(bool forward, int sweep_index) {
 // gamma of one root is symmetric (real wavefunctions); between roots a and b
 // the sweep takes the transition elements <a|E_ij|b> (tran_onepdm,
 // modules/onepdm/onepdm.C with the transition flag) from the same terms.
+// Each step's solve fixes every root only up to its sign, so the relative
+// sign of two roots may flip from one step to the next: every step also
+// takes the cross elements (p-1, j > p), which the neighbouring step takes
+// too, and flips root r when its largest shared element <r|E_ij|0>
+// changes sign (the phase the reference carries along its sweep through the
+// transformed guesses).
 void SweepDriver::rdm_extras(int p, CatalogSpec& specL, CatalogSpec& specR) const {
   auto add = [](CatalogSpec& s, const OpKey& k) {
     if (std::find(s.extra.begin(), s.extra.end(), k) == s.extra.end()) s.extra.push_back(k);
@@ -658,6 +674,10 @@ void SweepDriver::rdm_step(int p, const Superblock& sb) {
     at.push_back({a, b});
   };
   for (int j = p + 1; j < N_; ++j) cross(p, j);
+  const size_t nfirst = terms.size();
+  if (p >= 1)  // the shared elements of the neighbouring step p - 1
+    for (int j = p + 1; j < N_; ++j) cross(p - 1, j);
+  const size_t nlink = terms.size();
   if (p == 1) {
     for (int j = 2; j < N_; ++j) cross(0, j);
     inside(true, 0, 0);
@@ -676,19 +696,45 @@ void SweepDriver::rdm_step(int p, const Superblock& sb) {
   const size_t nt = terms.size();
   const int nr = (int)std::lround(std::sqrt((double)(v.size() / std::max<size_t>(nt, 1))));
   if ((int)rdm_.size() < nr * nr) rdm_.resize((size_t)nr * nr, std::vector<double>((size_t)N_ * N_, 0.0));
+  auto val = [&](int a, int b, size_t t) { return v[((size_t)a * nr + b) * nt + t]; };
+  // phase of every root relative to root 0, from the elements shared with
+  // the previous step
+  std::vector<double> sgn(nr, 1.0);
+  for (int r = 1; r < nr; ++r) {
+    double best = 0.0, cur = 0.0;
+    for (size_t t = 0; t < nlink; ++t) {
+      auto it = rdm_link_.find(at[t]);
+      if (it == rdm_link_.end()) continue;
+      const double prev = it->second[r];
+      if (std::fabs(prev) > std::fabs(best)) {
+        best = prev;
+        cur = val(r, 0, t);
+      }
+    }
+    if (std::fabs(best) > 1e-8 && (cur < 0.0) != (best < 0.0)) sgn[r] = -1.0;
+  }
+  rdm_link_.clear();
+  for (size_t t = 0; t < nlink; ++t) {
+    std::vector<double> col(nr);
+    for (int r = 0; r < nr; ++r) col[r] = sgn[r] * val(r, 0, t);
+    rdm_link_[at[t]] = col;
+  }
   // <a|E_ij|b> from the term (i, j); <a|E_ji|b> = <b|E_ij|a> (real vectors)
   for (int a = 0; a < nr; ++a)
     for (int b = 0; b < nr; ++b)
       for (size_t t = 0; t < nt; ++t) {
+        if (t >= nfirst && t < nlink) continue;  // taken by the neighbouring step
         const int i = at[t].first, j = at[t].second;
-        rdm_[(size_t)a * nr + b][(size_t)i * N_ + j] = v[((size_t)a * nr + b) * nt + t];
-        rdm_[(size_t)a * nr + b][(size_t)j * N_ + i] = v[((size_t)b * nr + a) * nt + t];
+        const double s = sgn[a] * sgn[b];
+        rdm_[(size_t)a * nr + b][(size_t)i * N_ + j] = s * val(a, b, t);
+        rdm_[(size_t)a * nr + b][(size_t)j * N_ + i] = s * val(b, a, t);
       }
 }
 
 std::vector<std::vector<double>> SweepDriver::onepdm_sweep(bool forward, int sweep_index) {
   if (N_ < 4) throw std::runtime_error("onepdm needs at least 4 orbitals");
   rdm_.clear();
+  rdm_link_.clear();
   rdm_pass_ = true;
   try {
     sweep(forward, sweep_index);

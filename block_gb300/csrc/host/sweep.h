@@ -10,6 +10,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "checkpoint.h"
@@ -321,6 +322,9 @@ class SweepDriver {
   // density-matrix sweep: the operators each step needs and the elements
   bool rdm_pass_ = false;
   std::vector<std::vector<double>> rdm_;
+  // the previous step's cross elements (i, j) -> <r|E_ij|0> per root r, after
+  // its phase fix: consecutive steps share the elements (min p, j >= min p + 2)
+  std::map<std::pair<int, int>, std::vector<double>> rdm_link_;
   void rdm_extras(int p, CatalogSpec& specL, CatalogSpec& specR) const;
   void rdm_step(int p, const Superblock& sb);
   std::vector<double> sweep_refined_best_;

@@ -12,7 +12,9 @@ gamma), a run whose orbitals the sweep reorders, with gamma reported in
 the input orbital order (save_onepdm_spatial_text, onepdm.C:504-528), and
 the two state-averaged roots of the 8-site Hubbard case with its final
 Davidson tolerance tightened to 1e-12 (one gamma per root, 2e-6: the
-second root's solve ends with a larger residual, observed 7e-7).
+second root's solve ends with a larger residual, observed 7e-7), and their
+transition matrices <1|E_pq|0> and <0|E_pq|1> up to one overall sign
+(elements from different sweep steps share the roots' relative phase).
 
 The reference's own tables pin the same sweep: its 8-site Hubbard roots 0
 and 1 and its C2v water roots 0, 1 and their transition matrix <1|E_kl|0>
@@ -30,16 +32,22 @@ from conftest import GOLDEN
 from test_oracle_fci import fci_operators, write_fcidump
 
 
-def fci_onepdm(t, v, ecore, nelec, energy, nroots=40):
+def fci_onepdm(t, v, ecore, nelec, energy, nroots=40, ket_energy=None):
+    """<bra|E_pq|ket> of the FCI eigenvectors at the given energies (ket =
+    bra without ket_energy)."""
     H, E = fci_operators(t, v, ecore, nelec)
     w, X = sla.eigsh(H, k=nroots, which="SA", tol=1e-13)
-    k = int(np.argmin(np.abs(w - energy)))
-    others = np.delete(w, k)
-    assert abs(w[k] - energy) <= 1e-8, (w[k], energy)
-    assert np.min(np.abs(others - w[k])) > 1e-6  # a non-degenerate state
-    x = X[:, k]
+
+    def state(en):
+        k = int(np.argmin(np.abs(w - en)))
+        assert abs(w[k] - en) <= 1e-8, (w[k], en)
+        assert np.min(np.abs(np.delete(w, k) - w[k])) > 1e-6  # a non-degenerate state
+        return X[:, k]
+
+    x = state(energy)
+    y = x if ket_energy is None else state(ket_energy)
     n = t.shape[0]
-    return np.array([[x @ (E[p, q] @ x) for q in range(n)] for p in range(n)])
+    return np.array([[x @ (E[p, q] @ y) for q in range(n)] for p in range(n)])
 
 
 def read_spatial_onepdm(path):
@@ -90,6 +98,14 @@ def test_onepdm_matches_fci(oracle, tmp_path, name, spin, reorder, tol):
         # the text file holds the same matrix
         gt = read_spatial_onepdm(tmp_path / ("spatial_onepdm.%d.%d.txt" % (r, r)))
         assert np.max(np.abs(gt - g)) <= 1e-13 * np.max(np.abs(g))
+    if len(e) > 1:
+        # transition matrices: one relative sign of the two roots for all
+        # elements, however many sweep steps they come from
+        gf = fci_onepdm(t, v, ecore, 8, e[1], ket_energy=e[0])
+        for a, b, ref in ((1, 0, gf), (0, 1, gf.T)):
+            g = oracle.transition_onepdm(a, b, 8)
+            d = min(np.max(np.abs(g - ref)), np.max(np.abs(g + ref)))
+            assert d <= tol, (a, b, d)
 
 
 def test_onepdm_needs_the_keyword(oracle):
