@@ -81,6 +81,7 @@ def parse():
                     help="dmrg.conf of the large split-precision sweep ('none' to skip)")
     ap.add_argument("--sweep-fp64", action="store_true",
                     help="also run the large sweep in FP64 (close to an hour at M=2000) for a measured ratio and dE")
+    ap.add_argument("--no-exact", action="store_true", help="skip the exact-slice tensor-core product")
     ap.add_argument("--profile", action="store_true",
                     help="open the CUDA profiler range around the device-timed steps only")
     return ap.parse_args()
@@ -407,6 +408,7 @@ def run_ours(a):
             sched["tuning"] = {"histograms_tuned": tuned, "seconds": secs}
         line["schedules"] = sched
     ms64 = None
+    ref64 = None
     if split:
         # plain FP64 path on the same superblock and input: one device-timed
         # product, whose result is also the reference for the split error
@@ -449,6 +451,19 @@ def run_ours(a):
                 dv["fp64_derived_seconds"] = prods * ms64 * 1e-3
                 dv["speedup_vs_derived_fp64"] = dv["fp64_derived_seconds"] / dv[a.precision]["seconds"]
         line["davidson"] = dv
+    if split and ref64 is not None and not a.no_exact:
+        # the exact-slice tensor-core product (FP64-level, the restart
+        # products of defect correction) on the same superblock and input
+        ctx.set_precision("exacttc")
+        yx = ctx.device_alloc(n)
+        msx = ctx.sigma_timed(sb, x, yx, 2)[0] / 2
+        px = ctx.to_host(yx, n)
+        ctx.device_free(yx)
+        ctx.set_precision(a.precision)
+        line["exact_path"] = {"ms_per_step": msx, "tflops": flops / (msx * 1e-3) / 1e12,
+                              "speedup_vs_fp64": ms64 / msx,
+                              "sigma_rel_err_vs_fp64": float(np.linalg.norm(px - ref64) / np.linalg.norm(ref64)),
+                              "products_per_logical_product": 21}
     if rank == 0 and not a.no_cpu_baseline:
         threads = os.cpu_count() or 1
         r = cpu_sample(a.conf, a.partition, a.cpu_reps)

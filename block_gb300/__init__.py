@@ -16,7 +16,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libblockgb300.so")
 
 OP = dict(HAM=0, CRE=1, CRE_DES=2, CRE_CRE=3, CRE_DESCOMP=4, DES_DESCOMP=5, CRE_CRE_DESCOMP=6, OVERLAP=7)
-PREC = dict(fp64=0, bf16x3=1, bf16x6=2, bf16x3tc=3, fp16x2tc=4)
+PREC = dict(fp64=0, bf16x3=1, bf16x6=2, bf16x3tc=3, fp16x2tc=4, exacttc=5)
 # BGPU_NOALLOC_SCRATCH_DOUBLES: doubles of the fixed array behind bgpu_sigma_noalloc
 NOALLOC_SCRATCH_DOUBLES = 4 * 1024 * 1024
 
@@ -434,9 +434,10 @@ class Context:
         return v.value
 
     def set_refinement(self, mode):
-        """Split-precision solves: "defect" (FP64-residual defect correction,
-        default) or "energy" (FP64 Rayleigh quotients only)."""
-        self._check(self.lib.bgpu_set_refinement(self.h, {"energy": 0, "defect": 1}[mode]))
+        """Split-precision solves: "defect" (FP64-residual defect correction
+        with FP64 products), "exact" (the same with the exact-slice
+        tensor-core products) or "energy" (FP64 Rayleigh quotients only)."""
+        self._check(self.lib.bgpu_set_refinement(self.h, {"energy": 0, "defect": 1, "exact": 2}[mode]))
 
     def refinement_stats(self):
         """(FP64 restarts, FP64 products, how the last solve was verified:
@@ -503,10 +504,10 @@ class Context:
         self._check(self.lib.bgpu_sweep_energies(self.h, _dp(sw), len(sw), ctypes.byref(ns)))
         stats["sweep_energies"] = sw[:min(ns.value, len(sw))].copy()
         nsw = len(stats["sweep_energies"])
-        rs = np.zeros(8 + nsw)
+        rs = np.zeros(10 + nsw)
         self._check(self.lib.bgpu_run_stats(self.h, _dp(rs), len(rs)))
         stats.update(split_sigma_calls=int(rs[0]), split_sigma_seconds=rs[1], fp64_sigma_calls=int(rs[2]),
                      fp64_sigma_seconds=rs[3], defect_rounds=int(rs[4]), derived_fp64_sigma_seconds=rs[5],
-                     warmup_seconds=rs[6], bounded_verifications=int(rs[7]),
-                     sweep_seconds=rs[8:8 + nsw].copy())
+                     warmup_seconds=rs[6], bounded_verifications=int(rs[7]), exact_sigma_calls=int(rs[8]),
+                     exact_sigma_seconds=rs[9], sweep_seconds=rs[10:10 + nsw].copy())
         return e[:nroots].copy(), stats

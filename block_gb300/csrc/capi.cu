@@ -235,7 +235,9 @@ int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n) {
 int bgpu_set_refinement(bgpu_ctx* ctx, int mode) {
   return guarded(ctx, [&] {
     need(ctx->eng != nullptr, "no device");
-    need(mode == 0 || mode == 1, "refinement mode must be 0 (energy only) or 1 (defect correction)");
+    need(mode == 0 || mode == 1 || mode == 2,
+         "refinement mode must be 0 (energy only), 1 (defect correction) or 2 (defect correction, exact-slice "
+         "tensor-core products)");
     ctx->eng->refine_mode = mode;
   });
 }
@@ -253,7 +255,7 @@ int bgpu_refinement_stats(bgpu_ctx* ctx, int64_t* rounds, int64_t* fp64_products
 int bgpu_set_precision(bgpu_ctx* ctx, int p) {
   return guarded(ctx, [&] {
     need(p == BGPU_PREC_FP64 || p == BGPU_PREC_BF16X3 || p == BGPU_PREC_BF16X6 || p == BGPU_PREC_BF16X3_TC ||
-             p == BGPU_PREC_FP16X2_TC,
+             p == BGPU_PREC_FP16X2_TC || p == BGPU_PREC_EXACT_TC,
          "unknown precision");
     need(ctx->eng != nullptr, "no device");
     ctx->eng->precision = (Precision)p;
@@ -942,7 +944,9 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     const double d0 = ctx->eng->renorm_device_seconds;
     const long c0 = ctx->eng->sigma_calls;
     GpuEngine& E = *ctx->eng;
-    const long sc0 = E.split_calls, fc0 = E.fp64_calls, dr0 = E.defect_rounds_, db0 = E.defect_bounded_;
+    const long sc0 = E.split_calls, fc0 = E.fp64_calls, dr0 = E.defect_rounds_, db0 = E.defect_bounded_,
+               xc0 = E.exact_calls;
+    const double xs0 = E.exact_seconds;
     const double ss0 = E.split_seconds, fs0 = E.fp64_seconds, dv0 = E.derived_fp64_sigma_seconds;
     SweepResult r;
     {
@@ -955,7 +959,8 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     ctx->tonepdm = r.transition_onepdm;
     ctx->run_stats = {(double)(E.split_calls - sc0), E.split_seconds - ss0, (double)(E.fp64_calls - fc0),
                       E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
-                      r.warmup_seconds, (double)(E.defect_bounded_ - db0)};
+                      r.warmup_seconds, (double)(E.defect_bounded_ - db0), (double)(E.exact_calls - xc0),
+                      E.exact_seconds - xs0};
     for (double t : r.sweep_seconds) ctx->run_stats.push_back(t);
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {

@@ -847,6 +847,17 @@ void GpuEngine::free_tc(SigmaPlan& p) {
   p.tc_partials = nullptr;
   p.tc_partial_cap = 0;
   p.tc_host.reset();
+  for (int i = 0; i < dev::kTcPools; ++i) {
+    if (p.tcx_ex[i]) cudaFreeAsync(p.tcx_ex[i], stream_);
+    p.tcx_ex[i] = nullptr;
+    p.tcx_ex_n[i] = 0;
+  }
+  if (p.tcx_t) cudaFreeAsync(p.tcx_t, stream_);
+  p.tcx_t = nullptr;
+  p.tcx_t_n = 0;
+  p.tcx_tpack.release(stream_);
+  p.tcx_w1.release(stream_);
+  p.tcx_w2.release(stream_);
   p.tc_l1.clear();
   p.tc_l2.clear();
   p.tc_tuned = false;
@@ -1099,7 +1110,13 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   const Block& R = *sb.R;
   if (!plan.tc_nb_set) plan.tc_nb = tc_choose_nb(sb);
   if (plan.tc_nb != kTcRowsB && plan.tc_nb != kTcRowsBWide) plan.tc_nb = kTcRowsB;
+  if (plan.tcx) plan.tc_nb = kTcxNB;
   const int nb = plan.tc_nb;
+  // slices per packed element: bf16 hi and lo, or six exact digits
+  const int64_t nsl = plan.tcx ? kTcxSlices : 2;
+  int64_t ex_n[kTcPools] = {0, 0, 0, 0, 0};  // rows of each pool (row exponents)
+  std::vector<TcPack> t_packs;                // exact: T -> pool S, per stage-1 product
+  int64_t t_n = 0;
   const auto by_l = sectors_by_left(sb);
   const int nsec = (int)sb.sectors.size();
   std::vector<std::vector<Coupling>> per_t(sb.terms.size());
@@ -1131,12 +1148,15 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     p.src = (uint8_t)pool;  // 0: L arena, 1: R arena
     p.pool = (uint8_t)pool;
     p.dst_off = pool_n[pool];
-    pool_n[pool] += 2 * (int64_t)p.rows_p * p.kp;  // hi and lo
+    pool_n[pool] += nsl * (int64_t)p.rows_p * p.kp;  // all slices
+    p.ex_off = (int32_t)ex_n[pool];
+    ex_n[pool] += p.rows_p;
     m.emplace(key, (int)ops_packs.size());
     ops_packs.push_back(p);
     return p;
   };
   std::vector<int64_t> psi_off(nsec), psit_off(nsec);
+  std::vector<int32_t> psi_ex(nsec), psit_ex(nsec);
   for (int s = 0; s < nsec; ++s) {
     const auto& S = sb.sectors[s];
     TcPack a{};
@@ -1150,7 +1170,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     a.kp = tc_round16(S.cols);
     a.rt = kTcRowsA;
     a.dst_off = psi_off[s] = pool_n[kTcPoolPsi];
-    pool_n[kTcPoolPsi] += 2 * (int64_t)a.rows_p * a.kp;
+    pool_n[kTcPoolPsi] += nsl * (int64_t)a.rows_p * a.kp;
+    a.ex_off = psi_ex[s] = (int32_t)ex_n[kTcPoolPsi];
+    ex_n[kTcPoolPsi] += a.rows_p;
     psi_packs.push_back(a);
     TcPack t = a;
     t.pool = kTcPoolPsiT;
@@ -1161,7 +1183,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     t.kp = tc_round16(S.rows);
     t.rt = nb;
     t.dst_off = psit_off[s] = pool_n[kTcPoolPsiT];
-    pool_n[kTcPoolPsiT] += 2 * (int64_t)t.rows_p * t.kp;
+    pool_n[kTcPoolPsiT] += nsl * (int64_t)t.rows_p * t.kp;
+    t.ex_off = psit_ex[s] = (int32_t)ex_n[kTcPoolPsiT];
+    ex_n[kTcPoolPsiT] += t.rows_p;
     psi_packs.push_back(t);
   }
   std::vector<TcItem> i1;
@@ -1174,6 +1198,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   for (auto& cl : per_t) {
     int cur_l = -1, cur_lp = -1, cur_rp = -1, cur_kp = 0, cur_item = -1;
     int64_t cur_s = -1;
+    int32_t cur_ex = 0;
     for (const Coupling& c : cl) {
       if (c.va.identity && c.vb.identity) throw std::runtime_error("identity x identity pair term");
       const auto& SV = sb.sectors[c.vs];
@@ -1187,6 +1212,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         it.b_off = pb.dst_off;
         it.kp = tc_round16(R.si.states[c.rQp]);
         it.alpha = (float)(c.f * c.vb.scale);
+        it.alpha64 = c.f * c.vb.scale;
+        it.a_ex = psi_ex[c.cs];
+        it.b_ex = pb.ex_off;
         const auto& C = sb.sectors[c.cs];
         if (tc_round8(C.rows) != out_rows_p || tc_round16(C.cols) != it.kp || pb.rows_p != out_cols_p ||
             pb.kp != it.kp)
@@ -1203,6 +1231,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         it.b_off = psit_off[c.cs];
         it.kp = tc_round16(L.si.states[c.lQp]);
         it.alpha = (float)(c.f * c.va.scale);
+        it.alpha64 = c.f * c.va.scale;
+        it.a_ex = pa.ex_off;
+        it.b_ex = psit_ex[c.cs];
         const auto& C = sb.sectors[c.cs];
         if (pa.rows_p != out_rows_p || pa.kp != it.kp || tc_round8(C.cols) != out_cols_p ||
             tc_round16(C.rows) != it.kp)
@@ -1215,7 +1246,25 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         const int mr = L.si.states[c.lQ], mc = R.si.states[c.rQp], k1 = L.si.states[c.lQp];
         const int rows_p = tc_round8(mr), skp = tc_round16(mc);
         cur_s = pool_n[kTcPoolS];
-        pool_n[kTcPoolS] += 2 * (int64_t)rows_p * skp;
+        pool_n[kTcPoolS] += nsl * (int64_t)rows_p * skp;
+        cur_ex = (int32_t)ex_n[kTcPoolS];
+        ex_n[kTcPoolS] += rows_p;
+        if (plan.tcx) {  // the FP64 product T, packed into pool S after phase 1
+          TcPack tp{};
+          tp.src = 3;
+          tp.src_off = t_n;
+          tp.ld = skp;
+          tp.rows_v = mr;
+          tp.cols_v = mc;
+          tp.rows_p = rows_p;
+          tp.kp = skp;
+          tp.rt = kTcRowsA;
+          tp.pool = kTcPoolS;
+          tp.dst_off = cur_s;
+          tp.ex_off = cur_ex;
+          t_packs.push_back(tp);
+          t_n += (int64_t)rows_p * skp;
+        }
         const TcPack pa = pack_view(0, c.va, lmap);
         TcItem a{};
         a.a_pool = kTcPoolL;
@@ -1224,6 +1273,10 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
         a.b_off = psit_off[c.cs];
         a.kp = tc_round16(k1);
         a.alpha = (float)c.va.scale;
+        a.alpha64 = c.va.scale;
+        a.a_ex = pa.ex_off;
+        a.b_ex = psit_ex[c.cs];
+        a.o_ex = cur_ex;
         const auto& C = sb.sectors[c.cs];
         if (pa.rows_p != rows_p || pa.kp != a.kp || tc_round8(C.cols) != tc_round8(mc) ||
             tc_round16(C.rows) != a.kp)
@@ -1260,6 +1313,9 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       it.b_off = pb.dst_off;
       it.kp = cur_kp;
       it.alpha = (float)(c.f * c.vb.scale);
+      it.alpha64 = c.f * c.vb.scale;
+      it.a_ex = cur_ex;
+      it.b_ex = pb.ex_off;
       if (pb.rows_p != out_cols_p || pb.kp != it.kp) fail();
       per_sector[c.vs].push_back(it);
       per_sector_s[c.vs].push_back(cur_item);
@@ -1281,6 +1337,8 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
           TcItem& u = i1[us[k]];
           u.alpha = (float)((double)u.alpha * (double)v[k].alpha);
           v[k].alpha = 1.0f;
+          u.alpha64 *= v[k].alpha64;
+          v[k].alpha64 = 1.0;
         }
     }
     // items with alpha = 1 first, so that they form long accumulation runs
@@ -1322,15 +1380,37 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
   // operator blocks are packed once per plan
   DevArray<TcPack> dops;
   dops.upload(ops_packs, stream_);
-  TcBufs b{};
-  b.src[0] = arena(L);
-  b.src[1] = arena(R);
-  for (int i = 0; i < kTcPools; ++i) {
-    b.pool[i] = plan.tc_pool[i];
+  if (plan.tcx) {
+    for (int i = 0; i < kTcPools; ++i) {
+      plan.tcx_ex_n[i] = ex_n[i];
+      cuda_check(cudaMallocAsync((void**)&plan.tcx_ex[i], (size_t)std::max<int64_t>(ex_n[i], 1) * sizeof(int), stream_),
+                 "tcx row exponents");
+    }
+    plan.tcx_t_n = t_n;
+    cuda_check(cudaMallocAsync((void**)&plan.tcx_t, (size_t)std::max<int64_t>(t_n, 1) * sizeof(double), stream_),
+               "tcx stage-1 products");
+    plan.tcx_tpack.upload(t_packs, stream_);
+    TcxBufs xb{};
+    xb.src[0] = arena(L);
+    xb.src[1] = arena(R);
+    for (int i = 0; i < kTcPools; ++i) {
+      xb.pool[i] = plan.tc_pool[i];
+      xb.ex[i] = plan.tcx_ex[i];
+    }
+    cuda_check(launch_tcx_rowexp(xb, dops.d, (int)ops_packs.size(), stream_), "tcx operator exponents");
+    cuda_check(launch_tcx_pack(xb, dops.d, (int)ops_packs.size(), stream_), "tcx pack operators");
+    plan.tc_fp16 = false;
+  } else {
+    TcBufs b{};
+    b.src[0] = arena(L);
+    b.src[1] = arena(R);
+    for (int i = 0; i < kTcPools; ++i) {
+      b.pool[i] = plan.tc_pool[i];
+    }
+    b.fp16 = precision == Precision::FP16X2_TC ? 1 : 0;
+    plan.tc_fp16 = b.fp16 != 0;
+    cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
   }
-  b.fp16 = precision == Precision::FP16X2_TC ? 1 : 0;
-  plan.tc_fp16 = b.fp16 != 0;
-  cuda_check(launch_tc_pack(b, dops.d, (int)ops_packs.size(), stream_), "tc pack operators");
   dops.release(stream_);
   laps.lap("pools + pack operators");
   TcKnobs kn = tc_default_knobs();
@@ -1469,9 +1549,11 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   std::vector<int> o1, o2;
   std::vector<int2> r1, r2, l1, l2;
   if (!seq) {
-    // persistent blocks: two per SM with 64-column tiles, one with 128
-    schedule_lpt(c1, H.bundle1, tc_blocks_per_sm(nb) * nsm, o1, r1);
-    schedule_lpt(c2, bundle2, tc_blocks_per_sm(nb) * nsm, o2, r2);
+    // persistent blocks: two per SM with 64-column tiles, one with 128 (and
+    // one for the exact kernels)
+    const int bps = plan.tcx ? tcx_blocks_per_sm() : tc_blocks_per_sm(nb);
+    schedule_lpt(c1, H.bundle1, bps * nsm, o1, r1);
+    schedule_lpt(c2, bundle2, bps * nsm, o2, r2);
   } else {
     // one block per task, tasks grouped by sector, one launch per group
     auto by_sector = [](const std::vector<int>& sec, std::vector<int>& o, std::vector<int2>& r,
@@ -1571,10 +1653,85 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
       }
     });
   };
+  // exact records: every item its own read-out (no accumulation groups:
+  // each item has its own row and column scales), FP64 alpha, pool
+  // offsets of six-slice blocks, row-exponent offsets; phase-1 outputs go to
+  // the FP64 T buffer (element offset = pool-S offset / kTcxSlices)
+  auto flatten_x = [&](int phase, const std::vector<TcTask>& tasks, const std::vector<TcItem>& items,
+                       const std::vector<int>& order, const std::vector<int2>& ranges, std::vector<TcxWork>& w,
+                       std::vector<int2>& wr) {
+    wr.assign(ranges.size(), make_int2(0, 0));
+    int64_t nrec = 0;
+    for (size_t j = 0; j < ranges.size(); ++j) {
+      wr[j].x = (int)nrec;
+      for (int k = ranges[j].x; k < ranges[j].y; ++k) {
+        const TcTask& T = tasks[order[k]];
+        nrec += std::max(1, T.iend - T.ibeg);
+      }
+      wr[j].y = (int)nrec;
+    }
+    if (nrec > INT32_MAX) throw std::runtime_error("tensor-core plan: too many work records");
+    w.assign(nrec, TcxWork{});
+    parallel_for((int)ranges.size(), [&](int j) {
+      const int2& rg = ranges[j];
+      int64_t pos = wr[j].x;
+      for (int k = rg.x; k < rg.y; ++k) {
+        const TcTask& T = tasks[order[k]];
+        TcxWork base{};
+        base.h_a = (int16_t)std::min(kTcRowsA, T.a_rows - kTcRowsA * T.tm);
+        base.h_b = (int16_t)std::min(nb, T.b_rows - nb * T.tn);
+        base.valid_rows = (int16_t)T.valid_rows;
+        base.valid_cols = (int16_t)T.valid_cols;
+        if (phase == 1) {
+          base.out_base = T.out_off / kTcxSlices + (int64_t)kTcRowsA * T.tm * T.out_kp;
+          base.out_ld = T.out_kp;
+          base.col0 = nb * T.tn;
+        } else if (T.direct) {
+          base.out_base = T.out_off + (int64_t)kTcRowsA * T.tm * T.out_kp + nb * T.tn;
+          base.out_ld = T.out_kp;
+        } else {
+          base.out_base = T.out_off;
+          base.out_ld = base.h_b;
+        }
+        const uint8_t f0 = (uint8_t)(T.direct ? kTcDirect : 0);
+        if (T.ibeg == T.iend) {
+          TcxWork x = base;
+          x.flags = (uint8_t)(f0 | kTcFirst | kTcLast | kTcEmpty);
+          w[pos++] = x;
+          continue;
+        }
+        for (int i = T.ibeg; i < T.iend; ++i) {
+          const TcItem& it = items[i];
+          TcxWork x = base;
+          x.a_base = it.a_off + (int64_t)kTcxSlices * kTcRowsA * T.tm * it.kp;
+          x.b_base = it.b_off + (int64_t)kTcxSlices * nb * T.tn * it.kp;
+          x.a_ex = it.a_ex + kTcRowsA * T.tm;
+          x.b_ex = it.b_ex + nb * T.tn;
+          x.o_ex = it.o_ex + kTcRowsA * T.tm;
+          x.kp = it.kp;
+          x.alpha = it.alpha64;
+          x.a_pool = it.a_pool;
+          x.b_pool = it.b_pool;
+          x.flags = (uint8_t)(f0 | (i == T.ibeg ? kTcFirst : 0) | (i + 1 == T.iend ? kTcLast : 0) | kTcGStart | kTcGEnd);
+          w[pos++] = x;
+        }
+      }
+    });
+  };
   std::vector<TcWork> w1, w2;
   std::vector<int2> wr1, wr2;
-  flatten(1, t1, i1, o1, r1, w1, wr1);
-  flatten(2, t2, i2, o2, r2, w2, wr2);
+  if (plan.tcx) {
+    std::vector<TcxWork> x1, x2;
+    flatten_x(1, t1, i1, o1, r1, x1, wr1);
+    flatten_x(2, t2, i2, o2, r2, x2, wr2);
+    plan.tcx_w1.release(stream_);
+    plan.tcx_w2.release(stream_);
+    plan.tcx_w1.upload(x1, stream_);
+    plan.tcx_w2.upload(x2, stream_);
+  } else {
+    flatten(1, t1, i1, o1, r1, w1, wr1);
+    flatten(2, t2, i2, o2, r2, w2, wr2);
+  }
   for (auto* d : {&plan.tc_w1, &plan.tc_w2}) d->release(stream_);
   for (auto* d : {&plan.tc_r1, &plan.tc_r2}) d->release(stream_);
   plan.tc_tiles.release(stream_);
@@ -1732,6 +1889,11 @@ void GpuEngine::load_tune_cache(const std::string& path) {
 }
 
 void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, double* out, cudaEvent_t* marks) {
+  if (p.tc && p.tcx) {  // packed for the exact kernels
+    free_tc(p);
+    p.tc_nb_set = false;
+  }
+  p.tcx = false;
   const bool fp16 = precision == Precision::FP16X2_TC;
   if (p.tc && p.tc_fp16 != fp16) free_tc(p);  // operators packed in the other format
   if (p.tc && tc_nb_mode && tc_nb_mode != p.tc_nb) {  // packed for the other tile width
@@ -1782,7 +1944,49 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   ++sigma_calls;
 }
 
+// Exact-slice product (plan p.tcx): psi's row exponents and digits, phase 1
+// (T in FP64, its row exponents reduced by the kernel), T's digits into pool
+// S, phase 2, FP64 sum of split tiles.
+void GpuEngine::sigma_tcx(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
+  if (!p.tcx) throw std::logic_error("sigma_tcx: not an exact-slice plan");
+  if (!p.tc) plan_tc(sb, p);
+  dev::TcxBufs b{};
+  b.src[0] = arena(*sb.L);
+  b.src[1] = arena(*sb.R);
+  b.src[2] = psi;
+  b.src[3] = p.tcx_t;
+  for (int i = 0; i < dev::kTcPools; ++i) {
+    b.pool[i] = p.tc_pool[i];
+    b.ex[i] = p.tcx_ex[i];
+  }
+  b.t = p.tcx_t;
+  b.partials = reinterpret_cast<double*>(p.tc_partials);
+  b.status = tc_status_;
+  constexpr uint64_t kWaitLimitNs = 1000000000ull;
+  cuda_check(dev::launch_tcx_rowexp(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tcx psi exponents");
+  cuda_check(dev::launch_tcx_pack(b, p.tc_psi_pack.d, (int)p.tc_psi_pack.n, stream_), "tcx pack psi");
+  cuda_check(dev::launch_fill_int(p.tcx_ex[dev::kTcPoolS], p.tcx_ex_n[dev::kTcPoolS], dev::kTcxNoExp, stream_),
+             "tcx T exponents");
+  cuda_check(dev::launch_tcx_sigma(1, b, p.tcx_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
+             "tcx phase 1");
+  cuda_check(dev::launch_tcx_pack(b, p.tcx_tpack.d, (int)p.tcx_tpack.n, stream_), "tcx pack T");
+  cuda_check(dev::launch_tcx_sigma(2, b, p.tcx_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
+             "tcx phase 2");
+  cuda_check(dev::launch_tcx_reduce(b, p.tc_tiles.d, p.tc_slots.d, (int)p.tc_tiles.n, out, stream_), "tcx reduce");
+  if (p.ecore != 0.0) cuda_check(dev::launch_axpy(p.ecore, psi, out, p.n, stream_), "ecore");
+  cuda_check(cudaMemcpyAsync(tc_status_host_, tc_status_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "status");
+  sigma_flops += p.flops;
+  ++sigma_calls;
+}
+
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
+  if (precision == Precision::EXACT_TC) {
+    if (p.tc && !p.tcx) free_tc(p);  // packed for the split kernels
+    p.tcx = true;
+    p.reuse_pools = false;
+    sigma_tcx(sb, p, psi, out);
+    return;
+  }
   const int ns = precision_slices(precision);
   if (precision_tc(precision)) sigma_tc(sb, p, psi, out);
   else if (ns) sigma_split(sb, p, ns, psi, out);
@@ -1800,6 +2004,29 @@ int GpuEngine::sigma_launches(const SigmaPlan& p) const {
 
 void GpuEngine::sigma_timed(const Superblock& sb, const SigmaPlan& p, const double* psi, double* out, int reps,
                             float* ms) {
+  ms[0] = ms[1] = ms[2] = 0.f;
+  if (precision == Precision::EXACT_TC) {
+    SigmaPlan& pm = const_cast<SigmaPlan&>(p);
+    sigma_any(sb, pm, psi, out);  // plans and packs the operators outside the timed region
+    sync();
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    for (int r = 0; r < reps; ++r) {
+      cuda_check(cudaEventRecord(e0, stream_), "record");
+      sigma_any(sb, pm, psi, out);
+      cuda_check(cudaEventRecord(e1, stream_), "record");
+      cuda_check(cudaEventSynchronize(e1), "sync");
+      float a;
+      cudaEventElapsedTime(&a, e0, e1);
+      ms[0] += a;
+      ms[1] += a;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sync();  // raises if a pipeline wait ran out
+    return;
+  }
   if (!precision_slices(precision) && !p.scratch) p.scratch = alloc(p.scratch_elems);
   dev::Bufs bufs{};
   bufs.p[0] = arena(*sb.L);
@@ -2110,22 +2337,47 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   bool fp64_verified = false;
   last_defect_rounds_ = 0;
   last_defect_bounded_ = false;
-  if (precision_slices(precision) && refine_mode == 1) {
+  last_plan_flops_ = plan_.flops;
+  if (precision_slices(precision) && (refine_mode == 1 || refine_mode == 2)) {
     constexpr double kEpsSafety = 4.0;
     double eps = 0.0;
     double* prev = alloc((int64_t)nroots * n);  // split-precision sigma rows
+    // mode 2: the FP64-level products on the tensor cores (exact slices),
+    // except until the FP64 product rate of this context is known: the
+    // first solve with a large product measures it on FP64 products (the
+    // rate prices the FP64 solves that these products stand in for)
+    const bool exact = refine_mode == 2 && (fp64_rate_ > 0.0 || plan_.flops < 2e10);
+    SigmaPlan xplan;
+    if (exact) {
+      xplan.tcx = true;
+      xplan.flops = plan_.flops;
+      xplan.bytes = plan_.bytes;
+      xplan.n = plan_.n;
+      xplan.ecore = plan_.ecore;
+    }
     for (int round = 0; round < kDefectRounds; ++round) {
       if (round == 0)
         cuda_check(cudaMemcpyAsync(prev, S, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
                    "copy sigma rows");
       for (int i = 0; i < nroots; ++i) {
+        if (exact && !xplan.tc) {  // exact pools packed outside the product's time
+          plan_tc(sb, xplan);
+          sync();
+        }
         auto t0 = std::chrono::steady_clock::now();
-        sigma(sb, plan_, row(B, i), row(S, i));
+        if (exact) sigma_tcx(sb, xplan, row(B, i), row(S, i));
+        else sigma(sb, plan_, row(B, i), row(S, i));
         sync();
         const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         sigma_seconds += dt;
-        fp64_seconds += dt;
-        ++fp64_calls;
+        if (exact) {
+          exact_seconds += dt;
+          ++exact_calls;
+        } else {
+          fp64_seconds += dt;
+          ++fp64_calls;
+          if (plan_.flops > 0.0 && dt > 0.0) fp64_rate_ = plan_.flops / dt;
+        }
         ++defect_fp64_sigma_;
       }
       if (round == 0) {
@@ -2175,6 +2427,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
       }
     }
     free(prev);
+    if (exact) free_plan(xplan);
     laps.lap("defect correction");
   }
   energies.assign(dav_host_->lam, dav_host_->lam + nroots);
@@ -2186,7 +2439,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
   last_fp64_verified_ = fp64_verified;
   // without a verified FP64 restart (energy-only mode, or rounds / iterations
   // exhausted): FP64 Rayleigh quotients of the final vectors
-  if (precision_slices(precision) && !fp64_verified && (!p.defer_refine || refine_mode == 1)) refine(sb, energies);
+  if (precision_slices(precision) && !fp64_verified && (!p.defer_refine || refine_mode >= 1)) refine(sb, energies);
   sync();
   return total_iter;
 }
@@ -2626,26 +2879,36 @@ void GpuEngine::drop_parked(int id) {
 }
 
 std::string GpuEngine::step_stats() {
-  char buf[200];
-  std::snprintf(buf, sizeof(buf), "  [split sigma %ld x %.4fs, fp64 sigma %ld x %.4fs%s]", split_calls - last_split_calls_,
+  char buf[320];
+  char exact_part[64] = "";
+  if (exact_calls > last_exact_calls_)
+    std::snprintf(exact_part, sizeof(exact_part), ", exact sigma %ld x %.4fs", exact_calls - last_exact_calls_,
+                  (exact_seconds - last_exact_seconds_) / (exact_calls - last_exact_calls_));
+  std::snprintf(buf, sizeof(buf), "  [split sigma %ld x %.4fs, fp64 sigma %ld x %.4fs%s%s]", split_calls - last_split_calls_,
                 split_calls > last_split_calls_ ? (split_seconds - last_split_seconds_) / (split_calls - last_split_calls_)
                                                 : 0.0,
                 fp64_calls - last_fp64_calls_,
                 fp64_calls > last_fp64_calls_ ? (fp64_seconds - last_fp64_seconds_) / (fp64_calls - last_fp64_calls_)
                                               : 0.0,
-                precision_slices(precision) && refine_mode == 1
+                exact_part,
+                precision_slices(precision) && (refine_mode == 1 || refine_mode == 2)
                     ? (last_fp64_verified_ ? (last_defect_bounded_ ? ", FP64 residual bounds met tol"
                                                                    : ", FP64 residuals met tol")
                                            : ", FP64 residuals NOT verified")
                     : "");
   // what the step's Davidson products would have cost in FP64: every product
-  // of the step (split or FP64) at the step's measured FP64 product time
-  const long ds = split_calls - last_split_calls_, df = fp64_calls - last_fp64_calls_;
-  if (df > 0) derived_fp64_sigma_seconds += (double)(ds + df) * ((fp64_seconds - last_fp64_seconds_) / df);
+  // of the step (split, exact or FP64) at the step's measured FP64 product
+  // time, or, without one, at the context's measured FP64 product rate
+  const long ds = split_calls - last_split_calls_, df = fp64_calls - last_fp64_calls_,
+             dx = exact_calls - last_exact_calls_;
+  if (df > 0) derived_fp64_sigma_seconds += (double)(ds + df + dx) * ((fp64_seconds - last_fp64_seconds_) / df);
+  else if (dx > 0 && fp64_rate_ > 0.0) derived_fp64_sigma_seconds += (double)(ds + dx) * (last_plan_flops_ / fp64_rate_);
   last_split_seconds_ = split_seconds;
   last_fp64_seconds_ = fp64_seconds;
   last_split_calls_ = split_calls;
   last_fp64_calls_ = fp64_calls;
+  last_exact_calls_ = exact_calls;
+  last_exact_seconds_ = exact_seconds;
   return buf;
 }
 

@@ -27,7 +27,9 @@ namespace bgpu {
 // accumulation (BF16X3 / BF16X6: warp-level MMA kernel with 2 / 3 slices;
 // BF16X3_TC: tcgen05 / TMEM kernels with 2 slices)
 // (FP16X2_TC: the tcgen05 kernels with 2 fp16 slices, 3 products)
-enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2, BF16X3_TC = 3, FP16X2_TC = 4 };
+// EXACT_TC: the exact-slice tensor-core products (k_tc.cuh), about 1e-13
+// relative; treated as FP64 by the solver (no defect correction)
+enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2, BF16X3_TC = 3, FP16X2_TC = 4, EXACT_TC = 5 };
 inline int precision_slices(Precision p) {
   return (p == Precision::BF16X3 || p == Precision::BF16X3_TC || p == Precision::FP16X2_TC) ? 2
          : p == Precision::BF16X6                                                        ? 3
@@ -123,6 +125,16 @@ struct SigmaPlan {
   // the pools come from (and return to) the engine's pool cache: set for the
   // plan of the sweep's consecutive solves, whose pools have similar sizes
   bool reuse_pools = false;
+  // exact-slice plans (dev::TcxWork; six digit slices per pool block,
+  // 64-column output tiles): row-exponent arrays of the pools, the FP64
+  // stage-1 products T and their packing units into pool S
+  bool tcx = false;
+  int* tcx_ex[dev::kTcPools] = {};
+  int64_t tcx_ex_n[dev::kTcPools] = {};
+  double* tcx_t = nullptr;
+  int64_t tcx_t_n = 0;
+  DevArray<dev::TcPack> tcx_tpack;
+  DevArray<dev::TcxWork> tcx_w1, tcx_w2;
 };
 
 class GpuEngine : public Engine {
@@ -176,6 +188,9 @@ class GpuEngine : public Engine {
   void plan_tc(const Superblock& sb, SigmaPlan& plan);
   void sigma_tc(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d,
                 cudaEvent_t* marks = nullptr);
+  // exact-slice product on tcgen05 (plan.tcx; see k_tc.cuh): pack psi,
+  // phase 1, pack T, phase 2, reduce
+  void sigma_tcx(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d);
   // (re)builds the device work lists of a tensor-core plan for the knobs
   void schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs& knobs);
   // chooses the knobs of a tensor-core plan by timing candidate schedules;
@@ -241,6 +256,15 @@ class GpuEngine : public Engine {
   bool last_defect_bounded_ = false;
   long defect_bounded_ = 0;
   double last_split_eps_ = 0.0;  // the bound eps of one split product (last solve)
+  // exact-slice products of defect correction (refinement mode 2), the FP64
+  // product rate measured in this context (flops / s), the last solve's
+  // FP64-equivalent flops per product
+  long exact_calls = 0;
+  double exact_seconds = 0.0;
+  long last_exact_calls_ = 0;
+  double last_exact_seconds_ = 0.0;
+  double fp64_rate_ = 0.0;
+  double last_plan_flops_ = 0.0;
   double sigma_seconds = 0.0;
   long sigma_calls = 0;
   double sigma_flops = 0.0;

@@ -50,16 +50,21 @@ enum : int { kTcPoolL = 0, kTcPoolR = 1, kTcPoolPsi = 2, kTcPoolPsiT = 3, kTcPoo
 struct TcPack {
   int64_t src_off, dst_off;
   int32_t ld, rows_v, cols_v, rows_p, kp, rt;
+  int32_t ex_off;  // exact pools: first row of this operand in the pool's row-exponent array
   uint8_t src, pool, trans, pad;
 };
 
-// out (+)= alpha * A * B^T over K = kp, A and B packed operands (host plan)
+// out (+)= alpha * A * B^T over K = kp, A and B packed operands (host plan);
+// a_ex / b_ex: the operands' first rows in their pools' row-exponent arrays,
+// o_ex: a stage-1 product's first row in pool S's (exact path)
 struct TcItem {
   int64_t a_off, b_off;
   int32_t kp;
   uint8_t a_pool, b_pool;
   uint16_t pad;
   float alpha;
+  double alpha64;
+  int32_t a_ex, b_ex, o_ex, pad2;
 };
 
 // One task of the host plan: output tile (tm, tn) -- rows 128 tm.. of the A
@@ -140,6 +145,68 @@ int tc_blocks_per_sm(int nb);
 cudaError_t launch_tc_wait_selftest(int* status, unsigned long long* out, uint64_t limit_ns, cudaStream_t s);
 cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
                              cudaStream_t s);
+
+// ---------------------------------------------------------------- exact
+//
+// Products exact to about 2^-42 of each operand row's largest element, on
+// the same tensor cores (the splitting of Ozaki et al., "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59 (2012) 95-118,
+// with fixed-point slices so that the f32 accumulation is exact).  Every
+// operand row r is scaled by 2^-e_r, e_r = 1 + the largest binary exponent
+// of its elements, and written as six balanced base-128 digits
+//   x = 2^e_r sum_{s=0..5} a_s 2^-7(s+1),  a_0 in [-128, 128], a_s in [-64, 63],
+// one bf16 slice per digit (integers of at most 8 bits are exact in bf16).
+// The 21 digit products with s + u <= 5 go to six f32 TMEM accumulators
+// J_q (q = s + u); every term is an integer of at most 2^15 per K element, so
+// that J_q is exact for K <= 512.  After each 512 K (and at the end of an
+// item) sum_q J_q 2^(7(5-q)) is formed exactly in int64 and added, times
+// alpha 2^(e_r + f_c - 49), to an FP64 accumulator of the output tile.
+// The pools hold six slices per block (tc_block_off times kTcxSlices) and an
+// int32 row-exponent array each (the largest unbiased exponent of the row,
+// kTcxNoExp for a zero row).  Output tiles are 128 x 64.
+constexpr int kTcxSlices = 6;
+constexpr int kTcxKBlock = 512;
+constexpr int kTcxNoExp = -100000;
+constexpr int kTcxNB = kTcRowsB;
+
+struct TcxBufs {
+  const double* src[4];  // packing sources: L arena, R arena, psi, T (phase-1 output)
+  __nv_bfloat16* pool[kTcPools];
+  int* ex[kTcPools];
+  double* t;         // phase-1 output T (FP64, the S operands before packing)
+  double* partials;  // phase-2 partial tiles (FP64)
+  int* status;
+};
+
+// One record of the exact kernels (80 bytes): as TcWork, with the FP64
+// alpha and the row-exponent offsets of A, B and (phase 1) of the T rows.
+struct __align__(16) TcxWork {
+  int64_t a_base, b_base, out_base;
+  double alpha;
+  int32_t kp, out_ld, col0;
+  int32_t a_ex, b_ex, o_ex;
+  int16_t h_a, h_b, valid_rows, valid_cols;
+  uint8_t a_pool, b_pool, flags, pad;
+  int32_t pad2[3];
+};
+static_assert(sizeof(TcxWork) == 80, "TcxWork is 80 bytes");
+
+// row exponents of the units' rows (not needed for units whose exponents
+// the phase-1 kernel has already reduced)
+cudaError_t launch_tcx_rowexp(const TcxBufs& b, const TcPack* units, int nunits, cudaStream_t s);
+// digit slices of the units
+cudaError_t launch_tcx_pack(const TcxBufs& b, const TcPack* units, int nunits, cudaStream_t s);
+// phase 1: T tiles (FP64) and the largest exponent of every T row
+// (atomicMax into ex[kTcPoolS], which must start at kTcxNoExp); phase 2:
+// sigma tiles or FP64 partial tiles
+cudaError_t launch_tcx_sigma(int phase, const TcxBufs& b, const TcxWork* work, const int2* ranges, int nblocks,
+                             double* sigma, uint64_t limit_ns, cudaStream_t s);
+int tcx_blocks_per_sm();
+cudaError_t launch_tcx_reduce(const TcxBufs& b, const TcTile* tiles, const int64_t* slots, int ntiles, double* sigma,
+                              cudaStream_t s);
+// every element of x (n ints) = v
+cudaError_t launch_fill_int(int* x, int64_t n, int v, cudaStream_t s);
 
 }  // namespace dev
 }  // namespace bgpu

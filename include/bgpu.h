@@ -62,6 +62,9 @@ extern "C" {
 #define BGPU_PREC_BF16X6 2
 #define BGPU_PREC_BF16X3_TC 3
 #define BGPU_PREC_FP16X2_TC 4
+/* products of six-digit integer slices on the tensor cores, accumulated
+ * exactly and summed in FP64: about 1e-13 relative to FP64 */
+#define BGPU_PREC_EXACT_TC 5
 
 typedef struct bgpu_ctx bgpu_ctx;
 
@@ -90,6 +93,11 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
  *     the first round's Ritz vectors; it is carried through the Ritz
  *     rotations.  Energies are then FP64 Ritz values and the vectors meet
  *     the FP64 convergence test of an FP64 solve.
+ *   mode 2: mode 1 with the restart products on the tensor cores
+ *     (BGPU_PREC_EXACT_TC, about 1e-13 relative to FP64) instead of the FP64
+ *     pipe; until this context has measured its FP64 product rate, a solve
+ *     whose product exceeds 2e10 flops still uses FP64 products (the rate
+ *     prices the FP64 solves in bgpu_run_stats).
  *   mode 0, energy only: one FP64 Rayleigh quotient per converged root, and
  *     in bgpu_run_dmrg only for the steps bgpu_set_refine_window selects.
  */
@@ -450,7 +458,8 @@ int bgpu_transition_onepdm(bgpu_ctx* ctx, int bra, int ket, double* gamma, int n
  * measured FP64 product time, summed over the steps with an FP64 product),
  * the warm-up's wall seconds, the solves accepted on the error bound of
  * their corrections (no FP64 product after the last restart; see
- * bgpu_refinement_stats), then the wall seconds of each sweep. */
+ * bgpu_refinement_stats), the exact-slice restart products and their
+ * seconds (refinement mode 2), then the wall seconds of each sweep. */
 int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n);
 /* Sweep energies (lowest root per sweep, Sweep::do_one's return value,
  * sweep.C:436-453) of the last bgpu_run_dmrg: *n = number of sweeps, up to
