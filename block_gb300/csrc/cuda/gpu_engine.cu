@@ -3034,6 +3034,16 @@ void GpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
     }
     eig_status = eigh_batched(dims, rho, aoff, /*copy_inputs=*/true, dm_vecs_, zoff, w, wo);
   }
+  {
+    // eigenvector signs as on every engine (the basis of the renormalised
+    // block, and so the random noise of later steps, depends on them)
+    DevArray<int> dall, dcm;
+    dall.upload(dm_dims_, stream_);
+    dcm.upload(std::vector<int>(dm_colmajor_.begin(), dm_colmajor_.end()), stream_);
+    cuda_check(dev::launch_canon_signs(dm_vecs_, doff.d, dall.d, dcm.d, nq, stream_), "eigenvector signs");
+    dall.release(stream_);
+    dcm.release(stream_);
+  }
   if (laps.on) {
     sync();
     char what[64];

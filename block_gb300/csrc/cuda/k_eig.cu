@@ -269,6 +269,50 @@ __global__ void __launch_bounds__(kBtThreads) eig_backtransform(EigBufs b, const
 
 }  // namespace
 
+// One CTA per matrix, one warp per eigenvector: the vector's largest
+// component (the first of equal ones) made positive.
+__global__ void __launch_bounds__(256) canon_signs_kernel(double* V, const int64_t* __restrict__ off,
+                                                          const int* __restrict__ dims, const int* __restrict__ colmajor) {
+  const int q = blockIdx.x, n = dims[q];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double* v = V + off[q];
+  const bool cm = colmajor[q] != 0;
+  for (int j = warp; j < n; j += 8) {
+    double best = -1.0, val = 0.0;
+    int bi = n;
+    for (int i = lane; i < n; i += 32) {
+      const double x = cm ? v[(int64_t)j * n + i] : v[(int64_t)i * n + j];
+      if (fabs(x) > best) {
+        best = fabs(x);
+        bi = i;
+        val = x;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double b2 = __shfl_xor_sync(0xffffffffu, best, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      const double v2 = __shfl_xor_sync(0xffffffffu, val, o);
+      if (b2 > best || (b2 == best && i2 < bi)) {
+        best = b2;
+        bi = i2;
+        val = v2;
+      }
+    }
+    if (val < 0.0)
+      for (int i = lane; i < n; i += 32) {
+        double& x = cm ? v[(int64_t)j * n + i] : v[(int64_t)i * n + j];
+        x = -x;
+      }
+  }
+}
+
+cudaError_t launch_canon_signs(double* V, const int64_t* off, const int* dims, const int* colmajor, int nmat,
+                               cudaStream_t s) {
+  if (nmat > 0) canon_signs_kernel<<<nmat, 256, 0, s>>>(V, off, dims, colmajor);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_eig_tridiag(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int tiles,
                                cudaStream_t s) {
   if (njobs <= 0) return cudaSuccess;

@@ -67,6 +67,13 @@ struct EigBufs {
 };
 cudaError_t launch_eig_tridiag(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int tiles,
                                cudaStream_t s);
+// Eigenvector signs made canonical: in matrix q (order dims[q] at V +
+// off[q], eigenvectors as columns, column-major when colmajor[q] else
+// row-major) every eigenvector's largest component (the first of equal
+// ones) positive.  Bases chosen from eigenvectors are then the same on every
+// engine up to rotations inside degenerate eigenspaces.
+cudaError_t launch_canon_signs(double* V, const int64_t* off, const int* dims, const int* colmajor, int nmat,
+                               cudaStream_t s);
 cudaError_t launch_eig_backtransform(const EigBufs& b, const EigJob* jobs, int njobs, int max_n, int bt_ctas,
                                      cudaStream_t s);
 

@@ -473,6 +473,17 @@ void CpuEngine::density(const Superblock& sb, bool left, const std::vector<doubl
     spec.eig[q].resize(d);
     dm_vecs_[q].resize((size_t)d * d);
     jacobi_eigh(d, rho[q].data(), spec.eig[q].data(), dm_vecs_[q].data());
+    // every eigenvector's largest component (the first of equal ones)
+    // positive, as on the GPU: the renormalised basis, and so the random
+    // noise of later steps, depends on the signs
+    double* v = dm_vecs_[q].data();
+    for (int j = 0; j < d; ++j) {
+      int bi = 0;
+      for (int i = 1; i < d; ++i)
+        if (std::fabs(v[(size_t)i * d + j]) > std::fabs(v[(size_t)bi * d + j])) bi = i;
+      if (v[(size_t)bi * d + j] < 0.0)
+        for (int i = 0; i < d; ++i) v[(size_t)i * d + j] = -v[(size_t)i * d + j];
+    }
   }
 }
 
