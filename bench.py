@@ -422,35 +422,6 @@ def run_ours(a):
         line["fp64_path"] = {"ms_per_step": ms64, "tflops": flops / (ms64 * 1e-3) / 1e12,
                              "speedup_of_split": ms64 / (t_step * 1e3),
                              "split_sigma_rel_err": float(np.linalg.norm(sp - ref64) / np.linalg.norm(ref64))}
-    if not a.no_davidson:
-        # Davidson solve of the superblock (tol 1e-8 on the squared residual,
-        # as in the schedule); split precision with defect correction against
-        # FP64 residuals
-        dv = {}
-        precs = [a.precision] + (["fp64"] if split and a.fp64_davidson else [])
-        for prec in precs:
-            ctx.set_precision(prec)
-            r0, f0, _ = ctx.refinement_stats()
-            t0 = time.perf_counter()
-            e, _, it = ctx.davidson(sb, n, nroots=1, tol=1e-8)
-            r1, f1, ver = ctx.refinement_stats()
-            dv[prec] = {"seconds": time.perf_counter() - t0, "iterations": it, "energy": float(e[0]),
-                        "graph_launches": ctx.davidson_graph_launches()}
-            if prec != "fp64":
-                dv[prec].update(defect_rounds=r1 - r0, fp64_products=f1 - f0, fp64_residual_verified=bool(ver),
-                                verified_on=["none", "fp64 residuals", "fp64 residual bounds"][ver])
-        ctx.set_precision(a.precision)
-        if split and ms64 is not None:
-            if "fp64" in dv:
-                dv["dE_split_minus_fp64"] = dv[a.precision]["energy"] - dv["fp64"]["energy"]
-                dv["speedup"] = dv["fp64"]["seconds"] / dv[a.precision]["seconds"]
-            else:
-                # the FP64 solve takes about as many products as the split
-                # one; its time is derived from the measured FP64 product
-                prods = dv[a.precision]["iterations"] + dv[a.precision]["fp64_products"]
-                dv["fp64_derived_seconds"] = prods * ms64 * 1e-3
-                dv["speedup_vs_derived_fp64"] = dv["fp64_derived_seconds"] / dv[a.precision]["seconds"]
-        line["davidson"] = dv
     if split and ref64 is not None and not a.no_exact:
         # the exact-slice tensor-core product (FP64-level, the restart
         # products of defect correction) on the same superblock and input
@@ -464,6 +435,40 @@ def run_ours(a):
                               "speedup_vs_fp64": ms64 / msx,
                               "sigma_rel_err_vs_fp64": float(np.linalg.norm(px - ref64) / np.linalg.norm(ref64)),
                               "products_per_logical_product": 21}
+    if not a.no_davidson:
+        # Davidson solve of the superblock (tol 1e-8 on the squared residual,
+        # as in the schedule); split precision with defect correction against
+        # FP64 residuals
+        dv = {}
+        runs = [(a.precision, "defect")] + ([(a.precision, "exact")] if split else []) + \
+               ([("fp64", "defect")] if split and a.fp64_davidson else [])
+        for prec, refine in runs:
+            ctx.set_precision(prec)
+            ctx.set_refinement(refine)
+            r0, f0, _ = ctx.refinement_stats()
+            t0 = time.perf_counter()
+            e, _, it = ctx.davidson(sb, n, nroots=1, tol=1e-8)
+            r1, f1, ver = ctx.refinement_stats()
+            key = prec if refine == "defect" else prec + "+exact_restarts"
+            dv[key] = {"seconds": time.perf_counter() - t0, "iterations": it, "energy": float(e[0]),
+                       "graph_launches": ctx.davidson_graph_launches()}
+            if prec != "fp64":
+                dv[key].update(defect_rounds=r1 - r0, restart_products=f1 - f0, fp64_residual_verified=bool(ver),
+                               verified_on=["none", "fp64 residuals", "fp64 residual bounds"][ver],
+                               restart_products_on="tensor cores, exact slices" if refine == "exact" else "FP64 pipe")
+        ctx.set_refinement("defect")
+        ctx.set_precision(a.precision)
+        if split and ms64 is not None:
+            if "fp64" in dv:
+                dv["dE_split_minus_fp64"] = dv[a.precision]["energy"] - dv["fp64"]["energy"]
+                dv["speedup"] = dv["fp64"]["seconds"] / dv[a.precision]["seconds"]
+            else:
+                # the FP64 solve takes about as many products as the split
+                # one; its time is derived from the measured FP64 product
+                prods = dv[a.precision]["iterations"] + dv[a.precision]["restart_products"]
+                dv["fp64_derived_seconds"] = prods * ms64 * 1e-3
+                dv["speedup_vs_derived_fp64"] = dv["fp64_derived_seconds"] / dv[a.precision]["seconds"]
+        line["davidson"] = dv
     if rank == 0 and not a.no_cpu_baseline:
         threads = os.cpu_count() or 1
         r = cpu_sample(a.conf, a.partition, a.cpu_reps)

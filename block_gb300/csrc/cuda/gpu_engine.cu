@@ -1981,9 +1981,13 @@ void GpuEngine::sigma_tcx(const Superblock& sb, SigmaPlan& p, const double* psi,
 
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
   if (precision == Precision::EXACT_TC) {
-    if (p.tc && !p.tcx) free_tc(p);  // packed for the split kernels
-    p.tcx = true;
     p.reuse_pools = false;
+    if (p.tc && !p.tcx) free_tc(p);  // packed for the split kernels
+    if (p.scratch) {  // FP64 intermediates (allocated again by an FP64 product)
+      free(p.scratch);
+      p.scratch = nullptr;
+    }
+    p.tcx = true;
     sigma_tcx(sb, p, psi, out);
     return;
   }
@@ -2346,7 +2350,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     // except until the FP64 product rate of this context is known: the
     // first solve with a large product measures it on FP64 products (the
     // rate prices the FP64 solves that these products stand in for)
-    const bool exact = refine_mode == 2 && (fp64_rate_ > 0.0 || plan_.flops < 2e10);
+    bool exact = refine_mode == 2 && (fp64_rate_ > 0.0 || plan_.flops < 2e10);
     SigmaPlan xplan;
     if (exact) {
       xplan.tcx = true;
@@ -2361,8 +2365,18 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
                    "copy sigma rows");
       for (int i = 0; i < nroots; ++i) {
         if (exact && !xplan.tc) {  // exact pools packed outside the product's time
-          plan_tc(sb, xplan);
-          sync();
+          try {
+            plan_tc(sb, xplan);
+            sync();
+          } catch (const CudaError&) {
+            // not enough device memory for the exact pools next to the
+            // split ones: this solve keeps FP64 restart products
+            cudaGetLastError();
+            free_plan(xplan);
+            sync();
+            exact = false;
+            ++exact_fallbacks_;
+          }
         }
         auto t0 = std::chrono::steady_clock::now();
         if (exact) sigma_tcx(sb, xplan, row(B, i), row(S, i));

@@ -27,7 +27,7 @@ namespace bgpu {
 // accumulation (BF16X3 / BF16X6: warp-level MMA kernel with 2 / 3 slices;
 // BF16X3_TC: tcgen05 / TMEM kernels with 2 slices)
 // (FP16X2_TC: the tcgen05 kernels with 2 fp16 slices, 3 products)
-// EXACT_TC: the exact-slice tensor-core products (k_tc.cuh), about 1e-13
+// EXACT_TC: the exact-slice tensor-core products (k_tc.cuh), about 1e-12
 // relative; treated as FP64 by the solver (no defect correction)
 enum class Precision : int { FP64 = 0, BF16X3 = 1, BF16X6 = 2, BF16X3_TC = 3, FP16X2_TC = 4, EXACT_TC = 5 };
 inline int precision_slices(Precision p) {
@@ -260,6 +260,7 @@ class GpuEngine : public Engine {
   // product rate measured in this context (flops / s), the last solve's
   // FP64-equivalent flops per product
   long exact_calls = 0;
+  long exact_fallbacks_ = 0;  // solves whose exact pools did not fit (FP64 products instead)
   double exact_seconds = 0.0;
   long last_exact_calls_ = 0;
   double last_exact_seconds_ = 0.0;

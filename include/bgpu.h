@@ -63,7 +63,7 @@ extern "C" {
 #define BGPU_PREC_BF16X3_TC 3
 #define BGPU_PREC_FP16X2_TC 4
 /* products of six-digit integer slices on the tensor cores, accumulated
- * exactly and summed in FP64: about 1e-13 relative to FP64 */
+ * exactly and summed in FP64: about 1e-12 relative to FP64 */
 #define BGPU_PREC_EXACT_TC 5
 
 typedef struct bgpu_ctx bgpu_ctx;
@@ -94,7 +94,7 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
  *     rotations.  Energies are then FP64 Ritz values and the vectors meet
  *     the FP64 convergence test of an FP64 solve.
  *   mode 2: mode 1 with the restart products on the tensor cores
- *     (BGPU_PREC_EXACT_TC, about 1e-13 relative to FP64) instead of the FP64
+ *     (BGPU_PREC_EXACT_TC, about 1e-12 relative to FP64) instead of the FP64
  *     pipe; until this context has measured its FP64 product rate, a solve
  *     whose product exceeds 2e10 flops still uses FP64 products (the rate
  *     prices the FP64 solves in bgpu_run_stats).

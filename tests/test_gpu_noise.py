@@ -6,7 +6,10 @@ same seed gives bit-identical sweep energies on a second run, and every
 sweep energy is within 1e-6 Eh of the oracle's run of the same input (the
 noise matrices themselves agree to 1e-13, tests/test_gpu_blocks.py; the
 sweeps part by the Davidson tolerance's effect on an unconverged
-trajectory, as without noise)."""
+trajectory, as without noise).  The random noise is drawn element by
+element in the basis of the renormalised blocks, which the density-matrix
+eigenvectors define: both engines make every eigenvector's largest
+component positive, so that their bases, and with them the noise, agree."""
 import numpy as np
 import pytest
 
