@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="bf16x3tc", choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc", "fp16x2tc"])
+    ap.add_argument("--precision", default="bf16x3tc",
+                    choices=["fp64", "bf16x3", "bf16x6", "bf16x3tc", "fp16x2tc", "exacttc"])
     ap.add_argument("--conf", default=DEFAULT_CONF)
     ap.add_argument("--partition", type=int, default=DEFAULT_PARTITION)
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson solve")
@@ -353,9 +354,10 @@ def run_ours(a):
                 "algorithmic_bytes_per_step": nbytes}
     else:
         pk = peaks.get("bf16_tflops", 1900.0)
-        prods = 6 if a.precision == "bf16x6" else 3
-        kname = ("tc_sigma_kernel<1>+<2> (tcgen05/TMEM two-phase sector GEMMs, bf16 slices)"
-                 if tc_path else "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)")
+        prods = {"bf16x6": 6, "exacttc": 21}.get(a.precision, 3)
+        kname = ("tc_sigma_kernel<1>+<2> (tcgen05/TMEM two-phase sector GEMMs, bf16 slices)" if tc_path else
+                 "tcx_sigma_kernel<1>+<2> (tcgen05/TMEM exact-slice sector GEMMs, 6 bf16 digits, FP64 sums)"
+                 if a.precision == "exacttc" else "fused_sigma_kernel (two-stage sector GEMMs, bf16 slices)")
         traffic = NCU_TRAFFIC.get((os.path.relpath(a.conf, ROOT), a.partition, a.precision))
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
                 "traffic": traffic, "traffic_unit": "bytes per sigma (both tensor-core kernels, ncu)",
@@ -364,7 +366,7 @@ def run_ours(a):
                 "peak_source": ("bf16_tflops of measured" if peaks else "fallback 1900"),
                 "products_per_logical_product": prods,
                 "tensor_issued_tflops": prods * achieved, "tensor_issued_frac": prods * achieved / pk,
-                "note_issued": "3 (6) bf16 products per logical FP64 product, without tile padding",
+                "note_issued": "bf16 products per logical FP64 product, without tile padding",
                 "fp64_peak_tflops_in_run": fp64, "algorithmic_bytes_per_step": nbytes}
     if tc_path:
         info = ctx.superblock_info(sb)
@@ -374,8 +376,9 @@ def run_ours(a):
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": {"fp64": "f64", "fp16x2tc": "fp16 slices, f32 accumulate"}.get(a.precision,
-                                                                                     "bf16 slices, f32 accumulate"),
+            "dtype": {"fp64": "f64", "fp16x2tc": "fp16 slices, f32 accumulate",
+                      "exacttc": "bf16 digit slices, exact f32 accumulate, f64 sums"}.get(a.precision,
+                                                                                          "bf16 slices, f32 accumulate"),
             "data": "synthetic",
             "config": config_dict(a.conf, a.partition, n, a.precision, nbytes / 1e6),
             "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
@@ -422,7 +425,7 @@ def run_ours(a):
         line["fp64_path"] = {"ms_per_step": ms64, "tflops": flops / (ms64 * 1e-3) / 1e12,
                              "speedup_of_split": ms64 / (t_step * 1e3),
                              "split_sigma_rel_err": float(np.linalg.norm(sp - ref64) / np.linalg.norm(ref64))}
-    if split and ref64 is not None and not a.no_exact:
+    if split and ref64 is not None and not a.no_exact and a.precision != "exacttc":
         # the exact-slice tensor-core product (FP64-level, the restart
         # products of defect correction) on the same superblock and input
         ctx.set_precision("exacttc")
@@ -431,6 +434,7 @@ def run_ours(a):
         px = ctx.to_host(yx, n)
         ctx.device_free(yx)
         ctx.set_precision(a.precision)
+        ctx.sigma_timed(sb, x, y, 1)  # back to the split pools (frees the exact ones)
         line["exact_path"] = {"ms_per_step": msx, "tflops": flops / (msx * 1e-3) / 1e12,
                               "speedup_vs_fp64": ms64 / msx,
                               "sigma_rel_err_vs_fp64": float(np.linalg.norm(px - ref64) / np.linalg.norm(ref64)),
@@ -440,7 +444,7 @@ def run_ours(a):
         # as in the schedule); split precision with defect correction against
         # FP64 residuals
         dv = {}
-        runs = [(a.precision, "defect")] + ([(a.precision, "exact")] if split else []) + \
+        runs = [(a.precision, "defect")] + ([(a.precision, "exact")] if split and a.precision != "exacttc" else []) + \
                ([("fp64", "defect")] if split and a.fp64_davidson else [])
         for prec, refine in runs:
             ctx.set_precision(prec)

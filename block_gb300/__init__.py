@@ -434,9 +434,10 @@ class Context:
         return v.value
 
     def set_refinement(self, mode):
-        """Split-precision solves: "defect" (FP64-residual defect correction
-        with FP64 products), "exact" (the same with the exact-slice
-        tensor-core products) or "energy" (FP64 Rayleigh quotients only)."""
+        """Split-precision solves: "exact" (FP64-residual defect correction
+        with exact-slice tensor-core restart products, the default),
+        "defect" (the same with FP64 products) or "energy" (FP64 Rayleigh
+        quotients only)."""
         self._check(self.lib.bgpu_set_refinement(self.h, {"energy": 0, "defect": 1, "exact": 2}[mode]))
 
     def refinement_stats(self):

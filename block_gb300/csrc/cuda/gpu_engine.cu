@@ -1979,6 +1979,66 @@ void GpuEngine::sigma_tcx(const Superblock& sb, SigmaPlan& p, const double* psi,
   ++sigma_calls;
 }
 
+void GpuEngine::sigma_exact(const Superblock& sb, const SigmaPlan& ref, const double* psi, double* out) {
+  // device bytes of one exact plan: six digit slices (12 B) per packed
+  // element of every pool, and the FP64 stage-1 products (8 B each); the
+  // split plan's pools hold two bf16 slices (4 B) per packed element
+  int64_t split_elems = 0;
+  for (int i = 0; i < dev::kTcPools; ++i) split_elems += ref.tc_pool_elems[i];
+  double need = 6.0 * (double)split_elems + 4.0 * (double)ref.tc_pool_elems[dev::kTcPoolS];
+  if (split_elems == 0) need = 0.0;  // no split plan to size from: one chunk
+  sync();
+  size_t free_b = 0, total_b = 0;
+  cuda_check(cudaMemGetInfo(&free_b, &total_b), "memory info");
+  const int nterm = (int)sb.terms.size();
+  int nchunks = need > 0.0 ? (int)std::ceil(need / (0.8 * (double)free_b)) : 1;
+  nchunks = std::max(1, std::min(nchunks, std::max(1, nterm)));
+  for (;;) {
+    bool ok = true;
+    double* tmp = nullptr;
+    try {
+      if (nchunks > 1) tmp = alloc(sb.size);
+      for (int c = 0; c < nchunks && ok; ++c) {
+        Superblock part = sb;
+        const int t0 = (int)((int64_t)nterm * c / nchunks), t1 = (int)((int64_t)nterm * (c + 1) / nchunks);
+        part.terms.assign(sb.terms.begin() + t0, sb.terms.begin() + t1);
+        part.ecore = c == 0 ? sb.ecore : 0.0;
+        SigmaPlan xp;
+        xp.tcx = true;
+        xp.n = ref.n;
+        xp.ecore = part.ecore;
+        xp.flops = ref.flops * (double)(t1 - t0) / std::max(1, nterm);
+        try {
+          plan_tc(part, xp);
+          sigma_tcx(part, xp, psi, nchunks > 1 ? tmp : out);
+          sync();
+        } catch (const CudaError&) {
+          cudaGetLastError();
+          free_plan(xp);
+          sync();
+          ok = false;
+          break;
+        }
+        free_plan(xp);
+        if (nchunks > 1) {
+          if (c == 0) cuda_check(cudaMemcpyAsync(out, tmp, sb.size * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy");
+          else cuda_check(dev::launch_axpy(1.0, tmp, out, sb.size, stream_), "sum of chunks");
+        }
+      }
+    } catch (const CudaError&) {  // the chunk buffer itself
+      cudaGetLastError();
+      ok = false;
+    }
+    if (tmp) free(tmp);
+    sync();
+    if (ok) break;
+    if (nchunks >= std::max(1, nterm) || nchunks >= 64) throw CudaError("exact product: device memory too small");
+    nchunks = std::min(std::max(1, nterm), nchunks * 2);
+    ++exact_fallbacks_;
+  }
+  last_exact_chunks_ = nchunks;
+}
+
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
   if (precision == Precision::EXACT_TC) {
     p.reuse_pools = false;
@@ -2348,38 +2408,18 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
     double* prev = alloc((int64_t)nroots * n);  // split-precision sigma rows
     // mode 2: the FP64-level products on the tensor cores (exact slices),
     // except until the FP64 product rate of this context is known: the
-    // first solve with a large product measures it on FP64 products (the
-    // rate prices the FP64 solves that these products stand in for)
-    bool exact = refine_mode == 2 && (fp64_rate_ > 0.0 || plan_.flops < 2e10);
-    SigmaPlan xplan;
-    if (exact) {
-      xplan.tcx = true;
-      xplan.flops = plan_.flops;
-      xplan.bytes = plan_.bytes;
-      xplan.n = plan_.n;
-      xplan.ecore = plan_.ecore;
-    }
+    // first solve with a product of at least kRateFlops measures it on FP64
+    // products (the rate prices the FP64 solves that these products stand
+    // in for; smaller products run below the FP64 pipe's rate)
+    constexpr double kRateFlops = 1e11;
+    const bool exact = refine_mode == 2 && (fp64_rate_ > 0.0 || plan_.flops < kRateFlops);
     for (int round = 0; round < kDefectRounds; ++round) {
       if (round == 0)
         cuda_check(cudaMemcpyAsync(prev, S, (size_t)nroots * n * sizeof(double), cudaMemcpyDeviceToDevice, stream_),
                    "copy sigma rows");
       for (int i = 0; i < nroots; ++i) {
-        if (exact && !xplan.tc) {  // exact pools packed outside the product's time
-          try {
-            plan_tc(sb, xplan);
-            sync();
-          } catch (const CudaError&) {
-            // not enough device memory for the exact pools next to the
-            // split ones: this solve keeps FP64 restart products
-            cudaGetLastError();
-            free_plan(xplan);
-            sync();
-            exact = false;
-            ++exact_fallbacks_;
-          }
-        }
         auto t0 = std::chrono::steady_clock::now();
-        if (exact) sigma_tcx(sb, xplan, row(B, i), row(S, i));
+        if (exact) sigma_exact(sb, plan_, row(B, i), row(S, i));
         else sigma(sb, plan_, row(B, i), row(S, i));
         sync();
         const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -2390,7 +2430,7 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
         } else {
           fp64_seconds += dt;
           ++fp64_calls;
-          if (plan_.flops > 0.0 && dt > 0.0) fp64_rate_ = plan_.flops / dt;
+          if (plan_.flops >= kRateFlops && dt > 0.0) fp64_rate_ = plan_.flops / dt;
         }
         ++defect_fp64_sigma_;
       }
@@ -2441,7 +2481,6 @@ int GpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
       }
     }
     free(prev);
-    if (exact) free_plan(xplan);
     laps.lap("defect correction");
   }
   energies.assign(dav_host_->lam, dav_host_->lam + nroots);

@@ -191,6 +191,11 @@ class GpuEngine : public Engine {
   // exact-slice product on tcgen05 (plan.tcx; see k_tc.cuh): pack psi,
   // phase 1, pack T, phase 2, reduce
   void sigma_tcx(const Superblock& sb, SigmaPlan& plan, const double* psi_d, double* out_d);
+  // one exact-slice product of sb with plans built and freed on the spot:
+  // the pair terms are cut into as many chunks as the free device memory
+  // needs (each chunk's plan packs only its own operators), the chunks'
+  // products summed; `ref` is a plan of sb (sizes of its split pools, flops)
+  void sigma_exact(const Superblock& sb, const SigmaPlan& ref, const double* psi_d, double* out_d);
   // (re)builds the device work lists of a tensor-core plan for the knobs
   void schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs& knobs);
   // chooses the knobs of a tensor-core plan by timing candidate schedules;
@@ -244,9 +249,11 @@ class GpuEngine : public Engine {
   void tridiagonal_dc(const std::vector<dev::EigJob>& jobs, const dev::EigJob* djobs, double* wk, int* status);
   int64_t wave_size() const { return wave_n_; }
   Precision precision = Precision::FP64;
-  // split-precision solves: 1 (default) defect correction against FP64
-  // residuals; 0 only FP64 Rayleigh quotients of the converged split vectors
-  int refine_mode = 1;
+  // split-precision solves: defect correction against FP64 residuals with
+  // restart products on the FP64 pipe (1) or exact-slice products on the
+  // tensor cores (2, default); 0 only FP64 Rayleigh quotients of the
+  // converged split vectors
+  int refine_mode = 2;
   static constexpr int kDefectRounds = 8;  // FP64 restarts per solve at most
   int last_defect_rounds_ = 0;             // FP64 restarts of the last solve
   bool last_fp64_verified_ = false;        // its roots met tol on FP64 residuals
@@ -260,7 +267,8 @@ class GpuEngine : public Engine {
   // product rate measured in this context (flops / s), the last solve's
   // FP64-equivalent flops per product
   long exact_calls = 0;
-  long exact_fallbacks_ = 0;  // solves whose exact pools did not fit (FP64 products instead)
+  long exact_fallbacks_ = 0;  // exact products retried with more term chunks after running out of memory
+  int last_exact_chunks_ = 0;  // term chunks of the last exact product
   double exact_seconds = 0.0;
   long last_exact_calls_ = 0;
   double last_exact_seconds_ = 0.0;

@@ -79,7 +79,7 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
 /*
  * Refinement of split-precision Davidson solves (no reference counterpart;
  * the reference iterates in FP64 throughout, linear.C:179-385):
- *   mode 1 (default), defect correction: after the split-precision solve
+ *   mode 1, defect correction: after the split-precision solve
  *     converges, its Ritz vectors get FP64 products and the Davidson
  *     restarts from them with their FP64 subspace matrix and residuals;
  *     further basis vectors (corrections) get split-precision products.
@@ -93,11 +93,12 @@ int bgpu_set_precision(bgpu_ctx* ctx, int precision);
  *     the first round's Ritz vectors; it is carried through the Ritz
  *     rotations.  Energies are then FP64 Ritz values and the vectors meet
  *     the FP64 convergence test of an FP64 solve.
- *   mode 2: mode 1 with the restart products on the tensor cores
+ *   mode 2 (default): mode 1 with the restart products on the tensor cores
  *     (BGPU_PREC_EXACT_TC, about 1e-12 relative to FP64) instead of the FP64
- *     pipe; until this context has measured its FP64 product rate, a solve
- *     whose product exceeds 2e10 flops still uses FP64 products (the rate
- *     prices the FP64 solves in bgpu_run_stats).
+ *     pipe, with the pair terms cut into as many chunks as the free device
+ *     memory needs; until this context has measured its FP64 product rate, a
+ *     solve whose product has at least 1e11 flops still uses FP64 products
+ *     (the rate prices the FP64 solves in bgpu_run_stats).
  *   mode 0, energy only: one FP64 Rayleigh quotient per converged root, and
  *     in bgpu_run_dmrg only for the steps bgpu_set_refine_window selects.
  */

@@ -35,7 +35,7 @@ pytestmark = pytest.mark.gpu
 def split_ctx(gpu_ctx):
     yield gpu_ctx
     gpu_ctx.set_precision("fp64")
-    gpu_ctx.set_refinement("defect")
+    gpu_ctx.set_refinement("exact")
 
 
 @pytest.mark.parametrize("prec", ["bf16x3tc", "fp16x2tc", "bf16x3"])

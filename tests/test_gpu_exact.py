@@ -31,7 +31,7 @@ def rel(a, b):
 def exact_ctx(gpu_ctx):
     yield gpu_ctx
     gpu_ctx.set_precision("fp64")
-    gpu_ctx.set_refinement("defect")
+    gpu_ctx.set_refinement("exact")
 
 
 @pytest.mark.parametrize("name,sweep,pos", SNAPS)
