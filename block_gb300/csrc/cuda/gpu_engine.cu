@@ -2039,6 +2039,156 @@ void GpuEngine::sigma_exact(const Superblock& sb, const SigmaPlan& ref, const do
   last_exact_chunks_ = nchunks;
 }
 
+void GpuEngine::gemm_exact(const dev::Bufs& bufs, const std::vector<dev::GemmUnit>& units,
+                           const std::vector<dev::GemmItem>& items) {
+  using namespace dev;
+  if (units.empty()) return;
+  const int c_buf = units[0].c_buf;
+  std::vector<TcPack> packs;
+  packs.reserve(2 * items.size());
+  int64_t pool_n[2] = {0, 0}, ex_n[2] = {0, 0};
+  struct Ref {
+    int64_t off;
+    int32_t ex;
+  };
+  std::vector<Ref> aref(items.size()), bref(items.size());
+  for (const GemmUnit& u : units) {
+    if (u.c_buf != c_buf || u.beta_one) throw std::logic_error("gemm_exact: one output buffer, overwritten");
+    for (int i = u.ibeg; i < u.iend; ++i) {
+      const GemmItem& g = items[i];
+      TcPack a{};  // A view: u.m x k
+      a.src = g.a_buf;
+      a.src_off = g.a_off;
+      a.ld = g.lda;
+      a.trans = g.ta;
+      a.rows_v = u.m;
+      a.cols_v = g.k;
+      a.rows_p = tc_round8(u.m);
+      a.kp = tc_round16(g.k);
+      a.rt = kTcRowsA;
+      a.pool = kTcPoolL;
+      a.dst_off = pool_n[0];
+      a.ex_off = (int32_t)ex_n[0];
+      pool_n[0] += (int64_t)kTcxSlices * a.rows_p * a.kp;
+      ex_n[0] += a.rows_p;
+      aref[i] = {a.dst_off, a.ex_off};
+      packs.push_back(a);
+      TcPack b{};  // B^T view: u.n x k (element (j, kk) = op(B)(kk, j))
+      b.src = g.b_buf;
+      b.src_off = g.b_off;
+      b.ld = g.ldb;
+      b.trans = g.tb ? 0 : 1;
+      b.rows_v = u.n;
+      b.cols_v = g.k;
+      b.rows_p = tc_round8(u.n);
+      b.kp = tc_round16(g.k);
+      b.rt = kTcxNB;
+      b.pool = kTcPoolR;
+      b.dst_off = pool_n[1];
+      b.ex_off = (int32_t)ex_n[1];
+      pool_n[1] += (int64_t)kTcxSlices * b.rows_p * b.kp;
+      ex_n[1] += b.rows_p;
+      bref[i] = {b.dst_off, b.ex_off};
+      packs.push_back(b);
+    }
+  }
+  if (ex_n[0] > INT32_MAX || ex_n[1] > INT32_MAX) throw std::runtime_error("gemm_exact: too many rows");
+  // tasks: 128 x 64 tiles of every unit, with the unit's items
+  struct Task {
+    int u, tm, tn;
+  };
+  std::vector<Task> tasks;
+  std::vector<double> cost;
+  for (int u = 0; u < (int)units.size(); ++u) {
+    const GemmUnit& U = units[u];
+    for (int tm = 0; tm < (U.m + kTcRowsA - 1) / kTcRowsA; ++tm)
+      for (int tn = 0; tn < (U.n + kTcxNB - 1) / kTcxNB; ++tn) {
+        tasks.push_back({u, tm, tn});
+        double c = 400.0;
+        for (int i = U.ibeg; i < U.iend; ++i) c += 400.0 + tc_round16(items[i].k);
+        cost.push_back(c);
+      }
+  }
+  std::vector<int64_t> bundle(tasks.size());
+  for (size_t t = 0; t < tasks.size(); ++t) bundle[t] = -(int64_t)t - 1;
+  std::vector<int> order;
+  std::vector<int2> ranges;
+  schedule_lpt(cost, bundle, tcx_blocks_per_sm() * sm_count(), order, ranges);
+  std::vector<TcxWork> w;
+  std::vector<int2> wr(ranges.size());
+  for (size_t j = 0; j < ranges.size(); ++j) {
+    wr[j].x = (int)w.size();
+    for (int k = ranges[j].x; k < ranges[j].y; ++k) {
+      const Task& T = tasks[order[k]];
+      const GemmUnit& U = units[T.u];
+      TcxWork base{};
+      base.h_a = (int16_t)std::min(kTcRowsA, tc_round8(U.m) - kTcRowsA * T.tm);
+      base.h_b = (int16_t)std::min(kTcxNB, tc_round8(U.n) - kTcxNB * T.tn);
+      base.valid_rows = (int16_t)std::min(kTcRowsA, U.m - kTcRowsA * T.tm);
+      base.valid_cols = (int16_t)std::min(kTcxNB, U.n - kTcxNB * T.tn);
+      base.out_base = U.c_off + (int64_t)kTcRowsA * T.tm * U.ldc + kTcxNB * T.tn;
+      base.out_ld = U.ldc;
+      if (U.ibeg == U.iend) {
+        TcxWork x = base;
+        x.flags = (uint8_t)(kTcDirect | kTcFirst | kTcLast | kTcEmpty);
+        w.push_back(x);
+        continue;
+      }
+      for (int i = U.ibeg; i < U.iend; ++i) {
+        const GemmItem& g = items[i];
+        TcxWork x = base;
+        const int kp = tc_round16(g.k);
+        x.a_base = aref[i].off + (int64_t)kTcxSlices * kTcRowsA * T.tm * kp;
+        x.b_base = bref[i].off + (int64_t)kTcxSlices * kTcxNB * T.tn * kp;
+        x.a_ex = aref[i].ex + kTcRowsA * T.tm;
+        x.b_ex = bref[i].ex + kTcxNB * T.tn;
+        x.kp = kp;
+        x.alpha = g.alpha;
+        x.a_pool = kTcPoolL;
+        x.b_pool = kTcPoolR;
+        x.flags = (uint8_t)(kTcDirect | (i == U.ibeg ? kTcFirst : 0) | (i + 1 == U.iend ? kTcLast : 0) |
+                            kTcGStart | kTcGEnd);
+        w.push_back(x);
+      }
+    }
+    wr[j].y = (int)w.size();
+  }
+  TcxBufs xb{};
+  for (int i = 0; i < 4; ++i) xb.src[i] = bufs.p[i];
+  __nv_bfloat16* pools[2] = {nullptr, nullptr};
+  int* exs[2] = {nullptr, nullptr};
+  for (int i = 0; i < 2; ++i) {
+    cuda_check(cudaMallocAsync((void**)&pools[i], (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16),
+                               stream_),
+               "exact gemm pool");
+    cuda_check(cudaMallocAsync((void**)&exs[i], (size_t)std::max<int64_t>(ex_n[i], 1) * sizeof(int), stream_),
+               "exact gemm exponents");
+  }
+  xb.pool[kTcPoolL] = pools[0];
+  xb.pool[kTcPoolR] = pools[1];
+  xb.ex[kTcPoolL] = exs[0];
+  xb.ex[kTcPoolR] = exs[1];
+  xb.status = tc_status_;
+  DevArray<TcPack> dp;
+  DevArray<TcxWork> dw;
+  DevArray<int2> dr;
+  dp.upload(packs, stream_);
+  dw.upload(w, stream_);
+  dr.upload(wr, stream_);
+  constexpr uint64_t kWaitLimitNs = 1000000000ull;
+  cuda_check(launch_tcx_rowexp(xb, dp.d, (int)packs.size(), stream_), "exact gemm exponents");
+  cuda_check(launch_tcx_pack(xb, dp.d, (int)packs.size(), stream_), "exact gemm pack");
+  cuda_check(launch_tcx_sigma(2, xb, dw.d, dr.d, (int)wr.size(), bufs.p[c_buf], kWaitLimitNs, stream_),
+             "exact gemm");
+  dp.release(stream_);
+  dw.release(stream_);
+  dr.release(stream_);
+  for (int i = 0; i < 2; ++i) {
+    cudaFreeAsync(pools[i], stream_);
+    cudaFreeAsync(exs[i], stream_);
+  }
+}
+
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
   if (precision == Precision::EXACT_TC) {
     p.reuse_pools = false;
@@ -3684,8 +3834,13 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
     bufs.p[1] = dst;
     bufs.p[2] = rot_;
     bufs.p[3] = tmp;
-    cuda_check(dev::launch_gemm(bufs, dua.d, dia.d, dta.d, (int)ta.size(), stream_), "rotate A");
-    cuda_check(dev::launch_gemm(bufs, dub.d, dib.d, dtb.d, (int)tb.size(), stream_), "rotate B");
+    if (renorm_exact()) {
+      gemm_exact(bufs, ua, ia);
+      gemm_exact(bufs, ub, ib);
+    } else {
+      cuda_check(dev::launch_gemm(bufs, dua.d, dia.d, dta.d, (int)ta.size(), stream_), "rotate A");
+      cuda_check(dev::launch_gemm(bufs, dub.d, dib.d, dtb.d, (int)tb.size(), stream_), "rotate B");
+    }
     for (auto* a : {&dua, &dub}) a->release(stream_);
     for (auto* a : {&dia, &dib}) a->release(stream_);
     for (auto* a : {&dta, &dtb}) a->release(stream_);

@@ -196,6 +196,16 @@ class GpuEngine : public Engine {
   // needs (each chunk's plan packs only its own operators), the chunks'
   // products summed; `ref` is a plan of sb (sizes of its split pools, flops)
   void sigma_exact(const Superblock& sb, const SigmaPlan& ref, const double* psi_d, double* out_d);
+  // grouped GEMM of gemm_fp64_kernel's work lists (units written, not
+  // accumulated) with the exact-slice kernels: every item's A and B^T views
+  // packed into six-digit pools, 128 x 64 output tiles, FP64 tile sums;
+  // stream-ordered (no host wait)
+  void gemm_exact(const dev::Bufs& bufs, const std::vector<dev::GemmUnit>& units,
+                  const std::vector<dev::GemmItem>& items);
+  // renormalisation products: 0 FP64 pipe, 1 exact-slice tensor cores for
+  // split-precision runs (default), 2 exact-slice always
+  int renorm_mode = 1;
+  bool renorm_exact() const { return renorm_mode == 2 || (renorm_mode == 1 && precision_slices(precision) > 0); }
   // (re)builds the device work lists of a tensor-core plan for the knobs
   void schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs& knobs);
   // chooses the knobs of a tensor-core plan by timing candidate schedules;

@@ -389,10 +389,12 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
                   if (c >= x.h_b) break;
                   const int eb = __ldg(exb + c);
                   if (eb <= kTcxNoExp / 2) continue;
+                  // the accumulators hold integers below 2^24 in magnitude:
+                  // 32-bit conversions (not the FP64 pipe's 64-bit ones)
                   long long a = 0;
 #pragma unroll
                   for (int q = 0; q < kTcxSlices; ++q)
-                    a += __float2ll_rn(__uint_as_float(v[q][e])) * (1ll << (7 * (kTcxSlices - 1 - q)));
+                    a += (long long)__float2int_rn(__uint_as_float(v[q][e])) * (1ll << (7 * (kTcxSlices - 1 - q)));
                   if (a == 0) continue;
                   const double y = scale_pow2((double)a, (ea + 1) + (eb + 1) - 7 * (kTcxSlices + 1));
                   double* p = accs + c * kTcRowsA + row;

@@ -8,8 +8,9 @@ vector (the convergence test of linear.C:301-335 applied to the FP64
 residual).  Tolerances written here:
   - the returned vectors' squared FP64 residual within the solve's tol;
   - energies within 1e-10 Eh of the FP64 solve on the same superblock;
-  - sweep by sweep, split-precision sweep energies within 1e-6 Eh of the
-    FP64 GPU sweeps, on two truncating C1 cases (16 orbitals at M=200 and 24
+  - sweep by sweep, split-precision sweep energies (exact-slice restart
+    products and renormalisation, the defaults) within 1e-6 Eh of the FP64
+    GPU sweeps, on two truncating C1 cases (16 orbitals at M=200 and 24
     orbitals at M=250, discarded weights up to 1e-2), and on the first the
     FP64 GPU sweeps within 1e-6 Eh of the oracle's.  These sweeps are far
     from converged, so two runs part by more than rounding as soon as their
@@ -100,7 +101,8 @@ def test_split_sweeps_track_fp64_sweeps(split_ctx, oracle, name):
         assert abs(a - b) <= 1e-6, (name, i, a, b)
     for a, b in zip(e64, es):
         assert abs(a - b) <= 1e-6, (name, a, b)
-    assert sts["fp64_sigma_calls"] > 0 and sts["split_sigma_calls"] > sts["fp64_sigma_calls"]
+    restarts = sts["fp64_sigma_calls"] + sts["exact_sigma_calls"]
+    assert restarts > 0 and sts["split_sigma_calls"] > restarts
     if name == "syn16_m200":
         eo, sto = oracle.run(conf(name))
         for i, (a, b) in enumerate(zip(s64, sto["sweep_energies"])):

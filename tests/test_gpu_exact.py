@@ -68,3 +68,20 @@ def test_exact_restart_products(exact_ctx, oracle, name, sweep, pos):
     r = exact_ctx.sigma(sb, v[0]) - e[0] * v[0]
     assert r @ r <= tol, (name, r @ r)
     assert abs(e[0] - e64[0]) <= 1e-10, (name, e[0], e64[0])
+
+
+@pytest.mark.parametrize("name,p", [("c2_d2h", 4), ("h2o_nosym", 5), ("hubbard12", 5)])
+def test_exact_renormalisation(exact_ctx, oracle, name, p):
+    """U^T O U of split-precision runs on the exact-slice kernels (the
+    renormalisation of every operator block, MatrixRotate,
+    MatrixBLAS.C:553-572) against the oracle's FP64 block within 1e-11 of
+    its largest element; FP64 runs keep the FP64 pipe (1e-12)."""
+    from test_gpu_blocks import case_of, density_and_rotations, rel_max
+
+    c = case_of(oracle, name, p)
+    big, sb, _, _, _ = density_and_rotations(exact_ctx, c, name)
+    exact_ctx.set_precision("bf16x3tc")
+    small, n, _ = exact_ctx.renormalise(big, c["kept"], c["small_keys"], rotations=c["rot"])
+    got = exact_ctx.block_download(small, n)
+    err = rel_max(got, c["small_arena"])
+    assert err <= 1e-11, (name, err)
