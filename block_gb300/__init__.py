@@ -505,10 +505,12 @@ class Context:
         self._check(self.lib.bgpu_sweep_energies(self.h, _dp(sw), len(sw), ctypes.byref(ns)))
         stats["sweep_energies"] = sw[:min(ns.value, len(sw))].copy()
         nsw = len(stats["sweep_energies"])
-        rs = np.zeros(10 + nsw)
+        rs = np.zeros(14 + nsw)
         self._check(self.lib.bgpu_run_stats(self.h, _dp(rs), len(rs)))
         stats.update(split_sigma_calls=int(rs[0]), split_sigma_seconds=rs[1], fp64_sigma_calls=int(rs[2]),
                      fp64_sigma_seconds=rs[3], defect_rounds=int(rs[4]), derived_fp64_sigma_seconds=rs[5],
                      warmup_seconds=rs[6], bounded_verifications=int(rs[7]), exact_sigma_calls=int(rs[8]),
-                     exact_sigma_seconds=rs[9], sweep_seconds=rs[10:10 + nsw].copy())
+                     exact_sigma_seconds=rs[9], sweep_renorm_flops=rs[10], fp64_rate=rs[11],
+                     renorm_exact=bool(rs[12]), sweep_renorm_device_seconds=rs[13],
+                     sweep_seconds=rs[14:14 + nsw].copy())
         return e[:nroots].copy(), stats

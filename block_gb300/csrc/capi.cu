@@ -960,7 +960,8 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
     ctx->run_stats = {(double)(E.split_calls - sc0), E.split_seconds - ss0, (double)(E.fp64_calls - fc0),
                       E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
                       r.warmup_seconds, (double)(E.defect_bounded_ - db0), (double)(E.exact_calls - xc0),
-                      E.exact_seconds - xs0};
+                      E.exact_seconds - xs0, r.sweep_renorm_flops, E.fp64_rate_, (double)E.renorm_exact(),
+                      r.sweep_renorm_device_seconds};
     for (double t : r.sweep_seconds) ctx->run_stats.push_back(t);
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {

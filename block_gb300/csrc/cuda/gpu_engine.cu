@@ -450,6 +450,43 @@ void schedule_lpt(const std::vector<double>& cost, const std::vector<int64_t>& b
   }
 }
 
+// Wave assignment: the tasks, in task order, cut into waves of `nblocks`;
+// within a wave the longest-processing-time rule places each task (longest
+// first) on the least-loaded block, so that all blocks work through the
+// waves together; block j runs order[ranges[j].x .. ranges[j].y) in task
+// order.
+void schedule_waves(const std::vector<double>& cost, int nblocks, std::vector<int>& order,
+                    std::vector<int2>& ranges) {
+  const int n = (int)cost.size();
+  order.clear();
+  ranges.clear();
+  if (n == 0) return;
+  nblocks = std::max(1, std::min(nblocks, n));
+  std::vector<std::vector<int>> per(nblocks);
+  std::vector<double> load(nblocks, 0.0);
+  std::vector<int> wave;
+  for (int w0 = 0; w0 < n; w0 += nblocks) {
+    const int w1 = std::min(n, w0 + nblocks);
+    wave.clear();
+    for (int i = w0; i < w1; ++i) wave.push_back(i);
+    std::stable_sort(wave.begin(), wave.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::priority_queue<std::pair<double, int>, std::vector<std::pair<double, int>>, std::greater<>> q;
+    for (int j = 0; j < nblocks; ++j) q.push({load[j], j});
+    for (int i : wave) {
+      auto [l, j] = q.top();
+      q.pop();
+      per[j].push_back(i);
+      load[j] = l + cost[i];
+      q.push({load[j], j});
+    }
+  }
+  for (auto& v : per) {
+    const int b = (int)order.size();
+    for (int i : v) order.push_back(i);
+    ranges.push_back(make_int2(b, (int)order.size()));
+  }
+}
+
 void add_tasks(std::vector<dev::GemmTask>& t, int unit, int m, int n) {
   for (int a = 0; a < (m + 63) / 64; ++a)
     for (int b = 0; b < (n + 63) / 64; ++b) t.push_back({unit, a, b});
@@ -1429,6 +1466,7 @@ TcKnobs GpuEngine::tc_default_knobs() const {
   k.item_cost = env_double("BGPU_TC_ITEM_COST", 400.0);
   k.split = env_double("BGPU_TC_SPLIT", 3.0);
   k.group = (int)env_double("BGPU_TC_GROUP", 16.0);
+  k.waves = (int)env_double("BGPU_TC_WAVES", 0.0);
   return k;
 }
 
@@ -1552,8 +1590,13 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
     // persistent blocks: two per SM with 64-column tiles, one with 128 (and
     // one for the exact kernels)
     const int bps = plan.tcx ? tcx_blocks_per_sm() : tc_blocks_per_sm(nb);
-    schedule_lpt(c1, H.bundle1, bps * nsm, o1, r1);
-    schedule_lpt(c2, bundle2, bps * nsm, o2, r2);
+    if (kn.waves) {
+      schedule_waves(c1, bps * nsm, o1, r1);
+      schedule_waves(c2, bps * nsm, o2, r2);
+    } else {
+      schedule_lpt(c1, H.bundle1, bps * nsm, o1, r1);
+      schedule_lpt(c2, bundle2, bps * nsm, o2, r2);
+    }
   } else {
     // one block per task, tasks grouped by sector, one launch per group
     auto by_sector = [](const std::vector<int>& sec, std::vector<int>& o, std::vector<int2>& r,
@@ -2157,24 +2200,41 @@ void GpuEngine::gemm_exact(const dev::Bufs& bufs, const std::vector<dev::GemmUni
   for (int i = 0; i < 4; ++i) xb.src[i] = bufs.p[i];
   __nv_bfloat16* pools[2] = {nullptr, nullptr};
   int* exs[2] = {nullptr, nullptr};
-  for (int i = 0; i < 2; ++i) {
-    cuda_check(cudaMallocAsync((void**)&pools[i], (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16),
-                               stream_),
-               "exact gemm pool");
-    cuda_check(cudaMallocAsync((void**)&exs[i], (size_t)std::max<int64_t>(ex_n[i], 1) * sizeof(int), stream_),
-               "exact gemm exponents");
+  auto release = [&]() {
+    for (int i = 0; i < 2; ++i) {
+      if (pools[i]) cudaFreeAsync(pools[i], stream_);
+      if (exs[i]) cudaFreeAsync(exs[i], stream_);
+      pools[i] = nullptr;
+      exs[i] = nullptr;
+    }
+  };
+  DevArray<TcPack> dp;
+  DevArray<TcxWork> dw;
+  DevArray<int2> dr;
+  try {
+    for (int i = 0; i < 2; ++i) {
+      cuda_check(cudaMallocAsync((void**)&pools[i], (size_t)std::max<int64_t>(pool_n[i], 8) * sizeof(__nv_bfloat16),
+                                 stream_),
+                 "exact gemm pool");
+      cuda_check(cudaMallocAsync((void**)&exs[i], (size_t)std::max<int64_t>(ex_n[i], 1) * sizeof(int), stream_),
+                 "exact gemm exponents");
+    }
+    dp.upload(packs, stream_);
+    dw.upload(w, stream_);
+    dr.upload(wr, stream_);
+  } catch (...) {
+    // nothing was launched: the caller may run the FP64 path instead
+    dp.release(stream_);
+    dw.release(stream_);
+    dr.release(stream_);
+    release();
+    throw;
   }
   xb.pool[kTcPoolL] = pools[0];
   xb.pool[kTcPoolR] = pools[1];
   xb.ex[kTcPoolL] = exs[0];
   xb.ex[kTcPoolR] = exs[1];
   xb.status = tc_status_;
-  DevArray<TcPack> dp;
-  DevArray<TcxWork> dw;
-  DevArray<int2> dr;
-  dp.upload(packs, stream_);
-  dw.upload(w, stream_);
-  dr.upload(wr, stream_);
   constexpr uint64_t kWaitLimitNs = 1000000000ull;
   cuda_check(launch_tcx_rowexp(xb, dp.d, (int)packs.size(), stream_), "exact gemm exponents");
   cuda_check(launch_tcx_pack(xb, dp.d, (int)packs.size(), stream_), "exact gemm pack");
@@ -2183,10 +2243,7 @@ void GpuEngine::gemm_exact(const dev::Bufs& bufs, const std::vector<dev::GemmUni
   dp.release(stream_);
   dw.release(stream_);
   dr.release(stream_);
-  for (int i = 0; i < 2; ++i) {
-    cudaFreeAsync(pools[i], stream_);
-    cudaFreeAsync(exs[i], stream_);
-  }
+  release();
 }
 
 void GpuEngine::sigma_any(const Superblock& sb, SigmaPlan& p, const double* psi, double* out) {
@@ -3834,13 +3891,23 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
     bufs.p[1] = dst;
     bufs.p[2] = rot_;
     bufs.p[3] = tmp;
-    if (renorm_exact()) {
-      gemm_exact(bufs, ua, ia);
-      gemm_exact(bufs, ub, ib);
-    } else {
-      cuda_check(dev::launch_gemm(bufs, dua.d, dia.d, dta.d, (int)ta.size(), stream_), "rotate A");
-      cuda_check(dev::launch_gemm(bufs, dub.d, dib.d, dtb.d, (int)tb.size(), stream_), "rotate B");
-    }
+    // exact-slice products where their pools fit, else the FP64 pipe
+    auto stage = [&](const std::vector<dev::GemmUnit>& u, const std::vector<dev::GemmItem>& it,
+                     DevArray<dev::GemmUnit>& du, DevArray<dev::GemmItem>& di, DevArray<dev::GemmTask>& dt,
+                     size_t ntask, const char* what) {
+      if (renorm_exact()) {
+        try {
+          gemm_exact(bufs, u, it);
+          return;
+        } catch (const CudaError&) {
+          cudaGetLastError();
+          ++renorm_exact_fallbacks_;
+        }
+      }
+      cuda_check(dev::launch_gemm(bufs, du.d, di.d, dt.d, (int)ntask, stream_), what);
+    };
+    stage(ua, ia, dua, dia, dta, ta.size(), "rotate A");
+    stage(ub, ib, dub, dib, dtb, tb.size(), "rotate B");
     for (auto* a : {&dua, &dub}) a->release(stream_);
     for (auto* a : {&dia, &dib}) a->release(stream_);
     for (auto* a : {&dta, &dtb}) a->release(stream_);
@@ -3963,6 +4030,7 @@ void GpuEngine::renormalise(Block& small, const Block& big) {
     }
   }
   flush();
+  renorm_flops_ += rflops;
   if (laps.on) {
     sync();
     char what[64];

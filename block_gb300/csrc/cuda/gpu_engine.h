@@ -63,9 +63,15 @@ struct TcKnobs {
   int group = 16;            // items per tensor-core accumulation group
   int per_sector = 0;        // 1: one launch per sector, one block per task (baseline)
   int nb = 64;               // output-tile width: 64 (two pipelines per SM) or 128 (one, wider MMAs)
+  // task order across the persistent blocks: 0 longest-processing-time
+  // assignment (column tiles of a row kept on one block), 1 waves (task
+  // order cut into waves of one task per block, balanced within each wave,
+  // so that the blocks work on neighbouring tiles of a sector together and
+  // share its operand tiles in L2)
+  int waves = 0;
   bool operator==(const TcKnobs& o) const {
     return item_cost == o.item_cost && split == o.split && group == o.group && per_sector == o.per_sector &&
-           nb == o.nb;
+           nb == o.nb && waves == o.waves;
   }
 };
 struct TcHostPlan;  // item lists of a tensor-core plan, kept for rescheduling
@@ -160,6 +166,7 @@ class GpuEngine : public Engine {
   bool get_rotation_record(const Block& b, RotationRecord& r) override;
   void set_rotation_record(const Block& b, const RotationRecord& r) override;
   // (synchronises, so that every renormalisation issued so far is counted)
+  double renorm_flops() const override { return renorm_flops_; }
   double device_renorm_seconds() override {
     sync();
     return renorm_device_seconds;
@@ -205,6 +212,8 @@ class GpuEngine : public Engine {
   // renormalisation products: 0 FP64 pipe, 1 exact-slice tensor cores for
   // split-precision runs (default), 2 exact-slice always
   int renorm_mode = 1;
+  long renorm_exact_fallbacks_ = 0;  // renormalisation stages run on the FP64 pipe for want of memory
+  double renorm_flops_ = 0.0;        // FP64-equivalent flops of all renormalisations
   bool renorm_exact() const { return renorm_mode == 2 || (renorm_mode == 1 && precision_slices(precision) > 0); }
   // (re)builds the device work lists of a tensor-core plan for the knobs
   void schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs& knobs);

@@ -771,6 +771,7 @@ SweepResult SweepDriver::run() {
     E_.device_renorm_seconds();  // waits for the warm-up's device work
     res.warmup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - tw).count();
   }
+  const double rd0 = E_.device_renorm_seconds(), rf0 = E_.renorm_flops();
   const int last_sched = C_.schedule.back().iter;
   for (int s = s_begin; s < C_.maxiter; ++s) {
     const bool forward = ((s - s_begin) % 2 == 0) == first_forward;
@@ -831,6 +832,8 @@ SweepResult SweepDriver::run() {
           std::fclose(f);
         }
   }
+  res.sweep_renorm_device_seconds = E_.device_renorm_seconds() - rd0;
+  res.sweep_renorm_flops = E_.renorm_flops() - rf0;
   res.energies = last_energies_;
   res.discarded = last_discarded_;
   res.build_seconds = phase_.build_seconds;

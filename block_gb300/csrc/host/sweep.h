@@ -151,6 +151,8 @@ class Engine {
   virtual void prepare_plan(const Superblock& sb) { (void)sb; }
   // device seconds of the renormalisations so far (< 0: not measured)
   virtual double device_renorm_seconds() { return -1.0; }
+  // FP64-equivalent flops of the renormalisations so far (0 if not counted)
+  virtual double renorm_flops() const { return 0.0; }
   // rotation that made a renormalised block (kept by engines that transform
   // wavefunction guesses), read and restored by checkpoints
   virtual bool get_rotation_record(const Block& b, RotationRecord& r) {
@@ -222,6 +224,8 @@ struct SweepResult {
   // renormalisation
   double build_seconds = 0.0, solve_seconds = 0.0, density_seconds = 0.0, renorm_seconds = 0.0;
   double renorm_device_seconds = -1.0;  // device time of the renormalisations (< 0: not measured)
+  // the same, and their flops, during the sweeps only (warm-up excluded)
+  double sweep_renorm_device_seconds = 0.0, sweep_renorm_flops = 0.0;
 };
 
 struct DriverOptions {

@@ -460,7 +460,11 @@ int bgpu_transition_onepdm(bgpu_ctx* ctx, int bra, int ket, double* gamma, int n
  * the warm-up's wall seconds, the solves accepted on the error bound of
  * their corrections (no FP64 product after the last restart; see
  * bgpu_refinement_stats), the exact-slice restart products and their
- * seconds (refinement mode 2), then the wall seconds of each sweep. */
+ * seconds (refinement mode 2), the FP64-equivalent flops of the sweeps'
+ * renormalisations (warm-up excluded), the FP64 product rate measured in
+ * this context (flops per second, 0 if none), whether the renormalisations
+ * ran on the exact-slice kernels (1) or the FP64 pipe (0), their device
+ * seconds during the sweeps, then the wall seconds of each sweep. */
 int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n);
 /* Sweep energies (lowest root per sweep, Sweep::do_one's return value,
  * sweep.C:436-453) of the last bgpu_run_dmrg: *n = number of sweeps, up to

@@ -2,7 +2,8 @@
 
 hubbard12: open 12-site Hubbard chain, t=1, U=4, half filling (FCIDUMP
 written here).  syn24 / syn30 / syn30_d2h / syn40 (and syn30_sweep1, syn30
-for one sweep; syn40_m1000, syn40 at M=1000): seeded synthetic
+for one sweep; syn30_m1000, syn30 at M=1000, the profiling size of the
+bench's kernels; syn40_m1000, syn40 at M=1000): seeded synthetic
 Cholesky Hamiltonians generated inside the library from the `orbitals
 synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>` spec; syn8 / syn8_d2h are
 small members of the same family used for FCI cross-checks.  syn16_m200
@@ -42,6 +43,7 @@ CONFS = {
                       "sweep_tol 1e-12\nnoreorder\n"),
     "syn30": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_sweep1": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 1\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn30_m1000": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 1000 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_d2h": ("synthetic:30:30:60:30:1", "nelec 30\nspin 0\nschedule\n0 1500 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn40_m1000": ("synthetic:40:40:80:40:0", "nelec 40\nspin 0\nnroots 3\nweights 0.333333333333 0.333333333333 0.333333333334\nschedule\n0 1000 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
     "syn40": ("synthetic:40:40:80:40:0", "nelec 40\nspin 0\nnroots 3\nweights 0.333333333333 0.333333333333 0.333333333334\nschedule\n0 4000 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
