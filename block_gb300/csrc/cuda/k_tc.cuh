@@ -46,12 +46,16 @@ enum : int { kTcPoolL = 0, kTcPoolR = 1, kTcPoolPsi = 2, kTcPoolPsiT = 3, kTcPoo
 
 // One packed operand filled from an FP64 block: view element (r, k) is
 // src[src_off + (trans ? k * ld + r : r * ld + k)] for r < rows_v, k < cols_v;
-// row tiles of rt rows; dst_off in elements of the pool.
+// row tiles of rt rows; dst_off in elements of the pool.  The rows_p rows
+// written are rows row0.. of a packed operand of dst_rows rows at dst_off
+// (row0 = 0 and dst_rows = rows_p, or 0, for a standalone operand; a stack
+// of small operators shares one operand, each member at its own row0).
 struct TcPack {
   int64_t src_off, dst_off;
   int32_t ld, rows_v, cols_v, rows_p, kp, rt;
   int32_t ex_off;  // exact pools: first row of this operand in the pool's row-exponent array
   uint8_t src, pool, trans, pad;
+  int32_t row0, dst_rows;
 };
 
 // out (+)= alpha * A * B^T over K = kp, A and B packed operands (host plan);
@@ -75,6 +79,9 @@ struct TcItem {
 //     direct: the FP64 tile (valid_rows x valid_cols) goes to sigma at
 //     out_off + (128 tm + r) * out_kp + 64 tn + c; otherwise the h_a x h_b
 //     (hi, lo) pairs go to partials + out_off for the reduce kernel.
+//   phase 1, stacked (A is a stack of small operators sharing the B
+//     operand): out_off is the first of the 128 TcRow entries that give each
+//     row's stage-1 operand.
 struct TcTask {
   int32_t a_rows, b_rows;
   int32_t tm, tn;
@@ -82,7 +89,18 @@ struct TcTask {
   int64_t out_off;
   int32_t out_kp, direct;
   int32_t valid_rows, valid_cols;
+  int32_t stacked, pad;
 };
+
+// Row r of a stacked phase-1 tile: row lrow of the packed stage-1 operand S
+// at s_off of pool S (h rows, K = the task's out_ld), scaled by alpha; h = 0
+// for rows past the stack.
+struct __align__(16) TcRow {
+  int64_t s_off;
+  int16_t h, lrow;
+  float alpha;
+};
+static_assert(sizeof(TcRow) == 16, "TcRow is 16 bytes");
 
 // sigma tile (rows r0.., cols c0.., h x w) = sum of the partial slots
 // slots[pbeg..pend) (each with row stride pad, the tile's padded width)
@@ -109,7 +127,8 @@ enum : uint32_t {
   kTcDirect = 4,   // phase 2: result straight into sigma
   kTcEmpty = 8,    // task without items (writes zeros)
   kTcGStart = 16,  // first item of an accumulation group
-  kTcGEnd = 32     // last item of an accumulation group
+  kTcGEnd = 32,    // last item of an accumulation group
+  kTcStacked = 64  // phase 1: A is a stack of operators; out_base indexes TcBufs::rows
 };
 struct __align__(16) TcWork {
   int64_t a_base, b_base, out_base;
@@ -125,6 +144,7 @@ static_assert(sizeof(TcWork) == 64, "TcWork is 64 bytes");
 struct TcBufs {
   const double* src[3];  // FP64 sources of packing: L arena, R arena, psi
   __nv_bfloat16* pool[kTcPools];
+  const TcRow* rows;  // row maps of the stacked phase-1 tiles
   float2* partials;
   int* status;  // set to 1 when a pipeline wait ran out
   int fp16;     // slices are fp16 (else bf16)
@@ -162,11 +182,13 @@ cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t
 // that J_q is exact for K <= 512.  After each 512 K (and at the end of an
 // item) sum_q J_q 2^(7(5-q)) is formed exactly in int64 and added, times
 // alpha 2^(e_r + f_c - 49), to an FP64 accumulator of the output tile.
-// The pools hold six slices per block (tc_block_off times kTcxSlices) and an
+// The pools hold six slices per block (tc_block_off times kTcxSlices; each
+// 16-column half of a block holds its six h x 16 slices together) and an
 // int32 row-exponent array each (the largest unbiased exponent of the row,
 // kTcxNoExp for a zero row).  Output tiles are 128 x 64.
 constexpr int kTcxSlices = 6;
 constexpr int kTcxKBlock = 512;
+constexpr int kTcxKS = 16;  // K per pipeline stage (half of a K-chunk)
 constexpr int kTcxNoExp = -100000;
 constexpr int kTcxNB = kTcRowsB;
 

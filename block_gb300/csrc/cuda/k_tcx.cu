@@ -88,7 +88,11 @@ __global__ void __launch_bounds__(256) tcx_rowexp_kernel(TcxBufs b, const TcPack
 }
 
 // Six digit slices per element; each thread writes one 16-byte core-matrix
-// row (8 consecutive K of one row) of every slice.
+// row (8 consecutive K of one row) of every slice.  Within the block of a
+// K-chunk (h rows x w columns, six slices), each 16-column half holds the six
+// slices of h x 16 one after another (slice s of half p at element
+// (6 p + s) h 16), each in the K-major core-matrix order, so that one bulk
+// copy moves the operand piece of one K=16 step.
 __global__ void __launch_bounds__(256) tcx_pack_kernel(TcxBufs b, const TcPack* __restrict__ units) {
   const TcPack u = units[blockIdx.x];
   const double* src = pick_x(b.src, u.src) + u.src_off;
@@ -122,26 +126,30 @@ __global__ void __launch_bounds__(256) tcx_pack_kernel(TcxBufs b, const TcPack* 
         else w[s][e >> 1] = v;
       }
     }
-    const int t = r / u.rt, c = k0 / kTcKC;
+    const int t = r / u.rt, c = k0 / kTcKC, kk = k0 % kTcKC;
     const int rest = u.rows_p - u.rt * t;
     const int h = rest < u.rt ? rest : u.rt;
-    const int wc = min(kTcKC, u.kp - kTcKC * c);
-    const int64_t off =
-        (int64_t)kTcxSlices * tc_block_off(u.rows_p, u.kp, t, c, u.rt) + (kmajor_off(r - u.rt * t, k0 % kTcKC, h) >> 1);
+    // half kk / 16 of the chunk: six slices of h x 16, one after another
+    const int64_t off = (int64_t)kTcxSlices * tc_block_off(u.rows_p, u.kp, t, c, u.rt) +
+                        (int64_t)(kk / kTcxKS) * kTcxSlices * h * kTcxKS + (kmajor_off(r - u.rt * t, kk % kTcxKS, h) >> 1);
 #pragma unroll
     for (int s = 0; s < kTcxSlices; ++s)
-      *(uint4*)(dst + off + (int64_t)s * h * wc) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+      *(uint4*)(dst + off + (int64_t)s * h * kTcxKS) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
   }
 }
 
-constexpr int kTcxSlots = 2;
-constexpr uint32_t kTcxStageBytes = (uint32_t)kTcxSlices * (kTcRowsA + kTcxNB) * kTcKC * 2;
+constexpr int kTcxSlots = 4;  // stages of one K=16 step
+constexpr uint32_t kTcxStageBytes = (uint32_t)kTcxSlices * (kTcRowsA + kTcxNB) * kTcxKS * 2;
 constexpr int kTcxAccBytes = kTcRowsA * kTcxNB * 8;  // FP64 tile accumulator, column-major
 constexpr int kTcxSmem = kTcxSlots * (int)kTcxStageBytes + kTcxAccBytes;
 constexpr uint32_t kTcxTmemCols = 512;  // six accumulators of 64 columns
-constexpr int kTcxThreads = 192;        // warps 0-3 epilogue, 4 producer, 5 MMA issuer
-constexpr int kTcxProducer = 4, kTcxIssuer = 5;
-constexpr int kTcxChunksPerBlock = kTcxKBlock / kTcKC;
+// warps 0-7 epilogue (warp w: TMEM lanes 32 (w % 4).., tile columns
+// 32 (w / 4)..), 8 producer, 9 MMA issuer
+constexpr int kTcxEpiWarps = 8;
+constexpr int kTcxThreads = 32 * (kTcxEpiWarps + 2);
+constexpr int kTcxProducer = kTcxEpiWarps, kTcxIssuer = kTcxEpiWarps + 1;
+constexpr int kTcxHalf = kTcxNB / 2;  // tile columns per epilogue warp
+constexpr int kTcxStepsPerBlock = kTcxKBlock / kTcxKS;
 
 struct TcxShared {
   uint64_t full[kTcxSlots], empty[kTcxSlots], acc_full, acc_empty, drain;
@@ -254,7 +262,7 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
       mbar_init(&sh.empty[i], 1);
     }
     mbar_init(&sh.acc_full, 1);
-    mbar_init(&sh.acc_empty, 4);
+    mbar_init(&sh.acc_empty, kTcxEpiWarps);
     mbar_init(&sh.drain, 1);
     sh.abort_flag = 0;
     mbar_fence_init();
@@ -278,19 +286,21 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
         if (lane == 0 && !(x.flags & kTcEmpty)) {
           const __nv_bfloat16* pa = pick_x(b.pool, x.a_pool) + x.a_base;
           const __nv_bfloat16* pb = pick_x(b.pool, x.b_pool) + x.b_base;
-          const int nck = (x.kp + kTcKC - 1) / kTcKC;
-          for (int c = 0; c < nck; ++c, ++k) {
-            const int w = min(kTcKC, x.kp - kTcKC * c);
-            const uint32_t abytes = (uint32_t)kTcxSlices * x.h_a * w * 2, bbytes = (uint32_t)kTcxSlices * x.h_b * w * 2;
+          // one stage per K=16 step: half st % 2 of chunk st / 2
+          const int nst = x.kp / kTcxKS;
+          const uint32_t abytes = (uint32_t)kTcxSlices * x.h_a * kTcxKS * 2;
+          const uint32_t bbytes = (uint32_t)kTcxSlices * x.h_b * kTcxKS * 2;
+          for (int st = 0; st < nst; ++st, ++k) {
             const int slot = (int)(k % kTcxSlots);
             if (!tcx_wait(&sh.empty[slot], ((k / kTcxSlots) & 1u) ^ 1u, abort_flag, b.status, limit_ns)) {
               ok = false;
               break;
             }
             uint8_t* dst = smem + slot * kTcxStageBytes;
+            const int64_t ha = (int64_t)kTcxSlices * x.h_a * kTcxKS, hb = (int64_t)kTcxSlices * x.h_b * kTcxKS;
             mbar_expect_tx(&sh.full[slot], abytes + bbytes);
-            bulk_g2s(dst, pa + (int64_t)kTcxSlices * x.h_a * kTcKC * c, abytes, &sh.full[slot]);
-            bulk_g2s(dst + abytes, pb + (int64_t)kTcxSlices * x.h_b * kTcKC * c, bbytes, &sh.full[slot]);
+            bulk_g2s(dst, pa + ha * st, abytes, &sh.full[slot]);
+            bulk_g2s(dst + abytes, pb + hb * st, bbytes, &sh.full[slot]);
           }
         }
         ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -310,15 +320,14 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
         const XRec x = xrec(r, j);
         if (lane == 0 && !(x.flags & kTcEmpty)) {
           const uint32_t idesc = idesc_bf16(128, (x.h_b + 15) & ~15);
-          const int nck = (x.kp + kTcKC - 1) / kTcKC;
-          for (int c = 0; c < nck && ok; ++c, ++k) {
-            const bool blk_first = (c % kTcxChunksPerBlock) == 0;
-            const bool blk_last = (c % kTcxChunksPerBlock) == kTcxChunksPerBlock - 1 || c == nck - 1;
+          const int nst = x.kp / kTcxKS;
+          for (int st = 0; st < nst && ok; ++st, ++k) {
+            const bool blk_first = (st % kTcxStepsPerBlock) == 0;
+            const bool blk_last = (st % kTcxStepsPerBlock) == kTcxStepsPerBlock - 1 || st == nst - 1;
             if (blk_first && !tcx_wait(&sh.acc_empty, (nblk & 1u) ^ 1u, abort_flag, b.status, limit_ns)) {
               ok = false;
               break;
             }
-            const int w = min(kTcKC, x.kp - kTcKC * c);
             const int slot = (int)(k % kTcxSlots);
             if (!tcx_wait(&sh.full[slot], (k / kTcxSlots) & 1u, abort_flag, b.status, limit_ns)) {
               ok = false;
@@ -326,20 +335,17 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
             }
             fence_after_sync();
             const uint32_t sa = smem_u32(smem + slot * kTcxStageBytes);
-            const uint32_t sa_slice = (uint32_t)x.h_a * w * 2, sb_slice = (uint32_t)x.h_b * w * 2;
+            const uint32_t sa_slice = (uint32_t)x.h_a * kTcxKS * 2, sb_slice = (uint32_t)x.h_b * kTcxKS * 2;
             const uint32_t sb = sa + (uint32_t)kTcxSlices * sa_slice;
-            for (int jj = 0; jj < w / 16; ++jj) {
-              const uint32_t ao = (uint32_t)(32 * jj * x.h_a), bo = (uint32_t)(32 * jj * x.h_b);
 #pragma unroll
-              for (int q = 0; q < kTcxSlices; ++q) {
-                const uint32_t d = tmem + (uint32_t)(q * kTcxNB);
+            for (int q = 0; q < kTcxSlices; ++q) {
+              const uint32_t d = tmem + (uint32_t)(q * kTcxNB);
 #pragma unroll
-                for (int s = 0; s <= q; ++s) {
-                  const int u = q - s;
-                  const uint64_t da = smem_desc(sa + (uint32_t)s * sa_slice + ao, x.h_a * 16, 128);
-                  const uint64_t db = smem_desc(sb + (uint32_t)u * sb_slice + bo, x.h_b * 16, 128);
-                  mma_bf16(d, da, db, idesc, (blk_first && jj == 0 && s == 0) ? 0u : 1u);
-                }
+              for (int s = 0; s <= q; ++s) {
+                const int u = q - s;
+                const uint64_t da = smem_desc(sa + (uint32_t)s * sa_slice, x.h_a * 16, 128);
+                const uint64_t db = smem_desc(sb + (uint32_t)u * sb_slice, x.h_b * 16, 128);
+                mma_bf16(d, da, db, idesc, (blk_first && s == 0) ? 0u : 1u);
               }
             }
             mma_commit(&sh.empty[slot]);
@@ -353,10 +359,12 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
       }
     }
   } else {
-    // ---- epilogue: thread `row` owns TMEM lane row and column `row` of
-    // the column-major FP64 tile accumulator
-    const int row = 32 * warp + lane;
-    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4).. and owns tile
+    // columns 32 (w / 4).. of its rows in the column-major FP64 tile
+    // accumulator; thread `row` owns row `row` of those columns
+    const int row = 32 * (warp & 3) + lane;
+    const int cb0 = kTcxHalf * (warp >> 2);
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
     uint32_t nblk = 0;
     bool ok = true;
     for (int base = rg.x; base < rg.y && ok; base += 32) {
@@ -366,40 +374,47 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
       for (int j = 0; j < cnt && ok; ++j) {
         const XRec x = xrec(r, j);
         if (x.flags & kTcFirst)
-          for (int c = 0; c < kTcxNB; ++c) accs[c * kTcRowsA + row] = 0.0;
+          for (int c = cb0; c < cb0 + kTcxHalf; ++c) accs[c * kTcRowsA + row] = 0.0;
         if (!(x.flags & kTcEmpty)) {
+          // row exponent of this thread's row, column exponent of the
+          // warp's column cb0 + lane (read before the wait, so that the
+          // loads overlap the MMAs)
           const int* exa = pick_x(b.ex, x.a_pool) + x.a_ex;
           const int* exb = pick_x(b.ex, x.b_pool) + x.b_ex;
-          const int ea = row < x.h_a ? exa[row] : kTcxNoExp;
-          const bool live = ea > kTcxNoExp / 2;
+          const int ea = row < x.h_a ? __ldg(exa + row) : kTcxNoExp;
+          const int eb_l = cb0 + lane < x.h_b ? __ldg(exb + cb0 + lane) : kTcxNoExp;
+          const bool live_a = ea > kTcxNoExp / 2;
           const int nkb = (x.kp + kTcxKBlock - 1) / kTcxKBlock;
           for (int kb = 0; kb < nkb; ++kb) {
             ok = __all_sync(0xffffffffu, tcx_wait(&sh.acc_full, nblk & 1u, abort_flag, b.status, limit_ns));
             if (!ok) break;
             fence_after_sync();
 #pragma unroll 1
-            for (int g = 0; g < kTcxNB / 16; ++g) {
-              if (16 * g >= x.h_b) break;  // warp-uniform
+            for (int g = 0; g < kTcxHalf / 16; ++g) {
+              const int cb = cb0 + 16 * g;
+              if (cb >= x.h_b) break;  // warp-uniform
               uint32_t v[kTcxSlices][16];
-              tmem_ld16x6(tmem + lane_base + (uint32_t)(16 * g), v);
-              if (live) {
+              tmem_ld16x6(tmem + lane_base + (uint32_t)cb, v);
+              double y[16];
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                  const int c = 16 * g + e;
-                  if (c >= x.h_b) break;
-                  const int eb = __ldg(exb + c);
-                  if (eb <= kTcxNoExp / 2) continue;
-                  // the accumulators hold integers below 2^24 in magnitude:
-                  // 32-bit conversions (not the FP64 pipe's 64-bit ones)
-                  long long a = 0;
+              for (int e = 0; e < 16; ++e) {
+                const int eb = __shfl_sync(0xffffffffu, eb_l, 16 * g + e);  // kTcxNoExp beyond h_b
+                // the accumulators hold integers below 2^24 in magnitude:
+                // 32-bit conversions (not the FP64 pipe's 64-bit ones)
+                long long a = 0;
 #pragma unroll
-                  for (int q = 0; q < kTcxSlices; ++q)
-                    a += (long long)__float2int_rn(__uint_as_float(v[q][e])) * (1ll << (7 * (kTcxSlices - 1 - q)));
-                  if (a == 0) continue;
-                  const double y = scale_pow2((double)a, (ea + 1) + (eb + 1) - 7 * (kTcxSlices + 1));
-                  double* p = accs + c * kTcRowsA + row;
-                  *p = fma(y, x.alpha, *p);
-                }
+                for (int q = 0; q < kTcxSlices; ++q)
+                  a += (long long)__float2int_rn(__uint_as_float(v[q][e])) * (1ll << (7 * (kTcxSlices - 1 - q)));
+                const bool live = live_a && eb > kTcxNoExp / 2 && a != 0;
+                y[e] = live ? scale_pow2((double)a, (ea + 1) + (eb + 1) - 7 * (kTcxSlices + 1)) : 0.0;
+              }
+              if (live_a) {
+                double* p = accs + cb * kTcRowsA + row;
+                double acc[16];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) acc[e] = p[e * kTcRowsA];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) p[e * kTcRowsA] = fma(y[e], x.alpha, acc[e]);
               }
             }
             // accumulators read: the MMA issuer may start the next K block
@@ -411,13 +426,14 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
           if (!ok) break;
         }
         if (!(x.flags & kTcLast)) continue;
-        // the task's tile is complete in this thread's row
+        // the task's tile is complete in this thread's row and columns
+        const int ce = cb0 + kTcxHalf;
         if (PHASE == 1) {
           if (row < x.h_a) {
             const int ncols = min(kTcxNB, x.out_ld - x.col0);
             double* out = b.t + x.out_base + (int64_t)row * x.out_ld + x.col0;
             int m = kTcxNoExp;
-            for (int c = 0; c < ncols; ++c) {
+            for (int c = cb0; c < min(ncols, ce); ++c) {
               const double v = c < x.h_b ? accs[c * kTcRowsA + row] : 0.0;
               out[c] = v;
               m = max(m, exp_of(v));
@@ -427,11 +443,11 @@ __global__ void __launch_bounds__(kTcxThreads, 1)
         } else if (x.flags & kTcDirect) {
           if (row < x.valid_rows) {
             double* out = sigma + x.out_base + (int64_t)row * x.out_ld;
-            for (int c = 0; c < x.valid_cols; ++c) out[c] = accs[c * kTcRowsA + row];
+            for (int c = cb0; c < min(x.valid_cols, ce); ++c) out[c] = accs[c * kTcRowsA + row];
           }
         } else if (row < x.h_a) {
           double* out = b.partials + x.out_base + (int64_t)row * x.h_b;
-          for (int c = 0; c < x.h_b; ++c) out[c] = accs[c * kTcRowsA + row];
+          for (int c = cb0; c < min(x.h_b, ce); ++c) out[c] = accs[c * kTcRowsA + row];
         }
       }
     }
