@@ -392,7 +392,8 @@ def run_ours(a):
         # autotuned knobs against the defaults
         sched = {"autotuned": not a.no_autotune,
                  "knobs": {k: info[k] for k in ("tc_item_cost", "tc_split", "tc_group", "tc_nb")},
-                 "launches_per_sigma": info["launches"], "ms_per_sigma": t_step * 1e3}
+                 "launches_per_sigma": info["launches"], "ms_per_sigma": t_step * 1e3,
+                 "stacks": {k: info[k] for k in ("tc_stacks", "tc_stacked_items", "tc_phase1_tasks")}}
         reps = 2
         ctx.set_autotune(False)
         ctx.set_tc_schedule(True)
@@ -405,6 +406,12 @@ def run_ours(a):
         info_d = ctx.superblock_info(sb)
         sched["default_knobs"] = {"ms_per_sigma": ms_d[0] / reps,
                                   "knobs": {k: info_d[k] for k in ("tc_item_cost", "tc_split", "tc_group", "tc_nb")}}
+        # stage-1 products of small blocks one tile each (no stacking)
+        ctx.set_tc_stacking(0)
+        ms_u = ctx.sigma_timed(sb, x, y, reps)
+        sched["unstacked"] = {"ms_per_sigma": ms_u[0] / reps,
+                              "phase1_tasks": ctx.superblock_info(sb)["tc_phase1_tasks"]}
+        ctx.set_tc_stacking(64)
         if not a.no_autotune:
             ctx.set_autotune(True)
             ctx.sigma_timed(sb, x, y, 1)  # cached knobs back on the plan

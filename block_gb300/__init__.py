@@ -67,6 +67,7 @@ _SIGS = {
     "bgpu_set_davidson_graph": (_I, [_P, _I]),
     "bgpu_set_tc_schedule": (_I, [_P, _I]),
     "bgpu_set_tc_tile_width": (_I, [_P, _I]),
+    "bgpu_set_tc_stacking": (_I, [_P, _I]),
     "bgpu_set_autotune": (_I, [_P, _I, _CP]),
     "bgpu_autotune_stats": (_I, [_P, _I64P, _I64P, _DP]),
     "bgpu_davidson_graph_launches": (_I, [_P, _I64P]),
@@ -385,7 +386,8 @@ class Context:
     INFO_KEYS = ("flops", "bytes", "tc_mma_flops", "tc_phase1_tasks", "tc_phase2_tasks", "tc_phase2_items",
                  "tc_phase2_stage1_items", "tc_split_tiles", "tc_pool_L", "tc_pool_R", "tc_pool_psi",
                  "tc_pool_S", "fp64_stage1_units", "fp64_items", "tc_item_cost", "tc_split", "tc_group",
-                 "tc_per_sector", "tc_tuned", "launches", "fp64_scratch", "tc_nb")
+                 "tc_per_sector", "tc_tuned", "launches", "fp64_scratch", "tc_nb", "tc_stacks",
+                 "tc_stacked_items")
 
     def tc_wait_selftest(self, limit_ms=20.0):
         """Bounded mbarrier wait on a barrier nothing arrives at: returns
@@ -414,6 +416,12 @@ class Context:
     def set_tc_tile_width(self, nb=0):
         """Output-tile width of the tensor-core sigma: 64, 128 or 0 (automatic)."""
         self._check(self.lib.bgpu_set_tc_tile_width(self.h, int(nb)))
+
+    def set_tc_stacking(self, rows=64):
+        """Stack the stage-1 products of operator blocks of at most `rows`
+        rows (multiple of 8, up to 128) that share a psi block into one
+        128-row tensor-core tile; 0 turns stacking off."""
+        self._check(self.lib.bgpu_set_tc_stacking(self.h, int(rows)))
 
     def set_autotune(self, on=True, cache_path=None):
         """Autotuner of the persistent tensor-core schedule, keyed on the

@@ -164,6 +164,14 @@ int bgpu_set_tc_tile_width(bgpu_ctx* ctx, int nb) {
   });
 }
 
+int bgpu_set_tc_stacking(bgpu_ctx* ctx, int rows) {
+  return guarded(ctx, [&] {
+    need(ctx->eng != nullptr, "no device");
+    need(rows >= 0 && rows <= dev::kTcRowsA && rows % 8 == 0, "stacking limit must be 0 or a multiple of 8 up to 128");
+    ctx->eng->tc_stack_rows = rows;
+  });
+}
+
 int bgpu_set_autotune(bgpu_ctx* ctx, int on, const char* cache_path) {
   return guarded(ctx, [&] {
     need(ctx->eng != nullptr, "no device");
@@ -466,7 +474,7 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
     auto& r = *it->second;
     if (!r.plan.tc) ctx->eng->plan_tc(r.sb, r.plan);
     const SigmaPlan& p = r.plan;
-    const double v[22] = {p.flops,
+    const double v[24] = {p.flops,
                           p.bytes,
                           p.tc_mma_flops,
                           (double)p.tc_stats[0],
@@ -487,8 +495,10 @@ int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n) {
                           p.tc_tuned ? 1.0 : 0.0,
                           (double)ctx->eng->sigma_launches(p),
                           (double)p.scratch_elems,
-                          (double)p.tc_nb};
-    for (int i = 0; i < n; ++i) info[i] = i < 22 ? v[i] : 0.0;
+                          (double)p.tc_nb,
+                          (double)p.tc_stacks,
+                          (double)p.tc_stacked_items};
+    for (int i = 0; i < n; ++i) info[i] = i < 24 ? v[i] : 0.0;
   });
 }
 

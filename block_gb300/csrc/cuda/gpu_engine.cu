@@ -880,6 +880,8 @@ void GpuEngine::free_tc(SigmaPlan& p) {
   p.tc_r2.release(stream_);
   p.tc_tiles.release(stream_);
   p.tc_slots.release(stream_);
+  p.tc_rows.release(stream_);
+  p.tc_stacks = p.tc_stacked_items = 0;
   if (p.tc_partials) cudaFreeAsync(p.tc_partials, stream_);
   p.tc_partials = nullptr;
   p.tc_partial_cap = 0;
@@ -1383,6 +1385,117 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
       std::stable_partition(v.begin(), v.end(), [](const TcItem& it) { return it.alpha == 1.0f; });
   }
   laps.lap("alpha folding");
+  // Stacks: phase-1 products of small operator blocks (at most tc_stack_rows
+  // rows) that read the same psi^T block (same B operand, same K) share one
+  // 128-row A tile.  Each member is packed again at its row offset of a
+  // stacked operand in pool L, and the phase-1 epilogue sends every row of
+  // the stacked tile, scaled by its member's alpha, to that member's
+  // stage-1 operand (TcRow).  Every row is the same dot product as in the
+  // unstacked tile; a stack takes one pass through the pipeline instead of
+  // one per member.
+  std::vector<TcRow> rows_tab;
+  int64_t n_stacks = 0, n_stacked = 0;
+  if (!plan.tcx && tc_stack_rows > 0) {
+    std::unordered_map<int64_t, int> lpack;  // pool-L offset -> its pack unit
+    for (size_t i = 0; i < ops_packs.size(); ++i)
+      if (ops_packs[i].pool == kTcPoolL) lpack.emplace(ops_packs[i].dst_off, (int)i);
+    const size_t ni = i1.size();
+    std::vector<std::vector<int>> tasks_of(ni);
+    for (size_t k = 0; k < t1.size(); ++k) tasks_of[t1[k].ibeg].push_back((int)k);
+    auto task_mma = [&](const TcTask& t) {
+      return 3.0 * 2.0 * 128 * tc_round16(std::min(nb, t.b_rows - nb * t.tn)) * i1[t.ibeg].kp;
+    };
+    // candidates grouped by (psi^T block, K), each group in item order
+    std::map<std::pair<int64_t, int>, std::vector<int>> groups;
+    for (size_t u = 0; u < ni; ++u) {
+      if (tasks_of[u].empty() || i1[u].a_pool != kTcPoolL) continue;
+      if (t1[tasks_of[u][0]].a_rows > std::min(tc_stack_rows, kTcRowsA)) continue;
+      groups[{i1[u].b_off, i1[u].kp}].push_back((int)u);
+    }
+    std::vector<char> drop(t1.size(), 0);
+    std::vector<TcTask> t_new;
+    std::vector<int> sec_new;
+    std::vector<int64_t> bun_new;
+    for (const auto& g : groups) {
+      const std::vector<int>& us = g.second;
+      size_t x = 0;
+      while (x < us.size()) {
+        size_t y = x;
+        int H = 0;
+        while (y < us.size() && H + t1[tasks_of[us[y]][0]].a_rows <= kTcRowsA) H += t1[tasks_of[us[y++]][0]].a_rows;
+        if (y - x < 2) {
+          x = y;
+          continue;
+        }
+        const int kp = i1[us[x]].kp;
+        const int64_t st_off = pool_n[kTcPoolL];
+        pool_n[kTcPoolL] += 2 * (int64_t)H * kp;
+        const int64_t base = (int64_t)rows_tab.size();
+        rows_tab.resize(base + kTcRowsA, TcRow{0, 0, 0, 0.f});
+        int r0 = 0;
+        for (size_t m = x; m < y; ++m) {
+          const int u = us[m];
+          const TcTask& T = t1[tasks_of[u][0]];
+          auto it = lpack.find(i1[u].a_off);
+          if (it == lpack.end() || i1[u].kp != kp || T.tm != 0) fail();
+          TcPack pk = ops_packs[it->second];
+          pk.dst_off = st_off;
+          pk.row0 = r0;
+          pk.dst_rows = H;
+          ops_packs.push_back(pk);
+          for (int lr = 0; lr < T.a_rows; ++lr)
+            rows_tab[base + r0 + lr] = TcRow{T.out_off, (int16_t)T.a_rows, (int16_t)lr, i1[u].alpha};
+          for (int k : tasks_of[u]) {
+            drop[k] = 1;
+            mma -= task_mma(t1[k]);
+          }
+          r0 += T.a_rows;
+        }
+        TcItem si = i1[us[x]];
+        si.a_off = st_off;
+        si.alpha = 1.0f;
+        si.alpha64 = 1.0;
+        const int idx = (int)i1.size();
+        i1.push_back(si);
+        for (int k : tasks_of[us[x]]) {
+          TcTask t = t1[k];
+          t.a_rows = H;
+          t.ibeg = idx;
+          t.iend = idx + 1;
+          t.out_off = base;
+          t.stacked = 1;
+          t_new.push_back(t);
+          sec_new.push_back(sec1[k]);
+          bun_new.push_back(((int64_t)1 << 50) + (n_stacks << 8));
+          mma += task_mma(t);
+        }
+        ++n_stacks;
+        n_stacked += (int64_t)(y - x);
+        x = y;
+      }
+    }
+    if (n_stacks > 0) {
+      std::vector<TcTask> tk;
+      std::vector<int> sk;
+      std::vector<int64_t> bk;
+      for (size_t k = 0; k < t1.size(); ++k)
+        if (!drop[k]) {
+          tk.push_back(t1[k]);
+          sk.push_back(sec1[k]);
+          bk.push_back(bundle1[k]);
+        }
+      tk.insert(tk.end(), t_new.begin(), t_new.end());
+      sk.insert(sk.end(), sec_new.begin(), sec_new.end());
+      bk.insert(bk.end(), bun_new.begin(), bun_new.end());
+      t1 = std::move(tk);
+      sec1 = std::move(sk);
+      bundle1 = std::move(bk);
+    }
+  }
+  plan.tc_stacks = n_stacks;
+  plan.tc_stacked_items = n_stacked;
+  plan.tc_stack_used = tc_stack_rows;
+  laps.lap("stacks");
   // the item lists stay on the host, so that the device work lists can be
   // rebuilt for other schedule knobs (autotuner, per-sector baseline)
   auto host = std::make_shared<TcHostPlan>();
@@ -1414,6 +1527,7 @@ void GpuEngine::plan_tc(const Superblock& sb, SigmaPlan& plan) {
     plan.tc_pool_cap[i] = cap;
   }
   plan.tc_psi_pack.upload(psi_packs, stream_);
+  plan.tc_rows.upload(rows_tab, stream_);
   // operator blocks are packed once per plan
   DevArray<TcPack> dops;
   dops.upload(ops_packs, stream_);
@@ -1662,7 +1776,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
           base.out_base = T.out_off;
           base.out_ld = base.h_b;
         }
-        const uint8_t f0 = (uint8_t)(T.direct ? kTcDirect : 0);
+        const uint8_t f0 = (uint8_t)((T.direct ? kTcDirect : 0) | (phase == 1 && T.stacked ? kTcStacked : 0));
         if (T.ibeg == T.iend) {
           TcWork x = base;
           x.flags = (uint8_t)(f0 | kTcFirst | kTcLast | kTcEmpty);
@@ -1943,6 +2057,7 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
     free_tc(p);
     p.tc_nb_set = false;
   }
+  if (p.tc && p.tc_stack_used != tc_stack_rows) free_tc(p);  // stacked for another limit
   if (!p.tc) plan_tc(sb, p);
   if (p.tc_knobs.per_sector != (tc_schedule_mode == 1 ? 1 : 0)) {
     TcKnobs k = tc_default_knobs();
@@ -1958,6 +2073,7 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   for (int i = 0; i < dev::kTcPools; ++i) {
     b.pool[i] = p.tc_pool[i];
   }
+  b.rows = p.tc_rows.d;
   b.partials = p.tc_partials;
   b.status = tc_status_;
   b.fp16 = fp16 ? 1 : 0;

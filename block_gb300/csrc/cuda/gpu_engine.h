@@ -117,6 +117,9 @@ struct SigmaPlan {
   DevArray<int2> tc_r1, tc_r2;         // per persistent block: its range of records
   DevArray<dev::TcTile> tc_tiles;
   DevArray<int64_t> tc_slots;
+  DevArray<dev::TcRow> tc_rows;  // row maps of the stacked phase-1 tiles (128 per stack)
+  int64_t tc_stacks = 0, tc_stacked_items = 0;  // stacks and the stage-1 products they replace
+  int tc_stack_used = 0;  // the engine's tc_stack_rows when the plan was built
   float2* tc_partials = nullptr;
   double tc_mma_flops = 0.0;  // tensor-core flops issued per product (3 bf16 products per logical one)
   // plan statistics: phase-1 tasks, phase-2 tasks, phase-2 items, phase-2
@@ -229,6 +232,10 @@ class GpuEngine : public Engine {
   // autotuner), else 64 or 128
   int tc_nb_mode = 0;
   int tc_choose_nb(const Superblock& sb) const;
+  // stage-1 products of operator blocks with at most this many rows that
+  // share their psi block are stacked into one 128-row tensor-core tile
+  // (0: no stacking)
+  int tc_stack_rows = 64;
   bool tc_autotune = false;
   std::map<std::string, TcKnobs> tune_cache;
   std::string tune_cache_path;  // file the cache is read from and appended to

@@ -197,11 +197,13 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(TcBufs b, const TcPack* __
         lw[e >> 1] = bl;
       }
     }
-    const int t = r / u.rt, c = k0 / kTcKC;
-    const int rest = u.rows_p - u.rt * t;
+    // row R of the destination operand (of H rows; a stack member starts at row0)
+    const int H = u.dst_rows > 0 ? u.dst_rows : u.rows_p, R = u.row0 + r;
+    const int t = R / u.rt, c = k0 / kTcKC;
+    const int rest = H - u.rt * t;
     const int h = rest < u.rt ? rest : u.rt;
     const int w = min(kTcKC, u.kp - kTcKC * c);
-    const int64_t off = 2 * tc_block_off(u.rows_p, u.kp, t, c, u.rt) + (kmajor_off(r - u.rt * t, k0 % kTcKC, h) >> 1);
+    const int64_t off = 2 * tc_block_off(H, u.kp, t, c, u.rt) + (kmajor_off(R - u.rt * t, k0 % kTcKC, h) >> 1);
     *(uint4*)(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *(uint4*)(dst + off + (int64_t)h * w) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
@@ -460,6 +462,17 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
         if (flags & kTcFirst) first = true;
         const bool have = (flags & kTcGEnd) && !(flags & kTcEmpty);
         const bool last = (flags & kTcLast) != 0;
+        // phase 1: the stage-1 operand, row and scale this thread's row goes to
+        int64_t s_base = out_base;
+        int s_h = h_a, s_row = row;
+        float s_alpha = alpha;
+        if (PHASE == 1 && (flags & kTcStacked) && have && row < h_a) {
+          const int4 e = __ldg(reinterpret_cast<const int4*>(b.rows + out_base + row));
+          s_base = (int64_t)(((uint64_t)(uint32_t)e.y << 32) | (uint32_t)e.x);
+          s_h = e.z & 0xffff;
+          s_row = (e.z >> 16) & 0xffff;
+          s_alpha = __int_as_float(e.w);
+        }
         if (have) {
           ok = __all_sync(0xffffffffu, tc_wait(&sh.acc_full[ab], aph, abort_flag, b.status, limit_ns));
           if (!ok) break;  // TMEM loads below need the whole warp
@@ -533,11 +546,11 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
                 }
               }
             }
-          } else if (have && row < h_a) {
+          } else if (have && row < h_a && s_h > 0) {
             // phase 1: S tile written as a packed operand (rows of this tile,
-            // K columns col0.. of S)
+            // K columns col0.. of S; row s_row of an s_h-row operand)
             const int ncols = min(NB, out_ld - col0);
-            __nv_bfloat16* sp = b.pool[kTcPoolS] + out_base;
+            __nv_bfloat16* sp = b.pool[kTcPoolS] + s_base;
 #pragma unroll
             for (int g8 = 0; g8 < 8; ++g8) {
               const int c0 = 64 * hh + 8 * g8;
@@ -545,7 +558,7 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
                 uint32_t hw4[4], lw4[4];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
-                  const float x = (c0 + e) < h_b ? __fmul_rn(alpha, v[8 * g8 + e]) : 0.f;
+                  const float x = (c0 + e) < h_b ? __fmul_rn(s_alpha, v[8 * g8 + e]) : 0.f;
                   uint32_t bh, bl;
                   split16(x, b.fp16 != 0, bh, bl);
                   if (e & 1) {
@@ -558,9 +571,9 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
                 }
                 const int C = col0 + c0;  // S column
                 const int cc = C / kTcKC, wc = min(kTcKC, out_ld - kTcKC * cc);
-                const int64_t off = 2 * (int64_t)h_a * kTcKC * cc + (kmajor_off(row, C % kTcKC, h_a) >> 1);
+                const int64_t off = 2 * (int64_t)s_h * kTcKC * cc + (kmajor_off(s_row, C % kTcKC, s_h) >> 1);
                 *(uint4*)(sp + off) = make_uint4(hw4[0], hw4[1], hw4[2], hw4[3]);
-                *(uint4*)(sp + off + (int64_t)h_a * wc) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
+                *(uint4*)(sp + off + (int64_t)s_h * wc) = make_uint4(lw4[0], lw4[1], lw4[2], lw4[3]);
               }
             }
           }

@@ -150,6 +150,15 @@ int bgpu_set_tc_schedule(bgpu_ctx* ctx, int mode);
  * least 128 columns wide, or lets the autotuner choose.  Applies to the next
  * product of every superblock (its operands are packed again). */
 int bgpu_set_tc_tile_width(bgpu_ctx* ctx, int nb);
+/* Stacking of small stage-1 products in the tensor-core sigma (no reference
+ * counterpart; the reference multiplies every operator block separately,
+ * operatorfunctions.C:515): the products of operator blocks of at most
+ * `rows` rows (0, or a multiple of 8 up to 128; default 64) that read the
+ * same psi block are stacked into one 128-row MMA tile, each row sent to its
+ * own stage-1 operand.  0 multiplies every block separately.  Results are the
+ * same dot products either way.  Applies to the next product of every
+ * superblock (its operators are packed again). */
+int bgpu_set_tc_stacking(bgpu_ctx* ctx, int rows);
 /* Autotuner of the persistent tensor-core schedule (no reference
  * counterpart): on = 1 times candidate tile widths (64, 128 columns) and,
  * for each, candidate knobs (cost model of the block assignment, splitting
@@ -256,8 +265,9 @@ int bgpu_tc_wait_selftest(bgpu_ctx* ctx, double limit_ms, int* gave_up, int* sta
  *   split, group, per-sector flag, 1 when chosen by the autotuner), the
  *   launches of one sigma at the current precision and the doubles of
  *   stage-1 intermediates the FP64 product needs (compare with
- *   BGPU_NOALLOC_SCRATCH_DOUBLES) and the output-tile width of the
- *   tensor-core plan.  Builds the tensor-core plan if needed. */
+ *   BGPU_NOALLOC_SCRATCH_DOUBLES), the output-tile width of the
+ *   tensor-core plan, its stacked phase-1 tiles and the stage-1 products
+ *   they hold.  Builds the tensor-core plan if needed. */
 int bgpu_superblock_info(bgpu_ctx* ctx, int sb, double* info, int n);
 /* Kernel launches of one sigma product. */
 int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);

@@ -6,7 +6,9 @@ for one sweep; syn30_m1000, syn30 at M=1000, the profiling size of the
 bench's kernels; syn40_m1000, syn40 at M=1000): seeded synthetic
 Cholesky Hamiltonians generated inside the library from the `orbitals
 synthetic:<norb>:<nelec>:<nchol>:<seed>:<d2h>` spec; syn8 / syn8_d2h are
-small members of the same family used for FCI cross-checks.  syn16_m200
+small members of the same family used for FCI cross-checks; syn20_d2h (20
+orbitals, D2h irreps, M=300) is a small batching case of many uneven
+sectors.  syn16_m200
 (16 orbitals, M=200, 4 sweeps) and syn24_m250_s2 (two sweeps of the
 24-orbital system at M=250) truncate heavily: the split-precision sweeps are
 compared with the FP64 ones sweep by sweep on them, with Davidson converged
@@ -45,6 +47,7 @@ CONFS = {
     "syn30_sweep1": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 2000 1e-8 0\nend\nmaxiter 1\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_m1000": ("synthetic:30:30:60:30:0", "nelec 30\nspin 0\nschedule\n0 1000 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
     "syn30_d2h": ("synthetic:30:30:60:30:1", "nelec 30\nspin 0\nschedule\n0 1500 1e-8 0\nend\nmaxiter 4\nsweep_tol 1e-12\nnoreorder\n"),
+    "syn20_d2h": ("synthetic:20:20:40:20:1", "nelec 20\nspin 0\nschedule\n0 300 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
     "syn40_m1000": ("synthetic:40:40:80:40:0", "nelec 40\nspin 0\nnroots 3\nweights 0.333333333333 0.333333333333 0.333333333334\nschedule\n0 1000 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
     "syn40": ("synthetic:40:40:80:40:0", "nelec 40\nspin 0\nnroots 3\nweights 0.333333333333 0.333333333333 0.333333333334\nschedule\n0 4000 1e-8 0\nend\nmaxiter 2\nsweep_tol 1e-12\nnoreorder\n"),
 }
