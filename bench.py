@@ -19,7 +19,11 @@ parity against the oracle on the 24-orbital M=500 superblock, and whole
 sweeps: the 12-site Hubbard chain in FP64, split precision and on the CPU
 oracle, and one sweep of the 30-orbital M=2000 system in split precision
 (its FP64 sweep time derived from the per-step FP64 product times unless
---sweep-fp64 runs it).
+--sweep-fp64 runs it).  `batching` repeats the sigma measurement, with its
+schedule comparisons, on the batching case: the middle bond of the
+30-orbital Hamiltonian with D2h irreps at M=1500 (many small uneven
+sectors), persistent launches with stacked stage-1 products against the
+unstacked plan and the per-sector-launch baseline.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
                   [--precision fp64|bf16x3|bf16x6|bf16x3tc|fp16x2tc] [--conf PATH --partition P]
@@ -50,6 +54,8 @@ PARITY_CONF, PARITY_PARTITION = os.path.join(GOLDEN, "syn24", "dmrg.conf"), 11
 SWEEP_CONF = os.path.join(GOLDEN, "hubbard12", "dmrg.conf")
 # 30 orbitals, M=2000: warm-up and one sweep
 BIG_SWEEP_CONF = os.path.join(GOLDEN, "syn30_sweep1", "dmrg.conf")
+# 30 orbitals with D2h irreps, M=1500: the batching case (many small sectors)
+BATCH_CONF, BATCH_PARTITION = os.path.join(GOLDEN, "syn30_d2h", "dmrg.conf"), 14
 METRIC = "sigma TFLOP/s & sweep time: split-prec batched vs FP64 GPU at |dE|<=1e-6 Eh"
 
 
@@ -85,6 +91,8 @@ def parse():
     ap.add_argument("--no-exact", action="store_true", help="skip the exact-slice tensor-core product")
     ap.add_argument("--profile", action="store_true",
                     help="open the CUDA profiler range around the device-timed steps only")
+    ap.add_argument("--no-batching", action="store_true",
+                    help="skip the batching case (D2h superblock, schedule comparisons)")
     return ap.parse_args()
 
 
@@ -576,11 +584,37 @@ def run_ours(a):
     ctx.device_free(x)
     ctx.device_free(y)
     ctx.close()
+    if tc_path and world == 1 and not a.no_batching and not a.no_schedules and \
+            os.path.abspath(a.conf) == os.path.abspath(DEFAULT_CONF):
+        line["batching"] = run_batching(a)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def run_batching(a):
+    """The sigma measurement of this script on the batching superblock, in a
+    child process that gets the whole device (the headline superblock's
+    context is closed by then); returns its schedules and timings."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--conf", BATCH_CONF, "--partition", str(BATCH_PARTITION),
+           "--precision", a.precision, "--steps", "10", "--warmup", "3", "--no-cpu-baseline", "--no-parity",
+           "--no-davidson", "--no-sweeps", "--no-exact", "--big-sweep-conf", "none", "--no-batching"]
+    t0 = time.perf_counter()
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        rec = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    except Exception as e:  # the headline line stands without this entry
+        return {"conf": os.path.relpath(BATCH_CONF, ROOT), "error": repr(e)[:300]}
+    info = rec["roofline"].get("tc_plan", {})
+    return {"conf": os.path.relpath(BATCH_CONF, ROOT), "partition": BATCH_PARTITION,
+            "workload": rec["config"]["workload"], "psi_elems": rec["config"]["psi_elems"],
+            "sigma_flops_per_step": rec["sigma_flops_per_step"], "ms_per_sigma": rec["ms_per_step"],
+            "tflops": rec["value"], "e2e_tflops": rec["e2e"]["value"], "clocks": rec["clocks"],
+            "tc_mma_flops": info.get("tc_mma_flops"), "tc_mma_issued_frac": rec["roofline"].get("tc_mma_issued_frac"),
+            "schedules": rec.get("schedules"), "fp64_path": rec.get("fp64_path"),
+            "prepare_seconds": rec.get("prepare_seconds"), "seconds": time.perf_counter() - t0}
 
 
 def main():
