@@ -64,6 +64,7 @@ _SIGS = {
     "bgpu_superblock_info": (_I, [_P, _I, _DP, _I]),
     "bgpu_set_refine_window": (_I, [_P, ctypes.c_double]),
     "bgpu_set_guess": (_I, [_P, _I]),
+    "bgpu_set_spill": (_I, [_P, _I]),
     "bgpu_set_davidson_graph": (_I, [_P, _I]),
     "bgpu_set_tc_schedule": (_I, [_P, _I]),
     "bgpu_set_tc_tile_width": (_I, [_P, _I]),
@@ -403,6 +404,11 @@ class Context:
         (True) or unit vectors (False)."""
         self._check(self.lib.bgpu_set_guess(self.h, int(bool(transform))))
 
+    def set_spill(self, on=True):
+        """run_dmrg keeps the stored blocks that the current step does not
+        read in host memory only (True) or all blocks on the device (False)."""
+        self._check(self.lib.bgpu_set_spill(self.h, int(bool(on))))
+
     def set_davidson_graph(self, on=True):
         """Davidson iterations as launches of a captured CUDA graph (True) or
         as the same launches issued one by one (False)."""
@@ -513,12 +519,13 @@ class Context:
         self._check(self.lib.bgpu_sweep_energies(self.h, _dp(sw), len(sw), ctypes.byref(ns)))
         stats["sweep_energies"] = sw[:min(ns.value, len(sw))].copy()
         nsw = len(stats["sweep_energies"])
-        rs = np.zeros(14 + nsw)
+        rs = np.zeros(18 + nsw)
         self._check(self.lib.bgpu_run_stats(self.h, _dp(rs), len(rs)))
         stats.update(split_sigma_calls=int(rs[0]), split_sigma_seconds=rs[1], fp64_sigma_calls=int(rs[2]),
                      fp64_sigma_seconds=rs[3], defect_rounds=int(rs[4]), derived_fp64_sigma_seconds=rs[5],
                      warmup_seconds=rs[6], bounded_verifications=int(rs[7]), exact_sigma_calls=int(rs[8]),
                      exact_sigma_seconds=rs[9], sweep_renorm_flops=rs[10], fp64_rate=rs[11],
                      renorm_exact=bool(rs[12]), sweep_renorm_device_seconds=rs[13],
-                     sweep_seconds=rs[14:14 + nsw].copy())
+                     spill_fetches=int(rs[14]), spill_bytes_up=rs[15], spill_bytes_down=rs[16],
+                     peak_block_bytes=rs[17], sweep_seconds=rs[18:18 + nsw].copy())
         return e[:nroots].copy(), stats

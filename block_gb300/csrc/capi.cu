@@ -26,6 +26,7 @@ struct bgpu_ctx {
   std::vector<std::vector<double>> onepdm;  // of the last bgpu_run_dmrg with `onepdm`
   std::vector<std::vector<double>> tonepdm;  // per root pair (bra * nroots + ket)
   bool transform_guess = true;  // see bgpu_set_guess
+  bool spill = false;           // see bgpu_set_spill
   int deferred_steps = 4;        // see bgpu_set_refine_window
   struct BlockRec {
     Block b;
@@ -139,6 +140,10 @@ const char* bgpu_last_error_string(const bgpu_ctx* ctx) { return ctx ? ctx->err.
 
 int bgpu_set_guess(bgpu_ctx* ctx, int transform) {
   return guarded(ctx, [&] { ctx->transform_guess = transform != 0; });
+}
+
+int bgpu_set_spill(bgpu_ctx* ctx, int on) {
+  return guarded(ctx, [&] { ctx->spill = on != 0; });
 }
 
 int bgpu_set_davidson_graph(bgpu_ctx* ctx, int on) {
@@ -950,6 +955,7 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
       opt.deferred_steps = ctx->deferred_steps;
     }
     opt.transform_guess = ctx->transform_guess;
+    opt.spill = ctx->spill;
     const double s0 = ctx->eng->sigma_seconds, f0 = ctx->eng->sigma_flops, p0 = ctx->eng->plan_seconds;
     const double d0 = ctx->eng->renorm_device_seconds;
     const long c0 = ctx->eng->sigma_calls;
@@ -971,7 +977,8 @@ int bgpu_run_dmrg(bgpu_ctx* ctx, const char* conf_path, int verbose, double* ene
                       E.fp64_seconds - fs0, (double)(E.defect_rounds_ - dr0), E.derived_fp64_sigma_seconds - dv0,
                       r.warmup_seconds, (double)(E.defect_bounded_ - db0), (double)(E.exact_calls - xc0),
                       E.exact_seconds - xs0, r.sweep_renorm_flops, E.fp64_rate_, (double)E.renorm_exact(),
-                      r.sweep_renorm_device_seconds};
+                      r.sweep_renorm_device_seconds, (double)r.spill_fetches, r.spill_bytes_up,
+                      r.spill_bytes_down, r.peak_block_bytes};
     for (double t : r.sweep_seconds) ctx->run_stats.push_back(t);
     for (int i = 0; i < max_roots && i < (int)r.energies.size(); ++i) energies[i] = r.energies[i];
     if (stats) {

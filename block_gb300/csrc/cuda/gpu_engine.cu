@@ -217,6 +217,7 @@ void GpuEngine::create_block(Block& b) {
   d.n = b.ops.arena;
   d.d = alloc(d.n);
   d.dot = b.is_dot;
+  block_bytes_ += 8 * d.n;
   cuda_check(cudaMemsetAsync(d.d, 0, (size_t)std::max<int64_t>(d.n, 1) * sizeof(double), stream_), "memset");
 }
 
@@ -230,6 +231,7 @@ void GpuEngine::release_block(Block& b) {
   auto it = blocks_.find(b.handle);
   if (it != blocks_.end()) {
     free(it->second.d);
+    block_bytes_ -= 8 * it->second.n;
     blocks_.erase(it);
   }
   auto rr = block_rot_.find(b.handle);

@@ -170,6 +170,7 @@ class GpuEngine : public Engine {
   void set_rotation_record(const Block& b, const RotationRecord& r) override;
   // (synchronises, so that every renormalisation issued so far is counted)
   double renorm_flops() const override { return renorm_flops_; }
+  int64_t block_bytes() const override { return block_bytes_; }
   double device_renorm_seconds() override {
     sync();
     return renorm_device_seconds;
@@ -334,6 +335,7 @@ class GpuEngine : public Engine {
   };
   std::map<int, DevBlock> blocks_;
   int next_handle_ = 0;
+  int64_t block_bytes_ = 0;  // bytes of the operator arenas held (blocks_)
   // current superblock plan (solve)
   SigmaPlan plan_;
   bool have_plan_ = false;

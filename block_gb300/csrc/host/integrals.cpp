@@ -334,6 +334,7 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
     else if (key == "deflation_min_size") { need(1); c.deflation_min = std::stoi(tok[1]); }
     else if (key == "warmup") { if (tok.size() > 1) c.warmup = lower(tok[1]); }
     else if (key == "restart" || key == "fullrestart") c.restart = true;
+    else if (key == "spill") c.spill = true;
     else if (key == "onepdm" || key == "onerdm" || key == "ordm") c.onepdm = true;
     else if (key == "tran_onepdm") c.onepdm = c.tran_onepdm = true;
     else if (key == "prefix" || key == "scratch") {

@@ -85,6 +85,10 @@ struct Config {
   // `reset_iter` then starts the schedule from its first entry again
   std::string checkpoint;
   bool restart = false, reset_iter = false;
+  // `spill`: stored blocks that the current block step does not read stay in
+  // host memory, copied back to the device when a step needs them (the
+  // reference keeps blocks on disk between steps, save_load_block.C:58-110)
+  bool spill = false;
   // `onepdm` (or onerdm, ordm): after the sweeps, one more sweep evaluates
   // the spin-summed spatial one-particle density matrix of every root;
   // `prefix <dir>`: where spatial_onepdm.<r>.<r>.txt files are written

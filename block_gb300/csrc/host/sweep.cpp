@@ -17,6 +17,7 @@ SweepDriver::SweepDriver(const Integrals& I, const Config& c, Engine& e, DriverO
     : I_(I), C_(c), E_(e), opt_(std::move(opt)) {
   g_ = PointGroup::from_name(C_.sym);
   N_ = I_.norb;
+  spill_ = C_.spill || opt_.spill;
   const int nelec = C_.nelec >= 0 ? C_.nelec : I_.nelec;
   filter_.nelec = nelec;
   filter_.s2 = C_.spin;
@@ -53,7 +54,46 @@ Block SweepDriver::make_dot_block(int x) {
   b.is_dot = true;
   E_.create_block(b);
   E_.upload_block(b, d.data);
+  note_peak();
   return b;
+}
+
+void SweepDriver::note_peak() { peak_bytes_ = std::max(peak_bytes_, (double)E_.block_bytes()); }
+
+void SweepDriver::resident(Block* b) {
+  if (!b || b->handle >= 0) return;
+  auto it = host_.find(b);
+  if (it == host_.end()) throw std::runtime_error("stored block has neither engine storage nor a host copy");
+  E_.create_block(*b);
+  E_.upload_block(*b, it->second.arena);
+  if (it->second.has_rot) E_.set_rotation_record(*b, it->second.rot);
+  ++spill_fetches_;
+  spill_up_ += 8.0 * (double)it->second.arena.size();
+  note_peak();
+}
+
+void SweepDriver::spill_idle(const Block* keep1, const Block* keep2) {
+  if (!spill_) return;
+  for (auto* v : {&left_, &right_})
+    for (auto& up : *v) {
+      Block* b = up.get();
+      if (!b || b->handle < 0 || b == keep1 || b == keep2) continue;
+      if (host_.find(b) == host_.end()) {
+        HostCopy hc;
+        E_.download_block(*b, hc.arena);
+        hc.has_rot = E_.get_rotation_record(*b, hc.rot);
+        spill_down_ += 8.0 * (double)hc.arena.size();
+        host_.emplace(b, std::move(hc));
+      }
+      E_.release_block(*b);
+    }
+}
+
+void SweepDriver::drop(std::unique_ptr<Block>& slot) {
+  if (!slot) return;
+  if (slot->handle >= 0) E_.release_block(*slot);
+  host_.erase(slot.get());
+  slot.reset();
 }
 
 bool SweepDriver::loop_is_left(int p) const { return (p + 1) <= (N_ - 1 - p); }
@@ -116,6 +156,7 @@ Block SweepDriver::make_enlarged(const Block& sys, int x, bool dot_on_right, con
         throw std::runtime_error("build of " + r.first.str() + " needs " + t.b.key.str() + " on right sub-block");
     }
   E_.create_block(big);
+  note_peak();
   E_.build_block(big, a, b, recipes);
   return big;
 }
@@ -152,12 +193,14 @@ Superblock SweepDriver::make_superblock(const Block& L, const Block& R) const {
 Block& SweepDriver::left_block(int last) {
   if (last == 0) return *dots_[0];
   if (!left_[last]) throw std::runtime_error("left block missing");
+  resident(left_[last].get());
   return *left_[last];
 }
 
 Block& SweepDriver::right_block(int first) {
   if (first == N_ - 1) return *dots_[N_ - 1];
   if (!right_[first]) throw std::runtime_error("right block missing");
+  resident(right_[first].get());
   return *right_[first];
 }
 
@@ -245,6 +288,7 @@ std::unique_ptr<Block> SweepDriver::renormalised(const Block& big, const std::ve
   for (const auto& kv : nb->ops.ops)
     if (!big.ops.has(kv.first)) throw std::runtime_error("renormalised block needs " + kv.first.str());
   E_.create_block(*nb);
+  note_peak();
   E_.renormalise(*nb, big);
   return nb;
 }
@@ -271,7 +315,14 @@ void SweepDriver::save_checkpoint(const std::string& path, int sweeps_done, bool
   for (int side = 0; side < 2; ++side)
     for (int p = 0; p < N_; ++p) {
       const Block* b = side == 0 ? left_[p].get() : right_[p].get();
-      if (!b || b->handle < 0) continue;
+      if (!b) continue;
+      if (b->handle < 0) {  // spilled: its host copy
+        auto it = host_.find(b);
+        if (it == host_.end()) continue;
+        w.block(side, p, b->sites, b->si, b->ops, it->second.arena, it->second.has_rot ? &it->second.rot : nullptr);
+        ++nb;
+        continue;
+      }
       E_.download_block(*b, arena);  // one block at a time on the host
       RotationRecord rr;
       const bool has = E_.get_rotation_record(*b, rr);
@@ -299,12 +350,14 @@ int SweepDriver::load_checkpoint(const std::string& path, bool& next_forward, do
     b->ops = make_opset(b->si, std::set<OpKey>(cb.keys.begin(), cb.keys.end()), I_.orbsym, g_);
     if (b->ops.arena != (int64_t)cb.arena.size())
       throw std::runtime_error("checkpoint: operator catalogue does not match its stored arena");
+    auto& slot = cb.side == 0 ? left_[cb.index] : right_[cb.index];
+    drop(slot);
     E_.create_block(*b);
     E_.upload_block(*b, cb.arena);
     if (cb.has_rot) E_.set_rotation_record(*b, cb.rot);
-    auto& slot = cb.side == 0 ? left_[cb.index] : right_[cb.index];
-    if (slot) E_.release_block(*slot);
+    note_peak();
     slot = std::move(b);
+    spill_idle();
   }
   cur_M_ = h.cur_M;
   last_discarded_ = h.discarded;
@@ -327,8 +380,9 @@ void SweepDriver::warmup() {
     for (int i = p; i < N_; ++i) own.push_back(i);
     CatalogSpec spec = renorm_spec(own, p - 1, !loop_is_left(p - 2));
     Block big = make_enlarged(sys, p, /*dot_on_right=*/false, spec);
+    spill_idle();  // the stored blocks are not read again by this step
     std::vector<int> kept = warmup_rotation(big, M, C_.seed + 7919ull * (uint64_t)p);
-    if (right_[p]) E_.release_block(*right_[p]);
+    drop(right_[p]);
     right_[p] = renormalised(big, kept, spec);
     E_.release_block(big);
     log(2, "warmup right block [%d..%d]: %ld states\n", p, N_ - 1, right_[p]->si.total_states());
@@ -343,8 +397,9 @@ void SweepDriver::warmup_left(int upto) {
     for (int i = 0; i <= q; ++i) own.push_back(i);
     CatalogSpec spec = renorm_spec(own, q + 1, loop_is_left(q + 1));
     Block big = make_enlarged(sys, q, /*dot_on_right=*/true, spec);
+    spill_idle();
     std::vector<int> kept = warmup_rotation(big, M, C_.seed + 6271ull * (uint64_t)q);
-    if (left_[q]) E_.release_block(*left_[q]);
+    drop(left_[q]);
     left_[q] = renormalised(big, kept, spec);
     E_.release_block(big);
   }
@@ -426,6 +481,13 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   Block L = make_enlarged(left_block(p - 1), p, true, specL);
   Block R = make_enlarged(right_block(p + 2), p + 1, false, specR);
   Superblock sb = make_superblock(L, R);
+  // spill: the stored blocks go to host memory, except the two the guess
+  // transform reads (the step's own source on the side it renormalises, and
+  // the previous sweep's block it expands)
+  if (opt_.transform_guess)
+    spill_idle(forward ? left_[p - 1].get() : right_[p + 2].get(), forward ? right_[p + 1].get() : left_[p].get());
+  else
+    spill_idle();
   phase_.build_seconds += secs(t0);
   t0 = clk::now();
   E_.prepare_plan(sb);
@@ -445,8 +507,11 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
     g.rotated = forward ? left_[p - 1].get() : right_[p + 2].get();
     g.expanded = forward ? right_[p + 1].get() : left_[p].get();
     g.dot = forward ? &dots_[p]->si : &dots_[p + 1]->si;
+    resident(forward ? left_[p - 1].get() : right_[p + 2].get());
+    resident(forward ? right_[p + 1].get() : left_[p].get());
     if (g.rotated && g.expanded) dp.use_guess = E_.transform_guess(g, sb);
   }
+  spill_idle();
   const int iters = E_.solve(sb, dp, energies);
   char prec_tag[64] = "";
   int parked = -1;
@@ -514,10 +579,10 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   phase_.density_seconds += secs(t0);
   t0 = clk::now();
   if (forward) {
-    if (left_[p]) E_.release_block(*left_[p]);
+    drop(left_[p]);
     left_[p] = renormalised(L, kept, keepspec);
   } else {
-    if (right_[p + 1]) E_.release_block(*right_[p + 1]);
+    drop(right_[p + 1]);
     right_[p + 1] = renormalised(R, kept, keepspec);
   }
   phase_.renorm_seconds += secs(t0);
@@ -841,6 +906,10 @@ SweepResult SweepDriver::run() {
   res.density_seconds = phase_.density_seconds;
   res.renorm_seconds = phase_.renorm_seconds;
   res.renorm_device_seconds = E_.device_renorm_seconds();
+  res.spill_fetches = spill_fetches_;
+  res.spill_bytes_up = spill_up_;
+  res.spill_bytes_down = spill_down_;
+  res.peak_block_bytes = peak_bytes_;
   return res;
 }
 

@@ -181,6 +181,8 @@ class Engine {
   virtual void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) = 0;
   // small = rotation^T big rotation for every operator of small's catalogue
   virtual void renormalise(Block& small, const Block& big) = 0;
+  // bytes of block storage (operator arenas) the engine holds now
+  virtual int64_t block_bytes() const { return 0; }
   // matrix elements <psi_a| coef * [l x r]^0 |psi_b> of single pair terms
   // between the last solve's vectors (nr of them):
   // out[(a * nr + b) * terms.size() + t]
@@ -226,6 +228,11 @@ struct SweepResult {
   double renorm_device_seconds = -1.0;  // device time of the renormalisations (< 0: not measured)
   // the same, and their flops, during the sweeps only (warm-up excluded)
   double sweep_renorm_device_seconds = 0.0, sweep_renorm_flops = 0.0;
+  // stored blocks copied back to the engine from host memory (`spill`), the
+  // bytes copied each way, and the most block storage the engine held at
+  // any point of the run (Engine::block_bytes after every block it made)
+  long spill_fetches = 0;
+  double spill_bytes_up = 0.0, spill_bytes_down = 0.0, peak_block_bytes = 0.0;
 };
 
 struct DriverOptions {
@@ -242,6 +249,9 @@ struct DriverOptions {
   // transform the previous step's wavefunction into the next step's guess
   // (TRANSFORM guess); off: unit-vector guesses (BASIC guess) at every step
   bool transform_guess = false;
+  // stored blocks that the current step does not read are kept in host
+  // memory only (as the `spill` keyword)
+  bool spill = false;
   // optional hooks for tests: called after each superblock solve
   std::function<void(const Superblock&, int sweep, int step)> on_step;
 };
@@ -301,6 +311,23 @@ class SweepDriver {
   std::vector<std::unique_ptr<Block>> left_;   // left_[p] = [0..p]
   std::vector<std::unique_ptr<Block>> right_;  // right_[p] = [p..N-1]
   std::vector<std::unique_ptr<Block>> dots_;
+  // spill: host copies of the stored blocks, made once per block (blocks do
+  // not change after they are made); a block whose handle is -1 lives only
+  // here until resident() gives it engine storage again
+  struct HostCopy {
+    std::vector<double> arena;
+    RotationRecord rot;
+    bool has_rot = false;
+  };
+  std::map<const Block*, HostCopy> host_;
+  bool spill_ = false;
+  long spill_fetches_ = 0;
+  double spill_up_ = 0.0, spill_down_ = 0.0, peak_bytes_ = 0.0;
+  void resident(Block* b);       // engine storage for a stored block (from its host copy)
+  // every stored block but keep1 / keep2 to host memory (copied once)
+  void spill_idle(const Block* keep1 = nullptr, const Block* keep2 = nullptr);
+  void drop(std::unique_ptr<Block>& slot);  // releases a stored block and its host copy
+  void note_peak();
   int cur_M_ = 0;
   std::vector<double> last_energies_;
   double last_discarded_ = 0.0;

@@ -124,6 +124,14 @@ int bgpu_set_refine_window(bgpu_ctx* ctx, double eh);
  * transform = 0 unit vectors on the lowest diagonal elements (BASIC guess,
  * guess_wavefunction.C:258-273). */
 int bgpu_set_guess(bgpu_ctx* ctx, int transform);
+/* Block store of bgpu_run_dmrg (replaces the reference's block files,
+ * save_load_block.C:58-110): on = 1 keeps every stored block that the
+ * current block step does not read in host memory only (copied there once,
+ * copied back when a step needs it), so that the device holds the step's
+ * own blocks; 0 (default) keeps all blocks on the device.  The `spill`
+ * keyword of dmrg.conf does the same.  bgpu_run_stats reports the copies
+ * and the peak block storage. */
+int bgpu_set_spill(bgpu_ctx* ctx, int on);
 /* Davidson iterations (bgpu_davidson, bgpu_run_dmrg) as launches of a
  * captured CUDA graph: on = 1 (default, unless the environment sets
  * BGPU_DAVIDSON_GRAPH=0) captures one iteration (the sigma of the newest
@@ -474,7 +482,10 @@ int bgpu_transition_onepdm(bgpu_ctx* ctx, int bra, int ket, double* gamma, int n
  * renormalisations (warm-up excluded), the FP64 product rate measured in
  * this context (flops per second, 0 if none), whether the renormalisations
  * ran on the exact-slice kernels (1) or the FP64 pipe (0), their device
- * seconds during the sweeps, then the wall seconds of each sweep. */
+ * seconds during the sweeps, the blocks copied back from host memory
+ * (bgpu_set_spill), the bytes copied to the device and to the host for
+ * them, the most operator-arena bytes the device held at once, then the
+ * wall seconds of each sweep. */
 int bgpu_run_stats(bgpu_ctx* ctx, double* out, int n);
 /* Sweep energies (lowest root per sweep, Sweep::do_one's return value,
  * sweep.C:436-453) of the last bgpu_run_dmrg: *n = number of sweeps, up to

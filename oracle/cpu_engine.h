@@ -42,6 +42,11 @@ class CpuEngine : public Engine {
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
   void renormalise(Block& small, const Block& big) override;
   void expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) override;
+  int64_t block_bytes() const override {
+    int64_t n = 0;
+    for (const auto& kv : store_) n += 8 * (int64_t)kv.second.size();
+    return n;
+  }
 
   // pieces exposed for tests and the bench
   void sigma(const Superblock& sb, const double* psi, double* out);

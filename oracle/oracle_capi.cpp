@@ -148,6 +148,10 @@ int oracle_sweep_energies(double* out, int cap) {
   return (int)g_last_sweep_energies.size();
 }
 
+// A whole run of dmrg.conf on the CPU engine.  stats (12 entries, may be
+// null): sweeps, sigma products, their seconds, 0, wall seconds, discarded
+// weight, last sweep energy, roots, blocks copied back from host memory
+// (`spill`), bytes copied each way for them, peak bytes of block storage.
 int oracle_run(const char* conf, int threads, int verbose, double* energies, int max_roots, double* stats) {
   g_last_onepdm.clear();
   g_last_tonepdm.clear();
@@ -177,6 +181,10 @@ int oracle_run(const char* conf, int threads, int verbose, double* energies, int
       stats[5] = r.discarded;
       stats[6] = r.sweep_energies.empty() ? 0.0 : r.sweep_energies.back();
       stats[7] = (double)r.energies.size();
+      stats[8] = (double)r.spill_fetches;
+      stats[9] = r.spill_bytes_up;
+      stats[10] = r.spill_bytes_down;
+      stats[11] = r.peak_block_bytes;
     }
     return 0;
   } catch (const std::exception& e) {

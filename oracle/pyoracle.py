@@ -125,7 +125,7 @@ def disable_blas():
 def run(conf, threads=0, verbose=0, max_roots=32):
     L = lib()
     e = np.zeros(max_roots)
-    st = np.zeros(8)
+    st = np.zeros(12)
     rc = L.oracle_run(conf.encode(), threads, verbose, e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), max_roots,
                       st.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     if rc != 0:
@@ -136,7 +136,9 @@ def run(conf, threads=0, verbose=0, max_roots=32):
     sw = np.zeros(256)
     ns = L.oracle_sweep_energies(sw.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(sw))
     return e[:n].copy(), dict(sweeps=int(st[0]), sigma_calls=int(st[1]), sigma_seconds=st[2], seconds=st[4],
-                              discarded=st[5], last_sweep_energy=st[6], sweep_energies=sw[:min(ns, 256)].copy())
+                              discarded=st[5], last_sweep_energy=st[6], sweep_energies=sw[:min(ns, 256)].copy(),
+                              spill_fetches=int(st[8]), spill_bytes_up=st[9], spill_bytes_down=st[10],
+                              peak_block_bytes=st[11])
 
 
 def _ptr(a, t):
