@@ -142,6 +142,26 @@ int oracle_transition_onepdm(int bra, int ket, double* out, int norb) {
   return 0;
 }
 
+// Spin-coupling coefficients of the shared host code (2j arguments), for the
+// tests: kind 0 clebsch(j1 m1 j2 m2 j3 m3), 1 six_j(6), 2 nine_j(9),
+// 3 ninej (the normalised 9j of the coupling tables, 9), 4
+// transpose_scaling(l r k).  Returns 0 on success, 1 for an unknown kind, 2
+// when the function refused its arguments.
+int oracle_su2(int kind, const int* a, double* out) {
+  try {
+    switch (kind) {
+      case 0: *out = clebsch(a[0], a[1], a[2], a[3], a[4], a[5]); return 0;
+      case 1: *out = six_j(a[0], a[1], a[2], a[3], a[4], a[5]); return 0;
+      case 2: *out = nine_j(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]); return 0;
+      case 3: *out = ninej(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]); return 0;
+      case 4: *out = transpose_scaling(a[0], a[1], a[2]); return 0;
+      default: return 1;
+    }
+  } catch (const std::exception&) {
+    return 2;
+  }
+}
+
 // the per-sweep energies of the last oracle_run (returns how many; copies up to cap)
 int oracle_sweep_energies(double* out, int cap) {
   for (int i = 0; i < cap && i < (int)g_last_sweep_energies.size(); ++i) out[i] = g_last_sweep_energies[i];

@@ -141,6 +141,22 @@ def run(conf, threads=0, verbose=0, max_roots=32):
                               peak_block_bytes=st[11])
 
 
+def su2(kind, *args):
+    """Spin-coupling coefficient of the shared host code (2j arguments):
+    kind "clebsch" (j1 m1 j2 m2 j3 m3), "six_j", "nine_j", "ninej" (the
+    normalised 9j of the coupling tables) or "transpose_scaling" (l r k)."""
+    kinds = {"clebsch": 0, "six_j": 1, "nine_j": 2, "ninej": 3, "transpose_scaling": 4}
+    L = lib()
+    L.oracle_su2.restype = ctypes.c_int
+    L.oracle_su2.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    a = (ctypes.c_int * 9)(*args)
+    out = ctypes.c_double()
+    rc = L.oracle_su2(kinds[kind], a, ctypes.byref(out))
+    if rc:
+        raise ValueError("%s%r refused (%d)" % (kind, args, rc))
+    return out.value
+
+
 def _ptr(a, t):
     return a.ctypes.data_as(ctypes.POINTER(t))
 
