@@ -163,6 +163,7 @@ void CpuEngine::fill_random(Block& b, uint64_t seed) {
 
 void CpuEngine::release_block(Block& b) {
   store_.erase(b.handle);
+  block_rot_.erase(b.handle);
   b.handle = -1;
 }
 
@@ -369,9 +370,14 @@ int CpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
                     [&](int64_t a, int64_t b) { return diag[a] < diag[b]; });
   Rng rng(p.seed);
   std::vector<std::vector<double>> b(nroots, std::vector<double>(n, 0.0)), sigma;
-  for (int r = 0; r < nroots; ++r) {
-    for (int64_t i = 0; i < n; ++i) b[r][i] = 1e-3 * (rng.uniform() - 0.5);
-    b[r][order[r]] = 1.0;
+  if (p.use_guess && (int)guess_.size() >= nroots && (int64_t)guess_[0].size() == n) {
+    // transformed previous wavefunctions (orthonormalised below)
+    for (int r = 0; r < nroots; ++r) b[r] = guess_[r];
+  } else {
+    for (int r = 0; r < nroots; ++r) {
+      for (int64_t i = 0; i < n; ++i) b[r][i] = 1e-3 * (rng.uniform() - 0.5);
+      b[r][order[r]] = 1.0;
+    }
   }
   for (int i = 0; i < nroots; ++i) {
     for (int j = 0; j < i; ++j) axpy(-dot(b[j], b[i]), b[j], b[i]);
@@ -672,6 +678,190 @@ void CpuEngine::renormalise(Block& small, const Block& big) {
       dgemm(true, false, mb, mk, bb.rows, 1.0, rot_[b].data(), mb, tmp.data(), mk, 0.0, dst, sbk.cols);
     }
   }
+  // keep the rotation with the block (guess transform of later steps)
+  Rot rec;
+  const int nq = (int)rot_kept_.size();
+  rec.m = rot_kept_;
+  rec.n.assign(nq, 0);
+  rec.small_of_big.assign(nq, -1);
+  rec.u.resize(nq);
+  for (int q = 0; q < nq; ++q) {
+    const int m = rot_kept_[q];
+    rec.n[q] = m > 0 ? (int)(rot_[q].size() / m) : (q < big.si.size() ? big.si.states[q] : 0);
+    if (m > 0) {
+      rec.small_of_big[q] = (int)rec.big_of_small.size();
+      rec.big_of_small.push_back(q);
+      rec.u[q] = rot_[q];
+    }
+  }
+  if (nq == big.si.size() && (int)rec.big_of_small.size() == small.si.size())
+    block_rot_[small.handle] = std::move(rec);
+}
+
+bool CpuEngine::get_rotation_record(const Block& b, RotationRecord& r) {
+  auto it = block_rot_.find(b.handle);
+  if (it == block_rot_.end()) return false;
+  const Rot& x = it->second;
+  r.n = x.n;
+  r.m = x.m;
+  r.small_of_big = x.small_of_big;
+  r.big_of_small = x.big_of_small;
+  r.off.assign(x.n.size(), 0);
+  r.data.clear();
+  for (size_t q = 0; q < x.n.size(); ++q) {
+    r.off[q] = (int64_t)r.data.size();
+    r.data.insert(r.data.end(), x.u[q].begin(), x.u[q].end());
+  }
+  if (r.data.empty()) r.data.push_back(0.0);
+  return true;
+}
+
+void CpuEngine::set_rotation_record(const Block& b, const RotationRecord& r) {
+  const size_t nq = r.off.size();
+  if (r.n.size() != nq || r.m.size() != nq || r.small_of_big.size() != nq)
+    throw std::runtime_error("rotation record: inconsistent sizes");
+  Rot x;
+  x.n = r.n;
+  x.m = r.m;
+  x.small_of_big = r.small_of_big;
+  x.big_of_small = r.big_of_small;
+  x.u.resize(nq);
+  for (size_t q = 0; q < nq; ++q) {
+    const int64_t sz = (int64_t)r.n[q] * r.m[q];
+    if (r.off[q] < 0 || r.off[q] + sz > (int64_t)r.data.size())
+      throw std::runtime_error("rotation record: sector outside its data");
+    if (r.m[q] > 0) x.u[q].assign(r.data.begin() + r.off[q], r.data.begin() + r.off[q] + sz);
+  }
+  block_rot_[b.handle] = std::move(x);
+}
+
+// The previous step's vectors in the next step's superblock (GuessWave::
+// transform_previous_wavefunction, guess_wavefunction.C:526-620, onto the
+// spin-adapted two-site blocks).  Forward (the dot moves right): the old
+// left big block is rotated to its kept states, phi = U^T psi per old
+// sector; each new sector (l, r) with l = (a, d) collects, for every old
+// right quantum J_R made of (d, b), the columns of phi(a, J_R) that belong
+// to (d, b), times the recoupling of (a d) l with (d b) J_R,
+//   W = (-1)^((j_a + j_d + j_b + J)/2) sqrt((2 j_l + 1)(2 j_R + 1))
+//       {j_a j_d j_l; j_b J j_R},
+// into chi (rows of l x kept states of b), and expands the right side with
+// the rotation V that made b: psi'(l, r) = chi V^T.  Backward is the mirror
+// image (psi V on the right, U chi on the left).
+bool CpuEngine::transform_guess(const GuessInput& g, const Superblock& sb) {
+  guess_.clear();
+  if (waves_.empty() || !g.rotated || !g.expanded || !g.dot) return false;
+  auto ri = block_rot_.find(g.rotated->handle);
+  auto ei = block_rot_.find(g.expanded->handle);
+  if (ri == block_rot_.end() || ei == block_rot_.end()) return false;
+  const Rot& rot = ri->second;
+  const Rot& exq = ei->second;
+  int64_t old_n = 0;
+  for (const auto& S : g.old_sectors) old_n = std::max<int64_t>(old_n, S.offset + (int64_t)S.rows * S.cols);
+  if (old_n != (int64_t)waves_[0].size()) return false;
+  const StateInfo& newL = sb.L->si;
+  const StateInfo& newR = sb.R->si;
+  const int J = sb.target.s2;
+  const StateInfo& rot_big = g.forward ? g.old_L : g.old_R;
+  const StateInfo& exp_big = g.forward ? newR : newL;
+  if ((int)rot.n.size() != rot_big.size() || (int)exq.n.size() != exp_big.size()) return false;
+  for (int q = 0; q < rot_big.size(); ++q)
+    if (rot.m[q] > 0 && rot.n[q] != rot_big.states[q]) return false;
+  for (int q = 0; q < exp_big.size(); ++q)
+    if (exq.m[q] > 0 && exq.n[q] != exp_big.states[q]) return false;
+  if (!g.forward && !(g.old_L.is_product() && newR.is_product())) return false;
+  if (g.forward && !(g.old_R.is_product() && newL.is_product())) return false;
+  auto W = [&](int ja, int jd, int jb, int jl, int jr) {
+    const int ph = (ja + jd + jb + J) / 2;
+    return ((ph & 1) ? -1.0 : 1.0) * std::sqrt((double)(jl + 1) * (jr + 1)) * six_j(ja, jd, jl, jb, J, jr);
+  };
+  const int nr = (int)waves_.size();
+  guess_.assign(nr, std::vector<double>(sb.size, 0.0));
+  for (int r = 0; r < nr; ++r) {
+    const std::vector<double>& psi = waves_[r];
+    std::map<std::pair<int, int>, std::pair<std::vector<double>, int>> phi;  // -> (block, its columns)
+    for (const auto& S : g.old_sectors) {
+      if (g.forward) {
+        const int a = rot.small_of_big[S.lq];
+        if (a < 0) continue;
+        const int m = rot.m[S.lq];
+        std::vector<double> P((size_t)m * S.cols);
+        dgemm(true, false, m, S.cols, S.rows, 1.0, rot.u[S.lq].data(), m, psi.data() + S.offset, S.cols, 0.0,
+              P.data(), S.cols);
+        phi[{a, S.rq}] = {std::move(P), S.cols};
+      } else {
+        const int b = rot.small_of_big[S.rq];
+        if (b < 0) continue;
+        const int m = rot.m[S.rq];
+        std::vector<double> P((size_t)S.rows * m);
+        dgemm(false, false, S.rows, m, S.cols, 1.0, psi.data() + S.offset, S.cols, rot.u[S.rq].data(), m, 0.0,
+              P.data(), m);
+        phi[{S.lq, b}] = {std::move(P), m};
+      }
+    }
+    for (const auto& S : sb.sectors) {
+      double* out = guess_[r].data() + S.offset;
+      if (g.forward) {
+        const int b = exq.small_of_big[S.rq];  // kept quantum of the expanded right block
+        if (b < 0) continue;
+        const int mb = exq.m[S.rq];
+        std::vector<double> chi((size_t)S.rows * mb, 0.0);
+        bool any = false;
+        for (const SectorPart& pt : newL.parts[S.lq]) {  // (a, d)
+          const int ja = g.old_L.quanta[rot.big_of_small[pt.lq]].s2;
+          const int jd = g.dot->quanta[pt.rq].s2;
+          const int jb = g.expanded->si.quanta[b].s2;
+          for (const auto& jp : g.old_R.parts_of(pt.rq, b)) {  // old right quantum made of (d, b)
+            auto f = phi.find({pt.lq, jp.first});
+            if (f == phi.end()) continue;
+            const double c = W(ja, jd, jb, newL.quanta[S.lq].s2, g.old_R.quanta[jp.first].s2);
+            if (c == 0.0) continue;
+            const std::vector<double>& P = f->second.first;
+            const int lds = f->second.second, c0 = g.old_R.parts[jp.first][jp.second].offset;
+            for (int i = 0; i < pt.size; ++i)
+              for (int j = 0; j < mb; ++j) chi[(size_t)(pt.offset + i) * mb + j] += c * P[(size_t)i * lds + c0 + j];
+            any = true;
+          }
+        }
+        if (any)
+          dgemm(false, true, S.rows, S.cols, mb, 1.0, chi.data(), mb, exq.u[S.rq].data(), mb, 0.0, out, S.cols);
+      } else {
+        const int a = exq.small_of_big[S.lq];  // kept quantum of the expanded left block
+        if (a < 0) continue;
+        const int ma = exq.m[S.lq];
+        std::vector<double> chi((size_t)ma * S.cols, 0.0);
+        bool any = false;
+        for (const SectorPart& pt : newR.parts[S.rq]) {  // (d, b)
+          const int ja = g.expanded->si.quanta[a].s2;
+          const int jd = g.dot->quanta[pt.lq].s2;
+          const int jb = g.old_R.quanta[rot.big_of_small[pt.rq]].s2;
+          for (const auto& jp : g.old_L.parts_of(a, pt.lq)) {  // old left quantum made of (a, d)
+            auto f = phi.find({jp.first, pt.rq});
+            if (f == phi.end()) continue;
+            const double c = W(ja, jd, jb, g.old_L.quanta[jp.first].s2, newR.quanta[S.rq].s2);
+            if (c == 0.0) continue;
+            const std::vector<double>& P = f->second.first;
+            const int lds = f->second.second, r0 = g.old_L.parts[jp.first][jp.second].offset;
+            for (int i = 0; i < ma; ++i)
+              for (int j = 0; j < pt.size; ++j)
+                chi[(size_t)i * S.cols + pt.offset + j] += c * P[(size_t)(r0 + i) * lds + j];
+            any = true;
+          }
+        }
+        if (any)
+          dgemm(false, false, S.rows, S.cols, ma, 1.0, exq.u[S.lq].data(), ma, chi.data(), S.cols, 0.0, out, S.cols);
+      }
+    }
+  }
+  // usable only if every root keeps a sizeable norm
+  for (const auto& v : guess_) {
+    double h = 0.0;
+    for (double x : v) h += x * x;
+    if (!std::isfinite(h) || h <= 1e-4) {
+      guess_.clear();
+      return false;
+    }
+  }
+  return true;
 }
 
 }  // namespace oracle

@@ -42,6 +42,12 @@ class CpuEngine : public Engine {
   void set_rotation(const std::vector<std::vector<double>>& rot, const std::vector<int>& kept) override;
   void renormalise(Block& small, const Block& big) override;
   void expectations(const Superblock& sb, const std::vector<PairTerm>& terms, std::vector<double>& out) override;
+  // TRANSFORM guess (guess_wavefunction.C:526-620): the last solve's vectors
+  // carried to the next step's superblock through the rotation kept with
+  // `rotated` and the one kept with `expanded`
+  bool transform_guess(const GuessInput& g, const Superblock& sb) override;
+  bool get_rotation_record(const Block& b, RotationRecord& r) override;
+  void set_rotation_record(const Block& b, const RotationRecord& r) override;
   int64_t block_bytes() const override {
     int64_t n = 0;
     for (const auto& kv : store_) n += 8 * (int64_t)kv.second.size();
@@ -78,6 +84,15 @@ class CpuEngine : public Engine {
                  const std::vector<Superblock::Sector>& out, int s2_out, std::vector<double>& phi);
   std::map<int, std::vector<double>> store_;
   int next_handle_ = 0;
+  // the rotation each renormalised block was made with, per big-block
+  // sector q: u[q] (n[q] x m[q], row-major, m[q] kept states), and the
+  // sector maps between the big and the renormalised block
+  struct Rot {
+    std::vector<int> n, m, small_of_big, big_of_small;
+    std::vector<std::vector<double>> u;
+  };
+  std::map<int, Rot> block_rot_;
+  std::vector<std::vector<double>> guess_;  // transformed vectors for the next solve
   std::vector<std::vector<double>> waves_;
   std::vector<std::vector<double>> dm_vecs_;  // eigenvectors per density-matrix sector (columns, ascending)
   std::vector<std::vector<double>> dm_rho_;   // the density matrix per sector

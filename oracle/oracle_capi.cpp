@@ -121,6 +121,14 @@ int oracle_use_blas(const char* path) {
 }
 
 static std::vector<double> g_last_sweep_energies;  // per sweep, lowest root, of the last oracle_run
+static bool g_guess = false;  // oracle_run's Davidson starts from transformed guesses
+
+// Davidson start of the next oracle_run steps: transformed previous
+// wavefunctions (on = 1, the TRANSFORM guess) or unit vectors (0, default).
+int oracle_set_guess(int on) {
+  g_guess = on != 0;
+  return 0;
+}
 static std::vector<std::vector<double>> g_last_onepdm;  // per root, of the last oracle_run with onepdm
 static std::vector<std::vector<double>> g_last_tonepdm;  // per root pair (bra * nroots + ket)
 
@@ -183,6 +191,7 @@ int oracle_run(const char* conf, int threads, int verbose, double* energies, int
     oracle::CpuEngine eng(threads);
     DriverOptions opt;
     opt.verbose = verbose;
+    opt.transform_guess = g_guess;
     SweepResult r;
     {
       SweepDriver drv(I, c, eng, opt);

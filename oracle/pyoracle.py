@@ -122,8 +122,13 @@ def disable_blas():
     _blas = None
 
 
-def run(conf, threads=0, verbose=0, max_roots=32):
+def run(conf, threads=0, verbose=0, max_roots=32, guess=False):
+    """A whole run of dmrg.conf on the oracle; guess=True starts every
+    Davidson solve it can from the transformed previous wavefunction."""
     L = lib()
+    L.oracle_set_guess.restype = ctypes.c_int
+    L.oracle_set_guess.argtypes = [ctypes.c_int]
+    L.oracle_set_guess(int(bool(guess)))
     e = np.zeros(max_roots)
     st = np.zeros(12)
     rc = L.oracle_run(conf.encode(), threads, verbose, e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), max_roots,
