@@ -531,11 +531,15 @@ def run_ours(a):
             po = oracle()
             po.enable_blas()
             t0 = time.perf_counter()
-            e, st = po.run(a.sweep_conf)
+            # transformed guesses, as the GPU sweeps (the reference's default)
+            e, st = po.run(a.sweep_conf, guess=True)
             sw["cpu_oracle"] = {"seconds": time.perf_counter() - t0, "energies": [float(v) for v in e],
                                 "sweep_energies": [float(v) for v in st["sweep_energies"]],
-                                "sweeps": st["sweeps"], "cores": os.cpu_count() or 1}
+                                "sweeps": st["sweeps"], "cores": os.cpu_count() or 1,
+                                "sigma_calls": st["sigma_calls"], "guess": "transformed"}
             sw["dE_fp64_minus_cpu"] = sw["fp64"]["energies"][0] - sw["cpu_oracle"]["energies"][0]
+            sw["dE_per_sweep_fp64_minus_cpu"] = [g - c for g, c in zip(sw["fp64"]["sweep_energies"],
+                                                                       sw["cpu_oracle"]["sweep_energies"])]
         sweeps["small"] = sw
         # large system: split precision with defect correction; its FP64
         # sweep time is derived from the per-step FP64 product times unless
