@@ -191,9 +191,12 @@ def fp64_peak_tflops():
 
 
 # DRAM bytes (read + write) of the two tensor-core sigma kernels per product,
-# from ncu captures of this bench's workloads (profiles/tc_sigma_*.md)
+# from ncu captures of this bench's workloads (profiles/tc_sigma_*.md), made
+# before the stage-1 products of small blocks were stacked (at M=2000 the
+# stacks hold 4 % of the stage-1 products; their operands are the same bytes)
 NCU_TRAFFIC = {("tests/golden/syn24/dmrg.conf", 11, "bf16x3tc"): 3.275e9,
                ("tests/golden/syn30/dmrg.conf", 14, "bf16x3tc"): 244.19e9}
+NCU_TRAFFIC_NOTE = "ncu capture before stacked stage-1 tiles (profiles/tc_sigma_bf16x3tc_syn30_m2000.md)"
 
 
 def measured_peaks():
@@ -370,6 +373,7 @@ def run_ours(a):
         traffic = NCU_TRAFFIC.get((os.path.relpath(a.conf, ROOT), a.partition, a.precision))
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
                 "traffic": traffic, "traffic_unit": "bytes per sigma (both tensor-core kernels, ncu)",
+                "traffic_source": NCU_TRAFFIC_NOTE if traffic else None,
                 "hbm_time_of_traffic_ms": (traffic / (peaks.get("hbm_gbs", 6800.0) * 1e9) * 1e3) if traffic else None,
                 "kernel": kname,
                 "peak_source": ("bf16_tflops of measured" if peaks else "fallback 1900"),
