@@ -193,7 +193,8 @@ def fp64_peak_tflops():
 # DRAM bytes (read + write) of the two tensor-core sigma kernels per product,
 # from ncu captures of this bench's workloads (profiles/tc_sigma_*.md), made
 # before the stage-1 products of small blocks were stacked (at M=2000 the
-# stacks hold 4 % of the stage-1 products; their operands are the same bytes)
+# stacks replace 37 % of the phase-1 tiles, all of small blocks; the
+# operands they read are the same bytes)
 NCU_TRAFFIC = {("tests/golden/syn24/dmrg.conf", 11, "bf16x3tc"): 3.275e9,
                ("tests/golden/syn30/dmrg.conf", 14, "bf16x3tc"): 244.19e9}
 NCU_TRAFFIC_NOTE = "ncu capture before stacked stage-1 tiles (profiles/tc_sigma_bf16x3tc_syn30_m2000.md)"
