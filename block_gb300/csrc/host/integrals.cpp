@@ -332,6 +332,11 @@ Config parse_config_text(const std::string& text, const std::string& base_dir) {
     else if (key == "seed") { need(1); c.seed = std::stoull(tok[1]); }
     else if (key == "deflation_max_size" || key == "max_deflation_size") { need(1); c.deflation_max = std::stoi(tok[1]); }
     else if (key == "deflation_min_size") { need(1); c.deflation_min = std::stoi(tok[1]); }
+    else if (key == "davidson_max_iter") {
+      need(1);
+      c.davidson_max_iter = std::stoi(tok[1]);
+      if (c.davidson_max_iter < 1) throw std::runtime_error("davidson_max_iter must be positive");
+    }
     else if (key == "warmup") { if (tok.size() > 1) c.warmup = lower(tok[1]); }
     else if (key == "restart" || key == "fullrestart") c.restart = true;
     else if (key == "spill") c.spill = true;

@@ -77,6 +77,9 @@ struct Config {
   std::string reorder = "fiedler";  // fiedler | noreorder | file:<path>
   int outputlevel = 0;
   int deflation_min = 2, deflation_max = 20;
+  // `davidson_max_iter <n>` (a keyword of this library; the reference's
+  // Davidson iterates until it converges): iteration limit of every solve
+  int davidson_max_iter = 200;
   uint64_t seed = 12345;  // warm-up rotations and Davidson guesses
   std::string warmup = "random";
   // sweep checkpoints (this project's restart format, host/checkpoint.h):

@@ -223,11 +223,16 @@ std::vector<int> SweepDriver::warmup_rotation(Block& big, int M, uint64_t seed) 
   double nhf = 0;
   for (int s : big.sites) nhf += occ[s];
   const double sig = std::max(1.0, std::sqrt((double)nsites));
+  // spin: low spins favoured for a singlet target; for a target of spin S
+  // the block's share of 2S (by its sites) is favoured instead, so that
+  // the first superblocks of a high-spin run hold enough states
+  const double s2_share = (double)target_.s2 * nsites / std::max(1, N_);
   std::vector<double> w(big.si.size());
   double tot = 0;
   for (int q = 0; q < big.si.size(); ++q) {
     const double dn = big.si.quanta[q].n - nhf;
-    w[q] = big.si.states[q] * std::exp(-dn * dn / (2 * sig * sig)) / (1.0 + big.si.quanta[q].s2);
+    const double ds = target_.s2 > 0 ? std::fabs(big.si.quanta[q].s2 - s2_share) : (double)big.si.quanta[q].s2;
+    w[q] = big.si.states[q] * std::exp(-dn * dn / (2 * sig * sig)) / (1.0 + ds);
     tot += w[q];
   }
   std::vector<int> kept(big.si.size(), 0);
@@ -496,6 +501,7 @@ double SweepDriver::step(bool forward, int p, int sweep_index, std::vector<doubl
   dp.tol = se.davidson_tol;
   dp.deflation_min = C_.deflation_min;
   dp.deflation_max = C_.deflation_max;
+  dp.max_iter = C_.davidson_max_iter;
   dp.seed = C_.seed + 104729ull * (uint64_t)(sweep_index * N_ + p);
   dp.defer_refine = opt_.refine_window > 0.0;
   if (opt_.transform_guess && prev_.valid && prev_.forward == forward && prev_.p == (forward ? p - 1 : p + 1)) {

@@ -439,6 +439,12 @@ int CpuEngine::solve(const Superblock& sb, const DavidsonParams& p, std::vector<
         scal(1.0 / std::sqrt(dot(r, r)), r);
         axpy(-dot(r, b[j]), b[j], r);
       }
+      // a correction that lies almost inside the subspace (few states left
+      // outside it, e.g. many roots of a small superblock) loses its
+      // orthogonality in the pass above: a second pass restores it (twice
+      // is enough, Kahan); the reference's single pass is kept otherwise
+      if (dot(r, r) < 1e-2)
+        for (size_t j = 0; j < b.size(); ++j) axpy(-dot(r, b[j]), b[j], r);
       scal(1.0 / std::sqrt(dot(r, r)), r);
       b.push_back(r);
     }

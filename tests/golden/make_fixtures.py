@@ -2,7 +2,7 @@
 
 Copies the FCIDUMP inputs of the reference's energy tests (data files only)
 and records the expected energies its test scripts check:
-  dmrg_tests/runtest:12,23,30 (test_energy.py tolerance 1e-6) and
+  dmrg_tests/runtest:12,23,30,70 (test_energy.py tolerance 1e-6) and
   pydmrg/tests/test_dmrg_simple.py:34 (10 decimal places);
 and copies the spatial one-particle density matrices its 1-RDM tests check
 (dmrg_tests/runtest:31,141,152-154; test_onepdm.py and
@@ -37,6 +37,21 @@ CASES = {
     "h2o_nosym": ("dmrg_tests/h2o_nosym/FCIDUMP",
                   "nelec 10\nspin 0\nirrep 1\nhf_occ integral\nschedule default\nstartM 100\nmaxM 300\nsweep_tol tight\n",
                   [-76.11460447], "dmrg_tests/runtest:23"),
+    # hubbard_stateSpecific/dmrg.conf (8-site ring, spin 6, 20 roots with
+    # equal weights, state-averaged, perturbative noise in the first three
+    # schedule entries) without twodot_to_onedot; davidson_max_iter lifts
+    # this library's default limit (the reference's Davidson has none) so
+    # that the degenerate top roots converge; the first 20 energies of the
+    # runtest:70 list
+    "hubbard_20roots": ("dmrg_tests/hubbard_stateSpecific/FCIDUMP",
+                        "nelec 8\nspin 6\nhf_occ integral\nschedule\n0 50 1.0e-6 1e-06\n4 150 1e-6 1e-6\n"
+                        "6 200 1e-6 1e-6\n8 200 1e-10 0.0\nend\nmaxiter 30\nsweep_tol 1e-9\nnroots 20\n"
+                        "weights" + " 0.1" * 20 + "\ndavidson_max_iter 1000\n",
+                        [-2.5065432138, -2.1684123422, -2.1684123422, -1.4755687956, -1.4755687956,
+                         -1.4142135624, -1.4142135624, -1.2897006828, -0.8284271247, -0.5180081887,
+                         -0.5180081887, -0.4079274397, -0.4079274397, 0.0, 0.0, 0.1224001196, 0.1224001196,
+                         0.5857864376, 0.5857864376, 0.5857864376],
+                        "dmrg_tests/runtest:70"),
     # h2o_transitionpdm/dmrg_onepdm.conf without its noise column and
     # twodot_to_onedot; no energy test in runtest (energies None)
     "h2o_c2v": ("dmrg_tests/h2o_transitionpdm/FCIDUMP",
