@@ -175,7 +175,8 @@ cudaError_t launch_tc_reduce(const TcBufs& b, const TcTile* tiles, const int64_t
 // with fixed-point slices so that the f32 accumulation is exact).  Every
 // operand row r is scaled by 2^-e_r, e_r = 1 + the largest binary exponent
 // of its elements, and written as six balanced base-128 digits
-//   x = 2^e_r sum_{s=0..5} a_s 2^-7(s+1),  a_0 in [-128, 128], a_s in [-64, 63],
+//   x = 2^e_r sum_{s=0..5} a_s 2^-7(s+1),  |a_0| <= 128, |a_s| <= 64 (the
+//   balanced digits of |x|, a_s in [-64, 63], times the sign of x),
 // one bf16 slice per digit (integers of at most 8 bits are exact in bf16).
 // The 21 digit products with s + u <= 5 go to six f32 TMEM accumulators
 // J_q (q = s + u); every term is an integer of at most 2^15 per K element, so
