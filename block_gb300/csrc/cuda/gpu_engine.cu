@@ -1583,6 +1583,7 @@ TcKnobs GpuEngine::tc_default_knobs() const {
   k.split = env_double("BGPU_TC_SPLIT", 3.0);
   k.group = (int)env_double("BGPU_TC_GROUP", 16.0);
   k.waves = (int)env_double("BGPU_TC_WAVES", 0.0);
+  k.pairs = (int)env_double("BGPU_TC_PAIRS", 0.0);
   return k;
 }
 
@@ -1625,67 +1626,171 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
     }
   }
   const double chunk = seq ? 1e300 : std::max(total / (2.0 * kn.split * nsm), 20000.0);
-  for (int s = 0; s < nsec; ++s) {
-    const auto& S = sb.sectors[s];
-    const int ib = (int)i2.size();
-    i2.insert(i2.end(), per_sector[s].begin(), per_sector[s].end());
-    const int ie = (int)i2.size();
-    const int rows_p = tc_round8(S.rows), cols_p = tc_round8(S.cols);
-    for (int tm = 0; tm < (S.rows + 127) / 128; ++tm)
-      for (int tn = 0; tn < (S.cols + nb - 1) / nb; ++tn) {
-        const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(nb, cols_p - nb * tn);
+  // cluster pairs (phase 2 with 128-column tiles): the column tiles tn and
+  // tn + 1 of a sigma row tile run on the two blocks of a cluster, which
+  // read the same items; a row tile with an odd number of column tiles
+  // pairs its last one with a ghost copy that writes nothing.  Split tiles
+  // cut every column tile of a row tile at the same items.  t2 holds the
+  // pairs' tasks one after the other (2p, 2p + 1), c2 their pair costs.
+  const bool pairs = kn.pairs != 0 && nb == kTcRowsBWide && !seq && !plan.tcx;
+  std::vector<double> cp;  // cost per pair
+  std::vector<int64_t> bundle_p;
+  if (pairs) {
+    for (int s = 0; s < nsec; ++s) {
+      const auto& S = sb.sectors[s];
+      const int ib = (int)i2.size();
+      i2.insert(i2.end(), per_sector[s].begin(), per_sector[s].end());
+      const int ie = (int)i2.size();
+      const int rows_p = tc_round8(S.rows), cols_p = tc_round8(S.cols);
+      const int ntn = (S.cols + nb - 1) / nb;
+      for (int tm = 0; tm < (S.rows + 127) / 128; ++tm) {
+        const int ha = std::min(128, rows_p - 128 * tm);
+        const int hb0 = std::min(nb, cols_p);  // the widest column tile
         double tile_cost = 0.0;
-        for (int x = ib; x < ie; ++x) tile_cost += item_cost(i2[x], hb);
-        TcTask t{};
-        t.a_rows = rows_p;
-        t.b_rows = cols_p;
-        t.tm = tm;
-        t.tn = tn;
-        t.valid_rows = std::min(128, S.rows - 128 * tm);
-        t.valid_cols = std::min(nb, S.cols - nb * tn);
-        for (int x = ib; x < ie; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
+        for (int x = ib; x < ie; ++x) tile_cost += item_cost(i2[x], hb0);
+        // item cuts shared by every column tile of this row tile
+        std::vector<int2> cuts;
         if (tile_cost <= chunk || ie - ib <= 1) {
-          t.ibeg = ib;
-          t.iend = ie;
-          t.direct = 1;
-          t.out_off = S.offset;
-          t.out_kp = S.cols;
-          t2.push_back(t);
-          c2.push_back(tile_cost);
-          sec2.push_back(s);
-          bundle2.push_back(((int64_t)s << 8) | tm);
-          continue;
+          cuts.push_back(make_int2(ib, ie));
+        } else {
+          int x0 = ib;
+          while (x0 < ie) {
+            double acc = 0.0;
+            int x1 = x0;
+            while (x1 < ie && (acc < chunk || x1 == x0)) acc += item_cost(i2[x1++], hb0);
+            cuts.push_back(make_int2(x0, x1));
+            x0 = x1;
+          }
         }
-        TcTile tl{};
-        tl.s_off = S.offset;
-        tl.lds = S.cols;
-        tl.h = t.valid_rows;
-        tl.w = t.valid_cols;
-        tl.r0 = 128 * tm;
-        tl.c0 = nb * tn;
-        tl.pad = hb;  // row stride of the partial slots
-        tl.pbeg = (int)slots.size();
-        int x0 = ib;
-        while (x0 < ie) {
-          double acc = 0.0;
-          int x1 = x0;
-          while (x1 < ie && (acc < chunk || x1 == x0)) acc += item_cost(i2[x1++], hb);
-          TcTask u = t;
-          u.ibeg = x0;
-          u.iend = x1;
-          u.direct = 0;
-          u.out_off = partial_n;
-          slots.push_back(partial_n);
-          partial_n += (int64_t)ha * hb;
-          t2.push_back(u);
-          c2.push_back(acc);
-          sec2.push_back(s);
-          bundle2.push_back(-(int64_t)t2.size());  // pieces of a split tile spread over blocks
-          x0 = x1;
+        const bool direct = cuts.size() == 1;
+        // per column tile: its tasks (one per cut), partial slots and tile
+        std::vector<std::vector<TcTask>> col(ntn);
+        std::vector<std::vector<double>> colc(ntn);
+        for (int tn = 0; tn < ntn; ++tn) {
+          const int hb = std::min(nb, cols_p - nb * tn);
+          TcTask t{};
+          t.a_rows = rows_p;
+          t.b_rows = cols_p;
+          t.tm = tm;
+          t.tn = tn;
+          t.valid_rows = std::min(128, S.rows - 128 * tm);
+          t.valid_cols = std::min(nb, S.cols - nb * tn);
+          for (int x = ib; x < ie; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
+          TcTile tl{};
+          if (!direct) {
+            tl.s_off = S.offset;
+            tl.lds = S.cols;
+            tl.h = t.valid_rows;
+            tl.w = t.valid_cols;
+            tl.r0 = 128 * tm;
+            tl.c0 = nb * tn;
+            tl.pad = hb;
+            tl.pbeg = (int)slots.size();
+          }
+          for (const int2& ct : cuts) {
+            TcTask u = t;
+            u.ibeg = ct.x;
+            u.iend = ct.y;
+            double acc = 0.0;
+            for (int x = ct.x; x < ct.y; ++x) acc += item_cost(i2[x], hb);
+            if (direct) {
+              u.direct = 1;
+              u.out_off = S.offset;
+              u.out_kp = S.cols;
+            } else {
+              u.direct = 0;
+              u.out_off = partial_n;
+              slots.push_back(partial_n);
+              partial_n += (int64_t)ha * hb;
+            }
+            col[tn].push_back(u);
+            colc[tn].push_back(acc);
+          }
+          if (!direct) {
+            tl.pend = (int)slots.size();
+            tiles.push_back(tl);
+          }
         }
-        tl.pend = (int)slots.size();
-        tiles.push_back(tl);
+        for (int tn = 0; tn < ntn; tn += 2)
+          for (size_t k = 0; k < cuts.size(); ++k) {
+            const TcTask& a = col[tn][k];
+            TcTask g = a;  // ghost partner of a last odd column tile
+            g.ghost = 1;
+            const TcTask& bt = tn + 1 < ntn ? col[tn + 1][k] : g;
+            t2.push_back(a);
+            t2.push_back(bt);
+            sec2.push_back(s);
+            sec2.push_back(s);
+            c2.push_back(colc[tn][k]);
+            c2.push_back(tn + 1 < ntn ? colc[tn + 1][k] : colc[tn][k]);
+            cp.push_back(std::max(c2[c2.size() - 2], c2.back()));
+            bundle_p.push_back(direct ? (((int64_t)s << 8) | tm) : -(int64_t)cp.size());
+          }
       }
+    }
+  } else {
+    for (int s = 0; s < nsec; ++s) {
+      const auto& S = sb.sectors[s];
+      const int ib = (int)i2.size();
+      i2.insert(i2.end(), per_sector[s].begin(), per_sector[s].end());
+      const int ie = (int)i2.size();
+      const int rows_p = tc_round8(S.rows), cols_p = tc_round8(S.cols);
+      for (int tm = 0; tm < (S.rows + 127) / 128; ++tm)
+        for (int tn = 0; tn < (S.cols + nb - 1) / nb; ++tn) {
+          const int ha = std::min(128, rows_p - 128 * tm), hb = std::min(nb, cols_p - nb * tn);
+          double tile_cost = 0.0;
+          for (int x = ib; x < ie; ++x) tile_cost += item_cost(i2[x], hb);
+          TcTask t{};
+          t.a_rows = rows_p;
+          t.b_rows = cols_p;
+          t.tm = tm;
+          t.tn = tn;
+          t.valid_rows = std::min(128, S.rows - 128 * tm);
+          t.valid_cols = std::min(nb, S.cols - nb * tn);
+          for (int x = ib; x < ie; ++x) mma += 3.0 * 2.0 * 128 * tc_round16(hb) * i2[x].kp;
+          if (tile_cost <= chunk || ie - ib <= 1) {
+            t.ibeg = ib;
+            t.iend = ie;
+            t.direct = 1;
+            t.out_off = S.offset;
+            t.out_kp = S.cols;
+            t2.push_back(t);
+            c2.push_back(tile_cost);
+            sec2.push_back(s);
+            bundle2.push_back(((int64_t)s << 8) | tm);
+            continue;
+          }
+          TcTile tl{};
+          tl.s_off = S.offset;
+          tl.lds = S.cols;
+          tl.h = t.valid_rows;
+          tl.w = t.valid_cols;
+          tl.r0 = 128 * tm;
+          tl.c0 = nb * tn;
+          tl.pad = hb;  // row stride of the partial slots
+          tl.pbeg = (int)slots.size();
+          int x0 = ib;
+          while (x0 < ie) {
+            double acc = 0.0;
+            int x1 = x0;
+            while (x1 < ie && (acc < chunk || x1 == x0)) acc += item_cost(i2[x1++], hb);
+            TcTask u = t;
+            u.ibeg = x0;
+            u.iend = x1;
+            u.direct = 0;
+            u.out_off = partial_n;
+            slots.push_back(partial_n);
+            partial_n += (int64_t)ha * hb;
+            t2.push_back(u);
+            c2.push_back(acc);
+            sec2.push_back(s);
+            bundle2.push_back(-(int64_t)t2.size());  // pieces of a split tile spread over blocks
+            x0 = x1;
+          }
+          tl.pend = (int)slots.size();
+          tiles.push_back(tl);
+        }
+    }
   }
   std::vector<double> c1;
   for (const TcTask& t : t1)
@@ -1708,9 +1813,26 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
     const int bps = plan.tcx ? tcx_blocks_per_sm() : tc_blocks_per_sm(nb);
     if (kn.waves) {
       schedule_waves(c1, bps * nsm, o1, r1);
-      schedule_waves(c2, bps * nsm, o2, r2);
     } else {
       schedule_lpt(c1, H.bundle1, bps * nsm, o1, r1);
+    }
+    if (pairs) {
+      // pairs to clusters of two blocks; block 2c runs the first task of
+      // each of cluster c's pairs, block 2c + 1 the second
+      std::vector<int> op;
+      std::vector<int2> rp;
+      schedule_lpt(cp, bundle_p, bps * nsm / 2, op, rp);
+      o2.clear();
+      r2.clear();
+      for (const int2& g : rp)
+        for (int rank = 0; rank < 2; ++rank) {
+          const int b0 = (int)o2.size();
+          for (int k = g.x; k < g.y; ++k) o2.push_back(2 * op[k] + rank);
+          r2.push_back(make_int2(b0, (int)o2.size()));
+        }
+    } else if (kn.waves) {
+      schedule_waves(c2, bps * nsm, o2, r2);
+    } else {
       schedule_lpt(c2, bundle2, bps * nsm, o2, r2);
     }
   } else {
@@ -1778,7 +1900,8 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
           base.out_base = T.out_off;
           base.out_ld = base.h_b;
         }
-        const uint8_t f0 = (uint8_t)((T.direct ? kTcDirect : 0) | (phase == 1 && T.stacked ? kTcStacked : 0));
+        const uint8_t f0 = (uint8_t)((T.direct ? kTcDirect : 0) | (phase == 1 && T.stacked ? kTcStacked : 0) |
+                                     (phase == 2 && T.ghost ? kTcGhost : 0));
         if (T.ibeg == T.iend) {
           TcWork x = base;
           x.flags = (uint8_t)(f0 | kTcFirst | kTcLast | kTcEmpty);
@@ -1906,6 +2029,7 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   plan.tc_l2 = std::move(l2);
   plan.tc_knobs = kn;
   plan.tc_knobs.nb = nb;
+  plan.tc_pairs = pairs;
   {
     int64_t full = 0;
     for (const TcItem& it : i2) full += it.a_pool == kTcPoolS ? 1 : 0;
@@ -2094,8 +2218,12 @@ void GpuEngine::sigma_tc(const Superblock& sb, SigmaPlan& p, const double* psi, 
   } else {
     cuda_check(dev::launch_tc_sigma(1, p.tc_nb, b, p.tc_w1.d, p.tc_r1.d, (int)p.tc_r1.n, out, kWaitLimitNs, stream_),
                "tc phase 1");
-    cuda_check(dev::launch_tc_sigma(2, p.tc_nb, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
-               "tc phase 2");
+    if (p.tc_pairs)
+      cuda_check(dev::launch_tc_sigma_pairs(b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
+                 "tc phase 2 (cluster pairs)");
+    else
+      cuda_check(dev::launch_tc_sigma(2, p.tc_nb, b, p.tc_w2.d, p.tc_r2.d, (int)p.tc_r2.n, out, kWaitLimitNs, stream_),
+                 "tc phase 2");
   }
   if (marks) cuda_check(cudaEventRecord(marks[1], stream_), "record");
   cuda_check(dev::launch_tc_reduce(b, p.tc_tiles.d, p.tc_slots.d, (int)p.tc_tiles.n, out, stream_), "tc reduce");

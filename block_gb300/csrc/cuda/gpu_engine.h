@@ -69,9 +69,12 @@ struct TcKnobs {
   // so that the blocks work on neighbouring tiles of a sector together and
   // share its operand tiles in L2)
   int waves = 0;
+  // 1: phase 2 of 128-column plans on pairs of blocks in clusters of two,
+  // each A piece copied once for both column tiles (cluster multicast)
+  int pairs = 0;
   bool operator==(const TcKnobs& o) const {
     return item_cost == o.item_cost && split == o.split && group == o.group && per_sector == o.per_sector &&
-           nb == o.nb && waves == o.waves;
+           nb == o.nb && waves == o.waves && pairs == o.pairs;
   }
 };
 struct TcHostPlan;  // item lists of a tensor-core plan, kept for rescheduling
@@ -118,6 +121,7 @@ struct SigmaPlan {
   DevArray<dev::TcTile> tc_tiles;
   DevArray<int64_t> tc_slots;
   DevArray<dev::TcRow> tc_rows;  // row maps of the stacked phase-1 tiles (128 per stack)
+  bool tc_pairs = false;         // phase 2 runs on cluster pairs (TcKnobs::pairs)
   int64_t tc_stacks = 0, tc_stacked_items = 0;  // stacks and the stage-1 products they replace
   int tc_stack_used = 0;  // the engine's tc_stack_rows when the plan was built
   float2* tc_partials = nullptr;

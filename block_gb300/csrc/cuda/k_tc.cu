@@ -295,7 +295,7 @@ __device__ __forceinline__ int shfl32(int v, int j) { return __shfl_sync(0xfffff
 // ranges[j].y), each role loading them 32 at a time, and the pipeline runs
 // across task boundaries.  The epilogue folds each group sum into a
 // compensated (hi, lo) f32 pair held in registers.
-template <int PHASE, int NB>
+template <int PHASE, int NB, bool PAIR = false>
 __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
     tc_sigma_kernel(TcBufs b, const TcWork* __restrict__ work, const int2* __restrict__ ranges,
                     double* __restrict__ sigma, uint64_t limit_ns) {
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
   if (tid == 0) {
     for (int i = 0; i < kTcSlots; ++i) {
       mbar_init(&sh.full[i], 1);
-      mbar_init(&sh.empty[i], 1);
+      mbar_init(&sh.empty[i], PAIR ? 2 : 1);  // pairs: released by both blocks' MMAs
     }
     for (int i = 0; i < kTcAcc; ++i) {
       mbar_init(&sh.acc_full[i], 1);
@@ -328,6 +328,9 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
+  // pairs: both blocks' barriers exist before either block copies or commits into the other
+  if (PAIR) cluster_sync();
+  const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
   const uint32_t tmem = sh.tbase;
   volatile int* abort_flag = &sh.abort_flag;
 
@@ -361,7 +364,21 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
             }
             uint8_t* dst = smem + slot * kTcStageBytes;
             mbar_expect_tx(&sh.full[slot], abytes + bbytes);
-            bulk_g2s(dst, pa + 2 * (int64_t)h_a * kTcKC * c, abytes, &sh.full[slot]);
+            if constexpr (PAIR) {
+              // this block's half of the A piece's 8-column groups (hi and
+              // lo slices), into the same stage of both blocks of the pair
+              const int ng = w / 8;
+              const int g0 = rank ? (ng + 1) / 2 : 0, g1 = rank ? ng : (ng + 1) / 2;
+              if (g1 > g0) {
+                const uint32_t slice = (uint32_t)h_a * w * 2;
+                const uint32_t off = (uint32_t)g0 * h_a * 16, len = (uint32_t)(g1 - g0) * h_a * 16;
+                const uint8_t* src = reinterpret_cast<const uint8_t*>(pa + 2 * (int64_t)h_a * kTcKC * c);
+                bulk_g2s_mc(dst + off, src + off, len, &sh.full[slot], (uint16_t)3);
+                bulk_g2s_mc(dst + slice + off, src + slice + off, len, &sh.full[slot], (uint16_t)3);
+              }
+            } else {
+              bulk_g2s(dst, pa + 2 * (int64_t)h_a * kTcKC * c, abytes, &sh.full[slot]);
+            }
             bulk_g2s(dst + abytes, pb + 2 * (int64_t)h_b * kTcKC * c, bbytes, &sh.full[slot]);
           }
         }
@@ -372,6 +389,12 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
       // copies already issued still land in shared memory: wait for them
       for (uint32_t i = (k > kTcSlots ? k - kTcSlots : 0); i < k; ++i)
         mbar_wait_bounded(&sh.full[i % kTcSlots], (i / kTcSlots) & 1u, limit_ns);
+    }
+    if (PAIR && lane == 0 && ok) {
+      // the last stages released by both blocks: every multicast copy of
+      // this block has landed in the partner and been read there
+      for (uint32_t i = (k > kTcSlots ? k - kTcSlots : 0); i < k; ++i)
+        tc_wait(&sh.empty[i % kTcSlots], (i / kTcSlots) & 1u, abort_flag, b.status, limit_ns);
     }
   } else if (warp == kTcIssuer) {
     // ---- MMA issuer (lane 0)
@@ -420,7 +443,8 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
                 mma_bf16(d, dah, dbl, idesc, 1u);
                 mma_bf16(d, dal, dbh, idesc, 1u);
               }
-              mma_commit(&sh.empty[slot]);
+              if (PAIR) mma_commit_mc(&sh.empty[slot], (uint16_t)3);
+              else mma_commit(&sh.empty[slot]);
             }
             if (ok && (flags & kTcGEnd)) {
               mma_commit(&sh.acc_full[ab]);
@@ -526,6 +550,8 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
                 if (!last) {
                   tmem_st16(vh_t + (uint32_t)cb, vh);
                   tmem_st16(vl_t + (uint32_t)cb, vl);
+                } else if (PAIR && (flags & kTcGhost)) {
+                  // the partner's tile repeated for the pair: no output
                 } else if (flags & kTcDirect) {
                   const int vrows = vrc & 0xffff, vcols = (vrc >> 16) & 0xffff;
                   if (row < vrows) {
@@ -597,6 +623,8 @@ __global__ void __launch_bounds__(kTcThreads, TcCfg<NB>::kBlocksPerSm)
     fence_after_sync();
     tmem_dealloc(tmem, TcCfg<NB>::kTmemCols);
   }
+  // pairs: neither block leaves while the other may still copy into it
+  if (PAIR) cluster_sync();
 }
 
 template <int PHASE, int NB>
@@ -620,6 +648,31 @@ cudaError_t launch_tc_sigma(int phase, int nb, const TcBufs& b, const TcWork* wo
 }
 
 int tc_blocks_per_sm(int nb) { return nb == 64 ? TcCfg<64>::kBlocksPerSm : TcCfg<128>::kBlocksPerSm; }
+
+cudaError_t launch_tc_sigma_pairs(const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks, double* sigma,
+                                  uint64_t limit_ns, cudaStream_t s) {
+  if (nblocks <= 0) return cudaGetLastError();
+  if (nblocks % 2) return cudaErrorInvalidValue;
+  constexpr int smem = TcCfg<128>::kSmem;
+  auto kern = tc_sigma_kernel<2, 128, true>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(kTcThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, b, work, ranges, sigma, limit_ns);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
 
 __global__ void __launch_bounds__(256) tc_reduce_kernel(const float2* __restrict__ partials,
                                                          const TcTile* __restrict__ tiles,

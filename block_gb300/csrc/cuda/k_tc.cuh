@@ -89,7 +89,8 @@ struct TcTask {
   int64_t out_off;
   int32_t out_kp, direct;
   int32_t valid_rows, valid_cols;
-  int32_t stacked, pad;
+  int32_t stacked;
+  int32_t ghost;  // cluster pairs: repeats its partner's tile, writes nothing
 };
 
 // Row r of a stacked phase-1 tile: row lrow of the packed stage-1 operand S
@@ -128,7 +129,8 @@ enum : uint32_t {
   kTcEmpty = 8,    // task without items (writes zeros)
   kTcGStart = 16,  // first item of an accumulation group
   kTcGEnd = 32,    // last item of an accumulation group
-  kTcStacked = 64  // phase 1: A is a stack of operators; out_base indexes TcBufs::rows
+  kTcStacked = 64,  // phase 1: A is a stack of operators; out_base indexes TcBufs::rows
+  kTcGhost = 128    // cluster pairs: this block repeats its partner's tile and writes nothing
 };
 struct __align__(16) TcWork {
   int64_t a_base, b_base, out_base;
@@ -159,6 +161,14 @@ cudaError_t launch_tc_sigma(int phase, int nb, const TcBufs& b, const TcWork* wo
                             double* sigma, uint64_t limit_ns, cudaStream_t s);
 // persistent blocks per SM of the kernels with tile width nb
 int tc_blocks_per_sm(int nb);
+// Phase 2 with 128-column tiles on pairs of blocks in thread-block clusters
+// of two (blocks 2c and 2c + 1): the two blocks of a pair run record streams
+// of the same items (the column tiles tn and tn + 1, or a ghost copy, of one
+// sigma row tile); each copies half of every A piece into both blocks'
+// stages with a cluster-multicast bulk copy and its own B piece, and a stage
+// is refilled once both blocks' MMAs released it.  nblocks is even.
+cudaError_t launch_tc_sigma_pairs(const TcBufs& b, const TcWork* work, const int2* ranges, int nblocks, double* sigma,
+                                  uint64_t limit_ns, cudaStream_t s);
 // Bounded-wait self-check: one thread waits, with the sigma kernels' wait,
 // on an mbarrier that nothing arrives at; out[0] = 1 when the wait gave up,
 // out[1] = nanoseconds waited; *status is set by the wait.
