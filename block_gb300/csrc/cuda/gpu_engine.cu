@@ -2013,6 +2013,22 @@ void GpuEngine::schedule_tc(const Superblock& sb, SigmaPlan& plan, const TcKnobs
   } else {
     flatten(1, t1, i1, o1, r1, w1, wr1);
     flatten(2, t2, i2, o2, r2, w2, wr2);
+    if (pairs) {
+      // the two blocks of a cluster must stream the same A pieces in the
+      // same order (their stages are filled for each other)
+      if (wr2.size() % 2) throw std::runtime_error("tensor-core plan: odd number of blocks for cluster pairs");
+      for (size_t c = 0; c + 1 < wr2.size(); c += 2) {
+        const int2 a = wr2[c], bq = wr2[c + 1];
+        if (a.y - a.x != bq.y - bq.x) throw std::runtime_error("tensor-core plan: cluster pair streams differ");
+        for (int i = 0; i < a.y - a.x; ++i) {
+          const TcWork& x = w2[a.x + i];
+          const TcWork& y = w2[bq.x + i];
+          const int fx = x.flags & ~(kTcGhost | kTcDirect), fy = y.flags & ~(kTcGhost | kTcDirect);
+          if (x.a_base != y.a_base || x.kp != y.kp || x.h_a != y.h_a || x.a_pool != y.a_pool || fx != fy)
+            throw std::runtime_error("tensor-core plan: cluster pair streams differ");
+        }
+      }
+    }
   }
   for (auto* d : {&plan.tc_w1, &plan.tc_w2}) d->release(stream_);
   for (auto* d : {&plan.tc_r1, &plan.tc_r2}) d->release(stream_);
