@@ -339,6 +339,16 @@ def run_ours(a):
     if dist:
         dist.barrier()
     ctx.synchronize()
+    # end-to-end host buffers: page-locked ones from the library
+    # (bgpu_host_alloc), as a caller keeping its wavefunctions there would;
+    # ordinary arrays if they cannot be had
+    try:
+        h_in, h_out = ctx.host_array(n), ctx.host_array(n)
+        h_in[:] = psi
+        host_buffers = "page-locked (bgpu_host_alloc)"
+    except Exception:
+        h_in, h_out, host_buffers = psi, np.empty(n), "pageable"
+    ctx.sigma(sb, h_in, out=h_out)  # untimed: first use of the buffers
     with ClockSampler(local) as clk:
         if a.profile:
             ctx.profiler_start()
@@ -348,9 +358,12 @@ def run_ours(a):
         # end-to-end through the host-buffer C ABI call (H2D psi, D2H sigma per step)
         t0 = time.perf_counter()
         for _ in range(a.steps):
-            out = ctx.sigma(sb, psi)
+            ctx.sigma(sb, h_in, out=h_out)
         t_e2e = time.perf_counter() - t0
     ctx.synchronize()
+    if host_buffers != "pageable":
+        ctx.host_free(h_in)
+        ctx.host_free(h_out)
     clocks = clk.summary()
     t_step = ms[0] / a.steps * 1e-3
     t_step, t_e2e_step, value, e2e = whole_job(flops, t_step, t_e2e / a.steps, dist)
@@ -395,7 +408,8 @@ def run_ours(a):
                                                                                           "bf16 slices, f32 accumulate"),
             "data": "synthetic",
             "config": config_dict(a.conf, a.partition, n, a.precision, nbytes / 1e6),
-            "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+            "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                    "host_buffers": host_buffers},
             "gpu_launches": launches * a.steps, "clocks": clocks, "roofline": roof,
             "sigma_flops_per_step": flops, "kernel_ms_per_step": [ms[1] / a.steps, ms[2] / a.steps],
             "prepare_seconds": t_prep}

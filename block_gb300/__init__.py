@@ -47,6 +47,8 @@ _SIGS = {
     "bgpu_superblock_work": (_I, [_P, _I, _DP, _DP]),
     "bgpu_sigma": (_I, [_P, _I, _DP, _DP]),
     "bgpu_sigma_device": (_I, [_P, _I, _P, _P]),
+    "bgpu_host_alloc": (_I, [_P, _I64, ctypes.POINTER(_DP)]),
+    "bgpu_host_free": (_I, [_P, _DP]),
     "bgpu_hdiag": (_I, [_P, _I, _DP]),
     "bgpu_sigma_timed": (_I, [_P, _I, _P, _P, _I, _DP]),
     "bgpu_superblock_launches": (_I, [_P, _I, _IP]),
@@ -316,11 +318,27 @@ class Context:
         self._check(self.lib.bgpu_superblock_work(self.h, sb, ctypes.byref(f), ctypes.byref(b)))
         return f.value, b.value
 
-    def sigma(self, sb, psi):
+    def sigma(self, sb, psi, out=None):
+        """sigma = H psi on host arrays; `out` (optional): a contiguous
+        float64 array of psi's size that receives sigma (for example a
+        page-locked one from host_array)."""
         psi = np.ascontiguousarray(psi, dtype=np.float64)
-        out = np.empty_like(psi)
+        if out is None:
+            out = np.empty_like(psi)
+        elif out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != psi.size:
+            raise ValueError("out must be a contiguous float64 array of psi's size")
         self._check(self.lib.bgpu_sigma(self.h, sb, _dp(psi), _dp(out)))
         return out
+
+    def host_array(self, n):
+        """n doubles of page-locked host memory (bgpu_host_alloc) as a numpy
+        array; release it with host_free before the context closes."""
+        p = _DP()
+        self._check(self.lib.bgpu_host_alloc(self.h, int(n), ctypes.byref(p)))
+        return np.ctypeslib.as_array(p, shape=(int(n),))
+
+    def host_free(self, arr):
+        self._check(self.lib.bgpu_host_free(self.h, _dp(arr)))
 
     def sigma_device(self, sb, psi_ptr, out_ptr):
         self._check(self.lib.bgpu_sigma_device(self.h, sb, _P(psi_ptr), _P(out_ptr)))

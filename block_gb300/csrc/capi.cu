@@ -433,6 +433,21 @@ int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
   });
 }
 
+int bgpu_host_alloc(bgpu_ctx* ctx, int64_t n, double** p) {
+  return guarded(ctx, [&] {
+    need(p && n > 0, "bad arguments");
+    need(ctx->eng != nullptr, "no device");
+    *p = nullptr;
+    cuda_check(cudaMallocHost((void**)p, (size_t)n * sizeof(double)), "page-locked host buffer");
+  });
+}
+
+int bgpu_host_free(bgpu_ctx* ctx, double* p) {
+  return guarded(ctx, [&] {
+    if (p) cuda_check(cudaFreeHost(p), "free page-locked host buffer");
+  });
+}
+
 int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi, double* sigma) {
   return guarded(ctx, [&] {
     auto it = ctx->sbs.find(sb);

@@ -289,6 +289,12 @@ int bgpu_superblock_launches(bgpu_ctx* ctx, int sb, int* launches);
 int bgpu_sigma(bgpu_ctx* ctx, int sb, const double* psi, double* sigma);
 /* Same on device pointers (stream-ordered, asynchronous). */
 int bgpu_sigma_device(bgpu_ctx* ctx, int sb, const double* psi_dev, double* sigma_dev);
+/* n doubles of page-locked host memory (no reference counterpart): host
+ * buffers for bgpu_sigma whose copies to and from the device run at the
+ * host link's rate instead of through a pageable staging copy.  Release
+ * with bgpu_host_free. */
+int bgpu_host_alloc(bgpu_ctx* ctx, int64_t n, double** p);
+int bgpu_host_free(bgpu_ctx* ctx, double* p);
 /*
  * `reps` back-to-back sigma products on device buffers timed with CUDA
  * events on the context's stream; ms[0] = total.  FP64: ms[1] = first GEMM
