@@ -42,10 +42,22 @@ def test_valid_input_runs(oracle, tmp_path):
     BASE + "nonspinadapted\n",                                 # determinant basis
     BASE.replace("maxiter 2", "maxiter"),                      # keyword without its value
     BASE.replace("orbitals {orb}", "orbitals synthetic:0:0:0:0:0"),  # empty synthetic system
-], ids=["schedule-entries", "no-schedule", "hubbard", "onedot", "nonspinadapted", "no-value", "bad-synthetic"])
+    BASE + "davidson_max_iter 0\n",                          # iteration limit must be positive
+    BASE + "davidson_max_iter\n",                            # ... and given
+], ids=["schedule-entries", "no-schedule", "hubbard", "onedot", "nonspinadapted", "no-value", "bad-synthetic",
+        "max-iter-zero", "max-iter-missing"])
 def test_malformed_input_refused(oracle, tmp_path, text):
     with pytest.raises(RuntimeError):
         run_conf(oracle, tmp_path, text.format(orb=FCIDUMP))
+
+
+def test_davidson_max_iter_limits_the_solves(oracle, tmp_path):
+    """davidson_max_iter caps every solve: with one iteration per solve the
+    sweep still runs (each step keeps its best Ritz vector) and stays above
+    the converged energy."""
+    e_ref, _ = run_conf(oracle, tmp_path, BASE.format(orb=FCIDUMP))
+    e1, st1 = run_conf(oracle, tmp_path, BASE.format(orb=FCIDUMP) + "davidson_max_iter 1\n")
+    assert st1["sweeps"] == 2 and e1[0] > e_ref[0] + 1e-6
 
 
 def test_missing_fcidump_refused(oracle, tmp_path):
